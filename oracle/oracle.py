@@ -1,0 +1,407 @@
+"""CPU oracle for the force-evaluation path (ctypes front end of yaff_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker used by tests/, __graft_entry__.smoke()
+and the CPU-baseline leg of bench.py.  The product never imports it.
+
+``OracleForceField(spec)`` evaluates a configs.py spec the way the reference
+``ForceField.compute`` does (yaff/pes/ff.py:117-168, :268-273): a neighbour
+list update with the reference's skin policy (yaff/pes/nlist.py:144-218), then
+each part in turn -- pair terms (pair_pot.c), Ewald reciprocal / correction /
+neutralizing (ewald.c, ff.py:653-669) and the valence chain (dlist/iclist/
+vlist).  All arithmetic is FP64 in the order of the reference C code.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, 'yaff_oracle.c')
+BUILD_DIR = os.path.join(HERE, '_build')
+LIB = os.path.join(BUILD_DIR, 'libyaff_oracle.so')
+
+neigh_dtype = np.dtype([('a', 'i8'), ('b', 'i8'), ('d', 'f8'), ('dx', 'f8'), ('dy', 'f8'),
+                        ('dz', 'f8'), ('r0', 'i8'), ('r1', 'i8'), ('r2', 'i8')])
+scaling_dtype = np.dtype([('a', 'i8'), ('b', 'i8'), ('scale', 'f8'), ('nbond', 'i8')])
+delta_dtype = np.dtype([('dx', 'f8'), ('dy', 'f8'), ('dz', 'f8'), ('i', 'i8'), ('j', 'i8'),
+                        ('gx', 'f8'), ('gy', 'f8'), ('gz', 'f8')])
+iclist_dtype = np.dtype([('kind', 'i8'), ('i0', 'i8'), ('sign0', 'i8'), ('i1', 'i8'),
+                         ('sign1', 'i8'), ('i2', 'i8'), ('sign2', 'i8'), ('i3', 'i8'),
+                         ('sign3', 'i8'), ('value', 'f8'), ('grad', 'f8')])
+vlist_dtype = np.dtype([('kind', 'i8'), ('par0', 'f8'), ('par1', 'f8'), ('par2', 'f8'),
+                        ('par3', 'f8'), ('par4', 'f8'), ('par5', 'f8'), ('ic0', 'i8'),
+                        ('ic1', 'i8'), ('energy', 'f8')])
+
+_lib = None
+
+
+def build():
+    """Compile yaff_oracle.c (gcc, no FMA contraction) if stale."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + '.%d.tmp' % os.getpid()
+    subprocess.check_call(['gcc', '-O2', '-ffp-contract=off', '-fPIC', '-shared',
+                           '-o', tmp, SRC, '-lm'])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        I64 = ctypes.c_int64
+        D = ctypes.c_double
+        INT = ctypes.c_int
+        L.orc_nlist_build.restype = I64
+        L.orc_nlist_build.argtypes = [P, I64, D, P, P, P, INT, I64, I64, P, I64]
+        L.orc_nlist_recompute.restype = None
+        L.orc_nlist_recompute.argtypes = [P, P, P, P, INT, P, I64]
+        L.orc_pair_compute.restype = D
+        L.orc_pair_compute.argtypes = [P, I64, P, I64, INT, P, P, P, P, P, D, D, D, INT, D, P, P]
+        L.orc_ewald_reci.restype = D
+        L.orc_ewald_reci.argtypes = [P, I64, I64, I64, P, P, P, D, D, P, D, D, P, P, P]
+        L.orc_ewald_corr.restype = D
+        L.orc_ewald_corr.argtypes = [P, P, P, P, INT, D, P, I64, D, P, P, I64, I64, I64]
+        L.orc_ewald_prefactors.restype = None
+        L.orc_ewald_prefactors.argtypes = [P, D, D, P, D, P]
+        L.orc_ewald_structurefactors.restype = None
+        L.orc_ewald_structurefactors.argtypes = [P, I64, P, P, P, D, P, P]
+        L.orc_ewald_deltae.restype = D
+        L.orc_ewald_deltae.argtypes = [P, P, P, P, P, I64]
+        L.orc_dlist_forward.restype = None
+        L.orc_dlist_forward.argtypes = [P, P, P, INT, P, I64]
+        L.orc_dlist_back.restype = None
+        L.orc_dlist_back.argtypes = [P, P, P, I64]
+        L.orc_iclist_forward.restype = INT
+        L.orc_iclist_forward.argtypes = [P, P, I64]
+        L.orc_iclist_back.restype = INT
+        L.orc_iclist_back.argtypes = [P, P, I64]
+        L.orc_vlist_forward.restype = D
+        L.orc_vlist_forward.argtypes = [P, P, I64]
+        L.orc_vlist_back.restype = None
+        L.orc_vlist_back.argtypes = [P, P, I64]
+        L.orc_mic_vec.restype = None
+        L.orc_mic_vec.argtypes = [P, P, P, INT]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleCell(object):
+    """Cell vectors, reciprocal vectors, spacings and volume computed the way
+    the reference Cell does (yaff/pes/ext.pyx:103-131, cell.c:37-79)."""
+
+    def __init__(self, rvecs):
+        rvecs = np.asarray(rvecs, dtype=np.float64)
+        if rvecs.size == 0:
+            self.nvec = 0
+            self.rvecs = np.identity(3)
+            self.gvecs = np.identity(3)
+        else:
+            self.nvec = len(rvecs)
+            up, sp, vt = np.linalg.svd(rvecs, full_matrices=True)
+            s = np.ones(3)
+            s[:self.nvec] = sp
+            u = np.identity(3)
+            u[:self.nvec, :self.nvec] = up
+            mod = np.dot(u * s, vt)
+            mod[:self.nvec] = rvecs
+            self.rvecs = np.ascontiguousarray(mod)
+            self.gvecs = np.ascontiguousarray(np.dot(u / s, vt))
+        g = self.gvecs
+        r = self.rvecs
+        self.rspacings = np.array([1.0 / np.sqrt(g[i, 0] * g[i, 0] + g[i, 1] * g[i, 1] + g[i, 2] * g[i, 2])
+                                   for i in range(3)])
+        self.gspacings = np.array([1.0 / np.sqrt(r[i, 0] * r[i, 0] + r[i, 1] * r[i, 1] + r[i, 2] * r[i, 2])
+                                   for i in range(3)])
+        if self.nvec == 3:
+            rv = r.ravel()
+            self.volume = abs(rv[0] * (rv[4] * rv[8] - rv[5] * rv[7]) +
+                              rv[1] * (rv[5] * rv[6] - rv[3] * rv[8]) +
+                              rv[2] * (rv[3] * rv[7] - rv[4] * rv[6]))
+        else:
+            self.volume = 0.0
+
+    def mic(self, delta):
+        d = np.ascontiguousarray(delta, dtype=np.float64).copy()
+        lib().orc_mic_vec(_p(d), _p(self.rvecs), _p(self.gvecs), self.nvec)
+        return d
+
+
+def build_scalings(natom, bonds, scalings):
+    """Sorted exclusion table (a > b, scale, nbond) from the bond graph, as
+    the reference Scalings builds it (yaff/pes/scaling.py:58-105)."""
+    s1, s2, s3, s4 = scalings
+    if bonds is None or len(bonds) == 0:
+        return np.zeros(0, scaling_dtype)
+    n1 = [set() for _ in range(natom)]
+    for i, j in bonds:
+        n1[int(i)].add(int(j))
+        n1[int(j)].add(int(i))
+    # graph distances up to 4 bonds
+    shells = []
+    for i0 in range(natom):
+        dist = {i0: 0}
+        front = [i0]
+        for depth in range(1, 5):
+            nxt = []
+            for a in front:
+                for b in n1[a]:
+                    if b not in dist:
+                        dist[b] = depth
+                        nxt.append(b)
+            front = nxt
+        shells.append(dist)
+    rows = []
+    for i0 in range(natom):
+        for i1, depth in shells[i0].items():
+            if i1 >= i0 or depth == 0:
+                continue
+            sc = (None, s1, s2, s3, s4)[depth]
+            if sc < 1.0:
+                rows.append((i0, i1, sc, depth))
+    rows.sort()
+    return np.array(rows, dtype=scaling_dtype)
+
+
+class OracleForceField(object):
+    """Reference-order FP64 evaluation of a configs.py spec on the CPU."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        self.natom = len(spec['pos'])
+        self.pos = np.ascontiguousarray(spec['pos'], dtype=np.float64).copy()
+        self.cell = OracleCell(spec['rvecs'])
+        self.nlow = spec.get('nlow', 0)
+        nh = spec.get('nhigh', -1)
+        self.nhigh = self.natom if nh == -1 else nh
+        self.rcut = spec['rcut']
+        self.skin = spec['skin']
+        self.stab = build_scalings(self.natom, spec.get('bonds'), spec['scalings'])
+        self.neighs = np.zeros(16, neigh_dtype)
+        self.nneigh = 0
+        self.pos_old = None
+        self.rebuild_next = True
+        self.update_rmax()
+        self._setup_valence()
+        self.part_energies = {}
+        self.part_gpos = {}
+        self.part_vtens = {}
+
+    # -- neighbour list (yaff/pes/nlist.py:119-218) --
+    def update_rmax(self):
+        if self.cell.nvec > 0:
+            self.rmax = np.ceil((self.rcut + self.skin) / self.cell.rspacings[:self.cell.nvec] - 0.5).astype(np.int64)
+        else:
+            self.rmax = np.zeros(0, np.int64)
+        self.rebuild_next = True
+        if self.spec.get('ewald') is not None:
+            self.gmax = np.ceil(self.spec['ewald']['gcut'] / self.cell.gspacings - 0.5).astype(np.int64)
+
+    def need_rebuild(self):
+        if self.skin <= 0 or self.pos_old is None or self.rebuild_next:
+            return True
+        disp = np.sqrt(((self.pos - self.pos_old) ** 2).sum(axis=1).max())
+        disp *= 2 * (self.rmax.max() + 1)
+        return disp >= self.skin
+
+    def update_nlist(self):
+        L = lib()
+        if self.need_rebuild():
+            rmax3 = np.zeros(3, np.int64)
+            rmax3[:len(self.rmax)] = self.rmax
+            while True:
+                n = L.orc_nlist_build(_p(self.pos), self.natom, self.rcut + self.skin, _p(rmax3),
+                                      _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.nvec,
+                                      self.nlow, self.nhigh, _p(self.neighs), len(self.neighs))
+                if n <= len(self.neighs):
+                    break
+                self.neighs = np.zeros(int(n * 1.1) + 16, neigh_dtype)
+            self.nneigh = int(n)
+            if self.skin > 0:
+                self.pos_old = self.pos.copy()
+            self.rebuild_next = False
+            return True
+        L.orc_nlist_recompute(_p(self.pos), _p(self.pos_old), _p(self.cell.rvecs),
+                              _p(self.cell.gvecs), self.cell.nvec, _p(self.neighs), self.nneigh)
+        return False
+
+    def pair_set(self):
+        """Sorted (a, b, r0, r1, r2) rows of the current list (int64 array)."""
+        nb = self.neighs[:self.nneigh]
+        keys = np.stack([nb['a'], nb['b'], nb['r0'], nb['r1'], nb['r2']], 1)
+        order = np.lexsort(keys.T[::-1])
+        return keys[order], nb[order]
+
+    # -- valence layers (yaff/pes/dlist.py, iclist.py, vlist.py) --
+    def _setup_valence(self):
+        spec = self.spec
+        bt = spec.get('bond_terms')
+        at = spec.get('bend_terms')
+        self.has_valence = (bt is not None and len(bt)) or (at is not None and len(at))
+        if not self.has_valence:
+            return
+        deltas = []
+        lookup = {}
+
+        def add_delta(i, j):
+            row = lookup.get((i, j))
+            if row is not None:
+                return row, 1
+            row = lookup.get((j, i))
+            if row is not None:
+                return row, -1
+            lookup[(i, j)] = len(deltas)
+            deltas.append((i, j))
+            return len(deltas) - 1, 1
+
+        ics = []
+        iclook = {}
+
+        def add_ic(kind, pairs):
+            rs = [add_delta(i, j) for i, j in pairs]
+            key = (kind,) + sum(rs, ())
+            row = iclook.get(key)
+            if row is None:
+                row = len(ics)
+                iclook[key] = row
+                rec = [kind, -1, 0, -1, 0, -1, 0, -1, 0]
+                for k, (r, s) in enumerate(rs):
+                    rec[1 + 2 * k] = r
+                    rec[2 + 2 * k] = s
+                ics.append(rec)
+            return row
+
+        terms = []
+        for i, j, K, r0 in (bt if bt is not None else []):
+            terms.append((0, K, r0, add_ic(0, [(int(i), int(j))])))
+        for i, j, k, K, t0 in (at if at is not None else []):
+            terms.append((0, K, t0, add_ic(2, [(int(j), int(i)), (int(j), int(k))])))
+        self.dl = np.zeros(len(deltas), delta_dtype)
+        for r, (i, j) in enumerate(deltas):
+            self.dl[r]['i'] = i
+            self.dl[r]['j'] = j
+        self.ic = np.zeros(len(ics), iclist_dtype)
+        for r, rec in enumerate(ics):
+            self.ic[r] = tuple(rec) + (np.nan, np.nan)
+        self.vt = np.zeros(len(terms), vlist_dtype)
+        for r, (kind, K, q0, ic0) in enumerate(terms):
+            self.vt[r] = (kind, K, q0, -1, -1, -1, -1, ic0, -1, np.nan)
+
+    def compute_valence(self, gpos, vtens):
+        L = lib()
+        c = self.cell
+        L.orc_dlist_forward(_p(self.pos), _p(c.rvecs), _p(c.gvecs), c.nvec, _p(self.dl), len(self.dl))
+        assert L.orc_iclist_forward(_p(self.dl), _p(self.ic), len(self.ic)) == 0
+        e = L.orc_vlist_forward(_p(self.ic), _p(self.vt), len(self.vt))
+        if gpos is not None or vtens is not None:
+            L.orc_vlist_back(_p(self.ic), _p(self.vt), len(self.vt))
+            assert L.orc_iclist_back(_p(self.dl), _p(self.ic), len(self.ic)) == 0
+            L.orc_dlist_back(_p(gpos), _p(vtens), _p(self.dl), len(self.dl))
+        return e
+
+    # -- parts --
+    def part_names(self):
+        names = ['pair_%s' % p['kind'] for p in self.spec['pair']]
+        if self.spec.get('ewald') is not None and self.cell.nvec == 3:
+            names += ['ewald_reci', 'ewald_cor', 'ewald_neut']
+        if self.has_valence:
+            names.append('valence')
+        return names
+
+    def _pair(self, pdef, gpos, vtens):
+        spec = self.spec
+        kind = {'lj': 0, 'mm3': 1, 'ei': 2}[pdef['kind']]
+        tr = spec.get('tr')
+        if pdef['kind'] == 'ei':
+            tr = None if not pdef.get('smooth', False) else tr
+        trk, trp = 0, 0.0
+        if tr is not None:
+            trk = {'hammer': 1, 'switch3': 2}[tr[0]]
+            trp = tr[1]
+        sig = pdef.get('sigmas')
+        eps = pdef.get('epsilons')
+        op = pdef.get('onlypaulis')
+        q = spec['charges']
+        radii = pdef.get('radii')
+        if kind == 2 and radii is None:
+            radii = np.zeros(self.natom)
+        ew = spec.get('ewald')
+        alpha = ew['alpha'] if (ew is not None and self.cell.nvec == 3) else 0.0
+        keep = [np.ascontiguousarray(x) if x is not None else None for x in (sig, eps, op, q, radii)]
+        if keep[2] is not None:
+            keep[2] = keep[2].astype(np.int32)
+        return lib().orc_pair_compute(
+            _p(self.neighs), self.nneigh, _p(self.stab), len(self.stab), kind,
+            _p(keep[0]), _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4]),
+            alpha, spec.get('dielectric', 1.0), self.rcut, trk, trp, _p(gpos), _p(vtens))
+
+    def compute(self, gpos=None, vtens=None):
+        """Total energy; gpos and vtens (if given) are ADDED to, like the
+        reference ForcePart.compute.  Per-part results are kept in
+        part_energies / part_gpos / part_vtens."""
+        spec = self.spec
+        self.update_nlist()
+        L = lib()
+        total = 0.0
+        for name in self.part_names():
+            g = np.zeros((self.natom, 3)) if gpos is not None else None
+            v = np.zeros((3, 3)) if vtens is not None else None
+            if name.startswith('pair_'):
+                pdef = [p for p in spec['pair'] if 'pair_' + p['kind'] == name][0]
+                e = self._pair(pdef, g, v)
+            elif name == 'ewald_reci':
+                ew = spec['ewald']
+                work = np.zeros(2 * self.natom) if g is not None else None
+                e = L.orc_ewald_reci(_p(self.pos), self.natom, self.nlow, self.nhigh,
+                                     _p(np.ascontiguousarray(spec['charges'])), _p(self.cell.rvecs),
+                                     _p(self.cell.gvecs), self.cell.volume, ew['alpha'], _p(self.gmax),
+                                     ew['gcut'], spec.get('dielectric', 1.0), _p(g), _p(work), _p(v))
+            elif name == 'ewald_cor':
+                ew = spec['ewald']
+                e = L.orc_ewald_corr(_p(self.pos), _p(np.ascontiguousarray(spec['charges'])),
+                                     _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.nvec,
+                                     ew['alpha'], _p(self.stab), len(self.stab),
+                                     spec.get('dielectric', 1.0), _p(g), _p(v), self.natom,
+                                     self.nlow, self.nhigh)
+            elif name == 'ewald_neut':
+                e = self._neut(v)
+            elif name == 'valence':
+                e = self.compute_valence(g, v)
+            else:
+                raise AssertionError(name)
+            if np.isnan(e):
+                raise ValueError('The energy is not-a-number (nan).')
+            self.part_energies[name] = e
+            self.part_gpos[name] = g
+            self.part_vtens[name] = v
+            if gpos is not None:
+                gpos += g
+            if vtens is not None:
+                vtens += v
+            total += e
+        return total
+
+    def _neut(self, vtens):
+        """Neutralizing background, yaff/pes/ff.py:633-669 (point charges)."""
+        q = self.spec['charges']
+        alpha = self.spec['ewald']['alpha']
+        fac = q[:].sum() ** 2 / alpha ** 2
+        fac -= q[:self.nlow].sum() ** 2 / alpha ** 2
+        fac -= q[self.nhigh:].sum() ** 2 / alpha ** 2
+        pref = fac * np.pi / (2.0 * self.spec.get('dielectric', 1.0))
+        fac = pref / self.cell.volume
+        if vtens is not None:
+            vtens.ravel()[::4] -= fac
+        return fac
+
+    def update_pos(self, pos):
+        self.pos[:] = pos

@@ -1,0 +1,72 @@
+"""Builds the reference's own ForceField from a configs.py spec.
+
+TEST INFRASTRUCTURE ONLY: used (in the container that holds the reference
+checkout) to generate golden fixtures and to pin the oracle port against the
+reference itself.  Requires oracle/build_ref.sh to have been run.
+"""
+import numpy as np
+
+import ref_shim
+
+
+def build_reference_ff(spec):
+    """Reference ForceField with the parts a spec describes, built the way the
+    reference generator does (yaff/pes/generator.py:178-240)."""
+    ref_shim.import_reference()
+    from yaff.system import System
+    from yaff.pes.ff import (ForceField, ForcePartPair, ForcePartEwaldReciprocal,
+                             ForcePartEwaldCorrection, ForcePartEwaldNeutralizing,
+                             ForcePartValence)
+    from yaff.pes.nlist import NeighborList
+    from yaff.pes.scaling import Scalings
+    from yaff.pes.ext import PairPotLJ, PairPotMM3, PairPotEI, Switch3, Hammer
+    from yaff.pes.iclist import Bond, BendAngle
+    from yaff.pes.vlist import Harmonic
+
+    natom = len(spec['pos'])
+    bonds = spec.get('bonds')
+    system = System(numbers=np.full(natom, 6), pos=spec['pos'].copy(),
+                    rvecs=spec['rvecs'].copy() if len(spec['rvecs']) else None,
+                    charges=None if spec['charges'] is None else spec['charges'].copy(),
+                    bonds=np.zeros((0, 2), int) if bonds is None else np.asarray(bonds, dtype=int),
+                    masses=spec['masses'].copy())
+    nlist = NeighborList(system, skin=spec['skin'], nlow=spec.get('nlow', 0),
+                         nhigh=spec.get('nhigh', -1))
+    scalings = Scalings(system, *spec['scalings'])
+    tr = spec.get('tr')
+    trobj = None
+    if tr is not None:
+        trobj = Switch3(tr[1]) if tr[0] == 'switch3' else Hammer(tr[1])
+    parts = []
+    ew = spec.get('ewald')
+    alpha = ew['alpha'] if (ew is not None and system.cell.nvec == 3) else 0.0
+    for p in spec['pair']:
+        if p['kind'] == 'lj':
+            pp = PairPotLJ(p['sigmas'].copy(), p['epsilons'].copy(), spec['rcut'], trobj)
+        elif p['kind'] == 'mm3':
+            pp = PairPotMM3(p['sigmas'].copy(), p['epsilons'].copy(),
+                            np.asarray(p['onlypaulis'], dtype=np.intc).copy(), spec['rcut'], trobj)
+        elif p['kind'] == 'ei':
+            radii = p.get('radii')
+            pp = PairPotEI(spec['charges'].copy(), alpha, spec['rcut'],
+                           trobj if p.get('smooth', False) else None,
+                           spec.get('dielectric', 1.0), None if radii is None else radii.copy())
+        else:
+            raise ValueError(p['kind'])
+        parts.append(ForcePartPair(system, nlist, scalings, pp))
+    if ew is not None and system.cell.nvec == 3:
+        diel = spec.get('dielectric', 1.0)
+        nlow, nhigh = spec.get('nlow', 0), spec.get('nhigh', -1)
+        parts.append(ForcePartEwaldReciprocal(system, ew['alpha'], ew['gcut'], diel, nlow, nhigh))
+        parts.append(ForcePartEwaldCorrection(system, ew['alpha'], scalings, diel, nlow, nhigh))
+        parts.append(ForcePartEwaldNeutralizing(system, ew['alpha'], diel, nlow, nhigh))
+    bt = spec.get('bond_terms')
+    at = spec.get('bend_terms')
+    if (bt is not None and len(bt)) or (at is not None and len(at)):
+        pv = ForcePartValence(system)
+        for i, j, K, r0 in bt:
+            pv.add_term(Harmonic(K, r0, Bond(int(i), int(j))))
+        for i, j, k, K, t0 in at:
+            pv.add_term(Harmonic(K, t0, BendAngle(int(i), int(j), int(k))))
+        parts.append(pv)
+    return ForceField(system, parts, nlist)

@@ -1,0 +1,292 @@
+"""Seeded synthetic systems for the force-evaluation workloads.
+
+Every generator returns a *spec*: a plain dict of numpy arrays and scalars in
+atomic units that fully describes a system and its force field.  The same spec
+builds the GPU force field (``yaff_gb300.build_forcefield``) and, in tests,
+the CPU oracle, so both sides always see identical inputs.
+
+Spec keys
+---------
+name           str
+pos            (N, 3) float64, bohr
+rvecs          (3, 3) float64 rows = cell vectors (or shape (0, 3))
+charges        (N,) float64 or None
+masses         (N,) float64 (a.u. of mass)
+bonds          (nb, 2) int64 or None
+pair           list of dicts: {'kind': 'lj', 'sigmas', 'epsilons'} |
+               {'kind': 'mm3', 'sigmas', 'epsilons', 'onlypaulis'} |
+               {'kind': 'ei', 'radii' (optional)}
+rcut, skin     float (bohr)
+tr             None | ('switch3', width) | ('hammer', tau)
+ewald          None | {'alpha': a, 'gcut': g}      (reciprocal + corr + neut)
+dielectric     float
+scalings       (scale1, scale2, scale3, scale4)
+bond_terms     (nbt, 4): i, j, K, r0      harmonic bonds (Bond + Harmonic)
+bend_terms     (nat, 5): i, j, k, K, th0  harmonic bends (BendAngle + Harmonic)
+nlow, nhigh    ints (nhigh = -1 means N)
+"""
+import math
+
+import numpy as np
+
+from .units import angstrom, kjmol, amu, deg
+
+MASS_O = 15.999 * amu
+MASS_H = 1.008 * amu
+MASS_GENERIC = 12.011 * amu
+
+
+def triclinic_rvecs(a, b, c, alpha, beta, gamma):
+    """Cell vectors (rows) for lengths a, b, c and angles alpha, beta, gamma
+    (radians), a along x and b in the xy plane."""
+    ca, cb, cg = math.cos(alpha), math.cos(beta), math.cos(gamma)
+    sg = math.sin(gamma)
+    cx = c * cb
+    cy = c * (ca - cb * cg) / sg
+    cz = math.sqrt(max(c * c - cx * cx - cy * cy, 0.0))
+    return np.array([[a, 0.0, 0.0], [b * cg, b * sg, 0.0], [cx, cy, cz]])
+
+
+def ewald_params(rcut, alpha_scale=3.5, gcut_scale=1.1):
+    """alpha = alpha_scale / rcut and gcut = gcut_scale * alpha, the rule of the
+    reference's force-field generator (yaff/pes/generator.py:210, :229)."""
+    alpha = alpha_scale / rcut
+    return {'alpha': alpha, 'gcut': gcut_scale * alpha}
+
+
+def _base_spec(name, pos, rvecs):
+    n = len(pos)
+    return {
+        'name': name, 'pos': np.ascontiguousarray(pos, dtype=np.float64),
+        'rvecs': np.ascontiguousarray(rvecs, dtype=np.float64),
+        'charges': None, 'masses': np.full(n, MASS_GENERIC), 'bonds': None,
+        'pair': [], 'rcut': 0.0, 'skin': 0.0, 'tr': None, 'ewald': None,
+        'dielectric': 1.0, 'scalings': (0.0, 0.0, 1.0, 1.0),
+        'bond_terms': np.zeros((0, 4)), 'bend_terms': np.zeros((0, 5)),
+        'nlow': 0, 'nhigh': -1,
+    }
+
+
+def lattice_lj_ei(nside=10, spacing=2.5, jitter=0.3, rcut=12.0, skin=0.0, seed=0,
+                  name=None):
+    """Simple-cubic lattice of alternating A/B atoms with LJ + EI + Ewald.
+
+    The 1,000-atom default is the plain FP64 workload: 10x10x10 lattice,
+    2.5 A spacing, +-0.3 A uniform jitter (seed 0) in a 25 A cube; A: +0.5 e,
+    sigma 3.0 A, eps 0.5 kJ/mol; B: -0.5 e, sigma 3.2 A, eps 0.8 kJ/mol
+    (Lorentz-Berthelot via the LJ mixing rule); rcut 12 A, skin 0,
+    alpha_scale 3.5, gcut_scale 1.1, no exclusions.
+    """
+    rng = np.random.default_rng(seed)
+    g = np.arange(nside, dtype=float)
+    grid = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    pos = (grid * spacing + rng.uniform(-jitter, jitter, grid.shape)) * angstrom
+    box = nside * spacing * angstrom
+    spec = _base_spec(name or 'lattice%d' % (nside ** 3), pos, np.eye(3) * box)
+    n = len(pos)
+    isb = (np.arange(n) % 2 == 1)
+    spec['charges'] = np.where(isb, -0.5, 0.5)
+    sig = np.where(isb, 3.2, 3.0) * angstrom
+    eps = np.where(isb, 0.8, 0.5) * kjmol
+    spec['pair'] = [{'kind': 'lj', 'sigmas': sig, 'epsilons': eps}, {'kind': 'ei'}]
+    spec['rcut'] = rcut * angstrom
+    spec['skin'] = skin * angstrom
+    spec['ewald'] = ewald_params(spec['rcut'])
+    return spec
+
+
+def _random_rotations(rng, n):
+    """n uniformly random rotation matrices (from uniform unit quaternions)."""
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1),
+    ], 1)
+
+
+def water_geometry():
+    """Body-frame coordinates (O, H, H) of the 3-site water: O-H 0.96 A,
+    H-O-H 104.5 deg, O at the origin."""
+    half = 0.5 * 104.5 * deg
+    r = 0.96 * angstrom
+    return np.array([[0.0, 0.0, 0.0],
+                     [r * math.sin(half), 0.0, r * math.cos(half)],
+                     [-r * math.sin(half), 0.0, r * math.cos(half)]])
+
+
+def flexible_water(nside=20, box=62.1, jitter=0.2, rcut=10.0, skin=1.0, seed=1,
+                   name=None):
+    """Flexible 3-site water box with LJ (O only) + EI + Ewald + valence.
+
+    The default is the 8,000-molecule (24,000-atom) NVE workload: molecule
+    centres on a jittered 20^3 lattice in a 62.1 A cube, seeded uniformly
+    random orientations, q(O) -0.82 e, q(H) +0.41 e, LJ on O (sigma 3.166 A,
+    eps 0.65 kJ/mol), harmonic bonds K 4000 kJ/mol/A^2, r0 1.0 A, harmonic
+    bends K 300 kJ/mol/rad^2, theta0 109.47 deg, 1-2 and 1-3 pairs excluded,
+    rcut 10 A, skin 1 A.
+    """
+    rng = np.random.default_rng(seed)
+    spacing = box / nside
+    g = np.arange(nside, dtype=float)
+    centres = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    centres = (centres * spacing + rng.uniform(-jitter, jitter, centres.shape)) * angstrom
+    nmol = len(centres)
+    rot = _random_rotations(rng, nmol)
+    body = water_geometry()
+    pos = (centres[:, None, :] + np.einsum('mij,aj->mai', rot, body)).reshape(-1, 3)
+    spec = _base_spec(name or 'water%d' % nmol, pos, np.eye(3) * box * angstrom)
+    n = 3 * nmol
+    iso = (np.arange(n) % 3 == 0)
+    spec['charges'] = np.where(iso, -0.82, 0.41)
+    spec['masses'] = np.where(iso, MASS_O, MASS_H)
+    sig = np.where(iso, 3.166 * angstrom, 0.0)
+    eps = np.where(iso, 0.65 * kjmol, 0.0)
+    spec['pair'] = [{'kind': 'lj', 'sigmas': sig, 'epsilons': eps}, {'kind': 'ei'}]
+    o = 3 * np.arange(nmol)
+    spec['bonds'] = np.stack([np.stack([o, o + 1], 1), np.stack([o, o + 2], 1)], 1).reshape(-1, 2)
+    kb = 4000.0 * kjmol / angstrom ** 2
+    spec['bond_terms'] = np.column_stack([spec['bonds'].astype(float),
+                                          np.full(2 * nmol, kb), np.full(2 * nmol, 1.0 * angstrom)])
+    ka = 300.0 * kjmol
+    spec['bend_terms'] = np.column_stack([(o + 1).astype(float), o.astype(float), (o + 2).astype(float),
+                                          np.full(nmol, ka), np.full(nmol, 109.47 * deg)])
+    spec['scalings'] = (0.0, 0.0, 1.0, 1.0)
+    spec['rcut'] = rcut * angstrom
+    spec['skin'] = skin * angstrom
+    spec['ewald'] = ewald_params(spec['rcut'])
+    return spec
+
+
+def _rsa_fill(rng, rvecs, natom, dmin, max_tries=200):
+    """Random sequential insertion of natom points with minimum image distance
+    dmin in the periodic cell rvecs (rows).  Uses a fractional grid whose
+    cells are at least dmin wide, so only the 27 surrounding grid cells are
+    checked per trial."""
+    gvecs = np.linalg.inv(rvecs).T
+    spac = 1.0 / np.linalg.norm(gvecs, axis=1)
+    ng = np.maximum((spac / dmin).astype(int), 1)
+    grid = {}
+    out = np.empty((natom, 3))
+    dmin2 = dmin * dmin
+    count = 0
+    batch = 4096
+    while count < natom:
+        frac = rng.random((batch, 3))
+        for f in frac:
+            if count >= natom:
+                break
+            cell = tuple((f * ng).astype(int) % ng)
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        key = ((cell[0] + dx) % ng[0], (cell[1] + dy) % ng[1], (cell[2] + dz) % ng[2])
+                        lst = grid.get(key)
+                        if not lst:
+                            continue
+                        df = out[lst] - f @ rvecs
+                        fr = df @ gvecs.T
+                        fr -= np.round(fr)
+                        dd = fr @ rvecs
+                        if (np.einsum('ij,ij->i', dd, dd) < dmin2).any():
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                out[count] = f @ rvecs
+                grid.setdefault(cell, []).append(count)
+                count += 1
+    return out
+
+
+def triclinic_mm3_ei(natom=50000, density=50000 / 5.0313e5, angle=75.0, dmin=1.8,
+                     rcut=12.0, skin=1.0, seed=2, name=None, a=None):
+    """Triclinic exp-6 (MM3) + EI + Ewald system.
+
+    The default is the 50,000-atom precision-sweep workload: a=b=c=82 A,
+    alpha=beta=gamma=75 deg, three species (atom i has species i % 3) with
+    charges +1.2/-0.6/-0.6 e, MM3 sigma 3.4/3.0/3.0 A, eps 0.3/0.25/0.25
+    kJ/mol (the reference's MM3 mixing sums the sigmas), placed by seeded
+    random sequential insertion with a 1.8 A minimum separation; rcut 12 A,
+    skin 1 A, alpha_scale 3.5, gcut_scale 1.1.  50,000 is not a multiple of
+    three, so the 1:1:1 ratio leaves a net charge of +0.6 e, which the
+    neutralizing-background part accounts for.  Smaller natom keep the number
+    density and shrink the cell.
+    """
+    rng = np.random.default_rng(seed)
+    ang = angle * deg
+    if a is None:
+        if natom == 50000 and abs(density - 50000 / 5.0313e5) < 1e-12:
+            a = 82.0
+        else:
+            unit = triclinic_rvecs(1.0, 1.0, 1.0, ang, ang, ang)
+            a = (natom / density / abs(np.linalg.det(unit))) ** (1.0 / 3.0)
+    rvecs = triclinic_rvecs(a, a, a, ang, ang, ang) * angstrom
+    pos = _rsa_fill(rng, rvecs, natom, dmin * angstrom)
+    spec = _base_spec(name or 'triclinic%d' % natom, pos, rvecs)
+    sp = np.arange(natom) % 3
+    spec['charges'] = np.array([1.2, -0.6, -0.6])[sp]
+    spec['pair'] = [{'kind': 'mm3', 'sigmas': np.array([3.4, 3.0, 3.0])[sp] * angstrom,
+                     'epsilons': np.array([0.3, 0.25, 0.25])[sp] * kjmol,
+                     'onlypaulis': np.zeros(natom, np.int32)},
+                    {'kind': 'ei'}]
+    spec['rcut'] = rcut * angstrom
+    spec['skin'] = skin * angstrom
+    spec['ewald'] = ewald_params(spec['rcut'])
+    return spec
+
+
+def cfg0():
+    """1,000-atom LJ + EI + Ewald lattice (plain FP64 parity workload)."""
+    return lattice_lj_ei(name='cfg0')
+
+
+def cfg1():
+    """8,000-molecule flexible water NVE workload."""
+    return flexible_water(name='cfg1')
+
+
+def cfg2():
+    """50,000-atom triclinic MM3 + EI + Ewald workload (the headline)."""
+    return triclinic_mm3_ei(name='cfg2')
+
+
+def serving_request(natom, seed, rcut=10.0, density=0.064):
+    """One request of the batched-replica serving workload: an LJ + EI +
+    Ewald lattice-like system of natom atoms in a cube at 0.064 atoms/A^3
+    with rcut 10 A (A/B parameters of the 1,000-atom lattice)."""
+    rng = np.random.default_rng(seed)
+    box = (natom / density) ** (1.0 / 3.0)
+    nside = int(math.ceil(natom ** (1.0 / 3.0)))
+    spacing = box / nside
+    g = np.arange(nside, dtype=float)
+    grid = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    sel = rng.permutation(len(grid))[:natom]
+    pos = (grid[np.sort(sel)] + 0.5) * spacing
+    pos = (pos + rng.uniform(-0.12, 0.12, pos.shape) * spacing) * angstrom
+    spec = _base_spec('request%d_%d' % (natom, seed), pos, np.eye(3) * box * angstrom)
+    isb = (np.arange(natom) % 2 == 1)
+    spec['charges'] = np.where(isb, -0.5, 0.5)
+    if natom % 2 == 1:
+        spec['charges'] = spec['charges'].copy()
+        spec['charges'][-1] = 0.0
+    spec['pair'] = [{'kind': 'lj', 'sigmas': np.where(isb, 3.2, 3.0) * angstrom,
+                     'epsilons': np.where(isb, 0.8, 0.5) * kjmol}, {'kind': 'ei'}]
+    spec['rcut'] = rcut * angstrom
+    spec['ewald'] = ewald_params(spec['rcut'])
+    return spec
+
+
+def natom_of(spec):
+    return len(spec['pos'])
+
+
+def nhigh_of(spec):
+    nh = spec.get('nhigh', -1)
+    return natom_of(spec) if nh == -1 else nh
