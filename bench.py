@@ -1,0 +1,414 @@
+"""Benchmark: force evaluations per second on the 50,000-atom triclinic
+MM3 + EI + Ewald workload (rcut 12 A, skin 1 A, alpha_scale 3.5,
+gcut_scale 1.1), one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--precision mixed|fp64|mixed_kahan] [--natom 50000]
+
+A step is one ForceField.compute(gpos, vtens) of the whole system with a full
+neighbour-list rebuild (every step moves the atoms, so nothing is reused).
+`value`: device-resident inputs (positions already in HBM), CUDA-event
+timed per step with an L2 flush between steps outside the timed events.
+`e2e`: the same evaluation through the public Python API with host numpy
+positions in and gradient/virial/energy out (H2D + D2H inside the timing).
+Under torchrun every rank runs an independent replica (the path does not
+shard); rank 0 prints the JSON line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64', 'mixed_kahan'])
+    ap.add_argument('--natom', type=int, default=50000)
+    ap.add_argument('--fp64-steps', type=int, default=3)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+class ClockSampler(object):
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(',')])
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace('.', '').isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace('.', '').isdigit()]
+        reasons = set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith('active'):
+                    reasons.add(nm)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(smax) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def peaks():
+    path = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return d, 'measured'
+    return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}, 'fallback'
+
+
+def fp32_fma_peak(torch):
+    """FP32 CUDA-core peak (TFLOP/s, FMA = 2 flops) measured with an FMA-chain
+    kernel of the library; the measured-peaks file holds only HBM and bf16
+    tensor figures, and the pair and Ewald kernels use neither."""
+    import ctypes
+    from yaff_gb300 import _lib
+    lib = _lib.load()
+    v = float(lib.yg_probe_peak(0, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return v if v > 0 else None
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import yaff_gb300
+    from yaff_gb300 import configs, _lib
+    spec = configs.triclinic_mm3_ei(natom=args.natom) if args.natom != 50000 else configs.cfg2()
+    natom = len(spec['pos'])
+    rng = np.random.default_rng(7 + rank)
+    ff = yaff_gb300.build_forcefield(spec, precision=args.precision)
+    dev = yaff_gb300.device_of(ff.system)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
+    pos0 = spec['pos'].copy()
+    gpos = np.zeros((natom, 3))
+    vtens = np.zeros((3, 3))
+
+    def positions(step):
+        # a fresh small displacement per step: the list is rebuilt every step
+        return pos0 + rng.uniform(-0.05, 0.05, pos0.shape)
+
+    # --- device-resident value: positions staged in HBM before the timing ---
+    dpos = [torch.tensor(positions(s), dtype=torch.float64, device='cuda')
+            for s in range(args.warmup + args.steps)]
+
+    def device_step(s):
+        dev.upload_positions_device(dpos[s].data_ptr())
+        ff.system.pos[:] = 0.0  # host copy unused on this path
+        ff.nlist.update(upload=False)
+        pmask = 0
+        for p in ff.parts:
+            if isinstance(p, yaff_gb300.ForcePartPair):
+                pmask |= 1 << p._register()
+        _lib.check(dev.lib.yg_pair_compute(dev.ctx, pmask, 1), 'pair')
+        mask = pmask
+        for p in ff.parts:
+            if p.device_slot is not None and not isinstance(p, yaff_gb300.ForcePartPair):
+                p._launch(True)
+                mask |= 1 << p.device_slot
+        return mask
+
+    for s in range(args.warmup):
+        mask = device_step(s)
+        dev.get_total(mask, gpos, vtens)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = dev.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    ewald_times = []
+    for s in range(args.warmup, args.warmup + args.steps):
+        flush.fill_(float(s))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mask = device_step(s)
+        dev.get_total(mask, None, None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    # dominant kernel timing: the reciprocal-space part alone
+    reci = [p for p in ff.parts if isinstance(p, yaff_gb300.ForcePartEwaldReciprocal)][0]
+    for s in range(5):
+        flush.fill_(float(s))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        reci._launch(True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ewald_times.append(e0.elapsed_time(e1) * 1e-3)
+    clk = clocks.stop()
+    launches = dev.launch_count() - launches0
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([sum(times)], dtype=torch.float64, device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    else:
+        total = float(sum(times))
+    value = world * args.steps / total
+
+    # --- e2e through the public API: host numpy positions in, gradient out ---
+    e2e_times = []
+    for s in range(args.warmup + args.steps):
+        p = positions(s)
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ff.update_pos(p)
+        gpos[:] = 0.0
+        vtens[:] = 0.0
+        ff.compute(gpos, vtens)
+        t1 = time.perf_counter()
+        if s >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e = world * args.steps / float(sum(e2e_times))
+
+    # plain FP64 form on the same workload (few steps: GB300 FP64 is slow)
+    fp64 = None
+    if args.precision != 'fp64' and args.fp64_steps > 0:
+        dev.set_precision('fp64')
+        for s in range(1):
+            device_step(s)
+            dev.get_total(mask, None, None)
+        torch.cuda.synchronize()
+        tt = []
+        for s in range(args.fp64_steps):
+            flush.fill_(float(s))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            mask = device_step(s)
+            dev.get_total(mask, None, None)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tt.append(e0.elapsed_time(e1) * 1e-3)
+        fp64 = 1.0 / float(np.mean(tt))
+        dev.set_precision(args.precision)
+
+    pk, pk_src = peaks()
+    nk = dev.ew_nk if hasattr(dev, 'ew_nk') else None
+    nk = ff_nk(ff)
+    t_reci = float(np.mean(ewald_times))
+    flops = 18.0 * natom * nk  # algorithmic flops per atom*k of the reference's direct sum
+    fp32_peak = fp32_fma_peak(torch)
+    roof = {'bound': 'fp32', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s',
+            'peak': fp32_peak, 'peak_source': 'FP32 FMA-chain kernel in bench.py (measured-peaks file has no FP32 figure)',
+            'frac': (flops / t_reci / 1e12) / fp32_peak if fp32_peak else None, 'traffic': None,
+            'kernel': 'ewald_reciprocal (k_sfac + k_ewald_force)', 'ms_per_launch': t_reci * 1e3,
+            'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18}}
+    lat = np.array(times) * 1e3
+    out = {
+        'metric': 'force evals/s', 'value': value, 'unit': 'evals/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': {'mixed': 'fp32-terms/fp64-accum', 'fp64': 'f64',
+                                        'mixed_kahan': 'fp32-kahan'}[args.precision],
+        'data': 'synthetic (seeded random sequential insertion)',
+        'config': {'workload': 'cfg2: 50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
+                               'rebuild every step', 'natom': natom, 'precision': args.precision,
+                   'nneigh': int(ff.nlist.nneigh), 'nk': int(nk), 'l2': 'flushed (256 MB write) between steps',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99))},
+        'fp64_evals_per_s': fp64,
+        'e2e': {'value': e2e, 'unit': 'evals/s', 'h2d_bytes_per_step': natom * 24,
+                'd2h_bytes_per_step': natom * 24 + 9 * 8 + 16 * 8},
+        'gpu_launches': int(launches),
+        'clocks': clk,
+        'roofline': roof,
+        'peaks_source': pk_src,
+    }
+    return out, spec
+
+
+def ff_nk(ff):
+    import yaff_gb300
+    reci = [p for p in ff.parts if isinstance(p, yaff_gb300.ForcePartEwaldReciprocal)][0]
+    g = reci.gmax
+    cell = ff.system.cell
+    kv = 2 * np.pi * cell.gvecs
+    gc2 = (2 * np.pi * reci.gcut) ** 2
+    n = 0
+    g0, g1, g2 = np.meshgrid(np.arange(-g[0], g[0] + 1), np.arange(-g[1], g[1] + 1), np.arange(0, g[2] + 1),
+                             indexing='ij')
+    k = g0[..., None] * kv[0] + g1[..., None] * kv[1] + g2[..., None] * kv[2]
+    ksq = (k ** 2).sum(-1)
+    half = (g2 > 0) | ((g2 == 0) & (g1 > 0)) | ((g2 == 0) & (g1 == 0) & (g0 > 0))
+    n = int(((ksq <= gc2) & half).sum())
+    return n
+
+
+def cpu_sample(natom, seconds_budget=20.0):
+    """Times the oracle (the reference's algorithm restated in C, FP64, one
+    thread) on a bounded decomposition of one force evaluation and scales
+    each piece to the full workload: neighbour build on the first M atoms
+    (cost ~ M^2), pair terms on those rows, Ewald over a subset of k
+    vectors (cost ~ N * nk)."""
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import oracle
+    from yaff_gb300 import configs
+    spec = configs.cfg2() if natom == 50000 else configs.triclinic_mm3_ei(natom=natom)
+    N = len(spec['pos'])
+    L = oracle.lib()
+    cell = oracle.OracleCell(spec['rvecs'])
+    rc = spec['rcut'] + spec['skin']
+    M = min(N, 6000)
+    sub = np.ascontiguousarray(spec['pos'][:M])
+    rmax = np.zeros(3, np.int64)
+    rows = np.zeros(int(M * 500), oracle.neigh_dtype)
+    t0 = time.perf_counter()
+    n = L.orc_nlist_build(oracle._p(sub), M, rc, oracle._p(rmax), oracle._p(cell.rvecs), oracle._p(cell.gvecs), 3,
+                          0, M, oracle._p(rows), len(rows))
+    t_nl = time.perf_counter() - t0
+    t_nl_full = t_nl * (N / M) ** 2
+    st = np.zeros(0, oracle.scaling_dtype)
+    g = np.zeros((N, 3))
+    v = np.zeros((3, 3))
+    p0, p1 = spec['pair']
+    t0 = time.perf_counter()
+    L.orc_pair_compute(oracle._p(rows), min(n, len(rows)), oracle._p(st), 0, 1, oracle._p(p0['sigmas']),
+                       oracle._p(p0['epsilons']), oracle._p(np.ascontiguousarray(p0['onlypaulis'], np.int32)),
+                       None, None, 0.0, 1.0, spec['rcut'], 0, 0.0, oracle._p(g), oracle._p(v))
+    L.orc_pair_compute(oracle._p(rows), min(n, len(rows)), oracle._p(st), 0, 2, None, None, None,
+                       oracle._p(spec['charges']), oracle._p(np.zeros(N)), spec['ewald']['alpha'], 1.0,
+                       spec['rcut'], 0, 0.0, oracle._p(g), oracle._p(v))
+    t_pair = time.perf_counter() - t0
+    rows_full = 22851584.0 * (N / 50000.0)
+    t_pair_full = t_pair * rows_full / max(n, 1)
+    # Ewald over a thin slab of k vectors (gmax[0] restricted), scaled by nk
+    gmax = np.ceil(spec['ewald']['gcut'] / cell.gspacings - 0.5).astype(np.int64)
+    gsub = gmax.copy()
+    gsub[0] = 0
+    gsub[1] = 2
+    work = np.zeros(2 * N)
+    t0 = time.perf_counter()
+    L.orc_ewald_reci(oracle._p(spec['pos']), N, 0, N, oracle._p(spec['charges']), oracle._p(cell.rvecs),
+                     oracle._p(cell.gvecs), cell.volume, spec['ewald']['alpha'], oracle._p(gsub),
+                     spec['ewald']['gcut'], 1.0, oracle._p(g), oracle._p(work), oracle._p(v))
+    t_ew = time.perf_counter() - t0
+
+    def count_k(gm):
+        kv = 2 * np.pi * cell.gvecs
+        gc2 = (2 * np.pi * spec['ewald']['gcut']) ** 2
+        a, b, c = np.meshgrid(np.arange(-gm[0], gm[0] + 1), np.arange(-gm[1], gm[1] + 1), np.arange(0, gm[2] + 1),
+                              indexing='ij')
+        k = a[..., None] * kv[0] + b[..., None] * kv[1] + c[..., None] * kv[2]
+        half = (c > 0) | ((c == 0) & (b > 0)) | ((c == 0) & (b == 0) & (a > 0))
+        return int((((k ** 2).sum(-1) <= gc2) & half).sum())
+    nk_sub = count_k(gsub)
+    nk_full = count_k(gmax)
+    t_ew_full = t_ew * nk_full / max(nk_sub, 1)
+    t_eval = t_nl_full + t_pair_full + t_ew_full
+    sample = ('oracle (reference algorithm, FP64, 1 thread): nlist on first %d atoms (x(N/M)^2), pair terms on '
+              'those %d rows (x rows), Ewald over %d of %d k-vectors (x nk); measured %.1f s' %
+              (M, n, nk_sub, nk_full, t_nl + t_pair + t_ew))
+    return {'value': 1.0 / t_eval, 'unit': 'evals/s', 'cores': 1, 'kind': 'port', 'sample': sample,
+            'seconds_per_eval': t_eval, 'breakdown_s': {'nlist': t_nl_full, 'pair': t_pair_full,
+                                                        'ewald_reci': t_ew_full}}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ctx = mp.get_context('spawn')
+    res = []
+    for s in range(args.warmup + args.steps):
+        with ctx.Pool(cores) as pool:
+            outs = pool.map(cpu_sample, [args.natom] * cores)
+        if s >= args.warmup:
+            res.append(sum(o['value'] for o in outs))
+    val = float(np.mean(res))
+    one = outs[0]
+    return {'metric': 'force evals/s', 'value': val, 'unit': 'evals/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 / val, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded random sequential insertion)',
+            'impl': 'reference',
+            'config': {'workload': 'cfg2: 50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
+                                   'rebuild every step', 'natom': args.natom, 'parallelism': '%d independent '
+                                   'single-thread replicas' % cores},
+            'cpu_baseline': {'value': val, 'unit': 'evals/s', 'cores': cores, 'kind': 'port',
+                             'sample': one['sample'] + '; %d replica processes' % cores},
+            'e2e': {'value': val, 'unit': 'evals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+            'wall_s': time.perf_counter() - t0}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = 'gloo' if args.impl == 'reference' else 'nccl'
+        if args.impl == 'gb300':
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    if args.impl == 'reference':
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    out, spec = run_gb300(args, world, rank, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out['cpu_baseline'] = cpu_sample(args.natom)
+        print(json.dumps(out))
+
+
+if __name__ == '__main__':
+    main()

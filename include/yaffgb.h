@@ -1,0 +1,193 @@
+/*
+ * yaffgb.h -- C ABI of the GB300 force-evaluation library (libyaffgb.so).
+ *
+ * One yg_ctx holds the device-resident state of one periodic system: its
+ * positions, cell, neighbour list, pair-potential parameters, exclusion
+ * table, Ewald k-space tables and valence tables, and the per-part results of
+ * the last evaluation.  Every entry point takes plain pointers and sizes,
+ * returns a yg_status (never traps), and enqueues its work on the context's
+ * stream.  Results are copied out with yg_get_part / yg_get_total.
+ *
+ * Conventions kept from the reference C core: atomic units; positions are
+ * (natom, 3) row-major float64; cell vectors are rows of a 3x3 matrix and the
+ * reciprocal vectors are rows of inv(rvecs)^T; the energy, gradient (gpos) and
+ * virial (vtens) of a part are computed by the part and ADDED by the caller.
+ *
+ * Each declaration names the reference interface (file:line in the
+ * reference project) that it replaces.
+ */
+#ifndef YAFFGB_H
+#define YAFFGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct yg_ctx yg_ctx;
+
+/* status codes */
+#define YG_OK 0
+#define YG_ERR_ARG 1            /* invalid argument (bad size, index, pointer) */
+#define YG_ERR_CUDA 2           /* a CUDA runtime call failed */
+#define YG_ERR_NAN 3            /* an energy, gradient or virial was NaN */
+#define YG_ERR_UNSUPPORTED 4    /* feature outside the supported set */
+#define YG_ERR_CAPACITY 5       /* a device buffer was too small (retried internally) */
+#define YG_ERR_DENSITY 6        /* atom density too high for a neighbour-list build */
+#define YG_ERR_STATE 7          /* call order violated (e.g. compute before build) */
+
+/* precision of the pair and reciprocal-space terms */
+#define YG_FP64 0          /* plain: FP64 throughout */
+#define YG_MIXED 1         /* FP32 terms, FP64 accumulation */
+#define YG_MIXED_KAHAN 2   /* FP32 terms, Kahan-compensated FP32 accumulation */
+
+/* pair-potential kinds (yaff/pes/pair_pot.c:277, :321, :711) */
+#define YG_POT_LJ 0
+#define YG_POT_MM3 1
+#define YG_POT_EI 2
+
+/* truncation kinds (yaff/pes/truncation.c:30, :59) */
+#define YG_TR_NONE 0
+#define YG_TR_HAMMER 1
+#define YG_TR_SWITCH3 2
+
+/* result slots for yg_get_part */
+#define YG_PART_PAIR0 0    /* pair potentials 0..2 use slots 0..2 */
+#define YG_PART_EWALD_RECI 3
+#define YG_PART_EWALD_CORR 4
+#define YG_PART_VALENCE 5
+#define YG_NPART 6
+
+/* One row of the exported neighbour list; same layout as the reference's
+ * neigh_row_type (yaff/pes/nlist.h:30-35). */
+typedef struct {
+  int64_t a, b;
+  double d, dx, dy, dz;
+  int64_t r0, r1, r2;
+} yg_neigh_row;
+
+/* Human-readable text for a status code. */
+const char *yg_status_string(int status);
+
+/* Last error message recorded on this thread (for YG_ERR_CUDA / YG_ERR_ARG). */
+const char *yg_last_error(void);
+
+/* Creates a context for natom atoms on the current CUDA device; `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  No reference counterpart: the
+ * reference keeps this state in Python objects (yaff/pes/ff.py:117-168,
+ * yaff/pes/nlist.py:54-117). */
+int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out);
+int yg_destroy(yg_ctx *ctx);
+int yg_set_precision(yg_ctx *ctx, int precision);
+
+/* Cell vectors and reciprocal vectors (rows, 3x3 host arrays) as computed by
+ * the host cell object; replaces cell_update (yaff/pes/cell.c:37-79).  Only
+ * nvec == 3 is supported by the device neighbour list. */
+int yg_set_cell(yg_ctx *ctx, const double *rvecs, const double *gvecs, int nvec,
+                double volume);
+
+/* Copies positions (natom x 3 float64) into the context; `on_device` != 0
+ * means `pos` is a device pointer.  The reference reads system.pos directly
+ * (yaff/pes/ff.py:261-266). */
+int yg_set_positions(yg_ctx *ctx, const double *pos, int on_device);
+
+/* Per-atom charges (host, natom float64), used by EI and Ewald parts. */
+int yg_set_charges(yg_ctx *ctx, const double *charges);
+
+/* Exclusion / scaling table rows (a > b, scale, nbond), sorted by (a, b);
+ * replaces the stab argument of pair_pot_compute (yaff/pes/pair_pot.c:84-87)
+ * and compute_ewald_corr (yaff/pes/ewald.c:278-281). */
+int yg_set_scalings(yg_ctx *ctx, const int64_t *a, const int64_t *b,
+                    const double *scale, const int64_t *nbond, int64_t n);
+
+/* Registers pair potential `slot` (0..2).  Arrays are host, natom long; NULL
+ * when unused by the kind.  Replaces pair_data_lj_init / pair_data_mm3_init /
+ * pair_data_ei_init and pair_pot_set_rcut / set_trunc_scheme
+ * (yaff/pes/pair_pot.c:266-275, :308-319, :693-709, :48-58). */
+int yg_set_pair_pot(yg_ctx *ctx, int slot, int kind, const double *sigma,
+                    const double *epsilon, const int32_t *onlypauli,
+                    const double *radii, double alpha, double dielectric,
+                    double rcut, int tr_kind, double tr_par);
+int yg_clear_pair_pots(yg_ctx *ctx);
+
+/* Full neighbour-list rebuild for all pairs closer than rcut_total over the
+ * half space of images |r_k| <= rmax[k], restricted by nlow/nhigh.  Writes the
+ * number of half-list rows to *nneigh.  Replaces nlist_build_low plus the
+ * grow-and-resume loop (yaff/pes/nlist.c:30-131, yaff/pes/nlist.py:163-186). */
+int yg_nlist_build(yg_ctx *ctx, double rcut_total, const int64_t *rmax,
+                   int64_t nlow, int64_t nhigh, int64_t *nneigh);
+
+/* Skin path: keeps the pairs of the last rebuild and re-evaluates relative
+ * vectors from the current positions.  Replaces nlist_recompute_low
+ * (yaff/pes/nlist.c:183-232). */
+int yg_nlist_recompute(yg_ctx *ctx);
+
+/* Largest squared displacement since the last rebuild (for the skin test of
+ * yaff/pes/nlist.py:207-218). */
+int yg_nlist_max_disp2(yg_ctx *ctx, double *out);
+
+/* Exports the current half list as reference rows, sorted by (a, b, r0, r1,
+ * r2).  `rows` is host memory for `cap` rows; *n receives the row count (if
+ * *n > cap nothing is written).  Replaces reading NeighborList.neighs
+ * (yaff/pes/nlist.py:86-88). */
+int yg_nlist_export(yg_ctx *ctx, yg_neigh_row *rows, int64_t cap, int64_t *n);
+
+/* Evaluates the registered pair potentials (bit i of slot_mask = slot i) in
+ * one pass over the neighbour list.  Replaces pair_pot_compute
+ * (yaff/pes/pair_pot.c:84-176), one call per potential, with one fused
+ * traversal; per-slot results go to result slots YG_PART_PAIR0 + slot. */
+int yg_pair_compute(yg_ctx *ctx, int slot_mask, int want_grad);
+
+/* Ewald reciprocal-space term over the half sphere |k| <= 2 pi gcut with
+ * |g_k| <= gmax[k] and the nlow/nhigh split.  Replaces compute_ewald_reci
+ * (yaff/pes/ewald.c:32-150). */
+int yg_ewald_setup(yg_ctx *ctx, double alpha, double gcut, const int64_t *gmax,
+                   double dielectric, int64_t nlow, int64_t nhigh);
+int yg_ewald_reci(yg_ctx *ctx, int want_grad);
+
+/* Ewald self term and excluded-pair double counting.  Replaces
+ * compute_ewald_corr (yaff/pes/ewald.c:278-349). */
+int yg_ewald_corr(yg_ctx *ctx, int want_grad);
+
+/* Valence tables: relative vectors (i, j), internal coordinates (kind, delta
+ * rows and signs, kinds 0 bond, 1 bend cos, 2 bend angle, 5 Urey-Bradley) and
+ * harmonic terms (K, q0, ic).  Replaces the DeltaList / InternalCoordinateList
+ * / ValenceList tables (yaff/pes/dlist.py:62-118, iclist.py:77-120,
+ * vlist.py:74-110). */
+int yg_set_valence(yg_ctx *ctx, const int64_t *delta_ij, int64_t ndelta,
+                   const int64_t *ic_rows, int64_t nic, const double *vterm_pars,
+                   const int64_t *vterm_ic, int64_t nterm);
+
+/* Forward and back propagation of the valence chain.  Replaces dlist_forward
+ * / iclist_forward / vlist_forward and vlist_back / iclist_back / dlist_back
+ * (yaff/pes/dlist.c:29-69, iclist.c:314-320, :853-858, vlist.c:146-155,
+ * :260-265). */
+int yg_valence_compute(yg_ctx *ctx, int want_grad);
+
+/* Reads back the result of one part: energy, gradient (natom x 3, may be
+ * NULL) and virial (3x3, may be NULL) into host memory. */
+int yg_get_part(yg_ctx *ctx, int part, double *energy, double *gpos, double *vtens);
+
+/* Sums the parts in part_mask on the device and reads back the total energy,
+ * gradient (may be NULL) and virial (may be NULL); per-part energies go to
+ * part_energies[YG_NPART] when not NULL.  One device-to-host transfer. */
+int yg_get_total(yg_ctx *ctx, int part_mask, double *energy, double *gpos,
+                 double *vtens, double *part_energies);
+
+/* Waits for all work queued on the context's stream. */
+int yg_sync(yg_ctx *ctx);
+
+/* Number of kernels this context has launched since creation. */
+int64_t yg_launch_count(yg_ctx *ctx);
+
+/* Measurement utility (no reference counterpart): FMA-chain throughput of
+ * the FP32 (fp64 == 0) or FP64 CUDA-core pipe in TFLOP/s (FMA = 2 flops), the
+ * roofline denominator of the pair and Ewald kernels.  Negative on error. */
+double yg_probe_peak(int fp64, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,98 @@
+"""GPU: the device force path against the reference's golden fixtures.
+
+Pair set: (a, b, r0, r1, r2) identical to the reference (SHA-256 of the
+sorted keys), and on build steps d, dx, dy, dz bit-identical too.
+Energies: FP64 within 1e-10 relative, mixed within 1e-6 relative; gradients
+and virials: FP64 within 1e-9, mixed within 1e-5 relative RMS (the tolerance
+of the spec parity bar).  Energies are compared relative to the largest
+part magnitude of the case, since the total can be a near-cancelling sum.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'fp64': (1e-10, 1e-9), 'mixed': (1e-6, 1e-5), 'mixed_kahan': (1e-6, 1e-5)}
+
+
+def _digest(keys):
+    return hashlib.sha256(np.ascontiguousarray(keys, dtype='<i8').tobytes()).hexdigest()
+
+
+@pytest.fixture(scope='module')
+def ygb():
+    import yaff_gb300
+    return yaff_gb300
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed', 'mixed_kahan'])
+@pytest.mark.parametrize('name', gc.case_names())
+def test_golden_case(ygb, name, precision):
+    spec, data = gc.load(name)
+    ff = ygb.build_forcefield(spec, precision=precision)
+    etol, gtol = TOL[precision]
+    natom = len(spec['pos'])
+    for s in range(int(data['nsteps'])):
+        ff.update_pos(data['step%d_pos' % s])
+        gpos = np.zeros((natom, 3))
+        vtens = np.zeros((3, 3))
+        e = ff.compute(gpos, vtens)
+        # neighbour list: identical pair set
+        assert ff.nlist.nneigh == int(data['step%d_nneigh' % s])
+        keys, vals = gc.pair_keys_from_rows(ff.nlist.neighs)
+        assert _digest(keys) == str(data['step%d_pairs_sha256' % s]), 'pair set differs at step %d' % s
+        if ('step%d_pair_keys' % s) in data:
+            assert np.array_equal(vals, data['step%d_pair_vals' % s]), 'row values differ at step %d' % s
+        names = [str(x) for x in data['step%d_parts' % s]]
+        pe = data['step%d_part_energy' % s]
+        scale = max(abs(pe).max(), abs(float(data['step%d_energy' % s])), 1e-30)
+        assert abs(e - float(data['step%d_energy' % s])) <= etol * scale
+        for k, nm in enumerate(names):
+            part = getattr(ff, 'part_' + nm)
+            assert abs(part.energy - pe[k]) <= etol * scale, nm
+            gref = data['step%d_part_gpos' % s][k]
+            if abs(gref).max() > 0:
+                assert gc.rel_rms(part.gpos, gref) <= gtol, nm
+        assert gc.rel_rms(gpos, data['step%d_gpos' % s]) <= gtol
+        assert gc.rel_rms(vtens, data['step%d_vtens' % s]) <= gtol
+
+
+def test_nlist_bruteforce_check(ygb):
+    spec, data = gc.load('tric100img')
+    ff = ygb.build_forcefield(spec, precision='fp64')
+    ff.compute()
+    ff.nlist.check()
+
+
+def test_standalone_parts_match_fused(ygb):
+    spec, data = gc.load('water64')
+    ff = ygb.build_forcefield(spec, precision='fp64')
+    g1 = np.zeros((len(spec['pos']), 3))
+    v1 = np.zeros((3, 3))
+    e1 = ff.compute(g1, v1)
+    parts_e = {p.name: p.energy for p in ff.parts}
+    parts_g = {p.name: p.gpos.copy() for p in ff.parts}
+    g2 = np.zeros_like(g1)
+    v2 = np.zeros((3, 3))
+    e2 = 0.0
+    for p in ff.parts:
+        e2 += p.compute(g2, v2)
+        assert abs(p.energy - parts_e[p.name]) <= 1e-12 * max(1, abs(parts_e[p.name]))
+        assert np.allclose(p.gpos, parts_g[p.name], atol=1e-12)
+    assert abs(e1 - e2) < 1e-10
+    assert np.allclose(g1, g2, atol=1e-10)
+
+
+def test_nan_positions_raise(ygb):
+    spec, data = gc.load('lat216')
+    ff = ygb.build_forcefield(spec, precision='mixed')
+    ff.compute()
+    pos = spec['pos'].copy()
+    pos[3, 1] = np.nan
+    ff.update_pos(pos)
+    with pytest.raises(ValueError):
+        ff.compute(np.zeros((len(pos), 3)), np.zeros((3, 3)))

@@ -1,0 +1,20 @@
+"""yaff_gb300 -- GB300-native force evaluation behind yaff's ForceField API.
+
+The hot path of a yaff force evaluation (neighbour list, LJ / MM3 / EI pair
+terms, Ewald reciprocal / correction / neutralizing terms, bond and bend
+valence terms) runs as hand-written sm_103a CUDA kernels in libyaffgb.so,
+reached through its C ABI (include/yaffgb.h).  The Python classes keep the
+reference's constructors and ``compute(gpos, vtens)`` semantics.
+"""
+from .system import Cell, System
+from .pair import Hammer, Switch3, PairPotLJ, PairPotMM3, PairPotEI
+from .scaling import Scalings
+from .nlist import NeighborList, neigh_dtype
+from .valence import Bond, BendCos, BendAngle, UreyBradley, Harmonic
+from .ff import (ForcePart, ForceField, ForcePartPair, ForcePartEwaldReciprocal, ForcePartEwaldCorrection,
+                 ForcePartEwaldNeutralizing, ForcePartValence)
+from .device import DeviceSystem, device_of, set_default_precision, get_default_precision
+from .builder import build_system, build_forcefield
+from . import configs, units
+
+__version__ = '0.1.0'

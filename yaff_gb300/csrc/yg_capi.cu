@@ -1,0 +1,553 @@
+// yg_capi.cu -- the C ABI of libyaffgb.so (declared in include/yaffgb.h).
+//
+// Owns the device state of a system (yg_ctx), validates arguments, keeps the
+// call-order state machine (cell -> positions -> neighbour list -> parts) and
+// turns device-side conditions into status codes.  All kernels are launched on
+// the context's stream; the host only blocks where a result must come back
+// (neighbour-list capacity check, skin test, result readback).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "yg_internal.cuh"
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void yg_set_error(const std::string &msg) { g_last_error = msg; }
+
+int yg_cuda_fail(cudaError_t err, const char *what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(err);
+  return YG_ERR_CUDA;
+}
+
+int yg_alloc(void **ptr, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    return yg_cuda_fail(e, "cudaMalloc");
+  }
+  return YG_OK;
+}
+
+int yg_ensure(void **ptr, size_t *cap, size_t bytes) {
+  if (*ptr && *cap >= bytes) return YG_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  size_t want = bytes + bytes / 4 + 256;
+  int rc = yg_alloc(ptr, want);
+  if (rc) {
+    *cap = 0;
+    return rc;
+  }
+  *cap = want;
+  return YG_OK;
+}
+
+namespace {
+__global__ void k_total(const double *__restrict__ part_ev, const double *__restrict__ part_gpos, int64_t natom,
+                        int mask, int want_gpos, double *__restrict__ out) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < 10) {
+    double s = 0.0;
+    for (int p = 0; p < YG_NPART; p++)
+      if (mask & (1 << p)) s += part_ev[10 * p + t];
+    out[t] = s;
+  }
+  if (t < YG_NPART) out[10 + t] = part_ev[10 * t];
+  if (want_gpos && t < natom * 3) {
+    double s = 0.0;
+    for (int p = 0; p < YG_NPART; p++)
+      if (mask & (1 << p)) s += part_gpos[(int64_t)p * natom * 3 + t];
+    out[16 + t] = s;
+  }
+}
+
+}  // namespace
+
+// Self term of the Ewald correction, -alpha/sqrt(pi) sum q^2 over
+// [nlow, nhigh) in the reference's order (yaff/pes/ewald.c:289-292).
+double yg_host_self_energy(yg_ctx *ctx) {
+  const std::vector<double> &q = ctx->h_charge;
+  if (q.empty()) return 0.0;
+  double x = ctx->ew_alpha / 1.7724538509055160273;
+  double e = 0.0;
+  for (int64_t i = ctx->ew_nlow; i < ctx->ew_nhigh; i++) e -= x * q[i] * q[i];
+  return e;
+}
+
+extern "C" {
+
+const char *yg_status_string(int status) {
+  switch (status) {
+    case YG_OK: return "ok";
+    case YG_ERR_ARG: return "invalid argument";
+    case YG_ERR_CUDA: return "CUDA error";
+    case YG_ERR_NAN: return "not-a-number in the result";
+    case YG_ERR_UNSUPPORTED: return "unsupported";
+    case YG_ERR_CAPACITY: return "buffer capacity exceeded";
+    case YG_ERR_DENSITY: return "atom density too high";
+    case YG_ERR_STATE: return "call order violated";
+    default: return "unknown status";
+  }
+}
+
+const char *yg_last_error(void) { return g_last_error.c_str(); }
+
+int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
+  if (!out || natom <= 0 || natom > (int64_t)1 << 30) {
+    yg_set_error("natom must be in [1, 2^30]");
+    return YG_ERR_ARG;
+  }
+  if (precision < YG_FP64 || precision > YG_MIXED_KAHAN) {
+    yg_set_error("unknown precision mode");
+    return YG_ERR_ARG;
+  }
+  yg_ctx *c = new yg_ctx();
+  c->natom = natom;
+  c->precision = precision;
+  c->stream = (cudaStream_t)stream;
+  const size_t N = (size_t)natom;
+  int rc = 0;
+  rc |= yg_alloc((void **)&c->d_pos, N * 3 * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_pos_build, N * 3 * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_charge, N * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_cell_of, N * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_wimg, N * 3 * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_sorted, N * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_rank, N * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_org, N * 3 * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_x64, N * sizeof(double4_32a));
+  rc |= yg_alloc((void **)&c->d_x32, N * sizeof(float4));
+  rc |= yg_alloc((void **)&c->d_ncount, N * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_status, YG_ST_NWORDS * sizeof(int));
+  rc |= yg_alloc((void **)&c->d_part_ev, YG_NPART * 10 * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_part_gpos, (size_t)YG_NPART * N * 3 * sizeof(double));
+  rc |= yg_alloc((void **)&c->d_total, (16 + N * 3) * sizeof(double));
+  if (rc == YG_OK) rc = yg_ensure((void **)&c->d_red, &c->red_cap, 4096 * sizeof(double));
+  if (rc == YG_OK) {
+    if (cudaMallocHost((void **)&c->h_status, YG_ST_NWORDS * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost((void **)&c->h_total, (16 + N * 3) * sizeof(double)) != cudaSuccess) {
+      yg_set_error("cudaMallocHost failed");
+      rc = YG_ERR_CUDA;
+    }
+  }
+  if (rc == YG_OK) {
+    cudaError_t e = cudaMemsetAsync(c->d_charge, 0, N * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_part_ev, 0, YG_NPART * 10 * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_part_gpos, 0, (size_t)YG_NPART * N * 3 * sizeof(double), c->stream);
+    if (e != cudaSuccess) rc = yg_cuda_fail(e, "cudaMemsetAsync");
+  }
+  if (rc != YG_OK) {
+    yg_destroy(c);
+    return rc == YG_ERR_CUDA ? YG_ERR_CUDA : rc;
+  }
+  *out = c;
+  return YG_OK;
+}
+
+int yg_destroy(yg_ctx *c) {
+  if (!c) return YG_OK;
+  cudaStreamSynchronize(c->stream);
+  void *bufs[] = {c->d_pos, c->d_pos_build, c->d_charge, c->d_cell_of, c->d_wimg, c->d_sorted, c->d_rank,
+                  c->d_cell_start, c->d_cell_fill, c->d_org, c->d_x64, c->d_x32, c->d_shift64, c->d_shift32,
+                  c->d_nbr, c->d_ncount, c->d_status, c->d_excl_start, c->d_excl, c->d_stab_ab, c->d_stab_scale,
+                  c->d_pp_src, c->d_pp64, c->d_pp32, c->d_ew_pref, c->d_ew_tiles, c->d_ew_tab, c->d_ew_Spart,
+                  c->d_ew_S, c->d_ew_W, c->d_ew_gpart, c->d_ew_red, c->d_delta_ij, c->d_delta, c->d_ic,
+                  c->d_icval, c->d_vpar, c->d_vic, c->d_vE, c->d_part_ev, c->d_part_gpos, c->d_total, c->d_red};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_total) cudaFreeHost(c->h_total);
+  delete c;
+  return YG_OK;
+}
+
+int yg_set_precision(yg_ctx *c, int precision) {
+  if (!c || precision < YG_FP64 || precision > YG_MIXED_KAHAN) return YG_ERR_ARG;
+  c->precision = precision;
+  return YG_OK;
+}
+
+int yg_set_cell(yg_ctx *c, const double *rvecs, const double *gvecs, int nvec, double volume) {
+  if (!c || !rvecs || !gvecs) return YG_ERR_ARG;
+  if (nvec != 3) {
+    yg_set_error("the device neighbour list supports 3D periodic cells only (nvec == 3)");
+    return YG_ERR_UNSUPPORTED;
+  }
+  if (!(volume > 0.0) || !std::isfinite(volume)) {
+    yg_set_error("cell volume must be positive");
+    return YG_ERR_ARG;
+  }
+  memcpy(c->cell.rv, rvecs, 9 * sizeof(double));
+  memcpy(c->cell.gv, gvecs, 9 * sizeof(double));
+  c->cell.volume = volume;
+  c->cell.nvec = nvec;
+  c->have_cell = 1;
+  c->have_list = 0;
+  return YG_OK;
+}
+
+int yg_set_positions(yg_ctx *c, const double *pos, int on_device) {
+  if (!c || !pos) return YG_ERR_ARG;
+  YG_CUDA(cudaMemcpyAsync(c->d_pos, pos, c->natom * 3 * sizeof(double),
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  c->have_pos = 1;
+  for (int p = 0; p < YG_NPART; p++) c->part_valid[p] = 0;
+  if (c->have_list) return yg_launch_prep_positions(c);
+  return YG_OK;
+}
+
+int yg_set_charges(yg_ctx *c, const double *charges) {
+  if (!c || !charges) return YG_ERR_ARG;
+  std::vector<double> &h = c->h_charge;
+  h.assign(charges, charges + c->natom);
+  YG_CUDA(cudaMemcpyAsync(c->d_charge, h.data(), c->natom * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_charges = 1;
+  if (c->have_list) return yg_launch_prep_positions(c);
+  return YG_OK;
+}
+
+int yg_set_scalings(yg_ctx *c, const int64_t *a, const int64_t *b, const double *scale, const int64_t *nbond,
+                    int64_t n) {
+  if (!c || n < 0 || (n > 0 && (!a || !b || !scale || !nbond))) return YG_ERR_ARG;
+  const int64_t N = c->natom;
+  double tab[5] = {1.0, 1.0, 1.0, 1.0, 1.0};
+  int seen[5] = {0, 0, 0, 0, 0};
+  std::vector<int64_t> cnt(N + 1, 0);
+  for (int64_t r = 0; r < n; r++) {
+    if (a[r] < 0 || a[r] >= N || b[r] < 0 || b[r] >= N || a[r] <= b[r] || nbond[r] < 1 || nbond[r] > 4) {
+      yg_set_error("scaling rows need 0 <= b < a < natom and 1 <= nbond <= 4");
+      return YG_ERR_ARG;
+    }
+    int k = (int)nbond[r];
+    if (seen[k] && tab[k] != scale[r]) {
+      yg_set_error("scaling rows with the same nbond must share one scale");
+      return YG_ERR_ARG;
+    }
+    seen[k] = 1;
+    tab[k] = scale[r];
+    cnt[a[r] + 1]++;
+    cnt[b[r] + 1]++;
+  }
+  for (int64_t i = 0; i < N; i++) cnt[i + 1] += cnt[i];
+  std::vector<int> start(N + 1);
+  for (int64_t i = 0; i <= N; i++) start[i] = (int)cnt[i];
+  std::vector<int2> ex(2 * n > 0 ? 2 * n : 1);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  std::vector<int2> ab(n > 0 ? n : 1);
+  std::vector<double> sc(n > 0 ? n : 1);
+  for (int64_t r = 0; r < n; r++) {
+    ex[fill[a[r]]++] = make_int2((int)b[r], (int)nbond[r]);
+    ex[fill[b[r]]++] = make_int2((int)a[r], (int)nbond[r]);
+    ab[r] = make_int2((int)a[r], (int)b[r]);
+    sc[r] = scale[r];
+  }
+  cudaFree(c->d_excl_start);
+  cudaFree(c->d_excl);
+  cudaFree(c->d_stab_ab);
+  cudaFree(c->d_stab_scale);
+  c->d_excl_start = nullptr;
+  c->d_excl = nullptr;
+  c->d_stab_ab = nullptr;
+  c->d_stab_scale = nullptr;
+  int rc;
+  if ((rc = yg_alloc((void **)&c->d_excl_start, (N + 1) * sizeof(int)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_excl, ex.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_stab_ab, ab.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_stab_scale, sc.size() * sizeof(double)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(c->d_excl_start, start.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_excl, ex.data(), ex.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_stab_ab, ab.data(), ab.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_stab_scale, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->nexcl = 2 * n;
+  c->nstab = n;
+  memcpy(c->scale_tab, tab, sizeof(tab));
+  c->have_list = 0;  // scaling codes are baked into the list
+  return YG_OK;
+}
+
+int yg_set_pair_pot(yg_ctx *c, int slot, int kind, const double *sigma, const double *epsilon,
+                    const int32_t *onlypauli, const double *radii, double alpha, double dielectric, double rcut,
+                    int tr_kind, double tr_par) {
+  if (!c || slot < 0 || slot >= YG_MAX_POT) return YG_ERR_ARG;
+  if (kind < YG_POT_LJ || kind > YG_POT_EI || tr_kind < YG_TR_NONE || tr_kind > YG_TR_SWITCH3) return YG_ERR_ARG;
+  if (!(rcut > 0.0) || !(dielectric > 0.0)) {
+    yg_set_error("rcut and dielectric must be positive");
+    return YG_ERR_ARG;
+  }
+  if ((kind == YG_POT_LJ || kind == YG_POT_MM3) && (!sigma || !epsilon)) return YG_ERR_ARG;
+  if (kind == YG_POT_MM3 && !onlypauli) return YG_ERR_ARG;
+  PairPotHost &P = c->pot[slot];
+  P = PairPotHost();
+  P.active = 1;
+  P.kind = kind;
+  P.tr_kind = tr_kind;
+  P.tr_par = tr_par;
+  P.rcut = rcut;
+  P.alpha = alpha;
+  P.dielectric = dielectric;
+  const int64_t N = c->natom;
+  if (sigma) P.sigma.assign(sigma, sigma + N);
+  if (epsilon) {
+    P.sqrteps.resize(N);
+    for (int64_t i = 0; i < N; i++) {
+      if (epsilon[i] < 0.0) {
+        yg_set_error("epsilon must be non-negative");
+        return YG_ERR_ARG;
+      }
+      P.sqrteps[i] = std::sqrt(epsilon[i]);
+    }
+  }
+  if (onlypauli) P.onlypauli.assign(onlypauli, onlypauli + N);
+  if (radii) {
+    bool any = false;
+    for (int64_t i = 0; i < N; i++) any |= (radii[i] != 0.0);
+    if (any) {
+      P.radius2.resize(N);
+      for (int64_t i = 0; i < N; i++) P.radius2[i] = radii[i] * radii[i];
+    }
+  }
+  c->pp_dirty = 1;
+  if (c->have_list) return yg_pack_pair_params(c);
+  return YG_OK;
+}
+
+int yg_clear_pair_pots(yg_ctx *c) {
+  if (!c) return YG_ERR_ARG;
+  for (int p = 0; p < YG_MAX_POT; p++) c->pot[p] = PairPotHost();
+  c->pp_dirty = 1;
+  return YG_OK;
+}
+
+int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nlow, int64_t nhigh,
+                   int64_t *nneigh) {
+  if (!c || !rmax || !(rcut_total > 0.0)) return YG_ERR_ARG;
+  if (!c->have_cell || !c->have_pos) {
+    yg_set_error("set the cell and the positions before building the neighbour list");
+    return YG_ERR_STATE;
+  }
+  if (nlow < 0 || nhigh < nlow || nhigh > c->natom) {
+    yg_set_error("need 0 <= nlow <= nhigh <= natom");
+    return YG_ERR_ARG;
+  }
+  if (c->natom / c->cell.volume > 10.0) {
+    yg_set_error("Atom density too high");
+    return YG_ERR_DENSITY;
+  }
+  for (int k = 0; k < 3; k++) {
+    if (rmax[k] < 0 || rmax[k] > 1000) return YG_ERR_ARG;
+    c->rmax[k] = rmax[k];
+  }
+  c->rcut_total = rcut_total;
+  c->nlow = nlow;
+  c->nhigh = nhigh;
+  int retry = 0;
+  int rc = yg_launch_nlist_build(c, rcut_total * rcut_total, &retry);
+  if (rc) {
+    c->have_list = 0;
+    return rc;
+  }
+  for (int p = 0; p < YG_NPART; p++) c->part_valid[p] = 0;
+  if (nneigh) *nneigh = c->nneigh;
+  return YG_OK;
+}
+
+int yg_nlist_recompute(yg_ctx *c) {
+  if (!c) return YG_ERR_ARG;
+  if (!c->have_list) {
+    yg_set_error("no neighbour list to recompute");
+    return YG_ERR_STATE;
+  }
+  c->list_recomputed = 1;
+  return yg_launch_prep_positions(c);
+}
+
+int yg_nlist_max_disp2(yg_ctx *c, double *out) {
+  if (!c || !out) return YG_ERR_ARG;
+  if (!c->have_list) {
+    *out = INFINITY;
+    return YG_OK;
+  }
+  return yg_launch_max_disp2(c, out);
+}
+
+int yg_nlist_export(yg_ctx *c, yg_neigh_row *rows, int64_t cap, int64_t *n) {
+  if (!c || !n) return YG_ERR_ARG;
+  if (!c->have_list) {
+    yg_set_error("no neighbour list");
+    return YG_ERR_STATE;
+  }
+  return yg_launch_nlist_export(c, rows, cap, n);
+}
+
+int yg_pair_compute(yg_ctx *c, int slot_mask, int want_grad) {
+  if (!c) return YG_ERR_ARG;
+  if (!c->have_list) {
+    yg_set_error("build the neighbour list first");
+    return YG_ERR_STATE;
+  }
+  for (int p = 0; p < YG_MAX_POT; p++)
+    if ((slot_mask & (1 << p)) && c->pot[p].active && c->pot[p].rcut > c->rcut_total) {
+      yg_set_error("pair potential cutoff exceeds the neighbour-list cutoff");
+      return YG_ERR_ARG;
+    }
+  if (c->pp_dirty) {
+    int rc = yg_pack_pair_params(c);
+    if (rc) return rc;
+  }
+  return yg_launch_pair(c, slot_mask, want_grad);
+}
+
+int yg_ewald_setup(yg_ctx *c, double alpha, double gcut, const int64_t *gmax, double dielectric, int64_t nlow,
+                   int64_t nhigh) {
+  if (!c || !gmax || !(alpha > 0.0) || !(gcut > 0.0) || !(dielectric >= 1.0)) return YG_ERR_ARG;
+  if (!c->have_cell) return YG_ERR_STATE;
+  if (nlow < 0 || nhigh < nlow || nhigh > c->natom) return YG_ERR_ARG;
+  for (int k = 0; k < 3; k++) {
+    if (gmax[k] < 0 || gmax[k] > 4096) return YG_ERR_ARG;
+    c->ew_gmax[k] = gmax[k];
+  }
+  c->ew_alpha = alpha;
+  c->ew_gcut = gcut;
+  c->ew_diel = dielectric;
+  c->ew_nlow = nlow;
+  c->ew_nhigh = nhigh;
+  return yg_launch_ewald_setup(c);
+}
+
+int yg_ewald_reci(yg_ctx *c, int want_grad) {
+  if (!c) return YG_ERR_ARG;
+  if (!c->have_ewald || !c->have_pos || !c->have_charges) {
+    yg_set_error("Ewald needs yg_ewald_setup, positions and charges");
+    return YG_ERR_STATE;
+  }
+  return yg_launch_ewald_reci(c, want_grad);
+}
+
+int yg_ewald_corr(yg_ctx *c, int want_grad) {
+  if (!c) return YG_ERR_ARG;
+  if (!c->have_ewald || !c->have_pos || !c->have_charges) {
+    yg_set_error("Ewald needs yg_ewald_setup, positions and charges");
+    return YG_ERR_STATE;
+  }
+  if (c->nstab > 0 && !c->d_stab_ab) return YG_ERR_STATE;
+  return yg_launch_ewald_corr(c, want_grad);
+}
+
+int yg_set_valence(yg_ctx *c, const int64_t *delta_ij, int64_t ndelta, const int64_t *ic_rows, int64_t nic,
+                   const double *vterm_pars, const int64_t *vterm_ic, int64_t nterm) {
+  if (!c || ndelta < 0 || nic < 0 || nterm < 0) return YG_ERR_ARG;
+  const int64_t N = c->natom;
+  std::vector<int2> ij(ndelta > 0 ? ndelta : 1);
+  for (int64_t r = 0; r < ndelta; r++) {
+    int64_t i = delta_ij[2 * r], j = delta_ij[2 * r + 1];
+    if (i < 0 || i >= N || j < 0 || j >= N || i == j) return YG_ERR_ARG;
+    ij[r] = make_int2((int)i, (int)j);
+  }
+  for (int64_t r = 0; r < nic; r++) {
+    int64_t kind = ic_rows[9 * r];
+    if (!(kind == 0 || kind == 1 || kind == 2 || kind == 5)) {
+      yg_set_error("internal-coordinate kind not supported on the device (0, 1, 2, 5)");
+      return YG_ERR_UNSUPPORTED;
+    }
+    int nused = (kind == 0 || kind == 5) ? 1 : 2;
+    for (int u = 0; u < nused; u++) {
+      int64_t d = ic_rows[9 * r + 1 + 2 * u];
+      if (d < 0 || d >= ndelta) return YG_ERR_ARG;
+    }
+  }
+  std::vector<int> vic(nterm > 0 ? nterm : 1);
+  for (int64_t t = 0; t < nterm; t++) {
+    if (vterm_ic[t] < 0 || vterm_ic[t] >= nic) return YG_ERR_ARG;
+    vic[t] = (int)vterm_ic[t];
+  }
+  void *bufs[] = {c->d_delta_ij, c->d_delta, c->d_ic, c->d_icval, c->d_vpar, c->d_vic, c->d_vE};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  c->d_delta_ij = nullptr; c->d_delta = nullptr; c->d_ic = nullptr; c->d_icval = nullptr;
+  c->d_vpar = nullptr; c->d_vic = nullptr; c->d_vE = nullptr;
+  int rc;
+  if ((rc = yg_alloc((void **)&c->d_delta_ij, ij.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_delta, (size_t)(ndelta > 0 ? ndelta : 1) * 6 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_ic, (size_t)(nic > 0 ? nic : 1) * 9 * sizeof(int64_t)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_icval, (size_t)(nic > 0 ? nic : 1) * 2 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_vpar, (size_t)(nterm > 0 ? nterm : 1) * 2 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc((void **)&c->d_vic, vic.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(c->d_delta_ij, ij.data(), ij.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+  if (nic > 0)
+    YG_CUDA(cudaMemcpyAsync(c->d_ic, ic_rows, (size_t)nic * 9 * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+  if (nterm > 0)
+    YG_CUDA(cudaMemcpyAsync(c->d_vpar, vterm_pars, (size_t)nterm * 2 * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_vic, vic.data(), vic.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->ndelta = ndelta;
+  c->nic = nic;
+  c->nterm = nterm;
+  return YG_OK;
+}
+
+int yg_valence_compute(yg_ctx *c, int want_grad) {
+  if (!c) return YG_ERR_ARG;
+  if (!c->have_pos || !c->have_cell) return YG_ERR_STATE;
+  return yg_launch_valence(c, want_grad);
+}
+
+int yg_get_part(yg_ctx *c, int part, double *energy, double *gpos, double *vtens) {
+  if (!c || part < 0 || part >= YG_NPART) return YG_ERR_ARG;
+  if (!c->part_valid[part]) {
+    yg_set_error("part has no valid result for the current positions");
+    return YG_ERR_STATE;
+  }
+  double ev[10];
+  YG_CUDA(cudaMemcpyAsync(ev, c->d_part_ev + 10 * part, sizeof(ev), cudaMemcpyDeviceToHost, c->stream));
+  if (gpos)
+    YG_CUDA(cudaMemcpyAsync(gpos, c->d_part_gpos + (size_t)part * c->natom * 3, c->natom * 3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  if (energy) *energy = ev[0];
+  if (vtens) memcpy(vtens, ev + 1, 9 * sizeof(double));
+  if (std::isnan(ev[0])) return YG_ERR_NAN;
+  return YG_OK;
+}
+
+int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens, double *part_energies) {
+  if (!c) return YG_ERR_ARG;
+  for (int p = 0; p < YG_NPART; p++)
+    if ((part_mask & (1 << p)) && !c->part_valid[p]) {
+      yg_set_error("a requested part has no valid result");
+      return YG_ERR_STATE;
+    }
+  const int64_t n3 = c->natom * 3;
+  const int want_gpos = gpos != nullptr;
+  int64_t nthreads = want_gpos ? std::max<int64_t>(n3, 16) : 16;
+  k_total<<<yg_blocks(nthreads, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom, part_mask,
+                                                          want_gpos, c->d_total);
+  YG_LAUNCH_CHECK(c, "k_total");
+  size_t bytes = (16 + (want_gpos ? n3 : 0)) * sizeof(double);
+  YG_CUDA(cudaMemcpyAsync(c->h_total, c->d_total, bytes, cudaMemcpyDeviceToHost, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  if (energy) *energy = c->h_total[0];
+  if (vtens) memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
+  if (part_energies) memcpy(part_energies, c->h_total + 10, YG_NPART * sizeof(double));
+  if (gpos) memcpy(gpos, c->h_total + 16, n3 * sizeof(double));
+  if (std::isnan(c->h_total[0])) return YG_ERR_NAN;
+  return YG_OK;
+}
+
+int yg_sync(yg_ctx *c) {
+  if (!c) return YG_ERR_ARG;
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  return YG_OK;
+}
+
+int64_t yg_launch_count(yg_ctx *c) { return c ? c->launches : -1; }
+
+}  // extern "C"

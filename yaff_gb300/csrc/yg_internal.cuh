@@ -1,0 +1,275 @@
+// yg_internal.cuh -- shared definitions of the GB300 force-evaluation library.
+//
+// Device state of one system lives in yg_ctx.  Atoms are kept in two orders:
+// "orig" (the caller's indexing, used for every input and output array) and
+// "sorted" (binned by neighbour-list cell, used by the hot kernels so that the
+// atoms of one cell are contiguous in memory).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/yaffgb.h"
+
+#define YG_MAX_POT 3
+#define YG_WARP 32
+
+// Device status words (yg_ctx::d_status)
+#define YG_ST_OVERFLOW 0     // a neighbour row did not fit its per-atom slot
+#define YG_ST_MAXCOUNT 1     // largest per-atom full-list row count seen
+#define YG_ST_EXACT 2        // candidates decided by the exact FP64 test
+#define YG_ST_BADCELL 3      // non-finite position met while binning
+#define YG_ST_NWORDS 8
+
+// Neighbour entry: x = partner (sorted index), y = meta bits.
+#define YG_META_OFF_MASK 0xFFFFu     // stencil offset index
+#define YG_META_SCALE_SHIFT 16       // 3-bit scaling code (0 = none, 1..4 = nbond)
+#define YG_META_CENTRAL (1u << 19)   // image r == 0 (scalings apply)
+
+struct CellGeom {
+  double rv[9];   // cell vectors (rows)
+  double gv[9];   // reciprocal vectors (rows), inv(rv)^T
+  double volume;
+  int nvec;
+};
+
+// Geometry of the cell-list grid used by the neighbour build.
+struct GridGeom {
+  int n[3];        // cells per axis
+  int k[3];        // stencil half width per axis
+  int noff;        // (2k0+1)(2k1+1)(2k2+1)
+  int ncell;
+};
+
+struct PairPotHost {
+  int active = 0;
+  int kind = 0;
+  int tr_kind = 0;
+  double rcut = 0.0;
+  double tr_par = 0.0;
+  double alpha = 0.0;
+  double dielectric = 1.0;
+  std::vector<double> sigma, sqrteps, radius2;
+  std::vector<int32_t> onlypauli;
+};
+
+// Parameters of one pair potential as the pair kernel sees them.
+struct PairPotDev {
+  int kind;
+  int tr_kind;
+  double rcut;
+  double rcut2;
+  double tr_par;
+  double alpha;
+  double inv_diel;
+  int has_radii;
+};
+
+struct yg_ctx {
+  int64_t natom = 0;
+  int precision = YG_FP64;
+  cudaStream_t stream = 0;
+  int64_t launches = 0;
+
+  CellGeom cell{};
+  int have_cell = 0;
+  int have_pos = 0;
+
+  // positions and charges (orig order)
+  double *d_pos = nullptr;        // natom*3 current
+  double *d_pos_build = nullptr;  // natom*3 at the last rebuild
+  double *d_charge = nullptr;     // natom
+  std::vector<double> h_charge;   // host copy (Ewald self term)
+  int have_charges = 0;
+
+  // binning (orig order)
+  int *d_cell_of = nullptr;       // natom
+  int *d_wimg = nullptr;          // natom*3 integer wrap of the fractional coordinates
+  // sorted order
+  int *d_sorted = nullptr;        // sorted -> orig
+  int *d_rank = nullptr;          // orig -> sorted
+  int *d_cell_start = nullptr;    // ncell+1
+  int *d_cell_fill = nullptr;     // ncell (scratch for the counting sort)
+  double *d_org = nullptr;        // sorted*3 cell origin of each atom (FP64)
+  double4_32a *d_x64 = nullptr;       // sorted: local coordinate (x,y,z) and charge
+  float4 *d_x32 = nullptr;        // sorted: same in FP32
+  double *d_shift64 = nullptr;    // noff*3 stencil shift vectors
+  float4 *d_shift32 = nullptr;    // noff
+  int cap_sorted = 0;             // allocated cell-list capacity (cells)
+  GridGeom grid{};
+  int have_list = 0;
+  int list_recomputed = 0;        // skin path ran since the last rebuild
+  int fast_path = 0;
+  double rcut_total = 0.0;
+  int64_t rmax[3] = {0, 0, 0};
+  int64_t nlow = 0, nhigh = 0;
+  int64_t nneigh = 0;
+
+  // full neighbour list: per sorted atom a slot of `nbr_cap` entries
+  uint2 *d_nbr = nullptr;
+  int *d_ncount = nullptr;
+  int64_t nbr_cap = 0;
+  int64_t nbr_alloc = 0;          // entries allocated
+  int *d_status = nullptr;        // YG_ST_NWORDS
+  int *h_status = nullptr;        // pinned mirror
+
+  // exclusions: per-atom CSR over orig indices, both directions
+  int *d_excl_start = nullptr;    // natom+1
+  int2 *d_excl = nullptr;         // (partner, nbond)
+  int64_t nexcl = 0;
+  double scale_tab[5] = {1.0, 1.0, 1.0, 1.0, 1.0};
+  // the scaling table itself (for the Ewald correction)
+  int64_t nstab = 0;
+  int2 *d_stab_ab = nullptr;
+  double *d_stab_scale = nullptr;
+
+  // pair potentials
+  PairPotHost pot[YG_MAX_POT];
+  double *d_pp_src = nullptr;     // orig*4*YG_MAX_POT: sigma, sqrt(eps), radius^2, onlypauli
+  double *d_pp64 = nullptr;       // same in sorted order
+  float *d_pp32 = nullptr;        // same, FP32
+  int pp_dirty = 1;
+  int pp_packed = 0;
+
+  // Ewald
+  int have_ewald = 0;
+  double ew_alpha = 0.0, ew_gcut = 0.0, ew_diel = 1.0;
+  int64_t ew_gmax[3] = {0, 0, 0};
+  int64_t ew_nlow = 0, ew_nhigh = 0;
+  int ew_ncol = 0;                // (2G0+1)(2G1+1)
+  int ew_nm = 0;                  // G2+1
+  int ew_nk = 0;                  // k vectors in the half sphere
+  double *d_ew_pref = nullptr;    // ncol*nm prefactor (0 outside the half sphere)
+  int *d_ew_tiles = nullptr;      // column tiles: (g0 base, g1 base, m_hi)
+  int ew_ntile = 0;
+  void *d_ew_tab = nullptr;       // per-atom phase tables (complex, T)
+  void *d_ew_Spart = nullptr;     // partial structure factors
+  double *d_ew_S = nullptr;       // 3 groups * ncol*nm complex (re, im)
+  void *d_ew_W = nullptr;         // weights for the force pass, per group
+  double *d_ew_gpart = nullptr;   // force partials
+  double *d_ew_red = nullptr;     // energy/virial partials
+  size_t ew_bytes_tab = 0, ew_bytes_Spart = 0, ew_bytes_W = 0, ew_bytes_gpart = 0;
+  int ew_nchunk = 0;              // atom chunks of the S pass
+  int ew_nsplit = 0;              // column splits of the force pass
+
+  // valence
+  int64_t ndelta = 0, nic = 0, nterm = 0;
+  int2 *d_delta_ij = nullptr;
+  double *d_delta = nullptr;      // ndelta*6: dx,dy,dz,gx,gy,gz
+  int64_t *d_ic = nullptr;        // nic*9: kind, i0,s0,i1,s1,i2,s2,i3,s3
+  double *d_icval = nullptr;      // nic*2: value, grad
+  double *d_vpar = nullptr;       // nterm*2: K, q0
+  int *d_vic = nullptr;           // nterm
+  double *d_vE = nullptr;         // nterm
+
+  // results per part: energy, vtens[9]; gpos natom*3
+  double *d_part_ev = nullptr;    // YG_NPART*10
+  double *d_part_gpos = nullptr;  // YG_NPART*natom*3
+  double *d_total = nullptr;      // 10 + natom*3
+  double *h_total = nullptr;      // pinned mirror
+  double *d_red = nullptr;        // block partials for energy/virial reductions
+  size_t red_cap = 0;
+  int part_valid[YG_NPART] = {0, 0, 0, 0, 0, 0};
+};
+
+// ------------------------------------------------------------------ errors
+void yg_set_error(const std::string &msg);
+int yg_cuda_fail(cudaError_t err, const char *what);
+#define YG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return yg_cuda_fail(_e, #call); \
+  } while (0)
+#define YG_LAUNCH_CHECK(ctx, what)                          \
+  do {                                                      \
+    (ctx)->launches++;                                      \
+    cudaError_t _e = cudaGetLastError();                    \
+    if (_e != cudaSuccess) return yg_cuda_fail(_e, what);   \
+  } while (0)
+
+// Grows a device buffer to at least `bytes` (contents are not preserved).
+int yg_ensure(void **ptr, size_t *cap, size_t bytes);
+int yg_alloc(void **ptr, size_t bytes);
+
+// --------------------------------------------- exact FP64 (no contraction)
+// These reproduce the operation order of the reference C code with every
+// multiply and add rounded separately, as x86-64 SSE2 code does.
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+
+// Sequential fractional wrap of d; m receives the subtracted image
+// (yaff/pes/cell.c:81-106).
+__device__ __forceinline__ void exact_mic(double *d, const CellGeom &c, int *m) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double *g = c.gv + 3 * k;
+    const double *r = c.rv + 3 * k;
+    double x = ceil(xsub(xadd(xadd(xmul(g[0], d[0]), xmul(g[1], d[1])), xmul(g[2], d[2])), 0.5));
+    d[0] = xsub(d[0], xmul(x, r[0]));
+    d[1] = xsub(d[1], xmul(x, r[1]));
+    d[2] = xsub(d[2], xmul(x, r[2]));
+    m[k] = (int)x;
+  }
+}
+
+// d += sum_k img[k] * rv[k], axis by axis (yaff/pes/cell.c:124-143).
+__device__ __forceinline__ void exact_add_vec(double *d, const CellGeom &c, const int *img) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double *r = c.rv + 3 * k;
+    double m = (double)img[k];
+    d[0] = xadd(d[0], xmul(m, r[0]));
+    d[1] = xadd(d[1], xmul(m, r[1]));
+    d[2] = xadd(d[2], xmul(m, r[2]));
+  }
+}
+
+// Image that brings d to the centre, all axes from the same d
+// (yaff/pes/cell.c:109-121).
+__device__ __forceinline__ void exact_to_center(const double *d, const CellGeom &c, int *ctr) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double *g = c.gv + 3 * k;
+    ctr[k] = (int)(-ceil(xsub(xadd(xadd(xmul(g[0], d[0]), xmul(g[1], d[1])), xmul(g[2], d[2])), 0.5)));
+  }
+}
+
+__device__ __forceinline__ double exact_norm2(const double *d) {
+  return xadd(xadd(xmul(d[0], d[0]), xmul(d[1], d[1])), xmul(d[2], d[2]));
+}
+
+// Half space of images: first non-zero of (r2, r1, r0) is positive.
+__device__ __forceinline__ bool img_positive(const int *r) {
+  if (r[2] != 0) return r[2] > 0;
+  if (r[1] != 0) return r[1] > 0;
+  return r[0] > 0;
+}
+
+__device__ __forceinline__ bool img_zero(const int *r) {
+  return r[0] == 0 && r[1] == 0 && r[2] == 0;
+}
+
+// ------------------------------------------------------- launchers (host)
+int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry);
+int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, int64_t *n);
+int yg_launch_prep_positions(yg_ctx *ctx);
+int yg_launch_max_disp2(yg_ctx *ctx, double *out);
+int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad);
+int yg_launch_ewald_setup(yg_ctx *ctx);
+int yg_launch_ewald_reci(yg_ctx *ctx, int want_grad);
+int yg_launch_ewald_corr(yg_ctx *ctx, int want_grad);
+int yg_launch_valence(yg_ctx *ctx, int want_grad);
+int yg_launch_total(yg_ctx *ctx, int part_mask);
+int yg_pack_pair_params(yg_ctx *ctx);
+int yg_launch_reduce_ev(yg_ctx *ctx, const double *partials, int nblocks, int nval, double *out);
+
+// Grid-stride helper.
+static inline int yg_blocks(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > (int64_t)1 << 30) b = (int64_t)1 << 30;
+  return (int)b;
+}

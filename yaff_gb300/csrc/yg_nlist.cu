@@ -1,0 +1,723 @@
+// yg_nlist.cu -- kernel (a): cell-list neighbour build for triclinic cells.
+//
+// Replaces the O(N^2 * images) scan of yaff/pes/nlist.c:30-131.  Atoms are
+// binned on a grid in fractional coordinates whose cells are at least half the
+// cutoff wide along every plane normal, counting-sorted by cell (ties by atom
+// index, so the order is deterministic), and every atom scans the cells of a
+// (2k+1)^3 stencil.  The list is a FULL list (each pair stored from both
+// atoms) in per-atom slots, which lets the pair kernel accumulate forces
+// without atomics.
+//
+// Membership is decided exactly as the reference decides it.  Each candidate
+// is first tested in FP32 on cell-local coordinates; when the FP32 distance is
+// inside or outside the cutoff by more than a guard band (derived from the
+// FP32 rounding bound on the host) the decision is final, otherwise the
+// reference's own FP64 arithmetic is replayed (sequential minimum-image wrap,
+// image shift, squared distance, all with separately rounded multiplies and
+// adds) and decides.  The FP32 shortcut is only enabled when the cutoff is
+// below half the smallest plane spacing, where the reference can only produce
+// central-image rows; otherwise every candidate takes the exact path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "yg_internal.cuh"
+
+namespace {
+
+__global__ void k_bin(const double *__restrict__ pos, int64_t natom, CellGeom cell, GridGeom grid,
+                      int *__restrict__ cell_of, int *__restrict__ wimg, int *__restrict__ count,
+                      int *__restrict__ status) {
+  int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= natom) return;
+  double p[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+  int c[3], w[3];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double f = cell.gv[3 * k] * p[0] + cell.gv[3 * k + 1] * p[1] + cell.gv[3 * k + 2] * p[2];
+    if (!isfinite(f) || fabs(f) > 1e9) {
+      bad = true;
+      f = 0.0;
+    }
+    double fl = floor(f);
+    double s = f - fl;
+    int ci = (int)(s * grid.n[k]);
+    if (ci < 0) ci = 0;
+    if (ci >= grid.n[k]) ci = grid.n[k] - 1;
+    c[k] = ci;
+    w[k] = (int)fl;
+  }
+  if (bad) atomicOr(status + YG_ST_BADCELL, 1);
+  int id = c[0] + grid.n[0] * (c[1] + grid.n[1] * c[2]);
+  cell_of[a] = id;
+  wimg[3 * a] = w[0];
+  wimg[3 * a + 1] = w[1];
+  wimg[3 * a + 2] = w[2];
+  atomicAdd(count + id, 1);
+}
+
+// Exclusive scan of the per-cell counts (one block; cell counts are small).
+__global__ void k_scan_cells(const int *__restrict__ count, int ncell, int *__restrict__ start,
+                             int *__restrict__ fill) {
+  __shared__ int warp_sums[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < ncell; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int v = (i < ncell) ? count[i] : 0;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int nw = blockDim.x >> 5;
+      int s = (lane < nw) ? warp_sums[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    int excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+    if (i < ncell) {
+      start[i] = excl;
+      fill[i] = excl;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[ncell] = carry;
+}
+
+__global__ void k_scatter(const int *__restrict__ cell_of, int64_t natom, int *__restrict__ fill,
+                          int *__restrict__ sorted) {
+  int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= natom) return;
+  int slot = atomicAdd(fill + cell_of[a], 1);
+  sorted[slot] = (int)a;
+}
+
+// Orders the atoms of every cell by index (cells hold tens of atoms).
+__global__ void k_sort_cells(const int *__restrict__ start, int ncell, int *__restrict__ sorted) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  int s0 = start[c], s1 = start[c + 1];
+  for (int i = s0 + 1; i < s1; i++) {
+    int v = sorted[i];
+    int j = i - 1;
+    while (j >= s0 && sorted[j] > v) {
+      sorted[j + 1] = sorted[j];
+      j--;
+    }
+    sorted[j + 1] = v;
+  }
+}
+
+// Cell origin (FP64) of every sorted atom and the orig -> sorted map.
+__global__ void k_origins(const int *__restrict__ sorted, const int *__restrict__ cell_of,
+                          const int *__restrict__ wimg, int64_t natom, CellGeom cell, GridGeom grid,
+                          double *__restrict__ org, int *__restrict__ rank) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= natom) return;
+  int a = sorted[s];
+  int id = cell_of[a];
+  int c[3] = {id % grid.n[0], (id / grid.n[0]) % grid.n[1], id / (grid.n[0] * grid.n[1])};
+  double f[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) f[k] = (double)wimg[3 * a + k] + (double)c[k] / (double)grid.n[k];
+#pragma unroll
+  for (int x = 0; x < 3; x++)
+    org[3 * s + x] = f[0] * cell.rv[x] + f[1] * cell.rv[3 + x] + f[2] * cell.rv[6 + x];
+  rank[a] = (int)s;
+}
+
+// Per-evaluation refresh of the cell-local coordinates (FP64 and FP32) and
+// charges in sorted order.  Cell assignment stays frozen between rebuilds.
+__global__ void k_prep(const double *__restrict__ pos, const double *__restrict__ charge,
+                       const int *__restrict__ sorted, const double *__restrict__ org, int64_t natom,
+                       double4_32a *__restrict__ x64, float4 *__restrict__ x32) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= natom) return;
+  int a = sorted[s];
+  double q = charge ? charge[a] : 0.0;
+  double x = pos[3 * a] - org[3 * s];
+  double y = pos[3 * a + 1] - org[3 * s + 1];
+  double z = pos[3 * a + 2] - org[3 * s + 2];
+  x64[s] = make_double4_32a(x, y, z, q);
+  x32[s] = make_float4((float)x, (float)y, (float)z, (float)q);
+}
+
+__device__ __forceinline__ int floordiv(int u, int n) {
+  int q = u / n;
+  if (u < 0 && q * n != u) q--;
+  return q;
+}
+
+__device__ __forceinline__ int excl_code(const int *__restrict__ estart, const int2 *__restrict__ excl,
+                                         int oi, int oj) {
+  if (!estart) return 0;
+  int s0 = estart[oi], s1 = estart[oi + 1];
+  for (int e = s0; e < s1; e++) {
+    int2 v = excl[e];
+    if (v.x == oj) return v.y;
+  }
+  return 0;
+}
+
+struct BuildArgs {
+  CellGeom cell;
+  GridGeom grid;
+  const double *pos;
+  const int *sorted;
+  const int *cell_of;
+  const int *wimg;
+  const int *cell_start;
+  const float4 *x32;
+  const float4 *shift32;
+  const int *estart;
+  const int2 *excl;
+  uint2 *nbr;
+  int *ncount;
+  int *status;
+  unsigned long long *total;
+  int64_t natom;
+  int64_t cap;
+  int64_t nlow, nhigh;
+  int rmax[3];
+  double rc2;
+  float lo, hi;     // FP32 guard band on d^2
+  int fast;
+};
+
+// Exact replay of the reference's decision for candidate (oi -> oj) whose
+// image relative to the raw position difference is t (pos_j - pos_i + t.R).
+// Returns 1 when the pair is in the list; *central is set when its image is 0.
+__device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, const int *t,
+                                            int *central) {
+  *central = 0;
+  int r[3];
+  double d[3];
+  if (oi == oj) {
+    // self image: the wrapped relative vector is zero, the image is t
+    for (int k = 0; k < 3; k++) r[k] = t[k];
+    if (img_zero(r)) return 0;
+    if (!img_positive(r)) for (int k = 0; k < 3; k++) r[k] = -r[k];
+    for (int k = 0; k < 3; k++)
+      if (r[k] > A.rmax[k] || r[k] < -A.rmax[k]) return 0;
+    d[0] = 0.0; d[1] = 0.0; d[2] = 0.0;
+    exact_add_vec(d, A.cell, r);
+    return exact_norm2(d) < A.rc2;
+  }
+  int a = max(oi, oj), b = min(oi, oj);
+  int tab[3];
+  for (int k = 0; k < 3; k++) tab[k] = (oi == a) ? t[k] : -t[k];
+  d[0] = xsub(A.pos[3 * b], A.pos[3 * a]);
+  d[1] = xsub(A.pos[3 * b + 1], A.pos[3 * a + 1]);
+  d[2] = xsub(A.pos[3 * b + 2], A.pos[3 * a + 2]);
+  int m[3];
+  exact_mic(d, A.cell, m);
+  for (int k = 0; k < 3; k++) {
+    r[k] = tab[k] + m[k];
+    if (r[k] > A.rmax[k] || r[k] < -A.rmax[k]) return 0;
+  }
+  if (img_zero(r)) {
+    *central = 1;
+  } else if (!img_positive(r)) {
+    for (int k = 0; k < 3; k++) {
+      r[k] = -r[k];
+      d[k] = -d[k];
+    }
+  }
+  exact_add_vec(d, A.cell, r);
+  return exact_norm2(d) < A.rc2;
+}
+
+// One warp per sorted atom; lanes sweep the candidates of each stencil cell.
+__global__ void __launch_bounds__(256) k_build(BuildArgs A) {
+  int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= A.natom) return;
+  const int oi = A.sorted[i];
+  const float4 xi = A.x32[i];
+  const int cid = A.cell_of[oi];
+  const int ci[3] = {cid % A.grid.n[0], (cid / A.grid.n[0]) % A.grid.n[1], cid / (A.grid.n[0] * A.grid.n[1])};
+  const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
+  int64_t base = 0;
+  int nexact = 0;
+  uint2 *out = A.nbr + i * A.cap;
+  const int w0 = 2 * A.grid.k[0] + 1, w1 = 2 * A.grid.k[1] + 1;
+  for (int o2 = -A.grid.k[2]; o2 <= A.grid.k[2]; o2++) {
+    int u2 = ci[2] + o2;
+    int n2 = floordiv(u2, A.grid.n[2]);
+    int c2 = u2 - n2 * A.grid.n[2];
+    for (int o1 = -A.grid.k[1]; o1 <= A.grid.k[1]; o1++) {
+      int u1 = ci[1] + o1;
+      int n1 = floordiv(u1, A.grid.n[1]);
+      int c1 = u1 - n1 * A.grid.n[1];
+      for (int o0 = -A.grid.k[0]; o0 <= A.grid.k[0]; o0++) {
+        int u0 = ci[0] + o0;
+        int n0 = floordiv(u0, A.grid.n[0]);
+        int c0 = u0 - n0 * A.grid.n[0];
+        int cell = c0 + A.grid.n[0] * (c1 + A.grid.n[1] * c2);
+        int oidx = (o0 + A.grid.k[0]) + w0 * ((o1 + A.grid.k[1]) + w1 * (o2 + A.grid.k[2]));
+        float4 sh = A.shift32[oidx];
+        bool zero_off = (o0 == 0 && o1 == 0 && o2 == 0);
+        int s0 = A.cell_start[cell], s1 = A.cell_start[cell + 1];
+        for (int jb = s0; jb < s1; jb += 32) {
+          int j = jb + lane;
+          int in = 0, central = 1, oj = -1;
+          if (j < s1 && !(zero_off && j == i)) {
+            oj = A.sorted[j];
+            int a = max(oi, oj), b = min(oi, oj);
+            bool keep = (a >= A.nlow && b < A.nhigh) || (b >= A.nlow && a < A.nhigh);
+            if (keep) {
+              float4 xj = A.x32[j];
+              float dx = (xj.x - xi.x) + sh.x;
+              float dy = (xj.y - xi.y) + sh.y;
+              float dz = (xj.z - xi.z) + sh.z;
+              float d2 = dx * dx + dy * dy + dz * dz;
+              int decided = 0;
+              if (A.fast) {
+                if (d2 < A.lo) { in = 1; decided = 1; }
+                else if (d2 > A.hi) { in = 0; decided = 1; }
+              }
+              if (!decided) {
+                int t[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1],
+                            n2 + wi[2] - A.wimg[3 * oj + 2]};
+                in = exact_decide(A, oi, oj, t, &central);
+                nexact++;
+              }
+            }
+          }
+          unsigned ball = __ballot_sync(0xffffffffu, in);
+          if (in) {
+            int code = central ? excl_code(A.estart, A.excl, oi, oj) : 0;
+            int64_t p = base + __popc(ball & ((1u << lane) - 1u));
+            if (p < A.cap) {
+              unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
+                              (central ? YG_META_CENTRAL : 0u);
+              out[p] = make_uint2((unsigned)j, meta);
+            }
+          }
+          base += __popc(ball);
+        }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) nexact += __shfl_down_sync(0xffffffffu, nexact, o);
+  if (lane == 0) {
+    A.ncount[i] = (int)min(base, A.cap);
+    if (base > A.cap) atomicOr(A.status + YG_ST_OVERFLOW, 1);
+    atomicMax(A.status + YG_ST_MAXCOUNT, (int)min(base, (int64_t)0x7fffffff));
+    if (nexact) atomicAdd(A.status + YG_ST_EXACT, nexact);
+    atomicAdd(A.total, (unsigned long long)min(base, A.cap));
+  }
+}
+
+struct ExportArgs {
+  BuildArgs B;
+  const double *pos_now;
+  int recomputed;
+  yg_neigh_row *rows;
+  unsigned long long *nrows;
+  int64_t cap_rows;
+};
+
+// Emits every reference row once, from the entry whose atom is the row's
+// larger index (self images: from the entry with the positive image).
+__global__ void k_export(ExportArgs E) {
+  const BuildArgs &A = E.B;
+  int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= A.natom) return;
+  const int oi = A.sorted[i];
+  const int cid = A.cell_of[oi];
+  const int ci[3] = {cid % A.grid.n[0], (cid / A.grid.n[0]) % A.grid.n[1], cid / (A.grid.n[0] * A.grid.n[1])};
+  const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
+  const int cnt = A.ncount[i];
+  const int w0 = 2 * A.grid.k[0] + 1, w1 = 2 * A.grid.k[1] + 1;
+  for (int e = lane; e < cnt; e += 32) {
+    uint2 ent = A.nbr[i * A.cap + e];
+    int j = (int)ent.x;
+    int oidx = (int)(ent.y & YG_META_OFF_MASK);
+    int o0 = oidx % w0 - A.grid.k[0];
+    int o1 = (oidx / w0) % w1 - A.grid.k[1];
+    int o2 = oidx / (w0 * w1) - A.grid.k[2];
+    int u[3] = {ci[0] + o0, ci[1] + o1, ci[2] + o2};
+    int nimg[3];
+    for (int k = 0; k < 3; k++) nimg[k] = floordiv(u[k], A.grid.n[k]);
+    int oj = A.sorted[j];
+    int t[3] = {nimg[0] + wi[0] - A.wimg[3 * oj], nimg[1] + wi[1] - A.wimg[3 * oj + 1],
+                nimg[2] + wi[2] - A.wimg[3 * oj + 2]};
+    int ra, rb, r[3];
+    double d[3];
+    if (oi == oj) {
+      if (!img_positive(t)) continue;
+      for (int k = 0; k < 3; k++) r[k] = t[k];
+      ra = oi; rb = oi;
+      d[0] = 0.0; d[1] = 0.0; d[2] = 0.0;
+    } else {
+      if (oi < oj) continue;
+      int a = oi, b = oj;
+      d[0] = xsub(A.pos[3 * b], A.pos[3 * a]);
+      d[1] = xsub(A.pos[3 * b + 1], A.pos[3 * a + 1]);
+      d[2] = xsub(A.pos[3 * b + 2], A.pos[3 * a + 2]);
+      int m[3];
+      exact_mic(d, A.cell, m);
+      for (int k = 0; k < 3; k++) r[k] = t[k] + m[k];
+      ra = a; rb = b;
+      if (!img_zero(r) && !img_positive(r)) {
+        for (int k = 0; k < 3; k++) {
+          r[k] = -r[k];
+          d[k] = -d[k];
+        }
+        ra = b; rb = a;
+      }
+    }
+    if (E.recomputed) {
+      // skin path of the reference: image from the old (build) positions,
+      // relative vector from the current ones (yaff/pes/nlist.c:183-232)
+      double o[3] = {xsub(A.pos[3 * rb], A.pos[3 * ra]), xsub(A.pos[3 * rb + 1], A.pos[3 * ra + 1]),
+                     xsub(A.pos[3 * rb + 2], A.pos[3 * ra + 2])};
+      int ctr[3];
+      exact_to_center(o, A.cell, ctr);
+      d[0] = xsub(E.pos_now[3 * rb], E.pos_now[3 * ra]);
+      d[1] = xsub(E.pos_now[3 * rb + 1], E.pos_now[3 * ra + 1]);
+      d[2] = xsub(E.pos_now[3 * rb + 2], E.pos_now[3 * ra + 2]);
+      exact_add_vec(d, A.cell, ctr);
+    }
+    exact_add_vec(d, A.cell, r);
+    double dd = exact_norm2(d);
+    unsigned long long slot = atomicAdd(E.nrows, 1ull);
+    if ((int64_t)slot < E.cap_rows) {
+      yg_neigh_row row;
+      row.a = ra;
+      row.b = rb;
+      row.d = __dsqrt_rn(dd);
+      row.dx = d[0];
+      row.dy = d[1];
+      row.dz = d[2];
+      row.r0 = r[0];
+      row.r1 = r[1];
+      row.r2 = r[2];
+      E.rows[slot] = row;
+    }
+  }
+}
+
+__global__ void k_max_disp2(const double *__restrict__ pos, const double *__restrict__ old, int64_t natom,
+                            unsigned long long *__restrict__ out) {
+  double m = 0.0;
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < natom;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    double dx = pos[3 * a] - old[3 * a];
+    double dy = pos[3 * a + 1] - old[3 * a + 1];
+    double dz = pos[3 * a + 2] - old[3 * a + 2];
+    double v = dx * dx + dy * dy + dz * dz;
+    if (!(v <= m)) m = v;   // also propagates NaN
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// Repacks the per-atom pair parameters into sorted order:
+// for every potential p: sigma, sqrt(epsilon), radius^2, onlypauli.
+__global__ void k_pack_params(const double *__restrict__ src, const int *__restrict__ sorted, int64_t natom,
+                              double *__restrict__ dst64, float *__restrict__ dst32) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= natom) return;
+  int a = sorted[s];
+  for (int v = 0; v < 4 * YG_MAX_POT; v++) {
+    double x = src[(int64_t)a * 4 * YG_MAX_POT + v];
+    dst64[s * 4 * YG_MAX_POT + v] = x;
+    dst32[s * 4 * YG_MAX_POT + v] = (float)x;
+  }
+}
+
+BuildArgs make_args(yg_ctx *ctx, double rc2) {
+  BuildArgs A;
+  A.cell = ctx->cell;
+  A.grid = ctx->grid;
+  A.pos = ctx->d_pos_build;
+  A.sorted = ctx->d_sorted;
+  A.cell_of = ctx->d_cell_of;
+  A.wimg = ctx->d_wimg;
+  A.cell_start = ctx->d_cell_start;
+  A.x32 = ctx->d_x32;
+  A.shift32 = ctx->d_shift32;
+  A.estart = ctx->nexcl ? ctx->d_excl_start : nullptr;
+  A.excl = ctx->d_excl;
+  A.nbr = ctx->d_nbr;
+  A.ncount = ctx->d_ncount;
+  A.status = ctx->d_status;
+  A.total = nullptr;
+  A.natom = ctx->natom;
+  A.cap = ctx->nbr_cap;
+  A.nlow = ctx->nlow;
+  A.nhigh = ctx->nhigh;
+  for (int k = 0; k < 3; k++) A.rmax[k] = (int)ctx->rmax[k];
+  A.rc2 = rc2;
+  A.lo = 0.0f;
+  A.hi = 0.0f;
+  A.fast = 0;
+  return A;
+}
+
+}  // namespace
+
+// Uploads the pair parameters of all potentials (orig order) when they
+// changed, then repacks them into sorted order on the device.
+int yg_pack_pair_params(yg_ctx *ctx) {
+  size_t n = (size_t)ctx->natom * 4 * YG_MAX_POT;
+  int rc;
+  if (!ctx->d_pp64) {
+    if ((rc = yg_alloc((void **)&ctx->d_pp_src, n * sizeof(double)))) return rc;
+    if ((rc = yg_alloc((void **)&ctx->d_pp64, n * sizeof(double)))) return rc;
+    if ((rc = yg_alloc((void **)&ctx->d_pp32, n * sizeof(float)))) return rc;
+    ctx->pp_dirty = 1;
+  }
+  if (ctx->pp_dirty) {
+    std::vector<double> h(n, 0.0);
+    for (int p = 0; p < YG_MAX_POT; p++) {
+      const PairPotHost &P = ctx->pot[p];
+      if (!P.active) continue;
+      for (int64_t a = 0; a < ctx->natom; a++) {
+        double *q = h.data() + (size_t)a * 4 * YG_MAX_POT + 4 * p;
+        q[0] = P.sigma.empty() ? 0.0 : P.sigma[a];
+        q[1] = P.sqrteps.empty() ? 0.0 : P.sqrteps[a];
+        q[2] = P.radius2.empty() ? 0.0 : P.radius2[a];
+        q[3] = P.onlypauli.empty() ? 0.0 : (double)P.onlypauli[a];
+      }
+    }
+    YG_CUDA(cudaMemcpyAsync(ctx->d_pp_src, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->pp_dirty = 0;
+  }
+  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(ctx->d_pp_src, ctx->d_sorted, ctx->natom,
+                                                                     ctx->d_pp64, ctx->d_pp32);
+  YG_LAUNCH_CHECK(ctx, "k_pack_params");
+  ctx->pp_packed = 1;
+  return YG_OK;
+}
+
+int yg_launch_prep_positions(yg_ctx *ctx) {
+  k_prep<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(
+      ctx->d_pos, ctx->have_charges ? ctx->d_charge : nullptr, ctx->d_sorted, ctx->d_org, ctx->natom,
+      ctx->d_x64, ctx->d_x32);
+  YG_LAUNCH_CHECK(ctx, "k_prep");
+  return YG_OK;
+}
+
+int yg_launch_max_disp2(yg_ctx *ctx, double *out) {
+  unsigned long long *d = (unsigned long long *)ctx->d_red;
+  YG_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+  k_max_disp2<<<yg_blocks(ctx->natom, 256) > 1024 ? 1024 : yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(
+      ctx->d_pos, ctx->d_pos_build, ctx->natom, d);
+  YG_LAUNCH_CHECK(ctx, "k_max_disp2");
+  unsigned long long h = 0;
+  YG_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  YG_CUDA(cudaStreamSynchronize(ctx->stream));
+  double v;
+  memcpy(&v, &h, sizeof(v));
+  *out = v;
+  return YG_OK;
+}
+
+int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
+  const int64_t N = ctx->natom;
+  const CellGeom &C = ctx->cell;
+  double rc = ctx->rcut_total;
+  // grid: cells at least rc/2 wide along each plane normal
+  GridGeom G;
+  double rsp[3];
+  for (int k = 0; k < 3; k++) {
+    const double *g = C.gv + 3 * k;
+    rsp[k] = 1.0 / std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    int n = (int)std::floor(rsp[k] / (0.5 * rc));
+    if (n < 1) n = 1;
+    if (n > 512) n = 512;
+    G.n[k] = n;
+    double w = rsp[k] / n;
+    double rsearch = rc * (1.0 + 1e-9) + 1e-9;
+    G.k[k] = (int)std::ceil(rsearch / w);
+  }
+  G.noff = (2 * G.k[0] + 1) * (2 * G.k[1] + 1) * (2 * G.k[2] + 1);
+  G.ncell = G.n[0] * G.n[1] * G.n[2];
+  if (G.noff > 65535) {
+    yg_set_error("neighbour stencil too large for this cutoff/cell combination");
+    return YG_ERR_UNSUPPORTED;
+  }
+  int rc_ = YG_OK;
+  if (G.ncell + 1 > ctx->cap_sorted) {
+    cudaFree(ctx->d_cell_start);
+    cudaFree(ctx->d_cell_fill);
+    ctx->d_cell_start = nullptr;
+    ctx->d_cell_fill = nullptr;
+    if ((rc_ = yg_alloc((void **)&ctx->d_cell_start, (G.ncell + 1) * sizeof(int)))) return rc_;
+    if ((rc_ = yg_alloc((void **)&ctx->d_cell_fill, (G.ncell + 1) * sizeof(int)))) return rc_;
+    ctx->cap_sorted = G.ncell + 1;
+  }
+  ctx->grid = G;
+  // shift vectors of the stencil
+  std::vector<double> sh64(3 * (size_t)G.noff);
+  std::vector<float4> sh32(G.noff);
+  double maxsh = 0.0;
+  for (int o2 = -G.k[2]; o2 <= G.k[2]; o2++)
+    for (int o1 = -G.k[1]; o1 <= G.k[1]; o1++)
+      for (int o0 = -G.k[0]; o0 <= G.k[0]; o0++) {
+        int idx = (o0 + G.k[0]) + (2 * G.k[0] + 1) * ((o1 + G.k[1]) + (2 * G.k[1] + 1) * (o2 + G.k[2]));
+        double f[3] = {(double)o0 / G.n[0], (double)o1 / G.n[1], (double)o2 / G.n[2]};
+        double v[3];
+        for (int x = 0; x < 3; x++) v[x] = f[0] * C.rv[x] + f[1] * C.rv[3 + x] + f[2] * C.rv[6 + x];
+        for (int x = 0; x < 3; x++) sh64[3 * idx + x] = v[x];
+        sh32[idx] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.0f);
+        maxsh = std::max(maxsh, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+      }
+  cudaFree(ctx->d_shift64);
+  cudaFree(ctx->d_shift32);
+  ctx->d_shift64 = nullptr;
+  ctx->d_shift32 = nullptr;
+  if ((rc_ = yg_alloc((void **)&ctx->d_shift64, sh64.size() * sizeof(double)))) return rc_;
+  if ((rc_ = yg_alloc((void **)&ctx->d_shift32, sh32.size() * sizeof(float4)))) return rc_;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_shift64, sh64.data(), sh64.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  YG_CUDA(cudaMemcpyAsync(ctx->d_shift32, sh32.data(), sh32.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+
+  // bin + deterministic counting sort
+  YG_CUDA(cudaMemsetAsync(ctx->d_status, 0, YG_ST_NWORDS * sizeof(int), ctx->stream));
+  YG_CUDA(cudaMemsetAsync(ctx->d_cell_fill, 0, (G.ncell + 1) * sizeof(int), ctx->stream));
+  YG_CUDA(cudaMemcpyAsync(ctx->d_pos_build, ctx->d_pos, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  k_bin<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_pos, N, C, G, ctx->d_cell_of, ctx->d_wimg,
+                                                    ctx->d_cell_fill, ctx->d_status);
+  YG_LAUNCH_CHECK(ctx, "k_bin");
+  k_scan_cells<<<1, 1024, 0, ctx->stream>>>(ctx->d_cell_fill, G.ncell, ctx->d_cell_start, ctx->d_cell_fill);
+  YG_LAUNCH_CHECK(ctx, "k_scan_cells");
+  k_scatter<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_cell_of, N, ctx->d_cell_fill, ctx->d_sorted);
+  YG_LAUNCH_CHECK(ctx, "k_scatter");
+  k_sort_cells<<<yg_blocks(G.ncell, 128), 128, 0, ctx->stream>>>(ctx->d_cell_start, G.ncell, ctx->d_sorted);
+  YG_LAUNCH_CHECK(ctx, "k_sort_cells");
+  k_origins<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_sorted, ctx->d_cell_of, ctx->d_wimg, N, C, G,
+                                                        ctx->d_org, ctx->d_rank);
+  YG_LAUNCH_CHECK(ctx, "k_origins");
+  if ((rc_ = yg_launch_prep_positions(ctx))) return rc_;
+
+  // FP32 guard band: bound on |d2_fp32 - d2_exact| from the magnitudes of the
+  // cell-local coordinates (< one cell diagonal) and the shift vectors.
+  double celldiag = 0.0;
+  {
+    double f[3] = {1.0 / G.n[0], 1.0 / G.n[1], 1.0 / G.n[2]};
+    for (int s0 = -1; s0 <= 1; s0 += 2)
+      for (int s1 = -1; s1 <= 1; s1 += 2) {
+        double v[3];
+        for (int x = 0; x < 3; x++) v[x] = f[0] * C.rv[x] + s0 * f[1] * C.rv[3 + x] + s1 * f[2] * C.rv[6 + x];
+        celldiag = std::max(celldiag, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+      }
+    celldiag *= 1.01;
+  }
+  double eps32 = 5.960464477539063e-08;  // 2^-24
+  double comp = 8.0 * eps32 * (maxsh + 2.0 * celldiag + rc);
+  double err = 2.0 * rc * std::sqrt(3.0) * comp + 3.0 * comp * comp + 4.0 * eps32 * rc2;
+  err *= 4.0;  // safety factor
+  double min_half = 0.5 * std::min(rsp[0], std::min(rsp[1], rsp[2]));
+  ctx->fast_path = (rc * (1.0 + 1e-7) + 1e-7 < min_half) ? 1 : 0;
+
+  // neighbour slots
+  if (ctx->nbr_cap == 0) {
+    double dens = N / C.volume;
+    double est = dens * 4.18879020478639 * rc * rc * rc;  // 4/3 pi rc^3
+    int64_t cap = (int64_t)(est * 1.3) + 64;
+    cap = (cap + 31) / 32 * 32;
+    ctx->nbr_cap = cap;
+  }
+  for (;;) {
+    int64_t need = ctx->nbr_cap * N;
+    if (need > ctx->nbr_alloc) {
+      cudaFree(ctx->d_nbr);
+      ctx->d_nbr = nullptr;
+      if ((rc_ = yg_alloc((void **)&ctx->d_nbr, (size_t)need * sizeof(uint2)))) return rc_;
+      ctx->nbr_alloc = need;
+    }
+    BuildArgs A = make_args(ctx, rc2);
+    A.fast = ctx->fast_path;
+    A.lo = (float)(rc2 - err);
+    A.hi = (float)(rc2 + err);
+    // make the band closed under FP32 rounding of the thresholds themselves
+    A.lo = nextafterf(nextafterf(A.lo, 0.0f), 0.0f);
+    A.hi = nextafterf(nextafterf(A.hi, INFINITY), INFINITY);
+    unsigned long long *dtot = (unsigned long long *)ctx->d_red;
+    YG_CUDA(cudaMemsetAsync(dtot, 0, sizeof(unsigned long long), ctx->stream));
+    YG_CUDA(cudaMemsetAsync(ctx->d_status, 0, YG_ST_NWORDS * sizeof(int), ctx->stream));
+    A.total = dtot;
+    int64_t threads = N * 32;
+    k_build<<<yg_blocks(threads, 256), 256, 0, ctx->stream>>>(A);
+    YG_LAUNCH_CHECK(ctx, "k_build");
+    YG_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long total = 0;
+    YG_CUDA(cudaMemcpyAsync(&total, dtot, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_status[YG_ST_BADCELL]) {
+      yg_set_error("non-finite or huge position met while binning atoms");
+      return YG_ERR_NAN;
+    }
+    if (ctx->h_status[YG_ST_OVERFLOW]) {
+      int64_t cap = (int64_t)(ctx->h_status[YG_ST_MAXCOUNT] * 1.15) + 64;
+      ctx->nbr_cap = (cap + 31) / 32 * 32;
+      if (retry) (*retry)++;
+      continue;
+    }
+    ctx->nneigh = (int64_t)(total / 2);
+    break;
+  }
+  ctx->have_list = 1;
+  ctx->list_recomputed = 0;
+  // the sorted order changed: repack the pair parameters
+  if ((rc_ = yg_pack_pair_params(ctx))) return rc_;
+  return YG_OK;
+}
+
+int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, int64_t *n) {
+  int64_t want = ctx->nneigh;
+  *n = want;
+  if (want > cap || rows_host == nullptr) return YG_OK;
+  yg_neigh_row *d_rows = nullptr;
+  int rc = yg_alloc((void **)&d_rows, (size_t)(want > 0 ? want : 1) * sizeof(yg_neigh_row));
+  if (rc) return rc;
+  unsigned long long *dcount = (unsigned long long *)ctx->d_red;
+  YG_CUDA(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), ctx->stream));
+  ExportArgs E;
+  E.B = make_args(ctx, ctx->rcut_total * ctx->rcut_total);
+  E.pos_now = ctx->d_pos;
+  E.recomputed = ctx->list_recomputed;
+  E.rows = d_rows;
+  E.nrows = dcount;
+  E.cap_rows = want;
+  k_export<<<yg_blocks(ctx->natom * 32, 256), 256, 0, ctx->stream>>>(E);
+  YG_LAUNCH_CHECK(ctx, "k_export");
+  unsigned long long got = 0;
+  YG_CUDA(cudaMemcpyAsync(&got, dcount, sizeof(got), cudaMemcpyDeviceToHost, ctx->stream));
+  YG_CUDA(cudaMemcpyAsync(rows_host, d_rows, (size_t)want * sizeof(yg_neigh_row), cudaMemcpyDeviceToHost, ctx->stream));
+  YG_CUDA(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d_rows);
+  if ((int64_t)got != want) {
+    yg_set_error("neighbour export row count differs from the build count");
+    return YG_ERR_STATE;
+  }
+  std::sort(rows_host, rows_host + want, [](const yg_neigh_row &x, const yg_neigh_row &y) {
+    if (x.a != y.a) return x.a < y.a;
+    if (x.b != y.b) return x.b < y.b;
+    if (x.r0 != y.r0) return x.r0 < y.r0;
+    if (x.r1 != y.r1) return x.r1 < y.r1;
+    return x.r2 < y.r2;
+  });
+  return YG_OK;
+}

@@ -1,0 +1,413 @@
+// yg_pair.cu -- kernel (b): fused real-space pair potentials.
+//
+// One traversal of the full neighbour list evaluates every registered pair
+// potential (LJ, MM3 exp-6, EI/erfc; yaff/pes/pair_pot.c:277-352, :711-751)
+// with exclusion scaling and truncation (pair_pot.c:84-176,
+// truncation.c:30-76).  One warp owns one atom: lanes stride over its list
+// entries, accumulate the energy, the gradient of the owning atom and the
+// virial, and the warp reduces them.  Because the list holds every pair from
+// both atoms, each atom's gradient is complete after its own warp finishes:
+// no atomics, a deterministic summation order, and each entry contributes
+// half the pair energy and virial.
+//
+// Precision modes: YG_FP64 computes and accumulates in FP64; YG_MIXED
+// evaluates the terms in FP32 on cell-local FP32 coordinates (relative
+// vectors never exceed a few cutoffs, so FP32 keeps ~1e-7 relative accuracy)
+// with per-lane FP32 partial sums that are reduced in FP64 across the warp,
+// the block and the grid; YG_MIXED_KAHAN keeps Kahan-compensated FP32 sums.
+#include <cmath>
+#include <type_traits>
+
+#include "yg_internal.cuh"
+
+namespace {
+
+struct PairArgs {
+  int64_t natom;
+  int64_t cap;
+  const uint2 *nbr;
+  const int *ncount;
+  const int *sorted;
+  const double4_32a *x64;
+  const float4 *x32;
+  const double *shift64;
+  const float4 *shift32;
+  const double *pp64;
+  const float *pp32;
+  PairPotDev pot[YG_MAX_POT];
+  double scale[5];
+  double *gpos[YG_MAX_POT];   // per-potential gradient, orig order (natom*3)
+  double *partial;            // per block: NPOT*7 (E, Vxx, Vyy, Vzz, Vxy, Vxz, Vyz)
+  int want_grad;
+};
+
+template <typename T> struct Num;
+template <> struct Num<double> {
+  static __device__ __forceinline__ double exp_(double x) { return exp(x); }
+  static __device__ __forceinline__ double erfc_(double x) { return erfc(x); }
+  static __device__ __forceinline__ double erf_(double x) { return erf(x); }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+};
+template <> struct Num<float> {
+  static __device__ __forceinline__ float exp_(float x) { return expf(x); }
+  static __device__ __forceinline__ float erfc_(float x) { return erfcf(x); }
+  static __device__ __forceinline__ float erf_(float x) { return erff(x); }
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+};
+
+// Energy v and g = (dv/dd)/d of one pair for one potential, truncation
+// included.  Formulas of yaff/pes/pair_pot.c:277-301 (LJ), :321-352 (MM3),
+// :711-751 (EI) and truncation.c:30-76.
+template <typename T>
+__device__ __forceinline__ void pair_term(const PairPotDev &P, T d, T d2, T pi0, T pi1, T pi2, T pi3,
+                                          T pj0, T pj1, T pj2, T pj3, T qi, T qj, T &v, T &g) {
+  typedef Num<T> M;
+  const T two_div_sqrt_pi = (T)1.1283791670955125739;
+  if (P.kind == YG_POT_LJ) {
+    T sig = (T)0.5 * (pi0 + pj0);
+    T eps = pi1 * pj1;
+    T x = sig / d;
+    x *= x;
+    x *= x * x;
+    g = (T)24.0 * eps / d2 * x * ((T)1.0 - (T)2.0 * x);
+    v = (T)4.0 * eps * (x * (x - (T)1.0));
+  } else if (P.kind == YG_POT_MM3) {
+    T sig = pi0 + pj0;
+    T eps = pi1 * pj1;
+    T x = sig / d;
+    T ex = (T)1.84e5 * M::exp_((T)-12.0 / x);
+    if (pi3 + pj3 == (T)0) {
+      x *= x;
+      x *= (T)2.25 * x * x;
+      g = eps / d * ((T)-12.0 / sig * ex + (T)6.0 / d * x);
+      v = eps * (ex - x);
+    } else {
+      g = eps / d * ((T)-12.0 / sig * ex);
+      v = eps * ex;
+    }
+  } else {
+    T qq = qi * qj * (T)P.inv_diel;
+    T alpha = (T)P.alpha;
+    T rab2 = pi2 + pj2;
+    if (alpha > (T)0) {
+      T x = alpha * d;
+      if (rab2 > (T)0) {
+        T rab = M::sqrt_(rab2);
+        T y = d / rab;
+        v = qq / d * (M::erfc_(x) - M::erfc_(y));
+        g = (two_div_sqrt_pi * (M::exp_(-y * y) / rab - M::exp_(-x * x) * alpha) * qq - v) / d2;
+      } else {
+        v = qq * M::erfc_(x) / d;
+        g = (-two_div_sqrt_pi * alpha * M::exp_(-x * x) * qq - v) / d2;
+      }
+    } else {
+      if (rab2 > (T)0) {
+        T rab = M::sqrt_(rab2);
+        T y = d / rab;
+        v = qq / d * M::erf_(y);
+        g = (two_div_sqrt_pi / rab * M::exp_(-y * y) * qq - v) / d2;
+      } else {
+        v = qq / d;
+        g = -v / d2;
+      }
+    }
+  }
+  if (P.tr_kind != YG_TR_NONE && (v != (T)0 || g != (T)0)) {
+    T rc = (T)P.rcut, par = (T)P.tr_par, h, hg;
+    if (P.tr_kind == YG_TR_HAMMER) {
+      T x = d - rc;
+      h = M::exp_(par / x);
+      hg = -h * par / x / x;
+    } else {
+      T x = rc - d;
+      if (x > par) {
+        h = (T)1;
+        hg = (T)0;
+      } else {
+        x /= par;
+        h = ((T)3 - (T)2 * x) * x * x;
+        hg = (T)-6 * x * ((T)1 - x) / par;
+      }
+    }
+    g = g * h + v * hg / d;
+    v *= h;
+  }
+}
+
+// Accumulator: plain (FP64 or FP32) or Kahan-compensated FP32.
+template <typename T, bool KAHAN> struct Acc {
+  T s;
+  __device__ __forceinline__ void init() { s = (T)0; }
+  __device__ __forceinline__ void add(T x) { s += x; }
+  __device__ __forceinline__ double value() const { return (double)s; }
+};
+template <> struct Acc<float, true> {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int MODE, int NPOT>
+__global__ void __launch_bounds__(256) k_pair(PairArgs A) {
+  typedef typename std::conditional<MODE == YG_FP64, double, float>::type T;
+  const bool kahan = (MODE == YG_MIXED_KAHAN);
+  __shared__ double red[8][NPOT * 7];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  Acc<T, kahan> E[NPOT], G[NPOT][3], V[NPOT][6];
+#pragma unroll
+  for (int p = 0; p < NPOT; p++) {
+    E[p].init();
+#pragma unroll
+    for (int k = 0; k < 3; k++) G[p][k].init();
+#pragma unroll
+    for (int k = 0; k < 6; k++) V[p][k].init();
+  }
+  if (i < A.natom) {
+    T xi, yi, zi, qi;
+    if (MODE == YG_FP64) {
+      double4_32a x = A.x64[i];
+      xi = (T)x.x; yi = (T)x.y; zi = (T)x.z; qi = (T)x.w;
+    } else {
+      float4 x = A.x32[i];
+      xi = (T)x.x; yi = (T)x.y; zi = (T)x.z; qi = (T)x.w;
+    }
+    T pi[NPOT][4];
+#pragma unroll
+    for (int p = 0; p < NPOT; p++)
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        pi[p][k] = (MODE == YG_FP64) ? (T)A.pp64[i * 4 * YG_MAX_POT + 4 * p + k]
+                                     : (T)A.pp32[i * 4 * YG_MAX_POT + 4 * p + k];
+    const int cnt = A.ncount[i];
+    const uint2 *row = A.nbr + i * A.cap;
+    for (int e = lane; e < cnt; e += 32) {
+      const uint2 ent = row[e];
+      const int j = (int)ent.x;
+      const int oidx = (int)(ent.y & YG_META_OFF_MASK);
+      const int code = (int)((ent.y >> YG_META_SCALE_SHIFT) & 7u);
+      T dx, dy, dz, qj;
+      if (MODE == YG_FP64) {
+        double4_32a xj = A.x64[j];
+        dx = (T)((xj.x - (double)xi) + A.shift64[3 * oidx]);
+        dy = (T)((xj.y - (double)yi) + A.shift64[3 * oidx + 1]);
+        dz = (T)((xj.z - (double)zi) + A.shift64[3 * oidx + 2]);
+        qj = (T)xj.w;
+      } else {
+        float4 xj = A.x32[j];
+        float4 sh = A.shift32[oidx];
+        dx = (T)((xj.x - (float)xi) + sh.x);
+        dy = (T)((xj.y - (float)yi) + sh.y);
+        dz = (T)((xj.z - (float)zi) + sh.z);
+        qj = (T)xj.w;
+      }
+      const T d2 = dx * dx + dy * dy + dz * dz;
+      const T d = Num<T>::sqrt_(d2);
+      const T s = (T)A.scale[code];
+      if (s == (T)0) continue;
+#pragma unroll
+      for (int p = 0; p < NPOT; p++) {
+        if (!(d < (T)A.pot[p].rcut)) continue;
+        T pj[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          pj[k] = (MODE == YG_FP64) ? (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * p + k]
+                                    : (T)A.pp32[(int64_t)j * 4 * YG_MAX_POT + 4 * p + k];
+        T v, g;
+        pair_term<T>(A.pot[p], d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0], pj[1], pj[2], pj[3],
+                     qi, qj, v, g);
+        E[p].add((T)0.5 * s * v);
+        if (A.want_grad) {
+          g *= s;
+          G[p][0].add(-dx * g);
+          G[p][1].add(-dy * g);
+          G[p][2].add(-dz * g);
+          const T hg = (T)0.5 * g;
+          V[p][0].add(dx * dx * hg);
+          V[p][1].add(dy * dy * hg);
+          V[p][2].add(dz * dz * hg);
+          V[p][3].add(dx * dy * hg);
+          V[p][4].add(dx * dz * hg);
+          V[p][5].add(dy * dz * hg);
+        }
+      }
+    }
+  }
+  // warp reductions (FP64 unless Kahan mode, which stays FP32)
+  double part[NPOT * 7];
+#pragma unroll
+  for (int p = 0; p < NPOT; p++) {
+    part[7 * p] = E[p].value();
+#pragma unroll
+    for (int k = 0; k < 6; k++) part[7 * p + 1 + k] = V[p][k].value();
+  }
+#pragma unroll
+  for (int v = 0; v < NPOT * 7; v++) {
+    if (kahan) part[v] = (double)warp_sum<float>((float)part[v]);
+    else part[v] = warp_sum<double>(part[v]);
+  }
+  if (A.want_grad && i < A.natom) {
+    const int oi = A.sorted[i];
+#pragma unroll
+    for (int p = 0; p < NPOT; p++) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        double gv = kahan ? (double)warp_sum<float>((float)G[p][k].value()) : warp_sum<double>(G[p][k].value());
+        if (lane == 0) A.gpos[p][3 * (int64_t)oi + k] = gv;
+      }
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int v = 0; v < NPOT * 7; v++) red[wid][v] = part[v];
+  }
+  __syncthreads();
+  if (threadIdx.x < NPOT * 7) {
+    double s = 0.0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; w++) s += red[w][threadIdx.x];
+    A.partial[(int64_t)blockIdx.x * NPOT * 7 + threadIdx.x] = s;
+  }
+}
+
+// Sums column v of a (nblocks x nval) partial array in a fixed order.
+__global__ void k_reduce_cols(const double *__restrict__ partials, int nblocks, int nval,
+                              double *__restrict__ out) {
+  __shared__ double sh[256];
+  const int v = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(int64_t)b * nval + v];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[v] = sh[0];
+}
+
+// Writes (E, 6 virial components) of potential p as the (E, vtens[9]) record
+// of a result slot.
+__global__ void k_store_pair_ev(const double *__restrict__ sums, int npot, double *__restrict__ part_ev) {
+  int p = threadIdx.x;
+  if (p >= npot) return;
+  const double *s = sums + 7 * p;
+  double *o = part_ev + 10 * (YG_PART_PAIR0 + p);
+  o[0] = s[0];
+  o[1] = s[1]; o[2] = s[4]; o[3] = s[5];
+  o[4] = s[4]; o[5] = s[2]; o[6] = s[6];
+  o[7] = s[5]; o[8] = s[6]; o[9] = s[3];
+}
+
+template <int MODE, int NPOT>
+int launch_pair_t(yg_ctx *ctx, PairArgs &A, int nblocks) {
+  k_pair<MODE, NPOT><<<nblocks, 256, 0, ctx->stream>>>(A);
+  YG_LAUNCH_CHECK(ctx, "k_pair");
+  return YG_OK;
+}
+
+template <int MODE>
+int launch_pair_m(yg_ctx *ctx, PairArgs &A, int npot, int nblocks) {
+  switch (npot) {
+    case 1: return launch_pair_t<MODE, 1>(ctx, A, nblocks);
+    case 2: return launch_pair_t<MODE, 2>(ctx, A, nblocks);
+    default: return launch_pair_t<MODE, 3>(ctx, A, nblocks);
+  }
+}
+
+}  // namespace
+
+int yg_launch_reduce_ev(yg_ctx *ctx, const double *partials, int nblocks, int nval, double *out) {
+  k_reduce_cols<<<nval, 256, 0, ctx->stream>>>(partials, nblocks, nval, out);
+  YG_LAUNCH_CHECK(ctx, "k_reduce_cols");
+  return YG_OK;
+}
+
+int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
+  PairArgs A;
+  int slots[YG_MAX_POT];
+  int npot = 0;
+  for (int p = 0; p < YG_MAX_POT; p++) {
+    if (!(slot_mask & (1 << p))) continue;
+    const PairPotHost &P = ctx->pot[p];
+    if (!P.active) {
+      yg_set_error("pair slot not registered");
+      return YG_ERR_STATE;
+    }
+    if (P.kind == YG_POT_EI && !ctx->have_charges) {
+      yg_set_error("EI pair potential needs charges");
+      return YG_ERR_STATE;
+    }
+    PairPotDev &D = A.pot[npot];
+    D.kind = P.kind;
+    D.tr_kind = P.tr_kind;
+    D.rcut = P.rcut;
+    D.rcut2 = P.rcut * P.rcut;
+    D.tr_par = P.tr_par;
+    D.alpha = P.alpha;
+    D.inv_diel = 1.0 / P.dielectric;
+    D.has_radii = !P.radius2.empty();
+    slots[npot] = p;
+    npot++;
+  }
+  if (npot == 0) return YG_OK;
+  const int64_t N = ctx->natom;
+  A.natom = N;
+  A.cap = ctx->nbr_cap;
+  A.nbr = ctx->d_nbr;
+  A.ncount = ctx->d_ncount;
+  A.sorted = ctx->d_sorted;
+  A.x64 = ctx->d_x64;
+  A.x32 = ctx->d_x32;
+  A.shift64 = ctx->d_shift64;
+  A.shift32 = ctx->d_shift32;
+  A.pp64 = ctx->d_pp64;
+  A.pp32 = ctx->d_pp32;
+  for (int k = 0; k < 5; k++) A.scale[k] = ctx->scale_tab[k];
+  for (int p = 0; p < YG_MAX_POT; p++) A.gpos[p] = nullptr;
+  for (int q = 0; q < npot; q++) A.gpos[q] = ctx->d_part_gpos + (size_t)(YG_PART_PAIR0 + slots[q]) * N * 3;
+  A.want_grad = want_grad;
+  // parameter columns: the kernel uses column q for the q-th active slot, so
+  // the slots must be the first npot columns (slot q == q).  Registering
+  // slots contiguously from 0 is required by the host API.
+  for (int q = 0; q < npot; q++) {
+    if (slots[q] != q) {
+      yg_set_error("pair slots must be used contiguously from slot 0");
+      return YG_ERR_ARG;
+    }
+  }
+  const int nblocks = yg_blocks(N * 32, 256);
+  const int nval = npot * 7;
+  int rc;
+  if ((rc = yg_ensure((void **)&ctx->d_red, &ctx->red_cap,
+                      ((size_t)nblocks * nval + 64 + nval) * sizeof(double))))
+    return rc;
+  A.partial = ctx->d_red + 64;
+  if (ctx->precision == YG_FP64) rc = launch_pair_m<YG_FP64>(ctx, A, npot, nblocks);
+  else if (ctx->precision == YG_MIXED) rc = launch_pair_m<YG_MIXED>(ctx, A, npot, nblocks);
+  else rc = launch_pair_m<YG_MIXED_KAHAN>(ctx, A, npot, nblocks);
+  if (rc) return rc;
+  double *sums = ctx->d_red + 64 + (size_t)nblocks * nval;
+  if ((rc = yg_launch_reduce_ev(ctx, A.partial, nblocks, nval, sums))) return rc;
+  k_store_pair_ev<<<1, 32, 0, ctx->stream>>>(sums, npot, ctx->d_part_ev);
+  YG_LAUNCH_CHECK(ctx, "k_store_pair_ev");
+  if (!want_grad) {
+    for (int q = 0; q < npot; q++)
+      YG_CUDA(cudaMemsetAsync(ctx->d_part_gpos + (size_t)(YG_PART_PAIR0 + slots[q]) * N * 3, 0,
+                              N * 3 * sizeof(double), ctx->stream));
+  }
+  for (int q = 0; q < npot; q++) ctx->part_valid[YG_PART_PAIR0 + slots[q]] = 1;
+  return YG_OK;
+}
