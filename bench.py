@@ -305,7 +305,7 @@ def cpu_sample(natom, seconds_budget=20.0):
     L = oracle.lib()
     cell = oracle.OracleCell(spec['rvecs'])
     rc = spec['rcut'] + spec['skin']
-    M = min(N, 6000)
+    M = min(N, 16000)
     sub = np.ascontiguousarray(spec['pos'][:M])
     rmax = np.zeros(3, np.int64)
     rows = np.zeros(int(M * 500), oracle.neigh_dtype)
@@ -332,7 +332,7 @@ def cpu_sample(natom, seconds_budget=20.0):
     gmax = np.ceil(spec['ewald']['gcut'] / cell.gspacings - 0.5).astype(np.int64)
     gsub = gmax.copy()
     gsub[0] = 0
-    gsub[1] = 2
+    gsub[1] = 5
     work = np.zeros(2 * N)
     t0 = time.perf_counter()
     L.orc_ewald_reci(oracle._p(spec['pos']), N, 0, N, oracle._p(spec['charges']), oracle._p(cell.rvecs),

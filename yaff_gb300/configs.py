@@ -25,7 +25,9 @@ bond_terms     (nbt, 4): i, j, K, r0      harmonic bonds (Bond + Harmonic)
 bend_terms     (nat, 5): i, j, k, K, th0  harmonic bends (BendAngle + Harmonic)
 nlow, nhigh    ints (nhigh = -1 means N)
 """
+import hashlib
 import math
+import os
 
 import numpy as np
 
@@ -160,49 +162,86 @@ def flexible_water(nside=20, box=62.1, jitter=0.2, rcut=10.0, skin=1.0, seed=1,
     return spec
 
 
-def _rsa_fill(rng, rvecs, natom, dmin, max_tries=200):
+_CACHE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_build', 'cache')
+
+
+def _cached(kind, key, make):
+    """Positions generated by `make`, cached on disk under the package's
+    build folder keyed by the generator parameters (the insertion of the
+    50,000-atom system takes tens of seconds)."""
+    tag = hashlib.sha256(repr((kind, key)).encode()).hexdigest()[:24]
+    path = os.path.join(_CACHE_DIR, '%s_%s.npy' % (kind, tag))
+    if os.path.exists(path):
+        try:
+            return np.load(path)
+        except (OSError, ValueError):
+            pass
+    arr = make()
+    try:
+        os.makedirs(_CACHE_DIR, exist_ok=True)
+        tmp = path + '.%d.tmp.npy' % os.getpid()
+        np.save(tmp, arr)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+    return arr
+
+
+def _rsa_fill(rng, rvecs, natom, dmin, batch=1024, maxper=8):
     """Random sequential insertion of natom points with minimum image distance
-    dmin in the periodic cell rvecs (rows).  Uses a fractional grid whose
-    cells are at least dmin wide, so only the 27 surrounding grid cells are
-    checked per trial."""
+    dmin in the periodic cell rvecs (rows).
+
+    Trial points come in seeded batches.  A trial is rejected when it lies
+    within dmin of an accepted point (checked against the 27 surrounding
+    cells of a fractional grid whose cells are at least dmin wide) or of an
+    earlier trial of the same batch that passed that check; the survivors are
+    accepted in order.  Deterministic for a given seed."""
     gvecs = np.linalg.inv(rvecs).T
     spac = 1.0 / np.linalg.norm(gvecs, axis=1)
     ng = np.maximum((spac / dmin).astype(int), 1)
-    grid = {}
-    out = np.empty((natom, 3))
+    ncell = int(np.prod(ng))
+    cells = -np.ones((ncell, maxper), np.int64)
+    counts = np.zeros(ncell, np.int64)
+    frac_out = np.zeros((natom + 1, 3))
     dmin2 = dmin * dmin
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
     count = 0
-    batch = 4096
+    accept = 1.0
     while count < natom:
-        frac = rng.random((batch, 3))
-        for f in frac:
+        # batch size adapts to the acceptance rate (about 1000 survivors each)
+        batch = int(min(16384, max(1024, 1000.0 / max(accept, 1e-3))))
+        f = rng.random((batch, 3))
+        c = (f * ng).astype(np.int64) % ng
+        nc = (c[:, None, :] + offs[None, :, :]) % ng
+        nid = nc[..., 0] + ng[0] * (nc[..., 1] + ng[1] * nc[..., 2])
+        cand = cells[nid]                                   # (B, 27, maxper)
+        mask = cand >= 0
+        df = frac_out[np.where(mask, cand, natom)] - f[:, None, None, :]
+        df -= np.round(df)
+        dd = df @ rvecs
+        d2 = np.einsum('bcpi,bcpi->bcp', dd, dd)
+        keep = ~((mask & (d2 < dmin2)).any(axis=(1, 2)))
+        idx = np.nonzero(keep)[0]
+        if len(idx) > 1:
+            fk = f[idx]
+            dk = fk[None, :, :] - fk[:, None, :]
+            dk -= np.round(dk)
+            dc = dk @ rvecs
+            close = np.einsum('ijk,ijk->ij', dc, dc) < dmin2
+            close = np.tril(close, -1)                       # i conflicts with an earlier j
+            idx = idx[~close.any(axis=1)]
+        accept = max(len(idx), 1) / float(batch)
+        for t in idx:
             if count >= natom:
                 break
-            cell = tuple((f * ng).astype(int) % ng)
-            ok = True
-            for dx in (-1, 0, 1):
-                for dy in (-1, 0, 1):
-                    for dz in (-1, 0, 1):
-                        key = ((cell[0] + dx) % ng[0], (cell[1] + dy) % ng[1], (cell[2] + dz) % ng[2])
-                        lst = grid.get(key)
-                        if not lst:
-                            continue
-                        df = out[lst] - f @ rvecs
-                        fr = df @ gvecs.T
-                        fr -= np.round(fr)
-                        dd = fr @ rvecs
-                        if (np.einsum('ij,ij->i', dd, dd) < dmin2).any():
-                            ok = False
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if ok:
-                out[count] = f @ rvecs
-                grid.setdefault(cell, []).append(count)
-                count += 1
-    return out
+            cid = c[t, 0] + ng[0] * (c[t, 1] + ng[1] * c[t, 2])
+            if counts[cid] >= maxper:
+                continue
+            cells[cid, counts[cid]] = count
+            counts[cid] += 1
+            frac_out[count] = f[t]
+            count += 1
+    return frac_out[:natom] @ rvecs
 
 
 def triclinic_mm3_ei(natom=50000, density=50000 / 5.0313e5, angle=75.0, dmin=1.8,
@@ -228,7 +267,7 @@ def triclinic_mm3_ei(natom=50000, density=50000 / 5.0313e5, angle=75.0, dmin=1.8
             unit = triclinic_rvecs(1.0, 1.0, 1.0, ang, ang, ang)
             a = (natom / density / abs(np.linalg.det(unit))) ** (1.0 / 3.0)
     rvecs = triclinic_rvecs(a, a, a, ang, ang, ang) * angstrom
-    pos = _rsa_fill(rng, rvecs, natom, dmin * angstrom)
+    pos = _cached('rsa', (natom, a, angle, dmin, seed), lambda: _rsa_fill(rng, rvecs, natom, dmin * angstrom))
     spec = _base_spec(name or 'triclinic%d' % natom, pos, rvecs)
     sp = np.arange(natom) % 3
     spec['charges'] = np.array([1.2, -0.6, -0.6])[sp]

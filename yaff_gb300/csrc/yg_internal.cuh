@@ -65,6 +65,7 @@ struct PairPotDev {
   double alpha;
   double inv_diel;
   int has_radii;
+  int col;        // parameter column (= result slot) of this potential
 };
 
 struct yg_ctx {

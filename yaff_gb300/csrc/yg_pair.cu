@@ -189,8 +189,8 @@ __global__ void __launch_bounds__(256) k_pair(PairArgs A) {
     for (int p = 0; p < NPOT; p++)
 #pragma unroll
       for (int k = 0; k < 4; k++)
-        pi[p][k] = (MODE == YG_FP64) ? (T)A.pp64[i * 4 * YG_MAX_POT + 4 * p + k]
-                                     : (T)A.pp32[i * 4 * YG_MAX_POT + 4 * p + k];
+        pi[p][k] = (MODE == YG_FP64) ? (T)A.pp64[i * 4 * YG_MAX_POT + 4 * A.pot[p].col + k]
+                                     : (T)A.pp32[i * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
     const int cnt = A.ncount[i];
     const uint2 *row = A.nbr + i * A.cap;
     for (int e = lane; e < cnt; e += 32) {
@@ -223,8 +223,8 @@ __global__ void __launch_bounds__(256) k_pair(PairArgs A) {
         T pj[4];
 #pragma unroll
         for (int k = 0; k < 4; k++)
-          pj[k] = (MODE == YG_FP64) ? (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * p + k]
-                                    : (T)A.pp32[(int64_t)j * 4 * YG_MAX_POT + 4 * p + k];
+          pj[k] = (MODE == YG_FP64) ? (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k]
+                                    : (T)A.pp32[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
         T v, g;
         pair_term<T>(A.pot[p], d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0], pj[1], pj[2], pj[3],
                      qi, qj, v, g);
@@ -298,13 +298,18 @@ __global__ void k_reduce_cols(const double *__restrict__ partials, int nblocks, 
   if (threadIdx.x == 0) out[v] = sh[0];
 }
 
-// Writes (E, 6 virial components) of potential p as the (E, vtens[9]) record
-// of a result slot.
-__global__ void k_store_pair_ev(const double *__restrict__ sums, int npot, double *__restrict__ part_ev) {
+struct SlotMap {
+  int slot[YG_MAX_POT];
+};
+
+// Writes (E, 6 virial components) of the p-th evaluated potential as the
+// (E, vtens[9]) record of its result slot.
+__global__ void k_store_pair_ev(const double *__restrict__ sums, int npot, SlotMap map,
+                                double *__restrict__ part_ev) {
   int p = threadIdx.x;
   if (p >= npot) return;
   const double *s = sums + 7 * p;
-  double *o = part_ev + 10 * (YG_PART_PAIR0 + p);
+  double *o = part_ev + 10 * (YG_PART_PAIR0 + map.slot[p]);
   o[0] = s[0];
   o[1] = s[1]; o[2] = s[4]; o[3] = s[5];
   o[4] = s[4]; o[5] = s[2]; o[6] = s[6];
@@ -359,6 +364,7 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
     D.alpha = P.alpha;
     D.inv_diel = 1.0 / P.dielectric;
     D.has_radii = !P.radius2.empty();
+    D.col = p;
     slots[npot] = p;
     npot++;
   }
@@ -379,15 +385,8 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   for (int p = 0; p < YG_MAX_POT; p++) A.gpos[p] = nullptr;
   for (int q = 0; q < npot; q++) A.gpos[q] = ctx->d_part_gpos + (size_t)(YG_PART_PAIR0 + slots[q]) * N * 3;
   A.want_grad = want_grad;
-  // parameter columns: the kernel uses column q for the q-th active slot, so
-  // the slots must be the first npot columns (slot q == q).  Registering
-  // slots contiguously from 0 is required by the host API.
-  for (int q = 0; q < npot; q++) {
-    if (slots[q] != q) {
-      yg_set_error("pair slots must be used contiguously from slot 0");
-      return YG_ERR_ARG;
-    }
-  }
+  SlotMap map;
+  for (int q = 0; q < YG_MAX_POT; q++) map.slot[q] = q < npot ? slots[q] : 0;
   const int nblocks = yg_blocks(N * 32, 256);
   const int nval = npot * 7;
   int rc;
@@ -401,7 +400,7 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   if (rc) return rc;
   double *sums = ctx->d_red + 64 + (size_t)nblocks * nval;
   if ((rc = yg_launch_reduce_ev(ctx, A.partial, nblocks, nval, sums))) return rc;
-  k_store_pair_ev<<<1, 32, 0, ctx->stream>>>(sums, npot, ctx->d_part_ev);
+  k_store_pair_ev<<<1, 32, 0, ctx->stream>>>(sums, npot, map, ctx->d_part_ev);
   YG_LAUNCH_CHECK(ctx, "k_store_pair_ev");
   if (!want_grad) {
     for (int q = 0; q < npot; q++)

@@ -58,6 +58,8 @@ class DeviceSystem(object):
         self.ewald_key = None
         self.valence_key = None
         self._pos_staging = np.zeros((self.natom, 3))
+        # bumped whenever the device list is invalidated (cell or scalings)
+        self.list_epoch = 0
         self.sync_cell()
         if system.charges is not None:
             self.sync_charges()
@@ -90,6 +92,7 @@ class DeviceSystem(object):
         gv = np.ascontiguousarray(cell.full_gvecs())
         check(self.lib.yg_set_cell(self.ctx, ptr(rv), ptr(gv), cell.nvec, float(cell.volume)), 'yg_set_cell')
         self._cell_key = key
+        self.list_epoch += 1
         return True
 
     def sync_charges(self):
@@ -119,6 +122,7 @@ class DeviceSystem(object):
         nb = np.ascontiguousarray(st['nbond'], dtype=np.int64)
         check(self.lib.yg_set_scalings(self.ctx, ptr(a), ptr(b), ptr(s), ptr(nb), len(st)), 'yg_set_scalings')
         self.scalings_obj = scalings
+        self.list_epoch += 1
 
     def register_pair(self, part):
         if part in self.pair_slots:

@@ -221,6 +221,7 @@ class ForcePartPair(ForcePart):
         self.pair_pot = pair_pot
         self.nlist.request_rcut(pair_pot.rcut)
         self._slot = None
+        self._register()
 
     def _register(self):
         dev = device_of(self.system)

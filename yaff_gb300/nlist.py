@@ -39,6 +39,7 @@ class NeighborList(object):
             raise ValueError('nhigh must not be smaller than nlow, received %d.' % nhigh)
         self.nhigh = nhigh
         self._built = False
+        self._epoch = -1
         self.rebuild_next = False
         self._neighs_cache = None
         self.nrebuild = 0
@@ -60,6 +61,8 @@ class NeighborList(object):
 
     def _need_rebuild(self):
         if self.skin <= 0 or not self._built or self.rebuild_next:
+            return True
+        if self._epoch != self.device.list_epoch:
             return True
         d2 = ctypes.c_double()
         check(self.device.lib.yg_nlist_max_disp2(self.device.ctx, ctypes.byref(d2)), 'yg_nlist_max_disp2')
@@ -85,6 +88,7 @@ class NeighborList(object):
                                          ctypes.byref(n)), 'yg_nlist_build')
             self.nneigh = n.value
             self._built = True
+            self._epoch = dev.list_epoch
             self.rebuild_next = False
             self.nrebuild += 1
             return True
