@@ -143,9 +143,10 @@ def run_gb300(args, world, rank, local):
     dpos = [torch.tensor(positions(s), dtype=torch.float64, device='cuda')
             for s in range(args.warmup + args.steps)]
 
-    def device_step(s):
+    def device_step(s, rebuild=True):
         dev.upload_positions_device(dpos[s].data_ptr())
-        ff.system.pos[:] = 0.0  # host copy unused on this path
+        if rebuild:
+            ff.nlist.rebuild_next = True   # full neighbour-list rebuild every step
         ff.nlist.update(upload=False)
         pmask = 0
         for p in ff.parts:
@@ -166,6 +167,7 @@ def run_gb300(args, world, rank, local):
     if world > 1:
         torch.distributed.barrier()
     launches0 = dev.launch_count()
+    nrebuild0 = ff.nlist.nrebuild
     clocks = ClockSampler(local)
     clocks.start()
     times = []
@@ -180,6 +182,21 @@ def run_gb300(args, world, rank, local):
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) * 1e-3)
+    nrebuild_timed = ff.nlist.nrebuild
+    launches = dev.launch_count() - launches0
+    # skin path (the neighbour list of the last rebuild is reused, as yaff
+    # does while displacements stay inside the skin)
+    skin_times = []
+    for s in range(args.warmup, args.warmup + args.steps):
+        flush.fill_(float(s))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mask = device_step(s, rebuild=False)
+        dev.get_total(mask, None, None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        skin_times.append(e0.elapsed_time(e1) * 1e-3)
     # dominant kernel timing: the reciprocal-space part alone
     reci = [p for p in ff.parts if isinstance(p, yaff_gb300.ForcePartEwaldReciprocal)][0]
     for s in range(5):
@@ -192,7 +209,6 @@ def run_gb300(args, world, rank, local):
         torch.cuda.synchronize()
         ewald_times.append(e0.elapsed_time(e1) * 1e-3)
     clk = clocks.stop()
-    launches = dev.launch_count() - launches0
     t_step = float(np.mean(times))
     if world > 1:
         t = torch.tensor([sum(times)], dtype=torch.float64, device='cuda')
@@ -210,6 +226,7 @@ def run_gb300(args, world, rank, local):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ff.update_pos(p)
+        ff.nlist.rebuild_next = True   # same work as the device-resident steps
         gpos[:] = 0.0
         vtens[:] = 0.0
         ff.compute(gpos, vtens)
@@ -264,6 +281,8 @@ def run_gb300(args, world, rank, local):
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99))},
         'fp64_evals_per_s': fp64,
+        'skin_path_evals_per_s': 1.0 / float(np.mean(skin_times)),
+        'rebuilds_in_timed_steps': int(nrebuild_timed - nrebuild0),
         'e2e': {'value': e2e, 'unit': 'evals/s', 'h2d_bytes_per_step': natom * 24,
                 'd2h_bytes_per_step': natom * 24 + 9 * 8 + 16 * 8},
         'gpu_launches': int(launches),

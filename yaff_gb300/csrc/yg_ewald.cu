@@ -16,12 +16,13 @@
 //   P_ac = X[a][c],  W = 2 A(k) S_eff(k)
 //
 // is a second product over m.  Both run as shared-memory tiled kernels over
-// 8x8 blocks of (g0, g1) columns; blocks wholly outside the k-sphere are
-// skipped.  The phases are built per atom from FP64 fractional coordinates
+// tiles of (g0, g1) columns sorted by their extent in m inside the k-sphere,
+// so each tile loops only over the m values it needs.  The phases are built per atom from FP64 fractional coordinates
 // (reduced to [0,1) before the sine/cosine), so FP32 tables keep ~1e-7
 // absolute phase accuracy even where |k.r| reaches hundreds of radians.
 // Partial structure factors of atom chunks are summed in FP64 in a fixed
 // order; the energy, the virial and the prefactors are FP64.
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
 #include <vector>
@@ -30,10 +31,9 @@
 
 namespace {
 
-#define EW_TC 64     // columns per tile (8 x 8 in g0, g1)
-#define EW_MT 32     // m values per S-pass tile
-#define EW_KA 32     // atoms staged per step in the S pass
-#define EW_ATB 512   // atoms per S-pass block
+#define EW_SC 128    // columns per S-pass tile
+#define EW_FC 64     // columns per force-pass tile
+#define EW_MS 32     // m values per S-pass slab
 #define EW_MAXM 64   // largest supported G2 + 1
 
 template <typename T> struct C2;
@@ -93,113 +93,128 @@ __device__ __forceinline__ typename C2<T>::t tab_get(const typename C2<T>::t *__
   return v;
 }
 
-struct Tile {
-  int gb0, gb1, mhi;
-};
+// Sorted column descriptors: (g0, g1, dense column index, mhi), ordered by
+// decreasing mhi (the largest m of the column inside the half sphere) and
+// padded with (0, 0, -1, -1) to a multiple of EW_SC.  Grouping columns of
+// similar extent keeps the per-tile m range tight.
 
-// S pass.  grid = (tiles, atom chunks, m tiles); 128 threads, each owning
-// 4 columns x 4 m values of the 64 x 32 output tile.
+template <typename T> struct SfacCfg;
+template <> struct SfacCfg<float> { enum { KA = 32, ATB = 512 }; };
+template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
+
+// S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
+// Lane l owns columns 2l, 2l+1, 64+2l, 64+2l+1 of the tile (contiguous
+// 16-byte shared loads); warp w owns m = w + 4j, j < 8, of the slab, so the
+// m values beyond the tile's extent are skipped warp-uniformly.  Thread t
+// stages column t of X for the chunk's atoms.
 template <typename T, typename TA>
 __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restrict__ tab, int a0, int a1, int G0,
-                                              int G1, int G2, const int4 *__restrict__ tiles,
-                                              typename C2<TA>::t *__restrict__ Spart, int ntile) {
+                                              int G1, int G2, const int4 *__restrict__ cols,
+                                              typename C2<TA>::t *__restrict__ Spart, int nstile, int nslab) {
   typedef typename C2<T>::t CT;
-  __shared__ CT sX[EW_KA][EW_TC];
-  __shared__ CT sY[EW_KA][EW_MT];
+  const int KA = SfacCfg<T>::KA, ATB = SfacCfg<T>::ATB;
+  __shared__ __align__(16) CT sX[KA][EW_SC];
+  __shared__ __align__(16) CT sY[KA][EW_MS];
   const int L = G0 + G1 + G2 + 3;
-  const int4 tl = tiles[blockIdx.x];
-  const int mb = blockIdx.z * EW_MT;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int abeg = a0 + blockIdx.y * EW_ATB;
-  const int aend = min(a1, abeg + EW_ATB);
-  T acc_re[4][4], acc_im[4][4];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x, slab = blockIdx.z;
+  const int mb = slab * EW_MS;
+  const int4 mycol = cols[tile * EW_SC + threadIdx.x];
+  const int Mt = cols[tile * EW_SC].w + 1 - mb;
+  const int nj = (Mt > w) ? min(8, (Mt - w + 3) / 4) : 0;
+  const int abeg = a0 + blockIdx.y * ATB;
+  const int aend = min(a1, abeg + ATB);
+  T ar[4][8], ai[4][8];
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      acc_re[i][j] = (T)0;
-      acc_im[i][j] = (T)0;
+    for (int j = 0; j < 8; j++) {
+      ar[i][j] = (T)0;
+      ai[i][j] = (T)0;
     }
-  if (mb <= tl.z) {
-    for (int ab = abeg; ab < aend; ab += EW_KA) {
-      // stage X (E0 E1) and Y (q E2) for EW_KA atoms
-      for (int v = threadIdx.x; v < EW_KA * EW_TC; v += blockDim.x) {
-        int la = v / EW_TC, c = v % EW_TC;
-        int a = ab + la;
+  if (Mt > 0) {
+    const int ag0 = mycol.x < 0 ? -mycol.x : mycol.x, ag1 = mycol.y < 0 ? -mycol.y : mycol.y;
+    const T s0 = mycol.x < 0 ? (T)-1 : (T)1, s1 = mycol.y < 0 ? (T)-1 : (T)1;
+    for (int ab = abeg; ab < aend; ab += KA) {
+#pragma unroll 4
+      for (int la = 0; la < KA; la++) {
+        const int a = ab + la;
         CT x = cmk<T>((T)0, (T)0);
-        int g0 = tl.x + (c >> 3), g1 = tl.y + (c & 7);
-        if (a < aend && g0 <= G0 && g1 <= G1) {
+        if (a < aend && mycol.z >= 0) {
           const CT *row = tab + (int64_t)a * L;
-          CT e0 = tab_get<T>(row, 0, g0);
-          CT e1 = tab_get<T>(row, G0 + 1, g1);
+          CT e0 = row[ag0], e1 = row[G0 + 1 + ag1];
+          e0.y *= s0;
+          e1.y *= s1;
           x = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
         }
-        sX[la][c] = x;
+        sX[la][threadIdx.x] = x;
       }
-      for (int v = threadIdx.x; v < EW_KA * EW_MT; v += blockDim.x) {
-        int la = v / EW_MT, m = v % EW_MT;
-        int a = ab + la;
-        CT y = cmk<T>((T)0, (T)0);
-        if (a < aend && mb + m <= G2) y = tab[(int64_t)a * L + G0 + G1 + 2 + mb + m];
-        sY[la][m] = y;
+      for (int v = threadIdx.x; v < KA * EW_MS; v += blockDim.x) {
+        const int la = v / EW_MS, m = v % EW_MS;
+        const int a = ab + la, mm = mb + m;
+        sY[la][m] = (a < aend && mm <= G2) ? tab[(int64_t)a * L + G0 + G1 + 2 + mm] : cmk<T>((T)0, (T)0);
       }
       __syncthreads();
-#pragma unroll 4
-      for (int la = 0; la < EW_KA; la++) {
-        CT x[4], y[4];
+#pragma unroll 2
+      for (int la = 0; la < KA; la++) {
+        CT x[4];
+        x[0] = sX[la][2 * lane];
+        x[1] = sX[la][2 * lane + 1];
+        x[2] = sX[la][64 + 2 * lane];
+        x[3] = sX[la][64 + 2 * lane + 1];
 #pragma unroll
-        for (int i = 0; i < 4; i++) x[i] = sX[la][tx * 4 + i];
+        for (int j = 0; j < 8; j++) {
+          if (j < nj) {
+            const CT y = sY[la][w + 4 * j];
 #pragma unroll
-        for (int j = 0; j < 4; j++) y[j] = sY[la][ty * 4 + j];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            acc_re[i][j] += x[i].x * y[j].x - x[i].y * y[j].y;
-            acc_im[i][j] += x[i].x * y[j].y + x[i].y * y[j].x;
+            for (int i = 0; i < 4; i++) {
+              ar[i][j] += x[i].x * y.x - x[i].y * y.y;
+              ai[i][j] += x[i].x * y.y + x[i].y * y.x;
+            }
           }
+        }
       }
       __syncthreads();
     }
   }
-  // partial layout: [chunk][tile][mtile][c][m]
+  // partial layout: [chunk][tile][slab][c][m]
   typedef typename C2<TA>::t CA;
-  int64_t base = (((int64_t)blockIdx.y * ntile + blockIdx.x) * gridDim.z + blockIdx.z) * (EW_TC * EW_MT);
+  const int64_t base = (((int64_t)blockIdx.y * nstile + tile) * nslab + slab) * (EW_SC * EW_MS);
 #pragma unroll
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < 4; i++) {
+    const int c = 2 * lane + (i & 1) + 64 * (i >> 1);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < 8; j++) {
       CA v;
-      v.x = (TA)acc_re[i][j];
-      v.y = (TA)acc_im[i][j];
-      Spart[base + (tx * 4 + i) * EW_MT + ty * 4 + j] = v;
+      v.x = (TA)ar[i][j];
+      v.y = (TA)ai[i][j];
+      Spart[base + c * EW_MS + w + 4 * j] = v;
     }
+  }
 }
 
-// Sums the chunk partials in FP64 into the dense S[c][m] grid (re, im).
+// Sums the chunk partials in FP64 (fixed order) into the dense S[col][m].
 template <typename TA>
-__global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int nchunk, int ntile, int nmt,
-                              const int4 *__restrict__ tiles, int G0, int G1, int nm,
-                              double *__restrict__ S) {
-  int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t per = (int64_t)ntile * nmt * EW_TC * EW_MT;
+__global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int nchunk, int nstile, int nslab,
+                              const int4 *__restrict__ cols, int nm, double *__restrict__ S) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t per = (int64_t)nstile * nslab * EW_SC * EW_MS;
   if (idx >= per) return;
-  int m = (int)(idx % EW_MT);
-  int c = (int)((idx / EW_MT) % EW_TC);
-  int mt = (int)((idx / (EW_MT * EW_TC)) % nmt);
-  int t = (int)(idx / ((int64_t)EW_MT * EW_TC * nmt));
-  int4 tl = tiles[t];
-  int g0 = tl.x + (c >> 3), g1 = tl.y + (c & 7), mm = mt * EW_MT + m;
-  if (g0 > G0 || g1 > G1 || mm >= nm) return;
+  const int m = (int)(idx % EW_MS);
+  const int c = (int)((idx / EW_MS) % EW_SC);
+  const int slab = (int)((idx / (EW_MS * EW_SC)) % nslab);
+  const int tile = (int)(idx / ((int64_t)EW_MS * EW_SC * nslab));
+  const int4 col = cols[tile * EW_SC + c];
+  const int mm = slab * EW_MS + m;
+  if (col.z < 0 || mm > col.w) return;
   double re = 0.0, im = 0.0;
   for (int ch = 0; ch < nchunk; ch++) {
-    typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
+    const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
     re += (double)v.x;
     im += (double)v.y;
   }
-  int64_t col = (int64_t)(g0 + G0) * (2 * G1 + 1) + (g1 + G1);
-  S[2 * (col * nm + mm)] = re;
-  S[2 * (col * nm + mm) + 1] = im;
+  S[2 * ((int64_t)col.z * nm + mm)] = re;
+  S[2 * ((int64_t)col.z * nm + mm) + 1] = im;
 }
 
 // Energy and virial per k (FP64), plus the force-pass weights
@@ -291,25 +306,28 @@ template <> struct CompAcc<float> {
 };
 
 // Force pass.  grid = atom tiles (16*RA atoms) of one group; 256 threads:
-// ta = tid % 16 owns RA atoms, tc = tid / 16 owns 4 consecutive columns.
+// ta = tid % 16 owns atoms ta + 16 r (r < RA), tc = tid / 16 owns columns
+// 4 tc .. 4 tc + 3 of each 64-column tile (shared loads of Y are contiguous
+// across lanes, loads of W broadcast).  Tiles follow the sorted column list,
+// so the m loop of a tile stops at its extent.
 template <typename T, int RA>
 __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__restrict__ tab, int a0, int a1,
-                                                     int G0, int G1, int G2, const int4 *__restrict__ tiles,
-                                                     int ntile, const typename C2<T>::t *__restrict__ W,
+                                                     int G0, int G1, int G2, const int4 *__restrict__ cols,
+                                                     int nftile, const typename C2<T>::t *__restrict__ W,
                                                      double *__restrict__ gfrac) {
   typedef typename C2<T>::t CT;
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int NA = 16 * RA;
   const int nm = G2 + 1;
   CT *sY = reinterpret_cast<CT *>(smem_raw);          // [nm][NA]
-  CT *sW = sY + (size_t)nm * NA;                       // [nm][EW_TC]
+  CT *sW = sY + (size_t)nm * NA;                       // [nm][EW_FC]
+  int4 *scol = reinterpret_cast<int4 *>(sW + (size_t)nm * EW_FC);
   const int L = G0 + G1 + G2 + 3;
   const int ta = threadIdx.x & 15, tc = threadIdx.x >> 4;
   const int abase = a0 + blockIdx.x * NA;
-  // stage Y = q E2 for the block's atoms
   for (int v = threadIdx.x; v < nm * NA; v += blockDim.x) {
-    int m = v / NA, la = v % NA;
-    int a = abase + la;
+    const int m = v / NA, la = v % NA;
+    const int a = abase + la;
     sY[v] = (a < a1) ? tab[(int64_t)a * L + G0 + G1 + 2 + m] : cmk<T>((T)0, (T)0);
   }
   CompAcc<T> acc[RA][3];
@@ -317,21 +335,17 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
   for (int r = 0; r < RA; r++)
 #pragma unroll
     for (int q = 0; q < 3; q++) acc[r][q].init();
-  const int ncolrow = 2 * G1 + 1;
-  for (int t = 0; t < ntile; t++) {
-    const int4 tl = tiles[t];
-    const int mhi = tl.z;
+  for (int t = 0; t < nftile; t++) {
+    const int4 *tcols = cols + t * EW_FC;
+    const int Mt = tcols[0].w + 1;
+    if (Mt <= 0) continue;
     __syncthreads();
-    for (int v = threadIdx.x; v < (mhi + 1) * EW_TC; v += blockDim.x) {
-      int m = v / EW_TC, c = v % EW_TC;
-      int g0 = tl.x + (c >> 3), g1 = tl.y + (c & 7);
-      CT w = cmk<T>((T)0, (T)0);
-      if (g0 <= G0 && g1 <= G1) {
-        int64_t col = (int64_t)(g0 + G0) * ncolrow + (g1 + G1);
-        w = W[col * nm + m];
-      }
-      sW[m * EW_TC + c] = w;
+    for (int v = threadIdx.x; v < Mt * EW_FC; v += blockDim.x) {
+      const int m = v / EW_FC, c = v % EW_FC;
+      const int4 col = tcols[c];
+      sW[v] = (col.z >= 0 && m <= col.w) ? W[(int64_t)col.z * nm + m] : cmk<T>((T)0, (T)0);
     }
+    if (threadIdx.x < EW_FC) scol[threadIdx.x] = tcols[threadIdx.x];
     __syncthreads();
     T zr[RA][4], zi[RA][4], z2r[RA][4], z2i[RA][4];
 #pragma unroll
@@ -340,19 +354,19 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
       for (int i = 0; i < 4; i++) {
         zr[r][i] = (T)0; zi[r][i] = (T)0; z2r[r][i] = (T)0; z2i[r][i] = (T)0;
       }
-    for (int m = 0; m <= mhi; m++) {
+    for (int m = 0; m < Mt; m++) {
       CT y[RA], w[4];
 #pragma unroll
-      for (int r = 0; r < RA; r++) y[r] = sY[m * NA + ta * RA + r];
+      for (int r = 0; r < RA; r++) y[r] = sY[m * NA + ta + 16 * r];
 #pragma unroll
-      for (int i = 0; i < 4; i++) w[i] = sW[m * EW_TC + tc * 4 + i];
+      for (int i = 0; i < 4; i++) w[i] = sW[m * EW_FC + tc * 4 + i];
       const T fm = (T)m;
 #pragma unroll
       for (int r = 0; r < RA; r++)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          T pr = y[r].x * w[i].x - y[r].y * w[i].y;
-          T pi = y[r].x * w[i].y + y[r].y * w[i].x;
+          const T pr = y[r].x * w[i].x - y[r].y * w[i].y;
+          const T pi = y[r].x * w[i].y + y[r].y * w[i].x;
           zr[r][i] += pr;
           zi[r][i] += pi;
           z2r[r][i] += fm * pr;
@@ -360,26 +374,25 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
         }
     }
     // epilogue: P = E0 E1 of each (atom, column)
-    const int c0 = tc * 4;
-    const int g0 = tl.x + (c0 >> 3);
 #pragma unroll
-    for (int r = 0; r < RA; r++) {
-      int a = abase + ta * RA + r;
-      if (a >= a1) continue;
-      const CT *row = tab + (int64_t)a * L;
-      if (g0 > G0) continue;
-      CT e0 = tab_get<T>(row, 0, g0);
+    for (int i = 0; i < 4; i++) {
+      const int4 col = scol[tc * 4 + i];
+      if (col.z < 0) continue;
+      const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = col.y < 0 ? -col.y : col.y;
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
-        int g1 = tl.y + ((c0 + i) & 7);
-        if (g1 > G1) continue;
-        CT e1 = tab_get<T>(row, G0 + 1, g1);
-        T pr = e0.x * e1.x - e0.y * e1.y;
-        T pi = e0.x * e1.y + e0.y * e1.x;
-        T im1 = pr * zi[r][i] + pi * zr[r][i];
-        T im2 = pr * z2i[r][i] + pi * z2r[r][i];
-        acc[r][0].add((T)g0 * im1);
-        acc[r][1].add((T)g1 * im1);
+      for (int r = 0; r < RA; r++) {
+        const int a = abase + ta + 16 * r;
+        if (a >= a1) continue;
+        const CT *row = tab + (int64_t)a * L;
+        CT e0 = row[ag0], e1 = row[G0 + 1 + ag1];
+        if (col.x < 0) e0.y = -e0.y;
+        if (col.y < 0) e1.y = -e1.y;
+        const T pr = e0.x * e1.x - e0.y * e1.y;
+        const T pi = e0.x * e1.y + e0.y * e1.x;
+        const T im1 = pr * zi[r][i] + pi * zr[r][i];
+        const T im2 = pr * z2i[r][i] + pi * z2r[r][i];
+        acc[r][0].add((T)col.x * im1);
+        acc[r][1].add((T)col.y * im1);
         acc[r][2].add(im2);
       }
     }
@@ -390,11 +403,11 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
 #pragma unroll
   for (int r = 0; r < RA; r++)
 #pragma unroll
-    for (int q = 0; q < 3; q++) red[((size_t)tc * NA + ta * RA + r) * 3 + q] = acc[r][q].value();
+    for (int q = 0; q < 3; q++) red[((size_t)tc * NA + ta + 16 * r) * 3 + q] = acc[r][q].value();
   __syncthreads();
   for (int v = threadIdx.x; v < NA * 3; v += blockDim.x) {
-    int la = v / 3, q = v % 3;
-    int a = abase + la;
+    const int la = v / 3, q = v % 3;
+    const int a = abase + la;
     if (a >= a1) continue;
     double s = 0.0;
     for (int g = 0; g < 16; g++) s += red[((size_t)g * NA + la) * 3 + q];
@@ -485,7 +498,7 @@ __global__ void k_store_corr_ev(const double *__restrict__ sums, double eself, d
 }
 
 template <typename T> size_t force_smem(int nm, int RA) {
-  size_t a = (size_t)nm * (16 * RA + EW_TC) * sizeof(typename C2<T>::t);
+  size_t a = (size_t)nm * (16 * RA + EW_FC) * sizeof(typename C2<T>::t) + EW_FC * sizeof(int4);
   size_t b = (size_t)16 * 16 * RA * 3 * sizeof(double);
   return a > b ? a : b;
 }
@@ -498,8 +511,10 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   const int nm = G2 + 1;
   const int L = G0 + G1 + G2 + 3;
   const int64_t N = ctx->natom;
-  const int ntile = ctx->ew_ntile;
-  const int nmt = (nm + EW_MT - 1) / EW_MT;
+  const int nstile = ctx->ew_ntile;
+  const int nftile = 2 * nstile;
+  const int nslab = (nm + EW_MS - 1) / EW_MS;
+  const int ATB = SfacCfg<T>::ATB;
   const int64_t nk_dense = (int64_t)ctx->ew_ncol * nm;
   int rc;
   // tables
@@ -516,11 +531,11 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   int maxchunk = 0;
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
-    int nch = (int)((n + EW_ATB - 1) / EW_ATB);
+    int nch = (int)((n + ATB - 1) / ATB);
     if (nch > maxchunk) maxchunk = nch;
   }
   if (maxchunk < 1) maxchunk = 1;
-  size_t per = (size_t)ntile * nmt * EW_TC * EW_MT;
+  size_t per = (size_t)nstile * nslab * EW_SC * EW_MS;
   if ((rc = yg_ensure(&ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(CA)))) return rc;
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
@@ -529,14 +544,14 @@ int run_reci(yg_ctx *ctx, int want_grad) {
       YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
       continue;
     }
-    int nch = (int)((n + EW_ATB - 1) / EW_ATB);
-    dim3 grid(ntile, nch, nmt);
+    int nch = (int)((n + ATB - 1) / ATB);
+    dim3 grid(nstile, nch, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     k_sfac<T, TA><<<grid, 128, 0, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
-                                                 (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, ntile);
+                                                 (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
     k_sfac_reduce<TA><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
-        (const CA *)ctx->d_ew_Spart, nch, ntile, nmt, (const int4 *)ctx->d_ew_tiles, G0, G1, nm, S);
+        (const CA *)ctx->d_ew_Spart, nch, nstile, nslab, (const int4 *)ctx->d_ew_tiles, nm, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
   // energy, virial, weights
@@ -571,7 +586,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     const CT *Wg = (const CT *)ctx->d_ew_W + (size_t)(ngroup == 1 ? 0 : gidx[g]) * nk_dense;
     int nblk = (int)((n + 16 * RA - 1) / (16 * RA));
     k_ewald_force<T, RA><<<nblk, 256, smem, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
-                                                          (const int4 *)ctx->d_ew_tiles, ntile, Wg, ctx->d_ew_gpart);
+                                                          (const int4 *)ctx->d_ew_tiles, nftile, Wg, ctx->d_ew_gpart);
     YG_LAUNCH_CHECK(ctx, "k_ewald_force");
   }
   k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
@@ -621,23 +636,19 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
         if (g2 > colmhi[col]) colmhi[col] = g2;
         nk++;
       }
+  // active columns sorted by decreasing extent, padded to a multiple of EW_SC
   std::vector<int4> tiles;
-  for (int b0 = -G0; b0 <= G0; b0 += 8)
-    for (int b1 = -G1; b1 <= G1; b1 += 8) {
-      int mhi = -1;
-      for (int i0 = 0; i0 < 8; i0++)
-        for (int i1 = 0; i1 < 8; i1++) {
-          int g0 = b0 + i0, g1 = b1 + i1;
-          if (g0 > G0 || g1 > G1) continue;
-          int64_t col = (int64_t)(g0 + G0) * nc1 + (g1 + G1);
-          mhi = std::max(mhi, colmhi[col]);
-        }
-      if (mhi >= 0) tiles.push_back(make_int4(b0, b1, mhi, 0));
+  for (int g0 = -G0; g0 <= G0; g0++)
+    for (int g1 = -G1; g1 <= G1; g1++) {
+      int64_t col = (int64_t)(g0 + G0) * nc1 + (g1 + G1);
+      if (colmhi[col] >= 0) tiles.push_back(make_int4(g0, g1, (int)col, colmhi[col]));
     }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const int4 &x, const int4 &y) { return x.w > y.w; });
+  while (tiles.size() % EW_SC) tiles.push_back(make_int4(0, 0, -1, -1));
   ctx->ew_ncol = nc0 * nc1;
   ctx->ew_nm = nm;
   ctx->ew_nk = nk;
-  ctx->ew_ntile = (int)tiles.size();
+  ctx->ew_ntile = (int)(tiles.size() / EW_SC);
   cudaFree(ctx->d_ew_pref);
   cudaFree(ctx->d_ew_tiles);
   cudaFree(ctx->d_ew_S);

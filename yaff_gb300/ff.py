@@ -194,7 +194,8 @@ class ForceField(ForcePart):
         for part in self.parts:
             if isinstance(part, ForcePartEwaldNeutralizing):
                 pv = np.zeros((3, 3)) if vtens is not None else None
-                e = part.compute(None, pv)
+                pg = np.zeros((self.system.natom, 3)) if gpos is not None else None
+                e = part.compute(pg, pv)
                 host_energy += e
                 if pv is not None:
                     host_vtens += pv
