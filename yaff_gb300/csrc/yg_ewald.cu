@@ -99,7 +99,7 @@ __device__ __forceinline__ typename C2<T>::t tab_get(const typename C2<T>::t *__
 // similar extent keeps the per-tile m range tight.
 
 template <typename T> struct SfacCfg;
-template <> struct SfacCfg<float> { enum { KA = 32, ATB = 512 }; };
+template <> struct SfacCfg<float> { enum { KA = 32, ATB = 256 }; };
 template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
 
 // S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
@@ -113,9 +113,10 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
                                               typename C2<TA>::t *__restrict__ Spart, int nstile, int nslab) {
   typedef typename C2<T>::t CT;
   const int KA = SfacCfg<T>::KA, ATB = SfacCfg<T>::ATB;
-  __shared__ __align__(16) CT sX[KA][EW_SC];
-  __shared__ __align__(16) CT sY[KA][EW_MS];
   const int L = G0 + G1 + G2 + 3;
+  extern __shared__ __align__(16) unsigned char sfac_smem[];
+  CT (*sX)[EW_SC] = reinterpret_cast<CT (*)[EW_SC]>(sfac_smem);   // [KA][EW_SC]
+  CT *sRow = reinterpret_cast<CT *>(sfac_smem) + KA * EW_SC;      // [KA][L] table rows
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x, slab = blockIdx.z;
   const int mb = slab * EW_MS;
@@ -136,23 +137,23 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
     const int ag0 = mycol.x < 0 ? -mycol.x : mycol.x, ag1 = mycol.y < 0 ? -mycol.y : mycol.y;
     const T s0 = mycol.x < 0 ? (T)-1 : (T)1, s1 = mycol.y < 0 ? (T)-1 : (T)1;
     for (int ab = abeg; ab < aend; ab += KA) {
+      // coalesced copy of the chunk's table rows (contiguous in global memory)
+      const int nrow = min(KA, aend - ab);
+      const CT *src = tab + (int64_t)ab * L;
+      for (int v = threadIdx.x; v < KA * L; v += blockDim.x)
+        sRow[v] = (v < nrow * L) ? src[v] : cmk<T>((T)0, (T)0);
+      __syncthreads();
+      // column t of X = E0 E1 for every atom of the chunk
 #pragma unroll 4
       for (int la = 0; la < KA; la++) {
-        const int a = ab + la;
         CT x = cmk<T>((T)0, (T)0);
-        if (a < aend && mycol.z >= 0) {
-          const CT *row = tab + (int64_t)a * L;
-          CT e0 = row[ag0], e1 = row[G0 + 1 + ag1];
+        if (mycol.z >= 0) {
+          CT e0 = sRow[la * L + ag0], e1 = sRow[la * L + G0 + 1 + ag1];
           e0.y *= s0;
           e1.y *= s1;
           x = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
         }
         sX[la][threadIdx.x] = x;
-      }
-      for (int v = threadIdx.x; v < KA * EW_MS; v += blockDim.x) {
-        const int la = v / EW_MS, m = v % EW_MS;
-        const int a = ab + la, mm = mb + m;
-        sY[la][m] = (a < aend && mm <= G2) ? tab[(int64_t)a * L + G0 + G1 + 2 + mm] : cmk<T>((T)0, (T)0);
       }
       __syncthreads();
 #pragma unroll 2
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           if (j < nj) {
-            const CT y = sY[la][w + 4 * j];
+            const CT y = sRow[la * L + G0 + G1 + 2 + mb + w + 4 * j];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
               ar[i][j] += x[i].x * y.x - x[i].y * y.y;
@@ -547,7 +548,9 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     int nch = (int)((n + ATB - 1) / ATB);
     dim3 grid(nstile, nch, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
-    k_sfac<T, TA><<<grid, 128, 0, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
+    const size_t ssm = (size_t)SfacCfg<T>::KA * (EW_SC + L) * sizeof(CT);
+    YG_CUDA(cudaFuncSetAttribute(k_sfac<T, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    k_sfac<T, TA><<<grid, 128, ssm, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
                                                  (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
     k_sfac_reduce<TA><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(

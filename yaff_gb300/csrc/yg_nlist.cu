@@ -198,6 +198,7 @@ struct BuildArgs {
   double rc2;
   float lo, hi;     // FP32 guard band on d^2
   int fast;
+  int filter;       // nlow/nhigh restrict the pairs
 };
 
 // Exact replay of the reference's decision for candidate (oi -> oj) whose
@@ -243,7 +244,13 @@ __device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, 
   return exact_norm2(d) < A.rc2;
 }
 
-// One warp per sorted atom; lanes sweep the candidates of each stencil cell.
+#define YG_RUN_MAX 8   // cells per contiguous x run of the stencil
+
+// One warp per sorted atom.  Every (o1, o2) row of the stencil is swept as
+// runs of x-consecutive cells that share one periodic image; the atoms of a
+// run are contiguous in sorted order, so lanes walk them in full 32-wide
+// chunks and recover each candidate's x offset from the cell boundaries of
+// the run (kept in registers).
 __global__ void __launch_bounds__(256) k_build(BuildArgs A) {
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -251,67 +258,86 @@ __global__ void __launch_bounds__(256) k_build(BuildArgs A) {
   const int oi = A.sorted[i];
   const float4 xi = A.x32[i];
   const int cid = A.cell_of[oi];
-  const int ci[3] = {cid % A.grid.n[0], (cid / A.grid.n[0]) % A.grid.n[1], cid / (A.grid.n[0] * A.grid.n[1])};
+  const int N0 = A.grid.n[0], N1 = A.grid.n[1], N2 = A.grid.n[2];
+  const int ci[3] = {cid % N0, (cid / N0) % N1, cid / (N0 * N1)};
   const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
+  const bool need_oj = A.filter || A.estart != nullptr || !A.fast;
   int64_t base = 0;
   int nexact = 0;
   uint2 *out = A.nbr + i * A.cap;
-  const int w0 = 2 * A.grid.k[0] + 1, w1 = 2 * A.grid.k[1] + 1;
+  const int K0 = A.grid.k[0];
+  const int w0 = 2 * K0 + 1, w1 = 2 * A.grid.k[1] + 1;
   for (int o2 = -A.grid.k[2]; o2 <= A.grid.k[2]; o2++) {
-    int u2 = ci[2] + o2;
-    int n2 = floordiv(u2, A.grid.n[2]);
-    int c2 = u2 - n2 * A.grid.n[2];
+    const int u2 = ci[2] + o2;
+    const int n2 = floordiv(u2, N2);
+    const int c2 = u2 - n2 * N2;
     for (int o1 = -A.grid.k[1]; o1 <= A.grid.k[1]; o1++) {
-      int u1 = ci[1] + o1;
-      int n1 = floordiv(u1, A.grid.n[1]);
-      int c1 = u1 - n1 * A.grid.n[1];
-      for (int o0 = -A.grid.k[0]; o0 <= A.grid.k[0]; o0++) {
-        int u0 = ci[0] + o0;
-        int n0 = floordiv(u0, A.grid.n[0]);
-        int c0 = u0 - n0 * A.grid.n[0];
-        int cell = c0 + A.grid.n[0] * (c1 + A.grid.n[1] * c2);
-        int oidx = (o0 + A.grid.k[0]) + w0 * ((o1 + A.grid.k[1]) + w1 * (o2 + A.grid.k[2]));
-        float4 sh = A.shift32[oidx];
-        bool zero_off = (o0 == 0 && o1 == 0 && o2 == 0);
-        int s0 = A.cell_start[cell], s1 = A.cell_start[cell + 1];
+      const int u1 = ci[1] + o1;
+      const int n1 = floordiv(u1, N1);
+      const int c1 = u1 - n1 * N1;
+      const int rowcell = N0 * (c1 + N1 * c2);
+      const int orow = w0 * ((o1 + A.grid.k[1]) + w1 * (o2 + A.grid.k[2]));
+      for (int ox = -K0; ox <= K0;) {
+        const int u0 = ci[0] + ox;
+        const int n0 = floordiv(u0, N0);
+        const int c0 = u0 - n0 * N0;
+        int len = min(min(K0 - ox + 1, N0 - c0), YG_RUN_MAX);
+        int bnd[YG_RUN_MAX];
+#pragma unroll
+        for (int t = 0; t < YG_RUN_MAX; t++) bnd[t] = (t < len) ? A.cell_start[rowcell + c0 + t + 1] : 0x7fffffff;
+        const int s0 = A.cell_start[rowcell + c0], s1 = A.cell_start[rowcell + c0 + len];
         for (int jb = s0; jb < s1; jb += 32) {
-          int j = jb + lane;
-          int in = 0, central = 1, oj = -1;
-          if (j < s1 && !(zero_off && j == i)) {
-            oj = A.sorted[j];
-            int a = max(oi, oj), b = min(oi, oj);
-            bool keep = (a >= A.nlow && b < A.nhigh) || (b >= A.nlow && a < A.nhigh);
+          const int j = jb + lane;
+          int in = 0, central = 1, oj = -1, oidx = 0;
+          if (j < s1) {
+            int t = 0;
+#pragma unroll
+            for (int q = 0; q < YG_RUN_MAX - 1; q++) t += (j >= bnd[q]) ? 1 : 0;
+            const int oxj = ox + t;
+            oidx = (oxj + K0) + orow;
+            const bool self0 = (j == i) && oxj == 0 && o1 == 0 && o2 == 0;
+            bool keep = !self0;
+            if (keep && need_oj) {
+              oj = A.sorted[j];
+              if (A.filter) {
+                const int a = max(oi, oj), b = min(oi, oj);
+                keep = (a >= A.nlow && b < A.nhigh) || (b >= A.nlow && a < A.nhigh);
+              }
+            }
             if (keep) {
-              float4 xj = A.x32[j];
-              float dx = (xj.x - xi.x) + sh.x;
-              float dy = (xj.y - xi.y) + sh.y;
-              float dz = (xj.z - xi.z) + sh.z;
-              float d2 = dx * dx + dy * dy + dz * dz;
+              const float4 xj = A.x32[j];
+              const float4 sh = A.shift32[oidx];
+              const float dx = (xj.x - xi.x) + sh.x;
+              const float dy = (xj.y - xi.y) + sh.y;
+              const float dz = (xj.z - xi.z) + sh.z;
+              const float d2 = dx * dx + dy * dy + dz * dz;
               int decided = 0;
               if (A.fast) {
                 if (d2 < A.lo) { in = 1; decided = 1; }
                 else if (d2 > A.hi) { in = 0; decided = 1; }
               }
               if (!decided) {
-                int t[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1],
-                            n2 + wi[2] - A.wimg[3 * oj + 2]};
-                in = exact_decide(A, oi, oj, t, &central);
+                if (oj < 0) oj = A.sorted[j];
+                int tt[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1],
+                             n2 + wi[2] - A.wimg[3 * oj + 2]};
+                in = exact_decide(A, oi, oj, tt, &central);
                 nexact++;
               }
             }
           }
-          unsigned ball = __ballot_sync(0xffffffffu, in);
+          const unsigned ball = __ballot_sync(0xffffffffu, in);
           if (in) {
-            int code = central ? excl_code(A.estart, A.excl, oi, oj) : 0;
-            int64_t p = base + __popc(ball & ((1u << lane) - 1u));
+            const int code = (central && A.estart) ? excl_code(A.estart, A.excl, oi, oj) : 0;
+            const int64_t p = base + __popc(ball & ((1u << lane) - 1u));
             if (p < A.cap) {
-              unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
-                              (central ? YG_META_CENTRAL : 0u);
+              const unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
+                                    (central ? YG_META_CENTRAL : 0u);
               out[p] = make_uint2((unsigned)j, meta);
             }
           }
           base += __popc(ball);
         }
+        ox += len;
       }
     }
   }
@@ -471,6 +497,7 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.lo = 0.0f;
   A.hi = 0.0f;
   A.fast = 0;
+  A.filter = (ctx->nlow > 0 || ctx->nhigh < ctx->natom) ? 1 : 0;
   return A;
 }
 

@@ -36,6 +36,11 @@ struct PairArgs {
   const float *pp32;
   PairPotDev pot[YG_MAX_POT];
   double scale[5];
+  // FP32 copies of the per-potential constants (rcut, truncation parameter,
+  // alpha, 1/dielectric) and scalings: converting FP64 constants per pair
+  // would run on the FP64 pipe.
+  float fpot[YG_MAX_POT][4];
+  float fscale[5];
   double *gpos[YG_MAX_POT];   // per-potential gradient, orig order (natom*3)
   double *partial;            // per block: NPOT*7 (E, Vxx, Vyy, Vzz, Vxy, Vxz, Vyz)
   int want_grad;
@@ -59,8 +64,8 @@ template <> struct Num<float> {
 // included.  Formulas of yaff/pes/pair_pot.c:277-301 (LJ), :321-352 (MM3),
 // :711-751 (EI) and truncation.c:30-76.
 template <typename T>
-__device__ __forceinline__ void pair_term(const PairPotDev &P, T d, T d2, T pi0, T pi1, T pi2, T pi3,
-                                          T pj0, T pj1, T pj2, T pj3, T qi, T qj, T &v, T &g) {
+__device__ __forceinline__ void pair_term(const PairPotDev &P, T rcT, T parT, T alphaT, T invdT, T d, T d2, T pi0,
+                                          T pi1, T pi2, T pi3, T pj0, T pj1, T pj2, T pj3, T qi, T qj, T &v, T &g) {
   typedef Num<T> M;
   const T two_div_sqrt_pi = (T)1.1283791670955125739;
   if (P.kind == YG_POT_LJ) {
@@ -86,8 +91,8 @@ __device__ __forceinline__ void pair_term(const PairPotDev &P, T d, T d2, T pi0,
       v = eps * ex;
     }
   } else {
-    T qq = qi * qj * (T)P.inv_diel;
-    T alpha = (T)P.alpha;
+    T qq = qi * qj * invdT;
+    T alpha = alphaT;
     T rab2 = pi2 + pj2;
     if (alpha > (T)0) {
       T x = alpha * d;
@@ -113,7 +118,7 @@ __device__ __forceinline__ void pair_term(const PairPotDev &P, T d, T d2, T pi0,
     }
   }
   if (P.tr_kind != YG_TR_NONE && (v != (T)0 || g != (T)0)) {
-    T rc = (T)P.rcut, par = (T)P.tr_par, h, hg;
+    T rc = rcT, par = parT, h, hg;
     if (P.tr_kind == YG_TR_HAMMER) {
       T x = d - rc;
       h = M::exp_(par / x);
@@ -215,19 +220,23 @@ __global__ void __launch_bounds__(256) k_pair(PairArgs A) {
       }
       const T d2 = dx * dx + dy * dy + dz * dz;
       const T d = Num<T>::sqrt_(d2);
-      const T s = (T)A.scale[code];
+      const T s = (MODE == YG_FP64) ? (T)A.scale[code] : (T)A.fscale[code];
       if (s == (T)0) continue;
 #pragma unroll
       for (int p = 0; p < NPOT; p++) {
-        if (!(d < (T)A.pot[p].rcut)) continue;
+        const T rcT = (MODE == YG_FP64) ? (T)A.pot[p].rcut : (T)A.fpot[p][0];
+        if (!(d < rcT)) continue;
         T pj[4];
 #pragma unroll
         for (int k = 0; k < 4; k++)
           pj[k] = (MODE == YG_FP64) ? (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k]
                                     : (T)A.pp32[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
+        const T parT = (MODE == YG_FP64) ? (T)A.pot[p].tr_par : (T)A.fpot[p][1];
+        const T alphaT = (MODE == YG_FP64) ? (T)A.pot[p].alpha : (T)A.fpot[p][2];
+        const T invdT = (MODE == YG_FP64) ? (T)A.pot[p].inv_diel : (T)A.fpot[p][3];
         T v, g;
-        pair_term<T>(A.pot[p], d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0], pj[1], pj[2], pj[3],
-                     qi, qj, v, g);
+        pair_term<T>(A.pot[p], rcT, parT, alphaT, invdT, d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0],
+                     pj[1], pj[2], pj[3], qi, qj, v, g);
         E[p].add((T)0.5 * s * v);
         if (A.want_grad) {
           g *= s;
@@ -381,7 +390,16 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   A.shift32 = ctx->d_shift32;
   A.pp64 = ctx->d_pp64;
   A.pp32 = ctx->d_pp32;
-  for (int k = 0; k < 5; k++) A.scale[k] = ctx->scale_tab[k];
+  for (int k = 0; k < 5; k++) {
+    A.scale[k] = ctx->scale_tab[k];
+    A.fscale[k] = (float)ctx->scale_tab[k];
+  }
+  for (int q = 0; q < npot; q++) {
+    A.fpot[q][0] = (float)A.pot[q].rcut;
+    A.fpot[q][1] = (float)A.pot[q].tr_par;
+    A.fpot[q][2] = (float)A.pot[q].alpha;
+    A.fpot[q][3] = (float)A.pot[q].inv_diel;
+  }
   for (int p = 0; p < YG_MAX_POT; p++) A.gpos[p] = nullptr;
   for (int q = 0; q < npot; q++) A.gpos[q] = ctx->d_part_gpos + (size_t)(YG_PART_PAIR0 + slots[q]) * N * 3;
   A.want_grad = want_grad;
