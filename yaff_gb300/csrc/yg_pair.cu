@@ -139,6 +139,71 @@ __device__ __forceinline__ void pair_term(const PairPotDev &P, T rcT, T parT, T 
   }
 }
 
+// erfc(x) for x >= 0 in FP32 from the Chebyshev-fitted form of Numerical
+// Recipes (erfcc: t exp(-x^2 + P(t)), t = 1/(1 + x/2), fractional error below
+// 1.2e-7 everywhere), which keeps the relative accuracy of the tail where the
+// real-space Ewald term is evaluated.
+__device__ __forceinline__ float erfc_cheb(float x) {
+  const float t = 1.0f / (1.0f + 0.5f * x);
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  p = fmaf(p, t, -1.26551223f);
+  return t * expf(fmaf(-x, x, p));
+}
+
+// FP32 evaluation of one pair (mixed modes): one reciprocal square root per
+// pair instead of divisions.  Same formulas as pair_term; Gaussian charges,
+// bare Coulomb and truncation fall back to pair_term.
+__device__ __forceinline__ void pair_term_f32(const PairPotDev &P, float rcT, float parT, float alphaT, float invdT,
+                                              float d, float d2, float inv_d, float pi0, float pi1, float pi2,
+                                              float pi3, float pj0, float pj1, float pj2, float pj3, float qi,
+                                              float qj, float &v, float &g) {
+  const float inv_d2 = inv_d * inv_d;
+  if (P.tr_kind == YG_TR_NONE) {
+    if (P.kind == YG_POT_LJ) {
+      const float sig = 0.5f * (pi0 + pj0);
+      const float eps = pi1 * pj1;
+      const float s2 = sig * sig * inv_d2;
+      const float x = s2 * s2 * s2;
+      g = 24.0f * eps * inv_d2 * x * (1.0f - 2.0f * x);
+      v = 4.0f * eps * (x * (x - 1.0f));
+      return;
+    }
+    if (P.kind == YG_POT_MM3) {
+      const float sig = pi0 + pj0;
+      const float eps = pi1 * pj1;
+      const float inv_sig = 1.0f / sig;
+      const float ex = 1.84e5f * expf(-12.0f * d * inv_sig);
+      if (pi3 + pj3 == 0.0f) {
+        const float s2 = sig * sig * inv_d2;
+        const float x = 2.25f * s2 * s2 * s2;
+        g = eps * inv_d * (-12.0f * inv_sig * ex + 6.0f * inv_d * x);
+        v = eps * (ex - x);
+      } else {
+        g = eps * inv_d * (-12.0f * inv_sig * ex);
+        v = eps * ex;
+      }
+      return;
+    }
+    if (alphaT > 0.0f && pi2 + pj2 == 0.0f) {
+      const float qq = qi * qj * invdT;
+      const float x = alphaT * d;
+      const float e = expf(-x * x);
+      v = qq * erfc_cheb(x) * inv_d;
+      g = (-1.1283791670955126f * alphaT * e * qq - v) * inv_d2;
+      return;
+    }
+  }
+  pair_term<float>(P, rcT, parT, alphaT, invdT, d, d2, pi0, pi1, pi2, pi3, pj0, pj1, pj2, pj3, qi, qj, v, g);
+}
+
 // Accumulator: plain (FP64 or FP32) or Kahan-compensated FP32.
 template <typename T, bool KAHAN> struct Acc {
   T s;
@@ -219,24 +284,42 @@ __global__ void __launch_bounds__(256) k_pair(PairArgs A) {
         qj = (T)xj.w;
       }
       const T d2 = dx * dx + dy * dy + dz * dz;
-      const T d = Num<T>::sqrt_(d2);
+      T d, inv_d = (T)0;
+      if (MODE == YG_FP64) {
+        d = Num<T>::sqrt_(d2);
+      } else {
+        inv_d = (T)rsqrtf((float)d2);
+        d = d2 * inv_d;
+      }
       const T s = (MODE == YG_FP64) ? (T)A.scale[code] : (T)A.fscale[code];
       if (s == (T)0) continue;
 #pragma unroll
       for (int p = 0; p < NPOT; p++) {
         const T rcT = (MODE == YG_FP64) ? (T)A.pot[p].rcut : (T)A.fpot[p][0];
         if (!(d < rcT)) continue;
-        T pj[4];
+        T pj[4] = {(T)0, (T)0, (T)0, (T)0};
+        if (MODE == YG_FP64) {
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-          pj[k] = (MODE == YG_FP64) ? (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k]
-                                    : (T)A.pp32[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
+          for (int k = 0; k < 4; k++) pj[k] = (T)A.pp64[(int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
+        } else if (A.pot[p].kind != YG_POT_EI || A.pot[p].has_radii) {
+          const float4 q4 = *reinterpret_cast<const float4 *>(A.pp32 + (int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col);
+          pj[0] = (T)q4.x; pj[1] = (T)q4.y; pj[2] = (T)q4.z; pj[3] = (T)q4.w;
+        }
         const T parT = (MODE == YG_FP64) ? (T)A.pot[p].tr_par : (T)A.fpot[p][1];
         const T alphaT = (MODE == YG_FP64) ? (T)A.pot[p].alpha : (T)A.fpot[p][2];
         const T invdT = (MODE == YG_FP64) ? (T)A.pot[p].inv_diel : (T)A.fpot[p][3];
         T v, g;
-        pair_term<T>(A.pot[p], rcT, parT, alphaT, invdT, d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0],
-                     pj[1], pj[2], pj[3], qi, qj, v, g);
+        if (MODE == YG_FP64) {
+          pair_term<T>(A.pot[p], rcT, parT, alphaT, invdT, d, d2, pi[p][0], pi[p][1], pi[p][2], pi[p][3], pj[0],
+                       pj[1], pj[2], pj[3], qi, qj, v, g);
+        } else {
+          float fv, fg;
+          pair_term_f32(A.pot[p], (float)rcT, (float)parT, (float)alphaT, (float)invdT, (float)d, (float)d2,
+                        (float)inv_d, (float)pi[p][0], (float)pi[p][1], (float)pi[p][2], (float)pi[p][3],
+                        (float)pj[0], (float)pj[1], (float)pj[2], (float)pj[3], (float)qi, (float)qj, fv, fg);
+          v = (T)fv;
+          g = (T)fg;
+        }
         E[p].add((T)0.5 * s * v);
         if (A.want_grad) {
           g *= s;
