@@ -49,41 +49,47 @@ template <typename T> __device__ __forceinline__ typename C2<T>::t cmk(T a, T b)
 
 // Per-atom phase tables: for every atom L = (G0+1)+(G1+1)+(G2+1) complex
 // values, E0[0..G0], E1[0..G1], q*E2[0..G2].
+// One thread per (atom, axis): the fractional coordinate s is formed once in
+// FP64; every entry's argument g*s mod 1 is then reduced exactly -- in FP64
+// for the plain form, and for the FP32 forms from the split s = s_hi + s_lo
+// with the exact product error fmaf(g, s_hi, -g*s_hi) -- before the FP32 or
+// FP64 sine/cosine.
 template <typename T>
 __global__ void k_tables(const double *__restrict__ pos, const double *__restrict__ charge, int64_t natom,
                          CellGeom cell, int G0, int G1, int G2, typename C2<T>::t *__restrict__ tab) {
   const int L = G0 + G1 + G2 + 3;
-  int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx >= natom * L) return;
-  int64_t a = idx / L;
-  int e = (int)(idx - a * L);
-  int axis, g;
-  if (e <= G0) { axis = 0; g = e; }
-  else if (e <= G0 + 1 + G1) { axis = 1; g = e - G0 - 1; }
-  else { axis = 2; g = e - G0 - G1 - 2; }
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= natom * 3) return;
+  const int64_t a = idx / 3;
+  const int axis = (int)(idx - a * 3);
+  const int gmax = axis == 0 ? G0 : (axis == 1 ? G1 : G2);
+  const int base = axis == 0 ? 0 : (axis == 1 ? G0 + 1 : G0 + G1 + 2);
   const double *gv = cell.gv + 3 * axis;
   double s = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
   s -= floor(s);
-  double x = (double)g * s;
-  x -= rint(x);            // x in [-0.5, 0.5]
-  T sn, cs;
+  const T q = (axis == 2) ? (T)charge[a] : (T)1;
+  typename C2<T>::t *out = tab + a * L + base;
   if (sizeof(T) == 8) {
-    double dsn, dcs;
-    sincospi(2.0 * x, &dsn, &dcs);
-    sn = (T)dsn;
-    cs = (T)dcs;
+    for (int g = 0; g <= gmax; g++) {
+      double x = (double)g * s;
+      x -= rint(x);
+      double dsn, dcs;
+      sincospi(2.0 * x, &dsn, &dcs);
+      out[g] = cmk<T>((T)dcs * q, (T)dsn * q);
+    }
   } else {
-    float fsn, fcs;
-    sincospif(2.0f * (float)x, &fsn, &fcs);
-    sn = (T)fsn;
-    cs = (T)fcs;
+    const float s_hi = (float)s;
+    const float s_lo = (float)(s - (double)s_hi);
+    for (int g = 0; g <= gmax; g++) {
+      const float fg = (float)g;
+      const float p = fg * s_hi;
+      const float e = fmaf(fg, s_hi, -p);
+      const float x = (p - rintf(p)) + fmaf(fg, s_lo, e);
+      float fsn, fcs;
+      sincospif(2.0f * x, &fsn, &fcs);
+      out[g] = cmk<T>((T)fcs * q, (T)fsn * q);
+    }
   }
-  if (axis == 2) {
-    T q = (T)charge[a];
-    cs *= q;
-    sn *= q;
-  }
-  tab[idx] = cmk<T>(cs, sn);
 }
 
 template <typename T>
@@ -103,10 +109,11 @@ template <> struct SfacCfg<float> { enum { KA = 32, ATB = 256 }; };
 template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
 
 // S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
-// Lane l owns columns 2l, 2l+1, 64+2l, 64+2l+1 of the tile (contiguous
-// 16-byte shared loads); warp w owns m = w + 4j, j < 8, of the slab, so the
-// m values beyond the tile's extent are skipped warp-uniformly.  Thread t
-// stages column t of X for the chunk's atoms.
+// The table rows of KA atoms are staged in shared memory with coalesced
+// copies.  Lane l owns columns l, l+32, l+64, l+96 of the tile and forms
+// X = E0 E1 for them from the staged rows; warp w owns m = w + 4j, j < 8,
+// of the slab (broadcast loads of Y), so m values beyond the tile's extent
+// are skipped warp-uniformly.
 template <typename T, typename TA>
 __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restrict__ tab, int a0, int a1, int G0,
                                               int G1, int G2, const int4 *__restrict__ cols,
@@ -115,12 +122,10 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   const int KA = SfacCfg<T>::KA, ATB = SfacCfg<T>::ATB;
   const int L = G0 + G1 + G2 + 3;
   extern __shared__ __align__(16) unsigned char sfac_smem[];
-  CT (*sX)[EW_SC] = reinterpret_cast<CT (*)[EW_SC]>(sfac_smem);   // [KA][EW_SC]
-  CT *sRow = reinterpret_cast<CT *>(sfac_smem) + KA * EW_SC;      // [KA][L] table rows
+  CT *sRow = reinterpret_cast<CT *>(sfac_smem);      // [KA][L] table rows
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x, slab = blockIdx.z;
   const int mb = slab * EW_MS;
-  const int4 mycol = cols[tile * EW_SC + threadIdx.x];
   const int Mt = cols[tile * EW_SC].w + 1 - mb;
   const int nj = (Mt > w) ? min(8, (Mt - w + 3) / 4) : 0;
   const int abeg = a0 + blockIdx.y * ATB;
@@ -134,8 +139,18 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
       ai[i][j] = (T)0;
     }
   if (Mt > 0) {
-    const int ag0 = mycol.x < 0 ? -mycol.x : mycol.x, ag1 = mycol.y < 0 ? -mycol.y : mycol.y;
-    const T s0 = mycol.x < 0 ? (T)-1 : (T)1, s1 = mycol.y < 0 ? (T)-1 : (T)1;
+    int o0[4], o1[4];
+    T s0[4], s1[4], ok[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int4 col = cols[tile * EW_SC + lane + 32 * i];
+      o0[i] = col.x < 0 ? -col.x : col.x;
+      o1[i] = G0 + 1 + (col.y < 0 ? -col.y : col.y);
+      s0[i] = col.x < 0 ? (T)-1 : (T)1;
+      s1[i] = col.y < 0 ? (T)-1 : (T)1;
+      ok[i] = col.z >= 0 ? (T)1 : (T)0;
+    }
+    const int yb = G0 + G1 + 2 + mb + w;
     for (int ab = abeg; ab < aend; ab += KA) {
       // coalesced copy of the chunk's table rows (contiguous in global memory)
       const int nrow = min(KA, aend - ab);
@@ -143,30 +158,22 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
       for (int v = threadIdx.x; v < KA * L; v += blockDim.x)
         sRow[v] = (v < nrow * L) ? src[v] : cmk<T>((T)0, (T)0);
       __syncthreads();
-      // column t of X = E0 E1 for every atom of the chunk
-#pragma unroll 4
-      for (int la = 0; la < KA; la++) {
-        CT x = cmk<T>((T)0, (T)0);
-        if (mycol.z >= 0) {
-          CT e0 = sRow[la * L + ag0], e1 = sRow[la * L + G0 + 1 + ag1];
-          e0.y *= s0;
-          e1.y *= s1;
-          x = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
-        }
-        sX[la][threadIdx.x] = x;
-      }
-      __syncthreads();
 #pragma unroll 2
       for (int la = 0; la < KA; la++) {
+        const CT *row = sRow + la * L;
         CT x[4];
-        x[0] = sX[la][2 * lane];
-        x[1] = sX[la][2 * lane + 1];
-        x[2] = sX[la][64 + 2 * lane];
-        x[3] = sX[la][64 + 2 * lane + 1];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          CT e0 = row[o0[i]], e1 = row[o1[i]];
+          e0.x *= ok[i];
+          e0.y *= s0[i] * ok[i];
+          e1.y *= s1[i];
+          x[i] = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
+        }
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           if (j < nj) {
-            const CT y = sRow[la * L + G0 + G1 + 2 + mb + w + 4 * j];
+            const CT y = row[yb + 4 * j];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
               ar[i][j] += x[i].x * y.x - x[i].y * y.y;
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   const int64_t base = (((int64_t)blockIdx.y * nstile + tile) * nslab + slab) * (EW_SC * EW_MS);
 #pragma unroll
   for (int i = 0; i < 4; i++) {
-    const int c = 2 * lane + (i & 1) + 64 * (i >> 1);
+    const int c = lane + 32 * i;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       CA v;
@@ -522,7 +529,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   size_t tb = (size_t)N * L * sizeof(CT);
   if ((rc = yg_ensure(&ctx->d_ew_tab, &ctx->ew_bytes_tab, tb))) return rc;
   CT *tab = (CT *)ctx->d_ew_tab;
-  k_tables<T><<<yg_blocks(N * L, 256), 256, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2, tab);
+  k_tables<T><<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2, tab);
   YG_LAUNCH_CHECK(ctx, "k_tables");
   // atom groups: 0 = [nlow, nhigh) (always), 1 = [0, nlow), 2 = [nhigh, N)
   int64_t lo = ctx->ew_nlow, hi = ctx->ew_nhigh;
@@ -548,7 +555,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     int nch = (int)((n + ATB - 1) / ATB);
     dim3 grid(nstile, nch, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
-    const size_t ssm = (size_t)SfacCfg<T>::KA * (EW_SC + L) * sizeof(CT);
+    const size_t ssm = (size_t)SfacCfg<T>::KA * L * sizeof(CT);
     YG_CUDA(cudaFuncSetAttribute(k_sfac<T, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
     k_sfac<T, TA><<<grid, 128, ssm, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
                                                  (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab);

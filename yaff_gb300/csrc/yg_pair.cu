@@ -210,6 +210,8 @@ template <typename T, bool KAHAN> struct Acc {
   __device__ __forceinline__ void init() { s = (T)0; }
   __device__ __forceinline__ void add(T x) { s += x; }
   __device__ __forceinline__ double value() const { return (double)s; }
+  __device__ __forceinline__ float hi() const { return (float)s; }
+  __device__ __forceinline__ float lo() const { return 0.0f; }
 };
 template <> struct Acc<float, true> {
   float s, c;
@@ -221,12 +223,33 @@ template <> struct Acc<float, true> {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ float hi() const { return s; }
+  __device__ __forceinline__ float lo() const { return -c; }
 };
 
 template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// (h, l) += (xh, xl) with an error-free TwoSum of the high parts.
+__device__ __forceinline__ void two_sum_acc(float &h, float &l, float xh, float xl) {
+  const float s = h + xh;
+  const float bb = s - h;
+  const float e = (h - (s - bb)) + (xh - bb);
+  l = l + xl + e;
+  h = s;
+}
+
+// Butterfly warp sum of (hi, lo) pairs; every lane ends with the total.
+__device__ __forceinline__ void warp_twosum(float &h, float &l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+    two_sum_acc(h, l, oh, ol);
+  }
 }
 
 template <int MODE, int NPOT>
@@ -337,40 +360,92 @@ __global__ void __launch_bounds__(256) k_pair(PairArgs A) {
       }
     }
   }
-  // warp reductions (FP64 unless Kahan mode, which stays FP32)
-  double part[NPOT * 7];
-#pragma unroll
-  for (int p = 0; p < NPOT; p++) {
-    part[7 * p] = E[p].value();
-#pragma unroll
-    for (int k = 0; k < 6; k++) part[7 * p + 1 + k] = V[p][k].value();
-  }
-#pragma unroll
-  for (int v = 0; v < NPOT * 7; v++) {
-    if (kahan) part[v] = (double)warp_sum<float>((float)part[v]);
-    else part[v] = warp_sum<double>(part[v]);
-  }
-  if (A.want_grad && i < A.natom) {
-    const int oi = A.sorted[i];
+  if (MODE == YG_FP64) {
+    // FP64 warp, block and grid reductions
+    double part[NPOT * 7];
 #pragma unroll
     for (int p = 0; p < NPOT; p++) {
+      part[7 * p] = E[p].value();
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        double gv = kahan ? (double)warp_sum<float>((float)G[p][k].value()) : warp_sum<double>(G[p][k].value());
-        if (lane == 0) A.gpos[p][3 * (int64_t)oi + k] = gv;
+      for (int k = 0; k < 6; k++) part[7 * p + 1 + k] = V[p][k].value();
+    }
+#pragma unroll
+    for (int v = 0; v < NPOT * 7; v++) part[v] = warp_sum<double>(part[v]);
+    if (A.want_grad && i < A.natom) {
+      const int oi = A.sorted[i];
+#pragma unroll
+      for (int p = 0; p < NPOT; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const double gv = warp_sum<double>(G[p][k].value());
+          if (lane == 0) A.gpos[p][3 * (int64_t)oi + k] = gv;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int v = 0; v < NPOT * 7; v++) red[wid][v] = part[v];
+    }
+    __syncthreads();
+    if (threadIdx.x < NPOT * 7) {
+      double s = 0.0;
+      const int nw = blockDim.x >> 5;
+      for (int w = 0; w < nw; w++) s += red[w][threadIdx.x];
+      A.partial[(int64_t)blockIdx.x * NPOT * 7 + threadIdx.x] = s;
+    }
+  } else {
+    // Mixed modes: the FP32 lane partials are combined with error-free
+    // TwoSum steps into (hi, lo) FP32 pairs (about twice FP32 precision);
+    // FP64 is used only where a pair becomes an FP64 result, on the few
+    // lanes that store it.  A 32-lane FP64 instruction costs the GB300 FP64
+    // pipe tens of cycles, so per-warp FP64 reductions would dominate.
+    __shared__ float2 redf[8][NPOT * 7];
+    float hi[NPOT * 7], lo[NPOT * 7];
+#pragma unroll
+    for (int p = 0; p < NPOT; p++) {
+      hi[7 * p] = E[p].hi();
+      lo[7 * p] = E[p].lo();
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        hi[7 * p + 1 + k] = V[p][k].hi();
+        lo[7 * p + 1 + k] = V[p][k].lo();
       }
     }
-  }
-  if (lane == 0) {
 #pragma unroll
-    for (int v = 0; v < NPOT * 7; v++) red[wid][v] = part[v];
-  }
-  __syncthreads();
-  if (threadIdx.x < NPOT * 7) {
-    double s = 0.0;
-    const int nw = blockDim.x >> 5;
-    for (int w = 0; w < nw; w++) s += red[w][threadIdx.x];
-    A.partial[(int64_t)blockIdx.x * NPOT * 7 + threadIdx.x] = s;
+    for (int v = 0; v < NPOT * 7; v++) warp_twosum(hi[v], lo[v]);
+    if (A.want_grad && i < A.natom) {
+      const int oi = A.sorted[i];
+      float gh[NPOT * 3], gl[NPOT * 3];
+#pragma unroll
+      for (int p = 0; p < NPOT; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          gh[3 * p + k] = G[p][k].hi();
+          gl[3 * p + k] = G[p][k].lo();
+          warp_twosum(gh[3 * p + k], gl[3 * p + k]);
+        }
+      float h = gh[0], l = gl[0];
+#pragma unroll
+      for (int c = 1; c < NPOT * 3; c++)
+        if (lane == c) {
+          h = gh[c];
+          l = gl[c];
+        }
+      if (lane < NPOT * 3) A.gpos[lane / 3][3 * (int64_t)oi + lane % 3] = (double)h + (double)l;
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int v = 0; v < NPOT * 7; v++) redf[wid][v] = make_float2(hi[v], lo[v]);
+    }
+    __syncthreads();
+    if (threadIdx.x < NPOT * 7) {
+      float h = 0.0f, l = 0.0f;
+      const int nw = blockDim.x >> 5;
+      for (int w = 0; w < nw; w++) {
+        const float2 x = redf[w][threadIdx.x];
+        two_sum_acc(h, l, x.x, x.y);
+      }
+      A.partial[(int64_t)blockIdx.x * NPOT * 7 + threadIdx.x] = (double)h + (double)l;
+    }
   }
 }
 
