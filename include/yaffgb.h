@@ -181,6 +181,29 @@ int yg_sync(yg_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 int64_t yg_launch_count(yg_ctx *ctx);
 
+/* Ewald correction for callers that cannot let the library allocate device
+ * memory (an engine that owns all device memory through its own pool, or a
+ * step loop that must not block on an allocation).  No counterpart in the
+ * reference.  Computes what yg_ewald_corr computes -- the self term over
+ * [nlow, nhigh) and the excluded-pair correction of the scaling rows
+ * (stab_a > stab_b, stab_scale) -- from caller-owned DEVICE buffers: pos
+ * (natom x 3), charges (natom), stab_* (nstab), and writes the energy
+ * (1 double), the gradient gpos (natom x 3, overwritten; may be NULL) and
+ * the virial vtens (9 doubles), all device memory, on `stream`.  rvecs and
+ * gvecs are host 3x3 arrays.  Its only scratch is a fixed 229 KB device array
+ * inside the library, so nstab is limited to YG_NOALLOC_MAX_ROWS (larger
+ * tables return YG_ERR_CAPACITY).  The first call on a device looks up that
+ * array's device address; make it before capturing the stream in a graph.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialized by the caller. */
+#define YG_NOALLOC_MAX_ROWS (1 << 20)
+int yg_ewald_corr_noalloc(const double *pos, const double *charges, int64_t natom,
+                          const int64_t *stab_a, const int64_t *stab_b,
+                          const double *stab_scale, int64_t nstab,
+                          const double *rvecs, const double *gvecs, double volume,
+                          double alpha, double dielectric, int64_t nlow, int64_t nhigh,
+                          double *energy, double *gpos, double *vtens, void *stream);
+
 /* Measurement utility (no reference counterpart): FMA-chain throughput of
  * the FP32 (fp64 == 0) or FP64 CUDA-core pipe in TFLOP/s (FMA = 2 flops), the
  * roofline denominator of the pair and Ewald kernels.  Negative on error. */

@@ -69,6 +69,8 @@ SIGNATURES = {
     'yg_sync': (_I, [_P]),
     'yg_launch_count': (_I64, [_P]),
     'yg_probe_peak': (_D, [_I, _P]),
+    'yg_ewald_corr_noalloc': (_I, [_P, _P, _I64, _P, _P, _P, _I64, _P, _P, _D, _D, _D, _I64, _I64, _P, _P, _P,
+                                   _P]),
 }
 
 _lib = None
