@@ -123,6 +123,7 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
   rc |= yg_alloc((void **)&c->d_org, N * 3 * sizeof(double));
   rc |= yg_alloc((void **)&c->d_x64, N * sizeof(double4_32a));
   rc |= yg_alloc((void **)&c->d_x32, N * sizeof(float4));
+  rc |= yg_alloc((void **)&c->d_xb, N * sizeof(float4));
   rc |= yg_alloc((void **)&c->d_ncount, N * sizeof(int));
   rc |= yg_alloc((void **)&c->d_status, YG_ST_NWORDS * sizeof(int));
   rc |= yg_alloc((void **)&c->d_part_ev, YG_NPART * 10 * sizeof(double));
@@ -154,7 +155,7 @@ int yg_destroy(yg_ctx *c) {
   if (!c) return YG_OK;
   cudaStreamSynchronize(c->stream);
   void *bufs[] = {c->d_pos, c->d_pos_build, c->d_charge, c->d_cell_of, c->d_wimg, c->d_sorted, c->d_rank,
-                  c->d_cell_start, c->d_cell_fill, c->d_org, c->d_x64, c->d_x32, c->d_shift64, c->d_shift32,
+                  c->d_cell_start, c->d_cell_fill, c->d_org, c->d_x64, c->d_x32, c->d_xb, c->d_shift64, c->d_shift32,
                   c->d_nbr, c->d_ncount, c->d_status, c->d_excl_start, c->d_excl, c->d_stab_ab, c->d_stab_scale,
                   c->d_pp_src, c->d_pp64, c->d_pp32, c->d_ew_pref, c->d_ew_tiles, c->d_ew_tab, c->d_ew_Spart,
                   c->d_ew_S, c->d_ew_W, c->d_ew_gpart, c->d_ew_red, c->d_delta_ij, c->d_delta, c->d_ic,

@@ -215,11 +215,31 @@ __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int 
   const int4 col = cols[tile * EW_SC + c];
   const int mm = slab * EW_MS + m;
   if (col.z < 0 || mm > col.w) return;
-  double re = 0.0, im = 0.0;
-  for (int ch = 0; ch < nchunk; ch++) {
-    const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
-    re += (double)v.x;
-    im += (double)v.y;
+  double re, im;
+  if (sizeof(TA) == 8) {
+    re = 0.0;
+    im = 0.0;
+    for (int ch = 0; ch < nchunk; ch++) {
+      const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
+      re += (double)v.x;
+      im += (double)v.y;
+    }
+  } else {
+    // FP32 partials: error-free TwoSum accumulation in (hi, lo) pairs, one
+    // conversion to FP64 at the end (the FP64 pipe is the slow one)
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int ch = 0; ch < nchunk; ch++) {
+      const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
+      float s = rh + (float)v.x, bb = s - rh;
+      rl += (rh - (s - bb)) + ((float)v.x - bb);
+      rh = s;
+      s = ih + (float)v.y;
+      bb = s - ih;
+      il += (ih - (s - bb)) + ((float)v.y - bb);
+      ih = s;
+    }
+    re = (double)rh + (double)rl;
+    im = (double)ih + (double)il;
   }
   S[2 * ((int64_t)col.z * nm + mm)] = re;
   S[2 * ((int64_t)col.z * nm + mm) + 1] = im;

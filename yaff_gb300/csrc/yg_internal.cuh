@@ -96,6 +96,7 @@ struct yg_ctx {
   double *d_org = nullptr;        // sorted*3 cell origin of each atom (FP64)
   double4_32a *d_x64 = nullptr;       // sorted: local coordinate (x,y,z) and charge
   float4 *d_x32 = nullptr;        // sorted: same in FP32
+  float4 *d_xb = nullptr;         // sorted: FP32 coordinates, w = cell x index (build)
   double *d_shift64 = nullptr;    // noff*3 stencil shift vectors
   float4 *d_shift32 = nullptr;    // noff
   int cap_sorted = 0;             // allocated cell-list capacity (cells)

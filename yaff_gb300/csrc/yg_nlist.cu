@@ -108,20 +108,49 @@ __global__ void k_scatter(const int *__restrict__ cell_of, int64_t natom, int *_
   sorted[slot] = (int)a;
 }
 
-// Orders the atoms of every cell by index (cells hold tens of atoms).
+// Orders the atoms of every cell by index.  One warp per cell: each lane
+// holds up to 4 entries and computes their ranks by comparing with all
+// entries of the cell through shuffles (indices are distinct), then writes
+// them to their final slots.  Cells with more than 128 atoms (pathological
+// densities) fall back to an insertion sort by lane 0.
 __global__ void k_sort_cells(const int *__restrict__ start, int ncell, int *__restrict__ sorted) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (c >= ncell) return;
-  int s0 = start[c], s1 = start[c + 1];
-  for (int i = s0 + 1; i < s1; i++) {
-    int v = sorted[i];
-    int j = i - 1;
-    while (j >= s0 && sorted[j] > v) {
-      sorted[j + 1] = sorted[j];
-      j--;
+  const int s0 = start[c], s1 = start[c + 1];
+  const int n = s1 - s0;
+  if (n <= 1) return;
+  if (n > 128) {
+    if (lane == 0) {
+      for (int i = s0 + 1; i < s1; i++) {
+        int v = sorted[i];
+        int j = i - 1;
+        while (j >= s0 && sorted[j] > v) {
+          sorted[j + 1] = sorted[j];
+          j--;
+        }
+        sorted[j + 1] = v;
+      }
     }
-    sorted[j + 1] = v;
+    return;
   }
+  int v[4], rank[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    v[q] = (lane + 32 * q < n) ? sorted[s0 + lane + 32 * q] : 0x7fffffff;
+    rank[q] = 0;
+  }
+  for (int src = 0; src < n; src++) {
+    const int qs = src >> 5;
+    const int mine = qs == 0 ? v[0] : (qs == 1 ? v[1] : (qs == 2 ? v[2] : v[3]));
+    const int w = __shfl_sync(0xffffffffu, mine, src & 31);
+#pragma unroll
+    for (int q = 0; q < 4; q++) rank[q] += (w < v[q]) ? 1 : 0;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (lane + 32 * q < n) sorted[s0 + rank[q]] = v[q];
 }
 
 // Cell origin (FP64) of every sorted atom and the orig -> sorted map.
@@ -145,8 +174,9 @@ __global__ void k_origins(const int *__restrict__ sorted, const int *__restrict_
 // Per-evaluation refresh of the cell-local coordinates (FP64 and FP32) and
 // charges in sorted order.  Cell assignment stays frozen between rebuilds.
 __global__ void k_prep(const double *__restrict__ pos, const double *__restrict__ charge,
-                       const int *__restrict__ sorted, const double *__restrict__ org, int64_t natom,
-                       double4_32a *__restrict__ x64, float4 *__restrict__ x32) {
+                       const int *__restrict__ sorted, const double *__restrict__ org, const int *__restrict__ cell_of,
+                       int ncx, int64_t natom, double4_32a *__restrict__ x64, float4 *__restrict__ x32,
+                       float4 *__restrict__ xb) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= natom) return;
   int a = sorted[s];
@@ -156,6 +186,8 @@ __global__ void k_prep(const double *__restrict__ pos, const double *__restrict_
   double z = pos[3 * a + 2] - org[3 * s + 2];
   x64[s] = make_double4_32a(x, y, z, q);
   x32[s] = make_float4((float)x, (float)y, (float)z, (float)q);
+  // build coordinates: the 4th lane carries the cell's x index
+  xb[s] = make_float4((float)x, (float)y, (float)z, __int_as_float(cell_of[a] % ncx));
 }
 
 __device__ __forceinline__ int floordiv(int u, int n) {
@@ -184,6 +216,7 @@ struct BuildArgs {
   const int *wimg;
   const int *cell_start;
   const float4 *x32;
+  const float4 *xb;       // build coordinates, w = cell x index
   const float4 *shift32;
   const int *estart;
   const int2 *excl;
@@ -251,7 +284,7 @@ __device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, 
 // run are contiguous in sorted order, so lanes walk them in full 32-wide
 // chunks and recover each candidate's x offset from the cell boundaries of
 // the run (kept in registers).
-__global__ void __launch_bounds__(256) k_build(BuildArgs A) {
+__global__ void __launch_bounds__(256, 3) k_build(BuildArgs A) {
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (i >= A.natom) return;
@@ -281,21 +314,16 @@ __global__ void __launch_bounds__(256) k_build(BuildArgs A) {
         const int u0 = ci[0] + ox;
         const int n0 = floordiv(u0, N0);
         const int c0 = u0 - n0 * N0;
-        int len = min(min(K0 - ox + 1, N0 - c0), YG_RUN_MAX);
-        int bnd[YG_RUN_MAX];
-#pragma unroll
-        for (int t = 0; t < YG_RUN_MAX; t++) bnd[t] = (t < len) ? A.cell_start[rowcell + c0 + t + 1] : 0x7fffffff;
+        const int len = min(K0 - ox + 1, N0 - c0);
         const int s0 = A.cell_start[rowcell + c0], s1 = A.cell_start[rowcell + c0 + len];
+        const int obase = ox - c0 + K0 + orow;   // oidx = obase + (cell x of the candidate)
         for (int jb = s0; jb < s1; jb += 32) {
           const int j = jb + lane;
           int in = 0, central = 1, oj = -1, oidx = 0;
           if (j < s1) {
-            int t = 0;
-#pragma unroll
-            for (int q = 0; q < YG_RUN_MAX - 1; q++) t += (j >= bnd[q]) ? 1 : 0;
-            const int oxj = ox + t;
-            oidx = (oxj + K0) + orow;
-            const bool self0 = (j == i) && oxj == 0 && o1 == 0 && o2 == 0;
+            const float4 xj = A.xb[j];
+            oidx = obase + __float_as_int(xj.w);
+            const bool self0 = (j == i) && (oidx == (K0 + orow)) && o1 == 0 && o2 == 0 && n0 == 0;
             bool keep = !self0;
             if (keep && need_oj) {
               oj = A.sorted[j];
@@ -305,7 +333,6 @@ __global__ void __launch_bounds__(256) k_build(BuildArgs A) {
               }
             }
             if (keep) {
-              const float4 xj = A.x32[j];
               const float4 sh = A.shift32[oidx];
               const float dx = (xj.x - xi.x) + sh.x;
               const float dy = (xj.y - xi.y) + sh.y;
@@ -481,6 +508,7 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.wimg = ctx->d_wimg;
   A.cell_start = ctx->d_cell_start;
   A.x32 = ctx->d_x32;
+  A.xb = ctx->d_xb;
   A.shift32 = ctx->d_shift32;
   A.estart = ctx->nexcl ? ctx->d_excl_start : nullptr;
   A.excl = ctx->d_excl;
@@ -540,8 +568,8 @@ int yg_pack_pair_params(yg_ctx *ctx) {
 
 int yg_launch_prep_positions(yg_ctx *ctx) {
   k_prep<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(
-      ctx->d_pos, ctx->have_charges ? ctx->d_charge : nullptr, ctx->d_sorted, ctx->d_org, ctx->natom,
-      ctx->d_x64, ctx->d_x32);
+      ctx->d_pos, ctx->have_charges ? ctx->d_charge : nullptr, ctx->d_sorted, ctx->d_org, ctx->d_cell_of,
+      ctx->grid.n[0], ctx->natom, ctx->d_x64, ctx->d_x32, ctx->d_xb);
   YG_LAUNCH_CHECK(ctx, "k_prep");
   return YG_OK;
 }
@@ -631,7 +659,8 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   YG_LAUNCH_CHECK(ctx, "k_scan_cells");
   k_scatter<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_cell_of, N, ctx->d_cell_fill, ctx->d_sorted);
   YG_LAUNCH_CHECK(ctx, "k_scatter");
-  k_sort_cells<<<yg_blocks(G.ncell, 128), 128, 0, ctx->stream>>>(ctx->d_cell_start, G.ncell, ctx->d_sorted);
+  k_sort_cells<<<yg_blocks((int64_t)G.ncell * 32, 256), 256, 0, ctx->stream>>>(ctx->d_cell_start, G.ncell,
+                                                                                ctx->d_sorted);
   YG_LAUNCH_CHECK(ctx, "k_sort_cells");
   k_origins<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_sorted, ctx->d_cell_of, ctx->d_wimg, N, C, G,
                                                         ctx->d_org, ctx->d_rank);
