@@ -38,6 +38,10 @@ def parse():
     ap.add_argument('--natom', type=int, default=50000)
     ap.add_argument('--fp64-steps', type=int, default=3)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--serving-requests', type=int, default=4096,
+                    help='requests of the serving workload run after the main measurement (0: skip)')
+    ap.add_argument('--serving-rate', type=float, default=200.0, help='Poisson arrival rate, requests/s')
+    ap.add_argument('--serving-slots', type=int, default=16)
     return ap.parse_args()
 
 
@@ -407,6 +411,38 @@ def run_reference(args, world, rank):
             'wall_s': time.perf_counter() - t0}
 
 
+def run_serving(args):
+    """The serving workload: independent LJ + EI + Ewald systems (natom
+    log-uniform in [64, 4000], 0.064 atoms/A^3, rcut 10 A), seeded Poisson
+    arrivals, each request 50 resident MD steps of 0.5 fs in mixed precision;
+    against the plain FP64 per-system use (ForceField + host Verlet, one
+    request at a time) on a sample of the same requests."""
+    from yaff_gb300.serve import make_workload, ServingEngine, run_sequential, summarize
+    n = args.serving_requests
+    warm = make_workload(nreq=2 * args.serving_slots, rate=0.0, seed=7)
+    budget = 16 << 30
+    ServingEngine(nslots=args.serving_slots, budget_bytes=budget).run(warm, realtime=False)
+    reqs = make_workload(nreq=n, rate=args.serving_rate, seed=2024)
+    eng = ServingEngine(nslots=args.serving_slots, budget_bytes=budget)
+    wall = eng.run(reqs, realtime=True)
+    s = summarize(reqs, wall)
+    nseq = min(48, n)
+    seq = make_workload(nreq=n, rate=0.0, seed=2024)[:nseq]
+    wseq = run_sequential(seq, precision='fp64', mode='api')
+    sq = summarize(seq, wseq)
+    s.update({'arrival_rate_per_s': args.serving_rate, 'slots': args.serving_slots, 'budget_bytes': budget,
+              'peak_inflight': eng.peak_inflight, 'peak_inflight_bytes': eng.peak_inflight_bytes,
+              'max_bytes_high_over_estimate': max(r.bytes_high / float(r.estimate) for r in reqs if r.error is None),
+              'workload': '%d requests, natom log-uniform [64, 4000], 0.064/A^3, rcut 10 A, LJ+EI+Ewald, '
+                          '50 MD steps of 0.5 fs each, mixed precision, seeded Poisson arrivals' % n,
+              'sequential_fp64_api': {'requests': nseq, 'requests_per_s': sq['requests_per_s'],
+                                      'atom_steps_per_s': sq['atom_steps_per_s'],
+                                      'service_p50_ms': sq['service_p50_ms'],
+                                      'how': 'ForceField + host VerletIntegrator, FP64, one request at a time'}})
+    s['atom_steps_speedup_vs_sequential_fp64'] = s['atom_steps_per_s'] / sq['atom_steps_per_s']
+    return s
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -424,6 +460,8 @@ def main():
         return
     out, spec = run_gb300(args, world, rank, local)
     if rank == 0:
+        if args.serving_requests > 0 and world == 1:
+            out['serving'] = run_serving(args)
         if not args.no_cpu_baseline:
             out['cpu_baseline'] = cpu_sample(args.natom)
         print(json.dumps(out))

@@ -181,6 +181,39 @@ int yg_sync(yg_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 int64_t yg_launch_count(yg_ctx *ctx);
 
+/* Device memory held by the context: bytes now and the high-water mark since
+ * creation (no reference counterpart; the serving loop's admission check). */
+int yg_mem_usage(yg_ctx *ctx, int64_t *bytes_now, int64_t *bytes_high);
+
+/* The library's stream-ordered device pool on the current device (all
+ * contexts allocate from it; creating and destroying contexts never
+ * synchronizes the device): bytes in use, their high-water mark and bytes
+ * reserved from the driver.  Any pointer may be NULL. */
+int yg_pool_usage(int64_t *used_now, int64_t *used_high, int64_t *reserved);
+
+/* Device-resident velocity Verlet of yaff/sampling/verlet.py:320-367 for the
+ * serving loop: positions, velocities (host arrays here, natom x 3), masses
+ * and the neighbour list stay in HBM.  part_mask selects the result slots
+ * summed into the force (bit YG_PART_*); extra_energy is a constant added to
+ * the logged potential energy (the host-side neutralizing term); the energy
+ * log holds max_steps + 1 (epot, ekin) rows.  Requires a built list. */
+int yg_md_setup(yg_ctx *ctx, const double *masses, const double *vel, double dt,
+                int part_mask, double extra_energy, int64_t max_steps);
+
+/* Runs nsteps steps without host synchronization inside a batch of up to
+ * 128 steps: the skin test of yaff/pes/nlist.py:207-218 (rebuild when
+ * 2 (rmax+1) max|r - r_build| >= skin; skin <= 0: every step) runs on the
+ * device and gates the rebuild kernels.  With use_graph != 0 a whole step is
+ * replayed from a CUDA graph captured on first use.  The host reads the
+ * status words once per batch; a batch in which a rebuilt neighbour row
+ * overflowed its slot is rolled back and run again with larger slots.
+ * *nrebuild receives the number of rebuilds. */
+int yg_md_run(yg_ctx *ctx, int64_t nsteps, int use_graph, double skin, int64_t *nrebuild);
+
+/* Copies positions, velocities (natom x 3) and the energy log
+ * ((*nlog) x 2) to host memory; any pointer may be NULL. */
+int yg_md_get(yg_ctx *ctx, double *pos, double *vel, double *log, int64_t *nlog);
+
 /* Ewald correction for callers that cannot let the library allocate device
  * memory (an engine that owns all device memory through its own pool, or a
  * step loop that must not block on an allocation).  No counterpart in the

@@ -68,7 +68,12 @@ SIGNATURES = {
     'yg_get_total': (_I, [_P, _I, _P, _P, _P, _P]),
     'yg_sync': (_I, [_P]),
     'yg_launch_count': (_I64, [_P]),
+    'yg_mem_usage': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    'yg_pool_usage': (_I, [ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     'yg_probe_peak': (_D, [_I, _P]),
+    'yg_md_setup': (_I, [_P, _P, _P, _D, _I, _D, _I64]),
+    'yg_md_run': (_I, [_P, _I64, _I, _D, ctypes.POINTER(_I64)]),
+    'yg_md_get': (_I, [_P, _P, _P, _P, ctypes.POINTER(_I64)]),
     'yg_ewald_corr_noalloc': (_I, [_P, _P, _I64, _P, _P, _P, _I64, _P, _P, _D, _D, _D, _I64, _I64, _P, _P, _P,
                                    _P]),
 }

@@ -21,13 +21,13 @@ def build_system(spec):
                   bonds=np.zeros((0, 2), np.int64) if spec.get('bonds') is None else spec['bonds'])
 
 
-def build_forcefield(spec, precision=None, system=None):
+def build_forcefield(spec, precision=None, system=None, stream=None):
     """ForceField for `spec` whose parts all run on the GPU; `precision` is
-    'fp64' (plain), 'mixed' or 'mixed_kahan'."""
+    'fp64' (plain), 'mixed' or 'mixed_kahan'; `stream` a cudaStream_t handle."""
     if system is None:
         system = build_system(spec)
-    if precision is not None:
-        device_of(system, precision)
+    if precision is not None or stream is not None:
+        device_of(system, precision, stream=stream)
     nlist = NeighborList(system, skin=spec['skin'], nlow=spec.get('nlow', 0), nhigh=spec.get('nhigh', -1))
     scalings = Scalings(system, *spec['scalings'])
     tr = spec.get('tr')

@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -24,22 +26,100 @@ int yg_cuda_fail(cudaError_t err, const char *what) {
   return YG_ERR_CUDA;
 }
 
-int yg_alloc(void **ptr, size_t bytes) {
-  if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(ptr, bytes);
-  if (e != cudaSuccess) {
-    *ptr = nullptr;
-    return yg_cuda_fail(e, "cudaMalloc");
+namespace {
+std::mutex g_pool_mu;
+std::map<int, cudaMemPool_t> g_pools;
+// pinned host blocks of freed contexts, by power-of-two size class
+std::multimap<size_t, void *> g_pinned_free;
+
+// The library's own pool per device: freed memory up to the release
+// threshold stays mapped for the next context instead of going back to the
+// driver at every synchronization.
+int pool_of_current_device(cudaMemPool_t *out) {
+  int dev = 0;
+  YG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  auto it = g_pools.find(dev);
+  if (it != g_pools.end()) {
+    *out = it->second;
+    return YG_OK;
   }
+  cudaMemPoolProps props;
+  memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool;
+  YG_CUDA(cudaMemPoolCreate(&pool, &props));
+  uint64_t keep = (uint64_t)8 << 30;
+  YG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  g_pools[dev] = pool;
+  *out = pool;
   return YG_OK;
 }
 
-int yg_ensure(void **ptr, size_t *cap, size_t bytes) {
-  if (*ptr && *cap >= bytes) return YG_OK;
-  if (*ptr) cudaFree(*ptr);
+size_t pinned_class(size_t bytes) {
+  size_t c = 4096;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+
+int pinned_get(size_t bytes, void **out, size_t *cls) {
+  *cls = pinned_class(bytes);
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pinned_free.find(*cls);
+    if (it != g_pinned_free.end()) {
+      *out = it->second;
+      g_pinned_free.erase(it);
+      return YG_OK;
+    }
+  }
+  YG_CUDA(cudaMallocHost(out, *cls));
+  return YG_OK;
+}
+
+// Pinned blocks are recycled, never released: cudaFreeHost would synchronize
+// the device.
+void pinned_put(void *p, size_t cls) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_pinned_free.emplace(cls, p);
+}
+}  // namespace
+
+int yg_alloc(yg_ctx *ctx, void **ptr, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocFromPoolAsync(ptr, bytes, ctx->pool, ctx->stream);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    return yg_cuda_fail(e, "cudaMallocFromPoolAsync");
+  }
+  ctx->alloc_bytes[*ptr] = bytes;
+  ctx->alloc_calls++;
+  ctx->bytes_now += (int64_t)bytes;
+  if (ctx->bytes_now > ctx->bytes_high) ctx->bytes_high = ctx->bytes_now;
+  return YG_OK;
+}
+
+void yg_free(yg_ctx *ctx, void **ptr) {
+  if (*ptr) {
+    cudaFreeAsync(*ptr, ctx->stream);
+    auto it = ctx->alloc_bytes.find(*ptr);
+    if (it != ctx->alloc_bytes.end()) {
+      ctx->bytes_now -= (int64_t)it->second;
+      ctx->alloc_bytes.erase(it);
+    }
+  }
   *ptr = nullptr;
+}
+
+int yg_ensure(yg_ctx *ctx, void **ptr, size_t *cap, size_t bytes) {
+  if (*ptr && *cap >= bytes) return YG_OK;
+  yg_free(ctx, ptr);
   size_t want = bytes + bytes / 4 + 256;
-  int rc = yg_alloc(ptr, want);
+  int rc = yg_alloc(ctx, ptr, want);
   if (rc) {
     *cap = 0;
     return rc;
@@ -112,29 +192,37 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
   c->precision = precision;
   c->stream = (cudaStream_t)stream;
   const size_t N = (size_t)natom;
-  int rc = 0;
-  rc |= yg_alloc((void **)&c->d_pos, N * 3 * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_pos_build, N * 3 * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_charge, N * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_cell_of, N * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_wimg, N * 3 * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_sorted, N * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_rank, N * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_org, N * 3 * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_x64, N * sizeof(double4_32a));
-  rc |= yg_alloc((void **)&c->d_x32, N * sizeof(float4));
-  rc |= yg_alloc((void **)&c->d_xb, N * sizeof(float4));
-  rc |= yg_alloc((void **)&c->d_ncount, N * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_status, YG_ST_NWORDS * sizeof(int));
-  rc |= yg_alloc((void **)&c->d_part_ev, YG_NPART * 10 * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_part_gpos, (size_t)YG_NPART * N * 3 * sizeof(double));
-  rc |= yg_alloc((void **)&c->d_total, (16 + N * 3) * sizeof(double));
-  if (rc == YG_OK) rc = yg_ensure((void **)&c->d_red, &c->red_cap, 4096 * sizeof(double));
+  int rc = pool_of_current_device(&c->pool);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  rc |= yg_alloc(c, (void **)&c->d_pos, N * 3 * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_pos_build, N * 3 * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_charge, N * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_cell_of, N * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_wimg, N * 3 * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_sorted, N * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_rank, N * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_org, N * 3 * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_x64, N * sizeof(double4_32a));
+  rc |= yg_alloc(c, (void **)&c->d_x32, N * sizeof(float4));
+  rc |= yg_alloc(c, (void **)&c->d_xb, N * sizeof(float4));
+  rc |= yg_alloc(c, (void **)&c->d_ncount, N * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_status, YG_ST_NWORDS * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_part_ev, YG_NPART * 10 * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_part_gpos, (size_t)YG_NPART * N * 3 * sizeof(double));
+  rc |= yg_alloc(c, (void **)&c->d_total, (16 + N * 3) * sizeof(double));
+  if (rc == YG_OK) rc = yg_ensure(c, (void **)&c->d_red, &c->red_cap, 4096 * sizeof(double));
   if (rc == YG_OK) {
-    if (cudaMallocHost((void **)&c->h_status, YG_ST_NWORDS * sizeof(int)) != cudaSuccess ||
-        cudaMallocHost((void **)&c->h_total, (16 + N * 3) * sizeof(double)) != cudaSuccess) {
-      yg_set_error("cudaMallocHost failed");
+    // [h_total | 8 u64 words | status words]
+    const size_t tot = (16 + N * 3) * sizeof(double);
+    if (pinned_get(tot + 64 + YG_ST_NWORDS * sizeof(int), &c->h_block, &c->h_block_bytes) != YG_OK) {
       rc = YG_ERR_CUDA;
+    } else {
+      c->h_total = (double *)c->h_block;
+      c->h_u64 = (unsigned long long *)((char *)c->h_block + tot);
+      c->h_status = (int *)((char *)c->h_block + tot + 64);
     }
   }
   if (rc == YG_OK) {
@@ -154,16 +242,26 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
 int yg_destroy(yg_ctx *c) {
   if (!c) return YG_OK;
   cudaStreamSynchronize(c->stream);
-  void *bufs[] = {c->d_pos, c->d_pos_build, c->d_charge, c->d_cell_of, c->d_wimg, c->d_sorted, c->d_rank,
-                  c->d_cell_start, c->d_cell_fill, c->d_org, c->d_x64, c->d_x32, c->d_xb, c->d_shift64, c->d_shift32,
-                  c->d_nbr, c->d_ncount, c->d_status, c->d_excl_start, c->d_excl, c->d_stab_ab, c->d_stab_scale,
-                  c->d_pp_src, c->d_pp64, c->d_pp32, c->d_ew_pref, c->d_ew_tiles, c->d_ew_tab, c->d_ew_Spart,
-                  c->d_ew_S, c->d_ew_W, c->d_ew_gpart, c->d_ew_red, c->d_delta_ij, c->d_delta, c->d_ic,
-                  c->d_icval, c->d_vpar, c->d_vic, c->d_vE, c->d_part_ev, c->d_part_gpos, c->d_total, c->d_red};
-  for (void *b : bufs)
-    if (b) cudaFree(b);
-  if (c->h_status) cudaFreeHost(c->h_status);
-  if (c->h_total) cudaFreeHost(c->h_total);
+  void **bufs[] = {
+      (void **)&c->d_pos, (void **)&c->d_pos_build, (void **)&c->d_charge, (void **)&c->d_cell_of,
+      (void **)&c->d_wimg, (void **)&c->d_sorted, (void **)&c->d_rank, (void **)&c->d_cell_start,
+      (void **)&c->d_cell_fill, (void **)&c->d_org, (void **)&c->d_x64, (void **)&c->d_x32, (void **)&c->d_xb,
+      (void **)&c->d_shift64, (void **)&c->d_shift32, (void **)&c->d_nbr, (void **)&c->d_ncount,
+      (void **)&c->d_status, (void **)&c->d_excl_start, (void **)&c->d_excl, (void **)&c->d_stab_ab,
+      (void **)&c->d_stab_scale, (void **)&c->d_pp_src, (void **)&c->d_pp64, (void **)&c->d_pp32,
+      (void **)&c->d_ew_pref, (void **)&c->d_ew_tiles, (void **)&c->d_ew_tab, (void **)&c->d_ew_Spart,
+      (void **)&c->d_ew_S, (void **)&c->d_ew_W, (void **)&c->d_ew_gpart, (void **)&c->d_ew_red,
+      (void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval, (void **)&c->d_vpar,
+      (void **)&c->d_vic, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,
+      (void **)&c->d_total, (void **)&c->d_red, (void **)&c->d_vel, (void **)&c->d_invm, (void **)&c->d_md_ekpart,
+      (void **)&c->d_md_ekin, (void **)&c->d_md_log, (void **)&c->d_md_extra, (void **)&c->d_md_step,
+      (void **)&c->d_md_ctrl, (void **)&c->d_snap_pos, (void **)&c->d_snap_vel, (void **)&c->d_snap_total,
+      (void **)&c->d_snap_step};
+  if (c->md_graph_exec) cudaGraphExecDestroy(c->md_graph_exec);
+  if (c->md_cap_stream) cudaStreamDestroy(c->md_cap_stream);
+  if (c->pool)
+    for (void **b : bufs) yg_free(c, b);
+  pinned_put(c->h_block, c->h_block_bytes);
   delete c;
   return YG_OK;
 }
@@ -190,6 +288,7 @@ int yg_set_cell(yg_ctx *c, const double *rvecs, const double *gvecs, int nvec, d
   c->cell.nvec = nvec;
   c->have_cell = 1;
   c->have_list = 0;
+  c->geom_valid = 0;
   return YG_OK;
 }
 
@@ -249,19 +348,15 @@ int yg_set_scalings(yg_ctx *c, const int64_t *a, const int64_t *b, const double 
     ab[r] = make_int2((int)a[r], (int)b[r]);
     sc[r] = scale[r];
   }
-  cudaFree(c->d_excl_start);
-  cudaFree(c->d_excl);
-  cudaFree(c->d_stab_ab);
-  cudaFree(c->d_stab_scale);
-  c->d_excl_start = nullptr;
-  c->d_excl = nullptr;
-  c->d_stab_ab = nullptr;
-  c->d_stab_scale = nullptr;
+  yg_free(c, (void **)&c->d_excl_start);
+  yg_free(c, (void **)&c->d_excl);
+  yg_free(c, (void **)&c->d_stab_ab);
+  yg_free(c, (void **)&c->d_stab_scale);
   int rc;
-  if ((rc = yg_alloc((void **)&c->d_excl_start, (N + 1) * sizeof(int)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_excl, ex.size() * sizeof(int2)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_stab_ab, ab.size() * sizeof(int2)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_stab_scale, sc.size() * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_excl_start, (N + 1) * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_excl, ex.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_stab_ab, ab.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_stab_scale, sc.size() * sizeof(double)))) return rc;
   YG_CUDA(cudaMemcpyAsync(c->d_excl_start, start.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->d_excl, ex.data(), ex.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->d_stab_ab, ab.data(), ab.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
@@ -469,18 +564,16 @@ int yg_set_valence(yg_ctx *c, const int64_t *delta_ij, int64_t ndelta, const int
     if (vterm_ic[t] < 0 || vterm_ic[t] >= nic) return YG_ERR_ARG;
     vic[t] = (int)vterm_ic[t];
   }
-  void *bufs[] = {c->d_delta_ij, c->d_delta, c->d_ic, c->d_icval, c->d_vpar, c->d_vic, c->d_vE};
-  for (void *b : bufs)
-    if (b) cudaFree(b);
-  c->d_delta_ij = nullptr; c->d_delta = nullptr; c->d_ic = nullptr; c->d_icval = nullptr;
-  c->d_vpar = nullptr; c->d_vic = nullptr; c->d_vE = nullptr;
+  void **bufs[] = {(void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval,
+                   (void **)&c->d_vpar,     (void **)&c->d_vic,   (void **)&c->d_vE};
+  for (void **b : bufs) yg_free(c, b);
   int rc;
-  if ((rc = yg_alloc((void **)&c->d_delta_ij, ij.size() * sizeof(int2)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_delta, (size_t)(ndelta > 0 ? ndelta : 1) * 6 * sizeof(double)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_ic, (size_t)(nic > 0 ? nic : 1) * 9 * sizeof(int64_t)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_icval, (size_t)(nic > 0 ? nic : 1) * 2 * sizeof(double)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_vpar, (size_t)(nterm > 0 ? nterm : 1) * 2 * sizeof(double)))) return rc;
-  if ((rc = yg_alloc((void **)&c->d_vic, vic.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_delta_ij, ij.size() * sizeof(int2)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_delta, (size_t)(ndelta > 0 ? ndelta : 1) * 6 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_ic, (size_t)(nic > 0 ? nic : 1) * 9 * sizeof(int64_t)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_icval, (size_t)(nic > 0 ? nic : 1) * 2 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_vpar, (size_t)(nterm > 0 ? nterm : 1) * 2 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_vic, vic.size() * sizeof(int)))) return rc;
   YG_CUDA(cudaMemcpyAsync(c->d_delta_ij, ij.data(), ij.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
   if (nic > 0)
     YG_CUDA(cudaMemcpyAsync(c->d_ic, ic_rows, (size_t)nic * 9 * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
@@ -550,5 +643,32 @@ int yg_sync(yg_ctx *c) {
 }
 
 int64_t yg_launch_count(yg_ctx *c) { return c ? c->launches : -1; }
+
+int yg_mem_usage(yg_ctx *c, int64_t *bytes_now, int64_t *bytes_high) {
+  if (!c) return YG_ERR_ARG;
+  if (bytes_now) *bytes_now = c->bytes_now;
+  if (bytes_high) *bytes_high = c->bytes_high;
+  return YG_OK;
+}
+
+int yg_pool_usage(int64_t *used_now, int64_t *used_high, int64_t *reserved) {
+  cudaMemPool_t pool;
+  int rc = pool_of_current_device(&pool);
+  if (rc) return rc;
+  uint64_t v = 0;
+  if (used_now) {
+    YG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &v));
+    *used_now = (int64_t)v;
+  }
+  if (used_high) {
+    YG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &v));
+    *used_high = (int64_t)v;
+  }
+  if (reserved) {
+    YG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &v));
+    *reserved = (int64_t)v;
+  }
+  return YG_OK;
+}
 
 }  // extern "C"

@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <cmath>
 #include <type_traits>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "yg_internal.cuh"
@@ -525,6 +527,27 @@ __global__ void k_store_corr_ev(const double *__restrict__ sums, double eself, d
   for (int q = 0; q < 9; q++) ev[1 + q] = v[q];
 }
 
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum, once per (kernel, device): setting it per launch to the launch's
+// own size would race between host threads that drive different contexts.
+static int smem_optin(const void *kernel, size_t need) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  int dev = 0;
+  YG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count(std::make_pair(kernel, dev))) return YG_OK;
+  int optin = 0;
+  YG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (need > (size_t)optin) {
+    yg_set_error("Ewald tile needs more shared memory than the device offers");
+    return YG_ERR_UNSUPPORTED;
+  }
+  YG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  done.insert(std::make_pair(kernel, dev));
+  return YG_OK;
+}
+
 template <typename T> size_t force_smem(int nm, int RA) {
   size_t a = (size_t)nm * (16 * RA + EW_FC) * sizeof(typename C2<T>::t) + EW_FC * sizeof(int4);
   size_t b = (size_t)16 * 16 * RA * 3 * sizeof(double);
@@ -547,7 +570,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   int rc;
   // tables
   size_t tb = (size_t)N * L * sizeof(CT);
-  if ((rc = yg_ensure(&ctx->d_ew_tab, &ctx->ew_bytes_tab, tb))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_tab, &ctx->ew_bytes_tab, tb))) return rc;
   CT *tab = (CT *)ctx->d_ew_tab;
   k_tables<T><<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2, tab);
   YG_LAUNCH_CHECK(ctx, "k_tables");
@@ -564,7 +587,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   }
   if (maxchunk < 1) maxchunk = 1;
   size_t per = (size_t)nstile * nslab * EW_SC * EW_MS;
-  if ((rc = yg_ensure(&ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(CA)))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(CA)))) return rc;
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
     double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
@@ -576,7 +599,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     dim3 grid(nstile, nch, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     const size_t ssm = (size_t)SfacCfg<T>::KA * L * sizeof(CT);
-    YG_CUDA(cudaFuncSetAttribute(k_sfac<T, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    if ((rc = smem_optin((const void *)k_sfac<T, TA>, ssm))) return rc;
     k_sfac<T, TA><<<grid, 128, ssm, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
                                                  (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
@@ -586,9 +609,9 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   }
   // energy, virial, weights
   const int ngroup = (nS == 3) ? 3 : 1;
-  if ((rc = yg_ensure(&ctx->d_ew_W, &ctx->ew_bytes_W, (size_t)ngroup * nk_dense * sizeof(CT)))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_W, &ctx->ew_bytes_W, (size_t)ngroup * nk_dense * sizeof(CT)))) return rc;
   const int eb = yg_blocks(nk_dense, 256);
-  if ((rc = yg_ensure((void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
   double *partial = ctx->d_red + 64;
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
@@ -606,9 +629,9 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     return YG_OK;
   }
   // force pass, per atom group
-  if ((rc = yg_ensure((void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
   size_t smem = force_smem<T>(nm, RA);
-  YG_CUDA(cudaFuncSetAttribute(k_ewald_force<T, RA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if ((rc = smem_optin((const void *)k_ewald_force<T, RA>, smem))) return rc;
   const int gidx[3] = {0, 1, 2};
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
@@ -679,16 +702,16 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   ctx->ew_nm = nm;
   ctx->ew_nk = nk;
   ctx->ew_ntile = (int)(tiles.size() / EW_SC);
-  cudaFree(ctx->d_ew_pref);
-  cudaFree(ctx->d_ew_tiles);
-  cudaFree(ctx->d_ew_S);
+  yg_free(ctx, (void **)&ctx->d_ew_pref);
+  yg_free(ctx, (void **)&ctx->d_ew_tiles);
+  yg_free(ctx, (void **)&ctx->d_ew_S);
   ctx->d_ew_pref = nullptr;
   ctx->d_ew_tiles = nullptr;
   ctx->d_ew_S = nullptr;
   int rc;
-  if ((rc = yg_alloc((void **)&ctx->d_ew_pref, nk_dense * sizeof(double)))) return rc;
-  if ((rc = yg_alloc((void **)&ctx->d_ew_tiles, std::max<size_t>(1, tiles.size()) * sizeof(int4)))) return rc;
-  if ((rc = yg_alloc((void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_pref, nk_dense * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_tiles, std::max<size_t>(1, tiles.size()) * sizeof(int4)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_pref, pref.data(), nk_dense * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (!tiles.empty())
     YG_CUDA(cudaMemcpyAsync(ctx->d_ew_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice,
@@ -721,7 +744,7 @@ int yg_launch_ewald_corr(yg_ctx *ctx, int want_grad) {
   const int64_t n = ctx->nstab;
   const int nb = yg_blocks(n > 0 ? n : 1, 256);
   int rc;
-  if ((rc = yg_ensure((void **)&ctx->d_red, &ctx->red_cap, ((size_t)nb * 7 + 64 + 7) * sizeof(double)))) return rc;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)nb * 7 + 64 + 7) * sizeof(double)))) return rc;
   double *partial = ctx->d_red + 64;
   k_ewald_corr<<<nb, 256, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, ctx->d_stab_ab, ctx->d_stab_scale, n, ctx->cell,
                                             ctx->ew_alpha, ctx->ew_nlow, ctx->ew_nhigh, 1.0 / ctx->ew_diel,

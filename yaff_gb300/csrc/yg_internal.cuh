@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/yaffgb.h"
@@ -72,6 +73,12 @@ struct yg_ctx {
   int64_t natom = 0;
   int precision = YG_FP64;
   cudaStream_t stream = 0;
+  cudaMemPool_t pool = nullptr;   // stream-ordered pool of this context's device
+  void *h_block = nullptr;        // pinned host block holding h_status and h_total
+  size_t h_block_bytes = 0;
+  std::unordered_map<void *, size_t> alloc_bytes;  // live device buffers
+  int64_t bytes_now = 0, bytes_high = 0;
+  int64_t alloc_calls = 0;
   int64_t launches = 0;
 
   CellGeom cell{};
@@ -99,11 +106,15 @@ struct yg_ctx {
   float4 *d_xb = nullptr;         // sorted: FP32 coordinates, w = cell x index (build)
   double *d_shift64 = nullptr;    // noff*3 stencil shift vectors
   float4 *d_shift32 = nullptr;    // noff
+  size_t shift64_cap = 0, shift32_cap = 0;
   int cap_sorted = 0;             // allocated cell-list capacity (cells)
   GridGeom grid{};
   int have_list = 0;
   int list_recomputed = 0;        // skin path ran since the last rebuild
   int fast_path = 0;
+  int geom_valid = 0;             // grid, shifts and band match (cell, geom_rc)
+  double geom_rc = 0.0;
+  float band_lo = 0.0f, band_hi = 0.0f;  // FP32 guard band on d^2
   double rcut_total = 0.0;
   int64_t rmax[3] = {0, 0, 0};
   int64_t nlow = 0, nhigh = 0;
@@ -116,6 +127,7 @@ struct yg_ctx {
   int64_t nbr_alloc = 0;          // entries allocated
   int *d_status = nullptr;        // YG_ST_NWORDS
   int *h_status = nullptr;        // pinned mirror
+  unsigned long long *h_u64 = nullptr;  // pinned: 8 words for small readbacks
 
   // exclusions: per-atom CSR over orig indices, both directions
   int *d_excl_start = nullptr;    // natom+1
@@ -166,6 +178,30 @@ struct yg_ctx {
   int *d_vic = nullptr;           // nterm
   double *d_vE = nullptr;         // nterm
 
+  // device-resident velocity Verlet (yg_md_*)
+  double *d_vel = nullptr;        // natom*3
+  double *d_invm = nullptr;       // natom
+  double *d_md_ekpart = nullptr;
+  double *d_md_ekin = nullptr;
+  double *d_md_log = nullptr;     // (max_steps+1)*2: epot, ekin
+  double *d_md_extra = nullptr;   // host-side energy added to epot (neutralizing term)
+  int *d_md_step = nullptr;
+  double md_dt = 0.0;
+  int md_mask = 0;
+  int64_t md_max_steps = 0, md_steps_done = 0;
+  int md_ready = 0;
+  int md_graph_valid = 0;
+  cudaGraphExec_t md_graph_exec = nullptr;
+  cudaStream_t md_cap_stream = nullptr;  // capture stream of the step graph
+  // control words of the device-driven step: [0] rebuild gate of this step,
+  // [1] force a rebuild, [2] rebuilds so far, [4..5] pair count of the last
+  // rebuild (u64), [6..7] largest squared displacement bits (u64)
+  int *d_md_ctrl = nullptr;
+  double *d_snap_pos = nullptr, *d_snap_vel = nullptr, *d_snap_total = nullptr;
+  int *d_snap_step = nullptr;
+  int64_t md_rebuilds = 0;        // rebuild count at the end of the last run
+  double md_graph_skin = 0.0;
+
   // results per part: energy, vtens[9]; gpos natom*3
   double *d_part_ev = nullptr;    // YG_NPART*10
   double *d_part_gpos = nullptr;  // YG_NPART*natom*3
@@ -191,9 +227,14 @@ int yg_cuda_fail(cudaError_t err, const char *what);
     if (_e != cudaSuccess) return yg_cuda_fail(_e, what);   \
   } while (0)
 
+// Device buffers are stream-ordered allocations on the context's stream from
+// a per-device pool: creating and destroying contexts never synchronizes the
+// device, so contexts on different streams run concurrently.
 // Grows a device buffer to at least `bytes` (contents are not preserved).
-int yg_ensure(void **ptr, size_t *cap, size_t bytes);
-int yg_alloc(void **ptr, size_t bytes);
+int yg_ensure(yg_ctx *ctx, void **ptr, size_t *cap, size_t bytes);
+int yg_alloc(yg_ctx *ctx, void **ptr, size_t bytes);
+// Releases a buffer (stream-ordered) and clears the pointer.
+void yg_free(yg_ctx *ctx, void **ptr);
 
 // --------------------------------------------- exact FP64 (no contraction)
 // These reproduce the operation order of the reference C code with every
@@ -256,6 +297,8 @@ __device__ __forceinline__ bool img_zero(const int *r) {
 
 // ------------------------------------------------------- launchers (host)
 int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry);
+int yg_launch_nlist_build_gated(yg_ctx *ctx, const int *gate, unsigned long long *total);
+int yg_launch_max_disp2_async(yg_ctx *ctx, unsigned long long *out);
 int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, int64_t *n);
 int yg_launch_prep_positions(yg_ctx *ctx);
 int yg_launch_max_disp2(yg_ctx *ctx, double *out);

@@ -1,0 +1,353 @@
+// yg_md.cu -- device-resident velocity Verlet driven entirely by the GPU.
+//
+// The integration step of yaff/sampling/verlet.py:339-367 (half kick, drift,
+// force evaluation, half kick) with positions, velocities, masses and the
+// neighbour list resident in HBM.  The reference's skin test
+// (yaff/pes/nlist.py:207-218: rebuild when 2 (rmax+1) max|r - r_build| >=
+// skin) is evaluated on the device and gates the rebuild kernels, so a whole
+// step -- drift, skin test, conditional rebuild, cell-local coordinates,
+// fused pair terms, Ewald, valence, device-side sum of the parts, second
+// kick, energy log -- is one sequence with no host synchronization.  It is
+// captured once into a CUDA graph and replayed; the host reads the status
+// words once per batch of steps.  A neighbour row that overflowed its slot
+// during a device rebuild is detected at the end of the batch: the batch is
+// rolled back to its snapshot, the slots grow, and the batch runs again.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "yg_internal.cuh"
+
+#define YG_MD_BATCH 128   // steps between host status checks
+
+namespace {
+
+// vel += 0.5 dt a; pos += dt vel   (a = -gpos / m, gpos from the last total)
+__global__ void k_kick_drift(double *__restrict__ pos, double *__restrict__ vel, const double *__restrict__ gpos,
+                             const double *__restrict__ invm, int64_t natom, double dt) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= natom * 3) return;
+  const double a = -gpos[t] * invm[t / 3];
+  const double v = vel[t] + 0.5 * a * dt;
+  vel[t] = v;
+  pos[t] += dt * v;
+}
+
+// vel += 0.5 dt a; per-block partial kinetic energy
+__global__ void k_kick(double *__restrict__ vel, const double *__restrict__ gpos, const double *__restrict__ invm,
+                       int64_t natom, double dt, double *__restrict__ ekin_part) {
+  __shared__ double red[8];
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double ek = 0.0;
+  if (t < natom * 3) {
+    const double im = invm[t / 3];
+    const double v = vel[t] + 0.5 * (-gpos[t] * im) * dt;
+    vel[t] = v;
+    ek = 0.5 * v * v / im;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ek += __shfl_xor_sync(0xffffffffu, ek, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ek;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+    ekin_part[blockIdx.x] = s;
+  }
+}
+
+// log[step] = (epot, ekin) from the device-side totals; step++
+__global__ void k_md_log(const double *__restrict__ total, const double *__restrict__ ekin, const double *__restrict__ extra,
+                         double *__restrict__ log, int *__restrict__ step, int64_t max_rows) {
+  if (threadIdx.x != 0) return;
+  const int s = *step;
+  if (s < max_rows) {
+    log[2 * s] = total[0] + *extra;
+    log[2 * s + 1] = *ekin;
+  }
+  *step = s + 1;
+}
+
+__global__ void k_total_dev(const double *__restrict__ part_ev, const double *__restrict__ part_gpos, int64_t natom,
+                            int mask, double *__restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < 10) {
+    double s = 0.0;
+    for (int p = 0; p < YG_NPART; p++)
+      if (mask & (1 << p)) s += part_ev[10 * p + t];
+    out[t] = s;
+  }
+  if (t < natom * 3) {
+    double s = 0.0;
+    for (int p = 0; p < YG_NPART; p++)
+      if (mask & (1 << p)) s += part_gpos[(int64_t)p * natom * 3 + t];
+    out[16 + t] = s;
+  }
+}
+
+// The skin test of the step: gate = force || !(sqrt(d2) * factor < skin)
+// (also set for NaN); clears the displacement word for the next step.
+__global__ void k_skin_gate(int *__restrict__ ctrl, double factor, double skin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long *d2w = (unsigned long long *)(ctrl + 6);
+  const double d2 = __longlong_as_double((long long)*d2w);
+  *d2w = 0ull;
+  const double disp = sqrt(d2) * factor;
+  const int gate = ctrl[1] || !(disp < skin);
+  ctrl[0] = gate;
+  if (gate) {
+    ctrl[1] = 0;
+    ctrl[2] += 1;
+  }
+}
+
+__global__ void k_set_int(int *__restrict__ p, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p = v;
+}
+
+}  // namespace
+
+// Force evaluation for the current device positions on the kept list,
+// summed on the device into d_total; no host synchronization.  prep = 0
+// when the cell-local coordinates are already current.
+static int md_force_async(yg_ctx *c, int prep) {
+  int rc;
+  if (prep && (rc = yg_launch_prep_positions(c))) return rc;
+  int pmask = 0;
+  for (int p = 0; p < YG_MAX_POT; p++)
+    if (c->pot[p].active && (c->md_mask & (1 << p))) pmask |= 1 << p;
+  if (pmask && (rc = yg_launch_pair(c, pmask, 1))) return rc;
+  if ((c->md_mask & (1 << YG_PART_EWALD_RECI)) && (rc = yg_launch_ewald_reci(c, 1))) return rc;
+  if ((c->md_mask & (1 << YG_PART_EWALD_CORR)) && (rc = yg_launch_ewald_corr(c, 1))) return rc;
+  if ((c->md_mask & (1 << YG_PART_VALENCE)) && (rc = yg_launch_valence(c, 1))) return rc;
+  k_total_dev<<<yg_blocks(c->natom * 3, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom,
+                                                                  c->md_mask, c->d_total);
+  YG_LAUNCH_CHECK(c, "k_total_dev");
+  return YG_OK;
+}
+
+// second kick, kinetic energy, energy log row
+static int md_finish_step(yg_ctx *c, double dt) {
+  int rc;
+  const int nb = yg_blocks(c->natom * 3, 256);
+  k_kick<<<nb, 256, 0, c->stream>>>(c->d_vel, c->d_total + 16, c->d_invm, c->natom, dt, c->d_md_ekpart);
+  YG_LAUNCH_CHECK(c, "k_kick");
+  if ((rc = yg_launch_reduce_ev(c, c->d_md_ekpart, nb, 1, c->d_md_ekin))) return rc;
+  k_md_log<<<1, 32, 0, c->stream>>>(c->d_total, c->d_md_ekin, c->d_md_extra, c->d_md_log, c->d_md_step,
+                                    c->md_max_steps + 1);
+  YG_LAUNCH_CHECK(c, "k_md_log");
+  return YG_OK;
+}
+
+// One whole step, enqueued without host synchronization.
+static int md_step_device(yg_ctx *c, double factor, double skin) {
+  int rc;
+  const int nb = yg_blocks(c->natom * 3, 256);
+  k_kick_drift<<<nb, 256, 0, c->stream>>>(c->d_pos, c->d_vel, c->d_total + 16, c->d_invm, c->natom, c->md_dt);
+  YG_LAUNCH_CHECK(c, "k_kick_drift");
+  if ((rc = yg_launch_max_disp2_async(c, (unsigned long long *)(c->d_md_ctrl + 6)))) return rc;
+  k_skin_gate<<<1, 32, 0, c->stream>>>(c->d_md_ctrl, factor, skin);
+  YG_LAUNCH_CHECK(c, "k_skin_gate");
+  // the build sequence refreshes the cell-local coordinates in any case
+  if ((rc = yg_launch_nlist_build_gated(c, c->d_md_ctrl, (unsigned long long *)(c->d_md_ctrl + 4)))) return rc;
+  if ((rc = md_force_async(c, 0))) return rc;
+  return md_finish_step(c, c->md_dt);
+}
+
+static void md_drop_graph(yg_ctx *c) {
+  if (c->md_graph_exec) cudaGraphExecDestroy(c->md_graph_exec);
+  c->md_graph_exec = nullptr;
+  c->md_graph_valid = 0;
+}
+
+// Records one step into the context's graph (on a private stream: the legacy
+// default stream cannot be captured; the graph is replayed on the context's
+// own stream).
+static int md_capture(yg_ctx *c, double factor, double skin) {
+  md_drop_graph(c);
+  if (!c->md_cap_stream) YG_CUDA(cudaStreamCreateWithFlags(&c->md_cap_stream, cudaStreamNonBlocking));
+  cudaStream_t own = c->stream;
+  cudaGraph_t g;
+  YG_CUDA(cudaStreamBeginCapture(c->md_cap_stream, cudaStreamCaptureModeRelaxed));
+  c->stream = c->md_cap_stream;
+  const int64_t nalloc = c->alloc_calls;
+  int crc = md_step_device(c, factor, skin);
+  c->stream = own;
+  cudaError_t ce = cudaStreamEndCapture(c->md_cap_stream, &g);
+  if (crc) return crc;
+  if (ce != cudaSuccess) return yg_cuda_fail(ce, "cudaStreamEndCapture");
+  if (c->alloc_calls != nalloc) {
+    cudaGraphDestroy(g);
+    yg_set_error("a buffer was allocated while capturing the step");
+    return YG_ERR_STATE;
+  }
+  ce = cudaGraphInstantiate(&c->md_graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return yg_cuda_fail(ce, "cudaGraphInstantiate");
+  c->md_graph_valid = 1;
+  c->md_graph_skin = skin;
+  return YG_OK;
+}
+
+extern "C" {
+
+int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, int part_mask, double extra_energy,
+                int64_t max_steps) {
+  if (!c || !masses || !vel || !(dt > 0.0) || max_steps < 1) return YG_ERR_ARG;
+  if (!c->have_list) {
+    yg_set_error("yg_md_setup: build the neighbour list first");
+    return YG_ERR_STATE;
+  }
+  const int64_t N = c->natom;
+  std::vector<double> invm(N);
+  for (int64_t i = 0; i < N; i++) {
+    if (!(masses[i] > 0.0)) return YG_ERR_ARG;
+    invm[i] = 1.0 / masses[i];
+  }
+  int rc;
+  const int nb = yg_blocks(N * 3, 256);
+  md_drop_graph(c);
+  void **bufs[] = {(void **)&c->d_vel,      (void **)&c->d_invm,     (void **)&c->d_md_ekpart,
+                   (void **)&c->d_md_ekin,  (void **)&c->d_md_log,   (void **)&c->d_md_extra,
+                   (void **)&c->d_md_step,  (void **)&c->d_md_ctrl,  (void **)&c->d_snap_pos,
+                   (void **)&c->d_snap_vel, (void **)&c->d_snap_total, (void **)&c->d_snap_step};
+  for (void **b : bufs) yg_free(c, b);
+  if ((rc = yg_alloc(c, (void **)&c->d_vel, N * 3 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_invm, N * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_ekpart, (size_t)nb * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_ekin, sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_log, (size_t)(max_steps + 1) * 2 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_extra, sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_step, sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_ctrl, 16 * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_snap_pos, N * 3 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_snap_vel, N * 3 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_snap_total, (16 + N * 3) * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_snap_step, sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(c->d_vel, vel, N * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_invm, invm.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_md_extra, &extra_energy, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemsetAsync(c->d_md_step, 0, sizeof(int), c->stream));
+  YG_CUDA(cudaMemsetAsync(c->d_md_ctrl, 0, 16 * sizeof(int), c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->md_dt = dt;
+  c->md_mask = part_mask;
+  c->md_max_steps = max_steps;
+  c->md_steps_done = 0;
+  c->md_rebuilds = 0;
+  c->md_ready = 1;
+  // step 0: forces and energies at the initial positions (yaff's initialize);
+  // a kick with dt = 0 only evaluates the kinetic energy
+  if ((rc = md_force_async(c, 1))) return rc;
+  return md_finish_step(c, 0.0);
+}
+
+// Runs nsteps velocity-Verlet steps in batches of at most YG_MD_BATCH: each
+// batch snapshots the state, enqueues its steps (graph replay when
+// use_graph is set; the graph is captured on first use after one eager step
+// and again whenever the neighbour slots were reallocated), then reads the
+// status words once.  skin <= 0 rebuilds every step.
+int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nrebuild) {
+  if (!c || nsteps < 0) return YG_ERR_ARG;
+  if (!c->md_ready) {
+    yg_set_error("yg_md_run: call yg_md_setup first");
+    return YG_ERR_STATE;
+  }
+  if (c->md_steps_done + nsteps > c->md_max_steps) {
+    yg_set_error("yg_md_run: more steps than the energy log holds");
+    return YG_ERR_CAPACITY;
+  }
+  int rc;
+  const int64_t rmaxmax = std::max(c->rmax[0], std::max(c->rmax[1], c->rmax[2]));
+  const double factor = 2.0 * (double)(rmaxmax + 1);
+  const int64_t N = c->natom;
+  const int64_t reb0 = c->md_rebuilds;
+  int64_t left = nsteps;
+  int replays = 0;
+  if (c->md_graph_valid && c->md_graph_skin != skin) md_drop_graph(c);  // the skin is baked into the graph
+  while (left > 0) {
+    const int64_t nb = std::min<int64_t>(left, YG_MD_BATCH);
+    // snapshot
+    YG_CUDA(cudaMemcpyAsync(c->d_snap_pos, c->d_pos, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    YG_CUDA(cudaMemcpyAsync(c->d_snap_vel, c->d_vel, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    YG_CUDA(cudaMemcpyAsync(c->d_snap_total, c->d_total, (16 + N * 3) * sizeof(double), cudaMemcpyDeviceToDevice,
+                            c->stream));
+    YG_CUDA(cudaMemcpyAsync(c->d_snap_step, c->d_md_step, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    YG_CUDA(cudaMemsetAsync(c->d_status, 0, YG_ST_NWORDS * sizeof(int), c->stream));
+    for (int64_t s = 0; s < nb; s++) {
+      if (use_graph && c->md_graph_valid) {
+        YG_CUDA(cudaGraphLaunch(c->md_graph_exec, c->stream));
+        c->launches++;
+        continue;
+      }
+      // eager step (sizes every scratch buffer), then capture for the rest
+      if ((rc = md_step_device(c, factor, skin))) return rc;
+      if (use_graph) {
+        YG_CUDA(cudaStreamSynchronize(c->stream));
+        if ((rc = md_capture(c, factor, skin))) return rc;
+      }
+    }
+    // one readback per batch: status words and control words
+    YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    YG_CUDA(cudaMemcpyAsync(c->h_u64, c->d_md_ctrl, 16 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    YG_CUDA(cudaStreamSynchronize(c->stream));
+    const int *ctrl = (const int *)c->h_u64;
+    if (c->h_status[YG_ST_BADCELL]) {
+      yg_set_error("non-finite or huge position met while rebuilding the neighbour list");
+      return YG_ERR_NAN;
+    }
+    if (c->h_status[YG_ST_OVERFLOW]) {
+      if (++replays > 8) {
+        yg_set_error("neighbour slots kept overflowing during device rebuilds");
+        return YG_ERR_CAPACITY;
+      }
+      // roll back to the snapshot, grow the slots, rebuild at the first step
+      YG_CUDA(cudaMemcpyAsync(c->d_pos, c->d_snap_pos, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      YG_CUDA(cudaMemcpyAsync(c->d_vel, c->d_snap_vel, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      YG_CUDA(cudaMemcpyAsync(c->d_total, c->d_snap_total, (16 + N * 3) * sizeof(double), cudaMemcpyDeviceToDevice,
+                              c->stream));
+      YG_CUDA(cudaMemcpyAsync(c->d_md_step, c->d_snap_step, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+      int64_t cap = (int64_t)(c->h_status[YG_ST_MAXCOUNT] * 1.15) + 64;
+      cap = (cap + 31) / 32 * 32;
+      if (cap > c->nbr_cap) c->nbr_cap = cap;
+      if (c->nbr_cap * N > c->nbr_alloc) {
+        yg_free(c, (void **)&c->d_nbr);
+        if ((rc = yg_alloc(c, (void **)&c->d_nbr, (size_t)(c->nbr_cap * N) * sizeof(uint2)))) return rc;
+        c->nbr_alloc = c->nbr_cap * N;
+      }
+      md_drop_graph(c);
+      k_set_int<<<1, 32, 0, c->stream>>>(c->d_md_ctrl + 1, 1);
+      YG_LAUNCH_CHECK(c, "k_set_int");
+      k_set_int<<<1, 32, 0, c->stream>>>(c->d_md_ctrl + 2, (int)c->md_rebuilds);
+      YG_LAUNCH_CHECK(c, "k_set_int");
+      continue;
+    }
+    if (ctrl[2] != (int)c->md_rebuilds) c->nneigh = (int64_t)(c->h_u64[2] / 2);
+    c->md_rebuilds = ctrl[2];
+    c->md_steps_done += nb;
+    left -= nb;
+  }
+  c->list_recomputed = 1;
+  for (int p = 0; p < YG_NPART; p++) c->part_valid[p] = 0;
+  if (nrebuild) *nrebuild = c->md_rebuilds - reb0;
+  return YG_OK;
+}
+
+// Copies positions, velocities (natom x 3, may be NULL) and the energy log
+// ((steps done + 1) x (epot, ekin), may be NULL) to host memory.
+int yg_md_get(yg_ctx *c, double *pos, double *vel, double *log, int64_t *nlog) {
+  if (!c || !c->md_ready) return YG_ERR_STATE;
+  if (pos) YG_CUDA(cudaMemcpyAsync(pos, c->d_pos, c->natom * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (vel) YG_CUDA(cudaMemcpyAsync(vel, c->d_vel, c->natom * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  const int64_t n = c->md_steps_done + 1;
+  if (log) YG_CUDA(cudaMemcpyAsync(log, c->d_md_log, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  if (nlog) *nlog = n;
+  if (log && std::isnan(log[2 * (n - 1)])) {
+    yg_set_error("not-a-number energy in the trajectory");
+    return YG_ERR_NAN;
+  }
+  return YG_OK;
+}
+
+}  // extern "C"

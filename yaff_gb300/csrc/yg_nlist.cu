@@ -26,9 +26,10 @@
 
 namespace {
 
-__global__ void k_bin(const double *__restrict__ pos, int64_t natom, CellGeom cell, GridGeom grid,
+__global__ void k_bin(const int *__restrict__ gate, const double *__restrict__ pos, int64_t natom, CellGeom cell, GridGeom grid,
                       int *__restrict__ cell_of, int *__restrict__ wimg, int *__restrict__ count,
                       int *__restrict__ status) {
+  if (gate && !*gate) return;
   int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a >= natom) return;
   double p[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
@@ -59,8 +60,9 @@ __global__ void k_bin(const double *__restrict__ pos, int64_t natom, CellGeom ce
 }
 
 // Exclusive scan of the per-cell counts (one block; cell counts are small).
-__global__ void k_scan_cells(const int *__restrict__ count, int ncell, int *__restrict__ start,
+__global__ void k_scan_cells(const int *__restrict__ gate, const int *__restrict__ count, int ncell, int *__restrict__ start,
                              int *__restrict__ fill) {
+  if (gate && !*gate) return;
   __shared__ int warp_sums[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -100,8 +102,9 @@ __global__ void k_scan_cells(const int *__restrict__ count, int ncell, int *__re
   if (threadIdx.x == 0) start[ncell] = carry;
 }
 
-__global__ void k_scatter(const int *__restrict__ cell_of, int64_t natom, int *__restrict__ fill,
+__global__ void k_scatter(const int *__restrict__ gate, const int *__restrict__ cell_of, int64_t natom, int *__restrict__ fill,
                           int *__restrict__ sorted) {
+  if (gate && !*gate) return;
   int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a >= natom) return;
   int slot = atomicAdd(fill + cell_of[a], 1);
@@ -113,7 +116,8 @@ __global__ void k_scatter(const int *__restrict__ cell_of, int64_t natom, int *_
 // entries of the cell through shuffles (indices are distinct), then writes
 // them to their final slots.  Cells with more than 128 atoms (pathological
 // densities) fall back to an insertion sort by lane 0.
-__global__ void k_sort_cells(const int *__restrict__ start, int ncell, int *__restrict__ sorted) {
+__global__ void k_sort_cells(const int *__restrict__ gate, const int *__restrict__ start, int ncell, int *__restrict__ sorted) {
+  if (gate && !*gate) return;
   const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= ncell) return;
@@ -154,9 +158,10 @@ __global__ void k_sort_cells(const int *__restrict__ start, int ncell, int *__re
 }
 
 // Cell origin (FP64) of every sorted atom and the orig -> sorted map.
-__global__ void k_origins(const int *__restrict__ sorted, const int *__restrict__ cell_of,
+__global__ void k_origins(const int *__restrict__ gate, const int *__restrict__ sorted, const int *__restrict__ cell_of,
                           const int *__restrict__ wimg, int64_t natom, CellGeom cell, GridGeom grid,
                           double *__restrict__ org, int *__restrict__ rank) {
+  if (gate && !*gate) return;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= natom) return;
   int a = sorted[s];
@@ -232,6 +237,7 @@ struct BuildArgs {
   float lo, hi;     // FP32 guard band on d^2
   int fast;
   int filter;       // nlow/nhigh restrict the pairs
+  const int *gate;  // device flag: build only when set (nullptr: always)
 };
 
 // Exact replay of the reference's decision for candidate (oi -> oj) whose
@@ -285,6 +291,7 @@ __device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, 
 // chunks and recover each candidate's x offset from the cell boundaries of
 // the run (kept in registers).
 __global__ void __launch_bounds__(256, 3) k_build(BuildArgs A) {
+  if (A.gate && !*A.gate) return;
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (i >= A.natom) return;
@@ -486,8 +493,9 @@ __global__ void k_max_disp2(const double *__restrict__ pos, const double *__rest
 
 // Repacks the per-atom pair parameters into sorted order:
 // for every potential p: sigma, sqrt(epsilon), radius^2, onlypauli.
-__global__ void k_pack_params(const double *__restrict__ src, const int *__restrict__ sorted, int64_t natom,
+__global__ void k_pack_params(const int *__restrict__ gate, const double *__restrict__ src, const int *__restrict__ sorted, int64_t natom,
                               double *__restrict__ dst64, float *__restrict__ dst32) {
+  if (gate && !*gate) return;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= natom) return;
   int a = sorted[s];
@@ -526,6 +534,7 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.hi = 0.0f;
   A.fast = 0;
   A.filter = (ctx->nlow > 0 || ctx->nhigh < ctx->natom) ? 1 : 0;
+  A.gate = nullptr;
   return A;
 }
 
@@ -537,9 +546,9 @@ int yg_pack_pair_params(yg_ctx *ctx) {
   size_t n = (size_t)ctx->natom * 4 * YG_MAX_POT;
   int rc;
   if (!ctx->d_pp64) {
-    if ((rc = yg_alloc((void **)&ctx->d_pp_src, n * sizeof(double)))) return rc;
-    if ((rc = yg_alloc((void **)&ctx->d_pp64, n * sizeof(double)))) return rc;
-    if ((rc = yg_alloc((void **)&ctx->d_pp32, n * sizeof(float)))) return rc;
+    if ((rc = yg_alloc(ctx, (void **)&ctx->d_pp_src, n * sizeof(double)))) return rc;
+    if ((rc = yg_alloc(ctx, (void **)&ctx->d_pp64, n * sizeof(double)))) return rc;
+    if ((rc = yg_alloc(ctx, (void **)&ctx->d_pp32, n * sizeof(float)))) return rc;
     ctx->pp_dirty = 1;
   }
   if (ctx->pp_dirty) {
@@ -559,7 +568,7 @@ int yg_pack_pair_params(yg_ctx *ctx) {
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->pp_dirty = 0;
   }
-  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(ctx->d_pp_src, ctx->d_sorted, ctx->natom,
+  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(nullptr, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
                                                                      ctx->d_pp64, ctx->d_pp32);
   YG_LAUNCH_CHECK(ctx, "k_pack_params");
   ctx->pp_packed = 1;
@@ -571,6 +580,15 @@ int yg_launch_prep_positions(yg_ctx *ctx) {
       ctx->d_pos, ctx->have_charges ? ctx->d_charge : nullptr, ctx->d_sorted, ctx->d_org, ctx->d_cell_of,
       ctx->grid.n[0], ctx->natom, ctx->d_x64, ctx->d_x32, ctx->d_xb);
   YG_LAUNCH_CHECK(ctx, "k_prep");
+  return YG_OK;
+}
+
+// Largest squared displacement since the last rebuild, as the bits of a
+// non-negative double, max-combined into *out (which the caller zeroes).
+int yg_launch_max_disp2_async(yg_ctx *ctx, unsigned long long *out) {
+  k_max_disp2<<<yg_blocks(ctx->natom, 256) > 1024 ? 1024 : yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(
+      ctx->d_pos, ctx->d_pos_build, ctx->natom, out);
+  YG_LAUNCH_CHECK(ctx, "k_max_disp2");
   return YG_OK;
 }
 
@@ -589,10 +607,13 @@ int yg_launch_max_disp2(yg_ctx *ctx, double *out) {
   return YG_OK;
 }
 
-int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
-  const int64_t N = ctx->natom;
+// Host-side geometry of a build for the current cell and cutoff: the cell
+// grid, the stencil shift vectors (uploaded) and the FP32 guard band.  Kept
+// until the cell or the cutoff changes.
+static int nlist_geometry(yg_ctx *ctx, double rc2) {
+  const double rc = ctx->rcut_total;
+  if (ctx->geom_valid && ctx->geom_rc == rc) return YG_OK;
   const CellGeom &C = ctx->cell;
-  double rc = ctx->rcut_total;
   // grid: cells at least rc/2 wide along each plane normal
   GridGeom G;
   double rsp[3];
@@ -615,12 +636,10 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   }
   int rc_ = YG_OK;
   if (G.ncell + 1 > ctx->cap_sorted) {
-    cudaFree(ctx->d_cell_start);
-    cudaFree(ctx->d_cell_fill);
-    ctx->d_cell_start = nullptr;
-    ctx->d_cell_fill = nullptr;
-    if ((rc_ = yg_alloc((void **)&ctx->d_cell_start, (G.ncell + 1) * sizeof(int)))) return rc_;
-    if ((rc_ = yg_alloc((void **)&ctx->d_cell_fill, (G.ncell + 1) * sizeof(int)))) return rc_;
+    yg_free(ctx, (void **)&ctx->d_cell_start);
+    yg_free(ctx, (void **)&ctx->d_cell_fill);
+    if ((rc_ = yg_alloc(ctx, (void **)&ctx->d_cell_start, (G.ncell + 1) * sizeof(int)))) return rc_;
+    if ((rc_ = yg_alloc(ctx, (void **)&ctx->d_cell_fill, (G.ncell + 1) * sizeof(int)))) return rc_;
     ctx->cap_sorted = G.ncell + 1;
   }
   ctx->grid = G;
@@ -639,33 +658,13 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
         sh32[idx] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.0f);
         maxsh = std::max(maxsh, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
       }
-  cudaFree(ctx->d_shift64);
-  cudaFree(ctx->d_shift32);
-  ctx->d_shift64 = nullptr;
-  ctx->d_shift32 = nullptr;
-  if ((rc_ = yg_alloc((void **)&ctx->d_shift64, sh64.size() * sizeof(double)))) return rc_;
-  if ((rc_ = yg_alloc((void **)&ctx->d_shift32, sh32.size() * sizeof(float4)))) return rc_;
+  // grow-only: buffers keep their addresses across rebuilds (captured graphs
+  // refer to them)
+  if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_shift64, &ctx->shift64_cap, sh64.size() * sizeof(double)))) return rc_;
+  if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_shift32, &ctx->shift32_cap, sh32.size() * sizeof(float4)))) return rc_;
   YG_CUDA(cudaMemcpyAsync(ctx->d_shift64, sh64.data(), sh64.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_shift32, sh32.data(), sh32.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-
-  // bin + deterministic counting sort
-  YG_CUDA(cudaMemsetAsync(ctx->d_status, 0, YG_ST_NWORDS * sizeof(int), ctx->stream));
-  YG_CUDA(cudaMemsetAsync(ctx->d_cell_fill, 0, (G.ncell + 1) * sizeof(int), ctx->stream));
-  YG_CUDA(cudaMemcpyAsync(ctx->d_pos_build, ctx->d_pos, N * 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  k_bin<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_pos, N, C, G, ctx->d_cell_of, ctx->d_wimg,
-                                                    ctx->d_cell_fill, ctx->d_status);
-  YG_LAUNCH_CHECK(ctx, "k_bin");
-  k_scan_cells<<<1, 1024, 0, ctx->stream>>>(ctx->d_cell_fill, G.ncell, ctx->d_cell_start, ctx->d_cell_fill);
-  YG_LAUNCH_CHECK(ctx, "k_scan_cells");
-  k_scatter<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_cell_of, N, ctx->d_cell_fill, ctx->d_sorted);
-  YG_LAUNCH_CHECK(ctx, "k_scatter");
-  k_sort_cells<<<yg_blocks((int64_t)G.ncell * 32, 256), 256, 0, ctx->stream>>>(ctx->d_cell_start, G.ncell,
-                                                                                ctx->d_sorted);
-  YG_LAUNCH_CHECK(ctx, "k_sort_cells");
-  k_origins<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_sorted, ctx->d_cell_of, ctx->d_wimg, N, C, G,
-                                                        ctx->d_org, ctx->d_rank);
-  YG_LAUNCH_CHECK(ctx, "k_origins");
-  if ((rc_ = yg_launch_prep_positions(ctx))) return rc_;
+  YG_CUDA(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
 
   // FP32 guard band: bound on |d2_fp32 - d2_exact| from the magnitudes of the
   // cell-local coordinates (< one cell diagonal) and the shift vectors.
@@ -686,40 +685,90 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   err *= 4.0;  // safety factor
   double min_half = 0.5 * std::min(rsp[0], std::min(rsp[1], rsp[2]));
   ctx->fast_path = (rc * (1.0 + 1e-7) + 1e-7 < min_half) ? 1 : 0;
+  float lo = (float)(rc2 - err), hi = (float)(rc2 + err);
+  // make the band closed under FP32 rounding of the thresholds themselves
+  ctx->band_lo = nextafterf(nextafterf(lo, 0.0f), 0.0f);
+  ctx->band_hi = nextafterf(nextafterf(hi, INFINITY), INFINITY);
 
   // neighbour slots
   if (ctx->nbr_cap == 0) {
-    double dens = N / C.volume;
+    double dens = ctx->natom / C.volume;
     double est = dens * 4.18879020478639 * rc * rc * rc;  // 4/3 pi rc^3
     int64_t cap = (int64_t)(est * 1.3) + 64;
     cap = (cap + 31) / 32 * 32;
     ctx->nbr_cap = cap;
   }
+  ctx->geom_rc = rc;
+  ctx->geom_valid = 1;
+  return YG_OK;
+}
+
+__global__ void k_build_reset(const int *__restrict__ gate, int *__restrict__ cell_fill, int ncell1,
+                              const double *__restrict__ pos, double *__restrict__ pos_build, int64_t n3,
+                              unsigned long long *__restrict__ total) {
+  if (gate && !*gate) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int64_t t = t0; t < ncell1; t += stride) cell_fill[t] = 0;
+  for (int64_t t = t0; t < n3; t += stride) pos_build[t] = pos[t];
+  if (t0 == 0) *total = 0ull;
+}
+
+// Enqueues one build for the current positions (no host synchronization):
+// reset, bin, counting sort, origins, cell-local coordinates, candidate
+// sweep.  With a gate, every kernel returns at once unless *gate is set.
+static int enqueue_build(yg_ctx *ctx, double rc2, const int *gate, unsigned long long *total) {
+  const int64_t N = ctx->natom;
+  const CellGeom &C = ctx->cell;
+  const GridGeom &G = ctx->grid;
+  const int64_t n3 = N * 3;
+  const int64_t big = std::max<int64_t>(n3, G.ncell + 1);
+  k_build_reset<<<(int)std::min<int64_t>(yg_blocks(big, 256), 1024), 256, 0, ctx->stream>>>(
+      gate, ctx->d_cell_fill, G.ncell + 1, ctx->d_pos, ctx->d_pos_build, n3, total);
+  YG_LAUNCH_CHECK(ctx, "k_build_reset");
+  k_bin<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(gate, ctx->d_pos, N, C, G, ctx->d_cell_of, ctx->d_wimg,
+                                                    ctx->d_cell_fill, ctx->d_status);
+  YG_LAUNCH_CHECK(ctx, "k_bin");
+  k_scan_cells<<<1, 1024, 0, ctx->stream>>>(gate, ctx->d_cell_fill, G.ncell, ctx->d_cell_start, ctx->d_cell_fill);
+  YG_LAUNCH_CHECK(ctx, "k_scan_cells");
+  k_scatter<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(gate, ctx->d_cell_of, N, ctx->d_cell_fill, ctx->d_sorted);
+  YG_LAUNCH_CHECK(ctx, "k_scatter");
+  k_sort_cells<<<yg_blocks((int64_t)G.ncell * 32, 256), 256, 0, ctx->stream>>>(gate, ctx->d_cell_start, G.ncell,
+                                                                                ctx->d_sorted);
+  YG_LAUNCH_CHECK(ctx, "k_sort_cells");
+  k_origins<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(gate, ctx->d_sorted, ctx->d_cell_of, ctx->d_wimg, N, C, G,
+                                                        ctx->d_org, ctx->d_rank);
+  YG_LAUNCH_CHECK(ctx, "k_origins");
+  int rc_;
+  if ((rc_ = yg_launch_prep_positions(ctx))) return rc_;
+  BuildArgs A = make_args(ctx, rc2);
+  A.fast = ctx->fast_path;
+  A.lo = ctx->band_lo;
+  A.hi = ctx->band_hi;
+  A.total = total;
+  A.gate = gate;
+  k_build<<<yg_blocks(N * 32, 256), 256, 0, ctx->stream>>>(A);
+  YG_LAUNCH_CHECK(ctx, "k_build");
+  return YG_OK;
+}
+
+int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
+  int rc_;
+  if ((rc_ = nlist_geometry(ctx, rc2))) return rc_;
+  const int64_t N = ctx->natom;
   for (;;) {
     int64_t need = ctx->nbr_cap * N;
     if (need > ctx->nbr_alloc) {
-      cudaFree(ctx->d_nbr);
-      ctx->d_nbr = nullptr;
-      if ((rc_ = yg_alloc((void **)&ctx->d_nbr, (size_t)need * sizeof(uint2)))) return rc_;
+      yg_free(ctx, (void **)&ctx->d_nbr);
+      if ((rc_ = yg_alloc(ctx, (void **)&ctx->d_nbr, (size_t)need * sizeof(uint2)))) return rc_;
       ctx->nbr_alloc = need;
     }
-    BuildArgs A = make_args(ctx, rc2);
-    A.fast = ctx->fast_path;
-    A.lo = (float)(rc2 - err);
-    A.hi = (float)(rc2 + err);
-    // make the band closed under FP32 rounding of the thresholds themselves
-    A.lo = nextafterf(nextafterf(A.lo, 0.0f), 0.0f);
-    A.hi = nextafterf(nextafterf(A.hi, INFINITY), INFINITY);
     unsigned long long *dtot = (unsigned long long *)ctx->d_red;
-    YG_CUDA(cudaMemsetAsync(dtot, 0, sizeof(unsigned long long), ctx->stream));
     YG_CUDA(cudaMemsetAsync(ctx->d_status, 0, YG_ST_NWORDS * sizeof(int), ctx->stream));
-    A.total = dtot;
-    int64_t threads = N * 32;
-    k_build<<<yg_blocks(threads, 256), 256, 0, ctx->stream>>>(A);
-    YG_LAUNCH_CHECK(ctx, "k_build");
+    if ((rc_ = enqueue_build(ctx, rc2, nullptr, dtot))) return rc_;
     YG_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    unsigned long long total = 0;
-    YG_CUDA(cudaMemcpyAsync(&total, dtot, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long *htot = ctx->h_u64;
+    YG_CUDA(cudaMemcpyAsync(htot, dtot, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (ctx->h_status[YG_ST_BADCELL]) {
       yg_set_error("non-finite or huge position met while binning atoms");
@@ -731,7 +780,7 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
       if (retry) (*retry)++;
       continue;
     }
-    ctx->nneigh = (int64_t)(total / 2);
+    ctx->nneigh = (int64_t)(*htot / 2);
     break;
   }
   ctx->have_list = 1;
@@ -741,12 +790,29 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   return YG_OK;
 }
 
+// A rebuild that runs only when *gate is set, for the device-driven step:
+// no host synchronization; overflow and bad positions accumulate in the
+// status words (cleared by the caller), the pair count goes to *total.
+int yg_launch_nlist_build_gated(yg_ctx *ctx, const int *gate, unsigned long long *total) {
+  int rc_;
+  if (!ctx->geom_valid || !ctx->have_list) {
+    yg_set_error("gated rebuild needs a host build first");
+    return YG_ERR_STATE;
+  }
+  const double rc2 = ctx->rcut_total * ctx->rcut_total;
+  if ((rc_ = enqueue_build(ctx, rc2, gate, total))) return rc_;
+  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(gate, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
+                                                                     ctx->d_pp64, ctx->d_pp32);
+  YG_LAUNCH_CHECK(ctx, "k_pack_params");
+  return YG_OK;
+}
+
 int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, int64_t *n) {
   int64_t want = ctx->nneigh;
   *n = want;
   if (want > cap || rows_host == nullptr) return YG_OK;
   yg_neigh_row *d_rows = nullptr;
-  int rc = yg_alloc((void **)&d_rows, (size_t)(want > 0 ? want : 1) * sizeof(yg_neigh_row));
+  int rc = yg_alloc(ctx, (void **)&d_rows, (size_t)(want > 0 ? want : 1) * sizeof(yg_neigh_row));
   if (rc) return rc;
   unsigned long long *dcount = (unsigned long long *)ctx->d_red;
   YG_CUDA(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), ctx->stream));
@@ -763,7 +829,7 @@ int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, in
   YG_CUDA(cudaMemcpyAsync(&got, dcount, sizeof(got), cudaMemcpyDeviceToHost, ctx->stream));
   YG_CUDA(cudaMemcpyAsync(rows_host, d_rows, (size_t)want * sizeof(yg_neigh_row), cudaMemcpyDeviceToHost, ctx->stream));
   YG_CUDA(cudaStreamSynchronize(ctx->stream));
-  cudaFree(d_rows);
+  yg_free(ctx, (void **)&d_rows);
   if ((int64_t)got != want) {
     yg_set_error("neighbour export row count differs from the build count");
     return YG_ERR_STATE;

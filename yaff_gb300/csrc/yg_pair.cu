@@ -566,7 +566,7 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   const int nblocks = yg_blocks(N * 32, 256);
   const int nval = npot * 7;
   int rc;
-  if ((rc = yg_ensure((void **)&ctx->d_red, &ctx->red_cap,
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap,
                       ((size_t)nblocks * nval + 64 + nval) * sizeof(double))))
     return rc;
   A.partial = ctx->d_red + 64;

@@ -176,7 +176,7 @@ int yg_launch_valence(yg_ctx *ctx, int want_grad) {
   const int nbd = yg_blocks(ctx->ndelta, 256);
   int rc;
   size_t need = 64 + (size_t)nbt + 1 + (size_t)nbd * 9 + 9;
-  if ((rc = yg_ensure((void **)&ctx->d_red, &ctx->red_cap, need * sizeof(double)))) return rc;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, need * sizeof(double)))) return rc;
   double *ep = ctx->d_red + 64;
   double *esum = ep + nbt;
   double *vp = esum + 1;

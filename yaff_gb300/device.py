@@ -28,11 +28,12 @@ def get_default_precision():
     return _default_precision
 
 
-def device_of(system, precision=None):
-    """The DeviceSystem of a System, created on first use."""
+def device_of(system, precision=None, stream=None):
+    """The DeviceSystem of a System, created on first use (on `stream`, a
+    cudaStream_t handle as int, default: the legacy default stream)."""
     dev = getattr(system, '_device', None)
     if dev is None:
-        dev = DeviceSystem(system, _default_precision if precision is None else precision)
+        dev = DeviceSystem(system, _default_precision if precision is None else precision, stream=stream)
         system._device = dev
     elif precision is not None:
         dev.set_precision(precision)
@@ -49,7 +50,9 @@ class DeviceSystem(object):
             precision = _lib.PRECISIONS[precision]
         self.precision = precision
         handle = ctypes.c_void_p()
-        check(self.lib.yg_create(self.natom, precision, stream, ctypes.byref(handle)), 'yg_create')
+        self.stream = stream
+        check(self.lib.yg_create(self.natom, precision, None if stream is None else ctypes.c_void_p(stream),
+                                 ctypes.byref(handle)), 'yg_create')
         self.ctx = handle
         self._cell_key = None
         self._charges_key = None
@@ -169,6 +172,19 @@ class DeviceSystem(object):
 
     def launch_count(self):
         return int(self.lib.yg_launch_count(self.ctx))
+
+    def mem_usage(self):
+        """(bytes now, high-water bytes) of device memory this system holds."""
+        now, high = ctypes.c_int64(), ctypes.c_int64()
+        check(self.lib.yg_mem_usage(self.ctx, ctypes.byref(now), ctypes.byref(high)), 'yg_mem_usage')
+        return now.value, high.value
+
+    def destroy(self):
+        """Releases the device state now (stream-ordered; no device sync)."""
+        ctx = getattr(self, 'ctx', None)
+        if ctx is not None and ctx.value:
+            check(self.lib.yg_destroy(ctx), 'yg_destroy')
+        self.ctx = None
 
     def sync(self):
         check(self.lib.yg_sync(self.ctx), 'yg_sync')

@@ -210,6 +210,25 @@ class ForceField(ForcePart):
             vtens[:] = v + host_vtens
         return energy
 
+    def device_md_terms(self):
+        """(result-slot mask, constant energy) for an integrator that sums the
+        force on the device: the slots the fused path fills, and the
+        neutralizing-background energy, which is evaluated on the host and
+        does not depend on the positions.  Valid after one compute()."""
+        dev = self._device_parts()
+        if dev is None:
+            raise NotImplementedError('the on-device integrator needs every part on the fused device path')
+        mask = 0
+        const = 0.0
+        for part in self.parts:
+            if isinstance(part, ForcePartEwaldNeutralizing):
+                const += part.compute()
+            elif isinstance(part, ForcePartPair):
+                mask |= 1 << part._register()
+            else:
+                mask |= 1 << part.device_slot
+        return dev, mask, const
+
 
 class ForcePartPair(ForcePart):
     """A pairwise non-bonding term evaluated over the shared neighbour list."""
