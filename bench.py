@@ -42,6 +42,7 @@ def parse():
                     help='requests of the serving workload run after the main measurement (0: skip)')
     ap.add_argument('--serving-rate', type=float, default=200.0, help='Poisson arrival rate, requests/s')
     ap.add_argument('--serving-slots', type=int, default=16)
+    ap.add_argument('--mc-rounds', type=int, default=10, help='MC trial-energy batches per precision (0: skip)')
     return ap.parse_args()
 
 
@@ -443,6 +444,53 @@ def run_serving(args):
     return s
 
 
+def run_mc(args):
+    """MC trial energies: 256 chains on one 2,000-atom framework (0-400 rigid
+    waters each), every chain submitting a request of 64 insertion /
+    deletion / translation trials; all pending requests go in one launch.
+    Host trial arrays in, energies out (H2D + D2H inside the timing)."""
+    import torch
+    from yaff_gb300 import configs
+    from yaff_gb300.mc import MCTrials
+    from yaff_gb300.system import Cell
+    work = configs.mc_workload()
+    cell = Cell(work['framework']['rvecs'])
+    nchain = len(work['chains'])
+    eng = MCTrials(work['framework'], work['guest'], cell, work['rcut'], work['alpha'], work['gcut'], nchain,
+                   work['max_guests'], close_contact=work['close_contact'], precision='mixed')
+    for c, g in enumerate(work['chains']):
+        eng.set_chain(c, g)
+    rng = np.random.default_rng(9)
+    batches = [configs.mc_trial_batch(rng, work, work['chains'], 64) for _ in range(args.mc_rounds + 2)]
+    out = {'workload': '256 chains x 64 trials per request (1/3 each insertion, deletion, translation of a rigid '
+                       'water), 2,000-atom framework in a 30 A cube, 0-400 guests per chain, rcut 12 A, Ewald '
+                       'alpha 3.5/rcut, gcut 1.1 alpha, close contact 0.4 A; one launch per 256 requests',
+           'trials_per_launch': int(len(batches[0][0])), 'nk': int(eng.prefactors().astype(bool).sum())}
+    energies = {}
+    for prec in ('mixed', 'fp64'):
+        eng.set_precision(prec)
+        for b in batches[:2]:
+            eng.trials(*b)
+        torch.cuda.synchronize()
+        lat = []
+        for b in batches[2:]:
+            t0 = time.perf_counter()
+            e = eng.trials(*b)
+            lat.append(time.perf_counter() - t0)
+        energies[prec] = eng.trials(*batches[2])
+        lat = np.array(lat)
+        out[prec] = {'trials_per_s': float(len(batches[0][0]) / lat.mean()),
+                     'request_latency_ms': {'p50': float(np.percentile(lat, 50) * 1e3),
+                                            'p99': float(np.percentile(lat, 99) * 1e3)}}
+    ok = np.abs(energies['fp64']) < 1e9
+    rel = np.abs(energies['mixed'][ok] - energies['fp64'][ok]) / np.maximum(np.abs(energies['fp64'][ok]), 1e-3)
+    out['mixed_vs_fp64_max_rel_err'] = float(rel.max())
+    out['close_contact_trials'] = int((~ok).sum())
+    out['speedup_mixed_vs_fp64'] = out['mixed']['trials_per_s'] / out['fp64']['trials_per_s']
+    eng.destroy()
+    return out
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -462,6 +510,8 @@ def main():
     if rank == 0:
         if args.serving_requests > 0 and world == 1:
             out['serving'] = run_serving(args)
+        if args.mc_rounds > 0 and world == 1:
+            out['mc_trials'] = run_mc(args)
         if not args.no_cpu_baseline:
             out['cpu_baseline'] = cpu_sample(args.natom)
         print(json.dumps(out))

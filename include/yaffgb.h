@@ -237,6 +237,76 @@ int yg_ewald_corr_noalloc(const double *pos, const double *charges, int64_t nato
                           double alpha, double dielectric, int64_t nlow, int64_t nhigh,
                           double *energy, double *gpos, double *vtens, void *stream);
 
+/* ------------------------------------------------ MC trial energies ---- */
+
+/* compute_ewald_prefactors (yaff/pes/ewald.c:441-471): fac1 exp(-k^2/4a^2)/k^2
+ * for every k of the half sphere |k| <= 2 pi gcut, in the reference's dense
+ * layout (2 gmax0+1) x (2 gmax1+1) x (gmax2+1) with the element of each k one
+ * position after its loop index (ewald.c:457); prefactors must hold that
+ * many doubles and is overwritten where k is inside the cutoff (the
+ * reference writes one element past the array when the last loop index is
+ * inside the cutoff; that element is dropped here).  Host FP64 set-up. */
+int yg_ewald_prefactors(const double *gvecs, double volume, double alpha,
+                        const int64_t *gmax, double gcut, double *prefactors);
+
+/* compute_ewald_structurefactors (ewald.c:473-506): q cos(k.r) and q sin(k.r)
+ * summed over the atoms, ADDED to cosfacs / sinfacs (host arrays, same dense
+ * layout).  Evaluated on the GPU in FP64 on `stream`. */
+int yg_ewald_structurefactors(const double *pos, int64_t natom, const double *charges,
+                              const double *rvecs, const double *gvecs, double volume,
+                              const int64_t *gmax, double gcut, double *cosfacs,
+                              double *sinfacs, void *stream);
+
+/* compute_ewald_deltae (ewald.c:508-522): 2 sum pref (cos dcos + sin dsin)
+ * over nk elements of host arrays, on the GPU. */
+int yg_ewald_deltae(const double *prefactors, const double *deltacosfacs,
+                    const double *cosfacs, const double *deltasinfacs,
+                    const double *sinfacs, int64_t nk, double *out);
+
+/* Batched trial energies of rigid-guest moves (the trial path of
+ * yaff/sampling/mctrials.py:69-126 with reci_ei = 'ewald_interaction',
+ * mc.py:596-597).  A context holds a rigid framework (nframe atoms with
+ * charges and LJ sigma/epsilon), the guest template (guest_natom <= 4
+ * atoms) and nchain chains of up to max_guests guests each, with each
+ * chain's structure factors resident in HBM.  rmax: real-space image range
+ * (ceil(rcut/spacing - 0.5)); close_contact: the reference's close-contact
+ * distance (a side of a trial within it counts 1e10; negative: off).
+ * precision: YG_FP64 or YG_MIXED (FP32 pair terms and sincos on FP64
+ * relative vectors and reduced phases, FP64 sums). */
+typedef struct yg_mc yg_mc;
+int yg_mc_create(const double *rvecs, const double *gvecs, double volume, const int64_t *rmax,
+                 double rcut, double alpha, double gcut, const int64_t *gmax, double dielectric,
+                 double close_contact, int64_t nframe, const double *frame_pos,
+                 const double *frame_charges, const double *frame_sigma,
+                 const double *frame_epsilon, int64_t guest_natom, const double *guest_charges,
+                 const double *guest_sigma, const double *guest_epsilon, int64_t nchain,
+                 int64_t max_guests, int precision, void *stream, yg_mc **out);
+int yg_mc_destroy(yg_mc *mc);
+int yg_mc_set_precision(yg_mc *mc, int precision);
+/* Sets a chain's guests (nguest x guest_natom x 3 host positions) and
+ * recomputes its structure factors (framework + guests). */
+int yg_mc_set_chain(yg_mc *mc, int64_t chain, int64_t nguest, const double *guest_pos);
+/* Reads a chain back: guest count, positions and structure factors in the
+ * reference's dense layout (any pointer may be NULL). */
+int yg_mc_get_chain(yg_mc *mc, int64_t chain, int64_t *nguest, double *guest_pos,
+                    double *cosfacs, double *sinfacs);
+/* The prefactor array of the context (dense layout; *nk_dense elements). */
+int yg_mc_prefactors(yg_mc *mc, double *prefactors, int64_t *nk_dense);
+/* Energy differences of ntrial trials (host arrays): kind 0 inserts a guest
+ * at newpos, 1 deletes guest `guest`, 2 translates guest `guest` to newpos
+ * (newpos: ntrial x guest_natom x 3, rows of deletions ignored).  Each is the
+ * reference's U(after) - U(before) against the chain's current state: the
+ * guest's LJ + real-space EI with the framework and the other guests and
+ * its reciprocal interaction through the structure factors. */
+int yg_mc_trials(yg_mc *mc, int64_t ntrial, const int32_t *chain, const int32_t *kind,
+                 const int32_t *guest, const double *newpos, double *energy);
+/* Accepts trials of the last batch (at most one per chain): positions and
+ * structure factors are updated on the device as the reference's accept()
+ * does (mctrials.py:177-190); a deletion moves the chain's last guest into
+ * the freed slot. */
+int yg_mc_apply(yg_mc *mc, int64_t napply, const int32_t *trial_index);
+int64_t yg_mc_launch_count(yg_mc *mc);
+
 /* Measurement utility (no reference counterpart): FMA-chain throughput of
  * the FP32 (fp64 == 0) or FP64 CUDA-core pipe in TFLOP/s (FMA = 2 flops), the
  * roofline denominator of the pair and Ewald kernels.  Negative on error. */

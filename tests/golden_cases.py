@@ -10,7 +10,27 @@ GOLDEN = os.path.join(HERE, 'golden')
 
 
 def case_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz')))
+    """Force-field cases (the mc_* fixtures hold MC trial cases)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz'))
+                  if not os.path.basename(p).startswith('mc_'))
+
+
+def mc_case_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, 'mc_*.npz')))
+
+
+def load_mc(name):
+    """(case, data) of an MC trial fixture: case in the layout of
+    configs.mc_workload, data the raw arrays (chain, trials, reference
+    energies, prefactor and structure-factor arrays)."""
+    d = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
+    case = {'framework': {'pos': d['frame_pos'], 'charges': d['frame_charges'], 'sigmas': d['frame_sigmas'],
+                          'epsilons': d['frame_epsilons'], 'rvecs': d['rvecs']},
+            'guest': {'pos': d['guest_pos'], 'charges': d['guest_charges'], 'sigmas': d['guest_sigmas'],
+                      'epsilons': d['guest_epsilons']},
+            'rcut': float(d['rcut']), 'alpha': float(d['alpha']), 'gcut': float(d['gcut']),
+            'close_contact': float(d['close_contact'])}
+    return case, d
 
 
 def load(name):

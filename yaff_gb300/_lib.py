@@ -74,7 +74,20 @@ SIGNATURES = {
     'yg_md_setup': (_I, [_P, _P, _P, _D, _I, _D, _I64]),
     'yg_md_run': (_I, [_P, _I64, _I, _D, ctypes.POINTER(_I64)]),
     'yg_md_get': (_I, [_P, _P, _P, _P, ctypes.POINTER(_I64)]),
-    'yg_ewald_corr_noalloc': (_I, [_P, _P, _I64, _P, _P, _P, _I64, _P, _P, _D, _D, _D, _I64, _I64, _P, _P, _P,
+    'yg_ewald_prefactors': (_I, [_P, _D, _D, _P, _D, _P]),
+    'yg_ewald_structurefactors': (_I, [_P, _I64, _P, _P, _P, _D, _P, _D, _P, _P, _P]),
+    'yg_ewald_deltae': (_I, [_P, _P, _P, _P, _P, _I64, _P]),
+    'yg_mc_create': (_I, [_P, _P, _D, _P, _D, _D, _D, _P, _D, _D, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I64,
+                          _I64, _I, _P, ctypes.POINTER(_P)]),
+    'yg_mc_destroy': (_I, [_P]),
+    'yg_mc_set_precision': (_I, [_P, _I]),
+    'yg_mc_set_chain': (_I, [_P, _I64, _I64, _P]),
+    'yg_mc_get_chain': (_I, [_P, _I64, ctypes.POINTER(_I64), _P, _P, _P]),
+    'yg_mc_prefactors': (_I, [_P, _P, ctypes.POINTER(_I64)]),
+    'yg_mc_trials': (_I, [_P, _I64, _P, _P, _P, _P, _P]),
+    'yg_mc_apply': (_I, [_P, _I64, _P]),
+    'yg_mc_launch_count': (_I64, [_P]),
+    'yg_ewald_corr_noalloc':(_I, [_P, _P, _I64, _P, _P, _P, _I64, _P, _P, _D, _D, _D, _I64, _I64, _P, _P, _P,
                                    _P]),
 }
 

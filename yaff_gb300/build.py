@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, 'libyaffgb.so')
 INCLUDE = os.path.join(REPO, 'include')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
+NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-ffp-contract=off', '--expt-relaxed-constexpr',
               '-Xptxas', '-warn-spills']
 
 

@@ -329,3 +329,76 @@ def natom_of(spec):
 def nhigh_of(spec):
     nh = spec.get('nhigh', -1)
     return natom_of(spec) if nh == -1 else nh
+
+
+def mc_framework(natom=2000, box=30.0, jitter=0.3, seed=4):
+    """Rigid framework of the MC trial-energy workload: natom sites of a
+    13^3 simple-cubic grid in a 30 A cube (seeded choice, uniform jitter of
+    +-0.3 A), charges +-0.4 e alternating (neutral), LJ sigma 3.3 A,
+    eps 0.4 kJ/mol."""
+    rng = np.random.default_rng(seed)
+    nside = int(math.ceil(natom ** (1.0 / 3.0)))
+    spacing = box / nside
+    g = np.arange(nside, dtype=float)
+    grid = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    sel = np.sort(rng.permutation(len(grid))[:natom])
+    pos = ((grid[sel] + 0.5) * spacing + rng.uniform(-jitter, jitter, (natom, 3))) * angstrom
+    q = np.where(np.arange(natom) % 2 == 0, 0.4, -0.4)
+    return {'pos': pos, 'charges': q, 'sigmas': np.full(natom, 3.3 * angstrom),
+            'epsilons': np.full(natom, 0.4 * kjmol), 'rvecs': np.eye(3) * box * angstrom}
+
+
+def mc_guest():
+    """The rigid guest: the 3-site water of the NVE workload (O, H, H)."""
+    return {'pos': water_geometry(), 'charges': np.array([-0.82, 0.41, 0.41]),
+            'sigmas': np.array([3.166 * angstrom, 0.0, 0.0]),
+            'epsilons': np.array([0.65 * kjmol, 0.0, 0.0])}
+
+
+def mc_place_guests(rng, n, rvecs):
+    """n rigid waters at uniformly random centres and orientations."""
+    body = mc_guest()['pos']
+    frac = rng.uniform(0.0, 1.0, (n, 3))
+    centres = frac @ rvecs
+    rot = _random_rotations(rng, n)
+    return centres[:, None, :] + np.einsum('mij,aj->mai', rot, body)
+
+
+def mc_workload(nchain=256, max_guests=400, seed=5, rcut=12.0):
+    """The MC trial-energy workload: one framework, nchain chains with
+    seeded loadings uniform in [0, max_guests] rigid waters placed at random,
+    rcut 12 A, Ewald alpha 3.5/rcut and gcut 1.1 alpha."""
+    rng = np.random.default_rng(seed)
+    fw = mc_framework()
+    loads = rng.integers(0, max_guests + 1, nchain)
+    chains = [mc_place_guests(rng, int(n), fw['rvecs']) for n in loads]
+    ew = ewald_params(rcut * angstrom)
+    return {'framework': fw, 'guest': mc_guest(), 'chains': chains, 'rcut': rcut * angstrom,
+            'alpha': ew['alpha'], 'gcut': ew['gcut'], 'max_guests': max_guests,
+            'close_contact': 0.4 * angstrom}
+
+
+def mc_trial_batch(rng, work, chains_state, ntrial_per_chain=64, chain_ids=None, max_shift=1.0):
+    """Random trials for the given chains: a third each of insertions
+    (random position and orientation), deletions and translations (shift
+    uniform in a cube of +-max_shift A) of a random guest; deletions and
+    translations become insertions on an empty chain.  Returns (chain, kind,
+    guest, newpos) arrays."""
+    rv = work['framework']['rvecs']
+    ids = range(len(chains_state)) if chain_ids is None else chain_ids
+    ch, kind, guest, newpos = [], [], [], []
+    for c in ids:
+        n = len(chains_state[c])
+        k = rng.integers(0, 3, ntrial_per_chain)
+        if n == 0:
+            k[:] = 0
+        g = rng.integers(0, max(n, 1), ntrial_per_chain)
+        ins = mc_place_guests(rng, ntrial_per_chain, rv)
+        shift = rng.uniform(-max_shift, max_shift, (ntrial_per_chain, 1, 3)) * angstrom
+        npos = np.where((k == 2)[:, None, None], (chains_state[c][g] if n else ins) + shift, ins)
+        ch.append(np.full(ntrial_per_chain, c))
+        kind.append(k)
+        guest.append(np.where(k == 0, -1, g))
+        newpos.append(npos)
+    return (np.concatenate(ch).astype(np.int32), np.concatenate(kind).astype(np.int32),
+            np.concatenate(guest).astype(np.int32), np.ascontiguousarray(np.concatenate(newpos)))
