@@ -38,6 +38,12 @@ namespace {
 #define EW_MS 32     // m values per S-pass slab
 #define EW_MAXM 64   // largest supported G2 + 1
 
+// Row stride of the per-atom phase tables: the logical length G0+G1+G2+3
+// rounded up to an even count, so rows of FP32 complex values are whole
+// 16-byte units (bulk-copy granularity).
+__host__ __device__ __forceinline__ int ew_row_stride(int G0, int G1, int G2) { return (G0 + G1 + G2 + 4) & ~1; }
+
+
 template <typename T> struct C2;
 template <> struct C2<float> { typedef float2 t; };
 template <> struct C2<double> { typedef double2 t; };
@@ -59,7 +65,7 @@ template <typename T> __device__ __forceinline__ typename C2<T>::t cmk(T a, T b)
 template <typename T>
 __global__ void k_tables(const double *__restrict__ pos, const double *__restrict__ charge, int64_t natom,
                          CellGeom cell, int G0, int G1, int G2, typename C2<T>::t *__restrict__ tab) {
-  const int L = G0 + G1 + G2 + 3;
+  const int L = ew_row_stride(G0, G1, G2);
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= natom * 3) return;
   const int64_t a = idx / 3;
@@ -110,6 +116,57 @@ template <typename T> struct SfacCfg;
 template <> struct SfacCfg<float> { enum { KA = 32, ATB = 256 }; };
 template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
 
+// ---- bulk copies into shared memory completed on an mbarrier ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// The barrier's single arrival, announcing `bytes` of copies to come.
+__device__ __forceinline__ void bulk_expect(unsigned long long *bar, unsigned bytes) {
+  unsigned long long state;  // arrival token (unused: waits go by phase parity)
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(state)
+               : "r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// global into shared memory, completing on the barrier.
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  bulk_expect(bar, bytes);
+  bulk_copy(dst, src, bytes, bar);
+}
+
+// Waits for phase `parity` of the barrier; gives up after a bounded number
+// of polls (about a second), records the failure and returns false.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int *status) {
+  for (int it = 0; it < (1 << 24); it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  if (status) atomicOr(status + YG_ST_TIMEOUT, 1);
+  return false;
+}
+
 // S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
 // The table rows of KA atoms are staged in shared memory with coalesced
 // copies.  Lane l owns columns l, l+32, l+64, l+96 of the tile and forms
@@ -119,12 +176,14 @@ template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
 template <typename T, typename TA>
 __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restrict__ tab, int a0, int a1, int G0,
                                               int G1, int G2, const int4 *__restrict__ cols,
-                                              typename C2<TA>::t *__restrict__ Spart, int nstile, int nslab) {
+                                              typename C2<TA>::t *__restrict__ Spart, int nstile, int nslab,
+                                              int *__restrict__ status) {
   typedef typename C2<T>::t CT;
   const int KA = SfacCfg<T>::KA, ATB = SfacCfg<T>::ATB;
-  const int L = G0 + G1 + G2 + 3;
+  const int L = ew_row_stride(G0, G1, G2);
   extern __shared__ __align__(16) unsigned char sfac_smem[];
-  CT *sRow = reinterpret_cast<CT *>(sfac_smem);      // [KA][L] table rows
+  __shared__ unsigned long long bars[2];
+  CT *sRow = reinterpret_cast<CT *>(sfac_smem);      // 2 x [KA][L] table rows
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x, slab = blockIdx.z;
   const int mb = slab * EW_MS;
@@ -140,7 +199,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
       ar[i][j] = (T)0;
       ai[i][j] = (T)0;
     }
-  if (Mt > 0) {
+  if (Mt > 0 && aend > abeg) {
     int o0[4], o1[4];
     T s0[4], s1[4], ok[4];
 #pragma unroll
@@ -153,16 +212,37 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
       ok[i] = col.z >= 0 ? (T)1 : (T)0;
     }
     const int yb = G0 + G1 + 2 + mb + w;
-    for (int ab = abeg; ab < aend; ab += KA) {
-      // coalesced copy of the chunk's table rows (contiguous in global memory)
+    // the chunks' table rows are contiguous in global memory: double-buffered
+    // bulk copies, the next chunk in flight while this one is consumed
+    const int nchunk = (aend - abeg + KA - 1) / KA;
+    if (threadIdx.x == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int nrow = min(KA, aend - abeg);
+      bulk_load(sRow, tab + (int64_t)abeg * L, (unsigned)(nrow * L * sizeof(CT)), &bars[0]);
+    }
+    for (int c = 0; c < nchunk; c++) {
+      const int ab = abeg + c * KA;
       const int nrow = min(KA, aend - ab);
-      const CT *src = tab + (int64_t)ab * L;
-      for (int v = threadIdx.x; v < KA * L; v += blockDim.x)
-        sRow[v] = (v < nrow * L) ? src[v] : cmk<T>((T)0, (T)0);
-      __syncthreads();
+      if (threadIdx.x == 0 && c + 1 < nchunk) {
+        const int ab1 = ab + KA;
+        bulk_load(sRow + (size_t)((c + 1) & 1) * KA * L, tab + (int64_t)ab1 * L,
+                  (unsigned)(min(KA, aend - ab1) * L * sizeof(CT)), &bars[(c + 1) & 1]);
+      }
+      const bool arrived = mbar_wait(&bars[c & 1], (unsigned)((c >> 1) & 1), status);
+      if (__syncthreads_or(!arrived)) {
+        // a copy never completed: wait (bounded) for the one still in flight
+        if (threadIdx.x == 0 && c + 1 < nchunk) mbar_wait(&bars[(c + 1) & 1], (unsigned)(((c + 1) >> 1) & 1), status);
+        break;
+      }
+      const CT *buf = sRow + (size_t)(c & 1) * KA * L;
 #pragma unroll 2
-      for (int la = 0; la < KA; la++) {
-        const CT *row = sRow + la * L;
+      for (int la = 0; la < nrow; la++) {
+        const CT *row = buf + la * L;
         CT x[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -184,7 +264,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
           }
         }
       }
-      __syncthreads();
+      __syncthreads();  // every thread is done with this buffer before it is refilled
     }
   }
   // partial layout: [chunk][tile][slab][c][m]
@@ -252,7 +332,8 @@ __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int 
 template <typename T>
 __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_dense, const double *__restrict__ pref,
                                int G0, int G1, int nm, CellGeom cell, double fac2, int ngroup,
-                               typename C2<T>::t *__restrict__ W, double *__restrict__ partial) {
+                               const int *__restrict__ wslot, int64_t wstride, typename C2<T>::t *__restrict__ W,
+                               double *__restrict__ partial) {
   __shared__ double red[256 / 32][7];
   int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double e = 0.0, v[6] = {0, 0, 0, 0, 0, 0};
@@ -289,12 +370,18 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
     }
     // weights: group 0 = mid atoms (S0+S1+S2), 1 = low atoms (S0+S2),
     // 2 = high atoms (S0+S1); conj stored.
-    for (int g = 0; g < ngroup; g++) {
-      double wr = c0, wi = s0;
-      if (g == 0) { wr += c1 + c2; wi += s1 + s2; }
-      else if (g == 1) { wr += c2; wi += s2; }
-      else { wr += c1; wi += s1; }
-      W[(int64_t)g * nk_dense + idx] = cmk<T>((T)(2.0 * A * wr), (T)(-2.0 * A * wi));
+    const int64_t colx = idx / nm;
+    const int slot = wslot[colx];
+    if (slot >= 0) {
+      const int mm = (int)(idx - colx * nm);
+      const int64_t wpos = ((int64_t)(slot / EW_FC) * nm + mm) * EW_FC + (slot % EW_FC);
+      for (int g = 0; g < ngroup; g++) {
+        double wr = c0, wi = s0;
+        if (g == 0) { wr += c1 + c2; wi += s1 + s2; }
+        else if (g == 1) { wr += c2; wi += s2; }
+        else { wr += c1; wi += s1; }
+        W[(int64_t)g * wstride + wpos] = cmk<T>((T)(2.0 * A * wr), (T)(-2.0 * A * wi));
+      }
     }
   }
   // block reduction (fixed order)
@@ -343,40 +430,65 @@ template <> struct CompAcc<float> {
 template <typename T, int RA>
 __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__restrict__ tab, int a0, int a1,
                                                      int G0, int G1, int G2, const int4 *__restrict__ cols,
-                                                     int nftile, const typename C2<T>::t *__restrict__ W,
-                                                     double *__restrict__ gfrac) {
+                                                     int nftile, const typename C2<T>::t *__restrict__ Wt,
+                                                     double *__restrict__ gfrac, int *__restrict__ status) {
   typedef typename C2<T>::t CT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long bars[2];
   const int NA = 16 * RA;
   const int nm = G2 + 1;
+  const int L = ew_row_stride(G0, G1, G2);
+  const int LE = G0 + G1 + 2;                          // E0 and E1 entries of a row
   CT *sY = reinterpret_cast<CT *>(smem_raw);          // [nm][NA]
-  CT *sW = sY + (size_t)nm * NA;                       // [nm][EW_FC]
-  int4 *scol = reinterpret_cast<int4 *>(sW + (size_t)nm * EW_FC);
-  const int L = G0 + G1 + G2 + 3;
+  CT *sE = sY + (size_t)nm * NA;                       // [NA][LE]
+  CT *sWb = sE + (size_t)NA * LE;                      // 2 x [nm][EW_FC]
+  int4 *scolb = reinterpret_cast<int4 *>(sWb + (size_t)2 * nm * EW_FC);  // 2 x [EW_FC]
   const int ta = threadIdx.x & 15, tc = threadIdx.x >> 4;
   const int abase = a0 + blockIdx.x * NA;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
   for (int v = threadIdx.x; v < nm * NA; v += blockDim.x) {
     const int m = v / NA, la = v % NA;
     const int a = abase + la;
     sY[v] = (a < a1) ? tab[(int64_t)a * L + G0 + G1 + 2 + m] : cmk<T>((T)0, (T)0);
   }
+  for (int v = threadIdx.x; v < NA * LE; v += blockDim.x) {
+    const int la = v / LE, e = v % LE;
+    const int a = abase + la;
+    sE[v] = (a < a1) ? tab[(int64_t)a * L + e] : cmk<T>((T)0, (T)0);
+  }
+  __syncthreads();
+  // column tiles (weights tile-ordered: [m][EW_FC], plus the 64 column
+  // descriptors) through double-buffered bulk copies
+  auto issue = [&](int t) {
+    const int4 *tcols = cols + t * EW_FC;
+    const int Mt = tcols[0].w + 1;
+    const unsigned wbytes = (unsigned)(Mt * EW_FC * sizeof(CT));
+    const unsigned cbytes = (unsigned)(EW_FC * sizeof(int4));
+    unsigned long long *bar = &bars[t & 1];
+    bulk_expect(bar, wbytes + cbytes);
+    bulk_copy(sWb + (size_t)(t & 1) * nm * EW_FC, Wt + (size_t)t * nm * EW_FC, wbytes, bar);
+    bulk_copy(scolb + (t & 1) * EW_FC, tcols, cbytes, bar);
+  };
+  if (threadIdx.x == 0 && nftile > 0) issue(0);
   CompAcc<T> acc[RA][3];
 #pragma unroll
   for (int r = 0; r < RA; r++)
 #pragma unroll
     for (int q = 0; q < 3; q++) acc[r][q].init();
   for (int t = 0; t < nftile; t++) {
-    const int4 *tcols = cols + t * EW_FC;
-    const int Mt = tcols[0].w + 1;
-    if (Mt <= 0) continue;
-    __syncthreads();
-    for (int v = threadIdx.x; v < Mt * EW_FC; v += blockDim.x) {
-      const int m = v / EW_FC, c = v % EW_FC;
-      const int4 col = tcols[c];
-      sW[v] = (col.z >= 0 && m <= col.w) ? W[(int64_t)col.z * nm + m] : cmk<T>((T)0, (T)0);
+    if (threadIdx.x == 0 && t + 1 < nftile) issue(t + 1);
+    const bool arrived = mbar_wait(&bars[t & 1], (unsigned)((t >> 1) & 1), status);
+    if (__syncthreads_or(!arrived)) {
+      if (threadIdx.x == 0 && t + 1 < nftile) mbar_wait(&bars[(t + 1) & 1], (unsigned)(((t + 1) >> 1) & 1), status);
+      break;
     }
-    if (threadIdx.x < EW_FC) scol[threadIdx.x] = tcols[threadIdx.x];
-    __syncthreads();
+    const CT *sW = sWb + (size_t)(t & 1) * nm * EW_FC;
+    const int4 *scol = scolb + (t & 1) * EW_FC;
+    const int Mt = scol[0].w + 1;
     T zr[RA][4], zi[RA][4], z2r[RA][4], z2i[RA][4];
 #pragma unroll
     for (int r = 0; r < RA; r++)
@@ -403,7 +515,7 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
           z2i[r][i] += fm * pi;
         }
     }
-    // epilogue: P = E0 E1 of each (atom, column)
+    // epilogue: P = E0 E1 of each (atom, column), from the staged rows
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       const int4 col = scol[tc * 4 + i];
@@ -411,9 +523,7 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
       const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = col.y < 0 ? -col.y : col.y;
 #pragma unroll
       for (int r = 0; r < RA; r++) {
-        const int a = abase + ta + 16 * r;
-        if (a >= a1) continue;
-        const CT *row = tab + (int64_t)a * L;
+        const CT *row = sE + (size_t)(ta + 16 * r) * LE;
         CT e0 = row[ag0], e1 = row[G0 + 1 + ag1];
         if (col.x < 0) e0.y = -e0.y;
         if (col.y < 0) e1.y = -e1.y;
@@ -426,6 +536,7 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
         acc[r][2].add(im2);
       }
     }
+    __syncthreads();  // the buffer is refilled two tiles later
   }
   // reduce the 16 column groups of every atom in a fixed order
   __syncthreads();
@@ -539,6 +650,9 @@ static int smem_optin(const void *kernel, size_t need) {
   if (done.count(std::make_pair(kernel, dev))) return YG_OK;
   int optin = 0;
   YG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  YG_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  optin -= (int)fa.sharedSizeBytes;  // static shared memory counts against the same limit
   if (need > (size_t)optin) {
     yg_set_error("Ewald tile needs more shared memory than the device offers");
     return YG_ERR_UNSUPPORTED;
@@ -548,8 +662,10 @@ static int smem_optin(const void *kernel, size_t need) {
   return YG_OK;
 }
 
-template <typename T> size_t force_smem(int nm, int RA) {
-  size_t a = (size_t)nm * (16 * RA + EW_FC) * sizeof(typename C2<T>::t) + EW_FC * sizeof(int4);
+template <typename T> size_t force_smem(int G0, int G1, int nm, int RA) {
+  const size_t ct = sizeof(typename C2<T>::t);
+  size_t a = (size_t)nm * 16 * RA * ct + (size_t)16 * RA * (G0 + G1 + 2) * ct + (size_t)2 * nm * EW_FC * ct +
+             2 * EW_FC * sizeof(int4);
   size_t b = (size_t)16 * 16 * RA * 3 * sizeof(double);
   return a > b ? a : b;
 }
@@ -560,16 +676,17 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   typedef typename C2<TA>::t CA;
   const int G0 = (int)ctx->ew_gmax[0], G1 = (int)ctx->ew_gmax[1], G2 = (int)ctx->ew_gmax[2];
   const int nm = G2 + 1;
-  const int L = G0 + G1 + G2 + 3;
   const int64_t N = ctx->natom;
   const int nstile = ctx->ew_ntile;
-  const int nftile = 2 * nstile;
+  const int nftile = ctx->ew_nftile;              // force tiles with work
+  const int64_t wstride = (int64_t)2 * nstile * nm * EW_FC;  // tiled weights per group
   const int nslab = (nm + EW_MS - 1) / EW_MS;
   const int ATB = SfacCfg<T>::ATB;
   const int64_t nk_dense = (int64_t)ctx->ew_ncol * nm;
   int rc;
   // tables
-  size_t tb = (size_t)N * L * sizeof(CT);
+  const int Lp = ew_row_stride(G0, G1, G2);
+  size_t tb = (size_t)N * Lp * sizeof(CT);
   if ((rc = yg_ensure(ctx, &ctx->d_ew_tab, &ctx->ew_bytes_tab, tb))) return rc;
   CT *tab = (CT *)ctx->d_ew_tab;
   k_tables<T><<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2, tab);
@@ -598,10 +715,11 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     int nch = (int)((n + ATB - 1) / ATB);
     dim3 grid(nstile, nch, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
-    const size_t ssm = (size_t)SfacCfg<T>::KA * L * sizeof(CT);
+    const size_t ssm = (size_t)2 * SfacCfg<T>::KA * Lp * sizeof(CT);
     if ((rc = smem_optin((const void *)k_sfac<T, TA>, ssm))) return rc;
     k_sfac<T, TA><<<grid, 128, ssm, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
-                                                 (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab);
+                                                 (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab,
+                                                 ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
     k_sfac_reduce<TA><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
         (const CA *)ctx->d_ew_Spart, nch, nstile, nslab, (const int4 *)ctx->d_ew_tiles, nm, S);
@@ -609,13 +727,16 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   }
   // energy, virial, weights
   const int ngroup = (nS == 3) ? 3 : 1;
-  if ((rc = yg_ensure(ctx, &ctx->d_ew_W, &ctx->ew_bytes_W, (size_t)ngroup * nk_dense * sizeof(CT)))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_W, &ctx->ew_bytes_W, (size_t)ngroup * wstride * sizeof(CT)))) return rc;
+  // padding slots of the tiled weights stay zero
+  YG_CUDA(cudaMemsetAsync(ctx->d_ew_W, 0, (size_t)ngroup * wstride * sizeof(CT), ctx->stream));
   const int eb = yg_blocks(nk_dense, 256);
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
   double *partial = ctx->d_red + 64;
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
-                                                fac2, ngroup, (CT *)ctx->d_ew_W, partial);
+                                                fac2, ngroup, ctx->d_ew_wslot, wstride, (CT *)ctx->d_ew_W,
+                                                partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -630,16 +751,17 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   }
   // force pass, per atom group
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
-  size_t smem = force_smem<T>(nm, RA);
+  size_t smem = force_smem<T>(G0, G1, nm, RA);
   if ((rc = smem_optin((const void *)k_ewald_force<T, RA>, smem))) return rc;
   const int gidx[3] = {0, 1, 2};
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
     if (n <= 0) continue;
-    const CT *Wg = (const CT *)ctx->d_ew_W + (size_t)(ngroup == 1 ? 0 : gidx[g]) * nk_dense;
+    const CT *Wg = (const CT *)ctx->d_ew_W + (size_t)(ngroup == 1 ? 0 : gidx[g]) * wstride;
     int nblk = (int)((n + 16 * RA - 1) / (16 * RA));
     k_ewald_force<T, RA><<<nblk, 256, smem, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
-                                                          (const int4 *)ctx->d_ew_tiles, nftile, Wg, ctx->d_ew_gpart);
+                                                          (const int4 *)ctx->d_ew_tiles, nftile, Wg, ctx->d_ew_gpart,
+                                                          ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_ewald_force");
   }
   k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
@@ -702,6 +824,16 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   ctx->ew_nm = nm;
   ctx->ew_nk = nk;
   ctx->ew_ntile = (int)(tiles.size() / EW_SC);
+  // force tiles (EW_FC columns each) that hold work, and the tiled-weight
+  // slot of every dense column (-1: no k of the column is inside the cutoff)
+  std::vector<int> wslot((size_t)nc0 * nc1, -1);
+  int nft = 0;
+  for (size_t i = 0; i < tiles.size(); i++) {
+    if (tiles[i].z >= 0) wslot[tiles[i].z] = (int)i;
+    if (i % EW_FC == 0 && tiles[i].w >= 0) nft++;
+  }
+  ctx->ew_nftile = nft;
+  yg_free(ctx, (void **)&ctx->d_ew_wslot);
   yg_free(ctx, (void **)&ctx->d_ew_pref);
   yg_free(ctx, (void **)&ctx->d_ew_tiles);
   yg_free(ctx, (void **)&ctx->d_ew_S);
@@ -712,6 +844,9 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_pref, nk_dense * sizeof(double)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_tiles, std::max<size_t>(1, tiles.size()) * sizeof(int4)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_wslot, wslot.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_wslot, wslot.data(), wslot.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_pref, pref.data(), nk_dense * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (!tiles.empty())
     YG_CUDA(cudaMemcpyAsync(ctx->d_ew_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice,

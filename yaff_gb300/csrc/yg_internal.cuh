@@ -22,6 +22,7 @@
 #define YG_ST_MAXCOUNT 1     // largest per-atom full-list row count seen
 #define YG_ST_EXACT 2        // candidates decided by the exact FP64 test
 #define YG_ST_BADCELL 3      // non-finite position met while binning
+#define YG_ST_TIMEOUT 4      // a bounded wait on an asynchronous copy gave up
 #define YG_ST_NWORDS 8
 
 // Neighbour entry: x = partner (sorted index), y = meta bits.
@@ -158,6 +159,8 @@ struct yg_ctx {
   double *d_ew_pref = nullptr;    // ncol*nm prefactor (0 outside the half sphere)
   int *d_ew_tiles = nullptr;      // column tiles: (g0 base, g1 base, m_hi)
   int ew_ntile = 0;
+  int ew_nftile = 0;              // force tiles (EW_FC columns) with work
+  int *d_ew_wslot = nullptr;      // dense column -> slot in the tiled weights
   void *d_ew_tab = nullptr;       // per-atom phase tables (complex, T)
   void *d_ew_Spart = nullptr;     // partial structure factors
   double *d_ew_S = nullptr;       // 3 groups * ncol*nm complex (re, im)
