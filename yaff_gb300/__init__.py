@@ -4,7 +4,10 @@ The hot path of a yaff force evaluation (neighbour list, LJ / MM3 / EI pair
 terms, Ewald reciprocal / correction / neutralizing terms, bond and bend
 valence terms) runs as hand-written sm_103a CUDA kernels in libyaffgb.so,
 reached through its C ABI (include/yaffgb.h).  The Python classes keep the
-reference's constructors and ``compute(gpos, vtens)`` semantics.
+reference's constructors and ``compute(gpos, vtens)`` semantics.  Around it:
+velocity Verlet on the host or fully device-resident (``verlet``), a
+serving loop for many small systems (``serve``) and batched Monte Carlo
+trial energies with the reference's structure-factor functions (``mc``).
 """
 from .system import Cell, System
 from .pair import Hammer, Switch3, PairPotLJ, PairPotMM3, PairPotEI
@@ -15,6 +18,9 @@ from .ff import (ForcePart, ForceField, ForcePartPair, ForcePartEwaldReciprocal,
                  ForcePartEwaldNeutralizing, ForcePartValence)
 from .device import DeviceSystem, device_of, set_default_precision, get_default_precision
 from .builder import build_system, build_forcefield
+from .verlet import VerletIntegrator, DeviceVerlet, get_random_vel
+from .mc import (ForcePartEwaldReciprocalInteraction, MCTrials, compute_ewald_prefactors,
+                 compute_ewald_structurefactors, compute_ewald_deltae)
 from . import configs, units
 
 __version__ = '0.1.0'
