@@ -43,6 +43,8 @@ struct GridGeom {
   int k[3];        // stencil half width per axis
   int noff;        // (2k0+1)(2k1+1)(2k2+1)
   int ncell;
+  int nrow;        // stencil rows (o1, o2) that can hold neighbours
+  int rows_per_batch;  // rows whose runs fit the build kernel's run buffer
 };
 
 struct PairPotHost {
@@ -105,6 +107,8 @@ struct yg_ctx {
   double4_32a *d_x64 = nullptr;       // sorted: local coordinate (x,y,z) and charge
   float4 *d_x32 = nullptr;        // sorted: same in FP32
   float4 *d_xb = nullptr;         // sorted: FP32 coordinates, w = cell x index (build)
+  int4 *d_rows = nullptr;         // stencil rows (o1, o2, lo, hi) of the pruned stencil
+  size_t rows_cap = 0;
   double *d_shift64 = nullptr;    // noff*3 stencil shift vectors
   float4 *d_shift32 = nullptr;    // noff
   size_t shift64_cap = 0, shift32_cap = 0;

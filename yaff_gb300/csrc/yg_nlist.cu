@@ -24,6 +24,9 @@
 
 #include "yg_internal.cuh"
 
+#define YG_CELL_DIV 4      // grid cells at least r_c / 4 wide
+#define YG_BUILD_RUNS 192  // candidate runs per warp held in shared memory
+
 namespace {
 
 __global__ void k_bin(const int *__restrict__ gate, const double *__restrict__ pos, int64_t natom, CellGeom cell, GridGeom grid,
@@ -238,6 +241,7 @@ struct BuildArgs {
   int fast;
   int filter;       // nlow/nhigh restrict the pairs
   const int *gate;  // device flag: build only when set (nullptr: always)
+  const int4 *rows; // pruned stencil rows (o1, o2, lo, hi)
 };
 
 // Exact replay of the reference's decision for candidate (oi -> oj) whose
@@ -290,11 +294,27 @@ __device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, 
 // run are contiguous in sorted order, so lanes walk them in full 32-wide
 // chunks and recover each candidate's x offset from the cell boundaries of
 // the run (kept in registers).
-__global__ void __launch_bounds__(256, 3) k_build(BuildArgs A) {
+// One candidate run: atoms s0 .. s0+len-1 (contiguous in sorted order: one
+// to several x-consecutive cells of one stencil row sharing one periodic
+// image), oidx = obase + cell x of the candidate, packed images and the
+// home-row flag.
+__device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
+  return (n0 + 512) | ((n1 + 512) << 10) | ((n2 + 512) << 20) | (home << 30);
+}
+
+// One warp per sorted atom.  The candidates of all stencil rows of a batch
+// are laid out as runs in shared memory (lanes build the runs of different
+// rows in parallel), then swept as one flat index space 32 at a time, so
+// short runs of the fine grid do not leave lanes idle.
+__global__ void __launch_bounds__(256, 2) k_build(BuildArgs A) {
+  __shared__ int4 s_run[8][YG_BUILD_RUNS];
+  __shared__ int s_off[8][YG_BUILD_RUNS + 1];
   if (A.gate && !*A.gate) return;
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   if (i >= A.natom) return;
+  int4 *run = s_run[wv];
+  int *off = s_off[wv];
   const int oi = A.sorted[i];
   const float4 xi = A.x32[i];
   const int cid = A.cell_of[oi];
@@ -305,75 +325,120 @@ __global__ void __launch_bounds__(256, 3) k_build(BuildArgs A) {
   int64_t base = 0;
   int nexact = 0;
   uint2 *out = A.nbr + i * A.cap;
-  const int K0 = A.grid.k[0];
-  const int w0 = 2 * K0 + 1, w1 = 2 * A.grid.k[1] + 1;
-  for (int o2 = -A.grid.k[2]; o2 <= A.grid.k[2]; o2++) {
-    const int u2 = ci[2] + o2;
-    const int n2 = floordiv(u2, N2);
-    const int c2 = u2 - n2 * N2;
-    for (int o1 = -A.grid.k[1]; o1 <= A.grid.k[1]; o1++) {
-      const int u1 = ci[1] + o1;
-      const int n1 = floordiv(u1, N1);
-      const int c1 = u1 - n1 * N1;
+  const int K0 = A.grid.k[0], K1 = A.grid.k[1], K2 = A.grid.k[2];
+  const int w0 = 2 * K0 + 1, w1 = 2 * K1 + 1;
+  const int oidx_home = K0 + w0 * (K1 + w1 * K2);
+  for (int rb = 0; rb < A.grid.nrow; rb += A.grid.rows_per_batch) {
+    const int re = min(A.grid.nrow, rb + A.grid.rows_per_batch);
+    // runs per lane: count, warp scan, then write
+    int mine = 0;
+    for (int r = rb + lane; r < re; r += 32) {
+      const int4 row = A.rows[r];
+      for (int ox = row.z; ox <= row.w;) {
+        const int u0 = ci[0] + ox;
+        const int c0 = u0 - floordiv(u0, N0) * N0;
+        ox += min(row.w - ox + 1, N0 - c0);
+        mine++;
+      }
+    }
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int nrun = __shfl_sync(0xffffffffu, incl, 31);
+    int slot = incl - mine;
+    for (int r = rb + lane; r < re; r += 32) {
+      const int4 row = A.rows[r];
+      const int o1 = row.x, o2 = row.y;
+      const int u1 = ci[1] + o1, u2 = ci[2] + o2;
+      const int n1 = floordiv(u1, N1), n2 = floordiv(u2, N2);
+      const int c1 = u1 - n1 * N1, c2 = u2 - n2 * N2;
       const int rowcell = N0 * (c1 + N1 * c2);
-      const int orow = w0 * ((o1 + A.grid.k[1]) + w1 * (o2 + A.grid.k[2]));
-      for (int ox = -K0; ox <= K0;) {
+      const int orow = w0 * ((o1 + K1) + w1 * (o2 + K2));
+      for (int ox = row.z; ox <= row.w;) {
         const int u0 = ci[0] + ox;
         const int n0 = floordiv(u0, N0);
         const int c0 = u0 - n0 * N0;
-        const int len = min(K0 - ox + 1, N0 - c0);
+        const int len = min(row.w - ox + 1, N0 - c0);
         const int s0 = A.cell_start[rowcell + c0], s1 = A.cell_start[rowcell + c0 + len];
-        const int obase = ox - c0 + K0 + orow;   // oidx = obase + (cell x of the candidate)
-        for (int jb = s0; jb < s1; jb += 32) {
-          const int j = jb + lane;
-          int in = 0, central = 1, oj = -1, oidx = 0;
-          if (j < s1) {
-            const float4 xj = A.xb[j];
-            oidx = obase + __float_as_int(xj.w);
-            const bool self0 = (j == i) && (oidx == (K0 + orow)) && o1 == 0 && o2 == 0 && n0 == 0;
-            bool keep = !self0;
-            if (keep && need_oj) {
-              oj = A.sorted[j];
-              if (A.filter) {
-                const int a = max(oi, oj), b = min(oi, oj);
-                keep = (a >= A.nlow && b < A.nhigh) || (b >= A.nlow && a < A.nhigh);
-              }
-            }
-            if (keep) {
-              const float4 sh = A.shift32[oidx];
-              const float dx = (xj.x - xi.x) + sh.x;
-              const float dy = (xj.y - xi.y) + sh.y;
-              const float dz = (xj.z - xi.z) + sh.z;
-              const float d2 = dx * dx + dy * dy + dz * dz;
-              int decided = 0;
-              if (A.fast) {
-                if (d2 < A.lo) { in = 1; decided = 1; }
-                else if (d2 > A.hi) { in = 0; decided = 1; }
-              }
-              if (!decided) {
-                if (oj < 0) oj = A.sorted[j];
-                int tt[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1],
-                             n2 + wi[2] - A.wimg[3 * oj + 2]};
-                in = exact_decide(A, oi, oj, tt, &central);
-                nexact++;
-              }
-            }
-          }
-          const unsigned ball = __ballot_sync(0xffffffffu, in);
-          if (in) {
-            const int code = (central && A.estart) ? excl_code(A.estart, A.excl, oi, oj) : 0;
-            const int64_t p = base + __popc(ball & ((1u << lane) - 1u));
-            if (p < A.cap) {
-              const unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
-                                    (central ? YG_META_CENTRAL : 0u);
-              out[p] = make_uint2((unsigned)j, meta);
-            }
-          }
-          base += __popc(ball);
-        }
+        run[slot] = make_int4(s0, s1 - s0, ox - c0 + K0 + orow,
+                              pack_img(n0, n1, n2, (o1 == 0 && o2 == 0 && n0 == 0) ? 1 : 0));
+        slot++;
         ox += len;
       }
     }
+    __syncwarp();
+    // candidate offsets of the runs
+    int carry = 0;
+    for (int b = 0; b < nrun; b += 32) {
+      int v = (b + lane < nrun) ? run[b + lane].y : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+      }
+      if (b + lane < nrun) off[b + lane + 1] = carry + v;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+    if (lane == 0) off[0] = 0;
+    __syncwarp();
+    const int total = carry;
+    int r = 0;
+    for (int q0 = 0; q0 < total; q0 += 32) {
+      const int q = q0 + lane;
+      int in = 0, central = 1, oj = -1, oidx = 0, j = 0;
+      if (q < total) {
+        while (off[r + 1] <= q) r++;
+        const int4 rr = run[r];
+        j = rr.x + (q - off[r]);
+        const float4 xj = A.xb[j];
+        oidx = rr.z + __float_as_int(xj.w);
+        const int pk = rr.w;
+        const bool self0 = (pk >> 30) && (j == i) && (oidx == oidx_home);
+        bool keep = !self0;
+        if (keep && need_oj) {
+          oj = A.sorted[j];
+          if (A.filter) {
+            const int a = max(oi, oj), b = min(oi, oj);
+            keep = (a >= A.nlow && b < A.nhigh) || (b >= A.nlow && a < A.nhigh);
+          }
+        }
+        if (keep) {
+          const float4 sh = A.shift32[oidx];
+          const float dx = (xj.x - xi.x) + sh.x;
+          const float dy = (xj.y - xi.y) + sh.y;
+          const float dz = (xj.z - xi.z) + sh.z;
+          const float d2 = dx * dx + dy * dy + dz * dz;
+          int decided = 0;
+          if (A.fast) {
+            if (d2 < A.lo) { in = 1; decided = 1; }
+            else if (d2 > A.hi) { in = 0; decided = 1; }
+          }
+          if (!decided) {
+            if (oj < 0) oj = A.sorted[j];
+            const int n0 = (pk & 1023) - 512, n1 = ((pk >> 10) & 1023) - 512, n2 = ((pk >> 20) & 1023) - 512;
+            int tt[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1],
+                         n2 + wi[2] - A.wimg[3 * oj + 2]};
+            in = exact_decide(A, oi, oj, tt, &central);
+            nexact++;
+          }
+        }
+      }
+      const unsigned ball = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int code = (central && A.estart) ? excl_code(A.estart, A.excl, oi, oj) : 0;
+        const int64_t p = base + __popc(ball & ((1u << lane) - 1u));
+        if (p < A.cap) {
+          const unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
+                                (central ? YG_META_CENTRAL : 0u);
+          out[p] = make_uint2((unsigned)j, meta);
+        }
+      }
+      base += __popc(ball);
+    }
+    __syncwarp();  // the next batch overwrites this warp's runs
   }
   for (int o = 16; o > 0; o >>= 1) nexact += __shfl_down_sync(0xffffffffu, nexact, o);
   if (lane == 0) {
@@ -535,6 +600,7 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.fast = 0;
   A.filter = (ctx->nlow > 0 || ctx->nhigh < ctx->natom) ? 1 : 0;
   A.gate = nullptr;
+  A.rows = ctx->d_rows;
   return A;
 }
 
@@ -614,13 +680,13 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
   const double rc = ctx->rcut_total;
   if (ctx->geom_valid && ctx->geom_rc == rc) return YG_OK;
   const CellGeom &C = ctx->cell;
-  // grid: cells at least rc/2 wide along each plane normal
+  // grid: cells at least rc/YG_CELL_DIV wide along each plane normal
   GridGeom G;
   double rsp[3];
   for (int k = 0; k < 3; k++) {
     const double *g = C.gv + 3 * k;
     rsp[k] = 1.0 / std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-    int n = (int)std::floor(rsp[k] / (0.5 * rc));
+    int n = (int)std::floor(rsp[k] / (rc / YG_CELL_DIV));
     if (n < 1) n = 1;
     if (n > 512) n = 512;
     G.n[k] = n;
@@ -658,8 +724,69 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
         sh32[idx] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.0f);
         maxsh = std::max(maxsh, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
       }
+  // stencil rows that can hold neighbours, each with the interval of x offsets
+  // whose cells can lie within the cutoff: a cell pair at offset o is at
+  // least max_u (u.M o - sum_k |u.M_k|) apart (M_k = cell edge vectors; any
+  // unit u gives a lower bound), tried for u along M (o + clamp(-o)) and M o,
+  // and the slab bounds (|o_k| - 1) h_k along the plane normals
+  std::vector<int4> rows;
+  {
+    double Mk[3][3];  // Mk[k] = rv_k / n_k
+    for (int k = 0; k < 3; k++)
+      for (int x = 0; x < 3; x++) Mk[k][x] = C.rv[3 * k + x] / G.n[k];
+    const double keep_below = rc * (1.0 + 1e-6) + 1e-6;
+    auto lower_bound = [&](const int o[3]) {
+      double lb = 0.0;
+      for (int k = 0; k < 3; k++) lb = std::max(lb, (std::abs(o[k]) - 1.0) * rsp[k] / G.n[k]);
+      double mo[3], mt[3];
+      for (int x = 0; x < 3; x++) {
+        mo[x] = 0.0;
+        mt[x] = 0.0;
+        for (int k = 0; k < 3; k++) {
+          const double t = std::min(1.0, std::max(-1.0, (double)-o[k]));
+          mo[x] += o[k] * Mk[k][x];
+          mt[x] += (o[k] + t) * Mk[k][x];
+        }
+      }
+      for (const double *p : {mt, mo}) {
+        const double nrm = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        if (!(nrm > 0.0)) continue;
+        const double u[3] = {p[0] / nrm, p[1] / nrm, p[2] / nrm};
+        double v = u[0] * mo[0] + u[1] * mo[1] + u[2] * mo[2];
+        for (int k = 0; k < 3; k++) v -= std::abs(u[0] * Mk[k][0] + u[1] * Mk[k][1] + u[2] * Mk[k][2]);
+        lb = std::max(lb, v);
+      }
+      return lb;
+    };
+    for (int o2 = -G.k[2]; o2 <= G.k[2]; o2++)
+      for (int o1 = -G.k[1]; o1 <= G.k[1]; o1++) {
+        int lo = G.k[0] + 1, hi = -G.k[0] - 1;
+        for (int o0 = -G.k[0]; o0 <= G.k[0]; o0++) {
+          const int o[3] = {o0, o1, o2};
+          if (lower_bound(o) < keep_below) {
+            lo = std::min(lo, o0);
+            hi = std::max(hi, o0);
+          }
+        }
+        if (lo <= hi) rows.push_back(make_int4(o1, o2, lo, hi));
+      }
+  }
+  G.nrow = (int)rows.size();
+  {
+    const int maxruns = (2 * G.k[0] + 1 + G.n[0] - 1) / G.n[0] + 1;  // x wraps split a row
+    G.rows_per_batch = std::max(1, YG_BUILD_RUNS / maxruns);
+    if (maxruns > YG_BUILD_RUNS) {
+      yg_set_error("neighbour stencil row too long for the build kernel");
+      return YG_ERR_UNSUPPORTED;
+    }
+  }
+  ctx->grid = G;
   // grow-only: buffers keep their addresses across rebuilds (captured graphs
   // refer to them)
+  if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_rows, &ctx->rows_cap, std::max<size_t>(1, rows.size()) * sizeof(int4))))
+    return rc_;
+  if (!rows.empty())
+    YG_CUDA(cudaMemcpyAsync(ctx->d_rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
   if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_shift64, &ctx->shift64_cap, sh64.size() * sizeof(double)))) return rc_;
   if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_shift32, &ctx->shift32_cap, sh32.size() * sizeof(float4)))) return rc_;
   YG_CUDA(cudaMemcpyAsync(ctx->d_shift64, sh64.data(), sh64.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
