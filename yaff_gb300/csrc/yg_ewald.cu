@@ -112,6 +112,18 @@ __device__ __forceinline__ typename C2<T>::t tab_get(const typename C2<T>::t *__
 // padded with (0, 0, -1, -1) to a multiple of EW_SC.  Grouping columns of
 // similar extent keeps the per-tile m range tight.
 
+// acc += x y (complex).  FP32: two packed f32x2 FMAs,
+// acc += (xr, xr) (yr, yi) and acc += (-xi, xi) (yi, yr), half the issue
+// slots of four scalar FMAs; FP64: scalar.
+__device__ __forceinline__ void cmac(float2 &acc, float2 x, float2 y) {
+  acc = __ffma2_rn(make_float2(x.x, x.x), y, acc);
+  acc = __ffma2_rn(make_float2(-x.y, x.y), make_float2(y.y, y.x), acc);
+}
+__device__ __forceinline__ void cmac(double2 &acc, double2 x, double2 y) {
+  acc.x += x.x * y.x - x.y * y.y;
+  acc.y += x.x * y.y + x.y * y.x;
+}
+
 template <typename T> struct SfacCfg;
 template <> struct SfacCfg<float> { enum { KA = 32, ATB = 256 }; };
 template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
@@ -191,14 +203,11 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   const int nj = (Mt > w) ? min(8, (Mt - w + 3) / 4) : 0;
   const int abeg = a0 + blockIdx.y * ATB;
   const int aend = min(a1, abeg + ATB);
-  T ar[4][8], ai[4][8];
+  CT acc[4][8];
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      ar[i][j] = (T)0;
-      ai[i][j] = (T)0;
-    }
+    for (int j = 0; j < 8; j++) acc[i][j] = cmk<T>((T)0, (T)0);
   if (Mt > 0 && aend > abeg) {
     int o0[4], o1[4];
     T s0[4], s1[4], ok[4];
@@ -257,10 +266,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
           if (j < nj) {
             const CT y = row[yb + 4 * j];
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-              ar[i][j] += x[i].x * y.x - x[i].y * y.y;
-              ai[i][j] += x[i].x * y.y + x[i].y * y.x;
-            }
+            for (int i = 0; i < 4; i++) cmac(acc[i][j], x[i], y);
           }
         }
       }
@@ -276,8 +282,8 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       CA v;
-      v.x = (TA)ar[i][j];
-      v.y = (TA)ai[i][j];
+      v.x = (TA)acc[i][j].x;
+      v.y = (TA)acc[i][j].y;
       Spart[base + c * EW_MS + w + 4 * j] = v;
     }
   }
@@ -489,30 +495,40 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
     const CT *sW = sWb + (size_t)(t & 1) * nm * EW_FC;
     const int4 *scol = scolb + (t & 1) * EW_FC;
     const int Mt = scol[0].w + 1;
-    T zr[RA][4], zi[RA][4], z2r[RA][4], z2i[RA][4];
+    CT z[RA][4], z2[RA][4];
 #pragma unroll
     for (int r = 0; r < RA; r++)
 #pragma unroll
       for (int i = 0; i < 4; i++) {
-        zr[r][i] = (T)0; zi[r][i] = (T)0; z2r[r][i] = (T)0; z2i[r][i] = (T)0;
+        z[r][i] = cmk<T>((T)0, (T)0);
+        z2[r][i] = cmk<T>((T)0, (T)0);
       }
     for (int m = 0; m < Mt; m++) {
-      CT y[RA], w[4];
+      CT y[RA], ym[RA], w[4];
+      const T fm = (T)m;
 #pragma unroll
-      for (int r = 0; r < RA; r++) y[r] = sY[m * NA + ta + 16 * r];
+      for (int r = 0; r < RA; r++) {
+        y[r] = sY[m * NA + ta + 16 * r];
+        ym[r] = cmk<T>(fm * y[r].x, fm * y[r].y);
+      }
 #pragma unroll
       for (int i = 0; i < 4; i++) w[i] = sW[m * EW_FC + tc * 4 + i];
-      const T fm = (T)m;
 #pragma unroll
       for (int r = 0; r < RA; r++)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const T pr = y[r].x * w[i].x - y[r].y * w[i].y;
-          const T pi = y[r].x * w[i].y + y[r].y * w[i].x;
-          zr[r][i] += pr;
-          zi[r][i] += pi;
-          z2r[r][i] += fm * pr;
-          z2i[r][i] += fm * pi;
+          if (std::is_same<T, float>::value) {
+            cmac(z[r][i], y[r], w[i]);
+            cmac(z2[r][i], ym[r], w[i]);
+          } else {
+            // FP64: one product, reused (the FP64 pipe is the scarce one)
+            const T pr = y[r].x * w[i].x - y[r].y * w[i].y;
+            const T pi = y[r].x * w[i].y + y[r].y * w[i].x;
+            z[r][i].x += pr;
+            z[r][i].y += pi;
+            z2[r][i].x += fm * pr;
+            z2[r][i].y += fm * pi;
+          }
         }
     }
     // epilogue: P = E0 E1 of each (atom, column), from the staged rows
@@ -529,8 +545,8 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
         if (col.y < 0) e1.y = -e1.y;
         const T pr = e0.x * e1.x - e0.y * e1.y;
         const T pi = e0.x * e1.y + e0.y * e1.x;
-        const T im1 = pr * zi[r][i] + pi * zr[r][i];
-        const T im2 = pr * z2i[r][i] + pi * z2r[r][i];
+        const T im1 = pr * z[r][i].y + pi * z[r][i].x;
+        const T im2 = pr * z2[r][i].y + pi * z2[r][i].x;
         acc[r][0].add((T)col.x * im1);
         acc[r][1].add((T)col.y * im1);
         acc[r][2].add(im2);
