@@ -96,7 +96,7 @@ __device__ __forceinline__ void warp_twosum(float &h, float &l) {
 }
 
 template <int MODE, int NPOT>
-__global__ void __launch_bounds__(256) k_pair(PairArgs A) {
+__global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) k_pair(PairArgs A) {
   typedef typename std::conditional<MODE == YG_FP64, double, float>::type T;
   const bool kahan = (MODE == YG_MIXED_KAHAN);
   __shared__ double red[8][NPOT * 7];
