@@ -392,6 +392,71 @@ def cpu_sample(natom, seconds_budget=20.0):
                                                         'ewald_reci': t_ew_full}}
 
 
+def _cpu_serving_request(idx):
+    """CPU time of one serving request (50 Verlet steps of 0.5 fs) with the
+    oracle as the force field, one thread."""
+    import types
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    from oracle import OracleForceField
+    from yaff_gb300.serve import make_workload
+    from yaff_gb300.units import femtosecond
+    from yaff_gb300.verlet import VerletIntegrator
+    r = make_workload(nreq=idx + 1, rate=0.0, seed=2024)[idx]
+    t0 = time.perf_counter()
+    orc = OracleForceField(r.spec)
+    orc.system = types.SimpleNamespace(pos=orc.pos, masses=r.spec['masses'])
+    vi = VerletIntegrator(orc, 0.5 * femtosecond, temp0=300.0, rng=np.random.default_rng(r.seed))
+    vi.run(r.nsteps)
+    return r.natom, time.perf_counter() - t0
+
+
+def _cpu_mc_trials(seed):
+    """CPU time per trial of the MC trial energy with the oracle (the
+    reference's algorithm: full force-field evaluations with nlow = nhigh
+    plus the structure-factor interaction), one thread, two trials."""
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import mc_oracle
+    from yaff_gb300 import configs
+    work = configs.mc_workload()
+    case = {k: work[k] for k in ('framework', 'guest', 'rcut', 'alpha', 'gcut', 'close_contact')}
+    rng = np.random.default_rng(100 + seed)
+    c = int(rng.integers(0, len(work['chains'])))
+    ch, kind, guest, newpos = configs.mc_trial_batch(rng, work, work['chains'], 2, chain_ids=[c])
+    t0 = time.perf_counter()
+    for t in range(len(ch)):
+        mc_oracle.trial_energy(case, list(work['chains'][c]), int(kind[t]), int(guest[t]), newpos[t])
+    return (time.perf_counter() - t0) / len(ch)
+
+
+def cpu_replicas():
+    """Replica baselines of the throughput workloads on all host cores: one
+    independent single-thread process per core.  Serving: requests of the
+    workload with natom <= 1,100 are timed and t = a N^2 + b N is fitted
+    (neighbour build and Ewald both grow as N^2 at fixed density), then
+    averaged over the workload's natom distribution.  MC: two trials per core."""
+    import multiprocessing as mp
+    from yaff_gb300.serve import make_workload
+    cores = os.cpu_count() or 1
+    reqs = make_workload(nreq=4096, rate=0.0, seed=2024)
+    small = [i for i, r in enumerate(reqs) if r.natom <= 1100][:cores]
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(cores) as pool:
+        served = pool.map(_cpu_serving_request, small)
+        per_trial = pool.map(_cpu_mc_trials, list(range(cores)))
+    n = np.array([x[0] for x in served], float)
+    t = np.array([x[1] for x in served])
+    coef, *_ = np.linalg.lstsq(np.stack([n * n, n], 1), t, rcond=None)
+    na = np.array([r.natom for r in reqs], float)
+    mean_t = float(coef[0] * (na * na).mean() + coef[1] * na.mean())
+    mt = float(np.mean(per_trial))
+    return {'cores': cores, 'kind': 'port',
+            'serving': {'requests_per_s': cores / mean_t, 'mean_request_s': mean_t,
+                        'sample': '%d requests (natom %d-%d) timed with the oracle, t = %.3g N^2 + %.3g N' %
+                                  (len(small), int(n.min()), int(n.max()), coef[0], coef[1])},
+            'mc': {'trials_per_s': cores / mt, 'seconds_per_trial': mt,
+                   'sample': '%d trials on the 2,000-atom framework with the oracle' % (2 * cores)}}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -558,6 +623,12 @@ def main():
             out['mc_trials'] = run_mc(args)
         if args.nve_steps > 0 and world == 1:
             out['nve'] = run_nve(args)
+        if not args.no_cpu_baseline and world == 1 and (args.serving_requests > 0 or args.mc_rounds > 0):
+            rep = cpu_replicas()
+            if 'serving' in out:
+                out['serving']['cpu_replicas'] = dict(rep['serving'], cores=rep['cores'], kind=rep['kind'])
+            if 'mc_trials' in out:
+                out['mc_trials']['cpu_replicas'] = dict(rep['mc'], cores=rep['cores'], kind=rep['kind'])
         if not args.no_cpu_baseline:
             out['cpu_baseline'] = cpu_sample(args.natom)
         print(json.dumps(out))
