@@ -882,7 +882,7 @@ int yg_launch_ewald_reci(yg_ctx *ctx, int want_grad) {
     return YG_OK;
   }
   if (ctx->precision == YG_FP64) return run_reci<double, double, 2>(ctx, want_grad);
-  return run_reci<float, float, 4>(ctx, want_grad);
+  return run_reci<float, float, 2>(ctx, want_grad);
 }
 
 int yg_launch_ewald_corr(yg_ctx *ctx, int want_grad) {
