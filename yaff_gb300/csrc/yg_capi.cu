@@ -130,7 +130,7 @@ int yg_ensure(yg_ctx *ctx, void **ptr, size_t *cap, size_t bytes) {
 
 namespace {
 __global__ void k_total(const double *__restrict__ part_ev, const double *__restrict__ part_gpos, int64_t natom,
-                        int mask, int want_gpos, double *__restrict__ out) {
+                        int mask, int want_gpos, double *__restrict__ out, int *__restrict__ nan_flag) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < 10) {
     double s = 0.0;
@@ -144,6 +144,7 @@ __global__ void k_total(const double *__restrict__ part_ev, const double *__rest
     for (int p = 0; p < YG_NPART; p++)
       if (mask & (1 << p)) s += part_gpos[(int64_t)p * natom * 3 + t];
     out[16 + t] = s;
+    if (isnan(s)) atomicOr(nan_flag, 1);
   }
 }
 
@@ -622,17 +623,27 @@ int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double 
   const int64_t n3 = c->natom * 3;
   const int want_gpos = gpos != nullptr;
   int64_t nthreads = want_gpos ? std::max<int64_t>(n3, 16) : 16;
+  YG_CUDA(cudaMemsetAsync(c->d_status + YG_ST_NANGRAD, 0, sizeof(int), c->stream));
   k_total<<<yg_blocks(nthreads, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom, part_mask,
-                                                          want_gpos, c->d_total);
+                                                          want_gpos, c->d_total, c->d_status + YG_ST_NANGRAD);
   YG_LAUNCH_CHECK(c, "k_total");
   size_t bytes = (16 + (want_gpos ? n3 : 0)) * sizeof(double);
+  YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->h_total, c->d_total, bytes, cudaMemcpyDeviceToHost, c->stream));
   YG_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->h_status[YG_ST_TIMEOUT]) {
+    yg_set_error("a bounded wait on an asynchronous copy gave up; results are invalid");
+    return YG_ERR_CUDA;
+  }
   if (energy) *energy = c->h_total[0];
   if (vtens) memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
   if (part_energies) memcpy(part_energies, c->h_total + 10, YG_NPART * sizeof(double));
   if (gpos) memcpy(gpos, c->h_total + 16, n3 * sizeof(double));
   if (std::isnan(c->h_total[0])) return YG_ERR_NAN;
+  if (want_gpos && c->h_status[YG_ST_NANGRAD]) {
+    yg_set_error("not-a-number in the gradient");
+    return YG_ERR_NAN;
+  }
   return YG_OK;
 }
 

@@ -23,6 +23,7 @@
 #define YG_ST_EXACT 2        // candidates decided by the exact FP64 test
 #define YG_ST_BADCELL 3      // non-finite position met while binning
 #define YG_ST_TIMEOUT 4      // a bounded wait on an asynchronous copy gave up
+#define YG_ST_NANGRAD 5      // a summed gradient component was NaN (yg_get_total)
 #define YG_ST_NWORDS 8
 
 // Neighbour entry: x = partner (sorted index), y = meta bits.

@@ -28,6 +28,15 @@ def get_default_precision():
     return _default_precision
 
 
+def _pinned(shape):
+    """(array, owner): a zero-filled float64 host array in page-locked
+    memory (host-to-device copies from it are asynchronous DMA) and the
+    tensor that owns the memory (keep it alive as long as the array)."""
+    import torch
+    t = torch.zeros(shape, dtype=torch.float64, pin_memory=True)
+    return t.numpy(), t
+
+
 def device_of(system, precision=None, stream=None):
     """The DeviceSystem of a System, created on first use (on `stream`, a
     cudaStream_t handle as int, default: the legacy default stream)."""
@@ -60,7 +69,9 @@ class DeviceSystem(object):
         self.scalings_obj = None
         self.ewald_key = None
         self.valence_key = None
-        self._pos_staging = np.zeros((self.natom, 3))
+        self._pos_staging, self._pos_owner = _pinned((self.natom, 3))
+        self._parts_buf = np.zeros(_lib.NPART)
+        self._vt_buf = np.zeros(9)
         # bumped whenever the device list is invalidated (cell or scalings)
         self.list_epoch = 0
         self.sync_cell()
@@ -169,6 +180,23 @@ class DeviceSystem(object):
         v = None if vtens is None else np.zeros(9)
         check(self.lib.yg_get_total(self.ctx, mask, ctypes.byref(e), ptr(g), ptr(v), ptr(parts)), 'yg_get_total')
         return e.value, g, None if v is None else v.reshape(3, 3), parts
+
+    def get_total_into(self, mask, gpos=None, vtens=None):
+        """(energy, part energies); the summed gradient is written into gpos
+        and the virial into vtens (overwritten, float64 C-contiguous), each
+        skipped when None.  Raises ValueError on NaN energy or gradient."""
+        e = ctypes.c_double()
+        parts = self._parts_buf
+        g = gpos
+        if g is not None and not (g.flags['C_CONTIGUOUS'] and g.dtype == np.float64):
+            g = np.zeros((self.natom, 3))
+        v = self._vt_buf if vtens is not None else None
+        check(self.lib.yg_get_total(self.ctx, mask, ctypes.byref(e), ptr(g), ptr(v), ptr(parts)), 'yg_get_total')
+        if gpos is not None and g is not gpos:
+            gpos[:] = g
+        if vtens is not None:
+            vtens[:] = v.reshape(3, 3)
+        return e.value, parts.copy()
 
     def launch_count(self):
         return int(self.lib.yg_launch_count(self.ctx))

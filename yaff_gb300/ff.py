@@ -41,6 +41,11 @@ class ForcePart(object):
         self.clear()
 
     def _fetch(self):
+        if self._stale:
+            # cleared results read as NaN (filled on first access, not per step)
+            self._stale = False
+            self._gpos[:] = np.nan
+            self._vtens[:] = np.nan
         if self._lazy is not None:
             dev, slot, want_g, want_v = self._lazy
             self._lazy = None
@@ -54,6 +59,7 @@ class ForcePart(object):
     @gpos.setter
     def gpos(self, value):
         self._lazy = None
+        self._stale = False
         self._gpos = value
 
     @property
@@ -64,14 +70,15 @@ class ForcePart(object):
     @vtens.setter
     def vtens(self, value):
         self._lazy = None
+        self._stale = False
         self._vtens = value
 
     def clear(self):
-        """Fill the cached results with NaN (they no longer hold)."""
+        """The cached results no longer hold: energy, gpos and vtens read as
+        NaN until the next compute."""
         self._lazy = None
         self.energy = np.nan
-        self._gpos[:] = np.nan
-        self._vtens[:] = np.nan
+        self._stale = True
 
     def update_rvecs(self, rvecs):
         self.clear()
@@ -82,6 +89,7 @@ class ForcePart(object):
     def compute(self, gpos=None, vtens=None):
         """Energy; the gradient and virial are ADDED to gpos / vtens."""
         self._lazy = None
+        self._stale = False
         my_gpos = None
         if gpos is not None:
             my_gpos = self._gpos
@@ -190,25 +198,51 @@ class ForceField(ForcePart):
                 continue
             part._launch(want_grad)
             mask |= 1 << part.device_slot
-        energy, g, v, part_e = dev.get_total(mask, gpos, vtens)
+        # the summed gradient and virial land directly in the caller's arrays;
+        # NaN in the gradient is detected on the device
+        energy, part_e = dev.get_total_into(mask, gpos, vtens)
         for part in self.parts:
             if isinstance(part, ForcePartEwaldNeutralizing):
+                # position independent, no gradient (ff.py:653-669)
                 pv = np.zeros((3, 3)) if vtens is not None else None
-                pg = np.zeros((self.system.natom, 3)) if gpos is not None else None
-                e = part.compute(pg, pv)
-                host_energy += e
+                e = part._internal_compute(None, pv)
+                part.energy = e
+                part._lazy = None
+                part._stale = False
+                part._gpos[:] = 0.0
                 if pv is not None:
+                    part._vtens[:] = pv
                     host_vtens += pv
+                host_energy += e
                 continue
             slot = part._slot_index()
             part.energy = part_e[slot]
             part._lazy = (dev, slot, gpos is not None, vtens is not None)
         energy += host_energy
-        if gpos is not None:
-            gpos[:] = g
         if vtens is not None:
-            vtens[:] = v + host_vtens
+            vtens += host_vtens
         return energy
+
+    def compute(self, gpos=None, vtens=None):
+        """Energy; the gradient and virial are ADDED to gpos / vtens.  On the
+        fused device path the result is written once into the force field's
+        own buffers and added to the caller's (no extra passes over gpos)."""
+        if self._device_parts() is None:
+            return ForcePart.compute(self, gpos, vtens)
+        self._lazy = None
+        self._stale = False
+        my_gpos = self._gpos if gpos is not None else None
+        my_vtens = self._vtens if vtens is not None else None
+        self.energy = self._internal_compute(my_gpos, my_vtens)
+        if np.isnan(self.energy):
+            raise ValueError('The energy is not-a-number (nan).')
+        if gpos is not None:
+            gpos += my_gpos
+        if vtens is not None:
+            if np.isnan(my_vtens).any():
+                raise ValueError('Some vtens element(s) is/are not-a-number (nan).')
+            vtens += my_vtens
+        return self.energy
 
     def device_md_terms(self):
         """(result-slot mask, constant energy) for an integrator that sums the
