@@ -125,7 +125,7 @@ __device__ __forceinline__ void cmac(double2 &acc, double2 x, double2 y) {
 }
 
 template <typename T> struct SfacCfg;
-template <> struct SfacCfg<float> { enum { KA = 32, ATB = 256 }; };
+template <> struct SfacCfg<float> { enum { KA = 32, ATB = 512 }; };
 template <> struct SfacCfg<double> { enum { KA = 16, ATB = 256 }; };
 
 // ---- bulk copies into shared memory completed on an mbarrier ----
