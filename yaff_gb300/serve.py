@@ -33,9 +33,9 @@ import numpy as np
 from . import configs
 from .units import femtosecond
 
-__all__ = ['Request', 'make_workload', 'estimate_bytes', 'ServingEngine', 'run_sequential', 'summarize']
+__all__ = ['Request', 'make_workload', 'estimate_bytes', 'serve_request', 'ServingEngine', 'run_sequential',
+           'summarize']
 
-MIB = 1 << 20
 
 
 class Request(object):
