@@ -308,9 +308,10 @@ int yg_mc_apply(yg_mc *mc, int64_t napply, const int32_t *trial_index);
 int64_t yg_mc_launch_count(yg_mc *mc);
 
 /* Measurement utility (no reference counterpart): FMA-chain throughput of
- * the FP32 (fp64 == 0) or FP64 CUDA-core pipe in TFLOP/s (FMA = 2 flops), the
- * roofline denominator of the pair and Ewald kernels.  Negative on error. */
-double yg_probe_peak(int fp64, void *stream);
+ * the CUDA-core pipes in TFLOP/s (FMA = 2 flops), the roofline denominator of
+ * the pair and Ewald kernels.  kind 0: scalar FP32 FMAs; 1: FP64 FMAs; 2:
+ * packed FP32 pairs (f32x2, two FMAs per instruction).  Negative on error. */
+double yg_probe_peak(int kind, void *stream);
 
 #ifdef __cplusplus
 }

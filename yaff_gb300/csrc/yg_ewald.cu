@@ -179,6 +179,54 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
   return false;
 }
 
+// The S-pass MACs of one warp over the staged rows of a chunk: columns are
+// formed as X = E0 E1 (conjugated for negative g0, g1; zero for padding
+// columns) and acc[i][j] += X_i Y_j for the warp's nj m values.  FP32 takes
+// nj as the compile-time count NJ, so the m loop is straight-line code whose
+// shared loads the compiler issues ahead of the FMAs; FP64 (NJ == 0, twice
+// the registers per value) keeps a run-time count.
+template <typename T, int NJ>
+__device__ __forceinline__ void sfac_rows(const typename C2<T>::t *__restrict__ buf, int nrow, int L,
+                                          const int (&o0)[4], const int (&o1)[4], const T (&s0)[4],
+                                          const T (&s1)[4], const T (&ok)[4], int yb, int nj,
+                                          typename C2<T>::t (&acc)[4][8]) {
+  typedef typename C2<T>::t CT;
+  const int NY = NJ > 0 ? NJ : 1;
+#pragma unroll(NJ > 0 ? 1 : 2)
+  for (int la = 0; la < nrow; la++) {
+    const CT *row = buf + la * L;
+    CT y[NY];
+    if (NJ > 0) {
+#pragma unroll
+      for (int j = 0; j < NY; j++) y[j] = row[yb + 4 * j];
+    }
+    CT x[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      CT e0 = row[o0[i]], e1 = row[o1[i]];
+      e0.x *= ok[i];
+      e0.y *= s0[i] * ok[i];
+      e1.y *= s1[i];
+      x[i] = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
+    }
+    if (NJ > 0) {
+#pragma unroll
+      for (int j = 0; j < NY; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) cmac(acc[i][j], x[i], y[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if (j < nj) {
+          const CT yj = row[yb + 4 * j];
+#pragma unroll
+          for (int i = 0; i < 4; i++) cmac(acc[i][j], x[i], yj);
+        }
+      }
+    }
+  }
+}
+
 // S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
 // The table rows of KA atoms are staged in shared memory with coalesced
 // copies.  Lane l owns columns l, l+32, l+64, l+96 of the tile and forms
@@ -249,25 +297,20 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
         break;
       }
       const CT *buf = sRow + (size_t)(c & 1) * KA * L;
-#pragma unroll 2
-      for (int la = 0; la < nrow; la++) {
-        const CT *row = buf + la * L;
-        CT x[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          CT e0 = row[o0[i]], e1 = row[o1[i]];
-          e0.x *= ok[i];
-          e0.y *= s0[i] * ok[i];
-          e1.y *= s1[i];
-          x[i] = cmk<T>(e0.x * e1.x - e0.y * e1.y, e0.x * e1.y + e0.y * e1.x);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          if (j < nj) {
-            const CT y = row[yb + 4 * j];
-#pragma unroll
-            for (int i = 0; i < 4; i++) cmac(acc[i][j], x[i], y);
-          }
+      if (sizeof(T) == 8) {
+        sfac_rows<T, 0>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc);
+      } else {
+        // nj is warp-uniform: one branch per chunk selects a straight-line body
+        switch (nj) {
+          case 8: sfac_rows<T, 8>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 7: sfac_rows<T, 7>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 6: sfac_rows<T, 6>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 5: sfac_rows<T, 5>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 4: sfac_rows<T, 4>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 3: sfac_rows<T, 3>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 2: sfac_rows<T, 2>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          case 1: sfac_rows<T, 1>(buf, nrow, L, o0, o1, s0, s1, ok, yb, nj, acc); break;
+          default: break;
         }
       }
       __syncthreads();  // every thread is done with this buffer before it is refilled
@@ -445,9 +488,10 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
   const int nm = G2 + 1;
   const int L = ew_row_stride(G0, G1, G2);
   const int LE = G0 + G1 + 2;                          // E0 and E1 entries of a row
+  const int LEs = LE | 1;  // odd row stride: the 16 rows one load touches fall in distinct banks
   CT *sY = reinterpret_cast<CT *>(smem_raw);          // [nm][NA]
-  CT *sE = sY + (size_t)nm * NA;                       // [NA][LE]
-  CT *sWb = sE + (size_t)NA * LE;                      // 2 x [nm][EW_FC]
+  CT *sE = sY + (size_t)nm * NA;                       // [NA][LEs]
+  CT *sWb = sE + (size_t)NA * LEs;                     // 2 x [nm][EW_FC]
   int4 *scolb = reinterpret_cast<int4 *>(sWb + (size_t)2 * nm * EW_FC);  // 2 x [EW_FC]
   const int ta = threadIdx.x & 15, tc = threadIdx.x >> 4;
   const int abase = a0 + blockIdx.x * NA;
@@ -464,7 +508,7 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
   for (int v = threadIdx.x; v < NA * LE; v += blockDim.x) {
     const int la = v / LE, e = v % LE;
     const int a = abase + la;
-    sE[v] = (a < a1) ? tab[(int64_t)a * L + e] : cmk<T>((T)0, (T)0);
+    sE[la * LEs + e] = (a < a1) ? tab[(int64_t)a * L + e] : cmk<T>((T)0, (T)0);
   }
   __syncthreads();
   // column tiles (weights tile-ordered: [m][EW_FC], plus the 64 column
@@ -539,7 +583,7 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
       const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = col.y < 0 ? -col.y : col.y;
 #pragma unroll
       for (int r = 0; r < RA; r++) {
-        const CT *row = sE + (size_t)(ta + 16 * r) * LE;
+        const CT *row = sE + (size_t)(ta + 16 * r) * LEs;
         CT e0 = row[ag0], e1 = row[G0 + 1 + ag1];
         if (col.x < 0) e0.y = -e0.y;
         if (col.y < 0) e1.y = -e1.y;
@@ -680,7 +724,7 @@ static int smem_optin(const void *kernel, size_t need) {
 
 template <typename T> size_t force_smem(int G0, int G1, int nm, int RA) {
   const size_t ct = sizeof(typename C2<T>::t);
-  size_t a = (size_t)nm * 16 * RA * ct + (size_t)16 * RA * (G0 + G1 + 2) * ct + (size_t)2 * nm * EW_FC * ct +
+  size_t a = (size_t)nm * 16 * RA * ct + (size_t)16 * RA * ((G0 + G1 + 2) | 1) * ct + (size_t)2 * nm * EW_FC * ct +
              2 * EW_FC * sizeof(int4);
   size_t b = (size_t)16 * 16 * RA * 3 * sizeof(double);
   return a > b ? a : b;

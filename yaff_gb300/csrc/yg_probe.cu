@@ -3,8 +3,10 @@
 // The pair and Ewald kernels run on the FP32 (mixed) or FP64 (plain) CUDA-core
 // pipes, not on the tensor cores, so their roofline denominator is the FMA
 // issue rate of those pipes.  This probe runs independent FMA chains on every
-// SM and reports TFLOP/s (one FMA = 2 flops).  It is bounded: a fixed number
-// of iterations, no waits, no atomics.
+// SM and reports TFLOP/s (one FMA = 2 flops): scalar FP32, FP64, or packed
+// FP32 pairs (f32x2, two FMAs per instruction), so the FP32 denominator can be
+// taken as the larger of the scalar and packed rates.  It is bounded: a fixed
+// number of iterations, no waits, no atomics.
 #include "yg_internal.cuh"
 
 namespace {
@@ -24,22 +26,47 @@ __global__ void __launch_bounds__(256) k_fma_chain(T *out, int iters, T a, T b) 
   if (s == (T)12345.678) out[threadIdx.x] = s;  // keeps the chains live
 }
 
-template <typename T>
-double run_probe(cudaStream_t st) {
+// CH chains of float pairs: every step is one packed f32x2 FMA per chain.
+template <int CH>
+__global__ void __launch_bounds__(256) k_fma2_chain(float *out, int iters, float a, float b) {
+  float2 x[CH];
+#pragma unroll
+  for (int c = 0; c < CH; c++) x[c] = make_float2((float)(threadIdx.x + c), (float)(threadIdx.x - c));
+  const float2 a2 = make_float2(a, a), b2 = make_float2(b, b);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < CH; c++) x[c] = __ffma2_rn(x[c], a2, b2);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < CH; c++) s += x[c].x + x[c].y;
+  if (s == 12345.678f) out[threadIdx.x] = s;  // keeps the chains live
+}
+
+// kind: 0 scalar FP32, 1 FP64, 2 packed FP32 pairs.
+double run_probe(int kind, cudaStream_t st) {
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  T *out = nullptr;
-  if (cudaMalloc(&out, 256 * sizeof(T)) != cudaSuccess) return -1.0;
+  double *out = nullptr;
+  if (cudaMalloc(&out, 256 * sizeof(double)) != cudaSuccess) return -1.0;
   const int CH = 8;
-  const int iters = sizeof(T) == 8 ? 256 : 8192;
+  const int iters = kind == 1 ? 256 : 8192;
   const int blocks = nsm * 8;
+  auto launch = [&]() {
+    if (kind == 0)
+      k_fma_chain<float, CH><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
+    else if (kind == 1)
+      k_fma_chain<double, CH><<<blocks, 256, 0, st>>>(out, iters, 0.999, 0.001);
+    else
+      k_fma2_chain<CH><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
+  };
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_fma_chain<T, CH><<<blocks, 256, 0, st>>>(out, iters, (T)0.999, (T)0.001);
+  launch();
   cudaEventRecord(e0, st);
-  for (int r = 0; r < 5; r++) k_fma_chain<T, CH><<<blocks, 256, 0, st>>>(out, iters, (T)0.999, (T)0.001);
+  for (int r = 0; r < 5; r++) launch();
   cudaEventRecord(e1, st);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -48,13 +75,14 @@ double run_probe(cudaStream_t st) {
   cudaEventDestroy(e1);
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return -1.0;
-  double flops = 5.0 * 2.0 * CH * (double)iters * blocks * 256.0;
+  const double fma_per_step = (kind == 2 ? 2.0 : 1.0) * CH;
+  double flops = 5.0 * 2.0 * fma_per_step * (double)iters * blocks * 256.0;
   return flops / (ms * 1e-3) / 1e12;
 }
 
 }  // namespace
 
-extern "C" double yg_probe_peak(int fp64, void *stream) {
-  cudaStream_t st = (cudaStream_t)stream;
-  return fp64 ? run_probe<double>(st) : run_probe<float>(st);
+extern "C" double yg_probe_peak(int kind, void *stream) {
+  if (kind < 0 || kind > 2) return -1.0;
+  return run_probe(kind, (cudaStream_t)stream);
 }
