@@ -116,14 +116,16 @@ def peaks():
 
 def fp32_fma_peak(torch):
     """FP32 CUDA-core peak (TFLOP/s, FMA = 2 flops) measured with FMA-chain
-    kernels of the library, scalar and packed f32x2: (peak, {kind: TFLOP/s}),
-    peak = the larger of the two.  The measured-peaks file holds only HBM and
-    bf16 tensor figures, and the pair and Ewald kernels use neither."""
+    kernels of the library, scalar, packed f32x2 and the two interleaved:
+    (peak, {kind: TFLOP/s}), peak = the largest.  The measured-peaks file
+    holds only HBM and bf16 tensor figures, and the pair and Ewald kernels
+    use neither."""
     import ctypes
     from yaff_gb300 import _lib
     lib = _lib.load()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    both = {'scalar': float(lib.yg_probe_peak(0, st)), 'f32x2': float(lib.yg_probe_peak(2, st))}
+    both = {'scalar': float(lib.yg_probe_peak(0, st)), 'f32x2': float(lib.yg_probe_peak(2, st)),
+            'f32x2+scalar': float(lib.yg_probe_peak(3, st))}
     v = max(both.values())
     return (v if v > 0 else None), both
 
@@ -279,8 +281,8 @@ def run_gb300(args, world, rank, local):
     row = (int(sum(reci.gmax)) + 4) // 2 * 2
     traffic = 19.42e6 * (natom * row) / (20000 * 60)
     roof = {'bound': 'fp32', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s',
-            'peak': fp32_peak, 'peak_source': 'FP32 FMA-chain kernels in bench.py, the larger of scalar and packed '
-                                              'f32x2 (measured-peaks file has no FP32 figure)',
+            'peak': fp32_peak, 'peak_source': 'FP32 FMA-chain kernels in bench.py, the largest of scalar, packed '
+                                              'f32x2 and both interleaved (measured-peaks file has no FP32 figure)',
             'peak_probe_tflops': fp32_probe,
             'frac': (flops / t_reci / 1e12) / fp32_peak if fp32_peak else None, 'traffic': traffic,
             'traffic_source': 'ncu dram read+write of k_sfac + k_ewald_force at 20,000 atoms, scaled by atoms x row',

@@ -310,7 +310,8 @@ int64_t yg_mc_launch_count(yg_mc *mc);
 /* Measurement utility (no reference counterpart): FMA-chain throughput of
  * the CUDA-core pipes in TFLOP/s (FMA = 2 flops), the roofline denominator of
  * the pair and Ewald kernels.  kind 0: scalar FP32 FMAs; 1: FP64 FMAs; 2:
- * packed FP32 pairs (f32x2, two FMAs per instruction).  Negative on error. */
+ * packed FP32 pairs (f32x2, two FMAs per instruction); 3: packed and scalar
+ * FP32 FMAs interleaved one to one.  Negative on error. */
 double yg_probe_peak(int kind, void *stream);
 
 #ifdef __cplusplus

@@ -37,6 +37,10 @@ namespace {
 #define EW_FC 64     // columns per force-pass tile
 #define EW_MS 32     // m values per S-pass slab
 #define EW_MAXM 64   // largest supported G2 + 1
+#define EW_FEPI 3    // force-pass cost of a column tile's epilogue, in m iterations
+#ifndef YG_FORCE_MINB
+#define YG_FORCE_MINB 3  // resident FP32 force-pass blocks per SM the register budget is sized for
+#endif
 
 // Row stride of the per-atom phase tables: the logical length G0+G1+G2+3
 // rounded up to an even count, so rows of FP32 complex values are whole
@@ -227,7 +231,9 @@ __device__ __forceinline__ void sfac_rows(const typename C2<T>::t *__restrict__ 
   }
 }
 
-// S pass.  grid = (column tiles, atom chunks, m slabs), 128 threads = 4 warps.
+// S pass.  grid = (atom chunks, column tiles, m slabs), 128 threads = 4 warps:
+// blocks start in tile-major order, the tiles sorted by decreasing extent,
+// so the short blocks of the last tiles fill the tail of the launch.
 // The table rows of KA atoms are staged in shared memory with coalesced
 // copies.  Lane l owns columns l, l+32, l+64, l+96 of the tile and forms
 // X = E0 E1 for them from the staged rows; warp w owns m = w + 4j, j < 8,
@@ -245,11 +251,11 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   __shared__ unsigned long long bars[2];
   CT *sRow = reinterpret_cast<CT *>(sfac_smem);      // 2 x [KA][L] table rows
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int tile = blockIdx.x, slab = blockIdx.z;
+  const int tile = blockIdx.y, slab = blockIdx.z;
   const int mb = slab * EW_MS;
   const int Mt = cols[tile * EW_SC].w + 1 - mb;
   const int nj = (Mt > w) ? min(8, (Mt - w + 3) / 4) : 0;
-  const int abeg = a0 + blockIdx.y * ATB;
+  const int abeg = a0 + blockIdx.x * ATB;
   const int aend = min(a1, abeg + ATB);
   CT acc[4][8];
 #pragma unroll
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   }
   // partial layout: [chunk][tile][slab][c][m]
   typedef typename C2<TA>::t CA;
-  const int64_t base = (((int64_t)blockIdx.y * nstile + tile) * nslab + slab) * (EW_SC * EW_MS);
+  const int64_t base = (((int64_t)blockIdx.x * nstile + tile) * nslab + slab) * (EW_SC * EW_MS);
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int c = lane + 32 * i;
@@ -471,16 +477,35 @@ template <> struct CompAcc<float> {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-// Force pass.  grid = atom tiles (16*RA atoms) of one group; 256 threads:
-// ta = tid % 16 owns atoms ta + 16 r (r < RA), tc = tid / 16 owns columns
-// 4 tc .. 4 tc + 3 of each 64-column tile (shared loads of Y are contiguous
-// across lanes, loads of W broadcast).  Tiles follow the sorted column list,
-// so the m loop of a tile stops at its extent.
+// Force pass.  One block per atom tile (16*RA atoms) of one group, over all
+// column tiles -- except the tiles of the launch's last, partial wave, which
+// are split into `nsplit` blocks over column ranges of equal cost (fpre =
+// prefix sums of the column tiles' costs) so that the last wave is as full
+// as the others; those blocks write their sums to pieces
+// [tile - nfull][part][NA][3] that k_ewald_force_combine adds in order.
+// 256 threads: ta = tid % 16 owns atoms ta + 16 r (r < RA), tc = tid / 16
+// owns columns 4 tc .. 4 tc + 3 of each 64-column tile (shared loads of Y
+// are contiguous across lanes, loads of W broadcast).  Tiles follow the
+// sorted column list, so the m loop of a tile stops at its extent.
+__device__ __forceinline__ int split_cut(const int *__restrict__ fpre, int nftile, int part, int nsplit) {
+  // first column tile whose prefix cost reaches part/nsplit of the total
+  const long long want = (long long)fpre[nftile] * part;
+  int lo = 0, hi = nftile;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)fpre[mid] * nsplit >= want) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
 template <typename T, int RA>
-__global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__restrict__ tab, int a0, int a1,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? YG_FORCE_MINB : 1) k_ewald_force(const typename C2<T>::t *__restrict__ tab, int a0, int a1,
                                                      int G0, int G1, int G2, const int4 *__restrict__ cols,
-                                                     int nftile, const typename C2<T>::t *__restrict__ Wt,
-                                                     double *__restrict__ gfrac, int *__restrict__ status) {
+                                                     int nftile, const int *__restrict__ fpre, int nfull,
+                                                     int nsplit, const typename C2<T>::t *__restrict__ Wt,
+                                                     double *__restrict__ gfrac, double *__restrict__ piece,
+                                                     int *__restrict__ status) {
   typedef typename C2<T>::t CT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long bars[2];
@@ -494,7 +519,17 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
   CT *sWb = sE + (size_t)NA * LEs;                     // 2 x [nm][EW_FC]
   int4 *scolb = reinterpret_cast<int4 *>(sWb + (size_t)2 * nm * EW_FC);  // 2 x [EW_FC]
   const int ta = threadIdx.x & 15, tc = threadIdx.x >> 4;
-  const int abase = a0 + blockIdx.x * NA;
+  int atile, ct0 = 0, ct1 = nftile, part = -1;
+  if ((int)blockIdx.x < nfull) {
+    atile = blockIdx.x;
+  } else {
+    const int idx = blockIdx.x - nfull;
+    atile = nfull + idx / nsplit;
+    part = idx % nsplit;
+    ct0 = split_cut(fpre, nftile, part, nsplit);
+    ct1 = split_cut(fpre, nftile, part + 1, nsplit);
+  }
+  const int abase = a0 + atile * NA;
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
@@ -513,31 +548,32 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
   __syncthreads();
   // column tiles (weights tile-ordered: [m][EW_FC], plus the 64 column
   // descriptors) through double-buffered bulk copies
-  auto issue = [&](int t) {
+  auto issue = [&](int t, int k) {
     const int4 *tcols = cols + t * EW_FC;
     const int Mt = tcols[0].w + 1;
     const unsigned wbytes = (unsigned)(Mt * EW_FC * sizeof(CT));
     const unsigned cbytes = (unsigned)(EW_FC * sizeof(int4));
-    unsigned long long *bar = &bars[t & 1];
+    unsigned long long *bar = &bars[k & 1];
     bulk_expect(bar, wbytes + cbytes);
-    bulk_copy(sWb + (size_t)(t & 1) * nm * EW_FC, Wt + (size_t)t * nm * EW_FC, wbytes, bar);
-    bulk_copy(scolb + (t & 1) * EW_FC, tcols, cbytes, bar);
+    bulk_copy(sWb + (size_t)(k & 1) * nm * EW_FC, Wt + (size_t)t * nm * EW_FC, wbytes, bar);
+    bulk_copy(scolb + (k & 1) * EW_FC, tcols, cbytes, bar);
   };
-  if (threadIdx.x == 0 && nftile > 0) issue(0);
+  if (threadIdx.x == 0 && ct1 > ct0) issue(ct0, 0);
   CompAcc<T> acc[RA][3];
 #pragma unroll
   for (int r = 0; r < RA; r++)
 #pragma unroll
     for (int q = 0; q < 3; q++) acc[r][q].init();
-  for (int t = 0; t < nftile; t++) {
-    if (threadIdx.x == 0 && t + 1 < nftile) issue(t + 1);
-    const bool arrived = mbar_wait(&bars[t & 1], (unsigned)((t >> 1) & 1), status);
+  for (int t = ct0; t < ct1; t++) {
+    const int k = t - ct0;  // buffer k & 1, phase (k >> 1) & 1
+    if (threadIdx.x == 0 && t + 1 < ct1) issue(t + 1, k + 1);
+    const bool arrived = mbar_wait(&bars[k & 1], (unsigned)((k >> 1) & 1), status);
     if (__syncthreads_or(!arrived)) {
-      if (threadIdx.x == 0 && t + 1 < nftile) mbar_wait(&bars[(t + 1) & 1], (unsigned)(((t + 1) >> 1) & 1), status);
+      if (threadIdx.x == 0 && t + 1 < ct1) mbar_wait(&bars[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1), status);
       break;
     }
-    const CT *sW = sWb + (size_t)(t & 1) * nm * EW_FC;
-    const int4 *scol = scolb + (t & 1) * EW_FC;
+    const CT *sW = sWb + (size_t)(k & 1) * nm * EW_FC;
+    const int4 *scol = scolb + (k & 1) * EW_FC;
     const int Mt = scol[0].w + 1;
     CT z[RA][4], z2[RA][4];
 #pragma unroll
@@ -606,14 +642,31 @@ __global__ void __launch_bounds__(256) k_ewald_force(const typename C2<T>::t *__
 #pragma unroll
     for (int q = 0; q < 3; q++) red[((size_t)tc * NA + ta + 16 * r) * 3 + q] = acc[r][q].value();
   __syncthreads();
+  double *out = part < 0 ? nullptr : piece + ((int64_t)(atile - nfull) * nsplit + part) * NA * 3;
   for (int v = threadIdx.x; v < NA * 3; v += blockDim.x) {
     const int la = v / 3, q = v % 3;
     const int a = abase + la;
     if (a >= a1) continue;
     double s = 0.0;
     for (int g = 0; g < 16; g++) s += red[((size_t)g * NA + la) * 3 + q];
-    gfrac[(int64_t)a * 3 + q] = s;
+    if (out) out[v] = s;
+    else gfrac[(int64_t)a * 3 + q] = s;
   }
+}
+
+// Gradient sums of the split atom tiles: their pieces added in part order.
+__global__ void k_ewald_force_combine(const double *__restrict__ piece, int a0, int a1, int NA, int nfull,
+                                      int nsplit, double *__restrict__ gfrac) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t first = (int64_t)a0 + (int64_t)nfull * NA;
+  if (idx >= (a1 - first) * 3) return;
+  const int64_t la_all = idx / 3;
+  const int q = (int)(idx % 3);
+  const int64_t tile = la_all / NA;
+  const int la = (int)(la_all % NA);
+  double s = 0.0;
+  for (int p = 0; p < nsplit; p++) s += piece[((tile * nsplit + p) * NA + la) * 3 + q];
+  gfrac[(first + la_all) * 3 + q] = s;
 }
 
 // gpos = -2 pi (b0 f0 + b1 f1 + b2 f2) / dielectric (orig order).
@@ -722,6 +775,26 @@ static int smem_optin(const void *kernel, size_t need) {
   return YG_OK;
 }
 
+// Blocks of a kernel the device holds at once (all SMs), cached per
+// (kernel, dynamic shared memory).
+static int resident_blocks(const void *fn, int threads, size_t smem, yg_occ *oc, int *blocks) {
+  if (oc->fn != fn || oc->smem != smem || oc->blocks <= 0) {
+    int dev = 0, nsm = 0, occ = 0;
+    YG_CUDA(cudaGetDevice(&dev));
+    YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    YG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
+    if (occ < 1) {
+      yg_set_error("Ewald kernel does not fit on a multiprocessor");
+      return YG_ERR_UNSUPPORTED;
+    }
+    oc->fn = fn;
+    oc->smem = smem;
+    oc->blocks = occ * nsm;
+  }
+  *blocks = oc->blocks;
+  return YG_OK;
+}
+
 template <typename T> size_t force_smem(int G0, int G1, int nm, int RA) {
   const size_t ct = sizeof(typename C2<T>::t);
   size_t a = (size_t)nm * 16 * RA * ct + (size_t)16 * RA * ((G0 + G1 + 2) | 1) * ct + (size_t)2 * nm * EW_FC * ct +
@@ -773,7 +846,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
       continue;
     }
     int nch = (int)((n + ATB - 1) / ATB);
-    dim3 grid(nstile, nch, nslab);
+    dim3 grid(nch, nstile, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     const size_t ssm = (size_t)2 * SfacCfg<T>::KA * Lp * sizeof(CT);
     if ((rc = smem_optin((const void *)k_sfac<T, TA>, ssm))) return rc;
@@ -813,16 +886,35 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
   size_t smem = force_smem<T>(G0, G1, nm, RA);
   if ((rc = smem_optin((const void *)k_ewald_force<T, RA>, smem))) return rc;
-  const int gidx[3] = {0, 1, 2};
+  const int NA = 16 * RA;
+  int slots;
+  if ((rc = resident_blocks((const void *)k_ewald_force<T, RA>, 256, smem, &ctx->ew_occ_f, &slots))) return rc;
   for (int g = 0; g < nS; g++) {
     int64_t n = gb[g][1] - gb[g][0];
     if (n <= 0) continue;
-    const CT *Wg = (const CT *)ctx->d_ew_W + (size_t)(ngroup == 1 ? 0 : gidx[g]) * wstride;
-    int nblk = (int)((n + 16 * RA - 1) / (16 * RA));
+    const CT *Wg = (const CT *)ctx->d_ew_W + (size_t)(ngroup == 1 ? 0 : g) * wstride;
+    // whole atom tiles fill the full waves; the tiles of the last, partial
+    // wave are split over column ranges so that it is as full as the others
+    const int nat = (int)((n + NA - 1) / NA);
+    const int rem = nat % slots;
+    int nsplit = rem > 0 ? std::min(nftile, slots / rem) : 1;
+    if (nsplit < 2) nsplit = 1;
+    const int nfull = nsplit > 1 ? nat - rem : nat;
+    const int nblk = nfull + (nat - nfull) * nsplit;
+    if (nsplit > 1) {
+      const size_t pbytes = (size_t)(nat - nfull) * nsplit * NA * 3 * sizeof(double);
+      if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_fpiece, &ctx->ew_bytes_fpiece, pbytes))) return rc;
+    }
     k_ewald_force<T, RA><<<nblk, 256, smem, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
-                                                          (const int4 *)ctx->d_ew_tiles, nftile, Wg, ctx->d_ew_gpart,
+                                                          (const int4 *)ctx->d_ew_tiles, nftile, ctx->d_ew_fpre,
+                                                          nfull, nsplit, Wg, ctx->d_ew_gpart, ctx->d_ew_fpiece,
                                                           ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_ewald_force");
+    if (nsplit > 1) {
+      k_ewald_force_combine<<<yg_blocks((n - (int64_t)nfull * NA) * 3, 256), 256, 0, ctx->stream>>>(
+          ctx->d_ew_fpiece, (int)gb[g][0], (int)gb[g][1], NA, nfull, nsplit, ctx->d_ew_gpart);
+      YG_LAUNCH_CHECK(ctx, "k_ewald_force_combine");
+    }
   }
   k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
                                                            -6.2831853071795864769 / ctx->ew_diel, gpos);
@@ -893,6 +985,11 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
     if (i % EW_FC == 0 && tiles[i].w >= 0) nft++;
   }
   ctx->ew_nftile = nft;
+  // force-pass cost of each column tile (its m extent plus the epilogue), as prefix sums
+  std::vector<int> fpre(1, 0);
+  for (int t = 0; t < nft; t++) fpre.push_back(fpre.back() + tiles[(size_t)t * EW_FC].w + 1 + EW_FEPI);
+  yg_free(ctx, (void **)&ctx->d_ew_fpre);
+  ctx->d_ew_fpre = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_wslot);
   yg_free(ctx, (void **)&ctx->d_ew_pref);
   yg_free(ctx, (void **)&ctx->d_ew_tiles);
@@ -905,6 +1002,9 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_tiles, std::max<size_t>(1, tiles.size()) * sizeof(int4)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_wslot, wslot.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_fpre, fpre.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_fpre, fpre.data(), fpre.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_wslot, wslot.data(), wslot.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_pref, pref.data(), nk_dense * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));

@@ -73,6 +73,13 @@ struct PairPotDev {
   int col;        // parameter column (= result slot) of this potential
 };
 
+// Resident-block count of a kernel at a dynamic shared-memory size (cached).
+struct yg_occ {
+  const void *fn = nullptr;
+  size_t smem = 0;
+  int blocks = 0;  // resident blocks per SM x SMs
+};
+
 struct yg_ctx {
   int64_t natom = 0;
   int precision = YG_FP64;
@@ -173,8 +180,10 @@ struct yg_ctx {
   double *d_ew_gpart = nullptr;   // force partials
   double *d_ew_red = nullptr;     // energy/virial partials
   size_t ew_bytes_tab = 0, ew_bytes_Spart = 0, ew_bytes_W = 0, ew_bytes_gpart = 0;
-  int ew_nchunk = 0;              // atom chunks of the S pass
-  int ew_nsplit = 0;              // column splits of the force pass
+  int *d_ew_fpre = nullptr;       // prefix sums of the force column-tile costs (nftile + 1)
+  double *d_ew_fpiece = nullptr;  // force sums of the split atom tiles [tile][part][NA][3]
+  size_t ew_bytes_fpiece = 0;
+  yg_occ ew_occ_f;                // resident force-pass blocks
 
   // valence
   int64_t ndelta = 0, nic = 0, nterm = 0;

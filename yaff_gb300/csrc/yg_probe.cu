@@ -43,7 +43,33 @@ __global__ void __launch_bounds__(256) k_fma2_chain(float *out, int iters, float
   if (s == 12345.678f) out[threadIdx.x] = s;  // keeps the chains live
 }
 
-// kind: 0 scalar FP32, 1 FP64, 2 packed FP32 pairs.
+// CH chains of float pairs (packed FMAs) interleaved with CH scalar chains:
+// measures whether the two instruction forms share one pipe.
+template <int CH>
+__global__ void __launch_bounds__(256) k_fma_mix_chain(float *out, int iters, float a, float b) {
+  float2 x[CH];
+  float y[CH];
+#pragma unroll
+  for (int c = 0; c < CH; c++) {
+    x[c] = make_float2((float)(threadIdx.x + c), (float)(threadIdx.x - c));
+    y[c] = (float)(threadIdx.x * 3 + c);
+  }
+  const float2 a2 = make_float2(a, a), b2 = make_float2(b, b);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < CH; c++) {
+      x[c] = __ffma2_rn(x[c], a2, b2);
+      y[c] = fmaf(y[c], a, b);
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < CH; c++) s += x[c].x + x[c].y + y[c];
+  if (s == 12345.678f) out[threadIdx.x] = s;  // keeps the chains live
+}
+
+// kind: 0 scalar FP32, 1 FP64, 2 packed FP32 pairs, 3 packed and scalar
+// FP32 interleaved.
 double run_probe(int kind, cudaStream_t st) {
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
@@ -58,8 +84,10 @@ double run_probe(int kind, cudaStream_t st) {
       k_fma_chain<float, CH><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
     else if (kind == 1)
       k_fma_chain<double, CH><<<blocks, 256, 0, st>>>(out, iters, 0.999, 0.001);
-    else
+    else if (kind == 2)
       k_fma2_chain<CH><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
+    else
+      k_fma_mix_chain<CH / 2><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
   };
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -75,7 +103,7 @@ double run_probe(int kind, cudaStream_t st) {
   cudaEventDestroy(e1);
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return -1.0;
-  const double fma_per_step = (kind == 2 ? 2.0 : 1.0) * CH;
+  const double fma_per_step = (kind == 2 ? 2.0 * CH : (kind == 3 ? 1.5 * CH : 1.0 * CH));
   double flops = 5.0 * 2.0 * fma_per_step * (double)iters * blocks * 256.0;
   return flops / (ms * 1e-3) / 1e12;
 }
@@ -83,6 +111,6 @@ double run_probe(int kind, cudaStream_t st) {
 }  // namespace
 
 extern "C" double yg_probe_peak(int kind, void *stream) {
-  if (kind < 0 || kind > 2) return -1.0;
+  if (kind < 0 || kind > 3) return -1.0;
   return run_probe(kind, (cudaStream_t)stream);
 }
