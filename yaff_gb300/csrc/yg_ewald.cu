@@ -29,6 +29,8 @@
 #include <set>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "yg_internal.cuh"
 
 namespace {
@@ -340,16 +342,16 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
 
 // Sums the chunk partials in FP64 (fixed order) into the dense S[col][m].
 template <typename TA>
-__global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int nchunk, int nstile, int nslab,
-                              const int4 *__restrict__ cols, int nm, double *__restrict__ S) {
+__global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int nchunk, int nstile, int nslab, int sc,
+                              const int4 *__restrict__ cols, int nm, double unscale, double *__restrict__ S) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t per = (int64_t)nstile * nslab * EW_SC * EW_MS;
+  const int64_t per = (int64_t)nstile * nslab * sc * EW_MS;
   if (idx >= per) return;
   const int m = (int)(idx % EW_MS);
-  const int c = (int)((idx / EW_MS) % EW_SC);
-  const int slab = (int)((idx / (EW_MS * EW_SC)) % nslab);
-  const int tile = (int)(idx / ((int64_t)EW_MS * EW_SC * nslab));
-  const int4 col = cols[tile * EW_SC + c];
+  const int c = (int)((idx / EW_MS) % sc);
+  const int slab = (int)((idx / (EW_MS * sc)) % nslab);
+  const int tile = (int)(idx / ((int64_t)EW_MS * sc * nslab));
+  const int4 col = cols[tile * sc + c];
   const int mm = slab * EW_MS + m;
   if (col.z < 0 || mm > col.w) return;
   double re, im;
@@ -378,17 +380,28 @@ __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int 
     re = (double)rh + (double)rl;
     im = (double)ih + (double)il;
   }
-  S[2 * ((int64_t)col.z * nm + mm)] = re;
-  S[2 * ((int64_t)col.z * nm + mm) + 1] = im;
+  S[2 * ((int64_t)col.z * nm + mm)] = re * unscale;
+  S[2 * ((int64_t)col.z * nm + mm) + 1] = im * unscale;
 }
 
 // Energy and virial per k (FP64), plus the force-pass weights
 // conj(W_g) = conj(2 A S_eff,g) for the atom groups in use.
+// FP16 split of a weight pair into the force pass's B fragments (see the
+// tensor-core section below); words: Z hi b0, b1, lo b0, b1, then Z2.
+__device__ __forceinline__ void wb_put(unsigned *__restrict__ rec, int bsel, int off, float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 f = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - f.x, b - f.y);
+  rec[off + bsel] = *reinterpret_cast<const unsigned *>(&h);
+  rec[off + 2 + bsel] = *reinterpret_cast<const unsigned *>(&l);
+}
+
 template <typename T>
 __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_dense, const double *__restrict__ pref,
                                int G0, int G1, int nm, CellGeom cell, double fac2, int ngroup,
                                const int *__restrict__ wslot, int64_t wstride, typename C2<T>::t *__restrict__ W,
-                               double *__restrict__ partial) {
+                               unsigned *__restrict__ wbw, const int *__restrict__ woff, int64_t wbstride,
+                               double wsc1, double wsc2, double *__restrict__ partial) {
   __shared__ double red[256 / 32][7];
   int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double e = 0.0, v[6] = {0, 0, 0, 0, 0, 0};
@@ -435,7 +448,23 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
         if (g == 0) { wr += c1 + c2; wi += s1 + s2; }
         else if (g == 1) { wr += c2; wi += s2; }
         else { wr += c1; wi += s1; }
-        W[(int64_t)g * wstride + wpos] = cmk<T>((T)(2.0 * A * wr), (T)(-2.0 * A * wi));
+        const double ur = 2.0 * A * wr, ui = -2.0 * A * wi;  // U = conj(2 A S_eff)
+        if (W) W[(int64_t)g * wstride + wpos] = cmk<T>((T)ur, (T)ui);
+        const int ft = slot >> 2, ks = mm >> 3;
+        if (wbw && ks < woff[ft + 1] - woff[ft]) {  // m values past the tile's extent have no unit
+          // B[(m, re)][(c, re)] = Ur, B[(m, im)][(c, re)] = -Ui, B[(m, re)][(c, im)] = Ui,
+          // B[(m, im)][(c, im)] = Ur; lane 4 (2 cq + q) + (m & 3), b0 for m & 7 < 4
+          const int cq = slot & 3, ml = mm & 7;
+          const int bsel = ml >> 2;
+          unsigned *unit = wbw + (int64_t)g * wbstride + (int64_t)(woff[ft] + ks) * 256;
+          unsigned *rq0 = unit + (4 * (2 * cq) + (ml & 3)) * 8;
+          unsigned *rq1 = unit + (4 * (2 * cq + 1) + (ml & 3)) * 8;
+          const double a1 = wsc1, a2 = wsc2 * mm;  // weight scales of Z and Z2
+          wb_put(rq0, bsel, 0, (float)(a1 * ur), (float)(-a1 * ui));
+          wb_put(rq1, bsel, 0, (float)(a1 * ui), (float)(a1 * ur));
+          wb_put(rq0, bsel, 4, (float)(a2 * ur), (float)(-a2 * ui));
+          wb_put(rq1, bsel, 4, (float)(a2 * ui), (float)(a2 * ur));
+        }
       }
     }
   }
@@ -775,6 +804,421 @@ static int smem_optin(const void *kernel, size_t need) {
   return YG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core form of the mixed-precision reciprocal sum (G2 + 1 <= 32).
+//
+// Both passes are complex matrix products (S = X^T Y over atoms, Z = Y U
+// over m), run here as warp-level FP16 MMAs (m16n8k16, FP32 accumulation).
+// Every operand is split into FP16 hi + lo parts and a product is formed as
+// hi*hi + hi*lo + lo*hi, which keeps about 22 significant bits; each
+// 16-atom step of the S pass starts from a zero accumulator and is added to
+// the running FP32 sums with round-to-nearest, so no error builds up inside
+// the MMA accumulators.  Operands are scaled by powers of two into FP16
+// range (charges by qscale, weights by s1 and, for the m-weighted product,
+// s2) and unscaled exactly afterwards.
+//
+// Fragment layouts (m16n8k16; lane = 4 g + t):
+//   A (16 x 16): a0 = A[g][2t..2t+1], a1 = A[g+8][2t..], a2 = A[g][2t+8..],
+//                a3 = A[g+8][2t+8..];   B (16 x 8): b0 = B[2t..2t+1][g],
+//                b1 = B[2t+8..2t+9][g];  D: d0,d1 = D[g][2t..], d2,d3 = D[g+8][2t..]
+// with the lower column (row for B) in the low half of each register.
+
+#define EW_MMA_KS 32   // atoms per S-pass stage (two 16-atom steps)
+#define EW_MMA_ATB 512 // atoms per S-pass block
+#define EW_MMA_FT 8    // 4-column tiles per force-pass stage
+
+__device__ __forceinline__ unsigned h2_bits(__half2 h) { return *reinterpret_cast<unsigned *>(&h); }
+
+// (a, b) -> FP16 pairs hi = rn(a, b), lo = rn(a - hi, b - hi).
+__device__ __forceinline__ void split_h2(float a, float b, unsigned &hi, unsigned &lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 f = __half22float2(h);
+  hi = h2_bits(h);
+  lo = h2_bits(__floats2half2_rn(a - f.x, b - f.y));
+}
+
+__device__ __forceinline__ void mma_f16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// d = ah*bh + ah*bl + al*bh (d starts at zero).
+__device__ __forceinline__ void mma_split(float (&d)[4], const unsigned (&ah)[4], const unsigned (&al)[4],
+                                          unsigned bh0, unsigned bh1, unsigned bl0, unsigned bl1) {
+  d[0] = d[1] = d[2] = d[3] = 0.f;
+  mma_f16(d, ah, bh0, bh1);
+  mma_f16(d, ah, bl0, bl1);
+  mma_f16(d, al, bh0, bh1);
+}
+
+// MMA tables, one thread per (atom, axis) over the padded atom count:
+//   te[a][0..G0] = E0, te[a][G0+1..G0+G1+1] = E1 (float2, row stride lep);
+//   yf[a][m] = (hi, lo) FP16 pairs of qscale q E2[m] (re in the low half),
+//              m < nmf (zero beyond G2);
+//   ys: per 16 atoms, per m < nms and component q (re, im), per t < 4 a
+//       16-byte unit (hi(2t,2t+1), hi(2t+8,2t+9), lo(2t,2t+1), lo(2t+8,2t+9))
+//       -- the S pass's B fragments, stored as 16-bit halves.
+// The ys position of an atom is relative to its atom group ([lo, hi) first,
+// then [0, lo), then [hi, N), each padded to a multiple of 16 atoms: bases
+// 0, base1, base2), so a group's 16-atom blocks hold only its own atoms;
+// padding entries stay zero (the buffer is cleared before).  The phases
+// follow k_tables' FP32 form.
+__global__ void k_tables_mma(const double *__restrict__ pos, const double *__restrict__ charge, int64_t natom,
+                             int64_t lo, int64_t hi, int64_t base1, int64_t base2, CellGeom cell, int G0, int G1,
+                             int G2, float qscale, int lep, int nmf, int nms, float2 *__restrict__ te,
+                             uint2 *__restrict__ yf, unsigned short *__restrict__ ys) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= natom * 3) return;
+  const int64_t a = idx / 3;
+  const int axis = (int)(idx - a * 3);
+  float s_hi, s_lo;
+  {
+    const double *gv = cell.gv + 3 * axis;
+    double s = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
+    s -= floor(s);
+    s_hi = (float)s;
+    s_lo = (float)(s - (double)s_hi);
+  }
+  auto phase = [&](int g, float &c, float &sn) {
+    const float fg = (float)g;
+    const float p = fg * s_hi;
+    const float e = fmaf(fg, s_hi, -p);
+    const float x = (p - rintf(p)) + fmaf(fg, s_lo, e);
+    sincospif(2.0f * x, &sn, &c);
+  };
+  if (axis < 2) {
+    const int gmax = axis == 0 ? G0 : G1;
+    float2 *out = te + a * lep + (axis == 0 ? 0 : G0 + 1);
+    for (int g = 0; g <= gmax; g++) {
+      float c, sn;
+      phase(g, c, sn);
+      out[g] = make_float2(c, sn);
+    }
+    return;
+  }
+  const float q = (float)(charge[a] * (double)qscale);
+  const int64_t p = (a >= lo && a < hi) ? a - lo : (a < lo ? base1 + a : base2 + (a - hi));
+  const int64_t blk = p >> 4;
+  const int i = (int)(p & 15);
+  const int t = (i & 7) >> 1, half = i & 1, whi = i < 8 ? 0 : 1;
+  for (int m = 0; m < nmf; m++) {
+    float yr = 0.f, yi = 0.f;
+    if (m <= G2) {
+      float c, sn;
+      phase(m, c, sn);
+      yr = q * c;
+      yi = q * sn;
+    }
+    unsigned hi, lo;
+    split_h2(yr, yi, hi, lo);
+    yf[a * nmf + m] = make_uint2(hi, lo);
+    if (m < nms) {
+      // component q = 0 (re): low halves; q = 1 (im): high halves
+      for (int comp = 0; comp < 2; comp++) {
+        const int64_t unit = ((blk * nms + m) * 2 + comp) * 4 + t;
+        const unsigned short h16 = (unsigned short)(comp == 0 ? (hi & 0xffffu) : (hi >> 16));
+        const unsigned short l16 = (unsigned short)(comp == 0 ? (lo & 0xffffu) : (lo >> 16));
+        ys[(unit * 4 + whi) * 2 + half] = h16;
+        ys[(unit * 4 + 2 + whi) * 2 + half] = l16;
+      }
+    }
+  }
+}
+
+// S pass on the tensor cores.  grid = (atom chunks of EW_MMA_ATB, 64-column
+// tiles, m slabs); 4 warps, warp w owns columns 16 w .. 16 w + 15 of the
+// tile as two 8-column MMA row tiles (rows 0-7: Re X, rows 8-15: Im X) and
+// NT n-tiles of 4 m values (columns 0-3: Re Y, 4-7: Im Y) of the slab.  The
+// E0|E1 rows and the Y fragments of 32 atoms at a time arrive by
+// double-buffered bulk copies (te holds 32 rows past the last atom, ys two
+// blocks past the last group).  Partial layout as k_sfac with 64 columns:
+// [chunk][tile][slab][c][m].
+template <int NT>
+__device__ __forceinline__ void sfac_mma_stage(const float2 *__restrict__ sTE, const uint4 *__restrict__ sYS, int lep,
+                                               int nms, int mb, int nrow, const int (&o0)[2], const int (&o1)[2],
+                                               const float (&sg0)[2], const float (&sg1)[2], const float (&ok)[2],
+                                               int g, int t, float (&acc)[2][8][4]) {
+#pragma unroll 1
+  for (int kk = 0; kk < 2; kk++) {
+    if (kk * 16 >= nrow) break;
+    unsigned ah[2][4], al[2][4];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      float xr[4], xi[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int la = kk * 16 + 2 * t + (u & 1) + (u >> 1) * 8;  // atoms 2t, 2t+1, 2t+8, 2t+9
+        const float2 *row = sTE + (size_t)la * lep;
+        float2 e0 = row[o0[j]], e1 = row[o1[j]];
+        e0.x *= ok[j];
+        e0.y *= sg0[j] * ok[j];
+        e1.y *= sg1[j];
+        xr[u] = e0.x * e1.x - e0.y * e1.y;
+        xi[u] = e0.x * e1.y + e0.y * e1.x;
+      }
+      split_h2(xr[0], xr[1], ah[j][0], al[j][0]);
+      split_h2(xi[0], xi[1], ah[j][1], al[j][1]);
+      split_h2(xr[2], xr[3], ah[j][2], al[j][2]);
+      split_h2(xi[2], xi[3], ah[j][3], al[j][3]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++) {
+      const uint4 b = sYS[(((size_t)kk * nms + mb + nt * 4 + (g & 3)) * 2 + (g >> 2)) * 4 + t];
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        float d[4];
+        mma_split(d, ah[j], al[j], b.x, b.y, b.z, b.w);
+#pragma unroll
+        for (int e = 0; e < 4; e++) acc[j][nt][e] += d[e];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te, const uint4 *__restrict__ ys,
+                                                  int n, int G0, int lep, int nms,
+                                                  const int4 *__restrict__ cols, float2 *__restrict__ Spart,
+                                                  int ntile64, int nslab, int *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_mma[];
+  __shared__ unsigned long long bars[2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int tile = blockIdx.y, slab = blockIdx.z;
+  const int mb = slab * EW_MS;
+  const size_t te_bytes = (size_t)EW_MMA_KS * lep * sizeof(float2);
+  const size_t ys_bytes = (size_t)(EW_MMA_KS / 16) * nms * 2 * 4 * sizeof(uint4);
+  const size_t stage = te_bytes + ys_bytes;
+  const int wc0 = tile * 64 + w * 16;  // the warp's first column (largest extent)
+  const int Mw = cols[wc0].w + 1 - mb;
+  const int nt = Mw > 0 ? min(8, (Mw + 3) / 4) : 0;
+  int o0[2], o1[2];
+  float sg0[2], sg1[2], ok[2];
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const int4 col = cols[wc0 + 8 * j + g];
+    o0[j] = col.x < 0 ? -col.x : col.x;
+    o1[j] = G0 + 1 + (col.y < 0 ? -col.y : col.y);
+    sg0[j] = col.x < 0 ? -1.f : 1.f;
+    sg1[j] = col.y < 0 ? -1.f : 1.f;
+    ok[j] = col.z >= 0 ? 1.f : 0.f;
+  }
+  float acc[2][8][4];
+#pragma unroll
+  for (int j = 0; j < 2; j++)
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[j][n][e] = 0.f;
+  // te, ys start at the group's first atom and first 16-atom block
+  const int abeg = blockIdx.x * EW_MMA_ATB;
+  const int aend = min(n, abeg + EW_MMA_ATB);
+  const int tmax = cols[tile * 64].w + 1 - mb;    // the block's largest extent
+  if (tmax > 0 && aend > abeg) {
+    const int nstage = (aend - abeg + EW_MMA_KS - 1) / EW_MMA_KS;
+    if (threadIdx.x == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+    // stage s: the 32 padded rows from abeg + 32 s (te, ys of two 16-atom blocks)
+    auto issue = [&](int s) {
+      const int ab = abeg + s * EW_MMA_KS;
+      unsigned char *dst = smem_mma + (size_t)(s & 1) * stage;
+      unsigned long long *bar = &bars[s & 1];
+      bulk_expect(bar, (unsigned)stage);
+      bulk_copy(dst, te + (size_t)ab * lep, (unsigned)te_bytes, bar);
+      bulk_copy(dst + te_bytes, ys + (size_t)(ab / 16) * nms * 2 * 4, (unsigned)ys_bytes, bar);
+    };
+    if (threadIdx.x == 0) issue(0);
+    for (int s = 0; s < nstage; s++) {
+      if (threadIdx.x == 0 && s + 1 < nstage) issue(s + 1);
+      const bool arrived = mbar_wait(&bars[s & 1], (unsigned)((s >> 1) & 1), status);
+      if (__syncthreads_or(!arrived)) {
+        if (threadIdx.x == 0 && s + 1 < nstage) mbar_wait(&bars[(s + 1) & 1], (unsigned)(((s + 1) >> 1) & 1), status);
+        break;
+      }
+      const unsigned char *buf = smem_mma + (size_t)(s & 1) * stage;
+      const float2 *sTE = reinterpret_cast<const float2 *>(buf);
+      const uint4 *sYS = reinterpret_cast<const uint4 *>(buf + te_bytes);
+      const int nrow = min(EW_MMA_KS, aend - (abeg + s * EW_MMA_KS));
+      switch (nt) {
+        case 8: sfac_mma_stage<8>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 7: sfac_mma_stage<7>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 6: sfac_mma_stage<6>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 5: sfac_mma_stage<5>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 4: sfac_mma_stage<4>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 3: sfac_mma_stage<3>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 2: sfac_mma_stage<2>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        case 1: sfac_mma_stage<1>(sTE, sYS, lep, nms, mb, nrow, o0, o1, sg0, sg1, ok, g, t, acc); break;
+        default: break;
+      }
+      __syncthreads();  // the buffer is refilled two stages later
+    }
+  }
+  // S = (Re X Re Y - Im X Im Y) + i (Re X Im Y + Im X Re Y): lanes t and t^2
+  // hold the Re Y and Im Y columns of the same two m values
+  const int64_t base = (((int64_t)blockIdx.x * ntile64 + tile) * nslab + slab) * (64 * EW_MS);
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const int c = w * 16 + 8 * j + g;
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      const float p2 = __shfl_xor_sync(0xffffffffu, acc[j][n][2], 2);
+      const float p3 = __shfl_xor_sync(0xffffffffu, acc[j][n][3], 2);
+      if (n >= nt) continue;
+      const int m = n * 4 + 2 * (t & 1);
+      float *dst = reinterpret_cast<float *>(Spart + base + (int64_t)c * EW_MS + m);
+      if (t < 2) {
+        dst[0] = acc[j][n][0] - p2;  // Re S(m), Re S(m + 1)
+        dst[2] = acc[j][n][1] - p3;
+      } else {
+        dst[1] = acc[j][n][0] + p2;  // Im S(m), Im S(m + 1)
+        dst[3] = acc[j][n][1] + p3;
+      }
+    }
+  }
+}
+
+// Force pass on the tensor cores.  One warp per 16 atoms, 8 warps per
+// block; every warp sweeps all 4-column tiles.  Z = sum_m Y U and
+// Z2 = sum_m m Y U (U = the stored conj weights) come from MMAs with
+// M = 16 atoms, N = 4 columns x (re, im), K = 8 m x (re, im) per step; the Y
+// fragments of the warp's atoms stay in registers, the weight fragments of
+// EW_MMA_FT tiles at a time arrive by double-buffered bulk copies.  The
+// epilogue forms P = E0 E1 per (atom, column) from the E0|E1 table (through
+// L1) and accumulates g0 Im(P Z), g1 Im(P Z), Im(P Z2).
+__global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restrict__ te, const uint2 *__restrict__ yf,
+                                                         int a0, int a1, int G0, int lep, int nmf, int nks,
+                                                         const int4 *__restrict__ cols, int nft4,
+                                                         const int *__restrict__ woff, const uint4 *__restrict__ wb,
+                                                         double inv1, double inv2, double *__restrict__ gfrac,
+                                                         int *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_mma[];
+  __shared__ unsigned long long bars[2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int wbase = a0 + (blockIdx.x * 8 + w) * 16;  // a0: a multiple of 16
+  const int stage_units = EW_MMA_FT * nks;           // 1 KB units per stage (max)
+  const size_t stage = (size_t)stage_units * 1024 + EW_MMA_FT * 4 * sizeof(int4);
+  // Y fragments of the warp's atoms (rows beyond the group read padding or
+  // other groups' atoms; their sums are never stored)
+  unsigned yh[4][4], yl[4][4];
+  const int ra = min(wbase + g, a1 - 1), rb = min(wbase + g + 8, a1 - 1);
+  const bool va = wbase + g < a1, vb = wbase + g + 8 < a1;
+#pragma unroll
+  for (int ks = 0; ks < 4; ks++) {
+    if (ks < nks) {
+      const int m0 = ks * 8 + t, m1 = m0 + 4;
+      uint2 v;
+      v = yf[(size_t)ra * nmf + m0]; yh[ks][0] = va ? v.x : 0u; yl[ks][0] = va ? v.y : 0u;
+      v = yf[(size_t)rb * nmf + m0]; yh[ks][1] = vb ? v.x : 0u; yl[ks][1] = vb ? v.y : 0u;
+      v = yf[(size_t)ra * nmf + m1]; yh[ks][2] = va ? v.x : 0u; yl[ks][2] = va ? v.y : 0u;
+      v = yf[(size_t)rb * nmf + m1]; yh[ks][3] = vb ? v.x : 0u; yl[ks][3] = vb ? v.y : 0u;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; e++) yh[ks][e] = yl[ks][e] = 0u;
+    }
+  }
+  const float2 *rowa = te + (size_t)ra * lep, *rowb = te + (size_t)rb * lep;
+  CompAcc<float> acc[2][3];
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int q = 0; q < 3; q++) acc[r][q].init();
+  const int nstage = (nft4 + EW_MMA_FT - 1) / EW_MMA_FT;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int s) {
+    const int t0 = s * EW_MMA_FT, t1 = min(nft4, t0 + EW_MMA_FT);
+    unsigned char *dst = smem_mma + (size_t)(s & 1) * stage;
+    const unsigned wbytes = (unsigned)(woff[t1] - woff[t0]) * 1024u;
+    const unsigned cbytes = (unsigned)((t1 - t0) * 4 * sizeof(int4));
+    unsigned long long *bar = &bars[s & 1];
+    bulk_expect(bar, wbytes + cbytes);
+    bulk_copy(dst, wb + (size_t)woff[t0] * 64, wbytes, bar);
+    bulk_copy(dst + (size_t)stage_units * 1024, cols + t0 * 4, cbytes, bar);
+  };
+  if (threadIdx.x == 0 && nstage > 0) issue(0);
+  for (int s = 0; s < nstage; s++) {
+    if (threadIdx.x == 0 && s + 1 < nstage) issue(s + 1);
+    const bool arrived = mbar_wait(&bars[s & 1], (unsigned)((s >> 1) & 1), status);
+    if (__syncthreads_or(!arrived)) {
+      if (threadIdx.x == 0 && s + 1 < nstage) mbar_wait(&bars[(s + 1) & 1], (unsigned)(((s + 1) >> 1) & 1), status);
+      break;
+    }
+    const unsigned char *buf = smem_mma + (size_t)(s & 1) * stage;
+    const int4 *scol = reinterpret_cast<const int4 *>(buf + (size_t)stage_units * 1024);
+    const int t0 = s * EW_MMA_FT, t1 = min(nft4, t0 + EW_MMA_FT);
+    const int u0 = woff[t0];
+    float ps[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    for (int ft = t0; ft < t1; ft++) {
+      const int ku = woff[ft] - u0, kn = woff[ft + 1] - woff[ft];  // this tile's k-steps
+      const uint4 *fr = reinterpret_cast<const uint4 *>(buf) + (size_t)ku * 64 + lane * 2;
+      float z[4] = {0.f, 0.f, 0.f, 0.f}, z2[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int ks = 0; ks < 4; ks++) {
+        if (ks < kn) {
+          const uint4 b1 = fr[ks * 64], b2 = fr[ks * 64 + 1];
+          mma_f16(z, yh[ks], b1.x, b1.y);
+          mma_f16(z, yh[ks], b1.z, b1.w);
+          mma_f16(z, yl[ks], b1.x, b1.y);
+          mma_f16(z2, yh[ks], b2.x, b2.y);
+          mma_f16(z2, yh[ks], b2.z, b2.w);
+          mma_f16(z2, yl[ks], b2.x, b2.y);
+        }
+      }
+      // z[0], z[1]: Z of (atom g, column t); z[2], z[3]: atom g + 8
+      const int4 col = scol[(ft - t0) * 4 + t];
+      if (col.z >= 0) {
+        const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = G0 + 1 + (col.y < 0 ? -col.y : col.y);
+        const float sx = col.x < 0 ? -1.f : 1.f, sy = col.y < 0 ? -1.f : 1.f;
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+          const float2 *row = r ? rowb : rowa;
+          const float2 e0 = __ldg(row + ag0), e1 = __ldg(row + ag1);
+          const float e0y = sx * e0.y, e1y = sy * e1.y;
+          const float pr = e0.x * e1.x - e0y * e1y;
+          const float pi = e0.x * e1y + e0y * e1.x;
+          const float im1 = pr * z[2 * r + 1] + pi * z[2 * r];
+          const float im2 = pr * z2[2 * r + 1] + pi * z2[2 * r];
+          ps[r][0] += (float)col.x * im1;
+          ps[r][1] += (float)col.y * im1;
+          ps[r][2] += im2;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) acc[r][q].add(ps[r][q]);
+    __syncthreads();  // the buffer is refilled two stages later
+  }
+  // sum the four column lanes of every atom (fixed order), unscale, store
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    double v[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      v[q] = acc[r][q].value();
+      v[q] += __shfl_xor_sync(0xffffffffu, v[q], 1);
+      v[q] += __shfl_xor_sync(0xffffffffu, v[q], 2);
+    }
+    const int a = wbase + g + 8 * r;
+    if (t == 0 && a < a1) {
+      gfrac[(int64_t)a * 3] = v[0] * inv1;
+      gfrac[(int64_t)a * 3 + 1] = v[1] * inv1;
+      gfrac[(int64_t)a * 3 + 2] = v[2] * inv2;
+    }
+  }
+}
+
 // Blocks of a kernel the device holds at once (all SMs), cached per
 // (kernel, dynamic shared memory).
 static int resident_blocks(const void *fn, int threads, size_t smem, yg_occ *oc, int *blocks) {
@@ -855,7 +1299,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
                                                  ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
     k_sfac_reduce<TA><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
-        (const CA *)ctx->d_ew_Spart, nch, nstile, nslab, (const int4 *)ctx->d_ew_tiles, nm, S);
+        (const CA *)ctx->d_ew_Spart, nch, nstile, nslab, EW_SC, (const int4 *)ctx->d_ew_tiles, nm, 1.0, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
   // energy, virial, weights
@@ -869,7 +1313,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
                                                 fac2, ngroup, ctx->d_ew_wslot, wstride, (CT *)ctx->d_ew_W,
-                                                partial);
+                                                nullptr, nullptr, 0, 0.0, 0.0, partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -923,6 +1367,115 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   return YG_OK;
 }
 
+
+// Smallest power of two >= x (x > 0), as a double.
+static double pow2_ceil(double x) { return std::ldexp(1.0, (int)std::ceil(std::log2(x))); }
+
+// The mixed-precision reciprocal sum on the tensor cores (G2 + 1 <= 32).
+int run_reci_mma(yg_ctx *ctx, int want_grad) {
+  const int G0 = (int)ctx->ew_gmax[0], G1 = (int)ctx->ew_gmax[1], G2 = (int)ctx->ew_gmax[2];
+  const int nm = G2 + 1;
+  const int64_t N = ctx->natom;
+  const int ntile64 = 2 * ctx->ew_ntile;
+  const int64_t nk_dense = (int64_t)ctx->ew_ncol * nm;
+  const int lep = (G0 + G1 + 2 + 1) & ~1;  // E0|E1 row, even: 16-byte rows
+  const int nks = (nm + 7) / 8, nmf = 8 * nks, nms = (nm + 3) & ~3;
+  int rc;
+  // atom groups: 0 = [nlow, nhigh) (always), 1 = [0, nlow), 2 = [nhigh, N)
+  const int64_t lo = ctx->ew_nlow, hi = ctx->ew_nhigh;
+  const int64_t gb[3][2] = {{lo, hi}, {0, lo}, {hi, N}};
+  const int nS = (lo > 0 || hi < N) ? 3 : 1;
+  auto r16 = [](int64_t n) { return (n + 15) / 16 * 16; };
+  const int64_t gbase[3] = {0, r16(hi - lo), r16(hi - lo) + r16(lo)};
+  const int64_t ys_blocks = (r16(hi - lo) + r16(lo) + r16(N - hi)) / 16 + 2;
+  // operand scales (powers of two): |qscale q| <= 1; |s1 U| <= 2^13 and
+  // |s2 m U| <= 2^13 with |U| <= 2 max A sum |q|
+  const double qmax = ctx->h_qmax, qsum = ctx->h_qsum;
+  const double qscale = qmax > 0.0 ? 1.0 / pow2_ceil(qmax) : 1.0;
+  const double ub = 2.0 * ctx->ew_amax * qsum;
+  const double s1 = ub > 0.0 ? 8192.0 / pow2_ceil(ub) : 1.0;
+  const double s2 = s1 / pow2_ceil(std::max(1, G2));
+  // tables
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_te, &ctx->ew_bytes_te, (size_t)(N + EW_MMA_KS) * lep * sizeof(float2)))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_yf, &ctx->ew_bytes_yf, (size_t)N * nmf * sizeof(uint2)))) return rc;
+  const size_t ys_bytes = (size_t)ys_blocks * nms * 8 * sizeof(uint4);
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_ys, &ctx->ew_bytes_ys, ys_bytes))) return rc;
+  float2 *te = (float2 *)ctx->d_ew_te;
+  YG_CUDA(cudaMemsetAsync(te + (size_t)N * lep, 0, (size_t)EW_MMA_KS * lep * sizeof(float2), ctx->stream));
+  YG_CUDA(cudaMemsetAsync(ctx->d_ew_ys, 0, ys_bytes, ctx->stream));
+  k_tables_mma<<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(
+      ctx->d_pos, ctx->d_charge, N, lo, hi, gbase[1], gbase[2], ctx->cell, G0, G1, G2, (float)qscale, lep, nmf, nms,
+      te, (uint2 *)ctx->d_ew_yf, (unsigned short *)ctx->d_ew_ys);
+  YG_LAUNCH_CHECK(ctx, "k_tables_mma");
+  // structure factors
+  int maxchunk = 1;
+  for (int g = 0; g < nS; g++)
+    maxchunk = std::max(maxchunk, (int)((gb[g][1] - gb[g][0] + EW_MMA_ATB - 1) / EW_MMA_ATB));
+  const size_t per = (size_t)ntile64 * 64 * EW_MS;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(float2)))) return rc;
+  const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
+  if ((rc = smem_optin((const void *)k_sfac_mma, ssm))) return rc;
+  for (int g = 0; g < nS; g++) {
+    const int64_t n = gb[g][1] - gb[g][0];
+    double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
+    YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
+    if (n <= 0) continue;
+    const int nch = (int)((n + EW_MMA_ATB - 1) / EW_MMA_ATB);
+    dim3 grid(nch, ntile64, 1);
+    k_sfac_mma<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
+                                               (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8,
+                                               (int)n, G0, lep, nms, (const int4 *)ctx->d_ew_tiles,
+                                               (float2 *)ctx->d_ew_Spart, ntile64, 1, ctx->d_status);
+    YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
+    k_sfac_reduce<float><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
+        (const float2 *)ctx->d_ew_Spart, nch, ntile64, 1, 64, (const int4 *)ctx->d_ew_tiles, nm, 1.0 / qscale, S);
+    YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
+  }
+  // energy, virial, weight fragments
+  const int ngroup = (nS == 3) ? 3 : 1;
+  const int64_t wbstride = (int64_t)ctx->ew_wbunits * 256;  // 32-bit words per group
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_wb, &ctx->ew_bytes_wb, (size_t)ngroup * wbstride * 4))) return rc;
+  YG_CUDA(cudaMemsetAsync(ctx->d_ew_wb, 0, (size_t)ngroup * wbstride * 4, ctx->stream));
+  const int eb = yg_blocks(nk_dense, 256);
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
+  double *partial = ctx->d_red + 64;
+  const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
+  k_ewald_energy<float><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
+                                                    fac2, ngroup, ctx->d_ew_wslot, 0, nullptr,
+                                                    (unsigned *)ctx->d_ew_wb, ctx->d_ew_woff, wbstride, s1, s2,
+                                                    partial);
+  YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
+  double *sums = partial + (size_t)eb * 7;
+  if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
+  double *ev = ctx->d_part_ev + 10 * YG_PART_EWALD_RECI;
+  k_store_ewald_ev<<<1, 32, 0, ctx->stream>>>(sums, 1.0 / ctx->ew_diel, ev);
+  YG_LAUNCH_CHECK(ctx, "k_store_ewald_ev");
+  double *gpos = ctx->d_part_gpos + (size_t)YG_PART_EWALD_RECI * N * 3;
+  if (!want_grad) {
+    YG_CUDA(cudaMemsetAsync(gpos, 0, N * 3 * sizeof(double), ctx->stream));
+    ctx->part_valid[YG_PART_EWALD_RECI] = 1;
+    return YG_OK;
+  }
+  // force pass, per atom group
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
+  const size_t fsm = 2 * ((size_t)EW_MMA_FT * nks * 1024 + EW_MMA_FT * 4 * sizeof(int4));
+  if ((rc = smem_optin((const void *)k_ewald_force_mma, fsm))) return rc;
+  for (int g = 0; g < nS; g++) {
+    const int64_t n = gb[g][1] - gb[g][0];
+    if (n <= 0) continue;
+    const uint4 *wbg = (const uint4 *)ctx->d_ew_wb + (size_t)(ngroup == 1 ? 0 : g) * (wbstride / 4);
+    k_ewald_force_mma<<<(int)((n + 127) / 128), 256, fsm, ctx->stream>>>(
+        te, (const uint2 *)ctx->d_ew_yf, (int)gb[g][0], (int)gb[g][1], G0, lep, nmf, nks,
+        (const int4 *)ctx->d_ew_tiles, ctx->ew_nft4, ctx->d_ew_woff, wbg, 1.0 / (qscale * s1), 1.0 / (qscale * s2),
+        ctx->d_ew_gpart, ctx->d_status);
+    YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma");
+  }
+  k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
+                                                           -6.2831853071795864769 / ctx->ew_diel, gpos);
+  YG_LAUNCH_CHECK(ctx, "k_ewald_gpos");
+  ctx->part_valid[YG_PART_EWALD_RECI] = 1;
+  return YG_OK;
+}
 }  // namespace
 
 // Host-side k-space layout: prefactor grid in the reference's formula and
@@ -944,6 +1497,7 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   double gc2 = ctx->ew_gcut * tp;
   gc2 *= gc2;
   int nk = 0;
+  double amax = 0.0;
   std::vector<int> colmhi(nc0 * nc1, -1);
   for (int g0 = -G0; g0 <= G0; g0++)
     for (int g1 = -G1; g1 <= G1; g1++)
@@ -960,6 +1514,7 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
         if (ksq > gc2) continue;
         int64_t col = (int64_t)(g0 + G0) * nc1 + (g1 + G1);
         pref[col * nm + g2] = fac1 * std::exp(-ksq * fac2) / ksq;
+        amax = std::max(amax, pref[col * nm + g2]);
         if (g2 > colmhi[col]) colmhi[col] = g2;
         nk++;
       }
@@ -990,6 +1545,16 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   for (int t = 0; t < nft; t++) fpre.push_back(fpre.back() + tiles[(size_t)t * EW_FC].w + 1 + EW_FEPI);
   yg_free(ctx, (void **)&ctx->d_ew_fpre);
   ctx->d_ew_fpre = nullptr;
+  // tensor-core layout: 4-column tiles with work and their fragment units
+  // (one 1 KB unit per 8 m values of the tile's extent)
+  ctx->ew_amax = amax;
+  ctx->ew_mma = (nm <= 32) ? 1 : 0;
+  std::vector<int> woff(1, 0);
+  for (size_t t = 0; t * 4 < tiles.size() && tiles[t * 4].w >= 0; t++) woff.push_back(woff.back() + (tiles[t * 4].w + 8) / 8);
+  ctx->ew_nft4 = (int)woff.size() - 1;
+  ctx->ew_wbunits = woff.back();
+  yg_free(ctx, (void **)&ctx->d_ew_woff);
+  ctx->d_ew_woff = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_wslot);
   yg_free(ctx, (void **)&ctx->d_ew_pref);
   yg_free(ctx, (void **)&ctx->d_ew_tiles);
@@ -1003,6 +1568,9 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_wslot, wslot.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_fpre, fpre.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_woff, woff.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_woff, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_fpre, fpre.data(), fpre.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_wslot, wslot.data(), wslot.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -1026,6 +1594,7 @@ int yg_launch_ewald_reci(yg_ctx *ctx, int want_grad) {
     return YG_OK;
   }
   if (ctx->precision == YG_FP64) return run_reci<double, double, 2>(ctx, want_grad);
+  if (ctx->ew_mma) return run_reci_mma(ctx, want_grad);
   return run_reci<float, float, 2>(ctx, want_grad);
 }
 

@@ -101,6 +101,7 @@ struct yg_ctx {
   double *d_pos_build = nullptr;  // natom*3 at the last rebuild
   double *d_charge = nullptr;     // natom
   std::vector<double> h_charge;   // host copy (Ewald self term)
+  double h_qmax = 0.0, h_qsum = 0.0;  // max |q| and sum |q| of h_charge
   int have_charges = 0;
 
   // binning (orig order)
@@ -180,6 +181,17 @@ struct yg_ctx {
   double *d_ew_gpart = nullptr;   // force partials
   double *d_ew_red = nullptr;     // energy/virial partials
   size_t ew_bytes_tab = 0, ew_bytes_Spart = 0, ew_bytes_W = 0, ew_bytes_gpart = 0;
+  // tensor-core (warp MMA) form of the mixed-precision reciprocal sum
+  int ew_mma = 0;                 // 1 when the k-space layout suits it (G2 + 1 <= 32)
+  double ew_amax = 0.0;           // largest prefactor A(k)
+  int ew_nft4 = 0;                // 4-column force tiles with work
+  int ew_wbunits = 0;             // 1 KB fragment units of one group's weights
+  int *d_ew_woff = nullptr;       // first fragment unit of every 4-column tile (nft4 + 1)
+  void *d_ew_te = nullptr;        // E0|E1 rows (float2), atoms padded to a multiple of 32
+  void *d_ew_yf = nullptr;        // q E2 as FP16 (hi, lo) pairs per (atom, m)
+  void *d_ew_ys = nullptr;        // q E2 as FP16 B fragments per 16 atoms
+  void *d_ew_wb = nullptr;        // force weights as FP16 B fragments, per group
+  size_t ew_bytes_te = 0, ew_bytes_yf = 0, ew_bytes_ys = 0, ew_bytes_wb = 0;
   int *d_ew_fpre = nullptr;       // prefix sums of the force column-tile costs (nftile + 1)
   double *d_ew_fpiece = nullptr;  // force sums of the split atom tiles [tile][part][NA][3]
   size_t ew_bytes_fpiece = 0;
