@@ -387,7 +387,7 @@ __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int 
 // Energy and virial per k (FP64), plus the force-pass weights
 // conj(W_g) = conj(2 A S_eff,g) for the atom groups in use.
 // FP16 split of a weight pair into the force pass's B fragments (see the
-// tensor-core section below); words: Z hi b0, b1, lo b0, b1, then Z2.
+// tensor-core section below); record words: hi b0, hi b1, lo b0, lo b1.
 __device__ __forceinline__ void wb_put(unsigned *__restrict__ rec, int bsel, int off, float a, float b) {
   const __half2 h = __floats2half2_rn(a, b);
   const float2 f = __half22float2(h);
@@ -456,14 +456,15 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
           // B[(m, im)][(c, im)] = Ur; lane 4 (2 cq + q) + (m & 3), b0 for m & 7 < 4
           const int cq = slot & 3, ml = mm & 7;
           const int bsel = ml >> 2;
+          // unit: the 32 lanes' Z records (4 words each), then their Z2 records
           unsigned *unit = wbw + (int64_t)g * wbstride + (int64_t)(woff[ft] + ks) * 256;
-          unsigned *rq0 = unit + (4 * (2 * cq) + (ml & 3)) * 8;
-          unsigned *rq1 = unit + (4 * (2 * cq + 1) + (ml & 3)) * 8;
+          unsigned *rq0 = unit + (4 * (2 * cq) + (ml & 3)) * 4;
+          unsigned *rq1 = unit + (4 * (2 * cq + 1) + (ml & 3)) * 4;
           const double a1 = wsc1, a2 = wsc2 * mm;  // weight scales of Z and Z2
           wb_put(rq0, bsel, 0, (float)(a1 * ur), (float)(-a1 * ui));
           wb_put(rq1, bsel, 0, (float)(a1 * ui), (float)(a1 * ur));
-          wb_put(rq0, bsel, 4, (float)(a2 * ur), (float)(-a2 * ui));
-          wb_put(rq1, bsel, 4, (float)(a2 * ui), (float)(a2 * ur));
+          wb_put(rq0 + 128, bsel, 0, (float)(a2 * ur), (float)(-a2 * ui));
+          wb_put(rq1 + 128, bsel, 0, (float)(a2 * ui), (float)(a2 * ur));
         }
       }
     }
@@ -825,7 +826,9 @@ static int smem_optin(const void *kernel, size_t need) {
 
 #define EW_MMA_KS 32   // atoms per S-pass stage (two 16-atom steps)
 #define EW_MMA_ATB 512 // atoms per S-pass block
-#define EW_MMA_FT 8    // 4-column tiles per force-pass stage
+#define EW_MMA_FT 4    // 4-column tiles per force-pass stage
+#define EW_MMA_MAXR 8  // largest number of force-pass column ranges
+#define EW_MMA_TEPAD 128  // zero E0|E1 rows past the last atom
 
 __device__ __forceinline__ unsigned h2_bits(__half2 h) { return *reinterpret_cast<unsigned *>(&h); }
 
@@ -1082,29 +1085,47 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
   }
 }
 
-// Force pass on the tensor cores.  One warp per 16 atoms, 8 warps per
-// block; every warp sweeps all 4-column tiles.  Z = sum_m Y U and
+// Force pass on the tensor cores.  grid = (blocks of 128 atoms, column
+// ranges); one warp per 16 atoms, 8 warps per block; every warp sweeps the
+// 4-column tiles [crange[r], crange[r+1]) of its range r.  Z = sum_m Y U and
 // Z2 = sum_m m Y U (U = the stored conj weights) come from MMAs with
 // M = 16 atoms, N = 4 columns x (re, im), K = 8 m x (re, im) per step; the Y
-// fragments of the warp's atoms stay in registers, the weight fragments of
-// EW_MMA_FT tiles at a time arrive by double-buffered bulk copies.  The
-// epilogue forms P = E0 E1 per (atom, column) from the E0|E1 table (through
-// L1) and accumulates g0 Im(P Z), g1 Im(P Z), Im(P Z2).
+// fragments of the warp's atoms stay in registers, the block's E0|E1 rows
+// are staged in shared memory once, and the weight fragments of EW_MMA_FT
+// tiles at a time arrive by double-buffered bulk copies.  A weight unit
+// (1 KB per tile and 8 m values) holds the Z fragments of the 32 lanes
+// (16 B each) and then the Z2 fragments, so each fragment load reads 512
+// contiguous bytes.  The epilogue forms P = E0 E1 per (atom, column) and
+// accumulates g0 Im(P Z), g1 Im(P Z), Im(P Z2).  With one range the sums go
+// to gfrac; with several to out[r][atom][3] for k_ewald_force_mma_combine.
 __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restrict__ te, const uint2 *__restrict__ yf,
                                                          int a0, int a1, int G0, int lep, int nmf, int nks,
-                                                         const int4 *__restrict__ cols, int nft4,
+                                                         const int4 *__restrict__ cols, const int *__restrict__ crange,
                                                          const int *__restrict__ woff, const uint4 *__restrict__ wb,
-                                                         double inv1, double inv2, double *__restrict__ gfrac,
-                                                         int *__restrict__ status) {
+                                                         double inv1, double inv2, double *__restrict__ out,
+                                                         int64_t rstride, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_mma[];
-  __shared__ unsigned long long bars[2];
+  __shared__ unsigned long long bars[3];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
-  const int wbase = a0 + (blockIdx.x * 8 + w) * 16;  // a0: a multiple of 16
-  const int stage_units = EW_MMA_FT * nks;           // 1 KB units per stage (max)
+  const int bbase = a0 + blockIdx.x * 128;
+  const int wbase = bbase + w * 16;
+  const int cr0 = crange[blockIdx.y], cr1 = crange[blockIdx.y + 1];
+  const size_t te_bytes = (size_t)128 * lep * sizeof(float2);
+  const int stage_units = EW_MMA_FT * nks;  // 1 KB units per stage (max)
   const size_t stage = (size_t)stage_units * 1024 + EW_MMA_FT * 4 * sizeof(int4);
-  // Y fragments of the warp's atoms (rows beyond the group read padding or
-  // other groups' atoms; their sums are never stored)
+  const float2 *sTE = reinterpret_cast<const float2 *>(smem_mma);
+  unsigned char *sbuf = smem_mma + te_bytes;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // the block's 128 E0|E1 rows (te holds 128 zero rows past the last atom)
+  if (threadIdx.x == 0) bulk_load(smem_mma, te + (size_t)bbase * lep, (unsigned)te_bytes, &bars[2]);
+  // Y fragments of the warp's atoms (atoms past the group read zeros)
   unsigned yh[4][4], yl[4][4];
   const int ra = min(wbase + g, a1 - 1), rb = min(wbase + g + 8, a1 - 1);
   const bool va = wbase + g < a1, vb = wbase + g + 8 < a1;
@@ -1122,22 +1143,16 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
       for (int e = 0; e < 4; e++) yh[ks][e] = yl[ks][e] = 0u;
     }
   }
-  const float2 *rowa = te + (size_t)ra * lep, *rowb = te + (size_t)rb * lep;
+  const float2 *rowa = sTE + (size_t)(w * 16 + g) * lep, *rowb = rowa + (size_t)8 * lep;
   CompAcc<float> acc[2][3];
 #pragma unroll
   for (int r = 0; r < 2; r++)
 #pragma unroll
     for (int q = 0; q < 3; q++) acc[r][q].init();
-  const int nstage = (nft4 + EW_MMA_FT - 1) / EW_MMA_FT;
-  if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    mbar_init_fence();
-  }
-  __syncthreads();
+  const int nstage = (cr1 - cr0 + EW_MMA_FT - 1) / EW_MMA_FT;
   auto issue = [&](int s) {
-    const int t0 = s * EW_MMA_FT, t1 = min(nft4, t0 + EW_MMA_FT);
-    unsigned char *dst = smem_mma + (size_t)(s & 1) * stage;
+    const int t0 = cr0 + s * EW_MMA_FT, t1 = min(cr1, t0 + EW_MMA_FT);
+    unsigned char *dst = sbuf + (size_t)(s & 1) * stage;
     const unsigned wbytes = (unsigned)(woff[t1] - woff[t0]) * 1024u;
     const unsigned cbytes = (unsigned)((t1 - t0) * 4 * sizeof(int4));
     unsigned long long *bar = &bars[s & 1];
@@ -1146,6 +1161,11 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
     bulk_copy(dst + (size_t)stage_units * 1024, cols + t0 * 4, cbytes, bar);
   };
   if (threadIdx.x == 0 && nstage > 0) issue(0);
+  bool ok_te = mbar_wait(&bars[2], 0, status);
+  if (__syncthreads_or(!ok_te)) {
+    if (threadIdx.x == 0 && nstage > 0) mbar_wait(&bars[0], 0, status);
+    return;
+  }
   for (int s = 0; s < nstage; s++) {
     if (threadIdx.x == 0 && s + 1 < nstage) issue(s + 1);
     const bool arrived = mbar_wait(&bars[s & 1], (unsigned)((s >> 1) & 1), status);
@@ -1153,19 +1173,19 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
       if (threadIdx.x == 0 && s + 1 < nstage) mbar_wait(&bars[(s + 1) & 1], (unsigned)(((s + 1) >> 1) & 1), status);
       break;
     }
-    const unsigned char *buf = smem_mma + (size_t)(s & 1) * stage;
+    const unsigned char *buf = sbuf + (size_t)(s & 1) * stage;
+    const uint4 *fr = reinterpret_cast<const uint4 *>(buf);
     const int4 *scol = reinterpret_cast<const int4 *>(buf + (size_t)stage_units * 1024);
-    const int t0 = s * EW_MMA_FT, t1 = min(nft4, t0 + EW_MMA_FT);
-    const int u0 = woff[t0];
+    const int nt = min(cr1, cr0 + s * EW_MMA_FT + EW_MMA_FT) - (cr0 + s * EW_MMA_FT);
     float ps[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    for (int ft = t0; ft < t1; ft++) {
-      const int ku = woff[ft] - u0, kn = woff[ft + 1] - woff[ft];  // this tile's k-steps
-      const uint4 *fr = reinterpret_cast<const uint4 *>(buf) + (size_t)ku * 64 + lane * 2;
+    int ku = 0;  // first unit of the tile in the stage
+    for (int j = 0; j < nt; j++) {
+      const int kn = (scol[j * 4].w + 8) >> 3;  // the tile's k-steps: its first column's extent
       float z[4] = {0.f, 0.f, 0.f, 0.f}, z2[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int ks = 0; ks < 4; ks++) {
         if (ks < kn) {
-          const uint4 b1 = fr[ks * 64], b2 = fr[ks * 64 + 1];
+          const uint4 b1 = fr[(ku + ks) * 64 + lane], b2 = fr[(ku + ks) * 64 + 32 + lane];
           mma_f16(z, yh[ks], b1.x, b1.y);
           mma_f16(z, yh[ks], b1.z, b1.w);
           mma_f16(z, yl[ks], b1.x, b1.y);
@@ -1174,15 +1194,16 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
           mma_f16(z2, yl[ks], b2.x, b2.y);
         }
       }
+      ku += kn;
       // z[0], z[1]: Z of (atom g, column t); z[2], z[3]: atom g + 8
-      const int4 col = scol[(ft - t0) * 4 + t];
+      const int4 col = scol[j * 4 + t];
       if (col.z >= 0) {
         const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = G0 + 1 + (col.y < 0 ? -col.y : col.y);
         const float sx = col.x < 0 ? -1.f : 1.f, sy = col.y < 0 ? -1.f : 1.f;
 #pragma unroll
         for (int r = 0; r < 2; r++) {
           const float2 *row = r ? rowb : rowa;
-          const float2 e0 = __ldg(row + ag0), e1 = __ldg(row + ag1);
+          const float2 e0 = row[ag0], e1 = row[ag1];
           const float e0y = sx * e0.y, e1y = sy * e1.y;
           const float pr = e0.x * e1.x - e0y * e1y;
           const float pi = e0.x * e1y + e0y * e1.x;
@@ -1201,6 +1222,7 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
     __syncthreads();  // the buffer is refilled two stages later
   }
   // sum the four column lanes of every atom (fixed order), unscale, store
+  double *dst = out + (int64_t)blockIdx.y * rstride;
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     double v[3];
@@ -1212,11 +1234,22 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
     }
     const int a = wbase + g + 8 * r;
     if (t == 0 && a < a1) {
-      gfrac[(int64_t)a * 3] = v[0] * inv1;
-      gfrac[(int64_t)a * 3 + 1] = v[1] * inv1;
-      gfrac[(int64_t)a * 3 + 2] = v[2] * inv2;
+      dst[(int64_t)a * 3] = v[0] * inv1;
+      dst[(int64_t)a * 3 + 1] = v[1] * inv1;
+      dst[(int64_t)a * 3 + 2] = v[2] * inv2;
     }
   }
+}
+
+// gfrac of atoms [a0, a1) = the sum of the column ranges' parts, in order.
+__global__ void k_ewald_force_mma_combine(const double *__restrict__ part, int64_t rstride, int nrange, int a0,
+                                          int a1, double *__restrict__ gfrac) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)(a1 - a0) * 3) return;
+  const int64_t k = (int64_t)a0 * 3 + idx;
+  double s = 0.0;
+  for (int r = 0; r < nrange; r++) s += part[r * rstride + k];
+  gfrac[k] = s;
 }
 
 // Blocks of a kernel the device holds at once (all SMs), cached per
@@ -1396,12 +1429,13 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   const double s1 = ub > 0.0 ? 8192.0 / pow2_ceil(ub) : 1.0;
   const double s2 = s1 / pow2_ceil(std::max(1, G2));
   // tables
-  if ((rc = yg_ensure(ctx, &ctx->d_ew_te, &ctx->ew_bytes_te, (size_t)(N + EW_MMA_KS) * lep * sizeof(float2)))) return rc;
+  if ((rc = yg_ensure(ctx, &ctx->d_ew_te, &ctx->ew_bytes_te, (size_t)(N + EW_MMA_TEPAD) * lep * sizeof(float2))))
+    return rc;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_yf, &ctx->ew_bytes_yf, (size_t)N * nmf * sizeof(uint2)))) return rc;
   const size_t ys_bytes = (size_t)ys_blocks * nms * 8 * sizeof(uint4);
   if ((rc = yg_ensure(ctx, &ctx->d_ew_ys, &ctx->ew_bytes_ys, ys_bytes))) return rc;
   float2 *te = (float2 *)ctx->d_ew_te;
-  YG_CUDA(cudaMemsetAsync(te + (size_t)N * lep, 0, (size_t)EW_MMA_KS * lep * sizeof(float2), ctx->stream));
+  YG_CUDA(cudaMemsetAsync(te + (size_t)N * lep, 0, (size_t)EW_MMA_TEPAD * lep * sizeof(float2), ctx->stream));
   YG_CUDA(cudaMemsetAsync(ctx->d_ew_ys, 0, ys_bytes, ctx->stream));
   k_tables_mma<<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(
       ctx->d_pos, ctx->d_charge, N, lo, hi, gbase[1], gbase[2], ctx->cell, G0, G1, G2, (float)qscale, lep, nmf, nms,
@@ -1458,17 +1492,46 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   }
   // force pass, per atom group
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
-  const size_t fsm = 2 * ((size_t)EW_MMA_FT * nks * 1024 + EW_MMA_FT * 4 * sizeof(int4));
+  const size_t fsm = (size_t)128 * lep * sizeof(float2) +
+                     2 * ((size_t)EW_MMA_FT * nks * 1024 + EW_MMA_FT * 4 * sizeof(int4));
   if ((rc = smem_optin((const void *)k_ewald_force_mma, fsm))) return rc;
+  int slots;
+  if ((rc = resident_blocks((const void *)k_ewald_force_mma, 256, fsm, &ctx->ew_occ_fm, &slots))) return rc;
   for (int g = 0; g < nS; g++) {
     const int64_t n = gb[g][1] - gb[g][0];
     if (n <= 0) continue;
     const uint4 *wbg = (const uint4 *)ctx->d_ew_wb + (size_t)(ngroup == 1 ? 0 : g) * (wbstride / 4);
-    k_ewald_force_mma<<<(int)((n + 127) / 128), 256, fsm, ctx->stream>>>(
-        te, (const uint2 *)ctx->d_ew_yf, (int)gb[g][0], (int)gb[g][1], G0, lep, nmf, nks,
-        (const int4 *)ctx->d_ew_tiles, ctx->ew_nft4, ctx->d_ew_woff, wbg, 1.0 / (qscale * s1), 1.0 / (qscale * s2),
-        ctx->d_ew_gpart, ctx->d_status);
+    // column ranges: the count whose last wave is fullest (fewest on a tie)
+    const int nab = (int)((n + 127) / 128);
+    int nr = 1;
+    double best = 0.0;
+    for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nft4); r++) {
+      const double waves = (double)nab * r / slots;
+      const double eff = waves / std::ceil(waves);
+      if (eff > best + 1e-9) {
+        best = eff;
+        nr = r;
+      }
+    }
+    double *out = ctx->d_ew_gpart;
+    const int64_t rstride = N * 3;
+    if (nr > 1) {
+      if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_fpiece, &ctx->ew_bytes_fpiece, (size_t)nr * rstride * sizeof(double))))
+        return rc;
+      out = ctx->d_ew_fpiece;
+    }
+    dim3 grid(nab, nr);
+    k_ewald_force_mma<<<grid, 256, fsm, ctx->stream>>>(
+        te, (const uint2 *)ctx->d_ew_yf, (int)gb[g][0], (int)gb[g][1], G0, lep, nmf, nks, (const int4 *)ctx->d_ew_tiles,
+        ctx->d_ew_crange + (nr - 1) * (nr + 2) / 2, ctx->d_ew_woff, wbg, 1.0 / (qscale * s1), 1.0 / (qscale * s2),
+        out, rstride, ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma");
+    if (nr > 1) {
+      k_ewald_force_mma_combine<<<yg_blocks(n * 3, 256), 256, 0, ctx->stream>>>(ctx->d_ew_fpiece, rstride, nr,
+                                                                                (int)gb[g][0], (int)gb[g][1],
+                                                                                ctx->d_ew_gpart);
+      YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma_combine");
+    }
   }
   k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
                                                            -6.2831853071795864769 / ctx->ew_diel, gpos);
@@ -1548,11 +1611,28 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   // tensor-core layout: 4-column tiles with work and their fragment units
   // (one 1 KB unit per 8 m values of the tile's extent)
   ctx->ew_amax = amax;
-  ctx->ew_mma = (nm <= 32) ? 1 : 0;
+  // (the force pass stages 128 E0|E1 rows of G0 + G1 + 2 entries in shared memory)
+  ctx->ew_mma = (nm <= 32 && G0 + G1 + 2 <= 160) ? 1 : 0;
   std::vector<int> woff(1, 0);
   for (size_t t = 0; t * 4 < tiles.size() && tiles[t * 4].w >= 0; t++) woff.push_back(woff.back() + (tiles[t * 4].w + 8) / 8);
   ctx->ew_nft4 = (int)woff.size() - 1;
   ctx->ew_wbunits = woff.back();
+  // column ranges of the force pass for r = 1 .. EW_MMA_MAXR ranges, at
+  // (r - 1)(r + 2) / 2: bounds of equal cost (6 MMAs per k-step plus an
+  // epilogue worth about two)
+  std::vector<int> crange;
+  {
+    std::vector<long long> cost(1, 0);
+    for (int t = 0; t < ctx->ew_nft4; t++) cost.push_back(cost.back() + 6LL * (woff[t + 1] - woff[t]) + 2);
+    for (int r = 1; r <= EW_MMA_MAXR; r++)
+      for (int i = 0; i <= r; i++) {
+        int t = 0;
+        while (t < ctx->ew_nft4 && cost[t] * r < cost.back() * i) t++;
+        crange.push_back(t);
+      }
+  }
+  yg_free(ctx, (void **)&ctx->d_ew_crange);
+  ctx->d_ew_crange = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_woff);
   ctx->d_ew_woff = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_wslot);
@@ -1569,6 +1649,9 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_wslot, wslot.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_fpre, fpre.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_woff, woff.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_crange, crange.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_crange, crange.data(), crange.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_woff, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_fpre, fpre.data(), fpre.size() * sizeof(int), cudaMemcpyHostToDevice,

@@ -187,6 +187,8 @@ struct yg_ctx {
   int ew_nft4 = 0;                // 4-column force tiles with work
   int ew_wbunits = 0;             // 1 KB fragment units of one group's weights
   int *d_ew_woff = nullptr;       // first fragment unit of every 4-column tile (nft4 + 1)
+  int *d_ew_crange = nullptr;     // column-range bounds of the force pass for 1..EW_MMA_MAXR ranges
+  yg_occ ew_occ_fm;               // resident tensor-core force-pass blocks
   void *d_ew_te = nullptr;        // E0|E1 rows (float2), atoms padded to a multiple of 32
   void *d_ew_yf = nullptr;        // q E2 as FP16 (hi, lo) pairs per (atom, m)
   void *d_ew_ys = nullptr;        // q E2 as FP16 B fragments per 16 atoms
