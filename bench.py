@@ -130,6 +130,17 @@ def fp32_fma_peak(torch):
     return (v if v > 0 else None), both
 
 
+def warp_mma_peak(torch):
+    """Warp-level FP16 MMA (m16n8k16, FP32 accumulate) throughput in
+    TFLOP/s, measured with an MMA-chain kernel of the library: the ceiling of
+    the instruction the tensor-core Ewald kernels use."""
+    import ctypes
+    from yaff_gb300 import _lib
+    lib = _lib.load()
+    v = float(lib.yg_probe_peak(5, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return v if v > 0 else None
+
+
 def run_gb300(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -208,17 +219,30 @@ def run_gb300(args, world, rank, local):
         e1.record(stream)
         torch.cuda.synchronize()
         skin_times.append(e0.elapsed_time(e1) * 1e-3)
-    # dominant kernel timing: the reciprocal-space part alone
+    # per-phase timing of a full evaluation (L2 flushed first): neighbour
+    # build, pair terms, reciprocal-space sum -- the three dominant parts
     reci = [p for p in ff.parts if isinstance(p, yaff_gb300.ForcePartEwaldReciprocal)][0]
-    for s in range(5):
+    phase_times = {'neighbour_build': [], 'pair': [], 'ewald_reciprocal': []}
+    for s in range(args.warmup, args.warmup + 5):
         flush.fill_(float(s))
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        dev.upload_positions_device(dpos[s % len(dpos)].data_ptr())
+        ff.nlist.rebuild_next = True
+        ev[0].record(stream)
+        ff.nlist.update(upload=False)
+        ev[1].record(stream)
+        pmask = 0
+        for p in ff.parts:
+            if isinstance(p, yaff_gb300.ForcePartPair):
+                pmask |= 1 << p._register()
+        _lib.check(dev.lib.yg_pair_compute(dev.ctx, pmask, 1), 'pair')
+        ev[2].record(stream)
         reci._launch(True)
-        e1.record(stream)
+        ev[3].record(stream)
         torch.cuda.synchronize()
-        ewald_times.append(e0.elapsed_time(e1) * 1e-3)
+        for k, name in enumerate(('neighbour_build', 'pair', 'ewald_reciprocal')):
+            phase_times[name].append(ev[k].elapsed_time(ev[k + 1]) * 1e-3)
+    ewald_times = phase_times['ewald_reciprocal']
     clk = clocks.stop()
     t_step = float(np.mean(times))
     if world > 1:
@@ -269,25 +293,67 @@ def run_gb300(args, world, rank, local):
         dev.set_precision(args.precision)
 
     pk, pk_src = peaks()
-    nk = dev.ew_nk if hasattr(dev, 'ew_nk') else None
     nk = ff_nk(ff)
-    t_reci = float(np.mean(ewald_times))
-    flops = 18.0 * natom * nk  # algorithmic flops per atom*k of the reference's direct sum
     fp32_peak, fp32_probe = fp32_fma_peak(torch)
-    # DRAM traffic of k_sfac + k_ewald_force: both read every atom's phase-table row once per launch
-    # (everything else stays in L2); ncu measured 19.42 MB for the pair at 20,000 atoms with 60-entry rows,
-    # scaled here by atoms x row length
-    reci = [p for p in ff.parts if isinstance(p, yaff_gb300.ForcePartEwaldReciprocal)][0]
-    row = (int(sum(reci.gmax)) + 4) // 2 * 2
-    traffic = 19.42e6 * (natom * row) / (20000 * 60)
-    roof = {'bound': 'fp32', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s',
-            'peak': fp32_peak, 'peak_source': 'FP32 FMA-chain kernels in bench.py, the largest of scalar, packed '
-                                              'f32x2 and both interleaved (measured-peaks file has no FP32 figure)',
-            'peak_probe_tflops': fp32_probe,
-            'frac': (flops / t_reci / 1e12) / fp32_peak if fp32_peak else None, 'traffic': traffic,
-            'traffic_source': 'ncu dram read+write of k_sfac + k_ewald_force at 20,000 atoms, scaled by atoms x row',
-            'kernel': 'ewald_reciprocal (k_sfac + k_ewald_force)', 'ms_per_launch': t_reci * 1e3,
-            'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18}}
+    mma_probe = warp_mma_peak(torch)
+    nat_scale = natom / 50000.0
+    rooflines = {}
+    # (c) reciprocal-space sum: 18 flops per atom*k of the reference's direct sum
+    t_reci = float(np.mean(phase_times['ewald_reciprocal']))
+    flops = 18.0 * natom * nk
+    g = [int(x) for x in reci.gmax]
+    tensor_path = args.precision != 'fp64' and g[2] + 1 <= 32 and g[0] + g[1] + 2 <= 160
+    if tensor_path:
+        rooflines['ewald_reciprocal'] = {
+            'bound': 'tensor', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s', 'peak': pk['bf16_tflops'],
+            'peak_source': pk_src + ' dense bf16 (burst)', 'frac': flops / t_reci / 1e12 / pk['bf16_tflops'],
+            'kernel': 'k_sfac_mma + k_ewald_force_mma (warp MMA, FP16 hi/lo split, FP32 accumulate) + tables/reduce',
+            'ms': t_reci * 1e3, 'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18},
+            'tensor_flops_executed_per_atom_k': 72,
+            'tensor_tflops_executed': 72.0 * natom * nk / t_reci / 1e12,
+            'warp_mma_f16_peak_tflops': mma_probe,
+            'frac_of_warp_mma_peak': (72.0 * natom * nk / t_reci / 1e12 / mma_probe) if mma_probe else None,
+            'traffic': 75.3e6 * nat_scale,
+            'traffic_source': 'ncu dram read+write of k_sfac_mma (39.4 MB) + k_ewald_force_mma (35.9 MB) at 50,000 '
+                              'atoms' + ('' if natom == 50000 else ', scaled by atoms')}
+    else:
+        rooflines['ewald_reciprocal'] = {
+            'bound': 'fp32' if args.precision != 'fp64' else 'fp64', 'achieved': flops / t_reci / 1e12,
+            'unit': 'TFLOP/s', 'peak': fp32_peak, 'peak_source': 'FP32 FMA-chain kernels in bench.py',
+            'frac': flops / t_reci / 1e12 / fp32_peak if fp32_peak else None,
+            'kernel': 'k_sfac + k_ewald_force (CUDA cores)', 'ms': t_reci * 1e3,
+            'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18}, 'traffic': None}
+    # (a) neighbour build: 24 B per atom (positions) + 8 B per half-list row
+    t_build = float(np.mean(phase_times['neighbour_build']))
+    nrow = int(ff.nlist.nneigh)
+    bbytes = 24.0 * natom + 8.0 * nrow
+    rooflines['neighbour_build'] = {
+        'bound': 'hbm', 'achieved': bbytes / t_build / 1e9, 'unit': 'GB/s', 'peak': pk['hbm_gbs'],
+        'peak_source': pk_src, 'frac': bbytes / t_build / 1e9 / pk['hbm_gbs'],
+        'kernel': 'k_bin + k_scan_cells + k_scatter + k_sort_cells + k_origins + k_prep + k_build (full rows, '
+                  'exact FP64 decisions in the FP32 guard band)',
+        'ms': t_build * 1e3, 'units': {'rows': nrow, 'bytes': bbytes},
+        'traffic': 309.6e6 * nat_scale,
+        'traffic_source': 'ncu dram read+write of k_build (the candidate sweep) at 50,000 atoms: it writes both '
+                          'directions of every pair' + ('' if natom == 50000 else ', scaled by atoms')}
+    # (b) pair terms: 75 flops (+3 transcendentals) per half-list pair within rcut; the pairs within rcut
+    # are estimated from the list by the (rcut / (rcut + skin))^3 volume ratio
+    t_pair = float(np.mean(phase_times['pair']))
+    rcut, skin = float(spec['rcut']), float(spec['skin'])
+    npair = nrow * (rcut / (rcut + skin)) ** 3
+    rooflines['pair'] = {
+        'bound': 'fp32', 'achieved': 75.0 * npair / t_pair / 1e12, 'unit': 'TFLOP/s', 'peak': fp32_peak,
+        'peak_source': 'FP32 FMA-chain kernels in bench.py (measured-peaks file has no FP32 figure)',
+        'frac': (75.0 * npair / t_pair / 1e12 / fp32_peak) if fp32_peak else None,
+        'kernel': 'k_pair<MM3, EI> (one warp per atom over its full row; each pair is evaluated from both ends)',
+        'ms': t_pair * 1e3, 'units': {'pairs_within_rcut': npair, 'flops_per_pair': 75, 'transcendentals_per_pair': 3},
+        'traffic': 376.8e6 * nat_scale,
+        'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms' + ('' if natom == 50000 else
+                                                                             ', scaled by atoms')}
+    dom = max(rooflines, key=lambda k: rooflines[k]['ms'])
+    roof = dict(rooflines[dom])
+    roof['name'] = dom
+    roof['fp32_peak_probe_tflops'] = fp32_probe
     lat = np.array(times) * 1e3
     out = {
         'metric': 'force evals/s', 'value': value, 'unit': 'evals/s', 'n_gpus': world, 'steps': args.steps,
@@ -307,7 +373,7 @@ def run_gb300(args, world, rank, local):
                 'd2h_bytes_per_step': natom * 24 + 9 * 8 + 16 * 8},
         'gpu_launches': int(launches),
         'clocks': clk,
-        'roofline': roof,
+        'roofline': roof, 'rooflines': rooflines,
         'peaks_source': pk_src,
     }
     return out, spec
