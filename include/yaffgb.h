@@ -118,6 +118,11 @@ int yg_clear_pair_pots(yg_ctx *ctx);
 int yg_nlist_build(yg_ctx *ctx, double rcut_total, const int64_t *rmax,
                    int64_t nlow, int64_t nhigh, int64_t *nneigh);
 
+/* Statistics of the last host-driven build (no reference counterpart):
+ * candidates decided by the exact FP64 test (inside the FP32 guard band)
+ * and the longest per-atom row of the device list (both directions). */
+int yg_nlist_stats(yg_ctx *ctx, int64_t *nexact, int64_t *maxrow);
+
 /* Skin path: keeps the pairs of the last rebuild and re-evaluates relative
  * vectors from the current positions.  Replaces nlist_recompute_low
  * (yaff/pes/nlist.c:183-232). */

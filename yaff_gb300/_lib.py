@@ -55,6 +55,7 @@ SIGNATURES = {
     'yg_set_pair_pot': (_I, [_P, _I, _I, _P, _P, _P, _P, _D, _D, _D, _I, _D]),
     'yg_clear_pair_pots': (_I, [_P]),
     'yg_nlist_build': (_I, [_P, _D, _P, _I64, _I64, ctypes.POINTER(_I64)]),
+    'yg_nlist_stats': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     'yg_nlist_recompute': (_I, [_P]),
     'yg_nlist_max_disp2': (_I, [_P, ctypes.POINTER(_D)]),
     'yg_nlist_export': (_I, [_P, _P, _I64, ctypes.POINTER(_I64)]),

@@ -430,6 +430,13 @@ int yg_clear_pair_pots(yg_ctx *c) {
   return YG_OK;
 }
 
+int yg_nlist_stats(yg_ctx *c, int64_t *nexact, int64_t *maxrow) {
+  if (!c) return YG_ERR_ARG;
+  if (nexact) *nexact = c->h_status[YG_ST_EXACT];
+  if (maxrow) *maxrow = c->h_status[YG_ST_MAXCOUNT];
+  return YG_OK;
+}
+
 int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nlow, int64_t nhigh,
                    int64_t *nneigh) {
   if (!c || !rmax || !(rcut_total > 0.0)) return YG_ERR_ARG;
