@@ -22,10 +22,13 @@
 #include <cstring>
 #include <vector>
 
+#include <mutex>
+
 #include "yg_internal.cuh"
 
 #define YG_CELL_DIV 4      // grid cells at least r_c / 4 wide
 #define YG_BUILD_RUNS 192  // candidate runs per warp held in shared memory
+#define YG_BUILD_MAP 4096  // candidates per warp whose run index is tabulated
 
 namespace {
 
@@ -306,15 +309,19 @@ __device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
 // are laid out as runs in shared memory (lanes build the runs of different
 // rows in parallel), then swept as one flat index space 32 at a time, so
 // short runs of the fine grid do not leave lanes idle.
+// Dynamic shared memory of k_build per warp: runs, run offsets, candidate map.
+#define YG_BUILD_WARP_SMEM (YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4 + YG_BUILD_MAP)
+
 __global__ void __launch_bounds__(256, 2) k_build(BuildArgs A) {
-  __shared__ int4 s_run[8][YG_BUILD_RUNS];
-  __shared__ int s_off[8][YG_BUILD_RUNS + 1];
+  extern __shared__ __align__(16) unsigned char build_smem[];
   if (A.gate && !*A.gate) return;
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   if (i >= A.natom) return;
-  int4 *run = s_run[wv];
-  int *off = s_off[wv];
+  unsigned char *wsm = build_smem + (size_t)wv * YG_BUILD_WARP_SMEM;
+  int4 *run = reinterpret_cast<int4 *>(wsm);
+  int *off = reinterpret_cast<int *>(wsm + YG_BUILD_RUNS * 16);
+  unsigned char *map = wsm + YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4;  // run of every candidate of the batch
   const int oi = A.sorted[i];
   const float4 xi = A.x32[i];
   const int cid = A.cell_of[oi];
@@ -385,12 +392,25 @@ __global__ void __launch_bounds__(256, 2) k_build(BuildArgs A) {
     if (lane == 0) off[0] = 0;
     __syncwarp();
     const int total = carry;
+    // a batch whose candidates fit the map gets each candidate's run written
+    // once (lanes fill the runs' ranges), so the sweep looks it up instead of
+    // stepping through the run offsets
+    const bool mapped = total <= YG_BUILD_MAP && nrun <= 256;
+    if (mapped) {
+      for (int b = lane; b < nrun; b += 32) {
+        const int c1 = off[b + 1];
+        for (int c = off[b]; c < c1; c++) map[c] = (unsigned char)b;
+      }
+      __syncwarp();
+    }
     int r = 0;
     for (int q0 = 0; q0 < total; q0 += 32) {
       const int q = q0 + lane;
       int in = 0, central = 1, oj = -1, oidx = 0, j = 0;
       if (q < total) {
-        while (off[r + 1] <= q) r++;
+        if (mapped) r = map[q];
+        else
+          while (off[r + 1] <= q) r++;
         const int4 rr = run[r];
         j = rr.x + (q - off[r]);
         const float4 xj = A.xb[j];
@@ -874,7 +894,19 @@ static int enqueue_build(yg_ctx *ctx, double rc2, const int *gate, unsigned long
   A.hi = ctx->band_hi;
   A.total = total;
   A.gate = gate;
-  k_build<<<yg_blocks(N * 32, 256), 256, 0, ctx->stream>>>(A);
+  const size_t bsm = (size_t)8 * YG_BUILD_WARP_SMEM;
+  static int optin_dev = -1;  // the dynamic shared-memory limit is raised once per device
+  {
+    static std::mutex mu;
+    int dev = 0;
+    YG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (optin_dev != dev) {
+      YG_CUDA(cudaFuncSetAttribute((const void *)k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+      optin_dev = dev;
+    }
+  }
+  k_build<<<yg_blocks(N * 32, 256), 256, bsm, ctx->stream>>>(A);
   YG_LAUNCH_CHECK(ctx, "k_build");
   return YG_OK;
 }
