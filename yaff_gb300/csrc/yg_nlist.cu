@@ -404,7 +404,48 @@ __global__ void __launch_bounds__(256, 2) k_build(BuildArgs A) {
       __syncwarp();
     }
     int r = 0;
-    for (int q0 = 0; q0 < total; q0 += 32) {
+    if (mapped && A.fast && !need_oj) {
+      // common case (no exclusions, no nlow/nhigh filter, FP32 shortcut on):
+      // branch-free FP32 test, the exact replay only for the rare candidates
+      // inside the guard band; 32-bit row positions
+      const int cap32 = (int)min(A.cap, (int64_t)0x7fffffff);
+      int base32 = (int)base;
+      const unsigned lt = (1u << lane) - 1u;
+      for (int q0 = 0; q0 < total; q0 += 32) {
+        const int q = min(q0 + lane, total - 1);
+        const bool live = q0 + lane < total;
+        const int rq = map[q];
+        const int4 rr = run[rq];
+        const int j = rr.x + (q - off[rq]);
+        const float4 xj = A.xb[j];
+        const int oidx = rr.z + __float_as_int(xj.w);
+        const float4 sh = A.shift32[oidx];
+        const float dx = (xj.x - xi.x) + sh.x;
+        const float dy = (xj.y - xi.y) + sh.y;
+        const float dz = (xj.z - xi.z) + sh.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const bool self0 = (rr.w >> 30) && (j == i) && (oidx == oidx_home);
+        const bool ok = live && !self0;
+        int in = (ok && d2 < A.lo) ? 1 : 0;
+        int central = 1;
+        if (ok && d2 >= A.lo && d2 <= A.hi) {
+          const int oj = A.sorted[j];
+          const int pk = rr.w;
+          const int n0 = (pk & 1023) - 512, n1 = ((pk >> 10) & 1023) - 512, n2 = ((pk >> 20) & 1023) - 512;
+          int tt[3] = {n0 + wi[0] - A.wimg[3 * oj], n1 + wi[1] - A.wimg[3 * oj + 1], n2 + wi[2] - A.wimg[3 * oj + 2]};
+          in = exact_decide(A, oi, oj, tt, &central);
+          nexact++;
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, in);
+        if (in) {
+          const int pos = base32 + __popc(ball & lt);
+          if (pos < cap32) out[pos] = make_uint2((unsigned)j, (unsigned)oidx | (central ? YG_META_CENTRAL : 0u));
+        }
+        base32 += __popc(ball);
+      }
+      base = base32;
+    }
+    for (int q0 = (mapped && A.fast && !need_oj) ? total : 0; q0 < total; q0 += 32) {
       const int q = q0 + lane;
       int in = 0, central = 1, oj = -1, oidx = 0, j = 0;
       if (q < total) {
