@@ -95,7 +95,80 @@ __device__ __forceinline__ void warp_twosum(float &h, float &l) {
   }
 }
 
-template <int MODE, int NPOT>
+// One pair term of compile-time kind K in FP32 (mixed modes, no truncation,
+// EI without Gaussian radii and with alpha > 0): the formulas and operation
+// order of pair_term_f32, without its run-time dispatch.
+template <int K>
+__device__ __forceinline__ void pair_term_k(float alpha, float invd, float d, float inv_d, float inv_d2, float pi0,
+                                            float pi1, float pi3, float pj0, float pj1, float pj3, float qi, float qj,
+                                            float &v, float &g) {
+  if (K == YG_POT_LJ) {
+    const float sig = 0.5f * (pi0 + pj0);
+    const float eps = pi1 * pj1;
+    const float s2 = sig * sig * inv_d2;
+    const float x = s2 * s2 * s2;
+    g = 24.0f * eps * inv_d2 * x * (1.0f - 2.0f * x);
+    v = 4.0f * eps * (x * (x - 1.0f));
+  } else if (K == YG_POT_MM3) {
+    const float sig = pi0 + pj0;
+    const float eps = pi1 * pj1;
+    const float inv_sig = __frcp_rn(sig);  // = 1.0f / sig (both correctly rounded)
+    const float ex = 1.84e5f * expf(-12.0f * d * inv_sig);
+    if (pi3 + pj3 == 0.0f) {
+      const float s2 = sig * sig * inv_d2;
+      const float x = 2.25f * s2 * s2 * s2;
+      g = eps * inv_d * (-12.0f * inv_sig * ex + 6.0f * inv_d * x);
+      v = eps * (ex - x);
+    } else {
+      g = eps * inv_d * (-12.0f * inv_sig * ex);
+      v = eps * ex;
+    }
+  } else {
+    const float qq = qi * qj * invd;
+    const float x = alpha * d;
+    const float e = expf(-x * x);
+    v = qq * erfc_cheb(x) * inv_d;
+    g = (-1.1283791670955126f * alpha * e * qq - v) * inv_d2;
+  }
+}
+
+// One list entry of potential p (compile-time kind K) in the specialised
+// mixed kernel: the term, masked with d < r_c and a nonzero scale, added to
+// the potential's energy, gradient and virial sums.
+template <int K, typename AccT>
+__device__ __forceinline__ void pot_entry(const PairArgs &A, int p, int j, float d, float inv_d, float inv_d2, float dx,
+                                          float dy, float dz, float sc, const float (&fpi)[4], float fqi, float qj,
+                                          AccT &E, AccT (&G)[3], AccT (&V)[6]) {
+  float pj0 = 0.f, pj1 = 0.f, pj3 = 0.f;
+  if (K != YG_POT_EI) {
+    const float4 q4 = *reinterpret_cast<const float4 *>(A.pp32 + (int64_t)j * 4 * YG_MAX_POT + 4 * A.pot[p].col);
+    pj0 = q4.x;
+    pj1 = q4.y;
+    pj3 = q4.w;
+  }
+  float fv, fg;
+  pair_term_k<K>(A.fpot[p][2], A.fpot[p][3], d, inv_d, inv_d2, fpi[0], fpi[1], fpi[3], pj0, pj1, pj3, fqi, qj, fv, fg);
+  const bool in = (d < A.fpot[p][0]) && (sc != 0.0f);
+  const float v = in ? fv : 0.0f;
+  float g = in ? fg : 0.0f;
+  const float s = in ? sc : 0.0f;
+  E.add(0.5f * s * v);
+  if (A.want_grad) {
+    g *= s;
+    G[0].add(-dx * g);
+    G[1].add(-dy * g);
+    G[2].add(-dz * g);
+    const float hg = 0.5f * g;
+    V[0].add(dx * dx * hg);
+    V[1].add(dy * dy * hg);
+    V[2].add(dz * dz * hg);
+    V[3].add(dx * dy * hg);
+    V[4].add(dx * dz * hg);
+    V[5].add(dy * dz * hg);
+  }
+}
+
+template <int MODE, int NPOT, int K0 = -1, int K1 = -1>
 __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) k_pair(PairArgs A) {
   typedef typename std::conditional<MODE == YG_FP64, double, float>::type T;
   const bool kahan = (MODE == YG_MIXED_KAHAN);
@@ -129,7 +202,37 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
                                      : (T)A.pp32[i * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
     const int cnt = A.ncount[i];
     const uint2 *row = A.nbr + i * A.cap;
-    for (int e = lane; e < cnt; e += 32) {
+    if (K0 >= 0) {
+      // compile-time potential kinds (mixed modes): every term is evaluated
+      // and masked with d < r_c and a nonzero scale, no per-entry dispatch
+      float fpi[NPOT][4];
+#pragma unroll
+      for (int p = 0; p < NPOT; p++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) fpi[p][k] = (float)pi[p][k];
+      const float fxi = (float)xi, fyi = (float)yi, fzi = (float)zi, fqi = (float)qi;
+      for (int e = lane; e < cnt; e += 32) {
+        const uint2 ent = row[e];
+        const int j = (int)ent.x;
+        const int oidx = (int)(ent.y & YG_META_OFF_MASK);
+        const int code = (int)((ent.y >> YG_META_SCALE_SHIFT) & 7u);
+        const float4 xj = A.x32[j];
+        const float4 sh = A.shift32[oidx];
+        const float dx = (xj.x - fxi) + sh.x;
+        const float dy = (xj.y - fyi) + sh.y;
+        const float dz = (xj.z - fzi) + sh.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float inv_d = rsqrtf(d2);
+        const float d = d2 * inv_d;
+        const float inv_d2 = inv_d * inv_d;
+        const float sc = A.fscale[code];
+        pot_entry<(K0 >= 0 ? K0 : 0)>(A, 0, j, d, inv_d, inv_d2, dx, dy, dz, sc, fpi[0], fqi, xj.w, E[0], G[0], V[0]);
+        if (NPOT > 1)
+          pot_entry<(K1 >= 0 ? K1 : 0)>(A, NPOT > 1 ? 1 : 0, j, d, inv_d, inv_d2, dx, dy, dz, sc, fpi[NPOT > 1 ? 1 : 0],
+                                        fqi, xj.w, E[NPOT > 1 ? 1 : 0], G[NPOT > 1 ? 1 : 0], V[NPOT > 1 ? 1 : 0]);
+      }
+    }
+    for (int e = (K0 >= 0) ? cnt : lane; e < cnt; e += 32) {
       const uint2 ent = row[e];
       const int j = (int)ent.x;
       const int oidx = (int)(ent.y & YG_META_OFF_MASK);
@@ -333,6 +436,31 @@ int launch_pair_t(yg_ctx *ctx, PairArgs &A, int nblocks) {
   return YG_OK;
 }
 
+// The mixed-precision kernel specialised on the potential kinds, for one or
+// two potentials without truncation (EI without radii, alpha > 0).
+template <int K0, int K1>
+int launch_pair_k(yg_ctx *ctx, PairArgs &A, int nblocks) {
+  if (K1 < 0) k_pair<YG_MIXED, 1, K0, K1><<<nblocks, 256, 0, ctx->stream>>>(A);
+  else k_pair<YG_MIXED, 2, K0, K1><<<nblocks, 256, 0, ctx->stream>>>(A);
+  YG_LAUNCH_CHECK(ctx, "k_pair");
+  return YG_OK;
+}
+
+template <int K0>
+int launch_pair_k1(yg_ctx *ctx, PairArgs &A, int npot, int k1, int nblocks) {
+  if (npot == 1) return launch_pair_k<K0, -1>(ctx, A, nblocks);
+  if (k1 == YG_POT_LJ) return launch_pair_k<K0, YG_POT_LJ>(ctx, A, nblocks);
+  if (k1 == YG_POT_MM3) return launch_pair_k<K0, YG_POT_MM3>(ctx, A, nblocks);
+  return launch_pair_k<K0, YG_POT_EI>(ctx, A, nblocks);
+}
+
+int launch_pair_fast(yg_ctx *ctx, PairArgs &A, int npot, int nblocks) {
+  const int k0 = A.pot[0].kind, k1 = npot > 1 ? A.pot[1].kind : -1;
+  if (k0 == YG_POT_LJ) return launch_pair_k1<YG_POT_LJ>(ctx, A, npot, k1, nblocks);
+  if (k0 == YG_POT_MM3) return launch_pair_k1<YG_POT_MM3>(ctx, A, npot, k1, nblocks);
+  return launch_pair_k1<YG_POT_EI>(ctx, A, npot, k1, nblocks);
+}
+
 template <int MODE>
 int launch_pair_m(yg_ctx *ctx, PairArgs &A, int npot, int nblocks) {
   switch (npot) {
@@ -413,7 +541,15 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
                       ((size_t)nblocks * nval + 64 + nval) * sizeof(double))))
     return rc;
   A.partial = ctx->d_red + 64;
+  bool fast = ctx->precision == YG_MIXED && npot <= 2;
+  for (int q = 0; q < npot; q++) {
+    const PairPotDev &D = A.pot[q];
+    if (D.tr_kind != YG_TR_NONE || (D.kind != YG_POT_LJ && D.kind != YG_POT_MM3 && D.kind != YG_POT_EI) ||
+        (D.kind == YG_POT_EI && (D.has_radii || !(D.alpha > 0.0))))
+      fast = false;
+  }
   if (ctx->precision == YG_FP64) rc = launch_pair_m<YG_FP64>(ctx, A, npot, nblocks);
+  else if (fast) rc = launch_pair_fast(ctx, A, npot, nblocks);
   else if (ctx->precision == YG_MIXED) rc = launch_pair_m<YG_MIXED>(ctx, A, npot, nblocks);
   else rc = launch_pair_m<YG_MIXED_KAHAN>(ctx, A, npot, nblocks);
   if (rc) return rc;
