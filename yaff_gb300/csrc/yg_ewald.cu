@@ -826,7 +826,9 @@ static int smem_optin(const void *kernel, size_t need) {
 
 #define EW_MMA_KS 32   // atoms per S-pass stage (two 16-atom steps)
 #define EW_MMA_ATB 512 // atoms per S-pass block
+#ifndef EW_MMA_FT
 #define EW_MMA_FT 4    // 4-column tiles per force-pass stage
+#endif
 #define EW_MMA_MAXR 8  // largest number of force-pass column ranges
 #define EW_MMA_TEPAD 128  // zero E0|E1 rows past the last atom
 
@@ -1178,24 +1180,35 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
     const int4 *scol = reinterpret_cast<const int4 *>(buf + (size_t)stage_units * 1024);
     const int nt = min(cr1, cr0 + s * EW_MMA_FT + EW_MMA_FT) - (cr0 + s * EW_MMA_FT);
     float ps[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    // all MMAs of the stage's tiles first, then their epilogues: the FP32
+    // epilogue of one tile overlaps the MMAs of the next still in flight
+    float z[EW_MMA_FT][4], z2[EW_MMA_FT][4];
     int ku = 0;  // first unit of the tile in the stage
-    for (int j = 0; j < nt; j++) {
-      const int kn = (scol[j * 4].w + 8) >> 3;  // the tile's k-steps: its first column's extent
-      float z[4] = {0.f, 0.f, 0.f, 0.f}, z2[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int ks = 0; ks < 4; ks++) {
-        if (ks < kn) {
-          const uint4 b1 = fr[(ku + ks) * 64 + lane], b2 = fr[(ku + ks) * 64 + 32 + lane];
-          mma_f16(z, yh[ks], b1.x, b1.y);
-          mma_f16(z, yh[ks], b1.z, b1.w);
-          mma_f16(z, yl[ks], b1.x, b1.y);
-          mma_f16(z2, yh[ks], b2.x, b2.y);
-          mma_f16(z2, yh[ks], b2.z, b2.w);
-          mma_f16(z2, yl[ks], b2.x, b2.y);
+    for (int j = 0; j < EW_MMA_FT; j++) {
+#pragma unroll
+      for (int e = 0; e < 4; e++) z[j][e] = z2[j][e] = 0.f;
+      if (j < nt) {
+        const int kn = (scol[j * 4].w + 8) >> 3;  // the tile's k-steps: its first column's extent
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+          if (ks < kn) {
+            const uint4 b1 = fr[(ku + ks) * 64 + lane], b2 = fr[(ku + ks) * 64 + 32 + lane];
+            mma_f16(z[j], yh[ks], b1.x, b1.y);
+            mma_f16(z[j], yh[ks], b1.z, b1.w);
+            mma_f16(z[j], yl[ks], b1.x, b1.y);
+            mma_f16(z2[j], yh[ks], b2.x, b2.y);
+            mma_f16(z2[j], yh[ks], b2.z, b2.w);
+            mma_f16(z2[j], yl[ks], b2.x, b2.y);
+          }
         }
+        ku += kn;
       }
-      ku += kn;
-      // z[0], z[1]: Z of (atom g, column t); z[2], z[3]: atom g + 8
+    }
+#pragma unroll
+    for (int j = 0; j < EW_MMA_FT; j++) {
+      if (j >= nt) break;
+      // z[j][0], z[j][1]: Z of (atom g, column t); z[j][2], z[j][3]: atom g + 8
       const int4 col = scol[j * 4 + t];
       if (col.z >= 0) {
         const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = G0 + 1 + (col.y < 0 ? -col.y : col.y);
@@ -1207,8 +1220,8 @@ __global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restric
           const float e0y = sx * e0.y, e1y = sy * e1.y;
           const float pr = e0.x * e1.x - e0y * e1y;
           const float pi = e0.x * e1y + e0y * e1.x;
-          const float im1 = pr * z[2 * r + 1] + pi * z[2 * r];
-          const float im2 = pr * z2[2 * r + 1] + pi * z2[2 * r];
+          const float im1 = pr * z[j][2 * r + 1] + pi * z[j][2 * r];
+          const float im2 = pr * z2[j][2 * r + 1] + pi * z2[j][2 * r];
           ps[r][0] += (float)col.x * im1;
           ps[r][1] += (float)col.y * im1;
           ps[r][2] += im2;
