@@ -340,13 +340,24 @@ __global__ void __launch_bounds__(128) k_sfac(const typename C2<T>::t *__restric
   }
 }
 
-// Sums the chunk partials in FP64 (fixed order) into the dense S[col][m].
+// Sums the chunk partials in a fixed order into the dense S[col][m]: four
+// threads per element each sum every fourth chunk (FP64, or error-free
+// TwoSum (hi, lo) pairs of the FP32 partials), then the four sums are
+// combined by a fixed butterfly within the aligned group of four lanes.
+__device__ __forceinline__ void two_sum_f(float &h, float &l, float xh, float xl) {
+  const float s = h + xh, bb = s - h;
+  l += (h - (s - bb)) + (xh - bb) + xl;
+  h = s;
+}
+
 template <typename TA>
 __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int nchunk, int nstile, int nslab, int sc,
                               const int4 *__restrict__ cols, int nm, double unscale, double *__restrict__ S) {
-  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t idx = tid >> 2;
+  const int sub = (int)(tid & 3);
   const int64_t per = (int64_t)nstile * nslab * sc * EW_MS;
-  if (idx >= per) return;
+  if (idx >= per) return;  // whole groups of four leave together (per-group condition)
   const int m = (int)(idx % EW_MS);
   const int c = (int)((idx / EW_MS) % sc);
   const int slab = (int)((idx / (EW_MS * sc)) % nslab);
@@ -354,38 +365,58 @@ __global__ void k_sfac_reduce(const typename C2<TA>::t *__restrict__ Spart, int 
   const int4 col = cols[tile * sc + c];
   const int mm = slab * EW_MS + m;
   if (col.z < 0 || mm > col.w) return;
+  const unsigned gmask = 0xFu << (threadIdx.x & 28);
   double re, im;
   if (sizeof(TA) == 8) {
     re = 0.0;
     im = 0.0;
-    for (int ch = 0; ch < nchunk; ch++) {
+    for (int ch = sub; ch < nchunk; ch += 4) {
       const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
       re += (double)v.x;
       im += (double)v.y;
     }
+    re += __shfl_xor_sync(gmask, re, 1);
+    im += __shfl_xor_sync(gmask, im, 1);
+    re += __shfl_xor_sync(gmask, re, 2);
+    im += __shfl_xor_sync(gmask, im, 2);
   } else {
-    // FP32 partials: error-free TwoSum accumulation in (hi, lo) pairs, one
-    // conversion to FP64 at the end (the FP64 pipe is the slow one)
+    // FP32 partials: (hi, lo) pairs, one conversion to FP64 at the end (the
+    // FP64 pipe is the slow one)
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    for (int ch = 0; ch < nchunk; ch++) {
+    for (int ch = sub; ch < nchunk; ch += 4) {
       const typename C2<TA>::t v = Spart[(int64_t)ch * per + idx];
-      float s = rh + (float)v.x, bb = s - rh;
-      rl += (rh - (s - bb)) + ((float)v.x - bb);
-      rh = s;
-      s = ih + (float)v.y;
-      bb = s - ih;
-      il += (ih - (s - bb)) + ((float)v.y - bb);
-      ih = s;
+      two_sum_f(rh, rl, (float)v.x, 0.f);
+      two_sum_f(ih, il, (float)v.y, 0.f);
+    }
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      const float orh = __shfl_xor_sync(gmask, rh, o), orl = __shfl_xor_sync(gmask, rl, o);
+      const float oih = __shfl_xor_sync(gmask, ih, o), oil = __shfl_xor_sync(gmask, il, o);
+      // both lanes of a pair add in the same order: lower lane's value first
+      if (sub & o) {
+        float h = orh, l = orl;
+        two_sum_f(h, l, rh, rl);
+        rh = h;
+        rl = l;
+        h = oih;
+        l = oil;
+        two_sum_f(h, l, ih, il);
+        ih = h;
+        il = l;
+      } else {
+        two_sum_f(rh, rl, orh, orl);
+        two_sum_f(ih, il, oih, oil);
+      }
     }
     re = (double)rh + (double)rl;
     im = (double)ih + (double)il;
   }
-  S[2 * ((int64_t)col.z * nm + mm)] = re * unscale;
-  S[2 * ((int64_t)col.z * nm + mm) + 1] = im * unscale;
+  if (sub == 0) {
+    S[2 * ((int64_t)col.z * nm + mm)] = re * unscale;
+    S[2 * ((int64_t)col.z * nm + mm) + 1] = im * unscale;
+  }
 }
 
-// Energy and virial per k (FP64), plus the force-pass weights
-// conj(W_g) = conj(2 A S_eff,g) for the atom groups in use.
 // FP16 split of a weight pair into the force pass's B fragments (see the
 // tensor-core section below); record words: hi b0, hi b1, lo b0, lo b1.
 __device__ __forceinline__ void wb_put(unsigned *__restrict__ rec, int bsel, int off, float a, float b) {
@@ -858,78 +889,107 @@ __device__ __forceinline__ void mma_split(float (&d)[4], const unsigned (&ah)[4]
   mma_f16(d, al, bh0, bh1);
 }
 
-// MMA tables, one thread per (atom, axis) over the padded atom count:
+// MMA tables, one warp per atom (lanes 0-2 form the fractional coordinate
+// of one axis each in FP64, the lanes then share them and take one table
+// entry each):
 //   te[a][0..G0] = E0, te[a][G0+1..G0+G1+1] = E1 (float2, row stride lep);
 //   yf[a][m] = (hi, lo) FP16 pairs of qscale q E2[m] (re in the low half),
-//              m < nmf (zero beyond G2);
-//   ys: per 16 atoms, per m < nms and component q (re, im), per t < 4 a
-//       16-byte unit (hi(2t,2t+1), hi(2t+8,2t+9), lo(2t,2t+1), lo(2t+8,2t+9))
-//       -- the S pass's B fragments, stored as 16-bit halves.
-// The ys position of an atom is relative to its atom group ([lo, hi) first,
-// then [0, lo), then [hi, N), each padded to a multiple of 16 atoms: bases
-// 0, base1, base2), so a group's 16-atom blocks hold only its own atoms;
-// padding entries stay zero (the buffer is cleared before).  The phases
-// follow k_tables' FP32 form.
+//              m < nmf (zero beyond G2).
+// The phases follow k_tables' FP32 form.
 __global__ void k_tables_mma(const double *__restrict__ pos, const double *__restrict__ charge, int64_t natom,
-                             int64_t lo, int64_t hi, int64_t base1, int64_t base2, CellGeom cell, int G0, int G1,
-                             int G2, float qscale, int lep, int nmf, int nms, float2 *__restrict__ te,
-                             uint2 *__restrict__ yf, unsigned short *__restrict__ ys) {
-  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx >= natom * 3) return;
-  const int64_t a = idx / 3;
-  const int axis = (int)(idx - a * 3);
-  float s_hi, s_lo;
-  {
-    const double *gv = cell.gv + 3 * axis;
-    double s = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
-    s -= floor(s);
-    s_hi = (float)s;
-    s_lo = (float)(s - (double)s_hi);
+                             CellGeom cell, int G0, int G1, int G2, float qscale, int lep, int nmf,
+                             float2 *__restrict__ te, uint2 *__restrict__ yf) {
+  const int64_t a = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (a >= natom) return;
+  float sh = 0.f, sl = 0.f;
+  if (lane < 3) {
+    const double *gv = cell.gv + 3 * lane;
+    double sd = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
+    sd -= floor(sd);
+    sh = (float)sd;
+    sl = (float)(sd - (double)sh);
   }
-  auto phase = [&](int g, float &c, float &sn) {
-    const float fg = (float)g;
-    const float p = fg * s_hi;
-    const float e = fmaf(fg, s_hi, -p);
-    const float x = (p - rintf(p)) + fmaf(fg, s_lo, e);
-    sincospif(2.0f * x, &sn, &c);
-  };
-  if (axis < 2) {
-    const int gmax = axis == 0 ? G0 : G1;
-    float2 *out = te + a * lep + (axis == 0 ? 0 : G0 + 1);
-    for (int g = 0; g <= gmax; g++) {
-      float c, sn;
-      phase(g, c, sn);
-      out[g] = make_float2(c, sn);
-    }
-    return;
-  }
+  const float sh0 = __shfl_sync(0xffffffffu, sh, 0), sl0 = __shfl_sync(0xffffffffu, sl, 0);
+  const float sh1 = __shfl_sync(0xffffffffu, sh, 1), sl1 = __shfl_sync(0xffffffffu, sl, 1);
+  const float sh2 = __shfl_sync(0xffffffffu, sh, 2), sl2 = __shfl_sync(0xffffffffu, sl, 2);
   const float q = (float)(charge[a] * (double)qscale);
-  const int64_t p = (a >= lo && a < hi) ? a - lo : (a < lo ? base1 + a : base2 + (a - hi));
-  const int64_t blk = p >> 4;
-  const int i = (int)(p & 15);
-  const int t = (i & 7) >> 1, half = i & 1, whi = i < 8 ? 0 : 1;
-  for (int m = 0; m < nmf; m++) {
-    float yr = 0.f, yi = 0.f;
-    if (m <= G2) {
-      float c, sn;
-      phase(m, c, sn);
-      yr = q * c;
-      yi = q * sn;
+  const int ne = G0 + G1 + 2;
+  for (int slot = lane; slot < ne + nmf; slot += 32) {
+    int g;
+    float s_hi, s_lo;
+    if (slot <= G0) {
+      g = slot;
+      s_hi = sh0;
+      s_lo = sl0;
+    } else if (slot < ne) {
+      g = slot - (G0 + 1);
+      s_hi = sh1;
+      s_lo = sl1;
+    } else {
+      g = slot - ne;
+      s_hi = sh2;
+      s_lo = sl2;
     }
-    unsigned hi, lo;
-    split_h2(yr, yi, hi, lo);
-    yf[a * nmf + m] = make_uint2(hi, lo);
-    if (m < nms) {
-      // component q = 0 (re): low halves; q = 1 (im): high halves
-      for (int comp = 0; comp < 2; comp++) {
-        const int64_t unit = ((blk * nms + m) * 2 + comp) * 4 + t;
-        const unsigned short h16 = (unsigned short)(comp == 0 ? (hi & 0xffffu) : (hi >> 16));
-        const unsigned short l16 = (unsigned short)(comp == 0 ? (lo & 0xffffu) : (lo >> 16));
-        ys[(unit * 4 + whi) * 2 + half] = h16;
-        ys[(unit * 4 + 2 + whi) * 2 + half] = l16;
-      }
+    const float fg = (float)g;
+    const float pp = fg * s_hi;
+    const float e = fmaf(fg, s_hi, -pp);
+    const float x = (pp - rintf(pp)) + fmaf(fg, s_lo, e);
+    float sn, c;
+    sincospif(2.0f * x, &sn, &c);
+    if (slot < ne) {
+      te[a * lep + slot] = make_float2(c, sn);
+    } else {
+      const bool used = g <= G2;
+      unsigned hi, lo;
+      split_h2(used ? q * c : 0.f, used ? q * sn : 0.f, hi, lo);
+      yf[a * nmf + g] = make_uint2(hi, lo);
     }
   }
+}
+
+// The S pass's B fragments from yf: one thread per 16-byte unit (16-atom
+// block, m < nms, component q (re, im), t < 4) =
+// (hi(2t,2t+1), hi(2t+8,2t+9), lo(2t,2t+1), lo(2t+8,2t+9)).  Block positions
+// are relative to the atom group ([lo, hi) first, then [0, lo), then [hi, N),
+// each padded to a multiple of 16 atoms: bases 0, base1, base2), so a
+// group's blocks hold only its own atoms; padding entries are zero.
+__global__ void k_ys_mma(const uint2 *__restrict__ yf, int64_t natom, int64_t lo, int64_t hi, int64_t base1,
+                         int64_t base2, int64_t nblocks, int nmf, int nms, uint4 *__restrict__ ys) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= nblocks * nms * 8) return;
+  const int t = (int)(u & 3);
+  const int comp = (int)((u >> 2) & 1);
+  const int m = (int)((u >> 3) % nms);
+  const int64_t blk = (u >> 3) / nms;
+  const int64_t p0 = blk * 16;
+  int64_t a0, n, gbase;
+  if (p0 < base1) {
+    a0 = lo; n = hi - lo; gbase = 0;
+  } else if (p0 < base2) {
+    a0 = 0; n = lo; gbase = base1;
+  } else {
+    a0 = hi; n = natom - hi; gbase = base2;
+  }
+  unsigned w[4] = {0u, 0u, 0u, 0u};
+  const int ia[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+  unsigned short hv[4], lv[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int64_t r = p0 + ia[k] - gbase;
+    hv[k] = 0;
+    lv[k] = 0;
+    if (r >= 0 && r < n && m < nmf) {
+      const uint2 v = yf[(a0 + r) * nmf + m];
+      hv[k] = (unsigned short)(comp == 0 ? (v.x & 0xffffu) : (v.x >> 16));
+      lv[k] = (unsigned short)(comp == 0 ? (v.y & 0xffffu) : (v.y >> 16));
+    }
+  }
+  w[0] = (unsigned)hv[0] | ((unsigned)hv[1] << 16);
+  w[1] = (unsigned)hv[2] | ((unsigned)hv[3] << 16);
+  w[2] = (unsigned)lv[0] | ((unsigned)lv[1] << 16);
+  w[3] = (unsigned)lv[2] | ((unsigned)lv[3] << 16);
+  ys[u] = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // S pass on the tensor cores.  grid = (atom chunks of EW_MMA_ATB, 64-column
@@ -1344,7 +1404,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
                                                  (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab,
                                                  ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_sfac");
-    k_sfac_reduce<TA><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
+    k_sfac_reduce<TA><<<yg_blocks((int64_t)per * 4, 256), 256, 0, ctx->stream>>>(
         (const CA *)ctx->d_ew_Spart, nch, nstile, nslab, EW_SC, (const int4 *)ctx->d_ew_tiles, nm, 1.0, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
@@ -1449,11 +1509,12 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   if ((rc = yg_ensure(ctx, &ctx->d_ew_ys, &ctx->ew_bytes_ys, ys_bytes))) return rc;
   float2 *te = (float2 *)ctx->d_ew_te;
   YG_CUDA(cudaMemsetAsync(te + (size_t)N * lep, 0, (size_t)EW_MMA_TEPAD * lep * sizeof(float2), ctx->stream));
-  YG_CUDA(cudaMemsetAsync(ctx->d_ew_ys, 0, ys_bytes, ctx->stream));
-  k_tables_mma<<<yg_blocks(N * 3, 128), 128, 0, ctx->stream>>>(
-      ctx->d_pos, ctx->d_charge, N, lo, hi, gbase[1], gbase[2], ctx->cell, G0, G1, G2, (float)qscale, lep, nmf, nms,
-      te, (uint2 *)ctx->d_ew_yf, (unsigned short *)ctx->d_ew_ys);
+  k_tables_mma<<<yg_blocks(N * 32, 256), 256, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2,
+                                                                (float)qscale, lep, nmf, te, (uint2 *)ctx->d_ew_yf);
   YG_LAUNCH_CHECK(ctx, "k_tables_mma");
+  k_ys_mma<<<yg_blocks(ys_blocks * nms * 8, 256), 256, 0, ctx->stream>>>(
+      (const uint2 *)ctx->d_ew_yf, N, lo, hi, gbase[1], gbase[2], ys_blocks, nmf, nms, (uint4 *)ctx->d_ew_ys);
+  YG_LAUNCH_CHECK(ctx, "k_ys_mma");
   // structure factors
   int maxchunk = 1;
   for (int g = 0; g < nS; g++)
@@ -1474,7 +1535,7 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
                                                (int)n, G0, lep, nms, (const int4 *)ctx->d_ew_tiles,
                                                (float2 *)ctx->d_ew_Spart, ntile64, 1, ctx->d_status);
     YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
-    k_sfac_reduce<float><<<yg_blocks((int64_t)per, 256), 256, 0, ctx->stream>>>(
+    k_sfac_reduce<float><<<yg_blocks((int64_t)per * 4, 256), 256, 0, ctx->stream>>>(
         (const float2 *)ctx->d_ew_Spart, nch, ntile64, 1, 64, (const int4 *)ctx->d_ew_tiles, nm, 1.0 / qscale, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
