@@ -123,6 +123,12 @@ int yg_nlist_build(yg_ctx *ctx, double rcut_total, const int64_t *rmax,
  * and the longest per-atom row of the device list (both directions). */
 int yg_nlist_stats(yg_ctx *ctx, int64_t *nexact, int64_t *maxrow);
 
+/* Layout of the reciprocal sum set up by yg_ewald_setup (no reference
+ * counterpart): whether the mixed forms run it on the tensor cores (warp
+ * MMA, needs G2 + 1 <= 32 and G0 + G1 + 2 <= 160) and the number of k
+ * vectors in the half sphere. */
+int yg_ewald_info(yg_ctx *ctx, int *tensor_path, int64_t *nk);
+
 /* Skin path: keeps the pairs of the last rebuild and re-evaluates relative
  * vectors from the current positions.  Replaces nlist_recompute_low
  * (yaff/pes/nlist.c:183-232). */

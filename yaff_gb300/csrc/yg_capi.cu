@@ -430,6 +430,13 @@ int yg_clear_pair_pots(yg_ctx *c) {
   return YG_OK;
 }
 
+int yg_ewald_info(yg_ctx *c, int *tensor_path, int64_t *nk) {
+  if (!c) return YG_ERR_ARG;
+  if (tensor_path) *tensor_path = c->have_ewald ? c->ew_mma : 0;
+  if (nk) *nk = c->have_ewald ? c->ew_nk : 0;
+  return YG_OK;
+}
+
 int yg_nlist_stats(yg_ctx *c, int64_t *nexact, int64_t *maxrow) {
   if (!c) return YG_ERR_ARG;
   if (nexact) *nexact = c->h_status[YG_ST_EXACT];
