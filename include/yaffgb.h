@@ -129,6 +129,13 @@ int yg_nlist_stats(yg_ctx *ctx, int64_t *nexact, int64_t *maxrow);
  * vectors in the half sphere. */
 int yg_ewald_info(yg_ctx *ctx, int *tensor_path, int64_t *nk);
 
+/* The reciprocal sum runs on an auxiliary stream of the context, forked at
+ * yg_ewald_reci, so that it overlaps the neighbour build and the pair terms;
+ * every call that reads its results or changes its inputs joins it back.
+ * yg_ewald_wait makes the context's stream wait for it explicitly (no host
+ * synchronization), e.g. to time it with events on the context's stream. */
+int yg_ewald_wait(yg_ctx *ctx);
+
 /* Skin path: keeps the pairs of the last rebuild and re-evaluates relative
  * vectors from the current positions.  Replaces nlist_recompute_low
  * (yaff/pes/nlist.c:183-232). */

@@ -57,6 +57,7 @@ SIGNATURES = {
     'yg_nlist_build': (_I, [_P, _D, _P, _I64, _I64, ctypes.POINTER(_I64)]),
     'yg_nlist_stats': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     'yg_ewald_info': (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64)]),
+    'yg_ewald_wait': (_I, [_P]),
     'yg_nlist_recompute': (_I, [_P]),
     'yg_nlist_max_disp2': (_I, [_P, ctypes.POINTER(_D)]),
     'yg_nlist_export': (_I, [_P, _P, _I64, ctypes.POINTER(_I64)]),

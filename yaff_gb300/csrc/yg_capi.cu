@@ -242,6 +242,7 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
 
 int yg_destroy(yg_ctx *c) {
   if (!c) return YG_OK;
+  yg_ewald_join(c);
   cudaStreamSynchronize(c->stream);
   void **bufs[] = {
       (void **)&c->d_pos, (void **)&c->d_pos_build, (void **)&c->d_charge, (void **)&c->d_cell_of,
@@ -262,6 +263,9 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_snap_step};
   if (c->md_graph_exec) cudaGraphExecDestroy(c->md_graph_exec);
   if (c->md_cap_stream) cudaStreamDestroy(c->md_cap_stream);
+  if (c->ew_aux) cudaStreamDestroy(c->ew_aux);
+  if (c->ew_fork_ev) cudaEventDestroy(c->ew_fork_ev);
+  if (c->ew_join_ev) cudaEventDestroy(c->ew_join_ev);
   if (c->pool)
     for (void **b : bufs) yg_free(c, b);
   pinned_put(c->h_block, c->h_block_bytes);
@@ -270,12 +274,20 @@ int yg_destroy(yg_ctx *c) {
 }
 
 int yg_set_precision(yg_ctx *c, int precision) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || precision < YG_FP64 || precision > YG_MIXED_KAHAN) return YG_ERR_ARG;
   c->precision = precision;
   return YG_OK;
 }
 
 int yg_set_cell(yg_ctx *c, const double *rvecs, const double *gvecs, int nvec, double volume) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || !rvecs || !gvecs) return YG_ERR_ARG;
   if (nvec != 3) {
     yg_set_error("the device neighbour list supports 3D periodic cells only (nvec == 3)");
@@ -296,6 +308,10 @@ int yg_set_cell(yg_ctx *c, const double *rvecs, const double *gvecs, int nvec, d
 }
 
 int yg_set_positions(yg_ctx *c, const double *pos, int on_device) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || !pos) return YG_ERR_ARG;
   YG_CUDA(cudaMemcpyAsync(c->d_pos, pos, c->natom * 3 * sizeof(double),
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
@@ -306,6 +322,10 @@ int yg_set_positions(yg_ctx *c, const double *pos, int on_device) {
 }
 
 int yg_set_charges(yg_ctx *c, const double *charges) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || !charges) return YG_ERR_ARG;
   std::vector<double> &h = c->h_charge;
   h.assign(charges, charges + c->natom);
@@ -430,6 +450,11 @@ int yg_clear_pair_pots(yg_ctx *c) {
   return YG_OK;
 }
 
+int yg_ewald_wait(yg_ctx *c) {
+  if (!c) return YG_ERR_ARG;
+  return yg_ewald_join(c);
+}
+
 int yg_ewald_info(yg_ctx *c, int *tensor_path, int64_t *nk) {
   if (!c) return YG_ERR_ARG;
   if (tensor_path) *tensor_path = c->have_ewald ? c->ew_mma : 0;
@@ -472,7 +497,9 @@ int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nl
     c->have_list = 0;
     return rc;
   }
-  for (int p = 0; p < YG_NPART; p++) c->part_valid[p] = 0;
+  // a new list invalidates the pair parts only (the Ewald and valence parts
+  // do not use it; the reciprocal sum may already have been launched)
+  for (int p = 0; p < YG_MAX_POT; p++) c->part_valid[YG_PART_PAIR0 + p] = 0;
   if (nneigh) *nneigh = c->nneigh;
   return YG_OK;
 }
@@ -617,6 +644,10 @@ int yg_valence_compute(yg_ctx *c, int want_grad) {
 }
 
 int yg_get_part(yg_ctx *c, int part, double *energy, double *gpos, double *vtens) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || part < 0 || part >= YG_NPART) return YG_ERR_ARG;
   if (!c->part_valid[part]) {
     yg_set_error("part has no valid result for the current positions");
@@ -635,6 +666,10 @@ int yg_get_part(yg_ctx *c, int part, double *energy, double *gpos, double *vtens
 }
 
 int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens, double *part_energies) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c) return YG_ERR_ARG;
   for (int p = 0; p < YG_NPART; p++)
     if ((part_mask & (1 << p)) && !c->part_valid[p]) {
@@ -669,6 +704,10 @@ int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double 
 }
 
 int yg_sync(yg_ctx *c) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c) return YG_ERR_ARG;
   YG_CUDA(cudaStreamSynchronize(c->stream));
   return YG_OK;

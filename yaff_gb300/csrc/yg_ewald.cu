@@ -1414,8 +1414,9 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   // padding slots of the tiled weights stay zero
   YG_CUDA(cudaMemsetAsync(ctx->d_ew_W, 0, (size_t)ngroup * wstride * sizeof(CT), ctx->stream));
   const int eb = yg_blocks(nk_dense, 256);
-  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
-  double *partial = ctx->d_red + 64;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_red, &ctx->ew_red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double))))
+    return rc;
+  double *partial = ctx->d_ew_red + 64;
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
                                                 fac2, ngroup, ctx->d_ew_wslot, wstride, (CT *)ctx->d_ew_W,
@@ -1545,8 +1546,9 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   if ((rc = yg_ensure(ctx, &ctx->d_ew_wb, &ctx->ew_bytes_wb, (size_t)ngroup * wbstride * 4))) return rc;
   YG_CUDA(cudaMemsetAsync(ctx->d_ew_wb, 0, (size_t)ngroup * wbstride * 4, ctx->stream));
   const int eb = yg_blocks(nk_dense, 256);
-  if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double)))) return rc;
-  double *partial = ctx->d_red + 64;
+  if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_red, &ctx->ew_red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double))))
+    return rc;
+  double *partial = ctx->d_ew_red + 64;
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<float><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
                                                     fac2, ngroup, ctx->d_ew_wslot, 0, nullptr,
@@ -1618,6 +1620,8 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
 // Host-side k-space layout: prefactor grid in the reference's formula and
 // the list of 8x8 column tiles that intersect the half sphere.
 int yg_launch_ewald_setup(yg_ctx *ctx) {
+  int jrc;
+  if ((jrc = yg_ewald_join(ctx))) return jrc;
   const int G0 = (int)ctx->ew_gmax[0], G1 = (int)ctx->ew_gmax[1], G2 = (int)ctx->ew_gmax[2];
   if (G2 + 1 > EW_MAXM) {
     yg_set_error("Ewald gmax[2] too large (G2+1 must be <= 64)");
@@ -1741,7 +1745,38 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   return YG_OK;
 }
 
+int yg_ewald_join(yg_ctx *ctx) {
+  if (ctx->ew_pending) {
+    YG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ew_join_ev, 0));
+    ctx->ew_pending = 0;
+  }
+  return YG_OK;
+}
+
+static int launch_reci(yg_ctx *ctx, int want_grad);
+
+// The reciprocal sum depends only on the positions, the charges and the
+// k-space set-up, not on the neighbour list: it is forked onto the
+// context's auxiliary stream so that it overlaps the neighbour build and the
+// pair terms, and joined back by yg_ewald_join.
 int yg_launch_ewald_reci(yg_ctx *ctx, int want_grad) {
+  if (!ctx->ew_aux) {
+    YG_CUDA(cudaStreamCreateWithFlags(&ctx->ew_aux, cudaStreamNonBlocking));
+    YG_CUDA(cudaEventCreateWithFlags(&ctx->ew_fork_ev, cudaEventDisableTiming));
+    YG_CUDA(cudaEventCreateWithFlags(&ctx->ew_join_ev, cudaEventDisableTiming));
+  }
+  YG_CUDA(cudaEventRecord(ctx->ew_fork_ev, ctx->stream));
+  YG_CUDA(cudaStreamWaitEvent(ctx->ew_aux, ctx->ew_fork_ev, 0));
+  cudaStream_t own = ctx->stream;
+  ctx->stream = ctx->ew_aux;
+  const int rc = launch_reci(ctx, want_grad);
+  ctx->stream = own;
+  YG_CUDA(cudaEventRecord(ctx->ew_join_ev, ctx->ew_aux));
+  ctx->ew_pending = 1;
+  return rc;
+}
+
+static int launch_reci(yg_ctx *ctx, int want_grad) {
   if (ctx->ew_ntile == 0) {
     double *ev = ctx->d_part_ev + 10 * YG_PART_EWALD_RECI;
     YG_CUDA(cudaMemsetAsync(ev, 0, 10 * sizeof(double), ctx->stream));

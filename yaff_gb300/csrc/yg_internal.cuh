@@ -179,7 +179,14 @@ struct yg_ctx {
   double *d_ew_S = nullptr;       // 3 groups * ncol*nm complex (re, im)
   void *d_ew_W = nullptr;         // weights for the force pass, per group
   double *d_ew_gpart = nullptr;   // force partials
-  double *d_ew_red = nullptr;     // energy/virial partials
+  double *d_ew_red = nullptr;     // energy/virial partials of the reciprocal sum
+  size_t ew_red_cap = 0;
+  // the reciprocal sum runs on its own stream, forked from the context's
+  // stream at launch and joined back before its inputs change or its
+  // results are read
+  cudaStream_t ew_aux = nullptr;
+  cudaEvent_t ew_fork_ev = nullptr, ew_join_ev = nullptr;
+  int ew_pending = 0;
   size_t ew_bytes_tab = 0, ew_bytes_Spart = 0, ew_bytes_W = 0, ew_bytes_gpart = 0;
   // tensor-core (warp MMA) form of the mixed-precision reciprocal sum
   int ew_mma = 0;                 // 1 when the k-space layout suits it (G2 + 1 <= 32)
@@ -263,6 +270,9 @@ int yg_cuda_fail(cudaError_t err, const char *what);
 // device, so contexts on different streams run concurrently.
 // Grows a device buffer to at least `bytes` (contents are not preserved).
 int yg_ensure(yg_ctx *ctx, void **ptr, size_t *cap, size_t bytes);
+// Makes the context's stream wait for a reciprocal sum still running on its
+// auxiliary stream (no host synchronization).
+int yg_ewald_join(yg_ctx *ctx);
 int yg_alloc(yg_ctx *ctx, void **ptr, size_t bytes);
 // Releases a buffer (stream-ordered) and clears the pointer.
 void yg_free(yg_ctx *ctx, void **ptr);

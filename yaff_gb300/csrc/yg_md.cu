@@ -110,16 +110,17 @@ __global__ void k_set_int(int *__restrict__ p, int v) {
 // Force evaluation for the current device positions on the kept list,
 // summed on the device into d_total; no host synchronization.  prep = 0
 // when the cell-local coordinates are already current.
-static int md_force_async(yg_ctx *c, int prep) {
+static int md_force_async(yg_ctx *c, int prep, int reci_forked) {
   int rc;
   if (prep && (rc = yg_launch_prep_positions(c))) return rc;
+  if (!reci_forked && (c->md_mask & (1 << YG_PART_EWALD_RECI)) && (rc = yg_launch_ewald_reci(c, 1))) return rc;
   int pmask = 0;
   for (int p = 0; p < YG_MAX_POT; p++)
     if (c->pot[p].active && (c->md_mask & (1 << p))) pmask |= 1 << p;
   if (pmask && (rc = yg_launch_pair(c, pmask, 1))) return rc;
-  if ((c->md_mask & (1 << YG_PART_EWALD_RECI)) && (rc = yg_launch_ewald_reci(c, 1))) return rc;
   if ((c->md_mask & (1 << YG_PART_EWALD_CORR)) && (rc = yg_launch_ewald_corr(c, 1))) return rc;
   if ((c->md_mask & (1 << YG_PART_VALENCE)) && (rc = yg_launch_valence(c, 1))) return rc;
+  if ((rc = yg_ewald_join(c))) return rc;
   k_total_dev<<<yg_blocks(c->natom * 3, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom,
                                                                   c->md_mask, c->d_total);
   YG_LAUNCH_CHECK(c, "k_total_dev");
@@ -148,9 +149,14 @@ static int md_step_device(yg_ctx *c, double factor, double skin) {
   if ((rc = yg_launch_max_disp2_async(c, (unsigned long long *)(c->d_md_ctrl + 6)))) return rc;
   k_skin_gate<<<1, 32, 0, c->stream>>>(c->d_md_ctrl, factor, skin);
   YG_LAUNCH_CHECK(c, "k_skin_gate");
+  // the reciprocal sum needs only the new positions: it runs on the
+  // auxiliary stream while the list is rebuilt (when due) and the pair
+  // terms are evaluated
+  const int reci = (c->md_mask & (1 << YG_PART_EWALD_RECI)) != 0;
+  if (reci && (rc = yg_launch_ewald_reci(c, 1))) return rc;
   // the build sequence refreshes the cell-local coordinates in any case
   if ((rc = yg_launch_nlist_build_gated(c, c->d_md_ctrl, (unsigned long long *)(c->d_md_ctrl + 4)))) return rc;
-  if ((rc = md_force_async(c, 0))) return rc;
+  if ((rc = md_force_async(c, 0, reci))) return rc;
   return md_finish_step(c, c->md_dt);
 }
 
@@ -193,6 +199,10 @@ extern "C" {
 
 int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, int part_mask, double extra_energy,
                 int64_t max_steps) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || !masses || !vel || !(dt > 0.0) || max_steps < 1) return YG_ERR_ARG;
   if (!c->have_list) {
     yg_set_error("yg_md_setup: build the neighbour list first");
@@ -238,7 +248,7 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
   c->md_ready = 1;
   // step 0: forces and energies at the initial positions (yaff's initialize);
   // a kick with dt = 0 only evaluates the kinetic energy
-  if ((rc = md_force_async(c, 1))) return rc;
+  if ((rc = md_force_async(c, 1, 0))) return rc;
   return md_finish_step(c, 0.0);
 }
 
@@ -248,6 +258,10 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
 // and again whenever the neighbour slots were reallocated), then reads the
 // status words once.  skin <= 0 rebuilds every step.
 int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nrebuild) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || nsteps < 0) return YG_ERR_ARG;
   if (!c->md_ready) {
     yg_set_error("yg_md_run: call yg_md_setup first");
@@ -336,6 +350,10 @@ int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nr
 // Copies positions, velocities (natom x 3, may be NULL) and the energy log
 // ((steps done + 1) x (epot, ekin), may be NULL) to host memory.
 int yg_md_get(yg_ctx *c, double *pos, double *vel, double *log, int64_t *nlog) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
   if (!c || !c->md_ready) return YG_ERR_STATE;
   if (pos) YG_CUDA(cudaMemcpyAsync(pos, c->d_pos, c->natom * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (vel) YG_CUDA(cudaMemcpyAsync(vel, c->d_vel, c->natom * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -173,14 +173,19 @@ class ForceField(ForcePart):
                 self.nlist.update()
                 self.needs_nlist_update = False
             return sum([part.compute(gpos, vtens) for part in self.parts])
-        # fused device path
-        if self.needs_nlist_update:
-            self.nlist.update(upload=True)
-            self.needs_nlist_update = False
-        else:
-            dev.upload_positions()
+        # fused device path: positions first, then the reciprocal sum (it
+        # needs no neighbour list and runs on its own stream while the list
+        # is updated and the pair terms are evaluated)
+        dev.upload_positions()
         want_grad = (gpos is not None) or (vtens is not None)
         mask = 0
+        for part in self.parts:
+            if isinstance(part, ForcePartEwaldReciprocal):
+                part._launch(want_grad)
+                mask |= 1 << part.device_slot
+        if self.needs_nlist_update:
+            self.nlist.update(upload=False)
+            self.needs_nlist_update = False
         pair_parts = [p for p in self.parts if isinstance(p, ForcePartPair)]
         if pair_parts:
             slots = [p._register() for p in pair_parts]
@@ -192,9 +197,7 @@ class ForceField(ForcePart):
         host_energy = 0.0
         host_vtens = np.zeros((3, 3)) if vtens is not None else None
         for part in self.parts:
-            if isinstance(part, ForcePartPair):
-                continue
-            if isinstance(part, ForcePartEwaldNeutralizing):
+            if isinstance(part, (ForcePartPair, ForcePartEwaldNeutralizing, ForcePartEwaldReciprocal)):
                 continue
             part._launch(want_grad)
             mask |= 1 << part.device_slot

@@ -73,8 +73,12 @@ class NeighborList(object):
         """Rebuild or recompute the list for the current system positions."""
         assert self.rcut > 0
         dev = self.device
-        if dev.sync_cell():
+        dev.sync_cell()
+        if getattr(self, '_rmax_cell_key', None) != dev._cell_key:
+            # the cell changed since rmax was last derived (the change may
+            # have been synchronised to the device by another part)
             self.update_rmax()
+            self._rmax_cell_key = dev._cell_key
         if upload:
             dev.upload_positions()
         self._neighs_cache = None
