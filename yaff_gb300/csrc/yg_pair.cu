@@ -211,8 +211,11 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
 #pragma unroll
         for (int k = 0; k < 4; k++) fpi[p][k] = (float)pi[p][k];
       const float fxi = (float)xi, fyi = (float)yi, fzi = (float)zi, fqi = (float)qi;
+      // the next entry of the lane is loaded one step ahead
+      uint2 ent_next = lane < cnt ? row[lane] : make_uint2(0u, 0u);
       for (int e = lane; e < cnt; e += 32) {
-        const uint2 ent = row[e];
+        const uint2 ent = ent_next;
+        if (e + 32 < cnt) ent_next = row[e + 32];
         const int j = (int)ent.x;
         const int oidx = (int)(ent.y & YG_META_OFF_MASK);
         const int code = (int)((ent.y >> YG_META_SCALE_SHIFT) & 7u);
