@@ -193,6 +193,12 @@ int yg_get_part(yg_ctx *ctx, int part, double *energy, double *gpos, double *vte
 int yg_get_total(yg_ctx *ctx, int part_mask, double *energy, double *gpos,
                  double *vtens, double *part_energies);
 
+/* As yg_get_total, but the summed gradient and virial are ADDED to gpos and
+ * vtens (yaff's ForcePart.compute convention, ff.py:117-168) straight from
+ * the page-locked readback block, without an intermediate copy. */
+int yg_get_total_add(yg_ctx *ctx, int part_mask, double *energy, double *gpos,
+                     double *vtens, double *part_energies);
+
 /* Waits for all work queued on the context's stream. */
 int yg_sync(yg_ctx *ctx);
 

@@ -69,6 +69,7 @@ SIGNATURES = {
     'yg_valence_compute': (_I, [_P, _I]),
     'yg_get_part': (_I, [_P, _I, _P, _P, _P]),
     'yg_get_total': (_I, [_P, _I, _P, _P, _P, _P]),
+    'yg_get_total_add': (_I, [_P, _I, _P, _P, _P, _P]),
     'yg_sync': (_I, [_P]),
     'yg_launch_count': (_I64, [_P]),
     'yg_mem_usage': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

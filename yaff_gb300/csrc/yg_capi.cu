@@ -665,7 +665,22 @@ int yg_get_part(yg_ctx *c, int part, double *energy, double *gpos, double *vtens
   return YG_OK;
 }
 
+static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens, double *part_energies,
+                     int add);
+
 int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens, double *part_energies) {
+  return get_total(c, part_mask, energy, gpos, vtens, part_energies, 0);
+}
+
+int yg_get_total_add(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens,
+                     double *part_energies) {
+  return get_total(c, part_mask, energy, gpos, vtens, part_energies, 1);
+}
+
+// The summed parts: written into (add = 0) or added to (add = 1) the
+// caller's gpos / vtens, straight from the page-locked readback block.
+static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double *vtens, double *part_energies,
+                     int add) {
   if (c) {
     const int jrc = yg_ewald_join(c);
     if (jrc) return jrc;
@@ -692,13 +707,22 @@ int yg_get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, double 
     return YG_ERR_CUDA;
   }
   if (energy) *energy = c->h_total[0];
-  if (vtens) memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
   if (part_energies) memcpy(part_energies, c->h_total + 10, YG_NPART * sizeof(double));
-  if (gpos) memcpy(gpos, c->h_total + 16, n3 * sizeof(double));
   if (std::isnan(c->h_total[0])) return YG_ERR_NAN;
   if (want_gpos && c->h_status[YG_ST_NANGRAD]) {
     yg_set_error("not-a-number in the gradient");
     return YG_ERR_NAN;
+  }
+  if (add) {
+    if (vtens)
+      for (int k = 0; k < 9; k++) vtens[k] += c->h_total[1 + k];
+    if (gpos) {
+      const double *src = c->h_total + 16;
+      for (int64_t k = 0; k < n3; k++) gpos[k] += src[k];
+    }
+  } else {
+    if (vtens) memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
+    if (gpos) memcpy(gpos, c->h_total + 16, n3 * sizeof(double));
   }
   return YG_OK;
 }

@@ -198,6 +198,27 @@ class DeviceSystem(object):
             vtens[:] = v.reshape(3, 3)
         return e.value, parts.copy()
 
+    def get_total_add(self, mask, gpos=None, vtens=None):
+        """(energy, part energies); the summed gradient is ADDED to gpos and
+        the virial to vtens (float64 C-contiguous arrays are added to in
+        place by the library), each skipped when None.  Raises ValueError on
+        NaN energy or gradient."""
+        e = ctypes.c_double()
+        parts = self._parts_buf
+        g = gpos
+        if g is not None and not (g.flags['C_CONTIGUOUS'] and g.dtype == np.float64):
+            g = np.zeros((self.natom, 3))
+        v = vtens
+        if v is not None and not (v.flags['C_CONTIGUOUS'] and v.dtype == np.float64):
+            v = np.zeros((3, 3))
+        check(self.lib.yg_get_total_add(self.ctx, mask, ctypes.byref(e), ptr(g), ptr(v), ptr(parts)),
+              'yg_get_total')
+        if gpos is not None and g is not gpos:
+            gpos += g
+        if vtens is not None and v is not vtens:
+            vtens += v
+        return e.value, parts.copy()
+
     def launch_count(self):
         return int(self.lib.yg_launch_count(self.ctx))
 

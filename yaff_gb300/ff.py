@@ -124,6 +124,8 @@ class ForceField(ForcePart):
 
     def __init__(self, system, parts, nlist=None):
         ForcePart.__init__(self, 'all', system)
+        self._host_vtens = None
+        self._total_mask = 0
         self.system = system
         self.parts = []
         self.nlist = nlist
@@ -166,7 +168,7 @@ class ForceField(ForcePart):
         dev = device_of(self.system)
         return dev
 
-    def _internal_compute(self, gpos, vtens):
+    def _internal_compute(self, gpos, vtens, add=False):
         dev = self._device_parts()
         if dev is None:
             if self.needs_nlist_update:
@@ -201,9 +203,14 @@ class ForceField(ForcePart):
                 continue
             part._launch(want_grad)
             mask |= 1 << part.device_slot
-        # the summed gradient and virial land directly in the caller's arrays;
-        # NaN in the gradient is detected on the device
-        energy, part_e = dev.get_total_into(mask, gpos, vtens)
+        # the summed gradient and virial land directly in the caller's arrays
+        # (added to them with add=True); NaN in the gradient is detected on
+        # the device
+        if add:
+            energy, part_e = dev.get_total_add(mask, gpos, vtens)
+        else:
+            energy, part_e = dev.get_total_into(mask, gpos, vtens)
+        self._total_mask = mask
         for part in self.parts:
             if isinstance(part, ForcePartEwaldNeutralizing):
                 # position independent, no gradient (ff.py:653-669)
@@ -224,28 +231,39 @@ class ForceField(ForcePart):
         energy += host_energy
         if vtens is not None:
             vtens += host_vtens
+        self._host_vtens = host_vtens
         return energy
 
     def compute(self, gpos=None, vtens=None):
         """Energy; the gradient and virial are ADDED to gpos / vtens.  On the
-        fused device path the result is written once into the force field's
-        own buffers and added to the caller's (no extra passes over gpos)."""
+        fused device path they are added to the caller's arrays straight from
+        the library's page-locked readback (one pass over gpos); the force
+        field's own `gpos` / `vtens` are fetched from the device on access."""
         if self._device_parts() is None:
             return ForcePart.compute(self, gpos, vtens)
         self._lazy = None
         self._stale = False
-        my_gpos = self._gpos if gpos is not None else None
-        my_vtens = self._vtens if vtens is not None else None
-        self.energy = self._internal_compute(my_gpos, my_vtens)
+        self.energy = self._internal_compute(gpos, vtens, add=True)
         if np.isnan(self.energy):
             raise ValueError('The energy is not-a-number (nan).')
-        if gpos is not None:
-            gpos += my_gpos
-        if vtens is not None:
-            if np.isnan(my_vtens).any():
-                raise ValueError('Some vtens element(s) is/are not-a-number (nan).')
-            vtens += my_vtens
+        if vtens is not None and np.isnan(vtens).any():
+            raise ValueError('Some vtens element(s) is/are not-a-number (nan).')
+        self._lazy = ('total', self._device_parts(), self._total_mask, gpos is not None, vtens is not None)
         return self.energy
+
+    def _fetch(self):
+        if self._lazy is not None and self._lazy[0] == 'total':
+            _, dev, mask, want_g, want_v = self._lazy
+            self._lazy = None
+            dev.get_total_into(mask, self._gpos if want_g else None, self._vtens if want_v else None)
+            if want_v and self._host_vtens is not None:
+                self._vtens += self._host_vtens
+            if not want_g:
+                self._gpos[:] = np.nan
+            if not want_v:
+                self._vtens[:] = np.nan
+            return
+        ForcePart._fetch(self)
 
     def device_md_terms(self):
         """(result-slot mask, constant energy) for an integrator that sums the
