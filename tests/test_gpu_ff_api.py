@@ -28,7 +28,9 @@ def test_compute_adds_into_caller_arrays_and_keeps_totals():
     assert np.allclose(g1, base_g + g0, rtol=0, atol=1e-12 * np.abs(g0).max())
     assert np.allclose(v1, base_v + v0, rtol=0, atol=1e-12 * np.abs(v0).max())
     assert np.array_equal(ff.gpos, g0)
-    # energy only: no arrays touched, the totals read as not computed
+    # energy only: no arrays touched, the force field keeps the previous
+    # gradient and virial (as yaff's ForcePart does)
     e2 = ff.compute()
     assert e2 == e0
-    assert np.isnan(ff.gpos).all()
+    assert np.array_equal(ff.gpos, g0)
+    assert np.array_equal(ff.vtens, v0)

@@ -241,6 +241,10 @@ class ForceField(ForcePart):
         field's own `gpos` / `vtens` are fetched from the device on access."""
         if self._device_parts() is None:
             return ForcePart.compute(self, gpos, vtens)
+        if (gpos is None or vtens is None) and self._lazy is not None:
+            # yaff keeps the previous gpos / vtens when this call does not
+            # compute them: take them from the device before they are replaced
+            self._fetch()
         self._lazy = None
         self._stale = False
         self.energy = self._internal_compute(gpos, vtens, add=True)
@@ -258,10 +262,6 @@ class ForceField(ForcePart):
             dev.get_total_into(mask, self._gpos if want_g else None, self._vtens if want_v else None)
             if want_v and self._host_vtens is not None:
                 self._vtens += self._host_vtens
-            if not want_g:
-                self._gpos[:] = np.nan
-            if not want_v:
-                self._vtens[:] = np.nan
             return
         ForcePart._fetch(self)
 
