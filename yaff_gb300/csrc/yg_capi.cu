@@ -248,7 +248,7 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_pos, (void **)&c->d_pos_build, (void **)&c->d_charge, (void **)&c->d_cell_of,
       (void **)&c->d_wimg, (void **)&c->d_sorted, (void **)&c->d_rank, (void **)&c->d_cell_start,
       (void **)&c->d_cell_fill, (void **)&c->d_org, (void **)&c->d_x64, (void **)&c->d_x32, (void **)&c->d_xb,
-      (void **)&c->d_shift64, (void **)&c->d_shift32, (void **)&c->d_rows, (void **)&c->d_nbr, (void **)&c->d_ncount,
+      (void **)&c->d_shift64, (void **)&c->d_shift32, (void **)&c->d_cfrac, (void **)&c->d_rows, (void **)&c->d_nbr, (void **)&c->d_ncount,
       (void **)&c->d_status, (void **)&c->d_excl_start, (void **)&c->d_excl, (void **)&c->d_stab_ab,
       (void **)&c->d_stab_scale, (void **)&c->d_pp_src, (void **)&c->d_pp64, (void **)&c->d_pp32,
       (void **)&c->d_ew_pref, (void **)&c->d_ew_tiles, (void **)&c->d_ew_tab, (void **)&c->d_ew_Spart,

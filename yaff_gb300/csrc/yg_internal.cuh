@@ -121,6 +121,7 @@ struct yg_ctx {
   double *d_shift64 = nullptr;    // noff*3 stencil shift vectors
   float4 *d_shift32 = nullptr;    // noff
   size_t shift64_cap = 0, shift32_cap = 0;
+  double *d_cfrac = nullptr;      // 3 x 512: c / n_k of every grid index (IEEE division, on the host)
   int cap_sorted = 0;             // allocated cell-list capacity (cells)
   GridGeom grid{};
   int have_list = 0;

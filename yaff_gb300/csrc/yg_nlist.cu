@@ -166,7 +166,7 @@ __global__ void k_sort_cells(const int *__restrict__ gate, const int *__restrict
 // Cell origin (FP64) of every sorted atom and the orig -> sorted map.
 __global__ void k_origins(const int *__restrict__ gate, const int *__restrict__ sorted, const int *__restrict__ cell_of,
                           const int *__restrict__ wimg, int64_t natom, CellGeom cell, GridGeom grid,
-                          double *__restrict__ org, int *__restrict__ rank) {
+                          const double *__restrict__ cfrac, double *__restrict__ org, int *__restrict__ rank) {
   if (gate && !*gate) return;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= natom) return;
@@ -174,8 +174,9 @@ __global__ void k_origins(const int *__restrict__ gate, const int *__restrict__ 
   int id = cell_of[a];
   int c[3] = {id % grid.n[0], (id / grid.n[0]) % grid.n[1], id / (grid.n[0] * grid.n[1])};
   double f[3];
+  // c / n from the host table (the same IEEE quotient, without FP64 divisions here)
 #pragma unroll
-  for (int k = 0; k < 3; k++) f[k] = (double)wimg[3 * a + k] + (double)c[k] / (double)grid.n[k];
+  for (int k = 0; k < 3; k++) f[k] = (double)wimg[3 * a + k] + cfrac[512 * k + c[k]];
 #pragma unroll
   for (int x = 0; x < 3; x++)
     org[3 * s + x] = f[0] * cell.rv[x] + f[1] * cell.rv[3 + x] + f[2] * cell.rv[6 + x];
@@ -622,14 +623,14 @@ __global__ void k_max_disp2(const double *__restrict__ pos, const double *__rest
 __global__ void k_pack_params(const int *__restrict__ gate, const double *__restrict__ src, const int *__restrict__ sorted, int64_t natom,
                               double *__restrict__ dst64, float *__restrict__ dst32) {
   if (gate && !*gate) return;
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= natom) return;
-  int a = sorted[s];
-  for (int v = 0; v < 4 * YG_MAX_POT; v++) {
-    double x = src[(int64_t)a * 4 * YG_MAX_POT + v];
-    dst64[s * 4 * YG_MAX_POT + v] = x;
-    dst32[s * 4 * YG_MAX_POT + v] = (float)x;
-  }
+  // one thread per (sorted atom, value): coalesced stores
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= natom * 4 * YG_MAX_POT) return;
+  const int64_t s = idx / (4 * YG_MAX_POT);
+  const int v = (int)(idx - s * (4 * YG_MAX_POT));
+  const double x = src[(int64_t)sorted[s] * 4 * YG_MAX_POT + v];
+  dst64[idx] = x;
+  dst32[idx] = (float)x;
 }
 
 BuildArgs make_args(yg_ctx *ctx, double rc2) {
@@ -695,7 +696,7 @@ int yg_pack_pair_params(yg_ctx *ctx) {
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->pp_dirty = 0;
   }
-  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(nullptr, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
+  k_pack_params<<<yg_blocks(ctx->natom * 4 * YG_MAX_POT, 256), 256, 0, ctx->stream>>>(nullptr, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
                                                                      ctx->d_pp64, ctx->d_pp32);
   YG_LAUNCH_CHECK(ctx, "k_pack_params");
   ctx->pp_packed = 1;
@@ -852,6 +853,13 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
   if ((rc_ = yg_ensure(ctx, (void **)&ctx->d_shift32, &ctx->shift32_cap, sh32.size() * sizeof(float4)))) return rc_;
   YG_CUDA(cudaMemcpyAsync(ctx->d_shift64, sh64.data(), sh64.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_shift32, sh32.data(), sh32.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  // c / n_k for every grid index (n_k <= 512)
+  std::vector<double> cfrac(3 * 512, 0.0);
+  for (int k = 0; k < 3; k++)
+    for (int c = 0; c < G.n[k]; c++) cfrac[512 * k + c] = (double)c / (double)G.n[k];
+  if (!ctx->d_cfrac && (rc_ = yg_alloc(ctx, (void **)&ctx->d_cfrac, cfrac.size() * sizeof(double)))) return rc_;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_cfrac, cfrac.data(), cfrac.size() * sizeof(double), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
 
   // FP32 guard band: bound on |d2_fp32 - d2_exact| from the magnitudes of the
@@ -925,7 +933,7 @@ static int enqueue_build(yg_ctx *ctx, double rc2, const int *gate, unsigned long
                                                                                 ctx->d_sorted);
   YG_LAUNCH_CHECK(ctx, "k_sort_cells");
   k_origins<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(gate, ctx->d_sorted, ctx->d_cell_of, ctx->d_wimg, N, C, G,
-                                                        ctx->d_org, ctx->d_rank);
+                                                        ctx->d_cfrac, ctx->d_org, ctx->d_rank);
   YG_LAUNCH_CHECK(ctx, "k_origins");
   int rc_;
   if ((rc_ = yg_launch_prep_positions(ctx))) return rc_;
@@ -1001,7 +1009,7 @@ int yg_launch_nlist_build_gated(yg_ctx *ctx, const int *gate, unsigned long long
   }
   const double rc2 = ctx->rcut_total * ctx->rcut_total;
   if ((rc_ = enqueue_build(ctx, rc2, gate, total))) return rc_;
-  k_pack_params<<<yg_blocks(ctx->natom, 256), 256, 0, ctx->stream>>>(gate, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
+  k_pack_params<<<yg_blocks(ctx->natom * 4 * YG_MAX_POT, 256), 256, 0, ctx->stream>>>(gate, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
                                                                      ctx->d_pp64, ctx->d_pp32);
   YG_LAUNCH_CHECK(ctx, "k_pack_params");
   return YG_OK;
