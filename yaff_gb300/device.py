@@ -110,12 +110,14 @@ class DeviceSystem(object):
         return True
 
     def sync_charges(self):
-        q = np.ascontiguousarray(self.system.charges, dtype=np.float64)
-        key = q.tobytes()
-        if key == self._charges_key:
+        """Uploads the system's charges when they differ from the last upload
+        (an element-wise comparison: charges may be changed in place)."""
+        q = self.system.charges
+        if self._charges_key is not None and q.shape == self._charges_key.shape and np.array_equal(q, self._charges_key):
             return
+        q = np.ascontiguousarray(q, dtype=np.float64)
         check(self.lib.yg_set_charges(self.ctx, ptr(q)), 'yg_set_charges')
-        self._charges_key = key
+        self._charges_key = q.copy()
 
     def upload_positions(self, pos=None):
         """Copies the current positions (host array) to the device."""
