@@ -1160,7 +1160,10 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
 // contiguous bytes.  The epilogue forms P = E0 E1 per (atom, column) and
 // accumulates g0 Im(P Z), g1 Im(P Z), Im(P Z2).  With one range the sums go
 // to gfrac; with several to out[r][atom][3] for k_ewald_force_mma_combine.
-__global__ void __launch_bounds__(256) k_ewald_force_mma(const float2 *__restrict__ te, const uint2 *__restrict__ yf,
+#ifndef YG_FM_MINB
+#define YG_FM_MINB 2  // resident tensor-core force-pass blocks per SM the register budget is sized for
+#endif
+__global__ void __launch_bounds__(256, YG_FM_MINB) k_ewald_force_mma(const float2 *__restrict__ te, const uint2 *__restrict__ yf,
                                                          int a0, int a1, int G0, int lep, int nmf, int nks,
                                                          const int4 *__restrict__ cols, const int *__restrict__ crange,
                                                          const int *__restrict__ woff, const uint4 *__restrict__ wb,
