@@ -146,7 +146,7 @@ def run_gb300(args, world, rank, local):
     torch.cuda.set_device(local)
     import yaff_gb300
     from yaff_gb300 import configs, _lib
-    spec = configs.triclinic_mm3_ei(natom=args.natom) if args.natom != 50000 else configs.cfg2()
+    spec = configs.triclinic_mm3_ei(natom=args.natom) if args.natom != 50000 else configs.triclinic_50000()
     natom = len(spec['pos'])
     rng = np.random.default_rng(7 + rank)
     ff = yaff_gb300.build_forcefield(spec, precision=args.precision)
@@ -372,7 +372,7 @@ def run_gb300(args, world, rank, local):
         'vs_baseline': None, 'dtype': {'mixed': 'fp32-terms/fp64-accum', 'fp64': 'f64',
                                         'mixed_kahan': 'fp32-kahan'}[args.precision],
         'data': 'synthetic (seeded random sequential insertion)',
-        'config': {'workload': 'cfg2: 50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
+        'config': {'workload': '50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
                                'rebuild every step', 'natom': natom, 'precision': args.precision,
                    'nneigh': int(ff.nlist.nneigh), 'nk': int(nk), 'l2': 'flushed (256 MB write) between steps',
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
@@ -416,7 +416,7 @@ def cpu_sample(natom, seconds_budget=20.0):
     sys.path.insert(0, os.path.join(REPO, 'oracle'))
     import oracle
     from yaff_gb300 import configs
-    spec = configs.cfg2() if natom == 50000 else configs.triclinic_mm3_ei(natom=natom)
+    spec = configs.triclinic_50000() if natom == 50000 else configs.triclinic_mm3_ei(natom=natom)
     N = len(spec['pos'])
     L = oracle.lib()
     cell = oracle.OracleCell(spec['rvecs'])
@@ -560,7 +560,7 @@ def run_reference(args, world, rank):
             'warmup': args.warmup, 'ms_per_step': 1e3 / val, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded random sequential insertion)',
             'impl': 'reference',
-            'config': {'workload': 'cfg2: 50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
+            'config': {'workload': '50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
                                    'rebuild every step', 'natom': args.natom, 'parallelism': '%d independent '
                                    'single-thread replicas' % cores},
             'cpu_baseline': {'value': val, 'unit': 'evals/s', 'cores': cores, 'kind': 'port',
@@ -612,7 +612,7 @@ def run_nve(args):
     from yaff_gb300 import configs
     from yaff_gb300.units import femtosecond
     from yaff_gb300.verlet import DeviceVerlet, ConsErrTracker, drift_per_ps
-    spec = configs.cfg1()
+    spec = configs.water_24000()
     natom = len(spec['pos'])
     ff = yaff_gb300.build_forcefield(spec, precision='mixed')
     dt = 0.5 * femtosecond

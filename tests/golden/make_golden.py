@@ -192,8 +192,8 @@ def main():
     mc['nhigh'] = 100
     run_case('lat216split', mc)
 
-    big = configs.lattice_lj_ei(name='cfg0')
-    run_case('cfg0', big, full_rows=False)
+    big = configs.lattice_lj_ei(name='lattice1000')
+    run_case('lattice1000', big, full_rows=False)
 
     t2 = configs.triclinic_mm3_ei(natom=2000, name='tric2000')
     run_case('tric2000', t2, full_rows=False)

@@ -118,7 +118,7 @@ def test_apply_updates_like_recompute():
     assert _rel(e, np.array([ref])).max() <= 1e-9
 
 
-def test_cfg4_sized_trials_mixed_vs_fp64_and_oracle():
+def test_framework2000_trials_mixed_vs_fp64_and_oracle():
     """The 2,000-atom framework with a loaded chain: 64 mixed trials within
     1e-6 of the FP64 ones; a few FP64 trials against the oracle."""
     import mc_oracle

@@ -3,8 +3,8 @@
 Pair set: (a, b, r0, r1, r2) identical to the reference (SHA-256 of the
 sorted keys), and on build steps d, dx, dy, dz bit-identical too.
 Energies: FP64 within 1e-10 relative, mixed within 1e-6 relative; gradients
-and virials: FP64 within 1e-9, mixed within 1e-5 relative RMS (the tolerance
-of the spec parity bar).  Energies are compared relative to the largest
+and virials: FP64 within 1e-9, mixed within 1e-5 relative RMS (the parity
+tolerances of this path).  Energies are compared relative to the largest
 part magnitude of the case, since the total can be a near-cancelling sum.
 """
 import hashlib

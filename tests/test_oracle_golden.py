@@ -42,6 +42,6 @@ def test_oracle_matches_reference(name):
 
 
 def test_fixture_set_complete():
-    for want in ('lat216', 'water64', 'tric600', 'tric100img', 'water32', 'quartz', 'lat216split', 'cfg0',
+    for want in ('lat216', 'water64', 'tric600', 'tric100img', 'water32', 'quartz', 'lat216split', 'lattice1000',
                  'tric2000'):
         assert want in CASES

@@ -281,19 +281,19 @@ def triclinic_mm3_ei(natom=50000, density=50000 / 5.0313e5, angle=75.0, dmin=1.8
     return spec
 
 
-def cfg0():
+def lattice_1000():
     """1,000-atom LJ + EI + Ewald lattice (plain FP64 parity workload)."""
-    return lattice_lj_ei(name='cfg0')
+    return lattice_lj_ei(name='lattice1000')
 
 
-def cfg1():
-    """8,000-molecule flexible water NVE workload."""
-    return flexible_water(name='cfg1')
+def water_24000():
+    """8,000-molecule (24,000-atom) flexible water NVE workload."""
+    return flexible_water(name='water24000')
 
 
-def cfg2():
+def triclinic_50000():
     """50,000-atom triclinic MM3 + EI + Ewald workload (the headline)."""
-    return triclinic_mm3_ei(name='cfg2')
+    return triclinic_mm3_ei(name='triclinic50000')
 
 
 def serving_request(natom, seed, rcut=10.0, density=0.064):
