@@ -168,14 +168,16 @@ int yg_ewald_reci(yg_ctx *ctx, int want_grad);
  * compute_ewald_corr (yaff/pes/ewald.c:278-349). */
 int yg_ewald_corr(yg_ctx *ctx, int want_grad);
 
-/* Valence tables: relative vectors (i, j), internal coordinates (kind, delta
- * rows and signs, kinds 0 bond, 1 bend cos, 2 bend angle, 5 Urey-Bradley) and
- * harmonic terms (K, q0, ic).  Replaces the DeltaList / InternalCoordinateList
- * / ValenceList tables (yaff/pes/dlist.py:62-118, iclist.py:77-120,
- * vlist.py:74-110). */
+/* Valence tables: relative vectors (i, j), internal coordinates (9 int64 per
+ * row: kind 0..17, then delta row and sign for up to four deltas, as
+ * iclist_row_type of yaff/pes/iclist.h:30-38) and energy terms (kind 0..15,
+ * six parameters, two coordinate rows with -1 when unused, as vlist_row_type
+ * of yaff/pes/vlist.h:30-37).  Replaces the DeltaList /
+ * InternalCoordinateList / ValenceList tables (yaff/pes/dlist.py:62-118,
+ * iclist.py:77-120, vlist.py:74-110). */
 int yg_set_valence(yg_ctx *ctx, const int64_t *delta_ij, int64_t ndelta,
-                   const int64_t *ic_rows, int64_t nic, const double *vterm_pars,
-                   const int64_t *vterm_ic, int64_t nterm);
+                   const int64_t *ic_rows, int64_t nic, const int64_t *vterm_kind,
+                   const double *vterm_pars, const int64_t *vterm_ic, int64_t nterm);
 
 /* Forward and back propagation of the valence chain.  Replaces dlist_forward
  * / iclist_forward / vlist_forward and vlist_back / iclist_back / dlist_back

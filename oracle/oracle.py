@@ -172,6 +172,33 @@ def build_scalings(natom, bonds, scalings):
     return np.array(rows, dtype=scaling_dtype)
 
 
+# Relative vectors (i -> j) each internal-coordinate kind reads, from its
+# atoms; yaff/pes/iclist.py:231-530.
+IC_DELTAS = {
+    0: lambda i, j: [(i, j)],
+    1: lambda i, j, k: [(j, i), (j, k)],
+    2: lambda i, j, k: [(j, i), (j, k)],
+    3: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    4: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    5: lambda i, j, k: [(i, k)],
+    6: lambda i, j, k, l: [(i, l), (j, l), (k, l)],
+    7: lambda i, j, k, l: [(i, l), (j, l), (k, l)],
+    8: lambda i, j, k, l: [(i, l), (j, l), (k, l)],
+    9: lambda i, j, k, l: [(i, l), (j, l), (k, l)],
+    10: lambda i, j, k, l: [(i, j), (j, k), (k, l)],
+    11: lambda i, j, k, l: [(i, j), (j, k), (k, l)],
+    12: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    13: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    14: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    15: lambda i, j, k, l: [(j, i), (j, k), (k, l)],
+    16: lambda i, j, k: [(i, k), (j, k), (i, j)],
+    17: lambda i, j, k: [(i, k), (j, k), (i, j)],
+}
+
+# Parameters each energy-term kind stores; yaff/pes/vlist.py:179-700.
+TERM_NPARS = {0: 2, 1: 4, 2: 2, 3: 3, 4: 3, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 6, 11: 2, 12: 2, 13: 3, 14: 3, 15: 6}
+
+
 class OracleForceField(object):
     """Reference-order FP64 evaluation of a configs.py spec on the CPU."""
 
@@ -246,7 +273,8 @@ class OracleForceField(object):
         spec = self.spec
         bt = spec.get('bond_terms')
         at = spec.get('bend_terms')
-        self.has_valence = (bt is not None and len(bt)) or (at is not None and len(at))
+        vr = spec.get('valence')
+        self.has_valence = any(x is not None and len(x) for x in (bt, at, vr))
         if not self.has_valence:
             return
         deltas = []
@@ -280,11 +308,23 @@ class OracleForceField(object):
                 ics.append(rec)
             return row
 
-        terms = []
+        terms = []   # (term kind, pars, ic0, ic1)
         for i, j, K, r0 in (bt if bt is not None else []):
-            terms.append((0, K, r0, add_ic(0, [(int(i), int(j))])))
+            terms.append((0, [K, r0], add_ic(0, [(int(i), int(j))]), -1))
         for i, j, k, K, t0 in (at if at is not None else []):
-            terms.append((0, K, t0, add_ic(2, [(int(j), int(i)), (int(j), int(k))])))
+            terms.append((0, [K, t0], add_ic(2, [(int(j), int(i)), (int(j), int(k))]), -1))
+        for row in (vr if vr is not None else []):
+            kind = int(row[0])
+            term_ics = []
+            for c in (7, 12):
+                if row[c] >= 0:
+                    ick = int(row[c])
+                    atoms = [int(x) for x in row[c + 1:c + 5] if x >= 0]
+                    term_ics.append(add_ic(ick, IC_DELTAS[ick](*atoms)))
+            pars = list(row[1:1 + TERM_NPARS[kind]])
+            if kind in (1, 10):   # PolyFour / PolySix pad their coefficients with zeros
+                pars += [0.0] * ((4 if kind == 1 else 6) - len(pars))
+            terms.append((kind, pars, term_ics[0], term_ics[1] if len(term_ics) > 1 else -1))
         self.dl = np.zeros(len(deltas), delta_dtype)
         for r, (i, j) in enumerate(deltas):
             self.dl[r]['i'] = i
@@ -293,8 +333,9 @@ class OracleForceField(object):
         for r, rec in enumerate(ics):
             self.ic[r] = tuple(rec) + (np.nan, np.nan)
         self.vt = np.zeros(len(terms), vlist_dtype)
-        for r, (kind, K, q0, ic0) in enumerate(terms):
-            self.vt[r] = (kind, K, q0, -1, -1, -1, -1, ic0, -1, np.nan)
+        for r, (kind, pars, ic0, ic1) in enumerate(terms):
+            p = [float(x) for x in pars] + [-1.0] * (6 - len(pars))
+            self.vt[r] = (kind, p[0], p[1], p[2], p[3], p[4], p[5], ic0, ic1, np.nan)
 
     def compute_valence(self, gpos, vtens):
         L = lib()

@@ -62,11 +62,22 @@ def build_reference_ff(spec):
         parts.append(ForcePartEwaldNeutralizing(system, ew['alpha'], diel, nlow, nhigh))
     bt = spec.get('bond_terms')
     at = spec.get('bend_terms')
-    if (bt is not None and len(bt)) or (at is not None and len(at)):
+    vr = spec.get('valence')
+    if any(x is not None and len(x) for x in (bt, at, vr)):
         pv = ForcePartValence(system)
-        for i, j, K, r0 in bt:
+        for i, j, K, r0 in (bt if bt is not None else []):
             pv.add_term(Harmonic(K, r0, Bond(int(i), int(j))))
-        for i, j, k, K, t0 in at:
+        for i, j, k, K, t0 in (at if at is not None else []):
             pv.add_term(Harmonic(K, t0, BendAngle(int(i), int(j), int(k))))
+        if vr is not None and len(vr):
+            from yaff_gb300.valence import terms_from_rows
+            import yaff.pes.iclist as ric
+            import yaff.pes.vlist as rvl
+            icc = {c.kind: c for c in vars(ric).values()
+                   if isinstance(c, type) and issubclass(c, ric.InternalCoordinate) and c.kind is not None}
+            tcc = {c.kind: c for c in vars(rvl).values()
+                   if isinstance(c, type) and issubclass(c, rvl.ValenceTerm) and c.kind is not None}
+            for term in terms_from_rows(vr, icc, tcc):
+                pv.add_term(term)
         parts.append(pv)
     return ForceField(system, parts, nlist)

@@ -663,103 +663,538 @@ void orc_dlist_back(double *gpos, double *vtens, const orc_delta *dl, int64_t n)
   }
 }
 
+/* Internal coordinates and valence terms.  Every kind of the reference's
+ * tables is restated here: iclist.c:31-320 (forward), :325-858 (back);
+ * vlist.c:30-155 (forward), :160-265 (back).  The arithmetic is written in
+ * the reference's evaluation order (operand order of every sum and product),
+ * so the results agree bit for bit with the reference build. */
+
+static double orc_dot3(const double *a, const double *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+/* o = a x b */
+static void orc_cross3(const double *a, const double *b, double *o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* Vector (dx, dy, dz) and gradient (gx, gy, gz) of a delta row. */
+#define ORC_D(r) (&(r)->dx)
+#define ORC_G(r) (&(r)->gx)
+
+/* ---- forward ---- */
+
 /* Bond length (kinds 0 and 5).  yaff/pes/iclist.c:31-35. */
 static double orc_ic_bond(const orc_ic *ic, const orc_delta *dl) {
-  const orc_delta *d = dl + ic->i0;
-  return sqrt(d->dx * d->dx + d->dy * d->dy + d->dz * d->dz);
+  const double *d = ORC_D(dl + ic->i0);
+  return sqrt(orc_dot3(d, d));
 }
 
 /* Cosine of the bend angle (kind 1).  yaff/pes/iclist.c:37-47. */
 static double orc_ic_bendcos(const orc_ic *ic, const orc_delta *dl) {
-  const orc_delta *a = dl + ic->i0, *b = dl + ic->i1;
-  double da = sqrt(a->dx * a->dx + a->dy * a->dy + a->dz * a->dz);
-  double db = sqrt(b->dx * b->dx + b->dy * b->dy + b->dz * b->dz);
+  const double *a = ORC_D(dl + ic->i0), *b = ORC_D(dl + ic->i1);
+  double da = sqrt(orc_dot3(a, a));
+  double db = sqrt(orc_dot3(b, b));
   double dot;
   if (da == 0 || db == 0) return 0.0;
-  dot = a->dx * b->dx + a->dy * b->dy + a->dz * b->dz;
+  dot = orc_dot3(a, b);
   return ic->sign0 * ic->sign1 * dot / da / db;
 }
 
-/* Layer 2 forward for bond (0), bend cos (1), bend angle (2) and
- * Urey-Bradley (5).  yaff/pes/iclist.c:31-55, :307-320.  Returns -1 if a
- * kind outside that set is present. */
-int orc_iclist_forward(const orc_delta *dl, orc_ic *ic, int64_t n) {
-  int64_t i;
-  for (i = 0; i < n; i++) {
-    double v;
-    switch (ic[i].kind) {
-      case 0: case 5: v = orc_ic_bond(ic + i, dl); break;
-      case 1: v = orc_ic_bendcos(ic + i, dl); break;
-      case 2:
-        v = orc_ic_bendcos(ic + i, dl);
-        if (v > 1.0) v = 1.0;
-        if (v < -1.0) v = -1.0;
-        v = acos(v);
-        break;
-      default: return -1;
-    }
-    ic[i].value = v;
-    ic[i].grad = 0.0;
+/* Cosine of the dihedral angle from the components of the outer deltas
+ * orthogonal to the central one (kind 3).  yaff/pes/iclist.c:57-76. */
+static double orc_ic_dihedcos(const orc_ic *ic, const orc_delta *dl) {
+  const double *d0 = ORC_D(dl + ic->i0), *d1 = ORC_D(dl + ic->i1), *d2 = ORC_D(dl + ic->i2);
+  double a[3], b[3], n1, p0, p2, na, nb;
+  int k;
+  n1 = sqrt(orc_dot3(d1, d1));
+  p0 = orc_dot3(d0, d1) / n1;
+  p2 = orc_dot3(d1, d2) / n1;
+  for (k = 0; k < 3; k++) {
+    a[k] = d0[k] - p0 * d1[k] / n1;
+    b[k] = d2[k] - p2 * d1[k] / n1;
   }
-  return 0;
+  na = sqrt(orc_dot3(a, a));
+  nb = sqrt(orc_dot3(b, b));
+  return ic->sign0 * ic->sign2 * orc_dot3(a, b) / na / nb;
 }
 
+/* Sine of the dihedral angle, (d1 x d0).d2 |d1| / |d1 x d0| / |d2 x d1|;
+ * used by the dihedral angle near 0 and pi.  yaff/pes/iclist.c:78-109. */
+static double orc_ic_dihedsin(const orc_ic *ic, const orc_delta *dl) {
+  const double *d0 = ORC_D(dl + ic->i0), *d1 = ORC_D(dl + ic->i1), *d2 = ORC_D(dl + ic->i2);
+  double a[3], b[3], r1, ra, rb;
+  orc_cross3(d1, d0, a);
+  orc_cross3(d2, d1, b);
+  r1 = sqrt(orc_dot3(d1, d1));
+  ra = sqrt(orc_dot3(a, a));
+  rb = sqrt(orc_dot3(b, b));
+  return ic->sign0 * ic->sign1 * ic->sign2 * orc_dot3(a, d2) * r1 / ra / rb;
+}
+
+/* d0 . (d1 x d2) times the three delta signs. */
+static double orc_dihed_det(const orc_ic *ic, const orc_delta *dl) {
+  const double *d0 = ORC_D(dl + ic->i0), *d1 = ORC_D(dl + ic->i1), *d2 = ORC_D(dl + ic->i2);
+  double c[3], det;
+  orc_cross3(d1, d2, c);
+  det = orc_dot3(d0, c);
+  det *= ic->sign0 * ic->sign1 * ic->sign2;
+  return det;
+}
+
+/* Signed dihedral angle: acos where |cos| < 1/2, asin otherwise (kind 4).
+ * yaff/pes/iclist.c:111-141. */
+static double orc_ic_dihedangle(const orc_ic *ic, const orc_delta *dl) {
+  double c = orc_ic_dihedcos(ic, dl), phi;
+  if (fabs(c) < 0.5) {
+    phi = acos(c);
+    if (orc_dihed_det(ic, dl) > 0) phi *= -1;
+  } else {
+    phi = asin(orc_ic_dihedsin(ic, dl));
+    if (c < 0) {
+      phi *= -1;
+      if (phi > 0) phi -= 0.5 * ORC_TWO_PI;
+      else phi += 0.5 * ORC_TWO_PI;
+    }
+  }
+  return phi;
+}
+
+/* Cosine of the angle between u2 and the plane of u0, u1.
+ * yaff/pes/iclist.c:143-158. */
+static double orc_oop_cos(const double *u0, const double *u1, const double *u2) {
+  double n[3], nsq, usq, nu;
+  orc_cross3(u0, u1, n);
+  nsq = orc_dot3(n, n);
+  usq = orc_dot3(u2, u2);
+  nu = orc_dot3(n, u2);
+  return sqrt(1.0 - nu * nu / usq / nsq);
+}
+
+/* yaff/pes/iclist.c:180-190. */
+static double orc_oop_angle(const double *u0, const double *u1, const double *u2) {
+  double c = orc_oop_cos(u0, u1, u2);
+  if (c > 1) c = 1;
+  else if (c < -1) c = -1;
+  return acos(c);
+}
+
+/* Signed distance of the end of d2 from the plane of d0, d1 (kind 10) and its
+ * square (kind 11).  yaff/pes/iclist.c:212-251. */
+static double orc_ic_oopdist(const orc_ic *ic, const orc_delta *dl, int squared) {
+  const double *d0 = ORC_D(dl + ic->i0), *d1 = ORC_D(dl + ic->i1), *d2 = ORC_D(dl + ic->i2);
+  double n[3], nn, nd;
+  orc_cross3(d0, d1, n);
+  nn = sqrt(orc_dot3(n, n));
+  if (nn == 0) return 0.0;
+  nd = orc_dot3(n, d2);
+  if (squared) {
+    nd /= nn;
+    return nd * nd;
+  }
+  return nd / nn * ic->sign0 * ic->sign1 * ic->sign2;
+}
+
+/* |d0 x d1|^2 / |d2|^2: squared distance of a point from a line (kind 17).
+ * yaff/pes/iclist.c:279-298. */
+static double orc_ic_plsq(const orc_ic *ic, const orc_delta *dl) {
+  const double *d0 = ORC_D(dl + ic->i0), *d1 = ORC_D(dl + ic->i1), *d2 = ORC_D(dl + ic->i2);
+  double n[3];
+  orc_cross3(d0, d1, n);
+  return orc_dot3(n, n) / orc_dot3(d2, d2);
+}
+
+/* Value of one internal coordinate; returns NAN-free results for every kind
+ * 0..17, sets *bad for an unknown kind.  yaff/pes/iclist.c:307-312. */
+static double orc_ic_value(const orc_ic *ic, const orc_delta *dl, int *bad) {
+  const double *d0, *d1, *d2;
+  double c, t;
+  switch (ic->kind) {
+    case 0: case 5: return orc_ic_bond(ic, dl);
+    case 1: return orc_ic_bendcos(ic, dl);
+    case 2:
+      c = orc_ic_bendcos(ic, dl);
+      if (c > 1.0) c = 1.0;
+      if (c < -1.0) c = -1.0;
+      return acos(c);
+    case 3: return orc_ic_dihedcos(ic, dl);
+    case 4: return orc_ic_dihedangle(ic, dl);
+    case 6: case 7: case 8: case 9:
+      d0 = ORC_D(dl + ic->i0); d1 = ORC_D(dl + ic->i1); d2 = ORC_D(dl + ic->i2);
+      if (ic->kind == 6) return orc_oop_cos(d0, d1, d2);
+      if (ic->kind == 8) return orc_oop_angle(d0, d1, d2);
+      if (ic->kind == 7) {
+        t = orc_oop_cos(d0, d1, d2);
+        t += orc_oop_cos(d2, d0, d1);
+        t += orc_oop_cos(d1, d2, d0);
+      } else {
+        t = orc_oop_angle(d0, d1, d2);
+        t += orc_oop_angle(d2, d0, d1);
+        t += orc_oop_angle(d1, d2, d0);
+      }
+      return t / 3;
+    case 10: return orc_ic_oopdist(ic, dl, 0);
+    case 11: return orc_ic_oopdist(ic, dl, 1);
+    case 12: c = orc_ic_dihedcos(ic, dl); return 2.0 * c * c - 1.0;
+    case 13: c = orc_ic_dihedcos(ic, dl); return c * (4.0 * c * c - 3.0);
+    case 14: c = orc_ic_dihedcos(ic, dl); c *= c; return 8.0 * c * (c - 1.0) + 1.0;
+    case 15: c = orc_ic_dihedcos(ic, dl); c *= 2.0 * c; return c * (4.0 * c * (c - 3.0) + 9.0) - 1.0;
+    case 16: c = orc_ic_plsq(ic, dl); if (c < 0) c = 0.0; return sqrt(c);
+    case 17: return orc_ic_plsq(ic, dl);
+    default: *bad = 1; return 0.0;
+  }
+}
+
+/* Layer 2 forward.  yaff/pes/iclist.c:314-320.  Returns -1 for an unknown
+ * kind. */
+int orc_iclist_forward(const orc_delta *dl, orc_ic *ic, int64_t n) {
+  int64_t i;
+  int bad = 0;
+  for (i = 0; i < n; i++) {
+    ic[i].value = orc_ic_value(ic + i, dl, &bad);
+    ic[i].grad = 0.0;
+  }
+  return bad ? -1 : 0;
+}
+
+/* ---- back ---- */
+
+/* yaff/pes/iclist.c:335-360. */
 static void orc_back_bendcos(const orc_ic *ic, orc_delta *dl, double value, double grad) {
   orc_delta *a = dl + ic->i0, *b = dl + ic->i1;
   double ea[3], eb[3], da, db, fac;
-  da = sqrt(a->dx * a->dx + a->dy * a->dy + a->dz * a->dz);
-  db = sqrt(b->dx * b->dx + b->dy * b->dy + b->dz * b->dz);
-  ea[0] = a->dx / da; ea[1] = a->dy / da; ea[2] = a->dz / da;
-  eb[0] = b->dx / db; eb[1] = b->dy / db; eb[2] = b->dz / db;
+  int k;
+  da = sqrt(orc_dot3(ORC_D(a), ORC_D(a)));
+  db = sqrt(orc_dot3(ORC_D(b), ORC_D(b)));
+  for (k = 0; k < 3; k++) { ea[k] = ORC_D(a)[k] / da; eb[k] = ORC_D(b)[k] / db; }
   fac = ic->sign0 * ic->sign1;
   grad *= fac;
   value *= fac;
   fac = grad / da;
-  a->gx += fac * (eb[0] - value * ea[0]);
-  a->gy += fac * (eb[1] - value * ea[1]);
-  a->gz += fac * (eb[2] - value * ea[2]);
+  for (k = 0; k < 3; k++) ORC_G(a)[k] += fac * (eb[k] - value * ea[k]);
   fac = grad / db;
-  b->gx += fac * (ea[0] - value * eb[0]);
-  b->gy += fac * (ea[1] - value * eb[1]);
-  b->gz += fac * (ea[2] - value * eb[2]);
+  for (k = 0; k < 3; k++) ORC_G(b)[k] += fac * (ea[k] - value * eb[k]);
 }
 
-/* Layer 2 back (chain rule into relative-vector gradients).
- * yaff/pes/iclist.c:325-364, :853-858. */
+/* Chain rule of the dihedral cosine through the projected vectors a, b and
+ * their Jacobians towards d0, d1, d2.  yaff/pes/iclist.c:366-439. */
+static void orc_back_dihedcos(const orc_ic *ic, orc_delta *dl, double value, double grad) {
+  orc_delta *r0 = dl + ic->i0, *r1 = dl + ic->i1, *r2 = dl + ic->i2;
+  const double *d0 = ORC_D(r0), *d1 = ORC_D(r1), *d2 = ORC_D(r2);
+  double a[3], b[3], ga[3], gb[3], ja0[9], ja1[9], jb1[9];
+  double n1, nn, n4, p0, p2, na, nb;
+  int r, c;
+  n1 = sqrt(orc_dot3(d1, d1));
+  p0 = orc_dot3(d0, d1);
+  p2 = orc_dot3(d1, d2);
+  nn = n1 * n1;
+  n4 = n1 * n1 * n1 * n1;
+  for (r = 0; r < 3; r++) {
+    a[r] = d0[r] - p0 * d1[r] / nn;
+    b[r] = d2[r] - p2 * d1[r] / nn;
+  }
+  na = sqrt(orc_dot3(a, a));
+  nb = sqrt(orc_dot3(b, b));
+  value *= ic->sign0 * ic->sign2;
+  grad *= ic->sign0 * ic->sign2;
+  for (r = 0; r < 3; r++) {
+    ga[r] = (b[r] / nb - value * a[r] / na) / na;
+    gb[r] = (a[r] / na - value * b[r] / nb) / nb;
+  }
+  for (r = 0; r < 3; r++)
+    for (c = 0; c < 3; c++) {
+      double t = d1[r] * d1[c] / nn;
+      double u0 = -(d0[r] * d1[c] / nn), u2 = -(d2[r] * d1[c] / nn);
+      ja0[3 * r + c] = (r == c) ? 1 - t : -t;
+      if (r == c) {
+        u0 = -(p0 / nn) - d0[r] * d1[c] / nn;
+        u2 = -(p2 / nn) - d2[r] * d1[c] / nn;
+      }
+      ja1[3 * r + c] = u0 + 2 * p0 / n4 * d1[r] * d1[c];
+      jb1[3 * r + c] = u2 + 2 * p2 / n4 * d1[r] * d1[c];
+    }
+  for (c = 0; c < 3; c++) {
+    ORC_G(r0)[c] += grad * (ga[0] * ja0[c] + ga[1] * ja0[3 + c] + ga[2] * ja0[6 + c]);
+    ORC_G(r1)[c] += grad * (ga[0] * ja1[c] + ga[1] * ja1[3 + c] + ga[2] * ja1[6 + c]
+                            + gb[0] * jb1[c] + gb[1] * jb1[3 + c] + gb[2] * jb1[6 + c]);
+    ORC_G(r2)[c] += grad * (gb[0] * ja0[c] + gb[1] * ja0[3 + c] + gb[2] * ja0[6 + c]);
+  }
+}
+
+/* Chain rule of the dihedral sine, a product of four factors.
+ * yaff/pes/iclist.c:441-510. */
+static void orc_back_dihedsin(const orc_ic *ic, orc_delta *dl, double value, double grad) {
+  orc_delta *r0 = dl + ic->i0, *r1 = dl + ic->i1, *r2 = dl + ic->i2;
+  const double *d0 = ORC_D(r0), *d1 = ORC_D(r1), *d2 = ORC_D(r2);
+  double a[3], b[3], c[3], t[3], n1, ra, rb, fac;
+  int k;
+  orc_cross3(d1, d0, a);
+  orc_cross3(d2, d1, b);
+  orc_cross3(d0, d2, c);
+  n1 = sqrt(orc_dot3(d1, d1));
+  ra = sqrt(orc_dot3(a, a));
+  rb = sqrt(orc_dot3(b, b));
+  value *= ic->sign0 * ic->sign1 * ic->sign2;
+  grad *= ic->sign0 * ic->sign1 * ic->sign2;
+  /* triple product (d1 x d0).d2 */
+  fac = grad * n1 / ra / rb;
+  for (k = 0; k < 3; k++) ORC_G(r0)[k] += fac * b[k];
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] += fac * c[k];
+  for (k = 0; k < 3; k++) ORC_G(r2)[k] += fac * a[k];
+  /* |d1| */
+  fac = grad * value / n1 / n1;
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] += fac * d1[k];
+  /* 1/|d1 x d0| */
+  fac = grad * value / ra / ra;
+  orc_cross3(a, d1, t);
+  for (k = 0; k < 3; k++) ORC_G(r0)[k] -= fac * t[k];
+  orc_cross3(a, d0, t);
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] += fac * t[k];
+  /* 1/|d2 x d1| */
+  fac = grad * value / rb / rb;
+  orc_cross3(b, d2, t);
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] -= fac * t[k];
+  orc_cross3(b, d1, t);
+  for (k = 0; k < 3; k++) ORC_G(r2)[k] += fac * t[k];
+}
+
+/* yaff/pes/iclist.c:512-541. */
+static void orc_back_dihedangle(const orc_ic *ic, orc_delta *dl, double grad) {
+  double c = orc_ic_dihedcos(ic, dl), s, tmp = grad;
+  if (fabs(c) < 0.5) {
+    s = sqrt(1 - c * c);
+    tmp /= -s;
+    if (orc_dihed_det(ic, dl) > 0) tmp *= -1;
+    orc_back_dihedcos(ic, dl, c, tmp);
+  } else {
+    s = orc_ic_dihedsin(ic, dl);
+    tmp /= c;
+    orc_back_dihedsin(ic, dl, s, tmp);
+  }
+}
+
+/* Gradient of the out-of-plane cosine towards the three deltas.
+ * yaff/pes/iclist.c:543-622. */
+static void orc_back_oopcos(orc_delta *r0, orc_delta *r1, orc_delta *r2, double value, double grad) {
+  const double *d0 = ORC_D(r0), *d1 = ORC_D(r1), *d2 = ORC_D(r2);
+  double c01[3], c12[3], c20[3], t[3], nsq, usq, nu, t0, t1, t2;
+  int k;
+  orc_cross3(d0, d1, c01);
+  orc_cross3(d1, d2, c12);
+  orc_cross3(d2, d0, c20);
+  nsq = orc_dot3(c01, c01);
+  usq = orc_dot3(d2, d2);
+  nu = orc_dot3(c01, d2);
+  t0 = nu / usq / nsq / value;
+  t1 = nu / nsq;
+  t2 = nu / usq;
+  orc_cross3(d1, c01, t);
+  for (k = 0; k < 3; k++) ORC_G(r0)[k] += -t0 * grad * (c12[k] - t1 * t[k]);
+  orc_cross3(c01, d0, t);
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] += -t0 * grad * (c20[k] - t1 * t[k]);
+  for (k = 0; k < 3; k++) ORC_G(r2)[k] += -t0 * grad * (c01[k] - t2 * d2[k]);
+}
+
+/* yaff/pes/iclist.c:646-650. */
+static void orc_back_oopangle(orc_delta *r0, orc_delta *r1, orc_delta *r2, double value, double grad) {
+  double s = sin(value);
+  if (s != 0.0) s = -grad / s;
+  orc_back_oopcos(r0, r1, r2, cos(value), s);
+}
+
+/* Signed out-of-plane distance (squared = 0) and its square (squared = 1).
+ * yaff/pes/iclist.c:674-754. */
+static void orc_back_oopdist(const orc_ic *ic, orc_delta *dl, double grad, int squared) {
+  orc_delta *r0 = dl + ic->i0, *r1 = dl + ic->i1, *r2 = dl + ic->i2;
+  const double *d0 = ORC_D(r0), *d1 = ORC_D(r1), *d2 = ORC_D(r2);
+  double c01[3], c12[3], c20[3], t[3], nn, nd, fac, t0;
+  int k;
+  orc_cross3(d0, d1, c01);
+  orc_cross3(d1, d2, c12);
+  orc_cross3(d2, d0, c20);
+  nn = sqrt(orc_dot3(c01, c01));
+  nd = orc_dot3(c01, d2);
+  if (squared) fac = 2 * nd / nn * grad / nn;
+  else fac = grad / nn * ic->sign0 * ic->sign1 * ic->sign2;
+  t0 = nd / nn / nn;
+  orc_cross3(d1, c01, t);
+  for (k = 0; k < 3; k++) ORC_G(r0)[k] += fac * (c12[k] - t0 * t[k]);
+  orc_cross3(c01, d0, t);
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] += fac * (c20[k] - t0 * t[k]);
+  for (k = 0; k < 3; k++) ORC_G(r2)[k] += fac * c01[k];
+}
+
+/* yaff/pes/iclist.c:800-833. */
+static void orc_back_plsq(const orc_ic *ic, orc_delta *dl, double grad) {
+  orc_delta *r0 = dl + ic->i0, *r1 = dl + ic->i1, *r2 = dl + ic->i2;
+  const double *d0 = ORC_D(r0), *d1 = ORC_D(r1), *d2 = ORC_D(r2);
+  double n[3], t[3], nsq, usq, fac;
+  int k;
+  orc_cross3(d0, d1, n);
+  nsq = orc_dot3(n, n);
+  usq = orc_dot3(d2, d2);
+  fac = 2.0 * grad / usq;
+  orc_cross3(d1, n, t);
+  for (k = 0; k < 3; k++) ORC_G(r0)[k] += fac * t[k];
+  orc_cross3(d0, n, t);
+  for (k = 0; k < 3; k++) ORC_G(r1)[k] -= fac * t[k];
+  fac = 2.0 * grad * nsq / (usq * usq);
+  for (k = 0; k < 3; k++) ORC_G(r2)[k] -= fac * d2[k];
+}
+
+/* Layer 2 back (chain rule into relative-vector gradients), every kind.
+ * yaff/pes/iclist.c:325-858. */
 int orc_iclist_back(orc_delta *dl, const orc_ic *ic, int64_t n) {
   int64_t i;
   for (i = 0; i < n; i++) {
     const orc_ic *c = ic + i;
+    double g = c->grad, v = c->value, x;
+    int k;
     switch (c->kind) {
       case 0: case 5: {
         orc_delta *d = dl + c->i0;
-        double x = c->grad / c->value;
-        d->gx += x * d->dx; d->gy += x * d->dy; d->gz += x * d->dz;
+        x = g / v;
+        for (k = 0; k < 3; k++) ORC_G(d)[k] += x * ORC_D(d)[k];
         break;
       }
-      case 1: orc_back_bendcos(c, dl, c->value, c->grad); break;
-      case 2: orc_back_bendcos(c, dl, cos(c->value), -c->grad / sin(c->value)); break;
+      case 1: orc_back_bendcos(c, dl, v, g); break;
+      case 2: orc_back_bendcos(c, dl, cos(v), -g / sin(v)); break;
+      case 3: orc_back_dihedcos(c, dl, v, g); break;
+      case 4: orc_back_dihedangle(c, dl, g); break;
+      case 6: orc_back_oopcos(dl + c->i0, dl + c->i1, dl + c->i2, v, g); break;
+      case 8: orc_back_oopangle(dl + c->i0, dl + c->i1, dl + c->i2, v, g); break;
+      case 7: case 9: {
+        orc_delta *r0 = dl + c->i0, *r1 = dl + c->i1, *r2 = dl + c->i2;
+        orc_delta *rot[3][3] = {{r0, r1, r2}, {r2, r0, r1}, {r1, r2, r0}};
+        for (k = 0; k < 3; k++) {
+          const double *u0 = ORC_D(rot[k][0]), *u1 = ORC_D(rot[k][1]), *u2 = ORC_D(rot[k][2]);
+          if (c->kind == 7)
+            orc_back_oopcos(rot[k][0], rot[k][1], rot[k][2], orc_oop_cos(u0, u1, u2), g / 3.0);
+          else
+            orc_back_oopangle(rot[k][0], rot[k][1], rot[k][2], orc_oop_angle(u0, u1, u2), g / 3.0);
+        }
+        break;
+      }
+      case 10: orc_back_oopdist(c, dl, g, 0); break;
+      case 11: orc_back_oopdist(c, dl, g, 1); break;
+      case 12: case 13: case 14: case 15: {
+        double cc = orc_ic_dihedcos(c, dl), t;
+        if (c->kind == 12) t = 4.0 * cc * g;
+        else if (c->kind == 13) t = (12.0 * cc * cc - 3.0) * g;
+        else if (c->kind == 14) t = 16.0 * cc * (2.0 * cc * cc - 1.0) * g;
+        else t = 12.0 * cc * (16.0 * cc * cc * (cc * cc - 1.0) + 3.0) * g;
+        orc_back_dihedcos(c, dl, cc, t);
+        break;
+      }
+      case 16:
+        x = (v == 0.0) ? 0.0 : 0.5 * g / v;
+        orc_back_plsq(c, dl, x);
+        break;
+      case 17: orc_back_plsq(c, dl, g); break;
       default: return -1;
     }
   }
   return 0;
 }
 
-/* Layer 3: harmonic terms 0.5 K (q - q0)^2 (kind 0).
- * yaff/pes/vlist.c:30-34, :146-155, :160-162, :260-265. */
+/* ---- layer 3: energy terms ---- */
+
+/* Energy of one term.  yaff/pes/vlist.c:30-144 (kinds 0..15). */
+static double orc_vterm_energy(const orc_vterm *t, const orc_ic *ic) {
+  double q = ic[t->ic0].value, x, x2, c, K, y;
+  switch (t->kind) {
+    case 0: x = q - t->par1; return 0.5 * (t->par0) * x * x;
+    case 1: return t->par0 * q + t->par1 * q * q + t->par2 * q * q * q + t->par3 * q * q * q * q;
+    case 2: x = t->par1 / q; return 0.5 * t->par0 * t->par1 * t->par1 * (1.0 + x * (x - 2.0));
+    case 3: return t->par0 * (q - t->par1) * (ic[t->ic1].value - t->par2);
+    case 4: return 0.5 * t->par1 * (1 - cos(t->par0 * (q - t->par2)));
+    case 5: return 0.5 * t->par0 * (1 + t->par1 * q);
+    case 6: c = q; return 0.5 * t->par0 * (1 + t->par1 * (2 * c * c - 1));
+    case 7: c = q; return 0.5 * t->par0 * (1 + t->par1 * c * (4 * c * c - 3));
+    case 8: c = q * q; return 0.5 * t->par0 * (1 + t->par1 * (8 * c * c - 8 * c + 1));
+    case 9: c = q * q; return 0.5 * t->par0 * (1 + t->par1 * (32 * c * c * c - 48 * c * c + 18 * c - 1));
+    case 10:
+      return t->par0 * q + t->par1 * q * q + t->par2 * q * q * q + t->par3 * q * q * q * q +
+             t->par4 * q * q * q * q * q + t->par5 * q * q * q * q * q * q;
+    case 11:
+      x = q - t->par1; x2 = x * x;
+      return 0.5 * (t->par0) * x2 * (1.0 - 1.349402 * x + 1.062183 * x2);
+    case 12:
+      x = q - t->par1; x2 = x * x;
+      return 0.5 * (t->par0) * x2 * (1.0 - 0.802141 * x + 0.183837 * x2 - 0.131664 * x2 * x + 0.237090 * x2 * x2);
+    case 13:
+      K = (t->par1 - t->par2) * (t->par1 - t->par2);
+      K *= K;
+      K = t->par0 / K;
+      x = q - t->par1;
+      y = q - t->par2;
+      y *= y;
+      return 0.5 * K * x * x * y * y;
+    case 14: x = t->par1 * (q - t->par2); return t->par0 * (exp(-2.0 * x) - 2.0 * exp(-x));
+    case 15:
+      x = q - t->par5;
+      return t->par0 + t->par1 * x + t->par2 * x * x + t->par3 * x * x * x + t->par4 * x * x * x * x;
+    default: return NAN;
+  }
+}
+
+/* Layer 3 forward, sequential sum.  yaff/pes/vlist.c:146-155. */
 double orc_vlist_forward(const orc_ic *ic, orc_vterm *vt, int64_t n) {
   int64_t i;
   double e = 0.0;
   for (i = 0; i < n; i++) {
-    double x = ic[vt[i].ic0].value - vt[i].par1;
-    vt[i].energy = 0.5 * (vt[i].par0) * x * x;
+    vt[i].energy = orc_vterm_energy(vt + i, ic);
     e += vt[i].energy;
   }
   return e;
 }
 
+/* Layer 3 back: dE/dq added to the coordinates' grad.
+ * yaff/pes/vlist.c:160-265. */
 void orc_vlist_back(orc_ic *ic, const orc_vterm *vt, int64_t n) {
   int64_t i;
-  for (i = 0; i < n; i++)
-    ic[vt[i].ic0].grad += (vt[i].par0) * (ic[vt[i].ic0].value - vt[i].par1);
+  for (i = 0; i < n; i++) {
+    const orc_vterm *t = vt + i;
+    double q = ic[t->ic0].value, x, q2, c, K, y, z;
+    double *g = &ic[t->ic0].grad;
+    switch (t->kind) {
+      case 0: *g += (t->par0) * (q - t->par1); break;
+      case 1: *g += t->par0 + 2.0 * t->par1 * q + 3.0 * t->par2 * q * q + 4.0 * t->par3 * q * q * q; break;
+      case 2: x = t->par1 / q; *g += t->par0 * t->par1 * (x * x - x * x * x); break;
+      case 3:
+        *g += t->par0 * (ic[t->ic1].value - t->par2);
+        ic[t->ic1].grad += t->par0 * (ic[t->ic0].value - t->par1);
+        break;
+      case 4: *g += 0.5 * t->par1 * t->par0 * sin(t->par0 * (q - t->par2)); break;
+      case 5: *g += 0.5 * t->par0 * t->par1; break;
+      case 6: *g += t->par1 * 2.0 * t->par0 * q; break;
+      case 7: c = q; *g += t->par1 * 1.5 * t->par0 * (4 * c * c - 1); break;
+      case 8: c = q; *g += t->par1 * 8 * t->par0 * c * (2 * c * c - 1); break;
+      case 9: c = q; *g += t->par1 * 6 * t->par0 * c * (16 * c * c * c * c - 16 * c * c + 3); break;
+      case 10:
+        *g += t->par0 + 2.0 * t->par1 * q + 3.0 * t->par2 * q * q + 4.0 * t->par3 * q * q * q +
+              5.0 * t->par4 * q * q * q * q + 6.0 * t->par5 * q * q * q * q * q;
+        break;
+      case 11: x = q - t->par1; *g += (t->par0) * (x - 2.024103 * x * x + 2.124366 * x * x * x); break;
+      case 12:
+        x = q - t->par1; q2 = x * x;
+        *g += (t->par0) * (x - 1.203211 * q2 + 0.367674 * q2 * x - 0.329159 * q2 * q2 + 0.711270 * q2 * q2 * x);
+        break;
+      case 13:
+        K = (t->par1 - t->par2) * (t->par1 - t->par2);
+        K *= K;
+        K = t->par0 / (K);
+        x = q - t->par1;
+        y = q - t->par2;
+        y *= y;
+        z = q - t->par2;
+        *g += 0.5 * K * (2 * x * y * y + 4 * x * x * y * z);
+        break;
+      case 14: x = t->par1 * (q - t->par2); *g += -2.0 * t->par1 * t->par0 * (exp(-2.0 * x) - exp(-x)); break;
+      case 15: x = q - t->par5; *g += t->par1 + 2.0 * t->par2 * x + 3.0 * t->par3 * x * x + 4.0 * t->par4 * x * x * x; break;
+      default: break;
+    }
+  }
 }

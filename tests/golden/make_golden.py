@@ -3,7 +3,7 @@
 Run in a container that holds the reference checkout (default /root/reference,
 or $YAFF_REFERENCE) after ``sh oracle/build_ref.sh``:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 For every case the script builds the reference's own ForceField (through the
 import shim in oracle/ref_shim.py), calls ForceField.compute(gpos, vtens) one
@@ -69,7 +69,12 @@ def spec_arrays(spec):
     return out
 
 
+ONLY = set()   # case names given on the command line: regenerate only those
+
+
 def run_case(name, spec, displacements=(), full_rows=True):
+    if ONLY and name not in ONLY:
+        return
     ff = build_reference_ff(spec)
     natom = len(spec['pos'])
     data = spec_arrays(spec)
@@ -198,6 +203,11 @@ def main():
     t2 = configs.triclinic_mm3_ei(natom=2000, name='tric2000')
     run_case('tric2000', t2, full_rows=False)
 
+    v = configs.valence_molecules(name='valence40')
+    run_case('valence40', v, displacements=[rng.uniform(-0.08, 0.08, (40, 3)) * angstrom,
+                                            rng.uniform(-0.08, 0.08, (40, 3)) * angstrom])
+
 
 if __name__ == '__main__':
+    ONLY.update(sys.argv[1:])
     main()

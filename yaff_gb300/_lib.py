@@ -65,7 +65,7 @@ SIGNATURES = {
     'yg_ewald_setup': (_I, [_P, _D, _D, _P, _D, _I64, _I64]),
     'yg_ewald_reci': (_I, [_P, _I]),
     'yg_ewald_corr': (_I, [_P, _I]),
-    'yg_set_valence': (_I, [_P, _P, _I64, _P, _I64, _P, _P, _I64]),
+    'yg_set_valence': (_I, [_P, _P, _I64, _P, _I64, _P, _P, _P, _I64]),
     'yg_valence_compute': (_I, [_P, _I]),
     'yg_get_part': (_I, [_P, _I, _P, _P, _P]),
     'yg_get_total': (_I, [_P, _I, _P, _P, _P, _P]),

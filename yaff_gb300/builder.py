@@ -9,7 +9,7 @@ from .nlist import NeighborList
 from .pair import PairPotLJ, PairPotMM3, PairPotEI, Switch3, Hammer
 from .scaling import Scalings
 from .system import System
-from .valence import Bond, BendAngle, Harmonic
+from .valence import Bond, BendAngle, Harmonic, terms_from_rows
 
 __all__ = ['build_system', 'build_forcefield']
 
@@ -56,11 +56,14 @@ def build_forcefield(spec, precision=None, system=None, stream=None):
         parts.append(ForcePartEwaldNeutralizing(system, ew['alpha'], diel, nlow, nhigh))
     bt = spec.get('bond_terms')
     at = spec.get('bend_terms')
-    if (bt is not None and len(bt)) or (at is not None and len(at)):
+    vr = spec.get('valence')
+    if any(x is not None and len(x) for x in (bt, at, vr)):
         pv = ForcePartValence(system)
         for i, j, K, r0 in (bt if bt is not None else []):
             pv.add_term(Harmonic(K, r0, Bond(int(i), int(j))))
         for i, j, k, K, t0 in (at if at is not None else []):
             pv.add_term(Harmonic(K, t0, BendAngle(int(i), int(j), int(k))))
+        for term in terms_from_rows(vr if vr is not None else np.zeros((0, 17))):
+            pv.add_term(term)
         parts.append(pv)
     return ForceField(system, parts, nlist)

@@ -162,6 +162,109 @@ def flexible_water(nside=20, box=62.1, jitter=0.2, rcut=10.0, skin=1.0, seed=1,
     return spec
 
 
+def _valence_row(term_kind, pars, ic0, ic1=None):
+    """One packed valence row: [term kind, par0..par5, ic kind, 4 atoms,
+    ic kind, 4 atoms], -1 where unused."""
+    row = [float(term_kind)] + [float(p) for p in pars] + [-1.0] * (6 - len(pars))
+    for ic in (ic0, ic1):
+        if ic is None:
+            row += [-1.0] * 5
+        else:
+            row += [float(ic[0])] + [float(a) for a in ic[1]] + [-1.0] * (4 - len(ic[1]))
+    return row
+
+
+def valence_molecules(nside=2, box=15.0, seed=7, rcut=6.0, skin=0.5, name=None):
+    """Periodic box of branched 5-atom molecules carrying every valence kind.
+
+    Molecule a-b-c-d with a branch b-e (bonds 1.45-1.6 A, bends 95-125 deg,
+    the dihedral a-b-c-d uniform in (-180, 180] deg so that the cosine and the
+    sine branches of the dihedral angle both occur), centres on a jittered
+    nside^3 lattice of a mildly triclinic 15 A cell so that molecules straddle
+    the cell faces.  Terms: every internal-coordinate kind 0-17 and every
+    energy-term kind 0-15 of the reference valence tables, several sharing a
+    coordinate; LJ (sigma 3.0 A, eps 0.2 kJ/mol) with 1-2 and 1-3 pairs
+    excluded, rcut 6 A, skin 0.5 A.
+    """
+    rng = np.random.default_rng(seed)
+    nmol = nside ** 3
+    g = np.arange(nside, dtype=float)
+    centres = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    centres = centres * (box / nside) + rng.uniform(-1.0, 1.0, centres.shape)
+    rvecs = np.array([[box, 0.0, 0.0], [0.1 * box, box, 0.0], [-0.07 * box, 0.13 * box, box]])
+    centres = centres @ (rvecs / box)
+    rot = _random_rotations(rng, nmol)
+    pos = []
+    for m in range(nmol):
+        r = rng.uniform(1.45, 1.6, 4)
+        th = rng.uniform(95.0, 125.0, 3) * math.pi / 180
+        phi = rng.uniform(-math.pi, math.pi, 2)
+        b = np.zeros(3)
+        c = np.array([r[1], 0.0, 0.0])
+        a = r[0] * np.array([math.cos(th[0]), math.sin(th[0]), 0.0])
+        # d: bend th[1] at c, dihedral phi[0] about b-c
+        u = np.array([-math.cos(th[1]), math.sin(th[1]) * math.cos(phi[0]), math.sin(th[1]) * math.sin(phi[0])])
+        d = c + r[2] * u
+        # e: bend th[2] at b against c, rotated out of the a-b-c plane
+        e = r[3] * np.array([math.cos(th[2]), math.sin(th[2]) * math.cos(phi[1] + math.pi),
+                             math.sin(th[2]) * math.sin(phi[1] + math.pi)])
+        mol = np.array([a, b, c, d, e])
+        mol -= mol.mean(0)
+        pos.append(centres[m] + mol @ rot[m].T)
+    pos = np.concatenate(pos) * angstrom
+    spec = _base_spec(name or 'valence%d' % (5 * nmol), pos, rvecs * angstrom)
+    n = len(pos)
+    spec['pair'] = [{'kind': 'lj', 'sigmas': np.full(n, 3.0 * angstrom), 'epsilons': np.full(n, 0.2 * kjmol)}]
+    spec['rcut'] = rcut * angstrom
+    spec['skin'] = skin * angstrom
+    spec['scalings'] = (0.0, 0.0, 1.0, 1.0)
+    A = angstrom
+    kb, kt = 2000 * kjmol / A ** 2, 300 * kjmol
+    rows, bonds = [], []
+    for m in range(nmol):
+        a, b, c, d, e = 5 * m + np.arange(5)
+        bonds += [(a, b), (b, c), (c, d), (b, e)]
+        B = lambda i, j: (0, (i, j))          # noqa: E731
+        rows += [
+            _valence_row(0, [kb, 1.5 * A], B(a, b)),                                  # Harmonic
+            _valence_row(1, [0.0, kb, -0.3 * kb / A, 0.05 * kb / A ** 2], B(a, b)),   # PolyFour, shared bond
+            _valence_row(2, [kb, 1.52 * A], B(b, c)),                                 # Fues
+            _valence_row(11, [kb, 1.55 * A], B(c, d)),                                # MM3Quartic
+            _valence_row(13, [50 * kjmol, 1.45 * A, 1.65 * A], B(c, d)),              # BondDoubleWell
+            _valence_row(14, [400 * kjmol, 2.0 / A, 1.5 * A], B(b, e)),               # Morse
+            _valence_row(10, [0.01, 0.02, -0.003, 1e-4, 2e-6, -1e-7], B(b, c)),       # PolySix
+            _valence_row(15, [0.1, 0.0, kb, 0.1 * kb / A, 0.01 * kb / A ** 2, 1.5 * A], B(b, e)),  # Poly4
+            _valence_row(0, [kt, 110 * deg], (2, (a, b, c))),                         # BendAngle
+            _valence_row(12, [kt, 112 * deg], (2, (c, b, e))),                        # MM3Bend
+            _valence_row(5, [20 * kjmol, -1.0], (1, (a, b, e))),                      # Chebychev1 on BendCos
+            _valence_row(0, [kt, -0.3], (1, (b, c, d))),                              # BendCos
+            _valence_row(0, [kb, 2.5 * A], (5, (a, b, c))),                           # UreyBradley
+            _valence_row(3, [0.3 * kb, 1.5 * A, 110 * deg], B(a, b), (2, (a, b, c))),  # Cross
+            _valence_row(3, [-0.2 * kb, 1.5 * A, 1.52 * A], B(a, b), B(b, c)),        # Cross of two bonds
+            _valence_row(4, [3, 10 * kjmol, 15 * deg], (4, (a, b, c, d))),            # Cosine on DihedAngle
+            _valence_row(0, [5 * kjmol, 60 * deg], (4, (e, b, c, d))),                # Harmonic on DihedAngle
+            _valence_row(6, [8 * kjmol, -1.0], (3, (a, b, c, d))),                    # Chebychev2 on DihedCos
+            _valence_row(7, [6 * kjmol, 1.0], (3, (a, b, c, d))),                     # Chebychev3
+            _valence_row(8, [4 * kjmol, -1.0], (3, (e, b, c, d))),                    # Chebychev4
+            _valence_row(9, [2 * kjmol, 1.0], (3, (e, b, c, d))),                     # Chebychev6
+            _valence_row(0, [3 * kjmol, 0.2], (12, (a, b, c, d))),                    # DihedCos2
+            _valence_row(0, [3 * kjmol, -0.1], (13, (a, b, c, d))),                   # DihedCos3
+            _valence_row(0, [3 * kjmol, 0.3], (14, (e, b, c, d))),                    # DihedCos4
+            _valence_row(0, [3 * kjmol, -0.4], (15, (e, b, c, d))),                   # DihedCos6
+            _valence_row(0, [40 * kjmol, 0.7], (6, (a, c, e, b))),                    # OopCos
+            _valence_row(0, [40 * kjmol, 0.8], (7, (a, c, e, b))),                    # OopMeanCos
+            _valence_row(0, [40 * kjmol, 30 * deg], (8, (a, c, e, b))),               # OopAngle
+            _valence_row(0, [40 * kjmol, 25 * deg], (9, (a, c, e, b))),               # OopMeanAngle
+            _valence_row(0, [kb, 0.2 * A], (10, (a, c, e, b))),                       # OopDist
+            _valence_row(1, [0.0, kb, 0.0, 0.0], (11, (a, c, e, b))),                 # PolyFour on SqOopDist
+            _valence_row(0, [kb, 0.8 * A], (16, (a, c, b))),                          # PointLineDistance
+            _valence_row(0, [kb / A ** 2, 0.5 * A ** 2], (17, (a, c, e))),            # SqPointLineDistance
+        ]
+    spec['bonds'] = np.array(bonds, dtype=np.int64)
+    spec['valence'] = np.array(rows, dtype=np.float64)
+    return spec
+
+
 _CACHE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_build', 'cache')
 
 

@@ -256,7 +256,7 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_ew_fpre, (void **)&c->d_ew_fpiece, (void **)&c->d_ew_woff, (void **)&c->d_ew_crange, (void **)&c->d_ew_te,
       (void **)&c->d_ew_yf, (void **)&c->d_ew_ys, (void **)&c->d_ew_wb,
       (void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval, (void **)&c->d_vpar,
-      (void **)&c->d_vic, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,
+      (void **)&c->d_vkind, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,
       (void **)&c->d_total, (void **)&c->d_red, (void **)&c->d_vel, (void **)&c->d_invm, (void **)&c->d_md_ekpart,
       (void **)&c->d_md_ekin, (void **)&c->d_md_log, (void **)&c->d_md_extra, (void **)&c->d_md_step,
       (void **)&c->d_md_ctrl, (void **)&c->d_snap_pos, (void **)&c->d_snap_vel, (void **)&c->d_snap_total,
@@ -587,8 +587,10 @@ int yg_ewald_corr(yg_ctx *c, int want_grad) {
 }
 
 int yg_set_valence(yg_ctx *c, const int64_t *delta_ij, int64_t ndelta, const int64_t *ic_rows, int64_t nic,
-                   const double *vterm_pars, const int64_t *vterm_ic, int64_t nterm) {
+                   const int64_t *vterm_kind, const double *vterm_pars, const int64_t *vterm_ic, int64_t nterm) {
   if (!c || ndelta < 0 || nic < 0 || nterm < 0) return YG_ERR_ARG;
+  if ((ndelta && !delta_ij) || (nic && !ic_rows) || (nterm && (!vterm_kind || !vterm_pars || !vterm_ic)))
+    return YG_ERR_ARG;
   const int64_t N = c->natom;
   std::vector<int2> ij(ndelta > 0 ? ndelta : 1);
   for (int64_t r = 0; r < ndelta; r++) {
@@ -597,39 +599,46 @@ int yg_set_valence(yg_ctx *c, const int64_t *delta_ij, int64_t ndelta, const int
     ij[r] = make_int2((int)i, (int)j);
   }
   for (int64_t r = 0; r < nic; r++) {
-    int64_t kind = ic_rows[9 * r];
-    if (!(kind == 0 || kind == 1 || kind == 2 || kind == 5)) {
-      yg_set_error("internal-coordinate kind not supported on the device (0, 1, 2, 5)");
+    const int64_t kind = ic_rows[9 * r];
+    if (kind < 0 || kind > 17) {
+      yg_set_error("unknown internal-coordinate kind (0..17)");
       return YG_ERR_UNSUPPORTED;
     }
-    int nused = (kind == 0 || kind == 5) ? 1 : 2;
+    // relative vectors a kind reads (yaff/pes/iclist.py:231-530)
+    const int nused = (kind == 0 || kind == 5) ? 1 : (kind == 1 || kind == 2) ? 2 : 3;
     for (int u = 0; u < nused; u++) {
-      int64_t d = ic_rows[9 * r + 1 + 2 * u];
-      if (d < 0 || d >= ndelta) return YG_ERR_ARG;
+      const int64_t d = ic_rows[9 * r + 1 + 2 * u], sg = ic_rows[9 * r + 2 + 2 * u];
+      if (d < 0 || d >= ndelta || (sg != 1 && sg != -1)) return YG_ERR_ARG;
     }
   }
-  std::vector<int> vic(nterm > 0 ? nterm : 1);
+  std::vector<int4> vk(nterm > 0 ? nterm : 1);
   for (int64_t t = 0; t < nterm; t++) {
-    if (vterm_ic[t] < 0 || vterm_ic[t] >= nic) return YG_ERR_ARG;
-    vic[t] = (int)vterm_ic[t];
+    const int64_t kind = vterm_kind[t], i0 = vterm_ic[2 * t], i1 = vterm_ic[2 * t + 1];
+    if (kind < 0 || kind > 15) {
+      yg_set_error("unknown valence-term kind (0..15)");
+      return YG_ERR_UNSUPPORTED;
+    }
+    if (i0 < 0 || i0 >= nic) return YG_ERR_ARG;
+    if (kind == 3 ? (i1 < 0 || i1 >= nic) : (i1 != -1)) return YG_ERR_ARG;
+    vk[t] = make_int4((int)kind, (int)i0, (int)i1, 0);
   }
   void **bufs[] = {(void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval,
-                   (void **)&c->d_vpar,     (void **)&c->d_vic,   (void **)&c->d_vE};
+                   (void **)&c->d_vpar,     (void **)&c->d_vkind, (void **)&c->d_vE};
   for (void **b : bufs) yg_free(c, b);
   int rc;
   if ((rc = yg_alloc(c, (void **)&c->d_delta_ij, ij.size() * sizeof(int2)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_delta, (size_t)(ndelta > 0 ? ndelta : 1) * 6 * sizeof(double)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_ic, (size_t)(nic > 0 ? nic : 1) * 9 * sizeof(int64_t)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_icval, (size_t)(nic > 0 ? nic : 1) * 2 * sizeof(double)))) return rc;
-  if ((rc = yg_alloc(c, (void **)&c->d_vpar, (size_t)(nterm > 0 ? nterm : 1) * 2 * sizeof(double)))) return rc;
-  if ((rc = yg_alloc(c, (void **)&c->d_vic, vic.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_vpar, (size_t)(nterm > 0 ? nterm : 1) * 6 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_vkind, vk.size() * sizeof(int4)))) return rc;
   YG_CUDA(cudaMemcpyAsync(c->d_delta_ij, ij.data(), ij.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
   if (nic > 0)
     YG_CUDA(cudaMemcpyAsync(c->d_ic, ic_rows, (size_t)nic * 9 * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
   if (nterm > 0)
-    YG_CUDA(cudaMemcpyAsync(c->d_vpar, vterm_pars, (size_t)nterm * 2 * sizeof(double), cudaMemcpyHostToDevice,
+    YG_CUDA(cudaMemcpyAsync(c->d_vpar, vterm_pars, (size_t)nterm * 6 * sizeof(double), cudaMemcpyHostToDevice,
                             c->stream));
-  YG_CUDA(cudaMemcpyAsync(c->d_vic, vic.data(), vic.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_vkind, vk.data(), vk.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
   YG_CUDA(cudaStreamSynchronize(c->stream));
   c->ndelta = ndelta;
   c->nic = nic;

@@ -213,8 +213,8 @@ struct yg_ctx {
   double *d_delta = nullptr;      // ndelta*6: dx,dy,dz,gx,gy,gz
   int64_t *d_ic = nullptr;        // nic*9: kind, i0,s0,i1,s1,i2,s2,i3,s3
   double *d_icval = nullptr;      // nic*2: value, grad
-  double *d_vpar = nullptr;       // nterm*2: K, q0
-  int *d_vic = nullptr;           // nterm
+  double *d_vpar = nullptr;       // nterm*6: par0..par5
+  int4 *d_vkind = nullptr;        // nterm: term kind, ic0, ic1 (-1 unused), 0
   double *d_vE = nullptr;         // nterm
 
   // device-resident velocity Verlet (yg_md_*)

@@ -479,11 +479,11 @@ class ForcePartValence(ForcePart):
         dev.sync_cell()
         key = (id(self.vlist), self.vlist.version)
         if getattr(dev, 'valence_key', None) != key:
-            dij, ics, pars, vic = self.vlist.arrays()
+            dij, ics, kinds, pars, vic = self.vlist.arrays()
             check(dev.lib.yg_set_valence(dev.ctx, _lib.ptr(np.ascontiguousarray(dij)), len(dij),
                                          _lib.ptr(np.ascontiguousarray(ics)), len(ics),
-                                         _lib.ptr(np.ascontiguousarray(pars)), _lib.ptr(np.ascontiguousarray(vic)),
-                                         len(vic)), 'yg_set_valence')
+                                         _lib.ptr(np.ascontiguousarray(kinds)), _lib.ptr(np.ascontiguousarray(pars)),
+                                         _lib.ptr(np.ascontiguousarray(vic)), len(kinds)), 'yg_set_valence')
             dev.valence_key = key
         check(dev.lib.yg_valence_compute(dev.ctx, int(want_grad)), 'yg_valence_compute')
 
