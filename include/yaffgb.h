@@ -42,10 +42,20 @@ typedef struct yg_ctx yg_ctx;
 #define YG_MIXED 1         /* FP32 terms, FP64 accumulation */
 #define YG_MIXED_KAHAN 2   /* FP32 terms, Kahan-compensated FP32 accumulation */
 
-/* pair-potential kinds (yaff/pes/pair_pot.c:277, :321, :711) */
+/* pair-potential kinds (yaff/pes/pair_pot.c:277, :321, :711; per-atom
+ * parameters: LJ, MM3, EI, MM3CAP :373, Grimme :434) and the kinds whose
+ * parameters are tables over pairs of atom types (ExpRep :473, QMDFFRep
+ * :506, LJCross :540, DampDisp :596, Disp68BJDamp :651) */
 #define YG_POT_LJ 0
 #define YG_POT_MM3 1
 #define YG_POT_EI 2
+#define YG_POT_MM3CAP 3
+#define YG_POT_GRIMME 4
+#define YG_POT_EXPREP 5
+#define YG_POT_QMDFFREP 6
+#define YG_POT_LJCROSS 7
+#define YG_POT_DAMPDISP 8
+#define YG_POT_DISP68BJ 9
 
 /* truncation kinds (yaff/pes/truncation.c:30, :59) */
 #define YG_TR_NONE 0
@@ -109,6 +119,21 @@ int yg_set_pair_pot(yg_ctx *ctx, int slot, int kind, const double *sigma,
                     const double *epsilon, const int32_t *onlypauli,
                     const double *radii, double alpha, double dielectric,
                     double rcut, int tr_kind, double tr_par);
+
+/* Registers a pair potential whose parameters are tables over pairs of atom
+ * types (kinds YG_POT_EXPREP .. YG_POT_DISP68BJ).  ffatype_ids: natom type
+ * indices in [0, nffatype); cross0/cross1/cross2: nffatype x nffatype
+ * row-major tables (amp/b for ExpRep and QMDFFRep, eps/sig for LJCross, cn/b
+ * for DampDisp, c6/c8/R for Disp68BJDamp; cross2 NULL except for the last);
+ * power: the dispersion power of DampDisp; scales: {c6_scale, c8_scale,
+ * bj_a, bj_b} of Disp68BJDamp, else NULL.  Replaces pair_data_exprep_init,
+ * pair_data_qmdffrep_init, pair_data_ljcross_init, pair_data_dampdisp_init
+ * and pair_data_disp68bjdamp_init (yaff/pes/pair_pot.c:458-471, :491-504,
+ * :524-538, :560-574, :631-649). */
+int yg_set_pair_table(yg_ctx *ctx, int slot, int kind, int64_t nffatype,
+                      const int64_t *ffatype_ids, const double *cross0,
+                      const double *cross1, const double *cross2, int64_t power,
+                      const double *scales, double rcut, int tr_kind, double tr_par);
 int yg_clear_pair_pots(yg_ctx *ctx);
 
 /* Full neighbour-list rebuild for all pairs closer than rcut_total over the

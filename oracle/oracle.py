@@ -63,6 +63,8 @@ def lib():
         L.orc_nlist_recompute.argtypes = [P, P, P, P, INT, P, I64]
         L.orc_pair_compute.restype = D
         L.orc_pair_compute.argtypes = [P, I64, P, I64, INT, P, P, P, P, P, D, D, D, INT, D, P, P]
+        L.orc_pair_compute_table.restype = D
+        L.orc_pair_compute_table.argtypes = [P, I64, P, I64, INT, P, I64, P, P, P, I64, P, D, INT, D, P, P]
         L.orc_ewald_reci.restype = D
         L.orc_ewald_reci.argtypes = [P, I64, I64, I64, P, P, P, D, D, P, D, D, P, P, P]
         L.orc_ewald_corr.restype = D
@@ -170,6 +172,80 @@ def build_scalings(natom, bonds, scalings):
                 rows.append((i0, i1, sc, depth))
     rows.sort()
     return np.array(rows, dtype=scaling_dtype)
+
+
+# Pair-potential kinds of the oracle (yaff/pes/pair_pot.c).
+PAIR_KINDS = {'lj': 0, 'mm3': 1, 'ei': 2, 'mm3cap': 3, 'grimme': 4, 'exprep': 5, 'qmdffrep': 6, 'ljcross': 7,
+              'dampdisp': 8, 'disp68bjdamp': 9}
+
+
+def type_pair_tables(pdef):
+    """Type-pair tables of a table potential after the mixing rules that the
+    reference's constructors apply to unset (zero) entries:
+    yaff/pes/ext.pyx:1146-1172 (ExpRep/QMDFFRep amplitude and decay),
+    :1560-1573 (DampDisp), :1690-1694 (Disp68BJDamp R from C8/C6)."""
+    kind = pdef['kind']
+    f = lambda k: np.array(pdef[k], dtype=np.float64)   # noqa: E731
+    if kind in ('exprep', 'qmdffrep'):
+        A, B = f('amp_cross'), f('b_cross')
+        n = len(A)
+        amps = pdef.get('amps')
+        if amps is not None:
+            amps = np.asarray(amps, float)
+            mix, x = int(pdef['amp_mix']), float(pdef['amp_mix_coeff'])
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if A[i0, i1] == 0.0:
+                        if mix == 0:
+                            A[i0, i1] = np.sqrt(amps[i0] * amps[i1])
+                        elif amps[i0] != 0.0 and amps[i1] != 0.0:
+                            a = (np.log(amps[i0]) + np.log(amps[i1])) / 2
+                            a *= 1 - x * abs(np.log(amps[i0] / amps[i1]))
+                            A[i0, i1] = np.exp(a)
+                        A[i1, i0] = A[i0, i1]
+        bs = pdef.get('bs')
+        if bs is not None:
+            bs = np.asarray(bs, float)
+            mix, x = int(pdef['b_mix']), float(pdef['b_mix_coeff'])
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if B[i0, i1] == 0.0:
+                        if mix == 0:
+                            B[i0, i1] = (bs[i0] + bs[i1]) / 2
+                        elif amps[i0] != 0.0 and amps[i1] != 0.0:
+                            b = (bs[i0] + bs[i1]) / 2
+                            b *= 1 - x * abs(np.log(amps[i0] / amps[i1]))
+                            B[i0, i1] = b
+                        B[i1, i0] = B[i0, i1]
+        return A, B
+    if kind == 'ljcross':
+        return f('eps_cross'), f('sig_cross')
+    if kind == 'dampdisp':
+        C, B = f('cn_cross'), f('b_cross')
+        n = len(C)
+        if pdef.get('cns') is not None:
+            cns, vols = np.asarray(pdef['cns'], float), np.asarray(pdef['vols'], float)
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if C[i0, i1] == 0.0 and vols[i0] != 0.0 and vols[i1] != 0.0:
+                        ratio = vols[i0] / vols[i1]
+                        C[i0, i1] = 2.0 * cns[i0] * cns[i1] / (cns[i0] / ratio + cns[i1] * ratio)
+                        C[i1, i0] = C[i0, i1]
+        if pdef.get('bs') is not None:
+            bs = np.asarray(pdef['bs'], float)
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if B[i0, i1] == 0.0 and bs[i0] != 0.0 and bs[i1] != 0.0:
+                        B[i0, i1] = 0.5 * (bs[i0] + bs[i1])
+                        B[i1, i0] = B[i0, i1]
+        return C, B
+    if kind == 'disp68bjdamp':
+        c6, c8, R = f('c6_cross'), f('c8_cross'), f('R_cross')
+        if np.all(R == 0.0):
+            m = c6 != 0.0
+            R[m] = np.sqrt(c8[m] / c6[m])
+        return c6, c8, R
+    raise ValueError(kind)
 
 
 # Relative vectors (i -> j) each internal-coordinate kind reads, from its
@@ -360,7 +436,7 @@ class OracleForceField(object):
 
     def _pair(self, pdef, gpos, vtens):
         spec = self.spec
-        kind = {'lj': 0, 'mm3': 1, 'ei': 2}[pdef['kind']]
+        kind = PAIR_KINDS[pdef['kind']]
         tr = spec.get('tr')
         if pdef['kind'] == 'ei':
             tr = None if not pdef.get('smooth', False) else tr
@@ -368,8 +444,19 @@ class OracleForceField(object):
         if tr is not None:
             trk = {'hammer': 1, 'switch3': 2}[tr[0]]
             trp = tr[1]
-        sig = pdef.get('sigmas')
-        eps = pdef.get('epsilons')
+        if kind >= 5:
+            tabs = type_pair_tables(pdef)
+            types = np.ascontiguousarray(pdef['ffatype_ids'], dtype=np.int64)
+            scales = None
+            if pdef['kind'] == 'disp68bjdamp':
+                scales = np.array([float(pdef.get(k, d)) for k, d in
+                                   (('c6_scale', 1.0), ('c8_scale', 1.0), ('bj_a', 0.0), ('bj_b', 0.0))])
+            return lib().orc_pair_compute_table(
+                _p(self.neighs), self.nneigh, _p(self.stab), len(self.stab), kind, _p(types), len(tabs[0]),
+                _p(tabs[0]), _p(tabs[1]), _p(tabs[2] if len(tabs) > 2 else None),
+                int(pdef.get('power', 6)), _p(scales), self.rcut, trk, trp, _p(gpos), _p(vtens))
+        sig = pdef.get('r0') if kind == 4 else pdef.get('sigmas')
+        eps = pdef.get('c6') if kind == 4 else pdef.get('epsilons')
         op = pdef.get('onlypaulis')
         q = spec['charges']
         radii = pdef.get('radii')

@@ -19,7 +19,7 @@ def build_reference_ff(spec):
                              ForcePartValence)
     from yaff.pes.nlist import NeighborList
     from yaff.pes.scaling import Scalings
-    from yaff.pes.ext import PairPotLJ, PairPotMM3, PairPotEI, Switch3, Hammer
+    from yaff.pes.ext import Switch3, Hammer
     from yaff.pes.iclist import Bond, BendAngle
     from yaff.pes.vlist import Harmonic
 
@@ -40,19 +40,15 @@ def build_reference_ff(spec):
     parts = []
     ew = spec.get('ewald')
     alpha = ew['alpha'] if (ew is not None and system.cell.nvec == 3) else 0.0
+    import yaff.pes.ext as rext
+    from yaff_gb300.builder import make_pair_pot
+    classes = {'lj': rext.PairPotLJ, 'mm3': rext.PairPotMM3, 'ei': rext.PairPotEI, 'mm3cap': rext.PairPotMM3CAP,
+               'grimme': rext.PairPotGrimme, 'exprep': rext.PairPotExpRep, 'qmdffrep': rext.PairPotQMDFFRep,
+               'ljcross': rext.PairPotLJCross, 'dampdisp': rext.PairPotDampDisp,
+               'disp68bjdamp': rext.PairPotDisp68BJDamp}
+    keep = []   # the reference's pair potentials borrow their argument arrays
     for p in spec['pair']:
-        if p['kind'] == 'lj':
-            pp = PairPotLJ(p['sigmas'].copy(), p['epsilons'].copy(), spec['rcut'], trobj)
-        elif p['kind'] == 'mm3':
-            pp = PairPotMM3(p['sigmas'].copy(), p['epsilons'].copy(),
-                            np.asarray(p['onlypaulis'], dtype=np.intc).copy(), spec['rcut'], trobj)
-        elif p['kind'] == 'ei':
-            radii = p.get('radii')
-            pp = PairPotEI(spec['charges'].copy(), alpha, spec['rcut'],
-                           trobj if p.get('smooth', False) else None,
-                           spec.get('dielectric', 1.0), None if radii is None else radii.copy())
-        else:
-            raise ValueError(p['kind'])
+        pp = make_pair_pot(p, spec, classes, trobj, alpha, keep)
         parts.append(ForcePartPair(system, nlist, scalings, pp))
     if ew is not None and system.cell.nvec == 3:
         diel = spec.get('dielectric', 1.0)
@@ -80,4 +76,6 @@ def build_reference_ff(spec):
             for term in terms_from_rows(vr, icc, tcc):
                 pv.add_term(term)
         parts.append(pv)
-    return ForceField(system, parts, nlist)
+    ff = ForceField(system, parts, nlist)
+    ff._borrowed_arrays = keep
+    return ff

@@ -241,15 +241,20 @@ void orc_nlist_recompute(const double *pos, const double *pos_old,
 
 /* --------------------------------------------------------- pair terms -- */
 
-enum { ORC_LJ = 0, ORC_MM3 = 1, ORC_EI = 2 };
+enum { ORC_LJ = 0, ORC_MM3 = 1, ORC_EI = 2, ORC_MM3CAP = 3, ORC_GRIMME = 4, ORC_EXPREP = 5, ORC_QMDFFREP = 6,
+       ORC_LJCROSS = 7, ORC_DAMPDISP = 8, ORC_DISP68BJ = 9 };
 enum { ORC_TR_NONE = 0, ORC_TR_HAMMER = 1, ORC_TR_SWITCH3 = 2 };
 
 typedef struct {
   int kind;
-  const double *sigma, *epsilon;   /* LJ, MM3 */
-  const int32_t *onlypauli;        /* MM3 */
+  const double *sigma, *epsilon;   /* LJ, MM3, MM3CAP; Grimme: r0, c6 */
+  const int32_t *onlypauli;        /* MM3, MM3CAP */
   const double *charges, *radii;   /* EI */
   double alpha, dielectric;        /* EI */
+  const int64_t *types;            /* type-pair table kinds */
+  int64_t ntype, power;
+  const double *cross0, *cross1, *cross2;
+  double c6_scale, c8_scale, bj_a, bj_b;
   double rcut;
   int tr_kind;
   double tr_par;
@@ -343,6 +348,124 @@ static double orc_ei(const orc_pairpot *p, int64_t i, int64_t j, double d, doubl
   return pot;
 }
 
+/* MM3 with a linear cap below x = d/sigma = 0.355114; below the cap the
+ * gradient is the unmodified MM3 expression evaluated at the cap's x (so it
+ * is not the derivative of the capped energy).  yaff/pes/pair_pot.c:373-419
+ * (pair_fn_mm3cap). */
+static double orc_mm3cap(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  double sig = p->sigma[i] + p->sigma[j];
+  double eps = sqrt(p->epsilon[i] * p->epsilon[j]);
+  int op = p->onlypauli[i] + p->onlypauli[j];
+  double x = d / sig, xmax = 0.355114, ex;
+  if (op != 0) return orc_mm3(p, i, j, d, g);
+  if (x > xmax) {
+    ex = 1.84e5 * exp(-12.0 * x);
+    x *= x;
+    x *= 1 / 2.25 * x * x;
+    if (g) *g = eps / d * (-12.0 / sig * ex + 6.0 / d / x);
+    return eps * (ex - 1 / x);
+  }
+  ex = 1.84e5 * exp(-12.0 * xmax);
+  xmax *= xmax;
+  xmax *= 1 / 2.25 * xmax * xmax;
+  if (g) *g = eps / d * (-12.0 / sig * ex + 6.0 / d / xmax);
+  return eps * (5799.303156 - 12182.86986 * x);
+}
+
+/* Damped dispersion -1.1 f c6/d^6, f = 1/(1 + exp(-20 (d/r0 - 1))), r0 the
+ * sum and c6 the geometric mean.  yaff/pes/pair_pot.c:434-455. */
+static double orc_grimme(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  double r0 = p->sigma[i] + p->sigma[j];
+  double c6 = sqrt(p->epsilon[i] * p->epsilon[j]);
+  double ex = exp(-20.0 * (d / r0 - 1.0));
+  double f = 1.0 / (1.0 + ex);
+  double d6 = d * d * d, e;
+  d6 *= d6;
+  e = 1.1 * f * c6 / d6;
+  if (g) *g = e / d * (6.0 / d - 20.0 / r0 * f * ex);
+  return -e;
+}
+
+static int64_t orc_tpair(const orc_pairpot *p, int64_t i, int64_t j) {
+  return p->types[i] * p->ntype + p->types[j];
+}
+
+/* A exp(-B d) (ExpRep) and A exp(-B d)/d (QMDFFRep) per type pair; zero
+ * when A or B is zero.  yaff/pes/pair_pot.c:473-489, :506-522. */
+static double orc_rep(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  int64_t k = orc_tpair(p, i, j);
+  double amp = p->cross0[k], b = p->cross1[k], e;
+  if (amp == 0.0 || b == 0.0) {
+    if (g) *g = 0.0;
+    return 0.0;
+  }
+  if (p->kind == ORC_EXPREP) {
+    e = amp * exp(-b * d);
+    if (g) *g = -e * b / d;
+  } else {
+    e = amp / d * exp(-b * d);
+    if (g) *g = -(b + 1 / d) * e / d;
+  }
+  return e;
+}
+
+/* Lennard-Jones with per-type-pair epsilon and sigma.
+ * yaff/pes/pair_pot.c:540-557. */
+static double orc_ljcross(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  int64_t k = orc_tpair(p, i, j);
+  double eps = p->cross0[k], sig = p->cross1[k], x = sig / d;
+  x *= x;
+  x *= x * x;
+  if (g) *g = 24.0 * eps / d / d * x * (1.0 - 2.0 * x);
+  return 4.0 * eps * (x * (x - 1.0));
+}
+
+/* Tang-Toennies damping 1 - exp(-x) sum_{k=0..n} x^k/k!; *g = exp(-x)
+ * x^n/n!.  yaff/pes/pair_pot.c:576-594. */
+static double orc_tang_toennies(double x, int order, double *g) {
+  double tmp = 1.0, poly = 0.0, last, e;
+  int k, fac = 1;
+  for (k = 0; k < order; k++) {
+    poly += tmp / fac;
+    fac *= k + 1;
+    tmp *= x;
+  }
+  last = tmp / fac;
+  poly += last;
+  e = exp(-x);
+  if (g) *g = e * last;
+  return 1.0 - poly * e;
+}
+
+/* -C/d^n, Tang-Toennies damped where B != 0.  yaff/pes/pair_pot.c:596-629. */
+static double orc_dampdisp(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  int64_t k = orc_tpair(p, i, j), q;
+  double cn = p->cross0[k], b = p->cross1[k], disp = 1.0, damp;
+  if (cn == 0.0) return 0.0;
+  for (q = 0; q < p->power; q++) disp *= d;
+  disp = -cn / disp;
+  if (b == 0.0) {
+    if (g) *g = -p->power * disp / (d * d);
+    return disp;
+  }
+  damp = orc_tang_toennies(b * d, (int)p->power, g);
+  if (g) *g = ((*g) * b - p->power / d * damp) * disp / d;
+  return damp * disp;
+}
+
+/* Becke-Johnson damped C6 + C8 dispersion, R = bj_a R_ij + bj_b.
+ * yaff/pes/pair_pot.c:651-677. */
+static double orc_disp68bj(const orc_pairpot *p, int64_t i, int64_t j, double d, double *g) {
+  int64_t k = orc_tpair(p, i, j);
+  double c6 = p->cross0[k], c8 = p->cross1[k];
+  double R = p->bj_a * p->cross2[k] + p->bj_b;
+  double R2 = R * R, R4 = R2 * R2, R6 = R4 * R2, R8 = R4 * R4;
+  double d2 = d * d, d4 = d2 * d2, d6 = d4 * d2, d8 = d4 * d4;
+  double pot = -p->c6_scale * c6 / (d6 + R6) - p->c8_scale * c8 / (d8 + R8);
+  if (g) *g = 6.0 * p->c6_scale * c6 / (d6 + R6) / (d6 + R6) * d4 + 8.0 * p->c8_scale * c8 / (d8 + R8) / (d8 + R8) * d6;
+  return pot;
+}
+
 /* Scaling factor of pair (a, b) from the (a, b)-sorted table, walked in lock
  * step with the (a, b)-sorted neighbour list.  yaff/pes/pair_pot.c:65-81. */
 static double orc_get_scaling(const orc_scale *st, int64_t a, int64_t b, int64_t *row, int64_t n) {
@@ -361,6 +484,26 @@ static double orc_get_scaling(const orc_scale *st, int64_t a, int64_t b, int64_t
   return 1.0;
 }
 
+typedef double (*orc_pair_fn)(const orc_pairpot *, int64_t, int64_t, double, double *);
+
+static orc_pair_fn orc_pair_fn_of(int kind) {
+  switch (kind) {
+    case ORC_LJ: return orc_lj;
+    case ORC_MM3: return orc_mm3;
+    case ORC_EI: return orc_ei;
+    case ORC_MM3CAP: return orc_mm3cap;
+    case ORC_GRIMME: return orc_grimme;
+    case ORC_EXPREP: case ORC_QMDFFREP: return orc_rep;
+    case ORC_LJCROSS: return orc_ljcross;
+    case ORC_DAMPDISP: return orc_dampdisp;
+    case ORC_DISP68BJ: return orc_disp68bj;
+    default: return 0;
+  }
+}
+
+static double orc_pair_loop(const orc_neigh *rows, int64_t n, const orc_scale *st, int64_t nst,
+                            const orc_pairpot *pp, double *gpos, double *vtens);
+
 /* Generic pair loop with exclusion scaling, truncation chain rule, gradient
  * and virial accumulation.  yaff/pes/pair_pot.c:84-176 (pair_pot_compute). */
 double orc_pair_compute(const orc_neigh *rows, int64_t n, const orc_scale *st,
@@ -369,12 +512,37 @@ double orc_pair_compute(const orc_neigh *rows, int64_t n, const orc_scale *st,
                         const double *charges, const double *radii,
                         double alpha, double dielectric, double rcut,
                         int tr_kind, double tr_par, double *gpos, double *vtens) {
-  orc_pairpot p;
-  int64_t i, srow = 0;
-  double energy = 0.0;
+  orc_pairpot p = {0};
   p.kind = kind; p.sigma = sigma; p.epsilon = epsilon; p.onlypauli = onlypauli;
   p.charges = charges; p.radii = radii; p.alpha = alpha; p.dielectric = dielectric;
   p.rcut = rcut; p.tr_kind = tr_kind; p.tr_par = tr_par;
+  return orc_pair_loop(rows, n, st, nst, &p, gpos, vtens);
+}
+
+/* The same loop for the type-pair table kinds (ExpRep, QMDFFRep, LJCross,
+ * DampDisp, Disp68BJDamp); tables are ntype x ntype row-major, scales =
+ * {c6_scale, c8_scale, bj_a, bj_b} or NULL. */
+double orc_pair_compute_table(const orc_neigh *rows, int64_t n, const orc_scale *st, int64_t nst, int kind,
+                              const int64_t *types, int64_t ntype, const double *cross0, const double *cross1,
+                              const double *cross2, int64_t power, const double *scales, double rcut,
+                              int tr_kind, double tr_par, double *gpos, double *vtens) {
+  orc_pairpot p = {0};
+  p.kind = kind; p.types = types; p.ntype = ntype; p.power = power;
+  p.cross0 = cross0; p.cross1 = cross1; p.cross2 = cross2;
+  if (scales) { p.c6_scale = scales[0]; p.c8_scale = scales[1]; p.bj_a = scales[2]; p.bj_b = scales[3]; }
+  p.rcut = rcut; p.tr_kind = tr_kind; p.tr_par = tr_par;
+  return orc_pair_loop(rows, n, st, nst, &p, gpos, vtens);
+}
+
+static double orc_pair_loop(const orc_neigh *rows, int64_t n, const orc_scale *st, int64_t nst,
+                            const orc_pairpot *pp, double *gpos, double *vtens) {
+  const orc_pairpot *p = pp;
+  orc_pair_fn fn = orc_pair_fn_of(p->kind);
+  const int tr_kind = p->tr_kind;
+  const double rcut = p->rcut, tr_par = p->tr_par;
+  int64_t i, srow = 0;
+  double energy = 0.0;
+  if (!fn) return NAN;
   for (i = 0; i < n; i++) {
     const orc_neigh *r = rows + i;
     double s, v, vg = 0.0, h, hg;
@@ -385,9 +553,7 @@ double orc_pair_compute(const orc_neigh *rows, int64_t n, const orc_scale *st,
     else
       s = 1.0;
     if (s == 0.0) continue;
-    if (kind == ORC_LJ) v = orc_lj(&p, r->a, r->b, r->d, want_g ? &vg : NULL);
-    else if (kind == ORC_MM3) v = orc_mm3(&p, r->a, r->b, r->d, want_g ? &vg : NULL);
-    else v = orc_ei(&p, r->a, r->b, r->d, want_g ? &vg : NULL);
+    v = fn(p, r->a, r->b, r->d, want_g ? &vg : NULL);
     if (!want_g) {
       if (tr_kind != ORC_TR_NONE && v != 0.0) {
         v *= (tr_kind == ORC_TR_HAMMER) ? orc_hammer(r->d, rcut, tr_par, NULL)

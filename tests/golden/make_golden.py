@@ -207,6 +207,10 @@ def main():
     run_case('valence40', v, displacements=[rng.uniform(-0.08, 0.08, (40, 3)) * angstrom,
                                             rng.uniform(-0.08, 0.08, (40, 3)) * angstrom])
 
+    for var in 'abc':
+        pp = configs.pair_potentials(var)
+        run_case(pp['name'], pp, displacements=[rng.uniform(-0.05, 0.05, (300, 3)) * angstrom])
+
 
 if __name__ == '__main__':
     ONLY.update(sys.argv[1:])

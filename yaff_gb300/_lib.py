@@ -25,6 +25,8 @@ MIXED_KAHAN = 2
 PRECISIONS = {'fp64': FP64, 'mixed': MIXED, 'mixed_kahan': MIXED_KAHAN}
 
 POT_LJ, POT_MM3, POT_EI = 0, 1, 2
+POT_MM3CAP, POT_GRIMME = 3, 4
+POT_EXPREP, POT_QMDFFREP, POT_LJCROSS, POT_DAMPDISP, POT_DISP68BJ = 5, 6, 7, 8, 9
 TR_NONE, TR_HAMMER, TR_SWITCH3 = 0, 1, 2
 
 PART_PAIR0 = 0
@@ -53,6 +55,7 @@ SIGNATURES = {
     'yg_set_charges': (_I, [_P, _P]),
     'yg_set_scalings': (_I, [_P, _P, _P, _P, _P, _I64]),
     'yg_set_pair_pot': (_I, [_P, _I, _I, _P, _P, _P, _P, _D, _D, _D, _I, _D]),
+    'yg_set_pair_table': (_I, [_P, _I, _I, _I64, _P, _P, _P, _P, _I64, _P, _D, _I, _D]),
     'yg_clear_pair_pots': (_I, [_P]),
     'yg_nlist_build': (_I, [_P, _D, _P, _I64, _I64, ctypes.POINTER(_I64)]),
     'yg_nlist_stats': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

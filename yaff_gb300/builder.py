@@ -6,12 +6,71 @@ from .device import device_of
 from .ff import (ForceField, ForcePartPair, ForcePartEwaldReciprocal, ForcePartEwaldCorrection,
                  ForcePartEwaldNeutralizing, ForcePartValence)
 from .nlist import NeighborList
-from .pair import PairPotLJ, PairPotMM3, PairPotEI, Switch3, Hammer
+from . import pair as _pair
+from .pair import Switch3, Hammer
 from .scaling import Scalings
 from .system import System
 from .valence import Bond, BendAngle, Harmonic, terms_from_rows
 
-__all__ = ['build_system', 'build_forcefield']
+__all__ = ['build_system', 'build_forcefield', 'make_pair_pot', 'PAIR_CLASSES']
+
+PAIR_CLASSES = {'lj': _pair.PairPotLJ, 'mm3': _pair.PairPotMM3, 'ei': _pair.PairPotEI,
+                'mm3cap': _pair.PairPotMM3CAP, 'grimme': _pair.PairPotGrimme, 'exprep': _pair.PairPotExpRep,
+                'qmdffrep': _pair.PairPotQMDFFRep, 'ljcross': _pair.PairPotLJCross,
+                'dampdisp': _pair.PairPotDampDisp, 'disp68bjdamp': _pair.PairPotDisp68BJDamp}
+
+
+def _opt(p, key, conv):
+    v = p.get(key)
+    return None if v is None else conv(v)
+
+
+def make_pair_pot(p, spec, classes, trobj, alpha, keep=None):
+    """The pair potential a workload entry describes, from `classes` (kind
+    name -> class with the reference's constructor arguments).  Tables are
+    passed as fresh C-contiguous arrays, since mixing rules fill them in
+    place; every array passed is also appended to `keep` when given (for
+    classes that hold borrowed pointers to their arguments)."""
+    k, rcut = p['kind'], spec['rcut']
+    keep = [] if keep is None else keep
+
+    def arr(key, dt=np.float64):
+        if p.get(key) is None:
+            return None
+        a = np.array(p[key], dtype=dt, order='C')
+        keep.append(a)
+        return a
+
+    cls = classes[k]
+    if k == 'lj':
+        return cls(arr('sigmas'), arr('epsilons'), rcut, trobj)
+    if k in ('mm3', 'mm3cap'):
+        return cls(arr('sigmas'), arr('epsilons'), arr('onlypaulis', np.intc), rcut, trobj)
+    if k == 'ei':
+        q = np.array(spec['charges'], dtype=np.float64)
+        keep.append(q)
+        return cls(q, alpha, rcut,
+                   trobj if p.get('smooth', False) else None, spec.get('dielectric', 1.0), arr('radii'))
+    if k == 'grimme':
+        return cls(arr('r0'), arr('c6'), rcut, trobj)
+    ids = arr('ffatype_ids', np.int64)
+    if k in ('exprep', 'qmdffrep'):
+        kw = {}
+        if p.get('amps') is not None:
+            kw.update(amps=arr('amps'), amp_mix=int(p['amp_mix']), amp_mix_coeff=float(p['amp_mix_coeff']))
+        if p.get('bs') is not None:
+            kw.update(bs=arr('bs'), b_mix=int(p['b_mix']), b_mix_coeff=float(p['b_mix_coeff']))
+        return cls(ids, arr('amp_cross'), arr('b_cross'), rcut, trobj, **kw)
+    if k == 'ljcross':
+        return cls(ids, arr('eps_cross'), arr('sig_cross'), rcut, trobj)
+    if k == 'dampdisp':
+        return cls(ids, arr('cn_cross'), arr('b_cross'), rcut, trobj, cns=arr('cns'), bs=arr('bs'), vols=arr('vols'),
+                   power=int(p.get('power', 6)))
+    if k == 'disp68bjdamp':
+        return cls(ids, arr('c6_cross'), arr('c8_cross'), arr('R_cross'), rcut, trobj,
+                   c6_scale=float(p.get('c6_scale', 1.0)), c8_scale=float(p.get('c8_scale', 1.0)),
+                   bj_a=float(p.get('bj_a', 0.0)), bj_b=float(p.get('bj_b', 0.0)))
+    raise ValueError(k)
 
 
 def build_system(spec):
@@ -38,15 +97,7 @@ def build_forcefield(spec, precision=None, system=None, stream=None):
     alpha = ew['alpha'] if (ew is not None and system.cell.nvec == 3) else 0.0
     parts = []
     for p in spec['pair']:
-        if p['kind'] == 'lj':
-            pp = PairPotLJ(p['sigmas'], p['epsilons'], spec['rcut'], trobj)
-        elif p['kind'] == 'mm3':
-            pp = PairPotMM3(p['sigmas'], p['epsilons'], p['onlypaulis'], spec['rcut'], trobj)
-        elif p['kind'] == 'ei':
-            pp = PairPotEI(spec['charges'], alpha, spec['rcut'], trobj if p.get('smooth', False) else None,
-                           spec.get('dielectric', 1.0), p.get('radii'))
-        else:
-            raise ValueError(p['kind'])
+        pp = make_pair_pot(p, spec, PAIR_CLASSES, trobj, alpha)
         parts.append(ForcePartPair(system, nlist, scalings, pp))
     if ew is not None and system.cell.nvec == 3:
         diel = spec.get('dielectric', 1.0)

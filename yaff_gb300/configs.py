@@ -14,8 +14,14 @@ charges        (N,) float64 or None
 masses         (N,) float64 (a.u. of mass)
 bonds          (nb, 2) int64 or None
 pair           list of dicts: {'kind': 'lj', 'sigmas', 'epsilons'} |
-               {'kind': 'mm3', 'sigmas', 'epsilons', 'onlypaulis'} |
-               {'kind': 'ei', 'radii' (optional)}
+               {'kind': 'mm3' or 'mm3cap', 'sigmas', 'epsilons', 'onlypaulis'} |
+               {'kind': 'ei', 'radii' (optional)} | {'kind': 'grimme', 'r0', 'c6'} |
+               type-pair tables over 'ffatype_ids': {'kind': 'exprep' or
+               'qmdffrep', 'amp_cross', 'b_cross', mixing keys} | {'kind':
+               'ljcross', 'eps_cross', 'sig_cross'} | {'kind': 'dampdisp',
+               'cn_cross', 'b_cross', 'power', mixing keys} | {'kind':
+               'disp68bjdamp', 'c6_cross', 'c8_cross', 'R_cross', 'c6_scale',
+               'c8_scale', 'bj_a', 'bj_b'}
 rcut, skin     float (bohr)
 tr             None | ('switch3', width) | ('hammer', tau)
 ewald          None | {'alpha': a, 'gcut': g}      (reciprocal + corr + neut)
@@ -23,6 +29,8 @@ dielectric     float
 scalings       (scale1, scale2, scale3, scale4)
 bond_terms     (nbt, 4): i, j, K, r0      harmonic bonds (Bond + Harmonic)
 bend_terms     (nat, 5): i, j, k, K, th0  harmonic bends (BendAngle + Harmonic)
+valence        (nv, 17) packed valence terms: term kind, par0..par5, then
+               per internal coordinate its kind and 4 atoms (-1 unused)
 nlow, nhigh    ints (nhigh = -1 means N)
 """
 import hashlib
@@ -262,6 +270,75 @@ def valence_molecules(nside=2, box=15.0, seed=7, rcut=6.0, skin=0.5, name=None):
         ]
     spec['bonds'] = np.array(bonds, dtype=np.int64)
     spec['valence'] = np.array(rows, dtype=np.float64)
+    return spec
+
+
+def pair_potentials(variant='a', natom=300, box=16.0, dmin=1.5, rcut=7.0, skin=0.5, seed=11, name=None):
+    """A dense periodic box (triclinic, 16 A edges) with three atom types and
+    three pair parts of the potentials beyond LJ / MM3 / EI, in atomic units.
+
+    variant 'a': MM3CAP (minimum separation 1.5 A, so that pairs fall below
+      the cap at d = 0.355 sigma_ij; some atoms only-Pauli), Grimme and ExpRep
+      with the geometric / arithmetic mixing rules filling unset table
+      entries, no truncation;
+    variant 'b': QMDFFRep, LJCross, DampDisp (power 6, Tang-Toennies damped,
+      one undamped type pair; C6 mixed from per-type C6 and volumes), Switch3
+      truncation over 2 A;
+    variant 'c': Disp68BJDamp (Becke-Johnson R from C8/C6), DampDisp (power
+      8) and ExpRep with the corrected mixing rules, Hammer truncation.
+    """
+    rng = np.random.default_rng(seed + ord(variant))
+    rvecs = triclinic_rvecs(box, box, box, 80 * deg, 85 * deg, 95 * deg) * angstrom
+    pos = _rsa_fill(rng, rvecs, natom, dmin * angstrom)
+    spec = _base_spec(name or 'pairpot%s%d' % (variant, natom), pos, rvecs)
+    types = np.arange(natom) % 3
+    A = angstrom
+    spec['rcut'] = rcut * A
+    spec['skin'] = skin * A
+    if variant == 'a':
+        sig = np.array([1.9, 1.7, 1.6])[types] * A
+        eps = np.array([0.4, 0.25, 0.3])[types] * kjmol
+        spec['pair'] = [
+            {'kind': 'mm3cap', 'sigmas': sig, 'epsilons': eps, 'onlypaulis': (np.arange(natom) % 7 == 0).astype(np.int32)},
+            {'kind': 'grimme', 'r0': np.array([1.5, 1.4, 1.3])[types] * A, 'c6': np.array([20.0, 12.0, 9.0])[types]},
+            {'kind': 'exprep', 'ffatype_ids': types.astype(np.int64),
+             'amp_cross': np.array([[60.0, 0.0, 0.0], [0.0, 40.0, 35.0], [0.0, 35.0, 30.0]]),
+             'b_cross': np.array([[2.1, 0.0, 0.0], [0.0, 2.0, 0.0], [0.0, 0.0, 1.9]]),
+             'amps': np.array([60.0, 40.0, 30.0]), 'amp_mix': 0, 'amp_mix_coeff': 0.0,
+             'bs': np.array([2.1, 2.0, 1.9]), 'b_mix': 0, 'b_mix_coeff': 0.0},
+        ]
+    elif variant == 'b':
+        spec['tr'] = ('switch3', 2.0 * A)
+        spec['pair'] = [
+            {'kind': 'qmdffrep', 'ffatype_ids': types.astype(np.int64),
+             'amp_cross': np.array([[90.0, 70.0, 60.0], [70.0, 50.0, 45.0], [60.0, 45.0, 40.0]]),
+             'b_cross': np.array([[2.2, 2.1, 2.0], [2.1, 2.0, 1.9], [2.0, 1.9, 1.8]])},
+            {'kind': 'ljcross', 'ffatype_ids': types.astype(np.int64),
+             'eps_cross': np.array([[0.5, 0.3, 0.4], [0.3, 0.2, 0.25], [0.4, 0.25, 0.35]]) * kjmol,
+             'sig_cross': np.array([[3.2, 3.0, 3.1], [3.0, 2.8, 2.9], [3.1, 2.9, 3.0]]) * A},
+            {'kind': 'dampdisp', 'ffatype_ids': types.astype(np.int64), 'power': 6,
+             'cn_cross': np.array([[30.0, 0.0, 20.0], [0.0, 15.0, 12.0], [20.0, 12.0, 10.0]]),
+             'b_cross': np.array([[1.8, 1.7, 0.0], [1.7, 1.6, 1.65], [0.0, 1.65, 1.5]]),
+             'cns': np.array([30.0, 15.0, 10.0]), 'vols': np.array([1.2, 1.0, 0.9]),
+             'bs': np.array([1.8, 1.6, 0.0])},
+        ]
+    else:
+        spec['tr'] = ('hammer', 0.8 * A)
+        spec['pair'] = [
+            {'kind': 'disp68bjdamp', 'ffatype_ids': types.astype(np.int64),
+             'c6_cross': np.array([[30.0, 22.0, 18.0], [22.0, 16.0, 13.0], [18.0, 13.0, 11.0]]),
+             'c8_cross': np.array([[900.0, 700.0, 600.0], [700.0, 520.0, 450.0], [600.0, 450.0, 400.0]]),
+             'R_cross': np.zeros((3, 3)), 'c6_scale': 1.0, 'c8_scale': 0.8, 'bj_a': 0.45, 'bj_b': 2.5},
+            {'kind': 'dampdisp', 'ffatype_ids': types.astype(np.int64), 'power': 8,
+             'cn_cross': np.array([[800.0, 600.0, 500.0], [600.0, 450.0, 400.0], [500.0, 400.0, 350.0]]),
+             'b_cross': np.array([[1.8, 0.0, 1.7], [0.0, 1.6, 0.0], [1.7, 0.0, 1.5]]),
+             'bs': np.array([1.8, 1.6, 1.5])},
+            {'kind': 'exprep', 'ffatype_ids': types.astype(np.int64),
+             'amp_cross': np.array([[0.0, 0.0, 45.0], [0.0, 0.0, 0.0], [45.0, 0.0, 0.0]]),
+             'b_cross': np.zeros((3, 3)),
+             'amps': np.array([60.0, 40.0, 30.0]), 'amp_mix': 1, 'amp_mix_coeff': 0.3,
+             'bs': np.array([2.1, 2.0, 1.9]), 'b_mix': 1, 'b_mix_coeff': 0.2},
+        ]
     return spec
 
 

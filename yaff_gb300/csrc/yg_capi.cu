@@ -266,8 +266,13 @@ int yg_destroy(yg_ctx *c) {
   if (c->ew_aux) cudaStreamDestroy(c->ew_aux);
   if (c->ew_fork_ev) cudaEventDestroy(c->ew_fork_ev);
   if (c->ew_join_ev) cudaEventDestroy(c->ew_join_ev);
-  if (c->pool)
+  if (c->pool) {
     for (void **b : bufs) yg_free(c, b);
+    for (int p = 0; p < YG_MAX_POT; p++) {
+      yg_free(c, (void **)&c->d_ptab64[p]);
+      yg_free(c, (void **)&c->d_ptab32[p]);
+    }
+  }
   pinned_put(c->h_block, c->h_block_bytes);
   delete c;
   return YG_OK;
@@ -401,13 +406,14 @@ int yg_set_pair_pot(yg_ctx *c, int slot, int kind, const double *sigma, const do
                     const int32_t *onlypauli, const double *radii, double alpha, double dielectric, double rcut,
                     int tr_kind, double tr_par) {
   if (!c || slot < 0 || slot >= YG_MAX_POT) return YG_ERR_ARG;
-  if (kind < YG_POT_LJ || kind > YG_POT_EI || tr_kind < YG_TR_NONE || tr_kind > YG_TR_SWITCH3) return YG_ERR_ARG;
+  if (kind < YG_POT_LJ || kind > YG_POT_GRIMME || tr_kind < YG_TR_NONE || tr_kind > YG_TR_SWITCH3) return YG_ERR_ARG;
   if (!(rcut > 0.0) || !(dielectric > 0.0)) {
     yg_set_error("rcut and dielectric must be positive");
     return YG_ERR_ARG;
   }
-  if ((kind == YG_POT_LJ || kind == YG_POT_MM3) && (!sigma || !epsilon)) return YG_ERR_ARG;
-  if (kind == YG_POT_MM3 && !onlypauli) return YG_ERR_ARG;
+  // Grimme: sigma = r0, epsilon = c6 (both mixed like MM3's, r0 summed, c6 geometric)
+  if (kind != YG_POT_EI && (!sigma || !epsilon)) return YG_ERR_ARG;
+  if ((kind == YG_POT_MM3 || kind == YG_POT_MM3CAP) && !onlypauli) return YG_ERR_ARG;
   PairPotHost &P = c->pot[slot];
   P = PairPotHost();
   P.active = 1;
@@ -438,6 +444,77 @@ int yg_set_pair_pot(yg_ctx *c, int slot, int kind, const double *sigma, const do
       for (int64_t i = 0; i < N; i++) P.radius2[i] = radii[i] * radii[i];
     }
   }
+  c->pp_dirty = 1;
+  if (c->have_list) return yg_pack_pair_params(c);
+  return YG_OK;
+}
+
+int yg_set_pair_table(yg_ctx *c, int slot, int kind, int64_t nffatype, const int64_t *ffatype_ids,
+                      const double *cross0, const double *cross1, const double *cross2, int64_t power,
+                      const double *scales, double rcut, int tr_kind, double tr_par) {
+  if (!c || slot < 0 || slot >= YG_MAX_POT) return YG_ERR_ARG;
+  if (kind < YG_POT_EXPREP || kind > YG_POT_DISP68BJ || tr_kind < YG_TR_NONE || tr_kind > YG_TR_SWITCH3)
+    return YG_ERR_ARG;
+  if (!(rcut > 0.0)) {
+    yg_set_error("rcut must be positive");
+    return YG_ERR_ARG;
+  }
+  if (nffatype <= 0 || nffatype > 4096 || !ffatype_ids || !cross0 || !cross1) return YG_ERR_ARG;
+  if (kind == YG_POT_DISP68BJ && (!cross2 || !scales)) return YG_ERR_ARG;
+  if (kind == YG_POT_DAMPDISP && (power < 0 || power > 30)) {
+    yg_set_error("DampDisp power must be in [0, 30]");
+    return YG_ERR_ARG;
+  }
+  const int64_t N = c->natom, nt = nffatype;
+  PairPotHost &P = c->pot[slot];
+  P = PairPotHost();
+  P.active = 1;
+  P.kind = kind;
+  P.tr_kind = tr_kind;
+  P.tr_par = tr_par;
+  P.rcut = rcut;
+  P.ntype = (int)nt;
+  P.power = (int)power;
+  P.types.resize(N);
+  for (int64_t i = 0; i < N; i++) {
+    if (ffatype_ids[i] < 0 || ffatype_ids[i] >= nt) {
+      yg_set_error("atom type index out of range");
+      P = PairPotHost();
+      return YG_ERR_ARG;
+    }
+    P.types[i] = (int32_t)ffatype_ids[i];
+  }
+  // Per type pair (a, b, c, d):
+  //   ExpRep, QMDFFRep: (amp, b, 0, 0); LJCross: (eps, sig, 0, 0);
+  //   DampDisp: (cn, b, 0, 0);
+  //   Disp68BJDamp: (c6_scale c6, c8_scale c8, R^6, R^8), R = bj_a R_cross + bj_b.
+  P.table.assign((size_t)nt * nt * 4, 0.0);
+  for (int64_t k = 0; k < nt * nt; k++) {
+    double *t = P.table.data() + 4 * k;
+    if (kind == YG_POT_DISP68BJ) {
+      const double R = scales[2] * cross2[k] + scales[3];
+      const double R2 = R * R, R4 = R2 * R2;
+      t[0] = scales[0] * cross0[k];
+      t[1] = scales[1] * cross1[k];
+      t[2] = R4 * R2;
+      t[3] = R4 * R4;
+    } else {
+      t[0] = cross0[k];
+      t[1] = cross1[k];
+    }
+  }
+  yg_free(c, (void **)&c->d_ptab64[slot]);
+  yg_free(c, (void **)&c->d_ptab32[slot]);
+  int rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_ptab64[slot], (size_t)nt * nt * sizeof(double4_32a)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_ptab32[slot], (size_t)nt * nt * sizeof(float4)))) return rc;
+  std::vector<float> t32(P.table.size());
+  for (size_t k = 0; k < t32.size(); k++) t32[k] = (float)P.table[k];
+  YG_CUDA(cudaMemcpyAsync(c->d_ptab64[slot], P.table.data(), P.table.size() * sizeof(double), cudaMemcpyHostToDevice,
+                          c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->d_ptab32[slot], t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice,
+                          c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
   c->pp_dirty = 1;
   if (c->have_list) return yg_pack_pair_params(c);
   return YG_OK;

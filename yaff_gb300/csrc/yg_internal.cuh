@@ -58,6 +58,11 @@ struct PairPotHost {
   double dielectric = 1.0;
   std::vector<double> sigma, sqrteps, radius2;
   std::vector<int32_t> onlypauli;
+  // type-pair table kinds: per-atom type, per type pair (a, b, c, d)
+  int ntype = 0;
+  int power = 0;
+  std::vector<int32_t> types;
+  std::vector<double> table;
 };
 
 // Parameters of one pair potential as the pair kernel sees them.
@@ -71,6 +76,10 @@ struct PairPotDev {
   double inv_diel;
   int has_radii;
   int col;        // parameter column (= result slot) of this potential
+  int ntype;      // type-pair table kinds: number of atom types
+  int power;      // DampDisp: power of 1/d
+  const double4_32a *tab64;  // ntype*ntype entries (FP64)
+  const float4 *tab32;       // same, FP32
 };
 
 // Resident-block count of a kernel at a dynamic shared-memory size (cached).
@@ -159,6 +168,8 @@ struct yg_ctx {
   double *d_pp_src = nullptr;     // orig*4*YG_MAX_POT: sigma, sqrt(eps), radius^2, onlypauli
   double *d_pp64 = nullptr;       // same in sorted order
   float *d_pp32 = nullptr;        // same, FP32
+  double4_32a *d_ptab64[YG_MAX_POT] = {nullptr, nullptr, nullptr};  // type-pair tables per slot
+  float4 *d_ptab32[YG_MAX_POT] = {nullptr, nullptr, nullptr};
   int pp_dirty = 1;
   int pp_packed = 0;
 

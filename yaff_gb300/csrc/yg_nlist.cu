@@ -686,7 +686,7 @@ int yg_pack_pair_params(yg_ctx *ctx) {
       if (!P.active) continue;
       for (int64_t a = 0; a < ctx->natom; a++) {
         double *q = h.data() + (size_t)a * 4 * YG_MAX_POT + 4 * p;
-        q[0] = P.sigma.empty() ? 0.0 : P.sigma[a];
+        q[0] = !P.types.empty() ? (double)P.types[a] : P.sigma.empty() ? 0.0 : P.sigma[a];
         q[1] = P.sqrteps.empty() ? 0.0 : P.sqrteps[a];
         q[2] = P.radius2.empty() ? 0.0 : P.radius2[a];
         q[3] = P.onlypauli.empty() ? 0.0 : (double)P.onlypauli[a];

@@ -506,6 +506,10 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
     D.inv_diel = 1.0 / P.dielectric;
     D.has_radii = !P.radius2.empty();
     D.col = p;
+    D.ntype = P.ntype;
+    D.power = P.power;
+    D.tab64 = ctx->d_ptab64[p];
+    D.tab32 = ctx->d_ptab32[p];
     slots[npot] = p;
     npot++;
   }

@@ -18,15 +18,121 @@ template <> struct Num<float> {
   static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
 };
 
+// Entry (a, b, c, d) of a type-pair table in the precision of the caller.
+template <typename T> struct TabEntry;
+template <> struct TabEntry<double> {
+  static __device__ __forceinline__ double4_32a get(const PairPotDev &P, int k) { return P.tab64[k]; }
+};
+template <> struct TabEntry<float> {
+  static __device__ __forceinline__ float4 get(const PairPotDev &P, int k) { return P.tab32[k]; }
+};
+
+// Kinds beyond LJ / MM3 / EI: MM3CAP and Grimme (per-atom parameters), and
+// the type-pair table kinds.  Formulas of yaff/pes/pair_pot.c:373-419
+// (MM3CAP, including its force below the cap, which the reference takes from
+// the unmodified MM3 expression at the cap's x), :434-455 (Grimme), :473-489
+// (ExpRep), :506-522 (QMDFFRep), :540-557 (LJCross), :576-629 (DampDisp with
+// the Tang-Toennies damping) and :651-677 (Disp68BJDamp).
+template <typename T>
+__device__ __noinline__ void pair_term_more(const PairPotDev &P, T d, T d2, T pi0, T pi1, T pi3, T pj0, T pj1,
+                                            T pj3, T &v, T &g) {
+  typedef Num<T> M;
+  if (P.kind == YG_POT_MM3CAP) {
+    const T sig = pi0 + pj0, eps = pi1 * pj1;
+    T x = d / sig;
+    if (pi3 + pj3 == (T)0) {
+      const T xmax = (T)0.355114;
+      const T xc = x > xmax ? x : xmax;
+      const T ex = (T)1.84e5 * M::exp_((T)-12.0 * xc);
+      T x6 = xc * xc;
+      x6 = x6 * x6 * x6 / (T)2.25;
+      g = eps / d * ((T)-12.0 / sig * ex + (T)6.0 / d / x6);
+      v = x > xmax ? eps * (ex - (T)1 / x6) : eps * ((T)5799.303156 - (T)12182.86986 * x);
+    } else {
+      const T ex = (T)1.84e5 * M::exp_((T)-12.0 * x);
+      g = eps / d * ((T)-12.0 / sig * ex);
+      v = eps * ex;
+    }
+    return;
+  }
+  if (P.kind == YG_POT_GRIMME) {
+    const T r0 = pi0 + pj0, c6 = pi1 * pj1;
+    const T ex = M::exp_((T)-20.0 * (d / r0 - (T)1.0));
+    const T f = (T)1.0 / ((T)1.0 + ex);
+    const T d6 = d2 * d2 * d2;
+    const T e = (T)1.1 * f * c6 / d6;
+    g = e / d * ((T)6.0 / d - (T)20.0 / r0 * f * ex);
+    v = -e;
+    return;
+  }
+  const auto t = TabEntry<T>::get(P, (int)pi0 * P.ntype + (int)pj0);
+  v = (T)0;
+  g = (T)0;
+  switch (P.kind) {
+    case YG_POT_EXPREP:
+      if (t.x != (T)0 && t.y != (T)0) {
+        v = t.x * M::exp_(-t.y * d);
+        g = -v * t.y / d;
+      }
+      break;
+    case YG_POT_QMDFFREP:
+      if (t.x != (T)0 && t.y != (T)0) {
+        v = t.x / d * M::exp_(-t.y * d);
+        g = -(t.y + (T)1 / d) * v / d;
+      }
+      break;
+    case YG_POT_LJCROSS: {
+      T x = t.y / d;
+      x *= x;
+      x *= x * x;
+      g = (T)24.0 * t.x / d2 * x * ((T)1.0 - (T)2.0 * x);
+      v = (T)4.0 * t.x * (x * (x - (T)1.0));
+      break;
+    }
+    case YG_POT_DAMPDISP: {
+      if (t.x == (T)0) break;
+      T dn = (T)1;
+      for (int j = 0; j < P.power; j++) dn *= d;
+      const T disp = -t.x / dn;
+      if (t.y == (T)0) {
+        v = disp;
+        g = -(T)P.power * disp / d2;
+      } else {
+        // 1 - exp(-x) sum_{k<=n} x^k / k!, x = b d, and its x-derivative
+        const T x = t.y * d;
+        T term = (T)1, poly = (T)1;
+        for (int k = 1; k <= P.power; k++) {
+          term = term * x / (T)k;
+          poly += term;
+        }
+        const T e = M::exp_(-x);
+        const T damp = (T)1 - poly * e;
+        g = (e * term * t.y - (T)P.power / d * damp) * disp / d;
+        v = damp * disp;
+      }
+      break;
+    }
+    default: {  // YG_POT_DISP68BJ: (s6 c6, s8 c8, R^6, R^8)
+      const T d4 = d2 * d2, d6 = d4 * d2, d8 = d4 * d4;
+      const T u6 = (T)1 / (d6 + t.z), u8 = (T)1 / (d8 + t.w);
+      v = -t.x * u6 - t.y * u8;
+      g = (T)6.0 * t.x * u6 * u6 * d4 + (T)8.0 * t.y * u8 * u8 * d6;
+      break;
+    }
+  }
+}
+
 // Energy v and g = (dv/dd)/d of one pair for one potential, truncation
 // included.  Formulas of yaff/pes/pair_pot.c:277-301 (LJ), :321-352 (MM3),
-// :711-751 (EI) and truncation.c:30-76.
+// :711-751 (EI) and truncation.c:30-76; the other kinds in pair_term_more.
 template <typename T>
 __device__ __forceinline__ void pair_term(const PairPotDev &P, T rcT, T parT, T alphaT, T invdT, T d, T d2, T pi0,
                                           T pi1, T pi2, T pi3, T pj0, T pj1, T pj2, T pj3, T qi, T qj, T &v, T &g) {
   typedef Num<T> M;
   const T two_div_sqrt_pi = (T)1.1283791670955125739;
-  if (P.kind == YG_POT_LJ) {
+  if (P.kind > YG_POT_EI) {
+    pair_term_more<T>(P, d, d2, pi0, pi1, pi3, pj0, pj1, pj3, v, g);
+  } else if (P.kind == YG_POT_LJ) {
     T sig = (T)0.5 * (pi0 + pj0);
     T eps = pi1 * pj1;
     T x = sig / d;
@@ -150,7 +256,7 @@ static __device__ __forceinline__ void pair_term_f32(const PairPotDev &P, float 
       }
       return;
     }
-    if (alphaT > 0.0f && pi2 + pj2 == 0.0f) {
+    if (P.kind == YG_POT_EI && alphaT > 0.0f && pi2 + pj2 == 0.0f) {
       const float qq = qi * qj * invdT;
       const float x = alphaT * d;
       const float e = expf(-x * x);

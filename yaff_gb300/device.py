@@ -148,13 +148,20 @@ class DeviceSystem(object):
         slot = len(self.pair_slots)
         self.pair_slots.append(part)
         pp = part.pair_pot
-        arrs = pp._device_arrays(self.natom)
         tr = pp.get_truncation()
         trk, trp = (_lib.TR_NONE, 0.0) if tr is None else (tr.kind, tr.par)
-        check(self.lib.yg_set_pair_pot(self.ctx, slot, pp.kind, ptr(arrs['sigma']), ptr(arrs['epsilon']),
-                                       ptr(arrs['onlypauli']), ptr(arrs['radii']), float(arrs['alpha']),
-                                       float(arrs['dielectric']), float(pp.rcut), trk, float(trp)),
-              'yg_set_pair_pot')
+        if getattr(pp, 'type_table', False):
+            t = pp._device_table(self.natom)
+            check(self.lib.yg_set_pair_table(self.ctx, slot, pp.kind, len(t['cross0']), ptr(t['ffatype_ids']),
+                                             ptr(t['cross0']), ptr(t['cross1']), ptr(t['cross2']),
+                                             int(t['power']), ptr(t['scales']), float(pp.rcut), trk, float(trp)),
+                  'yg_set_pair_table')
+        else:
+            arrs = pp._device_arrays(self.natom)
+            check(self.lib.yg_set_pair_pot(self.ctx, slot, pp.kind, ptr(arrs['sigma']), ptr(arrs['epsilon']),
+                                           ptr(arrs['onlypauli']), ptr(arrs['radii']), float(arrs['alpha']),
+                                           float(arrs['dielectric']), float(pp.rcut), trk, float(trp)),
+                  'yg_set_pair_pot')
         if pp.kind == _lib.POT_EI:
             self.sync_charges()
         return slot

@@ -2,7 +2,10 @@
 
 Same constructors, names and attributes as the reference's extension classes
 (yaff/pes/ext.pyx:524-620 Hammer/Switch3, :747-819 PairPotLJ, :822-908
-PairPotMM3, :1770-1857 PairPotEI).  The evaluation itself happens on the GPU
+PairPotMM3, :911-997 PairPotMM3CAP, :1000-1035 PairPotGrimme, :1038-1194
+PairPotExpRep, :1197-1354 PairPotQMDFFRep, :1357-1443 PairPotLJCross,
+:1446-1590 PairPotDampDisp, :1593-1767 PairPotDisp68BJDamp, :1770-1857
+PairPotEI), including the mixing rules that fill the type-pair tables.  The evaluation itself happens on the GPU
 through ForcePartPair; ``compute`` on a rows array is not offered (the device
 list never leaves the GPU in the hot path).
 """
@@ -10,7 +13,9 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ['Truncation', 'Hammer', 'Switch3', 'PairPot', 'PairPotLJ', 'PairPotMM3', 'PairPotEI']
+__all__ = ['Truncation', 'Hammer', 'Switch3', 'PairPot', 'PairPotLJ', 'PairPotMM3', 'PairPotEI', 'PairPotMM3CAP',
+           'PairPotGrimme', 'PairPotExpRep', 'PairPotQMDFFRep', 'PairPotLJCross', 'PairPotDampDisp',
+           'PairPotDisp68BJDamp']
 
 
 class Truncation(object):
@@ -141,3 +146,201 @@ class PairPotEI(PairPot):
         assert len(self.charges) == natom
         return {'sigma': None, 'epsilon': None, 'onlypauli': None, 'radii': self.radii,
                 'alpha': self.alpha, 'dielectric': self.dielectric}
+
+
+class PairPotMM3CAP(PairPotMM3):
+    """MM3 with the energy capped linearly below d = 0.355114 sigma_ij (for
+    Monte Carlo insertions); above the cap identical to MM3."""
+    name = 'mm3cap'
+    kind = _lib.POT_MM3CAP
+
+
+class PairPotGrimme(PairPot):
+    """-1.1 f(d) c6_ij / d^6 with f = 1/(1 + exp(-20 (d/r0_ij - 1))),
+    r0_ij = r0_i + r0_j, c6_ij = sqrt(c6_i c6_j)."""
+    name = 'grimme'
+    kind = _lib.POT_GRIMME
+
+    def __init__(self, r0, c6, rcut, tr=None):
+        PairPot.__init__(self, rcut, tr)
+        self.r0 = np.ascontiguousarray(r0, dtype=np.float64)
+        self.c6 = np.ascontiguousarray(c6, dtype=np.float64)
+        if self.r0.shape != self.c6.shape:
+            raise TypeError('r0 and c6 must have the same shape')
+
+    def _device_arrays(self, natom):
+        assert len(self.r0) == natom
+        return {'sigma': self.r0, 'epsilon': self.c6, 'onlypauli': None, 'radii': None,
+                'alpha': 0.0, 'dielectric': 1.0}
+
+
+class _TypeTablePot(PairPot):
+    """A pair potential whose parameters are tables over pairs of atom types."""
+    type_table = True
+
+    def __init__(self, ffatype_ids, rcut, tr):
+        PairPot.__init__(self, rcut, tr)
+        self.ffatype_ids = np.ascontiguousarray(ffatype_ids, dtype=np.int64)
+
+    @staticmethod
+    def _square(a, n=None):
+        a = np.array(a, dtype=np.float64, order='C')
+        if a.ndim != 2 or a.shape[0] != a.shape[1] or (n is not None and a.shape[0] != n):
+            raise TypeError('cross-parameter tables must be square, one row per atom type')
+        return a
+
+    def _check_types(self, n):
+        if len(self.ffatype_ids) and (self.ffatype_ids.min() < 0 or self.ffatype_ids.max() >= n):
+            raise ValueError('atom type index out of range')
+
+    def _device_table(self, natom):
+        assert len(self.ffatype_ids) == natom
+        return {'ffatype_ids': self.ffatype_ids, 'cross0': self._cross[0], 'cross1': self._cross[1],
+                'cross2': self._cross[2] if len(self._cross) > 2 else None, 'power': getattr(self, 'power', 0),
+                'scales': getattr(self, '_scales', None)}
+
+
+class _RepPot(_TypeTablePot):
+    def __init__(self, ffatype_ids, amp_cross, b_cross, rcut, tr=None, amps=None, amp_mix=-1, amp_mix_coeff=-1,
+                 bs=None, b_mix=-1, b_mix_coeff=-1):
+        _TypeTablePot.__init__(self, ffatype_ids, rcut, tr)
+        amp_cross = self._square(amp_cross)
+        n = amp_cross.shape[0]
+        b_cross = self._square(b_cross, n)
+        self._check_types(n)
+        if amps is not None:
+            amps = np.asarray(amps, dtype=np.float64)
+            if len(amps) != n or amp_mix not in (0, 1) or not 0 <= amp_mix_coeff <= 1:
+                raise ValueError('invalid amplitude mixing arguments')
+            self._mix_amp(n, amp_cross, amps, amp_mix, amp_mix_coeff)
+        if not (amp_cross == amp_cross.T).all():
+            raise ValueError('amp_cross must be symmetric')
+        if bs is not None:
+            bs = np.asarray(bs, dtype=np.float64)
+            if len(bs) != n or b_mix not in (0, 1) or not 0 <= b_mix_coeff <= 1:
+                raise ValueError('invalid decay mixing arguments')
+            self._mix_b(n, b_cross, bs, b_mix, b_mix_coeff, amps)
+        if not (b_cross == b_cross.T).all():
+            raise ValueError('b_cross must be symmetric')
+        self.amp_cross = amp_cross
+        self.b_cross = b_cross
+        self._cross = (amp_cross, b_cross)
+
+    @staticmethod
+    def _mix_amp(n, amp_cross, amps, amp_mix, coeff):
+        # unset (zero) entries: geometric mean (amp_mix 0) or the corrected
+        # geometric rule ln A_ij = (ln A_i + ln A_j)/2 (1 - x |ln(A_i/A_j)|)
+        for i0 in range(n):
+            for i1 in range(i0 + 1):
+                if amp_cross[i0, i1] == 0.0:
+                    if amp_mix == 0:
+                        amp_cross[i0, i1] = np.sqrt(amps[i0] * amps[i1])
+                    elif amps[i0] != 0.0 and amps[i1] != 0.0:
+                        a = (np.log(amps[i0]) + np.log(amps[i1])) / 2
+                        a *= 1 - coeff * abs(np.log(amps[i0] / amps[i1]))
+                        amp_cross[i0, i1] = np.exp(a)
+                    amp_cross[i1, i0] = amp_cross[i0, i1]
+
+    @staticmethod
+    def _mix_b(n, b_cross, bs, b_mix, coeff, amps):
+        # unset entries: arithmetic mean (b_mix 0) or the corrected rule
+        # B_ij = (B_i + B_j)/2 (1 - x |ln(A_i/A_j)|)
+        for i0 in range(n):
+            for i1 in range(i0 + 1):
+                if b_cross[i0, i1] == 0.0:
+                    if b_mix == 0:
+                        b_cross[i0, i1] = (bs[i0] + bs[i1]) / 2
+                    elif amps[i0] != 0.0 and amps[i1] != 0.0:
+                        b = (bs[i0] + bs[i1]) / 2
+                        b *= 1 - coeff * abs(np.log(amps[i0] / amps[i1]))
+                        b_cross[i0, i1] = b
+                    b_cross[i1, i0] = b_cross[i0, i1]
+
+
+class PairPotExpRep(_RepPot):
+    """A_ij exp(-B_ij d) over atom-type pairs."""
+    name = 'exprep'
+    kind = _lib.POT_EXPREP
+
+
+class PairPotQMDFFRep(_RepPot):
+    """A_ij exp(-B_ij d) / d over atom-type pairs."""
+    name = 'qmdffrep'
+    kind = _lib.POT_QMDFFREP
+
+
+class PairPotLJCross(_TypeTablePot):
+    """4 eps_ij ((sig_ij/d)^12 - (sig_ij/d)^6) over atom-type pairs."""
+    name = 'ljcross'
+    kind = _lib.POT_LJCROSS
+
+    def __init__(self, ffatype_ids, eps_cross, sig_cross, rcut, tr=None):
+        _TypeTablePot.__init__(self, ffatype_ids, rcut, tr)
+        self.eps_cross = self._square(eps_cross)
+        self.sig_cross = self._square(sig_cross, self.eps_cross.shape[0])
+        self._check_types(self.eps_cross.shape[0])
+        self._cross = (self.eps_cross, self.sig_cross)
+
+
+class PairPotDampDisp(_TypeTablePot):
+    """-C_ij f_n(B_ij d) / d^n with the Tang-Toennies damping f_n (undamped
+    where B_ij = 0), over atom-type pairs."""
+    name = 'dampdisp'
+    kind = _lib.POT_DAMPDISP
+
+    def __init__(self, ffatype_ids, cn_cross, b_cross, rcut, tr=None, cns=None, bs=None, vols=None, power=6):
+        _TypeTablePot.__init__(self, ffatype_ids, rcut, tr)
+        cn_cross = self._square(cn_cross)
+        n = cn_cross.shape[0]
+        b_cross = self._square(b_cross, n)
+        self._check_types(n)
+        if cns is not None or vols is not None:
+            if cns is None or vols is None:
+                raise ValueError('cns and vols are needed together')
+            cns = np.asarray(cns, dtype=np.float64)
+            vols = np.asarray(vols, dtype=np.float64)
+            # unset entries: 2 C_i C_j / (C_i v_j/v_i + C_j v_i/v_j)
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if cn_cross[i0, i1] == 0.0 and vols[i0] != 0.0 and vols[i1] != 0.0:
+                        ratio = vols[i0] / vols[i1]
+                        cn_cross[i0, i1] = 2.0 * cns[i0] * cns[i1] / (cns[i0] / ratio + cns[i1] * ratio)
+                        cn_cross[i1, i0] = cn_cross[i0, i1]
+        if bs is not None:
+            bs = np.asarray(bs, dtype=np.float64)
+            for i0 in range(n):
+                for i1 in range(i0 + 1):
+                    if b_cross[i0, i1] == 0.0 and bs[i0] != 0.0 and bs[i1] != 0.0:
+                        b_cross[i0, i1] = 0.5 * (bs[i0] + bs[i1])
+                        b_cross[i1, i0] = b_cross[i0, i1]
+        if not 0 <= int(power) <= 30:
+            raise ValueError('power must be in [0, 30]')
+        self.power = int(power)
+        self.cn_cross = cn_cross
+        self.b_cross = b_cross
+        self._cross = (cn_cross, b_cross)
+
+
+class PairPotDisp68BJDamp(_TypeTablePot):
+    """-s6 C6_ij / (d^6 + R^6) - s8 C8_ij / (d^8 + R^8), R = a R_ij + b
+    (Becke-Johnson damping), over atom-type pairs."""
+    name = 'disp68bjdamp'
+    kind = _lib.POT_DISP68BJ
+
+    def __init__(self, ffatype_ids, c6_cross, c8_cross, R_cross, rcut, tr=None, c6s=None, c8s=None, Rs=None,
+                 c6_scale=1.0, c8_scale=1.0, bj_a=0.0, bj_b=0.0):
+        _TypeTablePot.__init__(self, ffatype_ids, rcut, tr)
+        c6_cross = self._square(c6_cross)
+        n = c6_cross.shape[0]
+        c8_cross = self._square(c8_cross, n)
+        R_cross = self._square(R_cross, n)
+        self._check_types(n)
+        if c6s is not None or c8s is not None or Rs is not None:
+            raise NotImplementedError('per-type c6s / c8s / Rs mixing is not defined for this potential')
+        if np.all(R_cross == 0.0):
+            mask = c6_cross != 0.0
+            R_cross[mask] = np.sqrt(c8_cross[mask] / c6_cross[mask])
+        self.c6_cross, self.c8_cross, self.R_cross = c6_cross, c8_cross, R_cross
+        self.c6_scale, self.c8_scale, self.bj_a, self.bj_b = float(c6_scale), float(c8_scale), float(bj_a), float(bj_b)
+        self._cross = (c6_cross, c8_cross, R_cross)
+        self._scales = np.array([self.c6_scale, self.c8_scale, self.bj_a, self.bj_b])
