@@ -76,6 +76,10 @@ def build_reference_ff(spec):
             for term in terms_from_rows(vr, icc, tcc):
                 pv.add_term(term)
         parts.append(pv)
+    if spec.get('tailcorr', False):
+        from yaff.pes.ff import ForcePartTailCorrection
+        for part in [q for q in parts if isinstance(q, ForcePartPair) and q.name != 'pair_ei']:
+            parts.append(ForcePartTailCorrection(system, part, spec.get('nlow', 0), spec.get('nhigh', -1)))
     ff = ForceField(system, parts, nlist)
     ff._borrowed_arrays = keep
     return ff

@@ -96,6 +96,10 @@ def run_case(name, spec, displacements=(), full_rows=True):
         data['step%d_part_energy' % s] = np.array([p.energy for p in ff.parts])
         data['step%d_part_gpos' % s] = np.array([p.gpos for p in ff.parts])
         data['step%d_part_vtens' % s] = np.array([p.vtens for p in ff.parts])
+        for p in ff.parts:
+            if p.name.startswith('tailcorr_'):
+                data['%s_ecorr' % p.name] = np.array(p.ecorr)
+                data['%s_wcorr' % p.name] = np.array(p.wcorr)
         keys, vals = pair_keys(ff.nlist)
         data['step%d_nneigh' % s] = np.array(ff.nlist.nneigh)
         data['step%d_pairs_sha256' % s] = np.array(keys_digest(keys))
@@ -210,6 +214,10 @@ def main():
     for var in 'abc':
         pp = configs.pair_potentials(var)
         run_case(pp['name'], pp, displacements=[rng.uniform(-0.05, 0.05, (300, 3)) * angstrom])
+
+    for var in ('a', 'b', 'c', 'lj', 'mm3'):
+        tc = configs.tail_corrections(var)
+        run_case(tc['name'], tc)
 
 
 if __name__ == '__main__':

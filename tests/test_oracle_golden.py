@@ -32,13 +32,18 @@ def test_oracle_matches_reference(name):
             assert np.array_equal(keys, data['step%d_pair_keys' % s].astype(np.int64))
             vals = np.stack([rows['d'], rows['dx'], rows['dy'], rows['dz']], 1)
             assert np.array_equal(vals, data['step%d_pair_vals' % s])
-        ref_e = float(data['step%d_energy' % s])
+        names = [str(x) for x in data['step%d_parts' % s]]
+        # tail corrections are host scalars of the product, checked against
+        # the reference in test_tailcorr.py; the oracle covers the rest
+        tail = [k for k, nm in enumerate(names) if nm.startswith('tailcorr_')]
+        ref_e = float(data['step%d_energy' % s]) - sum(data['step%d_part_energy' % s][k] for k in tail)
+        ref_v = data['step%d_vtens' % s] - sum((data['step%d_part_vtens' % s][k] for k in tail), np.zeros((3, 3)))
         assert abs(e - ref_e) <= 1e-13 * max(1.0, abs(ref_e))
         assert np.allclose(gpos, data['step%d_gpos' % s], rtol=0, atol=1e-13 * max(1, abs(data['step%d_gpos' % s]).max()))
-        assert np.allclose(vtens, data['step%d_vtens' % s], rtol=0, atol=1e-13 * max(1, abs(data['step%d_vtens' % s]).max()))
-        names = [str(x) for x in data['step%d_parts' % s]]
+        assert np.allclose(vtens, ref_v, rtol=0, atol=1e-13 * max(1, abs(data['step%d_vtens' % s]).max()))
         for k, nm in enumerate(names):
-            assert orc.part_energies[nm] == data['step%d_part_energy' % s][k], nm
+            if k not in tail:
+                assert orc.part_energies[nm] == data['step%d_part_energy' % s][k], nm
 
 
 def test_fixture_set_complete():

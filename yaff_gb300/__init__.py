@@ -21,7 +21,7 @@ from .valence import (Bond, BendCos, BendAngle, DihedCos, DihedAngle, UreyBradle
                       Chebychev2, Chebychev3, Chebychev4, Chebychev6, PolySix, MM3Quartic, MM3Bend,
                       BondDoubleWell, Morse, Poly4)
 from .ff import (ForcePart, ForceField, ForcePartPair, ForcePartEwaldReciprocal, ForcePartEwaldCorrection,
-                 ForcePartEwaldNeutralizing, ForcePartValence)
+                 ForcePartEwaldNeutralizing, ForcePartTailCorrection, ForcePartValence)
 from .device import DeviceSystem, device_of, set_default_precision, get_default_precision
 from .builder import build_system, build_forcefield
 from .verlet import VerletIntegrator, DeviceVerlet, get_random_vel

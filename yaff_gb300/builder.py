@@ -4,7 +4,7 @@ import numpy as np
 
 from .device import device_of
 from .ff import (ForceField, ForcePartPair, ForcePartEwaldReciprocal, ForcePartEwaldCorrection,
-                 ForcePartEwaldNeutralizing, ForcePartValence)
+                 ForcePartEwaldNeutralizing, ForcePartTailCorrection, ForcePartValence)
 from .nlist import NeighborList
 from . import pair as _pair
 from .pair import Switch3, Hammer
@@ -117,4 +117,9 @@ def build_forcefield(spec, precision=None, system=None, stream=None):
         for term in terms_from_rows(vr if vr is not None else np.zeros((0, 17))):
             pv.add_term(term)
         parts.append(pv)
+    if spec.get('tailcorr', False):
+        # after every other part, as the reference generator appends them
+        # (yaff/pes/generator.py:2209-2223)
+        for part in [q for q in parts if isinstance(q, ForcePartPair) and q.name != 'pair_ei']:
+            parts.append(ForcePartTailCorrection(system, part, spec.get('nlow', 0), spec.get('nhigh', -1)))
     return ForceField(system, parts, nlist)

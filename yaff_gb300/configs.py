@@ -32,6 +32,7 @@ bend_terms     (nat, 5): i, j, k, K, th0  harmonic bends (BendAngle + Harmonic)
 valence        (nv, 17) packed valence terms: term kind, par0..par5, then
                per internal coordinate its kind and 4 atoms (-1 unused)
 nlow, nhigh    ints (nhigh = -1 means N)
+tailcorr       bool (optional): a tail correction per non-EI pair part
 """
 import hashlib
 import math
@@ -339,6 +340,32 @@ def pair_potentials(variant='a', natom=300, box=16.0, dmin=1.5, rcut=7.0, skin=0
              'amps': np.array([60.0, 40.0, 30.0]), 'amp_mix': 1, 'amp_mix_coeff': 0.3,
              'bs': np.array([2.1, 2.0, 1.9]), 'b_mix': 1, 'b_mix_coeff': 0.2},
         ]
+    return spec
+
+
+def tail_corrections(variant='a'):
+    """Small boxes with a tail correction per non-electrostatic pair part:
+    'a' the MM3CAP / Grimme / ExpRep box untruncated (150 atoms, nlow 20,
+    nhigh 130), 'b' the QMDFFRep / LJCross / DampDisp(7) box with Switch3, 'c'
+    the Disp68BJDamp / DampDisp(8) / ExpRep box with Switch3 instead of
+    Hammer, 'lj' the 216-atom LJ + EI lattice untruncated (rcut 6 A), 'mm3'
+    a 200-atom triclinic MM3 + EI box with Switch3 (2 A)."""
+    if variant in ('a', 'b', 'c'):
+        spec = pair_potentials(variant, natom=150, name='tailcorr%s150' % variant)
+        if variant == 'a':
+            spec['nlow'], spec['nhigh'] = 20, 130
+        if variant == 'b':
+            # the reference's Switch3 tail integral of DampDisp divides by
+            # (power - 6) (tailcorr.c:555-594), NaN at power 6
+            spec['pair'][2]['power'] = 7
+        if variant == 'c':
+            spec['tr'] = ('switch3', 1.5 * angstrom)
+    elif variant == 'lj':
+        spec = lattice_lj_ei(nside=6, spacing=2.5, rcut=6.0, name='tailcorrlj216')
+    else:
+        spec = triclinic_mm3_ei(natom=200, rcut=6.0, skin=0.5, name='tailcorrmm3200')
+        spec['tr'] = ('switch3', 2.0 * angstrom)
+    spec['tailcorr'] = True
     return spec
 
 

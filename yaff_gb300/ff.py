@@ -24,7 +24,7 @@ from .device import device_of
 from .valence import DeltaList, InternalCoordinateList, ValenceList
 
 __all__ = ['ForcePart', 'ForceField', 'ForcePartPair', 'ForcePartEwaldReciprocal', 'ForcePartEwaldCorrection',
-           'ForcePartEwaldNeutralizing', 'ForcePartValence']
+           'ForcePartEwaldNeutralizing', 'ForcePartTailCorrection', 'ForcePartValence']
 
 
 class ForcePart(object):
@@ -161,7 +161,7 @@ class ForceField(ForcePart):
         """The device system when every part can run fused on it, else None."""
         dev = None
         for part in self.parts:
-            if part.device_slot is None and not isinstance(part, ForcePartEwaldNeutralizing):
+            if part.device_slot is None and not getattr(part, 'host_scalar', False):
                 return None
         if self.system.cell.nvec != 3:
             return None
@@ -199,7 +199,7 @@ class ForceField(ForcePart):
         host_energy = 0.0
         host_vtens = np.zeros((3, 3)) if vtens is not None else None
         for part in self.parts:
-            if isinstance(part, (ForcePartPair, ForcePartEwaldNeutralizing, ForcePartEwaldReciprocal)):
+            if isinstance(part, (ForcePartPair, ForcePartEwaldReciprocal)) or getattr(part, 'host_scalar', False):
                 continue
             part._launch(want_grad)
             mask |= 1 << part.device_slot
@@ -212,8 +212,8 @@ class ForceField(ForcePart):
             energy, part_e = dev.get_total_into(mask, gpos, vtens)
         self._total_mask = mask
         for part in self.parts:
-            if isinstance(part, ForcePartEwaldNeutralizing):
-                # position independent, no gradient (ff.py:653-669)
+            if getattr(part, 'host_scalar', False):
+                # position independent, no gradient (ff.py:653-669, :1052-1058)
                 pv = np.zeros((3, 3)) if vtens is not None else None
                 e = part._internal_compute(None, pv)
                 part.energy = e
@@ -268,15 +268,15 @@ class ForceField(ForcePart):
     def device_md_terms(self):
         """(result-slot mask, constant energy) for an integrator that sums the
         force on the device: the slots the fused path fills, and the
-        neutralizing-background energy, which is evaluated on the host and
-        does not depend on the positions.  Valid after one compute()."""
+        energy of the host-evaluated parts (neutralizing background, tail
+        corrections), which does not depend on the positions.  Valid after one compute()."""
         dev = self._device_parts()
         if dev is None:
             raise NotImplementedError('the on-device integrator needs every part on the fused device path')
         mask = 0
         const = 0.0
         for part in self.parts:
-            if isinstance(part, ForcePartEwaldNeutralizing):
+            if getattr(part, 'host_scalar', False):
                 const += part.compute()
             elif isinstance(part, ForcePartPair):
                 mask |= 1 << part._register()
@@ -418,6 +418,7 @@ class ForcePartEwaldCorrection(ForcePart):
 class ForcePartEwaldNeutralizing(ForcePart):
     """Neutralizing-background term of a charged periodic system (host FP64,
     yaff/pes/ff.py:590-669)."""
+    host_scalar = True
 
     def __init__(self, system, alpha, dielectric=1.0, nlow=0, nhigh=-1, fluctuating_charges=False):
         ForcePart.__init__(self, 'ewald_neut', system)
@@ -452,6 +453,32 @@ class ForcePartEwaldNeutralizing(ForcePart):
         if vtens is not None:
             vtens.ravel()[::4] -= fac
         return fac
+
+
+class ForcePartTailCorrection(ForcePart):
+    """Long-range correction of a truncated pair potential, assuming a
+    homogeneous system beyond the cutoff: energy 2 pi C0 / V and virial
+    diagonal 2 pi C1 / V, with C0 and C1 summed once over atom pairs by
+    ``pair_pot.prepare_tailcorrections`` (yaff/pes/ff.py:1012-1058).  Host
+    FP64 scalars, no gradient; the energy depends on the volume only."""
+    host_scalar = True
+
+    def __init__(self, system, part_pair, nlow=0, nhigh=-1):
+        if system.cell.nvec != 3:
+            raise ValueError('Tail corrections can only be applied to 3D periodic systems')
+        if part_pair.name in ['pair_ei', 'pair_eidip']:
+            raise ValueError('Tail corrections are divergent for %s' % part_pair.name)
+        ForcePart.__init__(self, 'tailcorr_%s' % part_pair.name, system)
+        self.nlow, self.nhigh = _check_nlow_nhigh(system, nlow, nhigh)
+        self.ecorr, self.wcorr = part_pair.pair_pot.prepare_tailcorrections(system.natom, self.nlow, self.nhigh)
+
+    def _internal_compute(self, gpos, vtens):
+        if vtens is not None:
+            w = 2.0 * np.pi * self.wcorr / self.system.cell.volume
+            vtens[0, 0] += w
+            vtens[1, 1] += w
+            vtens[2, 2] += w
+        return 2.0 * np.pi * self.ecorr / self.system.cell.volume
 
 
 class ForcePartValence(ForcePart):

@@ -68,6 +68,52 @@ class Switch3(Truncation):
         return 'switch3 %s' % self.width
 
 
+# Gauss-Legendre rule for the switching interval of the tail integrals (the
+# integrand r^2 V(r) (1 - S(r)) is smooth there; 48 nodes reach FP64 rounding)
+_GL_X, _GL_W = np.polynomial.legendre.leggauss(48)
+
+
+def _tail_cut(terms, rc):
+    """sum over terms of int_rc^inf r^2 V_term(r) dr, in closed form:
+    ('pow', A, n): A r^-n; ('exp', A, b): A exp(-b r); ('expr', A, b):
+    A exp(-b r) / r.  A and the parameter are arrays over type pairs."""
+    out = 0.0
+    for form, A, q in terms:
+        A = np.asarray(A, float)
+        q = np.asarray(q, float)
+        if form == 'pow':
+            out = out + A * rc ** (3.0 - q) / (q - 3.0)
+        else:
+            b = np.where(q > 0, q, 1.0)
+            e = np.exp(-b * rc)
+            if form == 'exp':
+                v = A * e * (rc * rc / b + 2.0 * rc / (b * b) + 2.0 / (b * b * b))
+            else:
+                v = A * e * (rc / b + 1.0 / (b * b))
+            out = out + np.where((q > 0) & (A != 0), v, 0.0)
+    return out
+
+
+def _tail_switch(terms, rc, width):
+    """sum over terms of int_{rc-w}^{rc} r^2 V(r) (1 - S(r)) dr with the cubic
+    switch S = 3x^2 - 2x^3, x = (rc - r)/w (Gauss-Legendre)."""
+    r = rc - 0.5 * width * (1.0 - _GL_X)          # nodes on [rc - w, rc]
+    x = (rc - r) / width
+    f = r * r * (1.0 - (3.0 - 2.0 * x) * x * x) * (0.5 * width * _GL_W)
+    out = 0.0
+    for form, A, q in terms:
+        A = np.asarray(A, float)[..., None]
+        q = np.asarray(q, float)[..., None]
+        if form == 'pow':
+            v = A * r ** (-q)
+        elif form == 'exp':
+            v = np.where(A != 0, A * np.exp(-q * r), 0.0)
+        else:
+            v = np.where(A != 0, A * np.exp(-q * r) / r, 0.0)
+        out = out + (v * f).sum(-1)
+    return out
+
+
 class PairPot(object):
     name = None
     kind = None
@@ -88,6 +134,61 @@ class PairPot(object):
     def log(self):
         pass
 
+    # -- tail corrections (yaff/pes/ext.pyx:665-687, pair_pot.c:178-254) --
+    def _tail_params(self, natom):
+        """(natom, k) per-atom parameters that fix the pair terms."""
+        raise NotImplementedError('Tail corrections are not defined for %s' % self.name)
+
+    def _tail_terms(self, A, B):
+        """Long-range model of the pair potential for parameter rows A, B."""
+        raise NotImplementedError
+
+    def _tail_value(self, A, B, r):
+        """The untruncated pair potential at distance r."""
+        raise NotImplementedError
+
+    def _tail_switch_compat(self, A, B, rc, width):
+        """Deviation of the reference's Switch3 tail integral from the exact
+        one, where the reference's closed form has one (default: none)."""
+        return 0.0
+
+    def prepare_tailcorrections(self, natom, nlow=0, nhigh=-1):
+        """(C0, C1) summed over all ordered atom pairs (i, j), i = j included,
+        except pairs with both atoms below nlow or both at or above nhigh:
+        C0 = sum int r^2 V(r) (1 - h(r)) dr (h the truncation: a step at rcut,
+        or Switch3), C1 = -C0 - U(rcut) rcut^3 / 3 without truncation, -C0
+        with Switch3.  Atoms are grouped by their parameters, so the cost is
+        quadratic in the number of distinct parameter sets only."""
+        if nhigh == -1:
+            nhigh = natom
+        if not (0 <= nlow <= nhigh <= natom):
+            raise ValueError('invalid nlow / nhigh')
+        if self.tr is not None and not isinstance(self.tr, Switch3):
+            raise NotImplementedError('Tail corrections not supported for %s' % self.tr.get_log())
+        P = np.asarray(self._tail_params(natom), float).reshape(natom, -1)
+        keys, inv = np.unique(P, axis=0, return_inverse=True)
+        inv = inv.ravel()
+        nkey = len(keys)
+        cnt = [np.bincount(inv[lo:hi], minlength=nkey).astype(float)
+               for lo, hi in ((0, nlow), (nlow, nhigh), (nhigh, natom))]
+        tot = cnt[0] + cnt[1] + cnt[2]
+        mult = np.outer(tot, tot) - np.outer(cnt[0], cnt[0]) - np.outer(cnt[2], cnt[2])
+        ia, ib = np.nonzero(mult)
+        if len(ia) == 0:
+            return 0.0, 0.0
+        A, B, m = keys[ia], keys[ib], mult[ia, ib]
+        terms = self._tail_terms(A, B)
+        rc = self.rcut
+        c0 = _tail_cut(terms, rc)
+        if self.tr is not None:
+            c0 = c0 + _tail_switch(terms, rc, self.tr.width) + self._tail_switch_compat(A, B, rc, self.tr.width)
+        e = float((m * c0).sum())
+        if self.tr is None:
+            w = -e - float((m * self._tail_value(A, B, rc)).sum()) * rc ** 3 / 3.0
+        else:
+            w = -e
+        return e, w
+
 
 class PairPotLJ(PairPot):
     """4 eps_ij ((sigma_ij/d)^12 - (sigma_ij/d)^6), sigma_ij = (sigma_i +
@@ -106,6 +207,22 @@ class PairPotLJ(PairPot):
         assert len(self.sigmas) == natom
         return {'sigma': self.sigmas, 'epsilon': self.epsilons, 'onlypauli': None, 'radii': None,
                 'alpha': 0.0, 'dielectric': 1.0}
+
+    def _tail_params(self, natom):
+        return np.stack([self.sigmas, self.epsilons], 1)
+
+    @staticmethod
+    def _mix(A, B):
+        return 0.5 * (A[:, 0] + B[:, 0]), np.sqrt(A[:, 1] * B[:, 1])
+
+    def _tail_terms(self, A, B):
+        sig, eps = self._mix(A, B)
+        return [('pow', 4 * eps * sig ** 12, 12.0), ('pow', -4 * eps * sig ** 6, 6.0)]
+
+    def _tail_value(self, A, B, r):
+        sig, eps = self._mix(A, B)
+        x = (sig / r) ** 6
+        return 4.0 * eps * (x * (x - 1.0))
 
 
 class PairPotMM3(PairPot):
@@ -127,6 +244,24 @@ class PairPotMM3(PairPot):
         assert len(self.sigmas) == natom
         return {'sigma': self.sigmas, 'epsilon': self.epsilons, 'onlypauli': self.onlypaulis, 'radii': None,
                 'alpha': 0.0, 'dielectric': 1.0}
+
+    def _tail_params(self, natom):
+        return np.stack([self.sigmas, self.epsilons, self.onlypaulis.astype(float)], 1)
+
+    def _tail_terms(self, A, B):
+        # the capped form shares MM3's long-range model (pair_pot.c:361-365)
+        sig, eps = A[:, 0] + B[:, 0], np.sqrt(A[:, 1] * B[:, 1])
+        r6 = np.where(A[:, 2] + B[:, 2] == 0, 1.0, 0.0)
+        return [('exp', 1.84e5 * eps, 12.0 / sig), ('pow', -2.25 * r6 * eps * sig ** 6, 6.0)]
+
+    def _tail_value(self, A, B, r):
+        sig, eps = A[:, 0] + B[:, 0], np.sqrt(A[:, 1] * B[:, 1])
+        ex = 1.84e5 * np.exp(-12.0 * r / sig)
+        v = np.where(A[:, 2] + B[:, 2] == 0, eps * (ex - 2.25 * (sig / r) ** 6), eps * ex)
+        if self.kind == _lib.POT_MM3CAP:
+            x = r / sig
+            v = np.where((A[:, 2] + B[:, 2] == 0) & (x <= 0.355114), eps * (5799.303156 - 12182.86986 * x), v)
+        return v
 
 
 class PairPotEI(PairPot):
@@ -173,6 +308,18 @@ class PairPotGrimme(PairPot):
         return {'sigma': self.r0, 'epsilon': self.c6, 'onlypauli': None, 'radii': None,
                 'alpha': 0.0, 'dielectric': 1.0}
 
+    def _tail_params(self, natom):
+        return np.stack([self.r0, self.c6], 1)
+
+    def _tail_terms(self, A, B):
+        # undamped long-range model -1.1 c6 / r^6 (tailcorr.c:229-256)
+        return [('pow', -1.1 * np.sqrt(A[:, 1] * B[:, 1]), 6.0)]
+
+    def _tail_value(self, A, B, r):
+        r0, c6 = A[:, 0] + B[:, 0], np.sqrt(A[:, 1] * B[:, 1])
+        f = 1.0 / (1.0 + np.exp(-20.0 * (r / r0 - 1.0)))
+        return -1.1 * f * c6 / r ** 6
+
 
 class _TypeTablePot(PairPot):
     """A pair potential whose parameters are tables over pairs of atom types."""
@@ -192,6 +339,12 @@ class _TypeTablePot(PairPot):
     def _check_types(self, n):
         if len(self.ffatype_ids) and (self.ffatype_ids.min() < 0 or self.ffatype_ids.max() >= n):
             raise ValueError('atom type index out of range')
+
+    def _tail_params(self, natom):
+        return self.ffatype_ids.astype(float)[:, None]
+
+    def _tab(self, A, B, k):
+        return self._cross[k][A[:, 0].astype(np.int64), B[:, 0].astype(np.int64)]
 
     def _device_table(self, natom):
         assert len(self.ffatype_ids) == natom
@@ -257,10 +410,35 @@ class _RepPot(_TypeTablePot):
                     b_cross[i1, i0] = b_cross[i0, i1]
 
 
+    def _tail_terms(self, A, B):
+        amp, b = self._tab(A, B, 0), self._tab(A, B, 1)
+        amp = np.where(b == 0.0, 0.0, amp)
+        return [('exp' if self.kind == _lib.POT_EXPREP else 'expr', amp, b)]
+
+    def _tail_value(self, A, B, r):
+        amp, b = self._tab(A, B, 0), self._tab(A, B, 1)
+        ok = (amp != 0.0) & (b != 0.0)
+        v = amp * np.exp(-np.where(ok, b, 0.0) * r)
+        if self.kind == _lib.POT_QMDFFREP:
+            v = v / r
+        return np.where(ok, v, 0.0)
+
+
 class PairPotExpRep(_RepPot):
     """A_ij exp(-B_ij d) over atom-type pairs."""
     name = 'exprep'
     kind = _lib.POT_EXPREP
+
+    def _tail_switch_compat(self, A, B, rc, width):
+        # The reference's Switch3 integral truncates rcut^2 to an integer in
+        # one of its terms (yaff/pes/tailcorr.c:358); its value differs from
+        # the exact one by 6 A exp(-B rc) (floor(rc^2) - rc^2) / (B^3 w^2).
+        # Kept so that the energies equal the reference's.
+        amp, b = self._tab(A, B, 0), self._tab(A, B, 1)
+        ok = b > 0
+        bb = np.where(ok, b, 1.0)
+        d = 6.0 * amp * np.exp(-bb * rc) * (np.floor(rc * rc) - rc * rc) / (bb ** 3 * width * width)
+        return np.where(ok, d, 0.0)
 
 
 class PairPotQMDFFRep(_RepPot):
@@ -280,6 +458,15 @@ class PairPotLJCross(_TypeTablePot):
         self.sig_cross = self._square(sig_cross, self.eps_cross.shape[0])
         self._check_types(self.eps_cross.shape[0])
         self._cross = (self.eps_cross, self.sig_cross)
+
+    def _tail_terms(self, A, B):
+        eps, sig = self._tab(A, B, 0), self._tab(A, B, 1)
+        return [('pow', 4 * eps * sig ** 12, 12.0), ('pow', -4 * eps * sig ** 6, 6.0)]
+
+    def _tail_value(self, A, B, r):
+        eps, sig = self._tab(A, B, 0), self._tab(A, B, 1)
+        x = (sig / r) ** 6
+        return 4.0 * eps * (x * (x - 1.0))
 
 
 class PairPotDampDisp(_TypeTablePot):
@@ -320,6 +507,24 @@ class PairPotDampDisp(_TypeTablePot):
         self.b_cross = b_cross
         self._cross = (cn_cross, b_cross)
 
+    def _tail_terms(self, A, B):
+        # undamped long-range model -C / r^n (tailcorr.c:523-553)
+        return [('pow', -self._tab(A, B, 0), float(self.power))]
+
+    def _tail_value(self, A, B, r):
+        cn, b = self._tab(A, B, 0), self._tab(A, B, 1)
+        n = self.power
+        disp = -cn / r ** n
+        x = b * r
+        poly = np.zeros_like(x)
+        term = np.ones_like(x)
+        for k in range(n + 1):
+            if k:
+                term = term * x / k
+            poly = poly + term
+        damp = np.where(b == 0.0, 1.0, 1.0 - poly * np.exp(-x))
+        return np.where(cn == 0.0, 0.0, damp * disp)
+
 
 class PairPotDisp68BJDamp(_TypeTablePot):
     """-s6 C6_ij / (d^6 + R^6) - s8 C8_ij / (d^8 + R^8), R = a R_ij + b
@@ -344,3 +549,12 @@ class PairPotDisp68BJDamp(_TypeTablePot):
         self.c6_scale, self.c8_scale, self.bj_a, self.bj_b = float(c6_scale), float(c8_scale), float(bj_a), float(bj_b)
         self._cross = (c6_cross, c8_cross, R_cross)
         self._scales = np.array([self.c6_scale, self.c8_scale, self.bj_a, self.bj_b])
+
+    def _tail_terms(self, A, B):
+        # undamped long-range model (tailcorr.c:596-625)
+        return [('pow', -self.c6_scale * self._tab(A, B, 0), 6.0), ('pow', -self.c8_scale * self._tab(A, B, 1), 8.0)]
+
+    def _tail_value(self, A, B, r):
+        R = self.bj_a * self._tab(A, B, 2) + self.bj_b
+        return (-self.c6_scale * self._tab(A, B, 0) / (r ** 6 + R ** 6)
+                - self.c8_scale * self._tab(A, B, 1) / (r ** 8 + R ** 8))
