@@ -265,6 +265,25 @@ int yg_md_run(yg_ctx *ctx, int64_t nsteps, int use_graph, double skin, int64_t *
  * ((*nlog) x 2) to host memory; any pointer may be NULL. */
 int yg_md_get(yg_ctx *ctx, double *pos, double *vel, double *log, int64_t *nlog);
 
+/* Thermostat of the device step, applied where the reference calls its
+ * Verlet hooks: kind 0 none, 1 Berendsen (before the first half kick), 2
+ * Langevin (before and after), 3 CSVR (before), 4 Nose-Hoover chain (before
+ * and after).  kT = k_B T0, timecon the time constant, ndof the degrees of
+ * freedom; a chain of 1..8 beads takes its positions, velocities and masses;
+ * the Langevin and CSVR noise comes from a counter-based generator keyed by
+ * `seed` and the step number.  Replaces BerendsenThermostat,
+ * LangevinThermostat, CSVRThermostat and NHCThermostat with NHChain
+ * (yaff/sampling/nvt.py:110-270, :346-500) for yg_md_run.  Call after
+ * yg_md_setup (which resets it to none). */
+int yg_md_thermostat(yg_ctx *ctx, int kind, double kT, double timecon, int64_t ndof, int chain_length,
+                     const double *chain_pos, const double *chain_vel, const double *chain_masses,
+                     unsigned long long seed);
+
+/* The thermostat's conserved-energy correction (the sum the reference keeps
+ * in VerletHook.econs_correction) and the chain positions / velocities; any
+ * pointer may be NULL. */
+int yg_md_thermo_get(yg_ctx *ctx, double *econs_correction, double *chain_pos, double *chain_vel);
+
 /* Ewald correction for callers that cannot let the library allocate device
  * memory (an engine that owns all device memory through its own pool, or a
  * step loop that must not block on an allocation).  No counterpart in the

@@ -1,0 +1,83 @@
+"""Generate tests/golden/md_thermostats.npz by running the reference.
+
+Run in a container that holds the reference checkout (default /root/reference,
+or $YAFF_REFERENCE) after ``sh oracle/build_ref.sh``:
+
+    python tests/golden/make_md_golden.py
+
+For each thermostat of the reference (Berendsen, Langevin, CSVR, Nose-Hoover
+chain) the script runs the reference's own VerletIntegrator with that hook on
+the 64-molecule flexible water box (reference force field), 12 steps of
+0.5 fs from fixed initial velocities, and stores positions, velocities,
+kinetic, potential and conserved energies and the degrees of freedom per
+step.  The stochastic thermostats draw from NumPy's global generator, seeded
+per run (stored), in the reference's call order.
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+
+warnings.filterwarnings('ignore')
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, 'oracle'))
+
+from yaff_gb300 import configs  # noqa: E402
+from yaff_gb300.units import femtosecond, kelvin  # noqa: E402
+import ref_shim  # noqa: E402
+from ref_ff import build_reference_ff  # noqa: E402
+
+NSTEP = 12
+TIMESTEP = 0.5 * femtosecond
+TEMP = 300.0 * kelvin
+TIMECON = 20.0 * femtosecond
+
+
+def main():
+    if not ref_shim.reference_available():
+        raise SystemExit('reference not available: run oracle/build_ref.sh first')
+    ref_shim.import_reference()
+    from yaff.sampling.verlet import VerletIntegrator
+    from yaff.sampling.nvt import BerendsenThermostat, LangevinThermostat, CSVRThermostat, NHCThermostat
+    spec = configs.flexible_water(nside=4, box=12.42, rcut=5.0, skin=0.5, name='water64')
+    rng = np.random.default_rng(99)
+    natom = len(spec['pos'])
+    vel0 = rng.normal(0, 1, (natom, 3)) * np.sqrt(1.2 * 300.0 * 3.166811563e-6 / spec['masses'])[:, None]
+    chain_vel0 = np.array([1e-3, -2e-3, 5e-4]) / femtosecond * 1e-2
+    data = {'pos0': spec['pos'], 'vel0': vel0, 'timestep': np.array(TIMESTEP), 'temp': np.array(TEMP),
+            'timecon': np.array(TIMECON), 'chain_vel0': chain_vel0, 'nstep': np.array(NSTEP)}
+    makers = {
+        'berendsen': lambda: BerendsenThermostat(TEMP, timecon=TIMECON),
+        'langevin': lambda: LangevinThermostat(TEMP, timecon=TIMECON),
+        'csvr': lambda: CSVRThermostat(TEMP, timecon=TIMECON),
+        'nhc': lambda: NHCThermostat(TEMP, timecon=TIMECON, chainlength=3, chain_vel0=chain_vel0.copy()),
+    }
+    for k, (name, make) in enumerate(makers.items()):
+        ff = build_reference_ff(spec)
+        seed = 1000 + k
+        np.random.seed(seed)
+        hook = make()
+        vi = VerletIntegrator(ff, TIMESTEP, hooks=[hook], vel0=vel0.copy())
+        rows = {'pos': [vi.pos.copy()], 'vel': [vi.vel.copy()], 'ekin': [vi.ekin], 'epot': [vi.epot],
+                'econs': [vi.econs]}
+        for _ in range(NSTEP):
+            vi.propagate()
+            rows['pos'].append(vi.pos.copy())
+            rows['vel'].append(vi.vel.copy())
+            rows['ekin'].append(vi.ekin)
+            rows['epot'].append(vi.epot)
+            rows['econs'].append(vi.econs)
+        for key, v in rows.items():
+            data['%s_%s' % (name, key)] = np.array(v)
+        data['%s_seed' % name] = np.array(seed)
+        data['%s_ndof' % name] = np.array(vi.ndof)
+        print('%-10s ndof %d  T %.2f K  econs drift %.3e' % (name, vi.ndof, vi.temp / kelvin,
+                                                              rows['econs'][-1] - rows['econs'][0]))
+    np.savez_compressed(os.path.join(HERE, 'md_thermostats.npz'), **data)
+
+
+if __name__ == '__main__':
+    main()

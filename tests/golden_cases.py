@@ -10,9 +10,10 @@ GOLDEN = os.path.join(HERE, 'golden')
 
 
 def case_names():
-    """Force-field cases (the mc_* fixtures hold MC trial cases)."""
+    """Force-field cases (the mc_* fixtures hold MC trial cases, md_* MD
+    trajectories)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz'))
-                  if not os.path.basename(p).startswith('mc_'))
+                  if not os.path.basename(p).startswith(('mc_', 'md_')))
 
 
 def mc_case_names():

@@ -81,6 +81,8 @@ SIGNATURES = {
     'yg_md_setup': (_I, [_P, _P, _P, _D, _I, _D, _I64]),
     'yg_md_run': (_I, [_P, _I64, _I, _D, ctypes.POINTER(_I64)]),
     'yg_md_get': (_I, [_P, _P, _P, _P, ctypes.POINTER(_I64)]),
+    'yg_md_thermostat': (_I, [_P, _I, _D, _D, _I64, _I, _P, _P, _P, ctypes.c_ulonglong]),
+    'yg_md_thermo_get': (_I, [_P, _P, _P, _P]),
     'yg_ewald_prefactors': (_I, [_P, _D, _D, _P, _D, _P]),
     'yg_ewald_structurefactors': (_I, [_P, _I64, _P, _P, _P, _D, _P, _D, _P, _P, _P]),
     'yg_ewald_deltae': (_I, [_P, _P, _P, _P, _P, _I64, _P]),

@@ -235,6 +235,17 @@ struct yg_ctx {
   double *d_md_ekin = nullptr;
   double *d_md_log = nullptr;     // (max_steps+1)*2: epot, ekin
   double *d_md_extra = nullptr;   // host-side energy added to epot (neutralizing term)
+  // thermostat of the device step (0 none, 1 Berendsen, 2 Langevin, 3 CSVR,
+  // 4 Nose-Hoover chain); state block: [0] conserved-energy correction,
+  // [1] velocity factor, [2] kinetic energy before a stochastic update,
+  // [3] chi-square sum, [8..15] chain positions, [16..23] chain velocities,
+  // [24..31] chain masses
+  int md_thermo = 0;
+  double md_kT = 0.0, md_timecon = 0.0;
+  int64_t md_ndof = 0;
+  int md_nhc_len = 0;
+  unsigned long long md_seed = 0;
+  double *d_md_thermo = nullptr, *d_snap_thermo = nullptr;
   int *d_md_step = nullptr;
   double md_dt = 0.0;
   int md_mask = 0;

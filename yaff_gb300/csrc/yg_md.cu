@@ -105,7 +105,209 @@ __global__ void k_set_int(int *__restrict__ p, int v) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *p = v;
 }
 
+// --- thermostats (yaff/sampling/nvt.py:110-500) ---
+
+// Counter-based generator Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel
+// random numbers: as easy as 1, 2, 3", SC'11): ten rounds of two 32x32->64
+// multiplications with the round keys bumped by the Weyl constants.
+__device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const unsigned lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const unsigned lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// A standard normal number for (index, step, stage) of stream `seed`
+// (Box-Muller on two 32-bit uniforms in (0, 1)).
+__device__ __forceinline__ double normal01(unsigned long long seed, unsigned long long index, int step, int stage) {
+  const uint4 r = philox4x32(make_uint4((unsigned)index, (unsigned)(index >> 32), (unsigned)step, (unsigned)stage),
+                             make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+  const double u1 = ((double)r.x + 0.5) * 2.3283064365386963e-10;
+  const double u2 = ((double)r.y + 0.5) * 2.3283064365386963e-10;
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+// vel *= f[1]
+__global__ void k_scale_vel(double *__restrict__ vel, int64_t n3, const double *__restrict__ f) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n3) vel[t] *= f[1];
+}
+
+// Berendsen: c = sqrt(1 + dt/tau (T0/T - 1)) from the current kinetic energy
+// (nvt.py:150-156).
+__global__ void k_berendsen(double *__restrict__ th, double *__restrict__ ekin, double kT, double dt_tau, double ndof) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double ek = *ekin;
+  const double c = sqrt(1.0 + dt_tau * (kT * ndof / (2.0 * ek) - 1.0));
+  th[1] = c;
+  th[0] += (1.0 - c * c) * ek;
+  *ekin = c * c * ek;
+}
+
+// Langevin half step v = c1 v + sqrt((1 - c1^2) kT / m) xi (nvt.py:208-213),
+// with per-block partial kinetic energies of the new velocities.
+__global__ void k_langevin(double *__restrict__ vel, const double *__restrict__ invm, int64_t natom, double c1,
+                           double kT, unsigned long long seed, const int *__restrict__ step, int stage,
+                           double *__restrict__ ekin_part) {
+  __shared__ double red[8];
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double ek = 0.0;
+  if (t < natom * 3) {
+    const double im = invm[t / 3];
+    const double v = c1 * vel[t] + sqrt((1.0 - c1 * c1) * kT * im) * normal01(seed, (unsigned long long)t, *step, stage);
+    vel[t] = v;
+    ek = 0.5 * v * v / im;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ek += __shfl_xor_sync(0xffffffffu, ek, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ek;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+    ekin_part[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_save_ekin(double *__restrict__ th, const double *__restrict__ ekin) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) th[2] = *ekin;
+}
+
+// conserved-energy correction of a stochastic update: ekin before - after
+__global__ void k_ekin_delta(double *__restrict__ th, const double *__restrict__ ekin) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) th[0] += th[2] - *ekin;
+}
+
+// CSVR: per-block partial sums of the squares of ndof - 1 normal numbers
+__global__ void k_csvr_chi2(int64_t m, unsigned long long seed, const int *__restrict__ step,
+                            double *__restrict__ part) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+    const double z = normal01(seed, (unsigned long long)t, *step, 3);
+    s += z * z;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double q = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) q += red[w];
+    part[blockIdx.x] = q;
+  }
+}
+
+// CSVR rescaling factor alpha (nvt.py:255-265; Bussi and Parrinello, Comput.
+// Phys. Commun. 179, 26 (2008)).
+__global__ void k_csvr(double *__restrict__ th, double *__restrict__ ekin, double kT, double c, double ndof,
+                       unsigned long long seed, const int *__restrict__ step) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double R = normal01(seed, 0xFFFFFFFFFFFFull, *step, 2);
+  const double S = th[3];
+  const double ek = *ekin;
+  const double kin = 0.5 * ndof * kT;
+  const double fact = (1.0 - c) * kin / ndof / ek;
+  const double a2 = c + (S + R * R) * fact + 2.0 * R * sqrt(c * fact);
+  const double alpha = (R + sqrt(c / fact) >= 0.0 ? 1.0 : -1.0) * sqrt(a2);
+  th[1] = alpha;
+  th[0] += (1.0 - alpha * alpha) * ek;
+  *ekin = alpha * alpha * ek;
+}
+
+// One application of the Nose-Hoover chain propagator (nvt.py:378-417):
+// chain velocities a quarter step (reverse order), chain positions half a
+// step, the atomic velocity factor, chain velocities again (forward order).
+// post = 1 also stores the chain's conserved-energy correction.
+__global__ void k_nhc(double *__restrict__ th, double *__restrict__ ekin, int len, double dt, double kT, double ndof,
+                      int post) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double *xi = th + 8, *vxi = th + 16;
+  const double *Q = th + 24;
+  double ek = *ekin;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int q = 0; q < len; q++) {
+      const int k = pass == 0 ? len - 1 - q : q;
+      double g = (k == 0) ? 2.0 * ek - ndof * kT : Q[k - 1] * vxi[k - 1] * vxi[k - 1] - kT;
+      g /= Q[k];
+      if (k == len - 1) {
+        vxi[k] += g * dt / 4;
+      } else {
+        const double e = exp(-vxi[k + 1] * dt / 8);
+        vxi[k] *= e;
+        vxi[k] += g * dt / 4;
+        vxi[k] *= e;
+      }
+    }
+    if (pass == 0) {
+      for (int k = 0; k < len; k++) xi[k] += vxi[k] * dt / 2;
+      const double f = exp(-vxi[0] * dt / 2);
+      th[1] = f;
+      ek *= f * f;
+    }
+  }
+  *ekin = ek;
+  if (post) {
+    double e = 0.0, x = ndof * xi[0];
+    for (int k = 0; k < len; k++) e += vxi[k] * vxi[k] * Q[k];
+    for (int k = 1; k < len; k++) x += xi[k];
+    th[0] = 0.5 * e + kT * x;
+  }
+}
+
 }  // namespace
+
+// Thermostat stage of the device step: stage 0 before the first half kick
+// (the reference's pre hook), 1 after the second (its post hook).
+static int md_thermostat(yg_ctx *c, int stage) {
+  if (!c->md_thermo) return YG_OK;
+  const int64_t n3 = c->natom * 3;
+  const int nb = yg_blocks(n3, 256);
+  const double dt = c->md_dt, nd = (double)c->md_ndof;
+  int rc;
+  switch (c->md_thermo) {
+    case 1:  // Berendsen: pre only
+      if (stage != 0) return YG_OK;
+      k_berendsen<<<1, 32, 0, c->stream>>>(c->d_md_thermo, c->d_md_ekin, c->md_kT, dt / c->md_timecon, nd);
+      YG_LAUNCH_CHECK(c, "k_berendsen");
+      break;
+    case 2: {  // Langevin: pre and post
+      k_save_ekin<<<1, 32, 0, c->stream>>>(c->d_md_thermo, c->d_md_ekin);
+      YG_LAUNCH_CHECK(c, "k_save_ekin");
+      k_langevin<<<nb, 256, 0, c->stream>>>(c->d_vel, c->d_invm, c->natom, exp(-dt / c->md_timecon / 2), c->md_kT,
+                                            c->md_seed, c->d_md_step, stage, c->d_md_ekpart);
+      YG_LAUNCH_CHECK(c, "k_langevin");
+      if ((rc = yg_launch_reduce_ev(c, c->d_md_ekpart, nb, 1, c->d_md_ekin))) return rc;
+      k_ekin_delta<<<1, 32, 0, c->stream>>>(c->d_md_thermo, c->d_md_ekin);
+      YG_LAUNCH_CHECK(c, "k_ekin_delta");
+      return YG_OK;
+    }
+    case 3: {  // CSVR: pre only
+      if (stage != 0) return YG_OK;
+      const int64_t m = c->md_ndof - 1;
+      const int nbc = (int)std::max<int64_t>(1, std::min<int64_t>(yg_blocks(m, 256), nb));
+      k_csvr_chi2<<<nbc, 256, 0, c->stream>>>(m, c->md_seed, c->d_md_step, c->d_md_ekpart);
+      YG_LAUNCH_CHECK(c, "k_csvr_chi2");
+      if ((rc = yg_launch_reduce_ev(c, c->d_md_ekpart, nbc, 1, c->d_md_thermo + 3))) return rc;
+      k_csvr<<<1, 32, 0, c->stream>>>(c->d_md_thermo, c->d_md_ekin, c->md_kT, exp(-dt / c->md_timecon), nd,
+                                      c->md_seed, c->d_md_step);
+      YG_LAUNCH_CHECK(c, "k_csvr");
+      break;
+    }
+    default:  // Nose-Hoover chain: pre and post
+      k_nhc<<<1, 32, 0, c->stream>>>(c->d_md_thermo, c->d_md_ekin, c->md_nhc_len, dt, c->md_kT, nd, stage);
+      YG_LAUNCH_CHECK(c, "k_nhc");
+      break;
+  }
+  k_scale_vel<<<nb, 256, 0, c->stream>>>(c->d_vel, n3, c->d_md_thermo);
+  YG_LAUNCH_CHECK(c, "k_scale_vel");
+  return YG_OK;
+}
 
 // Force evaluation for the current device positions on the kept list,
 // summed on the device into d_total; no host synchronization.  prep = 0
@@ -127,13 +329,14 @@ static int md_force_async(yg_ctx *c, int prep, int reci_forked) {
   return YG_OK;
 }
 
-// second kick, kinetic energy, energy log row
-static int md_finish_step(yg_ctx *c, double dt) {
+// second kick, kinetic energy, post-step thermostat, energy log row
+static int md_finish_step(yg_ctx *c, double dt, int thermo) {
   int rc;
   const int nb = yg_blocks(c->natom * 3, 256);
   k_kick<<<nb, 256, 0, c->stream>>>(c->d_vel, c->d_total + 16, c->d_invm, c->natom, dt, c->d_md_ekpart);
   YG_LAUNCH_CHECK(c, "k_kick");
   if ((rc = yg_launch_reduce_ev(c, c->d_md_ekpart, nb, 1, c->d_md_ekin))) return rc;
+  if (thermo && (rc = md_thermostat(c, 1))) return rc;
   k_md_log<<<1, 32, 0, c->stream>>>(c->d_total, c->d_md_ekin, c->d_md_extra, c->d_md_log, c->d_md_step,
                                     c->md_max_steps + 1);
   YG_LAUNCH_CHECK(c, "k_md_log");
@@ -144,6 +347,7 @@ static int md_finish_step(yg_ctx *c, double dt) {
 static int md_step_device(yg_ctx *c, double factor, double skin) {
   int rc;
   const int nb = yg_blocks(c->natom * 3, 256);
+  if ((rc = md_thermostat(c, 0))) return rc;
   k_kick_drift<<<nb, 256, 0, c->stream>>>(c->d_pos, c->d_vel, c->d_total + 16, c->d_invm, c->natom, c->md_dt);
   YG_LAUNCH_CHECK(c, "k_kick_drift");
   if ((rc = yg_launch_max_disp2_async(c, (unsigned long long *)(c->d_md_ctrl + 6)))) return rc;
@@ -157,7 +361,7 @@ static int md_step_device(yg_ctx *c, double factor, double skin) {
   // the build sequence refreshes the cell-local coordinates in any case
   if ((rc = yg_launch_nlist_build_gated(c, c->d_md_ctrl, (unsigned long long *)(c->d_md_ctrl + 4)))) return rc;
   if ((rc = md_force_async(c, 0, reci))) return rc;
-  return md_finish_step(c, c->md_dt);
+  return md_finish_step(c, c->md_dt, 1);
 }
 
 static void md_drop_graph(yg_ctx *c) {
@@ -220,8 +424,10 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
   void **bufs[] = {(void **)&c->d_vel,      (void **)&c->d_invm,     (void **)&c->d_md_ekpart,
                    (void **)&c->d_md_ekin,  (void **)&c->d_md_log,   (void **)&c->d_md_extra,
                    (void **)&c->d_md_step,  (void **)&c->d_md_ctrl,  (void **)&c->d_snap_pos,
-                   (void **)&c->d_snap_vel, (void **)&c->d_snap_total, (void **)&c->d_snap_step};
+                   (void **)&c->d_snap_vel, (void **)&c->d_snap_total, (void **)&c->d_snap_step,
+                   (void **)&c->d_md_thermo, (void **)&c->d_snap_thermo};
   for (void **b : bufs) yg_free(c, b);
+  c->md_thermo = 0;
   if ((rc = yg_alloc(c, (void **)&c->d_vel, N * 3 * sizeof(double)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_invm, N * sizeof(double)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_md_ekpart, (size_t)nb * sizeof(double)))) return rc;
@@ -234,6 +440,9 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
   if ((rc = yg_alloc(c, (void **)&c->d_snap_vel, N * 3 * sizeof(double)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_snap_total, (16 + N * 3) * sizeof(double)))) return rc;
   if ((rc = yg_alloc(c, (void **)&c->d_snap_step, sizeof(int)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_md_thermo, 40 * sizeof(double)))) return rc;
+  if ((rc = yg_alloc(c, (void **)&c->d_snap_thermo, 40 * sizeof(double)))) return rc;
+  YG_CUDA(cudaMemsetAsync(c->d_md_thermo, 0, 40 * sizeof(double), c->stream));
   YG_CUDA(cudaMemcpyAsync(c->d_vel, vel, N * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->d_invm, invm.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->d_md_extra, &extra_energy, sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -249,7 +458,7 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
   // step 0: forces and energies at the initial positions (yaff's initialize);
   // a kick with dt = 0 only evaluates the kinetic energy
   if ((rc = md_force_async(c, 1, 0))) return rc;
-  return md_finish_step(c, 0.0);
+  return md_finish_step(c, 0.0, 0);
 }
 
 // Runs nsteps velocity-Verlet steps in batches of at most YG_MD_BATCH: each
@@ -287,6 +496,8 @@ int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nr
     YG_CUDA(cudaMemcpyAsync(c->d_snap_total, c->d_total, (16 + N * 3) * sizeof(double), cudaMemcpyDeviceToDevice,
                             c->stream));
     YG_CUDA(cudaMemcpyAsync(c->d_snap_step, c->d_md_step, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    YG_CUDA(cudaMemcpyAsync(c->d_snap_thermo, c->d_md_thermo, 40 * sizeof(double), cudaMemcpyDeviceToDevice,
+                            c->stream));
     YG_CUDA(cudaMemsetAsync(c->d_status, 0, YG_ST_NWORDS * sizeof(int), c->stream));
     for (int64_t s = 0; s < nb; s++) {
       if (use_graph && c->md_graph_valid) {
@@ -321,6 +532,8 @@ int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nr
       YG_CUDA(cudaMemcpyAsync(c->d_total, c->d_snap_total, (16 + N * 3) * sizeof(double), cudaMemcpyDeviceToDevice,
                               c->stream));
       YG_CUDA(cudaMemcpyAsync(c->d_md_step, c->d_snap_step, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+      YG_CUDA(cudaMemcpyAsync(c->d_md_thermo, c->d_snap_thermo, 40 * sizeof(double), cudaMemcpyDeviceToDevice,
+                              c->stream));
       int64_t cap = (int64_t)(c->h_status[YG_ST_MAXCOUNT] * 1.15) + 64;
       cap = (cap + 31) / 32 * 32;
       if (cap > c->nbr_cap) c->nbr_cap = cap;
@@ -364,6 +577,60 @@ int yg_md_get(yg_ctx *c, double *pos, double *vel, double *log, int64_t *nlog) {
   if (log && std::isnan(log[2 * (n - 1)])) {
     yg_set_error("not-a-number energy in the trajectory");
     return YG_ERR_NAN;
+  }
+  return YG_OK;
+}
+
+int yg_md_thermostat(yg_ctx *c, int kind, double kT, double timecon, int64_t ndof, int chain_length,
+                     const double *chain_pos, const double *chain_vel, const double *chain_masses,
+                     unsigned long long seed) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
+  if (!c || kind < 0 || kind > 4) return YG_ERR_ARG;
+  if (!c->md_ready) {
+    yg_set_error("yg_md_thermostat: call yg_md_setup first");
+    return YG_ERR_STATE;
+  }
+  if (kind != 0 && (!(kT > 0.0) || !(timecon > 0.0) || ndof < 2)) return YG_ERR_ARG;
+  if (kind == 4 && (chain_length < 1 || chain_length > 8 || !chain_pos || !chain_vel || !chain_masses)) {
+    yg_set_error("a Nose-Hoover chain needs 1..8 beads with positions, velocities and masses");
+    return YG_ERR_ARG;
+  }
+  double h[40] = {0.0};
+  if (kind == 4)
+    for (int k = 0; k < chain_length; k++) {
+      if (!(chain_masses[k] > 0.0)) return YG_ERR_ARG;
+      h[8 + k] = chain_pos[k];
+      h[16 + k] = chain_vel[k];
+      h[24 + k] = chain_masses[k];
+    }
+  YG_CUDA(cudaMemcpyAsync(c->d_md_thermo, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->md_thermo = kind;
+  c->md_kT = kT;
+  c->md_timecon = timecon;
+  c->md_ndof = ndof;
+  c->md_nhc_len = kind == 4 ? chain_length : 0;
+  c->md_seed = seed;
+  md_drop_graph(c);  // the step changed
+  return YG_OK;
+}
+
+int yg_md_thermo_get(yg_ctx *c, double *econs_correction, double *chain_pos, double *chain_vel) {
+  if (c) {
+    const int jrc = yg_ewald_join(c);
+    if (jrc) return jrc;
+  }
+  if (!c || !c->md_ready) return YG_ERR_STATE;
+  double h[40];
+  YG_CUDA(cudaMemcpyAsync(h, c->d_md_thermo, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  if (econs_correction) *econs_correction = h[0];
+  for (int k = 0; k < c->md_nhc_len; k++) {
+    if (chain_pos) chain_pos[k] = h[8 + k];
+    if (chain_vel) chain_vel[k] = h[16 + k];
   }
   return YG_OK;
 }

@@ -27,7 +27,7 @@
 #include "yg_internal.cuh"
 
 #define YG_CELL_DIV 4      // grid cells at least r_c / 4 wide
-#define YG_BUILD_RUNS 192  // candidate runs per warp held in shared memory
+#define YG_BUILD_RUNS 144  // candidate runs per warp held in shared memory (4 blocks of 8 warps fit an SM)
 #define YG_BUILD_MAP 4096  // candidates per warp whose run index is tabulated
 
 namespace {
@@ -313,7 +313,7 @@ __device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
 // Dynamic shared memory of k_build per warp: runs, run offsets, candidate map.
 #define YG_BUILD_WARP_SMEM (YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4 + YG_BUILD_MAP)
 
-__global__ void __launch_bounds__(256, 2) k_build(BuildArgs A) {
+__global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char build_smem[];
   if (A.gate && !*A.gate) return;
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;

@@ -70,6 +70,11 @@ class DeviceSystem(object):
         self.ewald_key = None
         self.valence_key = None
         self._pos_staging, self._pos_owner = _pinned((self.natom, 3))
+        # the system's positions move into the page-locked buffer (same
+        # values): ForceField.update_pos then writes straight into the memory
+        # the host->device copy reads, one host copy per step instead of two
+        self._pos_staging[:] = system.pos
+        system.pos = self._pos_staging
         self._parts_buf = np.zeros(_lib.NPART)
         self._vt_buf = np.zeros(9)
         # bumped whenever the device list is invalidated (cell or scalings)
@@ -122,8 +127,12 @@ class DeviceSystem(object):
     def upload_positions(self, pos=None):
         """Copies the current positions (host array) to the device."""
         src = self.system.pos if pos is None else pos
-        self._pos_staging[:] = src
+        if src is not self._pos_staging:
+            self._pos_staging[:] = src
         check(self.lib.yg_set_positions(self.ctx, ptr(self._pos_staging), 0), 'yg_set_positions')
+        # the copy reads the system's own (user-visible) positions
+        # asynchronously: wait for it, so that callers may write them again
+        check(self.lib.yg_sync(self.ctx), 'yg_sync')
 
     def upload_positions_device(self, dptr):
         check(self.lib.yg_set_positions(self.ctx, ctypes.c_void_p(dptr), 1), 'yg_set_positions')

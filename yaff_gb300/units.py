@@ -43,10 +43,11 @@ rad = 1.0
 
 pascal = joule / meter**3
 bar = 1e5 * pascal
+atm = 101325.0 * pascal
 
 __all__ = [
     'meter', 'angstrom', 'nanometer', 'bohr', 'joule', 'kjmol', 'kcalmol',
     'electronvolt', 'hartree', 'second', 'femtosecond', 'picosecond',
     'nanosecond', 'kilogram', 'amu', 'kelvin', 'boltzmann', 'deg', 'rad',
-    'pascal', 'bar',
+    'pascal', 'bar', 'atm',
 ]

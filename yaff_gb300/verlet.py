@@ -1,19 +1,63 @@
-"""Velocity Verlet (NVE) driving a force field through ForceField.compute.
+"""Velocity Verlet driving a force field through ForceField.compute, and
+the thermostats of the reference.
 
-Same integration step, initial-velocity recipe and conserved-quantity
-tracking as the reference's VerletIntegrator (yaff/sampling/verlet.py:320-390,
-:476-516) and get_random_vel (yaff/sampling/utils.py:42-77): positions and
-velocities stay FP64 NumPy arrays on the host; every step calls
-``ff.update_pos`` and ``ff.compute(gpos, vtens)`` exactly as the reference
-does, so the device force field is a drop-in for its force evaluation.
-Thermostat/barostat hooks, HDF5 output and restarts are not part of this
-module.
+Same integration step, initial-velocity recipe, Verlet-hook protocol (init /
+pre / post, conserved-energy corrections) and conserved-quantity tracking as
+the reference's VerletIntegrator (yaff/sampling/verlet.py:320-446) and
+get_random_vel (yaff/sampling/utils.py:42-77): positions and velocities stay
+FP64 NumPy arrays on the host; every step calls ``ff.update_pos`` and
+``ff.compute(gpos, vtens)`` exactly as the reference does, so the device
+force field is a drop-in for its force evaluation.  The Berendsen, Langevin,
+CSVR and Nose-Hoover-chain thermostats (yaff/sampling/nvt.py:110-500) work
+as host hooks of VerletIntegrator and, through ``DeviceVerlet(thermostat=)``,
+inside the device-resident step.  Barostats, HDF5 output and restarts are not
+part of this module.
 """
 import numpy as np
 
-from .units import boltzmann
+from .units import boltzmann, femtosecond
 
-__all__ = ['get_random_vel', 'ConsErrTracker', 'VerletIntegrator']
+__all__ = ['get_random_vel', 'ConsErrTracker', 'VerletIntegrator', 'VerletHook', 'clean_momenta',
+           'get_ndof_internal_md', 'BerendsenThermostat', 'LangevinThermostat', 'CSVRThermostat', 'NHChain',
+           'NHCThermostat', 'DeviceVerlet']
+
+
+def remove_com_moment(vel, masses):
+    """Subtracts the centre-of-mass velocity (yaff/sampling/utils.py:80-96)."""
+    com_vel = np.dot(masses, vel) / masses.sum()
+    vel[:] -= com_vel
+
+
+def remove_angular_moment(pos, vel, masses):
+    """Subtracts the rigid rotation with the system's angular momentum about
+    its centre of mass (yaff/sampling/utils.py:98-131)."""
+    com = np.dot(masses, pos) / masses.sum()
+    r = pos - com
+    ang = (np.cross(r, vel) * masses[:, None]).sum(0)
+    inert = (masses[:, None, None] * (np.eye(3)[None] * (r ** 2).sum(1)[:, None, None]
+                                      - r[:, :, None] * r[:, None, :])).sum(0)
+    omega = np.dot(np.linalg.pinv(inert), ang)
+    vel[:] -= np.cross(omega, r)
+
+
+def clean_momenta(pos, vel, masses, cell):
+    """Removes the external momenta a thermostat must not touch: the COM
+    velocity and, for isolated systems, the angular momentum
+    (yaff/sampling/utils.py:133-158)."""
+    remove_com_moment(vel, masses)
+    if cell.nvec == 0:
+        remove_angular_moment(pos, vel, masses)
+    elif cell.nvec == 1:
+        raise NotImplementedError
+
+
+def get_ndof_internal_md(natom, nper):
+    """Internal degrees of freedom (yaff/sampling/utils.py:259-287)."""
+    if nper == 0:
+        return {1: 0, 2: 1}.get(natom, 3 * natom - 6)
+    if nper == 1:
+        return 3 * natom - 4
+    return 3 * natom - 3
 
 
 def get_random_vel(temp0, scalevel0, masses, select=None, rng=None):
@@ -58,13 +102,229 @@ class ConsErrTracker(object):
         return 0.0
 
 
-class VerletIntegrator(object):
-    """NVE velocity Verlet.
+class VerletHook(object):
+    """A hook that acts inside the Verlet step (thermostats): ``init`` at
+    initialization, ``pre`` before the first half kick, ``post`` after the
+    second; ``econs_correction`` is added to the conserved energy
+    (yaff/sampling/verlet.py:418-446)."""
+    device_kind = None
 
-    ff: object with ``system`` (pos, masses), ``update_pos`` and
+    def __init__(self, start=0, step=1):
+        self.econs_correction = 0.0
+
+    def __call__(self, iterative):
+        pass
+
+    def init(self, iterative):
+        raise NotImplementedError
+
+    def pre(self, iterative, G1_add=None):
+        raise NotImplementedError
+
+    def post(self, iterative, G1_add=None):
+        raise NotImplementedError
+
+
+def _normal(rng, *shape):
+    """Standard normal numbers from `rng` (None: NumPy's global generator,
+    as the reference draws them)."""
+    return (np.random if rng is None else rng).normal(0, 1, shape if shape else None)
+
+
+class BerendsenThermostat(VerletHook):
+    """Weak-coupling velocity rescaling (yaff/sampling/nvt.py:110-159)."""
+    device_kind = 1
+
+    def __init__(self, temp, start=0, timecon=100 * femtosecond, restart=False):
+        self.temp = temp
+        self.timecon = timecon
+        self.restart = restart
+        VerletHook.__init__(self, start, 1)
+
+    def init(self, iterative):
+        if not self.restart:
+            clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        if iterative.ndof is None:
+            iterative.ndof = get_ndof_internal_md(iterative.pos.shape[0], iterative.ff.system.cell.nvec)
+
+    def pre(self, iterative, G1_add=None):
+        ekin = iterative.ekin
+        temp_inst = 2.0 * iterative.ekin / (boltzmann * iterative.ndof)
+        c = np.sqrt(1 + iterative.timestep / self.timecon * (self.temp / temp_inst - 1))
+        iterative.vel[:] = c * iterative.vel
+        iterative.ekin = iterative._compute_ekin()
+        self.econs_correction += (1 - c ** 2) * ekin
+
+    def post(self, iterative, G1_add=None):
+        pass
+
+
+class LangevinThermostat(VerletHook):
+    """Ornstein-Uhlenbeck velocity update for half a step before and after
+    each Verlet step (Bussi and Parrinello, Phys. Rev. E 75, 056707 (2007);
+    yaff/sampling/nvt.py:162-213)."""
+    device_kind = 2
+
+    def __init__(self, temp, start=0, timecon=100 * femtosecond, rng=None):
+        self.temp = temp
+        self.timecon = timecon
+        self.rng = rng
+        VerletHook.__init__(self, start, 1)
+
+    def init(self, iterative):
+        clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+
+    def pre(self, iterative, G1_add=None):
+        ekin0 = iterative.ekin
+        self.thermo(iterative)
+        self.econs_correction += ekin0 - iterative.ekin
+
+    def post(self, iterative, G1_add=None):
+        ekin0 = iterative.ekin
+        self.thermo(iterative)
+        self.econs_correction += ekin0 - iterative.ekin
+
+    def thermo(self, iterative):
+        c1 = np.exp(-iterative.timestep / self.timecon / 2)
+        c2 = np.sqrt((1.0 - c1 ** 2) * self.temp * boltzmann / iterative.masses).reshape(-1, 1)
+        iterative.vel[:] = c1 * iterative.vel + c2 * _normal(self.rng, *iterative.vel.shape)
+        iterative.ekin = iterative._compute_ekin()
+
+
+class CSVRThermostat(VerletHook):
+    """Canonical sampling through velocity rescaling (Bussi, Donadio and
+    Parrinello, J. Chem. Phys. 126, 014101 (2007); yaff/sampling/nvt.py:
+    215-268)."""
+    device_kind = 3
+
+    def __init__(self, temp, start=0, timecon=100 * femtosecond, rng=None):
+        self.temp = temp
+        self.timecon = timecon
+        self.rng = rng
+        VerletHook.__init__(self, start, 1)
+
+    def init(self, iterative):
+        clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        if iterative.ndof is None:
+            iterative.ndof = get_ndof_internal_md(iterative.pos.shape[0], iterative.ff.system.cell.nvec)
+        self.kin = 0.5 * iterative.ndof * boltzmann * self.temp
+
+    def pre(self, iterative, G1_add=None):
+        c = np.exp(-iterative.timestep / self.timecon)
+        R = _normal(self.rng)
+        S = (_normal(self.rng, iterative.ndof - 1) ** 2).sum()
+        iterative.ekin = iterative._compute_ekin()
+        fact = (1 - c) * self.kin / iterative.ndof / iterative.ekin
+        alpha = np.sign(R + np.sqrt(c / fact)) * np.sqrt(c + (S + R ** 2) * fact + 2 * R * np.sqrt(c * fact))
+        iterative.vel[:] = alpha * iterative.vel
+        ekin_new = alpha ** 2 * iterative.ekin
+        self.econs_correction += (1 - alpha ** 2) * iterative.ekin
+        iterative.ekin = ekin_new
+
+    def post(self, iterative, G1_add=None):
+        pass
+
+
+class NHChain(object):
+    """Nose-Hoover chain of `length` beads with masses from the time
+    constant; one call propagates it over half a step and rescales the
+    atomic velocities (Martyna, Tuckerman, Tobias and Klein, Mol. Phys. 87,
+    1117 (1996); yaff/sampling/nvt.py:346-427)."""
+
+    def __init__(self, length, timestep, temp, ndof, pos0, vel0, timecon=100 * femtosecond, rng=None):
+        self.length = length
+        self.timestep = timestep
+        self.temp = temp
+        self.timecon = timecon
+        self.rng = rng
+        self.restart_pos = pos0 is not None
+        self.restart_vel = vel0 is not None
+        self.pos = np.array(pos0, float) if self.restart_pos else np.zeros(length)
+        self.vel = np.array(vel0, float) if self.restart_vel else np.zeros(length)
+        if ndof > 0:
+            self.set_ndof(ndof)
+
+    def set_ndof(self, ndof):
+        self.ndof = ndof
+        angfreq = 2 * np.pi / self.timecon
+        self.masses = np.ones(self.length) * (boltzmann * self.temp / angfreq ** 2)
+        self.masses[0] *= ndof
+        if not self.restart_vel:
+            self.vel = self.get_random_vel_therm()
+
+    def get_random_vel_therm(self):
+        return _normal(self.rng, self.length) * np.sqrt(self.masses * boltzmann * self.temp) / self.masses
+
+    def __call__(self, ekin, vel, G1_add):
+        def do_bead(k, ekin):
+            if k == 0:
+                g = 2 * ekin - self.ndof * self.temp * boltzmann
+                if G1_add is not None:
+                    g += G1_add
+            else:
+                g = self.masses[k - 1] * self.vel[k - 1] ** 2 - self.temp * boltzmann
+            g /= self.masses[k]
+            if k == self.length - 1:
+                self.vel[k] += g * self.timestep / 4
+            else:
+                self.vel[k] *= np.exp(-self.vel[k + 1] * self.timestep / 8)
+                self.vel[k] += g * self.timestep / 4
+                self.vel[k] *= np.exp(-self.vel[k + 1] * self.timestep / 8)
+
+        for k in range(self.length - 1, -1, -1):
+            do_bead(k, ekin)
+        self.pos += self.vel * self.timestep / 2
+        factor = np.exp(-self.vel[0] * self.timestep / 2)
+        vel *= factor
+        ekin *= factor ** 2
+        for k in range(0, self.length):
+            do_bead(k, ekin)
+        return vel, ekin
+
+    def get_econs_correction(self):
+        kt = boltzmann * self.temp
+        return 0.5 * (self.vel ** 2 * self.masses).sum() + kt * (self.ndof * self.pos[0] + self.pos[1:].sum())
+
+
+class NHCThermostat(VerletHook):
+    """Nose-Hoover chain thermostat (Martyna, Klein and Tuckerman, J. Chem.
+    Phys. 97, 2635 (1992); yaff/sampling/nvt.py:430-498)."""
+    device_kind = 4
+
+    def __init__(self, temp, start=0, timecon=100 * femtosecond, chainlength=3, chain_pos0=None, chain_vel0=None,
+                 restart=False, rng=None):
+        self.temp = temp
+        self.restart = restart
+        self.chain = NHChain(chainlength, 0.0, temp, 0, chain_pos0, chain_vel0, timecon, rng)
+        VerletHook.__init__(self, start, 1)
+
+    def init(self, iterative):
+        if not self.restart:
+            clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        if iterative.ndof is None:
+            iterative.ndof = get_ndof_internal_md(iterative.pos.shape[0], iterative.ff.system.cell.nvec)
+        self.chain.timestep = iterative.timestep
+        self.chain.set_ndof(iterative.ndof)
+
+    def pre(self, iterative, G1_add=None):
+        vel_new, iterative.ekin = self.chain(iterative.ekin, iterative.vel, G1_add)
+        iterative.vel[:] = vel_new
+
+    def post(self, iterative, G1_add=None):
+        vel_new, iterative.ekin = self.chain(iterative.ekin, iterative.vel, G1_add)
+        iterative.vel[:] = vel_new
+        self.econs_correction = self.chain.get_econs_correction()
+
+
+class VerletIntegrator(object):
+    """Velocity Verlet with the reference's hook protocol.
+
+    ff: object with ``system`` (pos, masses, cell), ``update_pos`` and
     ``compute(gpos, vtens)``.  vel0: initial velocities (default: seeded
-    Maxwell-Boltzmann at temp0).  hooks: callables f(integrator) after every
-    step.
+    Maxwell-Boltzmann at temp0).  hooks: VerletHook objects (thermostats,
+    called before and after the Verlet step) and plain callables
+    f(integrator), called after every step.  ndof: degrees of freedom (None:
+    set by a thermostat's init, else 3 N).
     """
 
     def __init__(self, ff, timestep, vel0=None, temp0=300.0, scalevel0=True, hooks=None, rng=None, ndof=None):
@@ -78,16 +338,26 @@ class VerletIntegrator(object):
         self.vel = np.array(vel0, dtype=np.float64)
         self.gpos = np.zeros(self.pos.shape)
         self.vtens = np.zeros((3, 3))
+        if hooks is not None and not isinstance(hooks, (list, tuple)):
+            hooks = [hooks]
         self.hooks = list(hooks or [])
-        self.ndof = self.pos.size if ndof is None else ndof
+        self.ndof = ndof
         self.time = 0.0
         self.counter = 0
-        self.econs_correction = 0.0
         self.cons_err = ConsErrTracker()
         self.initialize()
 
+    def _verlet_hooks(self, kind):
+        for hook in self.hooks:
+            if isinstance(hook, VerletHook):
+                getattr(hook, kind)(self)
+
     def _compute_ekin(self):
-        return 0.5 * ((self.vel ** 2).sum(axis=1) * self.masses).sum()
+        return 0.5 * (self.vel ** 2 * self.masses.reshape(-1, 1)).sum()
+
+    @property
+    def econs_correction(self):
+        return sum(h.econs_correction for h in self.hooks if isinstance(h, VerletHook))
 
     def compute_properties(self):
         self.ekin = self._compute_ekin()
@@ -101,9 +371,13 @@ class VerletIntegrator(object):
         self.ff.update_pos(self.pos)
         self.epot = self.ff.compute(self.gpos)
         self.acc = -self.gpos / self.masses.reshape(-1, 1)
+        self._verlet_hooks('init')
+        if self.ndof is None:
+            self.ndof = self.pos.size
         self.compute_properties()
 
     def propagate(self):
+        self._verlet_hooks('pre')
         self.acc = -self.gpos / self.masses.reshape(-1, 1)
         self.vel += 0.5 * self.acc * self.timestep
         self.pos += self.timestep * self.vel
@@ -113,11 +387,14 @@ class VerletIntegrator(object):
         self.epot = self.ff.compute(self.gpos, self.vtens)
         self.acc = -self.gpos / self.masses.reshape(-1, 1)
         self.vel += 0.5 * self.acc * self.timestep
+        self.ekin = self._compute_ekin()
+        self._verlet_hooks('post')
         self.time += self.timestep
         self.counter += 1
         self.compute_properties()
         for hook in self.hooks:
-            hook(self)
+            if not isinstance(hook, VerletHook):
+                hook(self)
 
     def run(self, nstep):
         for _ in range(nstep):
@@ -134,8 +411,12 @@ def drift_per_ps(times, econs, natom):
 
 
 class DeviceVerlet(object):
-    """NVE velocity Verlet with positions, velocities, masses and the
-    neighbour list resident in HBM (yg_md_* of libyaffgb.so).
+    """Velocity Verlet with positions, velocities, masses and the neighbour
+    list resident in HBM (yg_md_* of libyaffgb.so); NVE, or NVT with
+    ``thermostat`` a BerendsenThermostat, LangevinThermostat, CSVRThermostat
+    or NHCThermostat (its init runs on the host, its pre / post updates in
+    the device step; the stochastic ones draw from a counter-based generator
+    keyed by ``seed``, not from NumPy).
 
     The same step as VerletIntegrator (yaff/sampling/verlet.py:339-367) and
     the same skin rule for rebuilding the list (yaff/pes/nlist.py:207-218),
@@ -147,7 +428,7 @@ class DeviceVerlet(object):
     """
 
     def __init__(self, ff, timestep, vel0=None, temp0=300.0, scalevel0=True, rng=None, max_steps=1000,
-                 use_graph=True):
+                 use_graph=True, thermostat=None, seed=0, ndof=None):
         from . import _lib
         from ._lib import check, ptr
         self._lib, self._check, self._ptr = _lib, check, ptr
@@ -159,18 +440,55 @@ class DeviceVerlet(object):
         self.masses = np.ascontiguousarray(system.masses, dtype=np.float64)
         if vel0 is None:
             vel0 = get_random_vel(temp0, scalevel0, self.masses, rng=rng)
-        vel0 = np.ascontiguousarray(vel0, dtype=np.float64)
+        vel0 = np.array(vel0, dtype=np.float64, order='C')
         # one evaluation through the fused path builds the list and uploads
         # every parameter the device step needs
         ff.update_pos(system.pos)
         ff.compute(np.zeros((self.natom, 3)))
+        self.thermostat = thermostat
+        self.ndof = ndof
+        if thermostat is not None:
+            # the thermostat's own init on the host (momenta, degrees of
+            # freedom, chain), as the reference's VerletIntegrator calls it
+            self.pos, self.vel, self.ekin = system.pos.copy(), vel0, None
+            self.ekin = self._compute_ekin()
+            thermostat.init(self)
+            if self.ndof is None:
+                self.ndof = get_ndof_internal_md(self.natom, system.cell.nvec)
+            vel0 = np.ascontiguousarray(self.vel)
         self.dev, self.mask, self.const_energy = ff.device_md_terms()
         self.skin = float(ff.nlist.skin) if ff.nlist is not None else 0.0
         self.max_steps = int(max_steps)
         check(self.dev.lib.yg_md_setup(self.dev.ctx, ptr(self.masses), ptr(vel0), self.timestep, self.mask,
                                        self.const_energy, self.max_steps), 'yg_md_setup')
+        if thermostat is not None:
+            kind = thermostat.device_kind
+            if kind is None:
+                raise NotImplementedError('%s has no device form' % type(thermostat).__name__)
+            timecon = thermostat.chain.timecon if kind == 4 else thermostat.timecon
+            nc = thermostat.chain.length if kind == 4 else 0
+            cp = np.ascontiguousarray(thermostat.chain.pos, float) if kind == 4 else None
+            cv = np.ascontiguousarray(thermostat.chain.vel, float) if kind == 4 else None
+            cm = np.ascontiguousarray(thermostat.chain.masses, float) if kind == 4 else None
+            check(self.dev.lib.yg_md_thermostat(self.dev.ctx, kind, boltzmann * thermostat.temp, float(timecon),
+                                                int(self.ndof), nc, ptr(cp), ptr(cv), ptr(cm), int(seed)),
+                  'yg_md_thermostat')
         self.counter = 0
         self.nrebuild = 0
+
+    def _compute_ekin(self):
+        return 0.5 * (self.vel ** 2 * self.masses.reshape(-1, 1)).sum()
+
+    def thermo_state(self):
+        """(conserved-energy correction, chain positions, chain velocities)
+        of the device thermostat."""
+        import ctypes
+        e = ctypes.c_double()
+        n = self.thermostat.chain.length if getattr(self.thermostat, 'device_kind', None) == 4 else 0
+        cp, cv = np.zeros(n), np.zeros(n)
+        self._check(self.dev.lib.yg_md_thermo_get(self.dev.ctx, ctypes.byref(e), self._ptr(cp), self._ptr(cv)),
+                    'yg_md_thermo_get')
+        return e.value, cp, cv
 
     def run(self, nstep):
         import ctypes
