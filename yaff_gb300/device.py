@@ -124,15 +124,18 @@ class DeviceSystem(object):
         check(self.lib.yg_set_charges(self.ctx, ptr(q)), 'yg_set_charges')
         self._charges_key = q.copy()
 
-    def upload_positions(self, pos=None):
-        """Copies the current positions (host array) to the device."""
+    def upload_positions(self, pos=None, wait=True):
+        """Copies the current positions (host array) to the device.  The copy
+        reads the system's own (user-visible, page-locked) positions
+        asynchronously; wait=True returns only when it is done, so that the
+        caller may write them again.  wait=False is for callers that
+        synchronize with the device before returning to user code."""
         src = self.system.pos if pos is None else pos
         if src is not self._pos_staging:
             self._pos_staging[:] = src
         check(self.lib.yg_set_positions(self.ctx, ptr(self._pos_staging), 0), 'yg_set_positions')
-        # the copy reads the system's own (user-visible) positions
-        # asynchronously: wait for it, so that callers may write them again
-        check(self.lib.yg_sync(self.ctx), 'yg_sync')
+        if wait:
+            check(self.lib.yg_sync(self.ctx), 'yg_sync')
 
     def upload_positions_device(self, dptr):
         check(self.lib.yg_set_positions(self.ctx, ctypes.c_void_p(dptr), 1), 'yg_set_positions')

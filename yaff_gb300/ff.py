@@ -177,8 +177,9 @@ class ForceField(ForcePart):
             return sum([part.compute(gpos, vtens) for part in self.parts])
         # fused device path: positions first, then the reciprocal sum (it
         # needs no neighbour list and runs on its own stream while the list
-        # is updated and the pair terms are evaluated)
-        dev.upload_positions()
+        # is updated and the pair terms are evaluated); the readback at the
+        # end synchronizes before the caller gets control back
+        dev.upload_positions(wait=False)
         want_grad = (gpos is not None) or (vtens is not None)
         mask = 0
         for part in self.parts:
