@@ -27,8 +27,8 @@
 #include "yg_internal.cuh"
 
 #define YG_CELL_DIV 4      // grid cells at least r_c / 4 wide
-#define YG_BUILD_RUNS 144  // candidate runs per warp held in shared memory (4 blocks of 8 warps fit an SM)
-#define YG_BUILD_MAP 4096  // candidates per warp whose run index is tabulated
+#define YG_BUILD_RUNS 192  // candidate runs per warp held in shared memory
+#define YG_BUILD_MAP 3072  // candidates per warp whose run index is tabulated (4 blocks of 8 warps fit an SM)
 
 namespace {
 
