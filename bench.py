@@ -324,8 +324,8 @@ def run_gb300(args, world, rank, local):
             'tensor_tflops_executed': 72.0 * natom * nk / t_reci / 1e12,
             'warp_mma_f16_peak_tflops': mma_probe,
             'frac_of_warp_mma_peak': (72.0 * natom * nk / t_reci / 1e12 / mma_probe) if mma_probe else None,
-            'traffic': 75.3e6 * nat_scale,
-            'traffic_source': 'ncu dram read+write of k_sfac_mma (39.4 MB) + k_ewald_force_mma (35.9 MB) at 50,000 '
+            'traffic': 76.3e6 * nat_scale,
+            'traffic_source': 'ncu dram read+write of k_sfac_mma (40.3 MB) + k_ewald_force_mma (36.0 MB) at 50,000 '
                               'atoms' + ('' if natom == 50000 else ', scaled by atoms')}
     else:
         rooflines['ewald_reciprocal'] = {
@@ -344,7 +344,7 @@ def run_gb300(args, world, rank, local):
         'kernel': 'k_bin + k_scan_cells + k_scatter + k_sort_cells + k_origins + k_prep + k_build (full rows, '
                   'exact FP64 decisions in the FP32 guard band)',
         'ms': t_build * 1e3, 'units': {'rows': nrow, 'bytes': bbytes},
-        'traffic': 309.6e6 * nat_scale,
+        'traffic': 310.2e6 * nat_scale,
         'traffic_source': 'ncu dram read+write of k_build (the candidate sweep) at 50,000 atoms: it writes both '
                           'directions of every pair' + ('' if natom == 50000 else ', scaled by atoms')}
     # (b) pair terms: 75 flops (+3 transcendentals) per half-list pair within rcut; the pairs within rcut
@@ -358,7 +358,7 @@ def run_gb300(args, world, rank, local):
         'frac': (75.0 * npair / t_pair / 1e12 / fp32_peak) if fp32_peak else None,
         'kernel': 'k_pair<MM3, EI> (one warp per atom over its full row; each pair is evaluated from both ends)',
         'ms': t_pair * 1e3, 'units': {'pairs_within_rcut': npair, 'flops_per_pair': 75, 'transcendentals_per_pair': 3},
-        'traffic': 376.8e6 * nat_scale,
+        'traffic': 380.1e6 * nat_scale,
         'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms' + ('' if natom == 50000 else
                                                                              ', scaled by atoms')}
     dom = max(rooflines, key=lambda k: rooflines[k]['ms'])
