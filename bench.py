@@ -27,6 +27,8 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
+from yaff_gb300 import replicas  # noqa: E402
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -99,10 +101,8 @@ class ClockSampler(object):
 
 
 def dist_setup():
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    return world, rank, local
+    from yaff_gb300.replicas import dist_env
+    return dist_env()
 
 
 def peaks():
@@ -256,12 +256,8 @@ def run_gb300(args, world, rank, local):
     ewald_times = phase_times['ewald_reciprocal']
     clk = clocks.stop()
     t_step = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([sum(times)], dtype=torch.float64, device='cuda')
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
-    else:
-        total = float(sum(times))
+    # independent replicas: the slowest rank's time (no collective in the steps)
+    total = replicas.max_over_ranks(sum(times))
     value = world * args.steps / total
 
     # --- e2e through the public API: host numpy positions in, gradient out ---
@@ -688,12 +684,7 @@ def main():
     args = parse()
     world, rank, local = dist_setup()
     if world > 1:
-        import torch
-        import torch.distributed as dist
-        backend = 'gloo' if args.impl == 'reference' else 'nccl'
-        if args.impl == 'gb300':
-            torch.cuda.set_device(local)
-        dist.init_process_group(backend)
+        replicas.init('gloo' if args.impl == 'reference' else 'nccl')
     if args.impl == 'reference':
         out = run_reference(args, world, rank)
         if out is not None:
