@@ -531,5 +531,11 @@ class OracleForceField(object):
             vtens.ravel()[::4] -= fac
         return fac
 
+    def update_rvecs(self, rvecs):
+        """New cell: rmax and gmax follow, the next list is a full rebuild
+        (yaff/pes/ff.py:97-103, nlist.py:102-110, ff.py:381-386)."""
+        self.cell = OracleCell(rvecs)
+        self.update_rmax()
+
     def update_pos(self, pos):
         self.pos[:] = pos

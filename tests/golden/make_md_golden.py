@@ -8,7 +8,9 @@ or $YAFF_REFERENCE) after ``sh oracle/build_ref.sh``:
 For each thermostat of the reference (Berendsen, Langevin, CSVR, Nose-Hoover
 chain) the script runs the reference's own VerletIntegrator with that hook on
 the 64-molecule flexible water box (reference force field), 12 steps of
-0.5 fs from fixed initial velocities, and stores positions, velocities,
+0.5 fs from fixed initial velocities (md_thermostats.npz), and the Berendsen
+barostat with the Berendsen thermostat, isotropic and anisotropic
+(md_barostats.npz), and stores positions, velocities,
 kinetic, potential and conserved energies and the degrees of freedom per
 step.  The stochastic thermostats draw from NumPy's global generator, seeded
 per run (stored), in the reference's call order.
@@ -77,6 +79,38 @@ def main():
         print('%-10s ndof %d  T %.2f K  econs drift %.3e' % (name, vi.ndof, vi.temp / kelvin,
                                                               rows['econs'][-1] - rows['econs'][0]))
     np.savez_compressed(os.path.join(HERE, 'md_thermostats.npz'), **data)
+    barostat_runs(spec, vel0)
+
+
+def barostat_runs(spec, vel0):
+    """Berendsen thermostat + Berendsen barostat (isotropic, and anisotropic
+    with the cell symmetrized first) at 1 GPa -> md_barostats.npz: positions,
+    cells, energies and the conserved energy per step."""
+    from yaff.sampling.verlet import VerletIntegrator
+    from yaff.sampling.nvt import BerendsenThermostat
+    from yaff.sampling.npt import BerendsenBarostat
+    from yaff_gb300.units import pascal
+    press = 1e9 * pascal
+    data = {'pos0': spec['pos'], 'vel0': vel0, 'timestep': np.array(TIMESTEP), 'temp': np.array(TEMP),
+            'timecon': np.array(TIMECON), 'press': np.array(press), 'baro_timecon': np.array(200 * femtosecond),
+            'nstep': np.array(NSTEP)}
+    for name, aniso in (('iso', False), ('aniso', True)):
+        ff = build_reference_ff(spec)
+        th = BerendsenThermostat(TEMP, timecon=TIMECON)
+        baro = BerendsenBarostat(ff, TEMP, press, timecon=200 * femtosecond, anisotropic=aniso)
+        vi = VerletIntegrator(ff, TIMESTEP, hooks=[th, baro], vel0=vel0.copy())
+        rows = {'pos': [vi.pos.copy()], 'rvecs': [ff.system.cell.rvecs.copy()], 'epot': [vi.epot],
+                'econs': [vi.econs]}
+        for _ in range(NSTEP):
+            vi.propagate()
+            rows['pos'].append(vi.pos.copy())
+            rows['rvecs'].append(ff.system.cell.rvecs.copy())
+            rows['epot'].append(vi.epot)
+            rows['econs'].append(vi.econs)
+        for key, v in rows.items():
+            data['%s_%s' % (name, key)] = np.array(v)
+        print('%-6s volume %.6f -> %.6f' % (name, np.linalg.det(rows['rvecs'][0]), np.linalg.det(rows['rvecs'][-1])))
+    np.savez_compressed(os.path.join(HERE, 'md_barostats.npz'), **data)
 
 
 if __name__ == '__main__':

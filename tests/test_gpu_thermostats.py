@@ -83,3 +83,27 @@ def test_device_stochastic_thermostat_temperature(name):
             assert abs(t_mean - temp) <= 0.03 * temp, (name, t_mean)
     # a replay with the same seed gives the same trajectory
     assert np.allclose(runs[0][1][:200], runs[1][1][:200], rtol=1e-9, atol=0)
+
+
+BARO = dict(np.load(os.path.join(gc.GOLDEN, 'md_barostats.npz')))
+
+
+@pytest.mark.parametrize('name', ['iso', 'aniso'])
+def test_barostat_on_device_force_field(name):
+    """The host Berendsen barostat (with the Berendsen thermostat) driving
+    the FP64 device force field through cell changes (ForceField.update_rvecs:
+    new cell, k-space set-up and list) follows the reference trajectory."""
+    import yaff_gb300
+    from yaff_gb300 import verlet
+    spec = _spec()
+    ff = yaff_gb300.build_forcefield(spec, precision='fp64')
+    T, tc = float(BARO['temp']), float(BARO['timecon'])
+    th = verlet.BerendsenThermostat(T, timecon=tc)
+    baro = verlet.BerendsenBarostat(ff, T, float(BARO['press']), timecon=float(BARO['baro_timecon']),
+                                    anisotropic=(name == 'aniso'))
+    vi = verlet.VerletIntegrator(ff, float(BARO['timestep']), vel0=BARO['vel0'].copy(), hooks=[th, baro])
+    vi.run(int(BARO['nstep']))
+    ref = BARO['%s_pos' % name][-1]
+    assert np.allclose(vi.pos, ref, rtol=0, atol=1e-8 * abs(ref).max())
+    assert np.allclose(ff.system.cell.rvecs, BARO['%s_rvecs' % name][-1], rtol=0, atol=1e-9 * 30)
+    assert abs(vi.econs - BARO['%s_econs' % name][-1]) <= 1e-8 * abs(BARO['%s_econs' % name][-1])

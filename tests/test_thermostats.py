@@ -2,7 +2,9 @@
 Langevin, CSVR, Nose-Hoover chain), driving the oracle force field, follows
 the reference's own VerletIntegrator trajectories stored in
 tests/golden/md_thermostats.npz (made by make_md_golden.py): positions,
-velocities, kinetic and conserved energies over 12 steps.  The stochastic
+velocities, kinetic and conserved energies over 12 steps; with the Berendsen
+barostat added (isotropic and anisotropic), positions, cells, potential and
+conserved energies follow tests/golden/md_barostats.npz.  The stochastic
 thermostats draw from NumPy's global generator in the reference's call
 order, seeded as the reference run was."""
 import os
@@ -64,3 +66,40 @@ def test_ndof_and_momenta():
     assert np.allclose(m @ vel, 0, atol=1e-12)
     com = m @ pos / m.sum()
     assert np.allclose((np.cross(pos - com, vel) * m[:, None]).sum(0), 0, atol=1e-10)
+
+
+BARO = dict(np.load(os.path.join(gc.GOLDEN, 'md_barostats.npz')))
+
+
+class _OracleAdapter(object):
+    """The oracle as a force field whose system follows its cell."""
+
+    def __init__(self, spec):
+        self.orc = OracleForceField(spec)
+        self.system = types.SimpleNamespace(pos=self.orc.pos, masses=spec['masses'], cell=self.orc.cell)
+
+    def __getattr__(self, name):
+        return getattr(self.orc, name)
+
+    def update_rvecs(self, rvecs):
+        self.orc.update_rvecs(rvecs)
+        self.system.cell = self.orc.cell
+
+
+@pytest.mark.parametrize('name', ['iso', 'aniso'])
+def test_host_barostat_matches_reference(name):
+    spec = configs.flexible_water(nside=4, box=12.42, rcut=5.0, skin=0.5, name='water64')
+    ff = _OracleAdapter(spec)
+    T, tc = float(BARO['temp']), float(BARO['timecon'])
+    th = verlet.BerendsenThermostat(T, timecon=tc)
+    baro = verlet.BerendsenBarostat(ff, T, float(BARO['press']), timecon=float(BARO['baro_timecon']),
+                                    anisotropic=(name == 'aniso'))
+    vi = verlet.VerletIntegrator(ff, float(BARO['timestep']), vel0=BARO['vel0'].copy(), hooks=[th, baro])
+    for s in range(int(BARO['nstep']) + 1):
+        if s:
+            vi.propagate()
+        ref = BARO['%s_pos' % name][s]
+        assert np.allclose(vi.pos, ref, rtol=0, atol=1e-11 * abs(ref).max()), (name, s)
+        assert np.allclose(ff.orc.cell.rvecs, BARO['%s_rvecs' % name][s], rtol=0, atol=1e-12 * 30), (name, s)
+        assert abs(vi.epot - BARO['%s_epot' % name][s]) <= 1e-10 * abs(BARO['%s_epot' % name][s])
+        assert abs(vi.econs - BARO['%s_econs' % name][s]) <= 1e-10 * abs(BARO['%s_econs' % name][s])

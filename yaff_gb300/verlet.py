@@ -10,15 +10,16 @@ FP64 NumPy arrays on the host; every step calls ``ff.update_pos`` and
 force field is a drop-in for its force evaluation.  The Berendsen, Langevin,
 CSVR and Nose-Hoover-chain thermostats (yaff/sampling/nvt.py:110-500) work
 as host hooks of VerletIntegrator and, through ``DeviceVerlet(thermostat=)``,
-inside the device-resident step.  Barostats, HDF5 output and restarts are not
-part of this module.
+inside the device-resident step; the Berendsen barostat (yaff/sampling/npt.py)
+as a host hook.  The other barostats, HDF5 output and restarts are not part of
+this module.
 """
 import numpy as np
 
 from .units import boltzmann, femtosecond
 
 __all__ = ['get_random_vel', 'ConsErrTracker', 'VerletIntegrator', 'VerletHook', 'clean_momenta',
-           'get_ndof_internal_md', 'BerendsenThermostat', 'LangevinThermostat', 'CSVRThermostat', 'NHChain',
+           'get_ndof_internal_md', 'get_ndof_baro', 'cell_symmetrize', 'BerendsenBarostat', 'BerendsenThermostat', 'LangevinThermostat', 'CSVRThermostat', 'NHChain',
            'NHCThermostat', 'DeviceVerlet']
 
 
@@ -49,6 +50,24 @@ def clean_momenta(pos, vel, masses, cell):
         remove_angular_moment(pos, vel, masses)
     elif cell.nvec == 1:
         raise NotImplementedError
+
+
+def get_ndof_baro(dim, anisotropic, vol_constraint):
+    """Degrees of freedom of the cell (yaff/sampling/utils.py:406-428)."""
+    n = dim * (dim + 1) // 2 if anisotropic else 1
+    return n - 1 if vol_constraint else n
+
+
+def cell_symmetrize(ff):
+    """Rotates the cell (and the positions with it) so that the cell matrix
+    is symmetric: rvecs @ V U^T from its singular value decomposition
+    (yaff/sampling/utils.py:289-331)."""
+    cell = ff.system.cell.rvecs.copy()
+    U, s, Vt = np.linalg.svd(cell)
+    rot_mat = np.dot(Vt.T, U.T)
+    ff.update_rvecs(np.dot(cell, rot_mat))
+    ff.update_pos(np.dot(ff.system.pos, rot_mat))
+    return rot_mat
 
 
 def get_ndof_internal_md(natom, nper):
@@ -316,6 +335,70 @@ class NHCThermostat(VerletHook):
         self.econs_correction = self.chain.get_econs_correction()
 
 
+class BerendsenBarostat(VerletHook):
+    """Weak-coupling cell rescaling towards the pressure `press`: after each
+    step positions and cell are multiplied by mu = 1 - dt/W (P0 - P) (made
+    symmetric; isotropic unless `anisotropic`), the forces are evaluated
+    again, and the energy change goes into the conserved-energy correction
+    (Berendsen et al., J. Chem. Phys. 81, 3684 (1984); yaff/sampling/npt.py:
+    232-330).  A host hook: each step makes one extra force evaluation at the
+    rescaled cell, through ForceField.update_rvecs."""
+
+    def __init__(self, ff, temp, press, start=0, step=1, timecon=1000 * femtosecond, beta=None,
+                 anisotropic=True, vol_constraint=False, restart=False):
+        from .units import bar
+        self.temp = temp
+        self.press = press
+        self.timecon_press = timecon
+        self.beta = 4.57e-5 / bar if beta is None else beta
+        self.mass_press = 3.0 * timecon / self.beta
+        self.anisotropic = anisotropic
+        self.vol_constraint = vol_constraint
+        self.dim = ff.system.cell.nvec
+        self.baro_ndof = get_ndof_baro(self.dim, self.anisotropic, self.vol_constraint)
+        if self.anisotropic:
+            cell_symmetrize(ff)
+        self.cell = ff.system.cell.rvecs.copy()
+        self.restart = restart
+        VerletHook.__init__(self, start, step)
+
+    def init(self, iterative):
+        self.timestep_press = iterative.timestep
+        if not self.restart:
+            clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        iterative.gpos[:] = 0.0
+        iterative.vtens[:] = 0.0
+        iterative.epot = iterative.ff.compute(iterative.gpos, iterative.vtens)
+        if iterative.ndof is None:
+            iterative.ndof = get_ndof_internal_md(iterative.pos.shape[0], iterative.ff.system.cell.nvec)
+        self.mass_press *= np.sqrt(iterative.ndof)
+
+    def pre(self, iterative, G1_add=None):
+        pass
+
+    def post(self, iterative, G1_add=None):
+        epot0 = iterative.epot
+        ptens = (np.dot(iterative.vel.T * iterative.masses, iterative.vel) - iterative.vtens) / \
+            iterative.ff.system.cell.volume
+        dmu = self.timestep_press / self.mass_press * (self.press * np.eye(3) - ptens)
+        if self.vol_constraint:
+            dmu -= np.trace(dmu) / self.dim * np.eye(self.dim)
+        mu = np.eye(3) - dmu
+        mu = 0.5 * (mu + mu.T)
+        if not self.anisotropic:
+            mu = ((np.trace(mu) / 3.0) ** (1.0 / 3.0)) * np.eye(3)
+        pos_new = np.dot(iterative.pos, mu)
+        rvecs_new = np.dot(iterative.rvecs, mu)
+        iterative.ff.update_pos(pos_new)
+        iterative.pos[:] = pos_new
+        iterative.ff.update_rvecs(rvecs_new)
+        iterative.rvecs[:] = rvecs_new
+        iterative.gpos[:] = 0.0
+        iterative.vtens[:] = 0.0
+        iterative.epot = iterative.ff.compute(iterative.gpos, iterative.vtens)
+        self.econs_correction += epot0 - iterative.epot
+
+
 class VerletIntegrator(object):
     """Velocity Verlet with the reference's hook protocol.
 
@@ -333,6 +416,8 @@ class VerletIntegrator(object):
         system = ff.system
         self.pos = system.pos.copy()
         self.masses = np.asarray(system.masses, dtype=np.float64)
+        cell = getattr(system, 'cell', None)
+        self.rvecs = cell.rvecs.copy() if cell is not None and cell.nvec > 0 else None
         if vel0 is None:
             vel0 = get_random_vel(temp0, scalevel0, self.masses, rng=rng)
         self.vel = np.array(vel0, dtype=np.float64)
