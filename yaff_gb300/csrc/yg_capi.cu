@@ -129,8 +129,12 @@ int yg_ensure(yg_ctx *ctx, void **ptr, size_t *cap, size_t bytes) {
 }
 
 namespace {
+// Sums the requested parts: scalars into out[0..16), the gradient into
+// gout[0..3N) (device memory, or the page-locked host mirror through its
+// device alias).
 __global__ void k_total(const double *__restrict__ part_ev, const double *__restrict__ part_gpos, int64_t natom,
-                        int mask, int want_gpos, double *__restrict__ out, int *__restrict__ nan_flag) {
+                        int mask, int want_gpos, double *__restrict__ out, double *__restrict__ gout,
+                        int *__restrict__ nan_flag) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < 10) {
     double s = 0.0;
@@ -143,7 +147,7 @@ __global__ void k_total(const double *__restrict__ part_ev, const double *__rest
     double s = 0.0;
     for (int p = 0; p < YG_NPART; p++)
       if (mask & (1 << p)) s += part_gpos[(int64_t)p * natom * 3 + t];
-    out[16 + t] = s;
+    gout[t] = s;
     if (isnan(s)) atomicOr(nan_flag, 1);
   }
 }
@@ -265,6 +269,8 @@ int yg_destroy(yg_ctx *c) {
   if (c->md_cap_stream) cudaStreamDestroy(c->md_cap_stream);
   if (c->ew_aux) cudaStreamDestroy(c->ew_aux);
   if (c->ew_fork_ev) cudaEventDestroy(c->ew_fork_ev);
+  for (int k = 0; k < YG_RB_CHUNKS; k++)
+    if (c->rb_ev[k]) cudaEventDestroy(c->rb_ev[k]);
   if (c->ew_join_ev) cudaEventDestroy(c->ew_join_ev);
   if (c->pool) {
     for (void **b : bufs) yg_free(c, b);
@@ -781,34 +787,72 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
   const int want_gpos = gpos != nullptr;
   int64_t nthreads = want_gpos ? std::max<int64_t>(n3, 16) : 16;
   YG_CUDA(cudaMemsetAsync(c->d_status + YG_ST_NANGRAD, 0, sizeof(int), c->stream));
+  // the gradient goes straight into the page-locked mirror when the device
+  // can address it (checked once per context), so no separate copy follows
+  if (c->h_total_dev_state == 0) {
+    void *alias = nullptr;
+    const cudaError_t ae = cudaHostGetDevicePointer(&alias, c->h_total, 0);
+    c->h_total_dev = (ae == cudaSuccess) ? (double *)alias : nullptr;
+    c->h_total_dev_state = 1;
+    if (ae != cudaSuccess) cudaGetLastError();  // clear the error of the query
+  }
+  double *gout = (want_gpos && c->h_total_dev) ? c->h_total_dev + 16 : c->d_total + 16;
   k_total<<<yg_blocks(nthreads, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom, part_mask,
-                                                          want_gpos, c->d_total, c->d_status + YG_ST_NANGRAD);
+                                                          want_gpos, c->d_total, gout, c->d_status + YG_ST_NANGRAD);
   YG_LAUNCH_CHECK(c, "k_total");
-  size_t bytes = (16 + (want_gpos ? n3 : 0)) * sizeof(double);
+  // status and scalars first, then the gradient in chunks: the host adds
+  // (or copies) chunk k while chunk k + 1 is still being transferred
   YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  YG_CUDA(cudaMemcpyAsync(c->h_total, c->d_total, bytes, cudaMemcpyDeviceToHost, c->stream));
-  YG_CUDA(cudaStreamSynchronize(c->stream));
+  YG_CUDA(cudaMemcpyAsync(c->h_total, c->d_total, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  const bool direct = want_gpos && c->h_total_dev;
+  const int nchunk = (!want_gpos || direct) ? 0 : (n3 >= (1 << 16) ? YG_RB_CHUNKS : 1);
+  int64_t cut[YG_RB_CHUNKS + 1];
+  for (int k = 0; k <= nchunk; k++) cut[k] = n3 * k / (nchunk ? nchunk : 1);
+  for (int k = 0; k < nchunk; k++) {
+    if (!c->rb_ev[k]) YG_CUDA(cudaEventCreateWithFlags(&c->rb_ev[k], cudaEventDisableTiming));
+    YG_CUDA(cudaMemcpyAsync(c->h_total + 16 + cut[k], c->d_total + 16 + cut[k], (cut[k + 1] - cut[k]) * sizeof(double),
+                            cudaMemcpyDeviceToHost, c->stream));
+    YG_CUDA(cudaEventRecord(c->rb_ev[k], c->stream));
+  }
+  if (nchunk) YG_CUDA(cudaEventSynchronize(c->rb_ev[0]));
+  else YG_CUDA(cudaStreamSynchronize(c->stream));
+  int rc = YG_OK;
   if (c->h_status[YG_ST_TIMEOUT]) {
     yg_set_error("a bounded wait on an asynchronous copy gave up; results are invalid");
-    return YG_ERR_CUDA;
-  }
-  if (energy) *energy = c->h_total[0];
-  if (part_energies) memcpy(part_energies, c->h_total + 10, YG_NPART * sizeof(double));
-  if (std::isnan(c->h_total[0])) return YG_ERR_NAN;
-  if (want_gpos && c->h_status[YG_ST_NANGRAD]) {
+    rc = YG_ERR_CUDA;
+  } else if (std::isnan(c->h_total[0])) {
+    rc = YG_ERR_NAN;
+  } else if (want_gpos && c->h_status[YG_ST_NANGRAD]) {
     yg_set_error("not-a-number in the gradient");
-    return YG_ERR_NAN;
+    rc = YG_ERR_NAN;
   }
-  if (add) {
-    if (vtens)
+  if (rc == YG_OK || rc == YG_ERR_NAN) {
+    if (energy) *energy = c->h_total[0];
+    if (part_energies) memcpy(part_energies, c->h_total + 10, YG_NPART * sizeof(double));
+  }
+  if (rc) {
+    YG_CUDA(cudaStreamSynchronize(c->stream));  // no copy left in flight into the mirror
+    return rc;
+  }
+  if (vtens) {
+    if (add)
       for (int k = 0; k < 9; k++) vtens[k] += c->h_total[1 + k];
-    if (gpos) {
-      const double *src = c->h_total + 16;
-      for (int64_t k = 0; k < n3; k++) gpos[k] += src[k];
-    }
-  } else {
-    if (vtens) memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
-    if (gpos) memcpy(gpos, c->h_total + 16, n3 * sizeof(double));
+    else
+      memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
+  }
+  if (direct) {
+    cut[0] = 0;
+    cut[1] = n3;
+  }
+  for (int k = 0; k < (direct ? 1 : nchunk); k++) {
+    if (k) YG_CUDA(cudaEventSynchronize(c->rb_ev[k]));
+    const double *src = c->h_total + 16 + cut[k];
+    double *dst = gpos + cut[k];
+    const int64_t m = cut[k + 1] - cut[k];
+    if (add)
+      for (int64_t q = 0; q < m; q++) dst[q] += src[q];
+    else
+      memcpy(dst, src, m * sizeof(double));
   }
   return YG_OK;
 }

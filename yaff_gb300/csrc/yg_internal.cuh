@@ -15,6 +15,7 @@
 #include "../../include/yaffgb.h"
 
 #define YG_MAX_POT 3
+#define YG_RB_CHUNKS 4   // chunks of the pipelined gradient readback
 #define YG_WARP 32
 
 // Device status words (yg_ctx::d_status)
@@ -268,6 +269,9 @@ struct yg_ctx {
   double *d_part_gpos = nullptr;  // YG_NPART*natom*3
   double *d_total = nullptr;      // 10 + natom*3
   double *h_total = nullptr;      // pinned mirror
+  cudaEvent_t rb_ev[YG_RB_CHUNKS] = {};  // chunks of the gradient readback
+  double *h_total_dev = nullptr;  // device alias of h_total (page-locked, mapped), when the device has one
+  int h_total_dev_state = 0;      // 0: not queried yet
   double *d_red = nullptr;        // block partials for energy/virial reductions
   size_t red_cap = 0;
   int part_valid[YG_NPART] = {0, 0, 0, 0, 0, 0};
