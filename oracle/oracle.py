@@ -18,8 +18,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, 'yaff_oracle.c')
+SRC_MT = os.path.join(HERE, 'yaff_oracle_mt.c')
 BUILD_DIR = os.path.join(HERE, '_build')
 LIB = os.path.join(BUILD_DIR, 'libyaff_oracle.so')
+LIB_MT = os.path.join(BUILD_DIR, 'libyaff_oracle_mt.so')
 
 neigh_dtype = np.dtype([('a', 'i8'), ('b', 'i8'), ('d', 'f8'), ('dx', 'f8'), ('dy', 'f8'),
                         ('dz', 'f8'), ('r0', 'i8'), ('r1', 'i8'), ('r2', 'i8')])
@@ -37,15 +39,41 @@ _lib = None
 
 
 def build():
-    """Compile yaff_oracle.c (gcc, no FMA contraction) if stale."""
+    """Compile yaff_oracle.c and its threaded timing form yaff_oracle_mt.c
+    (gcc, no FMA contraction) if stale."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
-        return LIB
-    tmp = LIB + '.%d.tmp' % os.getpid()
-    subprocess.check_call(['gcc', '-O2', '-ffp-contract=off', '-fPIC', '-shared',
-                           '-o', tmp, SRC, '-lm'])
-    os.replace(tmp, LIB)
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(SRC_MT))
+    for out, src, extra in ((LIB, SRC, []), (LIB_MT, SRC_MT, ['-pthread'])):
+        if os.path.exists(out) and os.path.getmtime(out) >= newest:
+            continue
+        tmp = out + '.%d.tmp' % os.getpid()
+        subprocess.check_call(['gcc', '-O2', '-ffp-contract=off', '-fPIC', '-shared'] + extra +
+                              ['-o', tmp, src, '-lm'])
+        os.replace(tmp, out)
     return LIB
+
+
+_lib_mt = None
+
+
+def lib_mt():
+    """The threaded whole-evaluation entry points (yaff_oracle_mt.c)."""
+    global _lib_mt
+    if _lib_mt is None:
+        build()
+        L = ctypes.CDLL(LIB_MT)
+        P = ctypes.c_void_p
+        I64 = ctypes.c_int64
+        D = ctypes.c_double
+        INT = ctypes.c_int
+        L.orc_mt_nlist_build.restype = I64
+        L.orc_mt_nlist_build.argtypes = [P, I64, D, P, P, P, INT, I64, I64, P, I64, I64, INT]
+        L.orc_mt_pair_compute.restype = D
+        L.orc_mt_pair_compute.argtypes = [P, I64, P, I64, INT, P, P, P, P, P, D, D, D, INT, D, P, P, I64, INT]
+        L.orc_mt_ewald_reci.restype = D
+        L.orc_mt_ewald_reci.argtypes = [P, I64, I64, I64, P, P, P, D, D, P, D, D, P, P, INT]
+        _lib_mt = L
+    return _lib_mt
 
 
 def lib():
@@ -276,10 +304,16 @@ TERM_NPARS = {0: 2, 1: 4, 2: 2, 3: 3, 4: 3, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 6,
 
 
 class OracleForceField(object):
-    """Reference-order FP64 evaluation of a configs.py spec on the CPU."""
+    """Reference-order FP64 evaluation of a configs.py spec on the CPU.
 
-    def __init__(self, spec):
+    threads > 1 runs the neighbour-list build, the point-charge / per-atom
+    pair terms and the Ewald reciprocal sum on that many host threads
+    (yaff_oracle_mt.c: the same list, sums in a different order); used to
+    time whole evaluations of benchmark-sized systems."""
+
+    def __init__(self, spec, threads=1):
         self.spec = spec
+        self.threads = int(threads)
         self.natom = len(spec['pos'])
         self.pos = np.ascontiguousarray(spec['pos'], dtype=np.float64).copy()
         self.cell = OracleCell(spec['rvecs'])
@@ -321,10 +355,25 @@ class OracleForceField(object):
         if self.need_rebuild():
             rmax3 = np.zeros(3, np.int64)
             rmax3[:len(self.rmax)] = self.rmax
+            if self.threads > 1 and len(self.neighs) <= 16 and self.cell.nvec == 3:
+                # first threaded build: size the list from the number density
+                # (half the atoms within rcut + skin, 10 % margin) instead of
+                # letting a whole build run into a 16-row buffer first
+                rc = self.rcut + self.skin
+                est = 0.55 * self.natom * self.natom / self.cell.volume * 4.0 / 3.0 * np.pi * rc ** 3
+                self.neighs = np.zeros(int(est) + 1024, neigh_dtype)
             while True:
-                n = L.orc_nlist_build(_p(self.pos), self.natom, self.rcut + self.skin, _p(rmax3),
-                                      _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.nvec,
-                                      self.nlow, self.nhigh, _p(self.neighs), len(self.neighs))
+                if self.threads > 1:
+                    n = lib_mt().orc_mt_nlist_build(_p(self.pos), self.natom, self.rcut + self.skin, _p(rmax3),
+                                                    _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.nvec,
+                                                    self.nlow, self.nhigh, _p(self.neighs), len(self.neighs),
+                                                    max(self.nneigh, 16 * self.natom), self.threads)
+                    if n < 0:
+                        raise MemoryError('threaded neighbour-list build: out of memory')
+                else:
+                    n = L.orc_nlist_build(_p(self.pos), self.natom, self.rcut + self.skin, _p(rmax3),
+                                          _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.nvec,
+                                          self.nlow, self.nhigh, _p(self.neighs), len(self.neighs))
                 if n <= len(self.neighs):
                     break
                 self.neighs = np.zeros(int(n * 1.1) + 16, neigh_dtype)
@@ -467,6 +516,12 @@ class OracleForceField(object):
         keep = [np.ascontiguousarray(x) if x is not None else None for x in (sig, eps, op, q, radii)]
         if keep[2] is not None:
             keep[2] = keep[2].astype(np.int32)
+        if self.threads > 1:
+            return lib_mt().orc_mt_pair_compute(
+                _p(self.neighs), self.nneigh, _p(self.stab), len(self.stab), kind,
+                _p(keep[0]), _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4]),
+                alpha, spec.get('dielectric', 1.0), self.rcut, trk, trp, _p(gpos), _p(vtens), self.natom,
+                self.threads)
         return lib().orc_pair_compute(
             _p(self.neighs), self.nneigh, _p(self.stab), len(self.stab), kind,
             _p(keep[0]), _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4]),
@@ -489,10 +544,16 @@ class OracleForceField(object):
             elif name == 'ewald_reci':
                 ew = spec['ewald']
                 work = np.zeros(2 * self.natom) if g is not None else None
-                e = L.orc_ewald_reci(_p(self.pos), self.natom, self.nlow, self.nhigh,
-                                     _p(np.ascontiguousarray(spec['charges'])), _p(self.cell.rvecs),
-                                     _p(self.cell.gvecs), self.cell.volume, ew['alpha'], _p(self.gmax),
-                                     ew['gcut'], spec.get('dielectric', 1.0), _p(g), _p(work), _p(v))
+                if self.threads > 1:
+                    e = lib_mt().orc_mt_ewald_reci(
+                        _p(self.pos), self.natom, self.nlow, self.nhigh, _p(np.ascontiguousarray(spec['charges'])),
+                        _p(self.cell.rvecs), _p(self.cell.gvecs), self.cell.volume, ew['alpha'], _p(self.gmax),
+                        ew['gcut'], spec.get('dielectric', 1.0), _p(g), _p(v), self.threads)
+                else:
+                    e = L.orc_ewald_reci(_p(self.pos), self.natom, self.nlow, self.nhigh,
+                                         _p(np.ascontiguousarray(spec['charges'])), _p(self.cell.rvecs),
+                                         _p(self.cell.gvecs), self.cell.volume, ew['alpha'], _p(self.gmax),
+                                         ew['gcut'], spec.get('dielectric', 1.0), _p(g), _p(work), _p(v))
             elif name == 'ewald_cor':
                 ew = spec['ewald']
                 e = L.orc_ewald_corr(_p(self.pos), _p(np.ascontiguousarray(spec['charges'])),

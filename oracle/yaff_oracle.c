@@ -141,16 +141,32 @@ static int orc_next_image(const orc_cell *c, int64_t *r, const int64_t *rmax) {
  * rows; returns the total number of rows (callers regrow and rerun when the
  * total exceeds `cap`).  yaff/pes/nlist.c:30-131 (nlist_build_low) with the
  * status protocol of yaff/pes/nlist.py:163-186 replaced by count-and-retry. */
+int64_t orc_nlist_build_range(const double *pos, int64_t natom, double rcut,
+                              const int64_t *rmax, const double *rv, const double *gv,
+                              int nvec, int64_t nlow, int64_t nhigh, int64_t a_begin,
+                              int64_t a_end, orc_neigh *out, int64_t cap);
+
 int64_t orc_nlist_build(const double *pos, int64_t natom, double rcut,
                         const int64_t *rmax, const double *rv, const double *gv,
                         int nvec, int64_t nlow, int64_t nhigh,
                         orc_neigh *out, int64_t cap) {
+  return orc_nlist_build_range(pos, natom, rcut, rmax, rv, gv, nvec, nlow, nhigh, nlow, natom, out, cap);
+}
+
+/* The rows of orc_nlist_build whose first loop index a lies in
+ * [a_begin, a_end), in the same order (the full list is the concatenation of
+ * consecutive ranges). */
+int64_t orc_nlist_build_range(const double *pos, int64_t natom, double rcut,
+                              const int64_t *rmax, const double *rv, const double *gv,
+                              int nvec, int64_t nlow, int64_t nhigh, int64_t a_begin,
+                              int64_t a_end, orc_neigh *out, int64_t cap) {
   orc_cell c;
   int64_t a, b, n = 0, k;
   double rc2 = rcut * rcut;
+  (void)natom;
   for (k = 0; k < 9; k++) { c.rv[k] = rv[k]; c.gv[k] = gv[k]; }
   c.nvec = nvec;
-  for (a = nlow; a < natom; a++) {
+  for (a = a_begin; a < a_end; a++) {
     for (b = 0; b <= a; b++) {
       double d0[3];
       int64_t r[3] = {0, 0, 0};
@@ -600,14 +616,38 @@ static double orc_pair_loop(const orc_neigh *rows, int64_t n, const orc_scale *s
 /* Direct reciprocal-space sum over the half sphere |k| <= 2 pi gcut, with
  * the nlow/nhigh split (E = S0 (S0 + 2 (S1+S2)) + 2 S1 S2).
  * yaff/pes/ewald.c:32-150 (compute_ewald_reci). */
+double orc_ewald_reci_range(const double *pos, int64_t natom, int64_t nlow, int64_t nhigh,
+                            const double *charges, const double *gv, double volume, double alpha,
+                            const int64_t *gmax, double gcut, int64_t k_begin, int64_t k_end,
+                            double *gpos, double *work, double *vtens);
+
 double orc_ewald_reci(const double *pos, int64_t natom, int64_t nlow, int64_t nhigh,
                       const double *charges, const double *rv, const double *gv,
                       double volume, double alpha, const int64_t *gmax,
                       double gcut, double dielectric, double *gpos,
                       double *work, double *vtens) {
-  double kv[9], energy = 0.0, fac1, fac2, gc2, dfac;
-  int64_t g0, g1, g2, i;
+  double energy, dfac;
+  int64_t i;
   (void)rv;
+  energy = orc_ewald_reci_range(pos, natom, nlow, nhigh, charges, gv, volume, alpha, gmax, gcut, 0, INT64_MAX,
+                                gpos, work, vtens);
+  if (vtens) { vtens[0] -= energy; vtens[4] -= energy; vtens[8] -= energy; }
+  dfac = 1.0 / dielectric;
+  if (gpos) for (i = 0; i < 3 * natom; i++) gpos[i] *= dfac;
+  if (vtens) for (i = 0; i < 9; i++) vtens[i] *= dfac;
+  return energy * dfac;
+}
+
+/* The k-vectors of orc_ewald_reci with index (in the loop order of the half
+ * sphere, counting only those inside the cutoff) in [k_begin, k_end): their
+ * energy sum, with their gradient and virial terms added to gpos / vtens,
+ * before the dielectric scaling and the -E diagonal of the virial. */
+double orc_ewald_reci_range(const double *pos, int64_t natom, int64_t nlow, int64_t nhigh,
+                            const double *charges, const double *gv, double volume, double alpha,
+                            const int64_t *gmax, double gcut, int64_t k_begin, int64_t k_end,
+                            double *gpos, double *work, double *vtens) {
+  double kv[9], energy = 0.0, fac1, fac2, gc2;
+  int64_t g0, g1, g2, i, kidx = -1;
   for (i = 0; i < 9; i++) kv[i] = ORC_TWO_PI * gv[i];
   fac1 = ORC_FOUR_PI / volume;
   fac2 = 0.25 / alpha / alpha;
@@ -626,6 +666,9 @@ double orc_ewald_reci(const double *pos, int64_t natom, int64_t nlow, int64_t nh
         k[2] = (g0 * kv[2] + g1 * kv[5] + g2 * kv[8]);
         ksq = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
         if (ksq > gc2) continue;
+        kidx++;
+        if (kidx < k_begin) continue;
+        if (kidx >= k_end) return energy;
         for (i = 0; i < natom; i++) {
           x = k[0] * pos[3 * i] + k[1] * pos[3 * i + 1] + k[2] * pos[3 * i + 2];
           c = charges[i] * cos(x);
@@ -663,11 +706,7 @@ double orc_ewald_reci(const double *pos, int64_t natom, int64_t nlow, int64_t nh
       }
     }
   }
-  if (vtens) { vtens[0] -= energy; vtens[4] -= energy; vtens[8] -= energy; }
-  dfac = 1.0 / dielectric;
-  if (gpos) for (i = 0; i < 3 * natom; i++) gpos[i] *= dfac;
-  if (vtens) for (i = 0; i < 9; i++) vtens[i] *= dfac;
-  return energy * dfac;
+  return energy;
 }
 
 /* Ewald self-energy and the reciprocal-space double counting of scaled

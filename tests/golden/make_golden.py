@@ -112,6 +112,49 @@ def run_case(name, spec, displacements=(), full_rows=True):
         name, natom, ff.nlist.nneigh, data['step0_energy'], ff.nlist.rmax))
 
 
+def run_big_case(name, spec, displacements=()):
+    """Compact fixture of a benchmark-sized system (file big_<name>.npz):
+    positions, total energy / gradient / virial in FP64, per-part energies
+    and virials in FP64, per-part gradients in FP32 (ample for the 1e-5
+    relative RMS checks), and the neighbour list as its row count and the
+    SHA-256 of the sorted pair keys.  Step 0 rebuilds the list; the later
+    steps displace the atoms by less than half the skin, so the reference
+    takes its skin (recompute) path."""
+    if ONLY and ('big_' + name) not in ONLY:
+        return
+    ff = build_reference_ff(spec)
+    natom = len(spec['pos'])
+    data = spec_arrays(spec)
+    data['case'] = np.array(name)
+    data['nsteps'] = np.array(1 + len(displacements))
+    pos = spec['pos'].copy()
+    steps = [np.zeros_like(pos)] + list(displacements)
+    for s, dpos in enumerate(steps):
+        pos = pos + dpos
+        ff.update_pos(pos)
+        gpos = np.zeros((natom, 3))
+        vtens = np.zeros((3, 3))
+        e = ff.compute(gpos, vtens)
+        if s > 0:
+            data['step%d_pos' % s] = pos.copy()
+        data['step%d_energy' % s] = np.array(e)
+        data['step%d_gpos' % s] = gpos
+        data['step%d_vtens' % s] = vtens
+        data['step%d_parts' % s] = np.array([p.name for p in ff.parts])
+        data['step%d_part_energy' % s] = np.array([p.energy for p in ff.parts])
+        data['step%d_part_gpos32' % s] = np.array([p.gpos for p in ff.parts], dtype=np.float32)
+        data['step%d_part_vtens' % s] = np.array([p.vtens for p in ff.parts])
+        keys, _ = pair_keys(ff.nlist)
+        data['step%d_nneigh' % s] = np.array(ff.nlist.nneigh)
+        data['step%d_pairs_sha256' % s] = np.array(keys_digest(keys))
+        data['step%d_rebuilt' % s] = np.array(s == 0)
+        print('  %s step %d: E %.12e nneigh %d' % (name, s, e, ff.nlist.nneigh), flush=True)
+    data['rmax'] = np.asarray(ff.nlist.rmax)
+    np.savez_compressed(os.path.join(HERE, 'big_' + name + '.npz'), **data)
+    print('%-14s natom %6d  nneigh %8d  E %.12e  rmax %s' % (
+        name, natom, ff.nlist.nneigh, data['step0_energy'], ff.nlist.rmax))
+
+
 def fixture_system(getter):
     ref_shim.import_reference()
     import importlib.util
@@ -218,6 +261,16 @@ def main():
     for var in ('a', 'b', 'c', 'lj', 'mm3'):
         tc = configs.tail_corrections(var)
         run_case(tc['name'], tc)
+
+    # benchmark-sized systems (minutes of reference CPU time each): only when
+    # named on the command line, e.g. big_triclinic50000 big_water24000
+    brng = np.random.default_rng(4321)
+    if 'big_triclinic50000' in ONLY:
+        t5 = configs.triclinic_50000()
+        run_big_case('triclinic50000', t5, displacements=[brng.uniform(-0.05, 0.05, (50000, 3)) * angstrom])
+    if 'big_water24000' in ONLY:
+        w24 = configs.water_24000()
+        run_big_case('water24000', w24, displacements=[brng.uniform(-0.05, 0.05, (24000, 3)) * angstrom])
 
 
 if __name__ == '__main__':

@@ -11,9 +11,9 @@ GOLDEN = os.path.join(HERE, 'golden')
 
 def case_names():
     """Force-field cases (the mc_* fixtures hold MC trial cases, md_* MD
-    trajectories)."""
+    trajectories, big_* compact fixtures of the benchmark-sized systems)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz'))
-                  if not os.path.basename(p).startswith(('mc_', 'md_')))
+                  if not os.path.basename(p).startswith(('mc_', 'md_', 'big_')))
 
 
 def mc_case_names():
@@ -36,7 +36,12 @@ def load_mc(name):
 
 def load(name):
     """(spec, data) for a golden case."""
-    data = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
+    return load_path(os.path.join(GOLDEN, name + '.npz'))
+
+
+def load_path(path):
+    """(spec, data) for the force-field fixture at `path`."""
+    data = dict(np.load(path, allow_pickle=False))
     spec = {'pair': [], 'ewald': None, 'tr': None, 'charges': None, 'bonds': None}
     i = 0
     while 'pair%d_kind' % i in data:
