@@ -1,9 +1,10 @@
 """Generate tests/golden/md_thermostats.npz by running the reference.
 
-Run in a container that holds the reference checkout (default /root/reference,
-or $YAFF_REFERENCE) after ``sh oracle/build_ref.sh``:
+Run in a container that holds the reference checkout ($YAFF_REFERENCE) after
+``sh oracle/build_ref.sh``:
 
-    python tests/golden/make_md_golden.py
+    python tests/golden/make_md_golden.py            # thermostats, barostats
+    python tests/golden/make_md_golden.py water24000 # md_water24000.npz only
 
 For each thermostat of the reference (Berendsen, Langevin, CSVR, Nose-Hoover
 chain) the script runs the reference's own VerletIntegrator with that hook on
@@ -113,5 +114,38 @@ def barostat_runs(spec, vel0):
     np.savez_compressed(os.path.join(HERE, 'md_barostats.npz'), **data)
 
 
+def nve_water24000(nstep=10):
+    """NVE of the 8,000-molecule (24,000-atom) flexible water workload with the
+    reference's own VerletIntegrator and force field: nstep steps of 0.5 fs
+    from seeded 300 K Maxwell velocities (stored) -> md_water24000.npz with the
+    potential, kinetic and conserved energies of every step and the positions
+    and velocities after the last step."""
+    ref_shim.import_reference()
+    from yaff.sampling.verlet import VerletIntegrator
+    spec = configs.water_24000()
+    natom = len(spec['pos'])
+    rng = np.random.default_rng(24000)
+    vel0 = rng.normal(0, 1, (natom, 3)) * np.sqrt(300.0 * 3.166811563e-6 / spec['masses'])[:, None]
+    vel0 -= (spec['masses'][:, None] * vel0).sum(0) / spec['masses'].sum()
+    ff = build_reference_ff(spec)
+    vi = VerletIntegrator(ff, TIMESTEP, vel0=vel0.copy())
+    rows = {'ekin': [vi.ekin], 'epot': [vi.epot], 'econs': [vi.econs]}
+    for s in range(nstep):
+        vi.propagate()
+        for key in rows:
+            rows[key].append(getattr(vi, key))
+        print('  step %d  epot %.12e  ekin %.12e  econs %.12e' % (s + 1, vi.epot, vi.ekin, vi.econs), flush=True)
+    data = {'vel0': vel0, 'timestep': np.array(TIMESTEP), 'nstep': np.array(nstep),
+            'pos_last': vi.pos.copy(), 'vel_last': vi.vel.copy(), 'nrebuild': np.array(-1)}
+    for key, v in rows.items():
+        data[key] = np.array(v)
+    np.savez_compressed(os.path.join(HERE, 'md_water24000.npz'), **data)
+
+
 if __name__ == '__main__':
-    main()
+    if sys.argv[1:] == ['water24000']:
+        if not ref_shim.reference_available():
+            raise SystemExit('reference not available: run oracle/build_ref.sh first')
+        nve_water24000()
+    else:
+        main()
