@@ -293,12 +293,15 @@ int yg_md_thermo_get(yg_ctx *ctx, double *econs_correction, double *chain_pos, d
  * (natom x 3), charges (natom), stab_* (nstab), and writes the energy
  * (1 double), the gradient gpos (natom x 3, overwritten; may be NULL) and
  * the virial vtens (9 doubles), all device memory, on `stream`.  rvecs and
- * gvecs are host 3x3 arrays.  Its only scratch is a fixed 229 KB device array
- * inside the library, so nstab is limited to YG_NOALLOC_MAX_ROWS (larger
- * tables return YG_ERR_CAPACITY).  The first call on a device looks up that
- * array's device address; make it before capturing the stream in a graph.
- * All calls share the array: calls that overlap on the GPU race and must be
- * serialized by the caller. */
+ * gvecs are host 3x3 arrays; nhigh = -1 means natom, as in the reference.
+ * Its only scratch is a fixed 256 KB device array inside the library, so
+ * nstab is limited to YG_NOALLOC_MAX_ROWS (larger tables return
+ * YG_ERR_CAPACITY).  The scaling rows are checked on the device: a row whose
+ * indices are not 0 <= stab_b < stab_a < natom is skipped without touching
+ * memory through it, and the call then stores a NaN energy.  The first call
+ * on a device looks up that array's device address; make it before capturing
+ * the stream in a graph.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialized by the caller. */
 #define YG_NOALLOC_MAX_ROWS (1 << 20)
 int yg_ewald_corr_noalloc(const double *pos, const double *charges, int64_t natom,
                           const int64_t *stab_a, const int64_t *stab_b,

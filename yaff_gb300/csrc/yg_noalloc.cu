@@ -12,6 +12,12 @@
 // that loads the library, which keeps it until exit) and keeps the contents of
 // the last call; calls that overlap on the GPU (different streams, or other
 // host threads) race on it and must be serialized by the caller.
+//
+// The scaling table comes from the caller's memory unchecked by the host, so
+// the kernel checks every row itself: a row whose indices are not
+// 0 <= b < a < natom is skipped (no access through it) and counted in the
+// scratch array, and a call that met such a row returns a NaN energy.
+#include <atomic>
 #include <cstring>
 
 #include "yg_internal.cuh"
@@ -20,26 +26,35 @@
 #define YG_NOALLOC_MAX_BLOCKS (YG_NOALLOC_MAX_ROWS / YG_NOALLOC_BLOCK)
 #define YG_NOALLOC_MAX_DEVICES 64
 
-// 4096 blocks x 7 partial sums (energy and 6 virial components): 229 KB.
-static __device__ __align__(256) double g_noalloc_scratch[YG_NOALLOC_MAX_BLOCKS * 7];
+// 4096 blocks x 8 partial sums (energy, 6 virial components and the count of
+// rejected rows): 256 KB.
+static __device__ __align__(256) double g_noalloc_scratch[YG_NOALLOC_MAX_BLOCKS * 8];
 
 namespace {
 
-double *g_scratch_addr[YG_NOALLOC_MAX_DEVICES];
+// Device address of the scratch array per device, resolved on the first call
+// made with that device current.  A cudaDeviceReset ends the context the
+// address belongs to; a process that resets a device must not call this entry
+// point on that device again.
+std::atomic<double *> g_scratch_addr[YG_NOALLOC_MAX_DEVICES];
 
 // One thread per scaling row: the excluded-pair correction of
 // yaff/pes/ewald.c:290-335 in FP64, gradients by FP64 atomics, energy and
-// virial as fixed-order block partials in the scratch array.
+// virial as fixed-order block partials in the scratch array (slot 7 of a
+// block counts its rows with indices outside 0 <= b < a < natom).
 __global__ void k_corr_rows(const double *__restrict__ pos, const double *__restrict__ q,
                             const int64_t *__restrict__ sa, const int64_t *__restrict__ sb,
-                            const double *__restrict__ scale, int64_t n, CellGeom cell, double alpha, int64_t nlow,
-                            int64_t nhigh, double inv_diel, double *__restrict__ gpos, double *__restrict__ partial) {
-  __shared__ double red[YG_NOALLOC_BLOCK / 32][7];
+                            const double *__restrict__ scale, int64_t n, int64_t natom, CellGeom cell, double alpha,
+                            int64_t nlow, int64_t nhigh, double inv_diel, double *__restrict__ gpos,
+                            double *__restrict__ partial) {
+  __shared__ double red[YG_NOALLOC_BLOCK / 32][8];
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double vals[7] = {0, 0, 0, 0, 0, 0, 0};
+  double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (r < n) {
     const int64_t a = sa[r], b = sb[r];
-    const bool skip = (a < nlow && b < nlow) || (a >= nhigh && b >= nhigh);
+    const bool bad = !(b >= 0 && b < a && a < natom);
+    const bool skip = bad || (a < nlow && b < nlow) || (a >= nhigh && b >= nhigh);
+    vals[7] = bad ? 1.0 : 0.0;
     if (!skip) {
       double d[3] = {pos[3 * b] - pos[3 * a], pos[3 * b + 1] - pos[3 * a + 1], pos[3 * b + 2] - pos[3 * a + 2]};
       int m[3];
@@ -67,40 +82,41 @@ __global__ void k_corr_rows(const double *__restrict__ pos, const double *__rest
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < 7; k++) {
+  for (int k = 0; k < 8; k++) {
     double v = vals[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[wid][k] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 7) {
+  if (threadIdx.x < 8) {
     double s = 0.0;
     for (int w = 0; w < YG_NOALLOC_BLOCK / 32; w++) s += red[w][threadIdx.x];
-    partial[(int64_t)blockIdx.x * 7 + threadIdx.x] = s;
+    partial[(int64_t)blockIdx.x * 8 + threadIdx.x] = s;
   }
 }
 
 // One block: fixed-order sum of the block partials plus the self term
-// -alpha/sqrt(pi) sum q^2 over [nlow, nhigh) (yaff/pes/ewald.c:289-292).
+// -alpha/sqrt(pi) sum q^2 over [nlow, nhigh) (yaff/pes/ewald.c:289-292); a
+// call with a rejected scaling row stores a NaN energy.
 __global__ void k_corr_finish(const double *__restrict__ partial, int nblocks, const double *__restrict__ q,
                               int64_t nlow, int64_t nhigh, double alpha, double inv_diel, double *__restrict__ energy,
                               double *__restrict__ vtens) {
-  __shared__ double sh[8][YG_NOALLOC_BLOCK];
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  __shared__ double sh[9][YG_NOALLOC_BLOCK];
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-    for (int k = 0; k < 7; k++) acc[k] += partial[(int64_t)b * 7 + k];
-  for (int64_t i = nlow + threadIdx.x; i < nhigh; i += blockDim.x) acc[7] += q[i] * q[i];
-  for (int k = 0; k < 8; k++) sh[k][threadIdx.x] = acc[k];
+    for (int k = 0; k < 8; k++) acc[k] += partial[(int64_t)b * 8 + k];
+  for (int64_t i = nlow + threadIdx.x; i < nhigh; i += blockDim.x) acc[8] += q[i] * q[i];
+  for (int k = 0; k < 9; k++) sh[k][threadIdx.x] = acc[k];
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w)
-      for (int k = 0; k < 8; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+      for (int k = 0; k < 9; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double eself = -alpha / 1.7724538509055160273 * sh[7][0];
-    if (energy) *energy = sh[0][0] + eself * inv_diel;
+    const double eself = -alpha / 1.7724538509055160273 * sh[8][0];
+    if (energy) *energy = sh[7][0] > 0.0 ? __longlong_as_double(0x7ff8000000000000LL) : sh[0][0] + eself * inv_diel;
     if (vtens) {
       const double v[9] = {sh[1][0], sh[4][0], sh[5][0], sh[4][0], sh[2][0], sh[6][0], sh[5][0], sh[6][0], sh[3][0]};
       for (int k = 0; k < 9; k++) vtens[k] = v[k];
@@ -127,6 +143,7 @@ extern "C" int yg_ewald_corr_noalloc(const double *pos, const double *charges, i
     yg_set_error("yg_ewald_corr_noalloc: more scaling rows than the fixed scratch holds (max 1048576)");
     return YG_ERR_CAPACITY;
   }
+  if (nhigh == -1) nhigh = natom;  // the reference's "up to the last atom" (ff.py _check_nlow_nhigh)
   if (!(alpha > 0.0) || !(dielectric >= 1.0) || nlow < 0 || nhigh < nlow || nhigh > natom) {
     yg_set_error("yg_ewald_corr_noalloc: bad alpha, dielectric or nlow/nhigh");
     return YG_ERR_ARG;
@@ -139,12 +156,14 @@ extern "C" int yg_ewald_corr_noalloc(const double *pos, const double *charges, i
   }
   // first call on this device: resolve the device address of the scratch
   // array (host code cannot use the symbol itself as a device pointer)
-  if (!g_scratch_addr[dev]) {
+  double *scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
     void *p = nullptr;
     YG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = (double *)p;
+    scratch = (double *)p;
+    // threads racing here all resolve the same address
+    g_scratch_addr[dev].store(scratch, std::memory_order_release);
   }
-  double *scratch = g_scratch_addr[dev];
   cudaStream_t st = (cudaStream_t)stream;
   CellGeom cell;
   memcpy(cell.rv, rvecs, 9 * sizeof(double));
@@ -155,8 +174,8 @@ extern "C" int yg_ewald_corr_noalloc(const double *pos, const double *charges, i
   const int nb = nstab > 0 ? (int)((nstab + YG_NOALLOC_BLOCK - 1) / YG_NOALLOC_BLOCK) : 0;
   const double inv_diel = 1.0 / dielectric;
   if (nb > 0) {
-    k_corr_rows<<<nb, YG_NOALLOC_BLOCK, 0, st>>>(pos, charges, stab_a, stab_b, stab_scale, nstab, cell, alpha, nlow,
-                                                  nhigh, inv_diel, gpos, scratch);
+    k_corr_rows<<<nb, YG_NOALLOC_BLOCK, 0, st>>>(pos, charges, stab_a, stab_b, stab_scale, nstab, natom, cell, alpha,
+                                                  nlow, nhigh, inv_diel, gpos, scratch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return yg_cuda_fail(e, "k_corr_rows");
   }
