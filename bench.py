@@ -299,6 +299,10 @@ def run_gb300(args, world, rank, local):
         fp64 = 1.0 / float(np.mean(tt))
         dev.set_precision(args.precision)
 
+    # precision sweep: every form's speed on this workload and its error
+    # against the reference's own FP64 evaluation of the same positions
+    sweep = precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64, 1.0 / t_step)
+
     pk, pk_src = peaks()
     nk = ff_nk(ff)
     fp32_peak, fp32_probe = fp32_fma_peak(torch)
@@ -368,12 +372,13 @@ def run_gb300(args, world, rank, local):
         'vs_baseline': None, 'dtype': {'mixed': 'fp32-terms/fp64-accum', 'fp64': 'f64',
                                         'mixed_kahan': 'fp32-kahan'}[args.precision],
         'data': 'synthetic (seeded random sequential insertion)',
-        'config': {'workload': '50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
-                               'rebuild every step', 'natom': natom, 'precision': args.precision,
-                   'nneigh': int(ff.nlist.nneigh), 'nk': int(nk), 'l2': 'flushed (256 MB write) between steps',
-                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'config': workload_config(natom),
+        'details': {'precision': args.precision, 'nneigh': int(ff.nlist.nneigh), 'nk': int(nk),
+                    'l2': 'flushed (256 MB write) between steps',
+                    'parallelism': 'independent replicas' if world > 1 else 'single GPU'},
         'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99))},
         'fp64_evals_per_s': fp64,
+        'precision_sweep': sweep,
         'skin_path_evals_per_s': 1.0 / float(np.mean(skin_times)),
         'rebuilds_in_timed_steps': int(nrebuild_timed - nrebuild0),
         'e2e': {'value': e2e, 'unit': 'evals/s', 'h2d_bytes_per_step': natom * 24,
@@ -384,6 +389,108 @@ def run_gb300(args, world, rank, local):
         'peaks_source': pk_src,
     }
     return out, spec
+
+
+def workload_config(natom):
+    """The `config` of both arms' JSON lines (the same workload)."""
+    return {'workload': '%s-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, rebuild every step'
+                        % format(natom, ','), 'natom': natom}
+
+
+def precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64_rate, main_rate):
+    """Each precision form against the reference: the error of one
+    ForceField.compute(gpos, vtens) at the workload's own positions against
+    tests/golden/big_triclinic50000.npz (the reference yaff ForceField.compute
+    on the same positions, FP64 on the CPU): energy relative to the total,
+    every part's energy relative to the largest part, gradient and virial
+    relative RMS; the pair set (SHA-256 of the sorted (a, b, r0, r1, r2)
+    keys) for the benchmarked form; and each form's evals/s on the timed
+    workload (rebuild every step, L2 flushed)."""
+    import hashlib
+    import torch
+    path = os.path.join(REPO, 'tests', 'golden', 'big_triclinic50000.npz')
+    if not os.path.exists(path) or len(spec['pos']) != 50000:
+        return None
+    ref = np.load(path)
+    if not np.array_equal(ref['spec_pos'], spec['pos']):
+        return {'error': 'fixture positions differ from the workload'}
+    natom = len(spec['pos'])
+    e_ref = float(ref['step0_energy'])
+    g_ref = ref['step0_gpos']
+    v_ref = ref['step0_vtens']
+    names = [str(x) for x in ref['step0_parts']]
+    pe = ref['step0_part_energy']
+    pv = ref['step0_part_vtens']
+
+    def rel_rms(a, b):
+        return float(np.sqrt(((a - b) ** 2).mean() / (b ** 2).mean()))
+
+    out = {'reference': 'yaff ForceField.compute, FP64, same positions (tests/golden/big_triclinic50000.npz)',
+           'reference_energy': e_ref, 'forms': {}}
+    for prec in ('fp64', 'mixed', 'mixed_kahan'):
+        dev.set_precision(prec)
+        ff.update_pos(spec['pos'])
+        ff.nlist.rebuild_next = True
+        g = np.zeros((natom, 3))
+        v = np.zeros((3, 3))
+        e = ff.compute(g, v)
+        row = {'energy_rel_err': abs(e - e_ref) / abs(e_ref), 'gpos_rel_rms': rel_rms(g, g_ref),
+               'vtens_rel_rms': rel_rms(v, v_ref), 'parts': {}}
+        scale = float(np.abs(pe).max())
+        for k, nm in enumerate(names):
+            part = getattr(ff, 'part_' + nm)
+            prow = {'energy_err_rel_largest_part': abs(part.energy - pe[k]) / scale}
+            if abs(pv[k]).max() > 0:
+                prow['vtens_rel_rms'] = rel_rms(part.vtens, pv[k])
+            gp = ref['step0_part_gpos32'][k].astype(np.float64)
+            if abs(gp).max() > 0:
+                prow['gpos_rel_rms_vs_fp32_copy'] = rel_rms(part.gpos, gp)
+            row['parts'][nm] = prow
+        row['within_tolerance'] = bool(row['energy_rel_err'] <= (1e-10 if prec == 'fp64' else 1e-6) and
+                                       row['gpos_rel_rms'] <= (1e-9 if prec == 'fp64' else 1e-5) and
+                                       row['vtens_rel_rms'] <= (1e-9 if prec == 'fp64' else 1e-5))
+        if prec == args.precision:
+            nb = ff.nlist.neighs
+            a = nb['a'].astype(np.int64)
+            b = nb['b'].astype(np.int64)
+            r = np.stack([nb['r0'], nb['r1'], nb['r2']], 1).astype(np.int64)
+            rm = int(np.abs(r).max())
+            key = a * natom + b
+            for kk in range(3):
+                key = key * (2 * rm + 1) + (r[:, kk] + rm)
+            order = np.argsort(key, kind='stable')
+            keys = np.concatenate([a[order, None], b[order, None], r[order]], 1)
+            sha = hashlib.sha256(np.ascontiguousarray(keys, dtype='<i8').tobytes()).hexdigest()
+            row['pair_set_equal'] = bool(sha == str(ref['step0_pairs_sha256']) and
+                                         len(nb) == int(ref['step0_nneigh']))
+            row['nneigh'] = int(len(nb))
+        if prec == 'fp64':
+            row['evals_per_s'] = fp64_rate
+        elif prec == args.precision:
+            row['evals_per_s'] = main_rate
+        else:
+            for s in range(2):
+                mask = device_step(s)
+                dev.get_total(mask, None, None)
+            torch.cuda.synchronize()
+            tt = []
+            for s in range(5):
+                flush.fill_(float(s))
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                mask = device_step(s)
+                dev.get_total(mask, None, None)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tt.append(e0.elapsed_time(e1) * 1e-3)
+            row['evals_per_s'] = 1.0 / float(np.mean(tt))
+        out['forms'][prec] = row
+    dev.set_precision(args.precision)
+    f = out['forms']
+    if f['fp64'].get('evals_per_s'):
+        out['mixed_over_fp64'] = f['mixed']['evals_per_s'] / f['fp64']['evals_per_s']
+    return out
 
 
 def ff_nk(ff):
@@ -472,6 +579,38 @@ def cpu_sample(natom, seconds_budget=20.0):
                                                         'ewald_reci': t_ew_full}}
 
 
+def cpu_whole_eval(natom, threads=None, max_evals=2, budget_s=60.0):
+    """Whole force evaluations of the workload with the oracle (the
+    reference's algorithm in FP64, yaff_oracle.c) spread over the host cores
+    (yaff_oracle_mt.c: the list build, the pair terms and the Ewald
+    reciprocal sum on `threads` threads): one untimed evaluation, then up to
+    max_evals timed ones (within budget_s), each a full ForceField.compute
+    with gradient and virial and a neighbour-list rebuild.  Also returns the
+    energy, which equals the reference's to rounding."""
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import oracle
+    from yaff_gb300 import configs
+    spec = configs.triclinic_50000() if natom == 50000 else configs.triclinic_mm3_ei(natom=natom)
+    threads = threads or os.cpu_count() or 1
+    orc = oracle.OracleForceField(spec, threads=threads)
+    n = len(spec['pos'])
+    g = np.zeros((n, 3))
+    v = np.zeros((3, 3))
+    t0 = time.perf_counter()
+    e = orc.compute(g, v)
+    t_warm = time.perf_counter() - t0
+    times = []
+    while len(times) < max_evals and sum(times) + t_warm < budget_s:
+        orc.rebuild_next = True
+        g[:] = 0.0
+        v[:] = 0.0
+        t0 = time.perf_counter()
+        e = orc.compute(g, v)
+        times.append(time.perf_counter() - t0)
+    return {'seconds_per_eval': float(np.mean(times)), 'evals': len(times), 'cores': threads, 'energy': e,
+            'nneigh': int(orc.nneigh)}
+
+
 def _cpu_serving_request(idx):
     """CPU time of one serving request (50 Verlet steps of 0.5 fs) with the
     oracle as the force field, one thread."""
@@ -537,32 +676,54 @@ def cpu_replicas():
                    'sample': '%d trials on the 2,000-atom framework with the oracle' % (2 * cores)}}
 
 
-def run_reference(args, world, rank):
+def run_reference(args, world, rank, budget_s=150.0):
+    """The reference's algorithm (the oracle port, FP64) on the host cores:
+    each step is one whole ForceField.compute(gpos, vtens) of the workload
+    with a neighbour-list rebuild, spread over all cores (yaff_oracle_mt.c).
+    One untimed warm-up evaluation; then up to --steps timed evaluations,
+    stopping early when budget_s is used up -- `steps` is the number that
+    actually ran."""
     if rank != 0:
         return None
-    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import oracle
+    from yaff_gb300 import configs
     cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    ctx = mp.get_context('spawn')
-    res = []
-    for s in range(args.warmup + args.steps):
-        with ctx.Pool(cores) as pool:
-            outs = pool.map(cpu_sample, [args.natom] * cores)
-        if s >= args.warmup:
-            res.append(sum(o['value'] for o in outs))
-    val = float(np.mean(res))
-    one = outs[0]
-    return {'metric': 'force evals/s', 'value': val, 'unit': 'evals/s', 'n_gpus': world, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': 1e3 / val, 'higher_is_better': True, 'scaling': 'weak',
-            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded random sequential insertion)',
-            'impl': 'reference',
-            'config': {'workload': '50,000-atom triclinic (82 A, 75 deg) MM3+EI+Ewald, rcut 12 A, skin 1 A, '
-                                   'rebuild every step', 'natom': args.natom, 'parallelism': '%d independent '
-                                   'single-thread replicas' % cores},
-            'cpu_baseline': {'value': val, 'unit': 'evals/s', 'cores': cores, 'kind': 'port',
-                             'sample': one['sample'] + '; %d replica processes' % cores},
+    t_start = time.perf_counter()
+    spec = configs.triclinic_50000() if args.natom == 50000 else configs.triclinic_mm3_ei(natom=args.natom)
+    n = len(spec['pos'])
+    orc = oracle.OracleForceField(spec, threads=cores)
+    rng = np.random.default_rng(7)
+    pos0 = spec['pos'].copy()
+    g = np.zeros((n, 3))
+    v = np.zeros((3, 3))
+    orc.compute(g, v)
+    times = []
+    energies = []
+    for s in range(args.steps):
+        if times and sum(times) + np.mean(times) > budget_s:
+            break
+        orc.update_pos(pos0 + rng.uniform(-0.05, 0.05, pos0.shape))
+        orc.rebuild_next = True
+        g[:] = 0.0
+        v[:] = 0.0
+        t0 = time.perf_counter()
+        energies.append(orc.compute(g, v))
+        times.append(time.perf_counter() - t0)
+    val = len(times) / float(sum(times))
+    sample = ('whole force evaluations (neighbour-list rebuild, MM3, EI, Ewald reciprocal / correction / '
+              'neutralizing, gradient and virial) of the oracle (the reference algorithm restated in C, FP64) on '
+              '%d host threads; %d timed evaluations of %.2f s each after one warm-up' %
+              (cores, len(times), float(np.mean(times))))
+    return {'metric': 'force evals/s', 'value': val, 'unit': 'evals/s', 'n_gpus': world, 'steps': len(times),
+            'steps_requested': args.steps, 'warmup': 1, 'ms_per_step': 1e3 / val, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic (seeded random sequential insertion)', 'impl': 'reference',
+            'config': workload_config(args.natom),
+            'details': {'precision': 'fp64', 'parallelism': 'one evaluation on %d host threads' % cores},
+            'cpu_baseline': {'value': val, 'unit': 'evals/s', 'cores': cores, 'kind': 'port', 'sample': sample},
             'e2e': {'value': val, 'unit': 'evals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
-            'wall_s': time.perf_counter() - t0}
+            'nneigh': int(orc.nneigh), 'wall_s': time.perf_counter() - t_start}
 
 
 def run_serving(args):
@@ -600,9 +761,12 @@ def run_serving(args):
 def run_nve(args):
     """NVE of the 8,000-molecule flexible water box (24,000 atoms, LJ + EI +
     Ewald + bonds + bends, rcut 10 A, skin 1 A) with the device-resident
-    velocity Verlet: 0.5 fs steps from seeded 300 K velocities, mixed
-    precision, each step replayed from a CUDA graph.  Reports steps/s, ns/day,
-    the conserved-energy drift and fluctuation ratio, and the rebuilds."""
+    velocity Verlet: 0.5 fs steps, each replayed from a CUDA graph, in the
+    mixed and the plain FP64 form.  Both start from the initial velocities of
+    tests/golden/md_water24000.npz (the reference's own VerletIntegrator on
+    this system) and are compared with the reference over its first steps;
+    then --nve-steps timed steps give steps/s, ns/day, the conserved-energy
+    drift and fluctuation ratio, and the rebuild count."""
     import torch
     import yaff_gb300
     from yaff_gb300 import configs
@@ -610,27 +774,58 @@ def run_nve(args):
     from yaff_gb300.verlet import DeviceVerlet, ConsErrTracker, drift_per_ps
     spec = configs.water_24000()
     natom = len(spec['pos'])
-    ff = yaff_gb300.build_forcefield(spec, precision='mixed')
     dt = 0.5 * femtosecond
     n = args.nve_steps
-    dv = DeviceVerlet(ff, dt, temp0=300.0, rng=np.random.default_rng(1), max_steps=n + 20, use_graph=True)
-    dv.run(20)  # warm-up: capture and first rebuilds
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    dv.run(n)
-    _, _, log = dv.fetch(pos=False, vel=False)
-    wall = time.perf_counter() - t0
-    econs = log[:, 0] + log[:, 1]
-    tr = ConsErrTracker()
-    for ep, ek in log:
-        tr.update(ek, ep + ek)
-    times = dt * np.arange(len(econs))
-    sps = n / wall
-    return {'workload': '8,000 flexible waters (24,000 atoms), LJ+EI+Ewald+bonds+bends, rcut 10 A, skin 1 A, '
-                        '0.5 fs velocity Verlet, seeded 300 K, mixed precision, device-resident, graph replay',
-            'steps': n, 'steps_per_s': sps, 'ns_per_day': sps * 0.5 * 86400 / 1e6,
-            'drift_ha_per_atom_ps': float(drift_per_ps(times, econs, natom)),
-            'cons_err_ratio': float(tr.get()), 'rebuilds': int(dv.nrebuild)}
+    path = os.path.join(REPO, 'tests', 'golden', 'md_water24000.npz')
+    ref = dict(np.load(path)) if os.path.exists(path) else None
+    out = {'workload': '8,000 flexible waters (24,000 atoms), LJ+EI+Ewald+bonds+bends, rcut 10 A, skin 1 A, '
+                       '0.5 fs velocity Verlet, 300 K initial velocities, device-resident, graph replay',
+           'steps': n, 'forms': {}}
+    for prec in ('mixed', 'fp64'):
+        ff = yaff_gb300.build_forcefield(spec, precision=prec)
+        vel0 = ref['vel0'] if ref is not None else None
+        dv = DeviceVerlet(ff, dt, vel0=vel0, temp0=300.0, rng=np.random.default_rng(1), max_steps=n + 40,
+                          use_graph=True)
+        row = {}
+        nref = 0
+        if ref is not None:
+            nref = int(ref['nstep'])
+            dv.run(nref)
+            pos, vel, log = dv.fetch()
+            ep, ek = log[:, 0], log[:, 1]
+            escale = float(np.abs(ref['epot']).max())
+            row['vs_reference_first_steps'] = {
+                'steps': nref,
+                'epot_max_abs_err_rel': float(np.abs(ep - ref['epot']).max() / escale),
+                'ekin_max_rel_err': float(np.abs(ek - ref['ekin']).max() / np.abs(ref['ekin']).max()),
+                'econs_max_abs_err_rel': float(np.abs(ep + ek - ref['econs']).max() / escale),
+                'pos_max_abs_err_bohr': float(np.abs(pos - ref['pos_last']).max()),
+                'vel_rel_rms': float(np.sqrt(((vel - ref['vel_last']) ** 2).mean() / (ref['vel_last'] ** 2).mean())),
+                'reference': 'yaff VerletIntegrator + ForceField, FP64 (tests/golden/md_water24000.npz)'}
+        dv.run(40 - nref)  # warm-up: capture and first rebuilds
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dv.run(n)
+        _, _, log = dv.fetch(pos=False, vel=False)
+        wall = time.perf_counter() - t0
+        log = log[40:]
+        econs = log[:, 0] + log[:, 1]
+        tr = ConsErrTracker()
+        for ep, ek in log:
+            tr.update(ek, ep + ek)
+        times = dt * np.arange(len(econs))
+        sps = n / wall
+        row.update({'steps_per_s': sps, 'ns_per_day': sps * 0.5 * 86400 / 1e6,
+                    'drift_ha_per_atom_ps': float(drift_per_ps(times, econs, natom)),
+                    'cons_err_ratio': float(tr.get()), 'rebuilds': int(dv.nrebuild)})
+        out['forms'][prec] = row
+        del dv, ff
+    f = out['forms']
+    out['mixed_over_fp64_steps_per_s'] = f['mixed']['steps_per_s'] / f['fp64']['steps_per_s']
+    # headline fields of the mixed form (as before)
+    for k in ('steps_per_s', 'ns_per_day', 'drift_ha_per_atom_ps', 'cons_err_ratio', 'rebuilds'):
+        out[k] = f['mixed'][k]
+    return out
 
 
 def run_mc(args):
@@ -705,7 +900,18 @@ def main():
             if 'mc_trials' in out:
                 out['mc_trials']['cpu_replicas'] = dict(rep['mc'], cores=rep['cores'], kind=rep['kind'])
         if not args.no_cpu_baseline:
-            out['cpu_baseline'] = cpu_sample(args.natom)
+            whole = cpu_whole_eval(args.natom)
+            one = cpu_sample(args.natom)
+            out['cpu_baseline'] = {
+                'value': 1.0 / whole['seconds_per_eval'], 'unit': 'evals/s', 'cores': whole['cores'],
+                'kind': 'port',
+                'sample': '%d whole force evaluation(s) of the workload (rebuild, MM3, EI, Ewald reciprocal / '
+                          'correction / neutralizing, gradient and virial) by the oracle on %d host threads, after '
+                          'one untimed evaluation' % (whole['evals'], whole['cores']),
+                'seconds_per_eval': whole['seconds_per_eval'], 'energy': whole['energy'],
+                'single_thread_estimate': {'seconds_per_eval': one['seconds_per_eval'],
+                                           'breakdown_s': one['breakdown_s'], 'sample': one['sample']},
+                'thread_speedup': one['seconds_per_eval'] / whole['seconds_per_eval']}
         print(json.dumps(out))
 
 
