@@ -40,6 +40,7 @@ def parse():
     ap.add_argument('--natom', type=int, default=50000)
     ap.add_argument('--fp64-steps', type=int, default=3)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-sweep', action='store_true', help='skip the precision sweep against the reference fixture')
     ap.add_argument('--serving-requests', type=int, default=4096,
                     help='requests of the serving workload run after the main measurement (0: skip)')
     ap.add_argument('--serving-rate', type=float, default=200.0, help='Poisson arrival rate, requests/s')
@@ -114,6 +115,23 @@ def peaks():
     return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}, 'fallback'
 
 
+_probe = None
+
+
+def probe_lib():
+    """The bench-only throughput probes (yaff_gb300/csrc/bench/yg_probe.cu,
+    built by yaff_gb300.build.build_probe; not part of libyaffgb.so):
+    double yg_probe_peak(int kind, cudaStream_t)."""
+    global _probe
+    if _probe is None:
+        import ctypes
+        from yaff_gb300 import build
+        _probe = ctypes.CDLL(build.build_probe())
+        _probe.yg_probe_peak.restype = ctypes.c_double
+        _probe.yg_probe_peak.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    return _probe
+
+
 def fp32_fma_peak(torch):
     """FP32 CUDA-core peak (TFLOP/s, FMA = 2 flops) measured with FMA-chain
     kernels of the library, scalar, packed f32x2 and the two interleaved:
@@ -121,8 +139,7 @@ def fp32_fma_peak(torch):
     holds only HBM and bf16 tensor figures, and the pair and Ewald kernels
     use neither."""
     import ctypes
-    from yaff_gb300 import _lib
-    lib = _lib.load()
+    lib = probe_lib()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     both = {'scalar': float(lib.yg_probe_peak(0, st)), 'f32x2': float(lib.yg_probe_peak(2, st)),
             'f32x2+scalar': float(lib.yg_probe_peak(3, st))}
@@ -135,8 +152,7 @@ def warp_mma_peak(torch):
     TFLOP/s, measured with an MMA-chain kernel of the library: the ceiling of
     the instruction the tensor-core Ewald kernels use."""
     import ctypes
-    from yaff_gb300 import _lib
-    lib = _lib.load()
+    lib = probe_lib()
     v = float(lib.yg_probe_peak(5, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return v if v > 0 else None
 
@@ -301,7 +317,8 @@ def run_gb300(args, world, rank, local):
 
     # precision sweep: every form's speed on this workload and its error
     # against the reference's own FP64 evaluation of the same positions
-    sweep = precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64, 1.0 / t_step)
+    sweep = None if args.no_sweep else precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64,
+                                                         1.0 / t_step)
 
     pk, pk_src = peaks()
     nk = ff_nk(ff)

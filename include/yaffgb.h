@@ -143,16 +143,40 @@ int yg_clear_pair_pots(yg_ctx *ctx);
 int yg_nlist_build(yg_ctx *ctx, double rcut_total, const int64_t *rmax,
                    int64_t nlow, int64_t nhigh, int64_t *nneigh);
 
+/* Per-atom neighbour-slot capacity of the next builds, rounded up to a
+ * multiple of 32 (no reference counterpart; the reference grows its row
+ * buffer the same way, yaff/pes/nlist.py:170-182).  The current list is
+ * dropped: host computes need a new yg_nlist_build, and a device-resident MD
+ * run rebuilds at its next step.  A build that needs more slots than this
+ * regrows as usual (the host build reruns; the MD rolls its batch back to
+ * the snapshot and reruns it). */
+int yg_nlist_set_capacity(yg_ctx *ctx, int64_t slots);
+
 /* Statistics of the last host-driven build (no reference counterpart):
  * candidates decided by the exact FP64 test (inside the FP32 guard band)
  * and the longest per-atom row of the device list (both directions). */
 int yg_nlist_stats(yg_ctx *ctx, int64_t *nexact, int64_t *maxrow);
 
 /* Layout of the reciprocal sum set up by yg_ewald_setup (no reference
- * counterpart): whether the mixed forms run it on the tensor cores (warp
- * MMA, needs G2 + 1 <= 32 and G0 + G1 + 2 <= 160) and the number of k
- * vectors in the half sphere. */
+ * counterpart): how the mixed forms run it -- 0 on the CUDA cores, 1 both
+ * contractions as warp-level MMAs (needs G2 + 1 <= 32 and G0 + G1 + 2 <=
+ * 160), 2 the force pass on tcgen05 with TMEM accumulators and the structure
+ * factors as warp-level MMAs (also needs G0 + G1 + 2 <= 63) -- and the number
+ * of k vectors in the half sphere. */
 int yg_ewald_info(yg_ctx *ctx, int *tensor_path, int64_t *nk);
+
+/* Failure-path self-check (no reference counterpart): runs the bounded
+ * mbarrier wait used by the kernels that stage data with bulk copies on a
+ * barrier nothing arrives at, giving up after `polls` polls (1 .. 2^24; the
+ * kernels use 2^24, about a second).  *timed_out is set to 1 when the wait
+ * gave up and recorded the timeout status, as it must; the context stays
+ * usable. */
+int yg_check_wait_timeout(yg_ctx *ctx, int64_t polls, int *timed_out);
+
+/* Selects the kernel of the mixed-precision reciprocal force pass (no
+ * reference counterpart): 0 automatic (tcgen05 where the layout allows), 1
+ * the warp-level MMA form.  Both compute the same sums. */
+int yg_ewald_force_path(yg_ctx *ctx, int path);
 
 /* The reciprocal sum runs on an auxiliary stream of the context, forked at
  * yg_ewald_reci, so that it overlaps the neighbour build and the pair terms;
@@ -379,13 +403,6 @@ int yg_mc_trials(yg_mc *mc, int64_t ntrial, const int32_t *chain, const int32_t 
  * the freed slot. */
 int yg_mc_apply(yg_mc *mc, int64_t napply, const int32_t *trial_index);
 int64_t yg_mc_launch_count(yg_mc *mc);
-
-/* Measurement utility (no reference counterpart): FMA-chain throughput of
- * the CUDA-core pipes in TFLOP/s (FMA = 2 flops), the roofline denominator of
- * the pair and Ewald kernels.  kind 0: scalar FP32 FMAs; 1: FP64 FMAs; 2:
- * packed FP32 pairs (f32x2, two FMAs per instruction); 3: packed and scalar
- * FP32 FMAs interleaved one to one.  Negative on error. */
-double yg_probe_peak(int kind, void *stream);
 
 #ifdef __cplusplus
 }

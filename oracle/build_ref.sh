@@ -31,4 +31,6 @@ if [ ! -f "$OUT/pes/ext$SUFFIX" ] || [ "$REF/yaff/pes/ext.pyx" -nt "$OUT/pes/ext
     "$P/grid.c" "$P/iclist.c" "$P/nlist.c" "$P/pair_pot.c" "$P/slater.c" \
     "$P/tailcorr.c" "$P/truncation.c" "$P/vlist.c" -lm -o "$OUT/pes/ext$SUFFIX"
 fi
+# the checkout this extension was built from, for oracle/ref_shim.py
+printf '%s\n' "$REF" > "$OUT/REFERENCE_ROOT"
 echo "build_ref: $OUT/pes/ext$SUFFIX"

@@ -17,8 +17,23 @@ import sys
 import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get('YAFF_REFERENCE', '/root/reference')
 REF_EXT_DIR = os.path.join(HERE, '_ref', 'pes')
+
+
+def _reference_root():
+    """The reference checkout: $YAFF_REFERENCE, else the one build_ref.sh
+    compiled the extension from (recorded in _ref/REFERENCE_ROOT)."""
+    root = os.environ.get('YAFF_REFERENCE')
+    if root:
+        return root
+    rec = os.path.join(HERE, '_ref', 'REFERENCE_ROOT')
+    if os.path.isfile(rec):
+        with open(rec) as fh:
+            return fh.read().strip()
+    return ''
+
+
+REF_ROOT = _reference_root()
 
 
 def reference_available():

@@ -1,9 +1,11 @@
 """Generate the golden fixtures in tests/golden/ by running the reference.
 
-Run in a container that holds the reference checkout (default /root/reference,
-or $YAFF_REFERENCE) after ``sh oracle/build_ref.sh``:
+Run in a container that holds the reference checkout, after
+``sh oracle/build_ref.sh`` has built its extension (the checkout is
+$YAFF_REFERENCE, else the one the recipe built from):
 
     python tests/golden/make_golden.py [case ...]
+    python tests/golden/make_golden.py big_triclinic50000 big_water24000
 
 For every case the script builds the reference's own ForceField (through the
 import shim in oracle/ref_shim.py), calls ForceField.compute(gpos, vtens) one
@@ -261,6 +263,15 @@ def main():
     for var in ('a', 'b', 'c', 'lj', 'mm3'):
         tc = configs.tail_corrections(var)
         run_case(tc['name'], tc)
+
+    # Gaussian charges (radii > 0) in both branches of the reference's EI
+    # term (yaff/pes/pair_pot.c:724-748): screened by Ewald, and alone
+    for name, ewald in (('gauss216', True), ('gauss216bare', False)):
+        gs = configs.lattice_lj_ei(nside=6, spacing=2.5, rcut=6.0, name=name)
+        gs['pair'][1]['radii'] = np.where(np.arange(216) % 2 == 0, 0.9, 1.2) * angstrom
+        if not ewald:
+            gs['ewald'] = None
+        run_case(name, gs, displacements=[rng.uniform(-0.05, 0.05, (216, 3)) * angstrom])
 
     # benchmark-sized systems (minutes of reference CPU time each): only when
     # named on the command line, e.g. big_triclinic50000 big_water24000

@@ -5,6 +5,7 @@ Run in a container that holds the reference checkout ($YAFF_REFERENCE) after
 
     python tests/golden/make_md_golden.py            # thermostats, barostats
     python tests/golden/make_md_golden.py water24000 # md_water24000.npz only
+    python tests/golden/make_md_golden.py npt        # md_npt.npz only (Langevin, MTK barostats)
 
 For each thermostat of the reference (Berendsen, Langevin, CSVR, Nose-Hoover
 chain) the script runs the reference's own VerletIntegrator with that hook on
@@ -114,6 +115,61 @@ def barostat_runs(spec, vel0):
     np.savez_compressed(os.path.join(HERE, 'md_barostats.npz'), **data)
 
 
+def npt_runs(spec, vel0):
+    """The reference's Langevin and MTK barostats with their thermostats
+    (combined by the reference's VerletIntegrator into a TBCombination) at
+    1 GPa -> md_npt.npz: positions, cells, energies and the conserved energy
+    per step.  The random draws (barostat and chain velocities, Langevin
+    forces) come from NumPy's global generator, seeded per run (stored)."""
+    from yaff.sampling.verlet import VerletIntegrator
+    from yaff.sampling.nvt import BerendsenThermostat, LangevinThermostat, NHCThermostat
+    from yaff.sampling.npt import LangevinBarostat, MTKBarostat
+    from yaff_gb300.units import pascal
+    press = 1e9 * pascal
+    btc = 200 * femtosecond
+    chain_vel0 = np.array([1e-3, -2e-3, 5e-4]) / femtosecond * 1e-2
+    data = {'pos0': spec['pos'], 'vel0': vel0, 'timestep': np.array(TIMESTEP), 'temp': np.array(TEMP),
+            'timecon': np.array(TIMECON), 'press': np.array(press), 'baro_timecon': np.array(btc),
+            'nstep': np.array(NSTEP), 'chain_vel0': chain_vel0}
+    runs = {
+        'mtk_nhc_aniso': lambda ff: [NHCThermostat(TEMP, timecon=TIMECON, chainlength=3, chain_vel0=chain_vel0.copy()),
+                                     MTKBarostat(ff, TEMP, press, timecon=btc, anisotropic=True)],
+        'mtk_nhc_iso': lambda ff: [NHCThermostat(TEMP, timecon=TIMECON, chainlength=3, chain_vel0=chain_vel0.copy()),
+                                   MTKBarostat(ff, TEMP, press, timecon=btc, anisotropic=False)],
+        'mtk_cellchain': lambda ff: [NHCThermostat(TEMP, timecon=TIMECON, chainlength=3, chain_vel0=chain_vel0.copy()),
+                                     MTKBarostat(ff, TEMP, press, timecon=btc, anisotropic=True,
+                                                 baro_thermo=NHCThermostat(TEMP, timecon=TIMECON, chainlength=3))],
+        'langevin_berendsen_aniso': lambda ff: [BerendsenThermostat(TEMP, timecon=TIMECON),
+                                                LangevinBarostat(ff, TEMP, press, timecon=btc, anisotropic=True)],
+        'langevin_langevin_iso': lambda ff: [LangevinThermostat(TEMP, timecon=TIMECON),
+                                             LangevinBarostat(ff, TEMP, press, timecon=btc, anisotropic=False)],
+    }
+    for k, (name, make) in enumerate(runs.items()):
+        ff = build_reference_ff(spec)
+        seed = 2000 + k
+        np.random.seed(seed)
+        hooks = make(ff)
+        vi = VerletIntegrator(ff, TIMESTEP, hooks=hooks, vel0=vel0.copy())
+        rows = {'pos': [vi.pos.copy()], 'vel': [vi.vel.copy()], 'rvecs': [ff.system.cell.rvecs.copy()],
+                'epot': [vi.epot], 'ekin': [vi.ekin], 'econs': [vi.econs]}
+        for _ in range(NSTEP):
+            vi.propagate()
+            rows['pos'].append(vi.pos.copy())
+            rows['vel'].append(vi.vel.copy())
+            rows['rvecs'].append(ff.system.cell.rvecs.copy())
+            rows['epot'].append(vi.epot)
+            rows['ekin'].append(vi.ekin)
+            rows['econs'].append(vi.econs)
+        for key, v in rows.items():
+            data['%s_%s' % (name, key)] = np.array(v)
+        data['%s_seed' % name] = np.array(seed)
+        data['%s_ndof' % name] = np.array(vi.ndof)
+        print('%-26s volume %.6f -> %.6f  econs %+.3e' % (name, np.linalg.det(rows['rvecs'][0]),
+                                                          np.linalg.det(rows['rvecs'][-1]),
+                                                          rows['econs'][-1] - rows['econs'][0]))
+    np.savez_compressed(os.path.join(HERE, 'md_npt.npz'), **data)
+
+
 def nve_water24000(nstep=10):
     """NVE of the 8,000-molecule (24,000-atom) flexible water workload with the
     reference's own VerletIntegrator and force field: nstep steps of 0.5 fs
@@ -147,5 +203,13 @@ if __name__ == '__main__':
         if not ref_shim.reference_available():
             raise SystemExit('reference not available: run oracle/build_ref.sh first')
         nve_water24000()
+    elif sys.argv[1:] == ['npt']:
+        if not ref_shim.reference_available():
+            raise SystemExit('reference not available: run oracle/build_ref.sh first')
+        ref_shim.import_reference()
+        spec = configs.flexible_water(nside=4, box=12.42, rcut=5.0, skin=0.5, name='water64')
+        rng = np.random.default_rng(99)
+        vel0 = rng.normal(0, 1, (len(spec['pos']), 3)) * np.sqrt(1.2 * 300.0 * 3.166811563e-6 / spec['masses'])[:, None]
+        npt_runs(spec, vel0)
     else:
         main()

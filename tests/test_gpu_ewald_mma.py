@@ -1,11 +1,17 @@
-"""GPU: the mixed-precision reciprocal sum on the tensor cores (warp MMA with
-FP16 hi/lo split operands) against the FP64 form of the same workload.
+"""GPU: the mixed-precision reciprocal sum on the tensor cores against the
+FP64 form of the same workload.
 
-Tolerances are those of the mixed form in the parity suite: energy 1e-6
-relative, gradient 1e-5 relative RMS, virial 1e-6 relative to its largest
-entry.  The 3,000-atom triclinic box has enough atoms for several S-pass
-chunks and a force pass split into column ranges; the nlow/nhigh case runs
-the three-group form (three structure factors, three weight sets)."""
+Two tensor-core forms of the force pass compute the same sums: the tcgen05
+kernel (MMAs issued by one thread into tensor-memory accumulators, operands
+in shared memory; yg_ewald_info reports 2) and the warp-level MMA kernel
+(yg_ewald_force_path(ctx, 1); reports 1).  Tolerances are those of the
+mixed form in the parity suite: energy 1e-6 relative, gradient 1e-5
+relative RMS, virial 1e-6 relative to its largest entry; the two force-pass
+kernels agree with each other within 2e-6 relative RMS (both FP16-split
+products with FP32 accumulation, summed in different orders).  The
+3,000-atom triclinic box has enough atoms for several 128-atom blocks and
+the force pass split into tile ranges; the nlow/nhigh case runs the
+three-group form (three structure factors, three weight sets)."""
 import ctypes
 
 import numpy as np
@@ -14,45 +20,61 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _reci(spec, precision, nlow=None, nhigh=None):
+def _reci(spec, precision, nlow=None, nhigh=None, force_path=0):
     import yaff_gb300 as ygb
     if nlow is not None:
         spec = dict(spec)
         spec['nlow'], spec['nhigh'] = nlow, nhigh
     ff = ygb.build_forcefield(spec, precision=precision)
+    dev = ygb.device_of(ff.system)
+    assert dev.lib.yg_ewald_force_path(dev.ctx, force_path) == 0
     n = len(spec['pos'])
     gpos = np.zeros((n, 3))
     vt = np.zeros((3, 3))
     ff.compute(gpos, vt)
     part = [p for p in ff.parts if p.name == 'ewald_reci'][0]
-    dev = ygb.device_of(ff.system)
     tensor, nk = ctypes.c_int(), ctypes.c_int64()
     dev.lib.yg_ewald_info(dev.ctx, ctypes.byref(tensor), ctypes.byref(nk))
     return part.energy, part.gpos.copy(), part.vtens.copy(), tensor.value, nk.value
+
+
+def _rel_rms(a, b):
+    return np.sqrt(((a - b) ** 2).mean()) / np.sqrt((b ** 2).mean())
 
 
 def _compare(ref, mix):
     e0, g0, v0 = ref[:3]
     e1, g1, v1 = mix[:3]
     assert abs(e1 - e0) <= 1e-6 * abs(e0)
-    grms = np.sqrt(((g1 - g0) ** 2).mean()) / np.sqrt((g0 ** 2).mean())
-    assert grms <= 1e-5, grms
+    assert _rel_rms(g1, g0) <= 1e-5, _rel_rms(g1, g0)
     assert np.abs(v1 - v0).max() <= 1e-6 * np.abs(v0).max()
 
 
-def test_tensor_core_reciprocal_matches_fp64():
+@pytest.mark.parametrize('force_path', [0, 1])
+def test_tensor_core_reciprocal_matches_fp64(force_path):
     from yaff_gb300 import configs
     spec = configs.triclinic_mm3_ei(natom=3000)
     ref = _reci(spec, 'fp64')
-    mix = _reci(spec, 'mixed')
-    assert mix[3] == 1 and mix[4] == ref[4] > 1000   # the tensor-core layout was used
+    mix = _reci(spec, 'mixed', force_path=force_path)
+    assert mix[3] == (2 if force_path == 0 else 1) and mix[4] == ref[4] > 1000
     _compare(ref, mix)
 
 
-def test_tensor_core_reciprocal_three_groups():
+@pytest.mark.parametrize('force_path', [0, 1])
+def test_tensor_core_reciprocal_three_groups(force_path):
     from yaff_gb300 import configs
     spec = configs.triclinic_mm3_ei(natom=3000)
     ref = _reci(spec, 'fp64', nlow=700, nhigh=2300)
-    mix = _reci(spec, 'mixed', nlow=700, nhigh=2300)
-    assert mix[3] == 1
+    mix = _reci(spec, 'mixed', nlow=700, nhigh=2300, force_path=force_path)
+    assert mix[3] == (2 if force_path == 0 else 1)
     _compare(ref, mix)
+
+
+def test_tcgen05_and_warp_mma_force_passes_agree():
+    from yaff_gb300 import configs
+    spec = configs.triclinic_mm3_ei(natom=3000)
+    a = _reci(spec, 'mixed', force_path=0)
+    b = _reci(spec, 'mixed', force_path=1)
+    assert a[3] == 2 and b[3] == 1
+    assert a[0] == b[0]   # same structure factors and energy kernel
+    assert _rel_rms(a[1], b[1]) <= 2e-6, _rel_rms(a[1], b[1])

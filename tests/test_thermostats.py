@@ -103,3 +103,56 @@ def test_host_barostat_matches_reference(name):
         assert np.allclose(ff.orc.cell.rvecs, BARO['%s_rvecs' % name][s], rtol=0, atol=1e-12 * 30), (name, s)
         assert abs(vi.epot - BARO['%s_epot' % name][s]) <= 1e-10 * abs(BARO['%s_epot' % name][s])
         assert abs(vi.econs - BARO['%s_econs' % name][s]) <= 1e-10 * abs(BARO['%s_econs' % name][s])
+
+
+NPT = dict(np.load(os.path.join(gc.GOLDEN, 'md_npt.npz')))
+
+
+def _npt_hooks(name, ff):
+    T, tc = float(NPT['temp']), float(NPT['timecon'])
+    press, btc = float(NPT['press']), float(NPT['baro_timecon'])
+    cv0 = NPT['chain_vel0']
+    if name == 'mtk_nhc_aniso':
+        return [verlet.NHCThermostat(T, timecon=tc, chainlength=3, chain_vel0=cv0.copy()),
+                verlet.MTKBarostat(ff, T, press, timecon=btc, anisotropic=True)]
+    if name == 'mtk_nhc_iso':
+        return [verlet.NHCThermostat(T, timecon=tc, chainlength=3, chain_vel0=cv0.copy()),
+                verlet.MTKBarostat(ff, T, press, timecon=btc, anisotropic=False)]
+    if name == 'mtk_cellchain':
+        return [verlet.NHCThermostat(T, timecon=tc, chainlength=3, chain_vel0=cv0.copy()),
+                verlet.MTKBarostat(ff, T, press, timecon=btc, anisotropic=True,
+                                   baro_thermo=verlet.NHCThermostat(T, timecon=tc, chainlength=3))]
+    if name == 'langevin_berendsen_aniso':
+        return [verlet.BerendsenThermostat(T, timecon=tc),
+                verlet.LangevinBarostat(ff, T, press, timecon=btc, anisotropic=True)]
+    return [verlet.LangevinThermostat(T, timecon=tc),
+            verlet.LangevinBarostat(ff, T, press, timecon=btc, anisotropic=False)]
+
+
+@pytest.mark.parametrize('name', ['mtk_nhc_aniso', 'mtk_nhc_iso', 'mtk_cellchain', 'langevin_berendsen_aniso',
+                                  'langevin_langevin_iso'])
+def test_host_npt_matches_reference(name):
+    """MTK barostat (with a particle Nose-Hoover chain, isotropic and
+    anisotropic, and with a chain of its own on the cell) and Langevin
+    barostat (with Berendsen and Langevin thermostats), combined as the
+    reference combines them, follow the reference's trajectories
+    (tests/golden/md_npt.npz): positions, velocities, cells, potential,
+    kinetic and conserved energies over 12 steps; random draws from NumPy's
+    global generator seeded as the reference run was."""
+    spec = configs.flexible_water(nside=4, box=12.42, rcut=5.0, skin=0.5, name='water64')
+    ff = _OracleAdapter(spec)
+    np.random.seed(int(NPT['%s_seed' % name]))
+    hooks = _npt_hooks(name, ff)
+    vi = verlet.VerletIntegrator(ff, float(NPT['timestep']), vel0=NPT['vel0'].copy(), hooks=hooks)
+    assert vi.ndof == int(NPT['%s_ndof' % name])
+    for s in range(int(NPT['nstep']) + 1):
+        if s:
+            vi.propagate()
+        ref = NPT['%s_pos' % name][s]
+        assert np.allclose(vi.pos, ref, rtol=0, atol=1e-10 * abs(ref).max()), (name, s)
+        vref = NPT['%s_vel' % name][s]
+        assert np.allclose(vi.vel, vref, rtol=0, atol=1e-8 * abs(vref).max()), (name, s)
+        assert np.allclose(ff.orc.cell.rvecs, NPT['%s_rvecs' % name][s], rtol=0, atol=1e-10 * 30), (name, s)
+        for key in ('epot', 'ekin', 'econs'):
+            r = NPT['%s_%s' % (name, key)][s]
+            assert abs(getattr(vi, key) - r) <= 1e-9 * max(abs(r), 1.0), (name, key, s)

@@ -10,7 +10,7 @@ velocity Verlet on the host or fully device-resident (``verlet``), a
 serving loop for many small systems (``serve``) and batched Monte Carlo
 trial energies with the reference's structure-factor functions (``mc``).
 """
-from .system import Cell, System
+from .system import Cell, System, SystemView, as_system
 from .pair import (Hammer, Switch3, PairPotLJ, PairPotMM3, PairPotEI, PairPotMM3CAP, PairPotGrimme, PairPotExpRep,
                    PairPotQMDFFRep, PairPotLJCross, PairPotDampDisp, PairPotDisp68BJDamp)
 from .scaling import Scalings

@@ -59,8 +59,11 @@ SIGNATURES = {
     'yg_clear_pair_pots': (_I, [_P]),
     'yg_nlist_build': (_I, [_P, _D, _P, _I64, _I64, ctypes.POINTER(_I64)]),
     'yg_nlist_stats': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    'yg_nlist_set_capacity': (_I, [_P, _I64]),
     'yg_ewald_info': (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64)]),
     'yg_ewald_wait': (_I, [_P]),
+    'yg_ewald_force_path': (_I, [_P, _I]),
+    'yg_check_wait_timeout': (_I, [_P, _I64, ctypes.POINTER(_I)]),
     'yg_nlist_recompute': (_I, [_P]),
     'yg_nlist_max_disp2': (_I, [_P, ctypes.POINTER(_D)]),
     'yg_nlist_export': (_I, [_P, _P, _I64, ctypes.POINTER(_I64)]),
@@ -77,7 +80,6 @@ SIGNATURES = {
     'yg_launch_count': (_I64, [_P]),
     'yg_mem_usage': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     'yg_pool_usage': (_I, [ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
-    'yg_probe_peak': (_D, [_I, _P]),
     'yg_md_setup': (_I, [_P, _P, _P, _D, _I, _D, _I64]),
     'yg_md_run': (_I, [_P, _I64, _I, _D, ctypes.POINTER(_I64)]),
     'yg_md_get': (_I, [_P, _P, _P, _P, ctypes.POINTER(_I64)]),

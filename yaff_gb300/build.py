@@ -41,7 +41,8 @@ def sources():
 
 def _stamp():
     h = hashlib.sha256()
-    for f in sorted(os.listdir(CSRC)) + [os.path.join(INCLUDE, 'yaffgb.h')]:
+    files = [f for f in sorted(os.listdir(CSRC)) if os.path.isfile(os.path.join(CSRC, f))]
+    for f in files + [os.path.join(INCLUDE, 'yaffgb.h')]:
         p = f if os.path.isabs(f) else os.path.join(CSRC, f)
         h.update(p.encode())
         with open(p, 'rb') as fh:
@@ -85,5 +86,26 @@ def build(force=False, verbose=False, extra_flags=()):
     return LIB
 
 
+PROBE_SRC = os.path.join(CSRC, 'bench', 'yg_probe.cu')
+PROBE_LIB = os.path.join(BUILD, 'libyaffgb_probe.so')
+
+
+def build_probe():
+    """Compile the bench-only throughput probes (csrc/bench/yg_probe.cu) into
+    _build/libyaffgb_probe.so; not part of libyaffgb.so.  Returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [PROBE_SRC, os.path.join(CSRC, 'yg_internal.cuh'), os.path.join(INCLUDE, 'yaffgb.h')]
+    if os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= max(os.path.getmtime(p) for p in deps):
+        return PROBE_LIB
+    tmp = PROBE_LIB + '.%d.tmp' % os.getpid()
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ['-I', INCLUDE, '-shared', PROBE_SRC, '-o', tmp, '-lcudart']
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (PROBE_SRC, res.stdout, res.stderr))
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
+
+
 if __name__ == '__main__':
     print(build(force='--force' in sys.argv, verbose=True))
+    print(build_probe())

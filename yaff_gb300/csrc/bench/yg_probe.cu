@@ -7,7 +7,7 @@
 // FP32 pairs (f32x2, two FMAs per instruction), so the FP32 denominator can be
 // taken as the larger of the scalar and packed rates.  It is bounded: a fixed
 // number of iterations, no waits, no atomics.
-#include "yg_internal.cuh"
+#include "../yg_internal.cuh"
 
 namespace {
 

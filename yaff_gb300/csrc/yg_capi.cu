@@ -258,7 +258,8 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_ew_pref, (void **)&c->d_ew_tiles, (void **)&c->d_ew_tab, (void **)&c->d_ew_Spart,
       (void **)&c->d_ew_S, (void **)&c->d_ew_W, (void **)&c->d_ew_wslot, (void **)&c->d_ew_gpart, (void **)&c->d_ew_red,
       (void **)&c->d_ew_fpre, (void **)&c->d_ew_fpiece, (void **)&c->d_ew_woff, (void **)&c->d_ew_crange, (void **)&c->d_ew_te,
-      (void **)&c->d_ew_yf, (void **)&c->d_ew_ys, (void **)&c->d_ew_wb,
+      (void **)&c->d_ew_yf, (void **)&c->d_ew_ys, (void **)&c->d_ew_wb, (void **)&c->d_ew_uoff,
+      (void **)&c->d_ew_urange, (void **)&c->d_ew_ya, (void **)&c->d_ew_ub,
       (void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval, (void **)&c->d_vpar,
       (void **)&c->d_vkind, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,
       (void **)&c->d_total, (void **)&c->d_red, (void **)&c->d_vel, (void **)&c->d_invm, (void **)&c->d_md_ekpart,
@@ -540,8 +541,32 @@ int yg_ewald_wait(yg_ctx *c) {
 
 int yg_ewald_info(yg_ctx *c, int *tensor_path, int64_t *nk) {
   if (!c) return YG_ERR_ARG;
-  if (tensor_path) *tensor_path = c->have_ewald ? c->ew_mma : 0;
+  if (tensor_path) {
+    int t = c->have_ewald ? c->ew_mma : 0;
+    if (t && c->ew_umma && c->ew_force_path == 0) t = 2;
+    *tensor_path = t;
+  }
   if (nk) *nk = c->have_ewald ? c->ew_nk : 0;
+  return YG_OK;
+}
+
+int yg_check_wait_timeout(yg_ctx *c, int64_t polls, int *timed_out) {
+  if (!c || polls < 1 || polls > (1LL << 24) || !timed_out) return YG_ERR_ARG;
+  int rc;
+  if ((rc = yg_ewald_join(c))) return rc;
+  YG_CUDA(cudaMemsetAsync(c->d_status, 0, YG_ST_NWORDS * sizeof(int), c->stream));
+  if ((rc = yg_launch_check_wait_timeout(c, polls))) return rc;
+  YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  *timed_out = c->h_status[YG_ST_TIMEOUT] ? 1 : 0;
+  return YG_OK;
+}
+
+int yg_ewald_force_path(yg_ctx *c, int path) {
+  if (!c || path < 0 || path > 1) return YG_ERR_ARG;
+  int rc;
+  if ((rc = yg_ewald_join(c))) return rc;
+  c->ew_force_path = path;
   return YG_OK;
 }
 

@@ -427,11 +427,23 @@ __device__ __forceinline__ void wb_put(unsigned *__restrict__ rec, int bsel, int
   rec[off + 2 + bsel] = *reinterpret_cast<const unsigned *>(&l);
 }
 
+// FP16 split of a weight pair into a B-operand unit of the tcgen05 force
+// pass: hi at word w of the unit's first 8 KB, lo at the same word of the
+// second.
+__device__ __forceinline__ void ub_put(unsigned *__restrict__ unit, int w, float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 f = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - f.x, b - f.y);
+  unit[w] = *reinterpret_cast<const unsigned *>(&h);
+  unit[w + 2048] = *reinterpret_cast<const unsigned *>(&l);
+}
+
 template <typename T>
 __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_dense, const double *__restrict__ pref,
                                int G0, int G1, int nm, CellGeom cell, double fac2, int ngroup,
                                const int *__restrict__ wslot, int64_t wstride, typename C2<T>::t *__restrict__ W,
                                unsigned *__restrict__ wbw, const int *__restrict__ woff, int64_t wbstride,
+                               unsigned *__restrict__ ubw, const int *__restrict__ uoff, int64_t ubstride,
                                double wsc1, double wsc2, double *__restrict__ partial) {
   __shared__ double red[256 / 32][7];
   int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -496,6 +508,21 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
           wb_put(rq1, bsel, 0, (float)(a1 * ui), (float)(a1 * ur));
           wb_put(rq0 + 128, bsel, 0, (float)(a2 * ur), (float)(-a2 * ui));
           wb_put(rq1 + 128, bsel, 0, (float)(a2 * ui), (float)(a2 * ur));
+        }
+        const int ut = slot >> 6, uks = mm >> 3;
+        if (ubw && uks < uoff[ut + 1] - uoff[ut]) {
+          // tcgen05 B operand: row n = 4 j + q of the tile (q: Z re, Z im,
+          // Z2 re, Z2 im), K element 2 ml + (re, im) of m = 8 ks + ml; in the
+          // no-swizzle K-major layout the (re, im) pair is one 32-bit word
+          unsigned *unit = ubw + (int64_t)g * ubstride + (int64_t)(uoff[ut] + uks) * 4096;
+          const int j = slot & 63, ml = mm & 7;
+          const double a1 = wsc1, a2 = wsc2 * mm;
+          const int wb0 = (ml >> 2) * 32 + (ml & 3);
+          const int n0 = 4 * j;
+          ub_put(unit, ((n0 + 0) >> 3) * 64 + ((n0 + 0) & 7) * 4 + wb0, (float)(a1 * ur), (float)(-a1 * ui));
+          ub_put(unit, ((n0 + 1) >> 3) * 64 + ((n0 + 1) & 7) * 4 + wb0, (float)(a1 * ui), (float)(a1 * ur));
+          ub_put(unit, ((n0 + 2) >> 3) * 64 + ((n0 + 2) & 7) * 4 + wb0, (float)(a2 * ur), (float)(-a2 * ui));
+          ub_put(unit, ((n0 + 3) >> 3) * 64 + ((n0 + 3) & 7) * 4 + wb0, (float)(a2 * ui), (float)(a2 * ur));
         }
       }
     }
@@ -812,10 +839,43 @@ __global__ void k_store_corr_ev(const double *__restrict__ sums, double eself, d
   for (int q = 0; q < 9; q++) ev[1 + q] = v[q];
 }
 
+// The bounded mbarrier wait of the kernels above on a barrier that nothing
+// arrives at (no copy in flight): after `polls` polls the wait gives up and
+// records YG_ST_TIMEOUT, exactly as a copy that never lands would make it.
+__global__ void k_check_wait_timeout(int64_t polls, int *__restrict__ status) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    bool done = false;
+    for (int64_t it = 0; it < polls && !done; it++) {
+      unsigned ok;
+      asm volatile(
+          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+          : "=r"(ok)
+          : "r"(smem_u32(&bar))
+          : "memory");
+      done = ok != 0;
+    }
+    if (!done) atomicOr(status + YG_ST_TIMEOUT, 1);
+  }
+}
+
+}  // namespace
+
+int yg_launch_check_wait_timeout(yg_ctx *ctx, int64_t polls) {
+  k_check_wait_timeout<<<1, 32, 0, ctx->stream>>>(polls, ctx->d_status);
+  YG_LAUNCH_CHECK(ctx, "k_check_wait_timeout");
+  return YG_OK;
+}
+
 // Raises a kernel's dynamic shared-memory limit to the device's opt-in
 // maximum, once per (kernel, device): setting it per launch to the launch's
 // own size would race between host threads that drive different contexts.
-static int smem_optin(const void *kernel, size_t need) {
+int yg_smem_optin(const void *kernel, size_t need) {
   static std::mutex mu;
   static std::set<std::pair<const void *, int>> done;
   int dev = 0;
@@ -835,6 +895,8 @@ static int smem_optin(const void *kernel, size_t need) {
   done.insert(std::make_pair(kernel, dev));
   return YG_OK;
 }
+
+namespace {
 
 // ---------------------------------------------------------------------------
 // Tensor-core form of the mixed-precision reciprocal sum (G2 + 1 <= 32).
@@ -1402,7 +1464,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
     dim3 grid(nch, nstile, nslab);
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     const size_t ssm = (size_t)2 * SfacCfg<T>::KA * Lp * sizeof(CT);
-    if ((rc = smem_optin((const void *)k_sfac<T, TA>, ssm))) return rc;
+    if ((rc = yg_smem_optin((const void *)k_sfac<T, TA>, ssm))) return rc;
     k_sfac<T, TA><<<grid, 128, ssm, ctx->stream>>>(tab, (int)gb[g][0], (int)gb[g][1], G0, G1, G2,
                                                  (const int4 *)ctx->d_ew_tiles, (CA *)ctx->d_ew_Spart, nstile, nslab,
                                                  ctx->d_status);
@@ -1423,7 +1485,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
                                                 fac2, ngroup, ctx->d_ew_wslot, wstride, (CT *)ctx->d_ew_W,
-                                                nullptr, nullptr, 0, 0.0, 0.0, partial);
+                                                nullptr, nullptr, 0, nullptr, nullptr, 0, 0.0, 0.0, partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -1439,7 +1501,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   // force pass, per atom group
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
   size_t smem = force_smem<T>(G0, G1, nm, RA);
-  if ((rc = smem_optin((const void *)k_ewald_force<T, RA>, smem))) return rc;
+  if ((rc = yg_smem_optin((const void *)k_ewald_force<T, RA>, smem))) return rc;
   const int NA = 16 * RA;
   int slots;
   if ((rc = resident_blocks((const void *)k_ewald_force<T, RA>, 256, smem, &ctx->ew_occ_f, &slots))) return rc;
@@ -1526,7 +1588,7 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   const size_t per = (size_t)ntile64 * 64 * EW_MS;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(float2)))) return rc;
   const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
-  if ((rc = smem_optin((const void *)k_sfac_mma, ssm))) return rc;
+  if ((rc = yg_smem_optin((const void *)k_sfac_mma, ssm))) return rc;
   for (int g = 0; g < nS; g++) {
     const int64_t n = gb[g][1] - gb[g][0];
     double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
@@ -1543,20 +1605,28 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
         (const float2 *)ctx->d_ew_Spart, nch, ntile64, 1, 64, (const int4 *)ctx->d_ew_tiles, nm, 1.0 / qscale, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
-  // energy, virial, weight fragments
+  // energy, virial, weights of the force pass: B operands of the tcgen05
+  // kernel, or fragments of the warp-level MMA kernel
   const int ngroup = (nS == 3) ? 3 : 1;
+  const bool umma = want_grad && ctx->ew_umma && ctx->ew_force_path == 0;
   const int64_t wbstride = (int64_t)ctx->ew_wbunits * 256;  // 32-bit words per group
-  if ((rc = yg_ensure(ctx, &ctx->d_ew_wb, &ctx->ew_bytes_wb, (size_t)ngroup * wbstride * 4))) return rc;
-  YG_CUDA(cudaMemsetAsync(ctx->d_ew_wb, 0, (size_t)ngroup * wbstride * 4, ctx->stream));
+  const int64_t ubstride = (int64_t)ctx->ew_ubunits * 4096;  // 32-bit words per group
+  if (umma) {
+    if ((rc = yg_ensure(ctx, &ctx->d_ew_ub, &ctx->ew_bytes_ub, (size_t)ngroup * ubstride * 4))) return rc;
+    YG_CUDA(cudaMemsetAsync(ctx->d_ew_ub, 0, (size_t)ngroup * ubstride * 4, ctx->stream));
+  } else {
+    if ((rc = yg_ensure(ctx, &ctx->d_ew_wb, &ctx->ew_bytes_wb, (size_t)ngroup * wbstride * 4))) return rc;
+    YG_CUDA(cudaMemsetAsync(ctx->d_ew_wb, 0, (size_t)ngroup * wbstride * 4, ctx->stream));
+  }
   const int eb = yg_blocks(nk_dense, 256);
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_red, &ctx->ew_red_cap, ((size_t)eb * 7 + 64 + 7) * sizeof(double))))
     return rc;
   double *partial = ctx->d_ew_red + 64;
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
-  k_ewald_energy<float><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
-                                                    fac2, ngroup, ctx->d_ew_wslot, 0, nullptr,
-                                                    (unsigned *)ctx->d_ew_wb, ctx->d_ew_woff, wbstride, s1, s2,
-                                                    partial);
+  k_ewald_energy<float><<<eb, 256, 0, ctx->stream>>>(
+      ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell, fac2, ngroup, ctx->d_ew_wslot, 0, nullptr,
+      umma ? nullptr : (unsigned *)ctx->d_ew_wb, ctx->d_ew_woff, wbstride, umma ? (unsigned *)ctx->d_ew_ub : nullptr,
+      ctx->d_ew_uoff, ubstride, s1, s2, partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -1571,9 +1641,105 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   }
   // force pass, per atom group
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
+  if (umma) {
+    // tcgen05: one CTA per SM (all of TMEM), blocks of 128 atoms x tile ranges
+    int dev = 0, nsm = 1;
+    YG_CUDA(cudaGetDevice(&dev));
+    YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int64_t maxblk = 1;
+    for (int g = 0; g < nS; g++) maxblk = std::max<int64_t>(maxblk, (gb[g][1] - gb[g][0] + 127) / 128);
+    if ((rc = yg_ensure(ctx, &ctx->d_ew_ya, &ctx->ew_bytes_ya, (size_t)maxblk * nks * 2 * 4096))) return rc;
+    for (int g = 0; g < nS; g++) {
+      const int64_t n = gb[g][1] - gb[g][0];
+      if (n <= 0) continue;
+      const int nab = (int)((n + 127) / 128);
+      if ((rc = yg_launch_ya_umma(ctx, ctx->d_ew_yf, gb[g][0], n, nmf, nks, nab, ctx->d_ew_ya))) return rc;
+      int nr = 1;
+      double best = 0.0;
+      for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
+        const double waves = (double)nab * r / nsm;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best + 1e-9) {
+          best = eff;
+          nr = r;
+        }
+      }
+      double *out = ctx->d_ew_gpart;
+      const int64_t rstride = N * 3;
+      if (nr > 1) {
+        if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_fpiece, &ctx->ew_bytes_fpiece, (size_t)nr * rstride * sizeof(double))))
+          return rc;
+        out = ctx->d_ew_fpiece;
+      }
+      const void *ubg = (const unsigned *)ctx->d_ew_ub + (size_t)(ngroup == 1 ? 0 : g) * ubstride;
+      if ((rc = yg_launch_force_umma(ctx, te, ctx->d_ew_ya, (int)gb[g][0], (int)gb[g][1], G0 + G1 + 2, G0, lep, nks,
+                                     ctx->d_ew_urange + (nr - 1) * (nr + 2) / 2, nr, ubg, 1.0 / (qscale * s1),
+                                     1.0 / (qscale * s2), out, rstride)))
+        return rc;
+      if (nr > 1) {
+        k_ewald_force_mma_combine<<<yg_blocks(n * 3, 256), 256, 0, ctx->stream>>>(ctx->d_ew_fpiece, rstride, nr,
+                                                                                  (int)gb[g][0], (int)gb[g][1],
+                                                                                  ctx->d_ew_gpart);
+        YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma_combine");
+      }
+    }
+    k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
+                                                             -6.2831853071795864769 / ctx->ew_diel, gpos);
+    YG_LAUNCH_CHECK(ctx, "k_ewald_gpos");
+    ctx->part_valid[YG_PART_EWALD_RECI] = 1;
+    return YG_OK;
+  }
+  if (umma) {
+    // tcgen05: one CTA per SM (all of TMEM), blocks of 128 atoms x tile ranges
+    int dev = 0, nsm = 1;
+    YG_CUDA(cudaGetDevice(&dev));
+    YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int64_t maxblk = 1;
+    for (int g = 0; g < nS; g++) maxblk = std::max<int64_t>(maxblk, (gb[g][1] - gb[g][0] + 127) / 128);
+    if ((rc = yg_ensure(ctx, &ctx->d_ew_ya, &ctx->ew_bytes_ya, (size_t)maxblk * nks * 2 * 4096))) return rc;
+    for (int g = 0; g < nS; g++) {
+      const int64_t n = gb[g][1] - gb[g][0];
+      if (n <= 0) continue;
+      const int nab = (int)((n + 127) / 128);
+      if ((rc = yg_launch_ya_umma(ctx, ctx->d_ew_yf, gb[g][0], n, nmf, nks, nab, ctx->d_ew_ya))) return rc;
+      int nr = 1;
+      double best = 0.0;
+      for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
+        const double waves = (double)nab * r / nsm;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best + 1e-9) {
+          best = eff;
+          nr = r;
+        }
+      }
+      double *out = ctx->d_ew_gpart;
+      const int64_t rstride = N * 3;
+      if (nr > 1) {
+        if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_fpiece, &ctx->ew_bytes_fpiece, (size_t)nr * rstride * sizeof(double))))
+          return rc;
+        out = ctx->d_ew_fpiece;
+      }
+      const void *ubg = (const unsigned *)ctx->d_ew_ub + (size_t)(ngroup == 1 ? 0 : g) * ubstride;
+      if ((rc = yg_launch_force_umma(ctx, te, ctx->d_ew_ya, (int)gb[g][0], (int)gb[g][1], G0 + G1 + 2, G0, lep, nks,
+                                     ctx->d_ew_urange + (nr - 1) * (nr + 2) / 2, nr, ubg, 1.0 / (qscale * s1),
+                                     1.0 / (qscale * s2), out, rstride)))
+        return rc;
+      if (nr > 1) {
+        k_ewald_force_mma_combine<<<yg_blocks(n * 3, 256), 256, 0, ctx->stream>>>(ctx->d_ew_fpiece, rstride, nr,
+                                                                                  (int)gb[g][0], (int)gb[g][1],
+                                                                                  ctx->d_ew_gpart);
+        YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma_combine");
+      }
+    }
+    k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
+                                                             -6.2831853071795864769 / ctx->ew_diel, gpos);
+    YG_LAUNCH_CHECK(ctx, "k_ewald_gpos");
+    ctx->part_valid[YG_PART_EWALD_RECI] = 1;
+    return YG_OK;
+  }
   const size_t fsm = (size_t)128 * lep * sizeof(float2) +
                      2 * ((size_t)EW_MMA_FT * nks * 1024 + EW_MMA_FT * 4 * sizeof(int4));
-  if ((rc = smem_optin((const void *)k_ewald_force_mma, fsm))) return rc;
+  if ((rc = yg_smem_optin((const void *)k_ewald_force_mma, fsm))) return rc;
   int slots;
   if ((rc = resident_blocks((const void *)k_ewald_force_mma, 256, fsm, &ctx->ew_occ_fm, &slots))) return rc;
   for (int g = 0; g < nS; g++) {
@@ -1712,6 +1878,31 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
         crange.push_back(t);
       }
   }
+  // tcgen05 force pass: 64-column tiles with work, their B-operand units (one
+  // per 8 m values of the tile's extent) and tile ranges of equal cost
+  // (three MMAs per K-step against an epilogue worth about four)
+  std::vector<int> uoff(1, 0);
+  const int ucols = yg_umma_cols();
+  for (size_t t = 0; t * ucols < tiles.size() && tiles[t * ucols].w >= 0; t++)
+    uoff.push_back(uoff.back() + (tiles[t * ucols].w + 8) / 8);
+  ctx->ew_nut = (int)uoff.size() - 1;
+  ctx->ew_ubunits = uoff.back();
+  ctx->ew_umma = (ctx->ew_mma && (nm + 7) / 8 <= yg_umma_kmax() && yg_umma_force_smem(G0 + G1 + 2) > 0) ? 1 : 0;
+  std::vector<int> urange;
+  {
+    std::vector<long long> cost(1, 0);
+    for (int t = 0; t < ctx->ew_nut; t++) cost.push_back(cost.back() + (uoff[t + 1] - uoff[t]) + 4);
+    for (int r = 1; r <= EW_MMA_MAXR; r++)
+      for (int i = 0; i <= r; i++) {
+        int t = 0;
+        while (t < ctx->ew_nut && cost[t] * r < cost.back() * i) t++;
+        urange.push_back(t);
+      }
+  }
+  yg_free(ctx, (void **)&ctx->d_ew_uoff);
+  ctx->d_ew_uoff = nullptr;
+  yg_free(ctx, (void **)&ctx->d_ew_urange);
+  ctx->d_ew_urange = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_crange);
   ctx->d_ew_crange = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_woff);
@@ -1731,6 +1922,12 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_fpre, fpre.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_woff, woff.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_crange, crange.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_uoff, uoff.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_urange, urange.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_uoff, uoff.data(), uoff.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_urange, urange.data(), urange.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_crange, crange.data(), crange.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_woff, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice,

@@ -214,6 +214,16 @@ struct yg_ctx {
   void *d_ew_ys = nullptr;        // q E2 as FP16 B fragments per 16 atoms
   void *d_ew_wb = nullptr;        // force weights as FP16 B fragments, per group
   size_t ew_bytes_te = 0, ew_bytes_yf = 0, ew_bytes_ys = 0, ew_bytes_wb = 0;
+  // tcgen05 form of the force pass (yg_ewald_umma.cu): 64-column tiles
+  int ew_umma = 0;                // 1 when the k-space layout suits it
+  int ew_force_path = 0;          // requested: 0 automatic, 1 warp-level MMA
+  int ew_nut = 0;                 // 64-column tiles with work
+  int ew_ubunits = 0;             // 16 KB B-operand units (tile x K-step) of one group's weights
+  int *d_ew_uoff = nullptr;       // first unit of every 64-column tile (nut + 1)
+  int *d_ew_urange = nullptr;     // tile-range bounds for 1..EW_MMA_MAXR ranges
+  void *d_ew_ya = nullptr;        // A operand (q E2 hi/lo) per 128-atom block and K-step
+  void *d_ew_ub = nullptr;        // B operand (weights hi/lo) per unit, per group
+  size_t ew_bytes_ya = 0, ew_bytes_ub = 0;
   int *d_ew_fpre = nullptr;       // prefix sums of the force column-tile costs (nftile + 1)
   double *d_ew_fpiece = nullptr;  // force sums of the split atom tiles [tile][part][NA][3]
   size_t ew_bytes_fpiece = 0;
@@ -378,6 +388,17 @@ int yg_launch_valence(yg_ctx *ctx, int want_grad);
 int yg_launch_total(yg_ctx *ctx, int part_mask);
 int yg_pack_pair_params(yg_ctx *ctx);
 int yg_launch_reduce_ev(yg_ctx *ctx, const double *partials, int nblocks, int nval, double *out);
+int yg_launch_check_wait_timeout(yg_ctx *ctx, int64_t polls);
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device).
+int yg_smem_optin(const void *kernel, size_t need);
+// tcgen05 force pass of the mixed reciprocal sum (yg_ewald_umma.cu)
+size_t yg_umma_force_smem(int ne);
+int yg_umma_kmax();
+int yg_umma_cols();
+int yg_launch_ya_umma(yg_ctx *ctx, const void *yf, int64_t a0, int64_t n, int nmf, int nks, int64_t nblk, void *ya);
+int yg_launch_force_umma(yg_ctx *ctx, const void *te, const void *ya, int a0, int a1, int ne, int G0, int lep,
+                         int nks, const int *urange, int nr, const void *ub, double inv1, double inv2, double *out,
+                         int64_t rstride);
 
 // Grid-stride helper.
 static inline int yg_blocks(int64_t n, int threads) {

@@ -401,6 +401,32 @@ static int md_capture(yg_ctx *c, double factor, double skin) {
 
 extern "C" {
 
+// Per-atom neighbour-slot capacity of the next builds (rounded up to 32,
+// at least 32).  Builds that need more slots regrow as usual: the host build
+// reruns, the device-resident MD rolls its batch back and reruns it.
+int yg_nlist_set_capacity(yg_ctx *c, int64_t slots) {
+  if (!c || slots < 1) return YG_ERR_ARG;
+  int rc;
+  if ((rc = yg_ewald_join(c))) return rc;
+  int64_t cap = (std::max<int64_t>(slots, 32) + 31) / 32 * 32;
+  c->nbr_cap = cap;
+  if (c->nbr_cap * c->natom > c->nbr_alloc) {
+    yg_free(c, (void **)&c->d_nbr);
+    if ((rc = yg_alloc(c, (void **)&c->d_nbr, (size_t)(c->nbr_cap * c->natom) * sizeof(uint2)))) return rc;
+    c->nbr_alloc = c->nbr_cap * c->natom;
+  }
+  md_drop_graph(c);  // the capacity is baked into a captured step
+  // the rows in the slots were laid out with the old capacity: no kernel may
+  // read them again; the host path rebuilds before its next use and the
+  // device-resident MD rebuilds at its next step
+  c->have_list = 0;
+  if (c->md_ready) {
+    k_set_int<<<1, 32, 0, c->stream>>>(c->d_md_ctrl + 1, 1);
+    YG_LAUNCH_CHECK(c, "k_set_int");
+  }
+  return YG_OK;
+}
+
 int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, int part_mask, double extra_energy,
                 int64_t max_steps) {
   if (c) {

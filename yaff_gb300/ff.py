@@ -21,6 +21,7 @@ import numpy as np
 from . import _lib
 from ._lib import check
 from .device import device_of
+from .system import as_system
 from .valence import DeltaList, InternalCoordinateList, ValenceList
 
 __all__ = ['ForcePart', 'ForceField', 'ForcePartPair', 'ForcePartEwaldReciprocal', 'ForcePartEwaldCorrection',
@@ -32,6 +33,7 @@ class ForcePart(object):
     device_slot = None
 
     def __init__(self, name, system):
+        system = as_system(system)
         self.name = name
         self.system = system
         self.energy = 0.0
@@ -123,10 +125,10 @@ class ForceField(ForcePart):
     """A complete force field: a neighbour list and a list of parts."""
 
     def __init__(self, system, parts, nlist=None):
+        system = as_system(system)
         ForcePart.__init__(self, 'all', system)
         self._host_vtens = None
         self._total_mask = 0
-        self.system = system
         self.parts = []
         self.nlist = nlist
         self.needs_nlist_update = nlist is not None
@@ -291,6 +293,7 @@ class ForcePartPair(ForcePart):
     device_slot = 'pair'
 
     def __init__(self, system, nlist, scalings, pair_pot):
+        system = as_system(system)
         ForcePart.__init__(self, 'pair_%s' % pair_pot.name, system)
         self.nlist = nlist
         self.scalings = scalings
@@ -331,6 +334,7 @@ class ForcePartEwaldReciprocal(ForcePart):
     device_slot = _lib.PART_EWALD_RECI
 
     def __init__(self, system, alpha, gcut=0.35, dielectric=1.0, nlow=0, nhigh=-1):
+        system = as_system(system)
         ForcePart.__init__(self, 'ewald_reci', system)
         if not system.cell.nvec == 3:
             raise TypeError('The system must have a 3D periodic cell.')
@@ -380,6 +384,7 @@ class ForcePartEwaldCorrection(ForcePart):
     device_slot = _lib.PART_EWALD_CORR
 
     def __init__(self, system, alpha, scalings, dielectric=1.0, nlow=0, nhigh=-1):
+        system = as_system(system)
         ForcePart.__init__(self, 'ewald_cor', system)
         if not system.cell.nvec == 3:
             raise TypeError('The system must have a 3D periodic cell')
@@ -422,6 +427,7 @@ class ForcePartEwaldNeutralizing(ForcePart):
     host_scalar = True
 
     def __init__(self, system, alpha, dielectric=1.0, nlow=0, nhigh=-1, fluctuating_charges=False):
+        system = as_system(system)
         ForcePart.__init__(self, 'ewald_neut', system)
         if not system.cell.nvec == 3:
             raise TypeError('The system must have a 3D periodic cell')
@@ -465,6 +471,7 @@ class ForcePartTailCorrection(ForcePart):
     host_scalar = True
 
     def __init__(self, system, part_pair, nlow=0, nhigh=-1):
+        system = as_system(system)
         if system.cell.nvec != 3:
             raise ValueError('Tail corrections can only be applied to 3D periodic systems')
         if part_pair.name in ['pair_ei', 'pair_eidip']:
@@ -488,6 +495,7 @@ class ForcePartValence(ForcePart):
     device_slot = _lib.PART_VALENCE
 
     def __init__(self, system, comlist=None):
+        system = as_system(system)
         ForcePart.__init__(self, 'valence', system)
         if comlist is not None:
             raise NotImplementedError('centre-of-mass layers are not supported on the device')

@@ -15,6 +15,7 @@ import numpy as np
 from . import _lib
 from ._lib import check, ptr
 from .device import device_of
+from .system import as_system
 
 __all__ = ['NeighborList', 'neigh_dtype']
 
@@ -23,6 +24,7 @@ neigh_dtype = _lib.neigh_dtype
 
 class NeighborList(object):
     def __init__(self, system, skin=0, nlow=0, nhigh=-1):
+        system = as_system(system)
         if skin < 0:
             raise ValueError('The skin parameter must be positive.')
         if nhigh == -1:
@@ -68,6 +70,15 @@ class NeighborList(object):
         check(self.device.lib.yg_nlist_max_disp2(self.device.ctx, ctypes.byref(d2)), 'yg_nlist_max_disp2')
         disp = np.sqrt(d2.value) * 2 * (self.rmax.max() + 1)
         return disp >= self.skin
+
+    def set_capacity(self, slots):
+        """Per-atom slot capacity of the device list's next builds (rounded
+        up to 32); the current list is dropped and the next update rebuilds.
+        Builds that need more slots regrow, as the reference's buffer does
+        (yaff/pes/nlist.py:170-182)."""
+        check(self.device.lib.yg_nlist_set_capacity(self.device.ctx, int(slots)), 'yg_nlist_set_capacity')
+        self.rebuild_next = True
+        self._neighs_cache = None
 
     def update(self, upload=True):
         """Rebuild or recompute the list for the current system positions."""

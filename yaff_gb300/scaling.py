@@ -2,6 +2,7 @@
 (yaff/pes/scaling.py:58-105): rows (a > b, scale, nbond) for 1-2, 1-3, 1-4
 and 1-5 pairs whose scale is below one, sorted by (a, b)."""
 import numpy as np
+from .system import as_system
 
 __all__ = ['Scalings', 'scaling_dtype']
 
@@ -10,6 +11,7 @@ scaling_dtype = np.dtype([('a', 'i8'), ('b', 'i8'), ('scale', 'f8'), ('nbond', '
 
 class Scalings(object):
     def __init__(self, system, scale1=0.0, scale2=0.0, scale3=1.0, scale4=1.0):
+        system = as_system(system)
         for name, s in (('scale1', scale1), ('scale2', scale2), ('scale3', scale3), ('scale4', scale4)):
             if s < -1 or s > 1:
                 raise ValueError('%s must be in the range [-1,1].' % name)

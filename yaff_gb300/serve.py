@@ -33,8 +33,8 @@ import numpy as np
 from . import configs
 from .units import femtosecond
 
-__all__ = ['Request', 'make_workload', 'estimate_bytes', 'serve_request', 'ServingEngine', 'run_sequential',
-           'summarize']
+__all__ = ['Request', 'Cancelled', 'make_workload', 'estimate_bytes', 'serve_request', 'ServingEngine',
+           'run_sequential', 'summarize']
 
 
 
@@ -54,10 +54,21 @@ class Request(object):
         self.bytes_high = 0
         self.slot = None
         self.error = None
+        self.cancelled = False
+
+    def cancel(self):
+        """Withdraws the request: one still waiting for admission is never
+        started; one in service stops at its next batch of MD steps and
+        releases its device memory.  Its error reads 'cancelled'."""
+        self.cancelled = True
 
     @property
     def latency(self):
         return None if self.t_done is None else self.t_done - self.arrival
+
+
+class Cancelled(Exception):
+    """A request was withdrawn while in service."""
 
 
 def request_spec(natom, seed, skin):
@@ -124,7 +135,8 @@ def estimate_bytes(spec, precision='mixed', nsteps=50):
     return int(total * 1.1) + 65536
 
 
-def serve_request(req, stream, precision='mixed', dt=0.5 * femtosecond, temp0=300.0, use_graph=True):
+def serve_request(req, stream, precision='mixed', dt=0.5 * femtosecond, temp0=300.0, use_graph=True,
+                  batch_steps=None):
     """Runs one request start to finish on `stream` (a cudaStream_t handle)
     through the C entry points directly: the same calls the ForceField path
     makes (cell, positions, charges, empty scaling table, the LJ and EI pair
@@ -132,7 +144,9 @@ def serve_request(req, stream, precision='mixed', dt=0.5 * femtosecond, temp0=30
     Ewald set-up with gmax = ceil(gcut/gspacing - 0.5), the neutralizing
     energy as a constant), without building the Python object graph, so
     that the per-request host work holding the GIL stays small.  Fills
-    req.log / pos / vel / nrebuild / bytes_high."""
+    req.log / pos / vel / nrebuild / bytes_high.  With batch_steps the MD
+    runs in batches of that many steps and a cancelled request stops between
+    two of them (raising Cancelled after its context is destroyed)."""
     from ctypes import byref, c_int64, c_void_p
     from . import _lib
     from ._lib import check, ptr
@@ -188,7 +202,17 @@ def serve_request(req, stream, precision='mixed', dt=0.5 * femtosecond, temp0=30
         check(lib.yg_md_setup(h, ptr(masses), ptr(vel), float(dt), mask, float(eneut), req.nsteps), 'yg_md_setup')
         tp.append(time.perf_counter())
         nreb = c_int64()
-        check(lib.yg_md_run(h, req.nsteps, int(use_graph), skin, byref(nreb)), 'yg_md_run')
+        left = req.nsteps
+        step = req.nsteps if not batch_steps else int(batch_steps)
+        nrebuild = 0
+        while left > 0:
+            if req.cancelled:
+                raise Cancelled()
+            nb = min(step, left)
+            check(lib.yg_md_run(h, nb, int(use_graph), skin, byref(nreb)), 'yg_md_run')
+            nrebuild += nreb.value
+            left -= nb
+        nreb.value = nrebuild
         tp.append(time.perf_counter())
         req.pos = np.zeros((n, 3))
         req.vel = np.zeros((n, 3))
@@ -221,7 +245,7 @@ class ServingEngine(object):
     """
 
     def __init__(self, nslots=8, budget_bytes=8 << 30, precision='mixed', use_graph=True,
-                 dt=0.5 * femtosecond, temp0=300.0):
+                 dt=0.5 * femtosecond, temp0=300.0, batch_steps=None):
         import torch
         self.nslots = int(nslots)
         self.budget = int(budget_bytes)
@@ -229,6 +253,7 @@ class ServingEngine(object):
         self.use_graph = use_graph
         self.dt = dt
         self.temp0 = temp0
+        self.batch_steps = batch_steps
         self.streams = [torch.cuda.Stream() for _ in range(self.nslots)]
         self._lock = threading.Condition()
         self._inflight = 0
@@ -239,8 +264,11 @@ class ServingEngine(object):
     # one request, on one slot's stream
     def _serve(self, req, slot):
         req.t_start = time.perf_counter()
-        serve_request(req, self.streams[slot].cuda_stream, self.precision, self.dt, self.temp0, self.use_graph)
         req.slot = slot
+        if req.cancelled:
+            raise Cancelled()
+        serve_request(req, self.streams[slot].cuda_stream, self.precision, self.dt, self.temp0, self.use_graph,
+                      self.batch_steps)
 
     def _worker(self, slot, inbox, done):
         while True:
@@ -249,6 +277,8 @@ class ServingEngine(object):
                 return
             try:
                 self._serve(req, slot)
+            except Cancelled:
+                req.error = 'cancelled'
             except Exception as exc:  # reported per request, the server keeps going
                 req.error = repr(exc)
             req.t_done = time.perf_counter()
@@ -262,11 +292,11 @@ class ServingEngine(object):
         """Serves `requests` (sorted by arrival); with realtime, a request is
         not admitted before its arrival time (offsets from the start of the
         run, written back as absolute perf_counter times).  Returns wall
-        seconds."""
+        seconds.  A request whose footprint estimate exceeds the whole budget
+        is rejected (its error says so) and the others are served; a request
+        cancelled before admission is not started."""
         for r in requests:
             r.estimate = estimate_bytes(r.spec, self.precision, r.nsteps)
-            if r.estimate > self.budget:
-                raise ValueError('request %d needs %d bytes, more than the whole budget' % (r.rid, r.estimate))
         inboxes = [queue.Queue() for _ in range(self.nslots)]
         done = queue.Queue()
         free = list(range(self.nslots))
@@ -283,6 +313,14 @@ class ServingEngine(object):
                     wait = r.arrival - time.perf_counter()
                     if wait > 0:
                         time.sleep(wait)
+                if r.estimate > self.budget:
+                    r.error = 'rejected: needs %d bytes, more than the whole budget of %d' % (r.estimate, self.budget)
+                    r.t_done = time.perf_counter()
+                    continue
+                if r.cancelled:
+                    r.error = 'cancelled'
+                    r.t_done = time.perf_counter()
+                    continue
                 # a free slot and room in the budget (arrival order: no overtaking)
                 while True:
                     while not done.empty():

@@ -9,7 +9,7 @@ charges, radii, masses and the bond graph with its 1-2 .. 1-4 neighbour sets.
 """
 import numpy as np
 
-__all__ = ['Cell', 'System']
+__all__ = ['Cell', 'System', 'SystemView', 'as_system']
 
 
 class Cell(object):
@@ -140,3 +140,109 @@ class System(object):
                             and i4 not in self.neighs3[i0]):
                         self.neighs4[i0].add(i4)
                         self.neighs4[i4].add(i0)
+
+
+class _ViewCell(Cell):
+    """The cell of a SystemView: follows the other program's cell object,
+    and passes cell changes made through this package on to it."""
+
+    def __init__(self, other):
+        self._other = other
+        self._src = np.array(other.rvecs, dtype=np.float64)
+        Cell.update_rvecs(self, self._src)
+
+    def refresh(self):
+        rv = np.asarray(self._other.rvecs, dtype=np.float64)
+        if rv.shape != self._src.shape or not np.array_equal(rv, self._src):
+            self._src = rv.copy()
+            Cell.update_rvecs(self, self._src)
+
+    def update_rvecs(self, rvecs):
+        if hasattr(self, '_other') and hasattr(self._other, 'update_rvecs'):
+            self._other.update_rvecs(rvecs)
+        self._src = np.array(rvecs, dtype=np.float64)
+        Cell.update_rvecs(self, self._src)
+
+
+class SystemView(System):
+    """This package's view of another program's System object -- for
+    instance the reference's own yaff.system.System (yaff/system.py:50-235)
+    -- so that the device parts and neighbour list can be built on it.
+
+    What the force evaluation reads is taken from the other object when it
+    is read: the positions (``pos`` is the other object's array; setting it
+    sets theirs, so the device path's page-locked position buffer becomes the
+    array the other program's ForceField.update_pos writes into), the cell
+    (re-derived whenever the other cell's rvecs change, with the same SVD
+    completion as the reference Cell), charges, radii and masses.  Bonds and
+    the 1-2 .. 1-4 neighbour sets are taken once (they are fixed for a
+    System, as in the reference)."""
+
+    def __init__(self, other):
+        self._other = other
+        natom = getattr(other, 'natom', None)
+        self.natom = int(natom) if natom is not None else len(other.pos)
+        numbers = getattr(other, 'numbers', None)
+        self.numbers = np.zeros(self.natom, int) if numbers is None else np.asarray(numbers)
+        self._cell = None
+        self.ffatypes = getattr(other, 'ffatypes', None)
+        bonds = getattr(other, 'bonds', None)
+        self.bonds = None if bonds is None else np.asarray(bonds, dtype=np.int64).reshape(-1, 2)
+        self._device = None
+        if self.bonds is not None:
+            if all(hasattr(other, 'neighs%d' % k) for k in (1, 2, 3)):
+                self.neighs1, self.neighs2, self.neighs3 = other.neighs1, other.neighs2, other.neighs3
+                self.neighs4 = getattr(other, 'neighs4', None)
+                if self.neighs4 is None:
+                    self._init_derived_bonds()
+            else:
+                self._init_derived_bonds()
+
+    @property
+    def pos(self):
+        return self._other.pos
+
+    @pos.setter
+    def pos(self, value):
+        self._other.pos = value
+
+    @property
+    def cell(self):
+        if self._cell is None:
+            other_cell = getattr(self._other, 'cell', None)
+            self._cell = _ViewCell(other_cell) if other_cell is not None else Cell(None)
+        if isinstance(self._cell, _ViewCell):
+            self._cell.refresh()
+        return self._cell
+
+    @property
+    def charges(self):
+        q = getattr(self._other, 'charges', None)
+        return None if q is None else np.asarray(q, dtype=np.float64)
+
+    @property
+    def radii(self):
+        r = getattr(self._other, 'radii', None)
+        return None if r is None else np.asarray(r, dtype=np.float64)
+
+    @property
+    def masses(self):
+        m = getattr(self._other, 'masses', None)
+        return None if m is None else np.asarray(m, dtype=np.float64)
+
+
+def as_system(system):
+    """`system` when it is this package's System, else the (cached)
+    SystemView of the other program's System object: every part, neighbour
+    list and scaling table built on the same object shares one view and so
+    one device context."""
+    if isinstance(system, System):
+        return system
+    view = getattr(system, '_yaff_gb300_view', None)
+    if view is None:
+        view = SystemView(system)
+        try:
+            system._yaff_gb300_view = view
+        except AttributeError:
+            raise TypeError('cannot attach a device view to %r; pass a yaff_gb300.System' % type(system).__name__)
+    return view

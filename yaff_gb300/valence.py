@@ -9,6 +9,7 @@ supported, with the same constructor arguments, the same relative vectors
 per coordinate and the same parameter slots.
 """
 import numpy as np
+from .system import as_system
 
 __all__ = ['DeltaList', 'InternalCoordinateList', 'ValenceList', 'InternalCoordinate', 'Bond', 'BendCos',
            'BendAngle', 'DihedCos', 'DihedAngle', 'UreyBradley', 'OopCos', 'OopMeanCos', 'OopAngle',
@@ -21,6 +22,7 @@ __all__ = ['DeltaList', 'InternalCoordinateList', 'ValenceList', 'InternalCoordi
 
 class DeltaList(object):
     def __init__(self, system):
+        system = as_system(system)
         self.system = system
         self.pairs = []
         self.lookup = {}

@@ -122,14 +122,23 @@ class ConsErrTracker(object):
 
 
 class VerletHook(object):
-    """A hook that acts inside the Verlet step (thermostats): ``init`` at
-    initialization, ``pre`` before the first half kick, ``post`` after the
-    second; ``econs_correction`` is added to the conserved energy
-    (yaff/sampling/verlet.py:418-446)."""
+    """A hook that acts inside the Verlet step (thermostats, barostats):
+    ``init`` at initialization, ``pre`` before the first half kick, ``post``
+    after the second, on the steps ``expects_call`` selects;
+    ``econs_correction`` is added to the conserved energy
+    (yaff/sampling/verlet.py:418-446).  ``method`` is 'thermostat' or
+    'barostat' (a VerletIntegrator given one of each combines them as
+    TBCombination does)."""
     device_kind = None
+    method = None
 
     def __init__(self, start=0, step=1):
+        self.start = start
+        self.step = step
         self.econs_correction = 0.0
+
+    def expects_call(self, counter):
+        return counter >= self.start and (counter - self.start) % self.step == 0
 
     def __call__(self, iterative):
         pass
@@ -152,6 +161,7 @@ def _normal(rng, *shape):
 
 class BerendsenThermostat(VerletHook):
     """Weak-coupling velocity rescaling (yaff/sampling/nvt.py:110-159)."""
+    method = 'thermostat'
     device_kind = 1
 
     def __init__(self, temp, start=0, timecon=100 * femtosecond, restart=False):
@@ -182,6 +192,7 @@ class LangevinThermostat(VerletHook):
     """Ornstein-Uhlenbeck velocity update for half a step before and after
     each Verlet step (Bussi and Parrinello, Phys. Rev. E 75, 056707 (2007);
     yaff/sampling/nvt.py:162-213)."""
+    method = 'thermostat'
     device_kind = 2
 
     def __init__(self, temp, start=0, timecon=100 * femtosecond, rng=None):
@@ -214,6 +225,7 @@ class CSVRThermostat(VerletHook):
     """Canonical sampling through velocity rescaling (Bussi, Donadio and
     Parrinello, J. Chem. Phys. 126, 014101 (2007); yaff/sampling/nvt.py:
     215-268)."""
+    method = 'thermostat'
     device_kind = 3
 
     def __init__(self, temp, start=0, timecon=100 * femtosecond, rng=None):
@@ -308,6 +320,7 @@ class NHChain(object):
 class NHCThermostat(VerletHook):
     """Nose-Hoover chain thermostat (Martyna, Klein and Tuckerman, J. Chem.
     Phys. 97, 2635 (1992); yaff/sampling/nvt.py:430-498)."""
+    method = 'thermostat'
     device_kind = 4
 
     def __init__(self, temp, start=0, timecon=100 * femtosecond, chainlength=3, chain_pos0=None, chain_vel0=None,
@@ -343,6 +356,7 @@ class BerendsenBarostat(VerletHook):
     (Berendsen et al., J. Chem. Phys. 81, 3684 (1984); yaff/sampling/npt.py:
     232-330).  A host hook: each step makes one extra force evaluation at the
     rescaled cell, through ForceField.update_rvecs."""
+    method = 'barostat'
 
     def __init__(self, ff, temp, press, start=0, step=1, timecon=1000 * femtosecond, beta=None,
                  anisotropic=True, vol_constraint=False, restart=False):
@@ -399,6 +413,319 @@ class BerendsenBarostat(VerletHook):
         self.econs_correction += epot0 - iterative.epot
 
 
+def get_random_vel_press(mass, temp, rng=None):
+    """Symmetric 3x3 barostat velocity drawn from the Maxwell-Boltzmann
+    distribution of a cell mass `mass` at `temp` (off-diagonal entries
+    divided by sqrt(2): p_ab = p_ba is one degree of freedom)
+    (yaff/sampling/utils.py:378-403)."""
+    rand = (np.random if rng is None else rng).normal(0, np.sqrt(mass * boltzmann * temp), (3, 3)) / mass
+    vel_press = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            vel_press[i, j] = rand[i, j] if i >= j else rand[j, i]
+            if i != j:
+                vel_press[i, j] /= np.sqrt(2)
+    return vel_press
+
+
+def _cell_propagate(iterative, vel_press, timestep, anisotropic, vol_constraint):
+    """The barostat's position, cell and velocity propagation around the
+    forces at the new cell: iL v_g h/2 on positions and cell vectors, a new
+    force evaluation, then -iL (v_g + Tr(v_g)/ndof) h/2 on the velocities
+    (yaff/sampling/npt.py:435-478, :642-688; Martyna, Tuckerman, Tobias and
+    Klein, Mol. Phys. 87, 1117 (1996))."""
+    if anisotropic:
+        dr, qg = np.linalg.eigh(vel_press)
+        rot = np.dot(np.dot(qg, np.diagflat(np.exp(dr * timestep / 2))), qg.T)
+        pos_new = np.dot(iterative.pos, rot)
+        rvecs_new = np.dot(iterative.rvecs, rot)
+    else:
+        c = np.exp(vel_press * timestep / 2)
+        pos_new = c * iterative.pos
+        rvecs_new = c * iterative.rvecs
+    iterative.ff.update_pos(pos_new)
+    iterative.pos[:] = pos_new
+    iterative.ff.update_rvecs(rvecs_new)
+    iterative.rvecs[:] = rvecs_new
+    iterative.gpos[:] = 0.0
+    iterative.vtens[:] = 0.0
+    iterative.epot = iterative.ff.compute(iterative.gpos, iterative.vtens)
+    if anisotropic:
+        if vol_constraint:
+            dg, eg = np.linalg.eigh(vel_press)
+        else:
+            dg, eg = np.linalg.eigh(vel_press + (np.trace(vel_press) / iterative.ndof) * np.eye(3))
+        rot = np.dot(np.dot(eg, np.diagflat(np.exp(-dg * timestep / 2))), eg.T)
+        vel_new = np.dot(iterative.vel, rot)
+    else:
+        vel_new = np.exp(-((1.0 + 3.0 / iterative.ndof) * vel_press) * timestep / 2) * iterative.vel
+    iterative.vel[:] = vel_new
+    iterative.ekin = iterative._compute_ekin()
+
+
+def _press_force(iterative, press, mass_press):
+    """G = (P_int V + (2 Ekin/ndof - P V) 1) / W, with P_int V the symmetrized
+    kinetic minus virial tensor."""
+    ptens_vol = np.dot(iterative.vel.T * iterative.masses, iterative.vel) - iterative.vtens
+    ptens_vol = 0.5 * (ptens_vol.T + ptens_vol)
+    vol = iterative.ff.system.cell.volume
+    return (ptens_vol + (2.0 * iterative.ekin / iterative.ndof - press * vol) * np.eye(3)) / mass_press
+
+
+class LangevinBarostat(VerletHook):
+    """Langevin piston barostat (Feller, Zhang, Pastor and Brooks, J. Chem.
+    Phys. 103, 4613 (1995); yaff/sampling/npt.py:333-512): the cell velocity
+    tensor feels the pressure difference, a friction 1/timecon and random
+    forces; positions, cell and velocities follow it as in the MTK
+    propagator.  Host hook; random numbers from `rng` (None: NumPy's global
+    generator, in the reference's call order)."""
+    method = 'barostat'
+
+    def __init__(self, ff, temp, press, start=0, step=1, timecon=1000 * femtosecond, anisotropic=True,
+                 vol_constraint=False, rng=None):
+        self.temp = temp
+        self.press = press
+        self.timecon = timecon
+        self.anisotropic = anisotropic
+        self.vol_constraint = vol_constraint
+        self.rng = rng
+        self.dim = ff.system.cell.nvec
+        self.baro_ndof = get_ndof_baro(self.dim, self.anisotropic, self.vol_constraint)
+        if self.anisotropic:
+            cell_symmetrize(ff)
+        self.cell = ff.system.cell.rvecs.copy()
+        VerletHook.__init__(self, start, step)
+
+    def init(self, iterative):
+        self.timestep_press = iterative.timestep
+        clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        if iterative.ndof is None:
+            iterative.ndof = iterative.pos.size
+        self.mass_press = (iterative.ndof + 3) / 3 * boltzmann * self.temp * (self.timecon / (2 * np.pi)) ** 2
+        self.vel_press = get_random_vel_press(self.mass_press, self.temp, self.rng)
+        if self.vol_constraint:
+            self.vel_press -= np.trace(self.vel_press) / 3 * np.eye(3)
+        if not self.anisotropic:
+            self.vel_press = self.vel_press[0][0]
+        iterative.gpos[:] = 0.0
+        iterative.vtens[:] = 0.0
+        iterative.epot = iterative.ff.compute(iterative.gpos, iterative.vtens)
+
+    def pre(self, iterative, chainvel0=None):
+        epot0, ekin0 = iterative.epot, iterative.ekin
+        self.baro(iterative, chainvel0)
+        self.econs_correction += epot0 - iterative.epot + ekin0 - iterative.ekin
+
+    def post(self, iterative, chainvel0=None):
+        epot0, ekin0 = iterative.epot, iterative.ekin
+        self.baro(iterative, chainvel0)
+        self.econs_correction += epot0 - iterative.epot + ekin0 - iterative.ekin
+
+    def baro(self, iterative, chainvel0):
+        def update_baro_vel():
+            self.vel_press *= np.exp(-self.timestep_press / (8 * self.timecon))
+            if chainvel0 is not None:
+                self.vel_press *= np.exp(-self.timestep_press * chainvel0 / 8)
+            g = _press_force(iterative, self.press, self.mass_press)
+            r = self.getR()
+            if self.vol_constraint:
+                g -= np.trace(g) / self.dim * np.eye(self.dim)
+                r -= np.trace(r) / self.dim * np.eye(self.dim)
+            if not self.anisotropic:
+                g = np.trace(g)
+                r = r[0][0]
+            self.vel_press += (g - r / self.mass_press) * self.timestep_press / 4
+            self.vel_press *= np.exp(-self.timestep_press / (8 * self.timecon))
+            if chainvel0 is not None:
+                self.vel_press *= np.exp(-self.timestep_press * chainvel0 / 8)
+
+        update_baro_vel()
+        _cell_propagate(iterative, self.vel_press, self.timestep_press, self.anisotropic, self.vol_constraint)
+        update_baro_vel()
+
+    def getR(self):
+        """Symmetric random force tensor of the piston."""
+        rand = (np.random if self.rng is None else self.rng).normal(0, 1, (3, 3)) * \
+            np.sqrt(2 * self.mass_press * boltzmann * self.temp / (self.timestep_press * self.timecon))
+        r = np.zeros((3, 3))
+        for i in range(3):
+            for j in range(3):
+                r[i, j] = rand[i, j] if i >= j else rand[j, i]
+        return r
+
+
+class MTKBarostat(VerletHook):
+    """Martyna-Tobias-Klein barostat (J. Chem. Phys. 101, 4177 (1994)) with
+    the symplectic propagator of Martyna, Tuckerman, Tobias and Klein (Mol.
+    Phys. 87, 1117 (1996)); yaff/sampling/npt.py:514-729.  Deterministic;
+    `baro_thermo` (an NHCThermostat) thermostats the cell velocity itself.
+    Host hook."""
+    method = 'barostat'
+
+    def __init__(self, ff, temp, press, start=0, step=1, timecon=1000 * femtosecond, anisotropic=True,
+                 vol_constraint=False, baro_thermo=None, vel_press0=None, restart=False, rng=None):
+        self.temp = temp
+        self.press = press
+        self.timecon_press = timecon
+        self.anisotropic = anisotropic
+        self.vol_constraint = vol_constraint
+        self.baro_thermo = baro_thermo
+        self.rng = rng
+        self.dim = ff.system.cell.nvec
+        self.restart = restart
+        self.baro_ndof = get_ndof_baro(self.dim, self.anisotropic, self.vol_constraint)
+        if self.anisotropic and not self.restart:
+            cell_symmetrize(ff)
+        self.cell = ff.system.cell.rvecs.copy()
+        self.vel_press = vel_press0
+        VerletHook.__init__(self, start, step)
+
+    def init(self, iterative):
+        self.timestep_press = iterative.timestep
+        if not self.restart:
+            clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.ff.system.cell)
+        if iterative.ndof is None:
+            iterative.ndof = get_ndof_internal_md(len(iterative.pos), iterative.ff.system.cell.nvec)
+        angfreq = 2 * np.pi / self.timecon_press
+        self.mass_press = (iterative.ndof + self.dim ** 2) * boltzmann * self.temp / angfreq ** 2
+        if self.vel_press is None:
+            self.vel_press = get_random_vel_press(self.mass_press, self.temp, self.rng)
+            if not self.anisotropic:
+                self.vel_press = self.vel_press[0][0]
+        if self.baro_thermo is not None:
+            self.baro_thermo.chain.timestep = iterative.timestep
+            self.baro_thermo.chain.set_ndof(self.baro_ndof)
+        if self.vol_constraint:
+            self.vel_press -= np.trace(self.vel_press) / 3 * np.eye(3)
+        iterative.gpos[:] = 0.0
+        iterative.vtens[:] = 0.0
+        iterative.epot = iterative.ff.compute(iterative.gpos, iterative.vtens)
+
+    def _thermostat_cell(self):
+        # the cell thermostat sees the cell kinetic energy; v_g itself is
+        # updated in baro()
+        vel_copy = np.zeros(np.shape(self.vel_press))
+        vel_copy[...] = self.vel_press
+        self.baro_thermo.chain(self._compute_ekin_baro(), vel_copy, 0)
+
+    def pre(self, iterative, chainvel0=None):
+        if self.baro_thermo is not None:
+            chainvel0 = self.baro_thermo.chain.vel[0]
+        self.baro(iterative, chainvel0)
+        if self.baro_thermo is not None:
+            self._thermostat_cell()
+
+    def post(self, iterative, chainvel0=None):
+        if self.baro_thermo is not None:
+            self._thermostat_cell()
+            chainvel0 = self.baro_thermo.chain.vel[0]
+        self.baro(iterative, chainvel0)
+        self.econs_correction = self._compute_ekin_baro()
+        if not self.vol_constraint:
+            self.econs_correction += self.press * iterative.ff.system.cell.volume
+        if self.baro_thermo is not None:
+            self.econs_correction += self.baro_thermo.chain.get_econs_correction()
+
+    def baro(self, iterative, chainvel0):
+        def update_baro_vel():
+            if chainvel0 is not None:
+                self.vel_press *= np.exp(-self.timestep_press * chainvel0 / 8)
+            g = _press_force(iterative, self.press, self.mass_press)
+            if not self.anisotropic:
+                g = np.trace(g)
+            if self.vol_constraint:
+                g -= np.trace(g) / self.dim * np.eye(self.dim)
+            self.vel_press += g * self.timestep_press / 4
+            if chainvel0 is not None:
+                self.vel_press *= np.exp(-self.timestep_press * chainvel0 / 8)
+
+        update_baro_vel()
+        _cell_propagate(iterative, self.vel_press, self.timestep_press, self.anisotropic, self.vol_constraint)
+        update_baro_vel()
+
+    def add_press_cont(self):
+        """The cell's contribution to the first chain bead's force of a
+        particle Nose-Hoover chain (zero when the cell has its own chain)."""
+        if self.baro_thermo is None:
+            return 2 * self._compute_ekin_baro() - self.baro_ndof * self.temp * boltzmann
+        return 0
+
+    def _compute_ekin_baro(self):
+        if self.anisotropic:
+            return 0.5 * self.mass_press * np.trace(np.dot(self.vel_press.T, self.vel_press))
+        return 0.5 * self.mass_press * self.vel_press ** 2
+
+
+class TBCombination(VerletHook):
+    """A thermostat and a barostat called in the reference's succession with
+    their coupling (yaff/sampling/npt.py:45-157): the barostat first in
+    ``pre`` and last in ``post``; with a Nose-Hoover chain the first bead's
+    velocity scales the cell velocity; with an MTK barostat the cell's
+    kinetic energy enters the chain's first bead."""
+
+    def __init__(self, thermostat, barostat, start=0):
+        if thermostat.method != 'thermostat':
+            thermostat, barostat = barostat, thermostat
+        if thermostat.method != 'thermostat' or barostat.method != 'barostat':
+            raise TypeError('TBCombination needs one thermostat and one barostat')
+        self.thermostat = thermostat
+        self.barostat = barostat
+        self.step_thermo = thermostat.step
+        self.step_baro = barostat.step
+        VerletHook.__init__(self, start, min(self.step_thermo, self.step_baro))
+
+    def init(self, iterative):
+        set_ndof = iterative.ndof is not None
+        self.thermostat.init(iterative)
+        self.barostat.init(iterative)
+        p_cm_fluct = isinstance(self.thermostat, LangevinThermostat) or isinstance(self.barostat, LangevinBarostat)
+        if (not set_ndof) and p_cm_fluct:
+            iterative.ndof = iterative.pos.size
+        self.chainvel0 = None
+        self.G1_add = None
+
+    def pre(self, iterative, G1_add=None):
+        if self._expects(iterative, self.step_baro):
+            if isinstance(self.thermostat, NHCThermostat):
+                self.chainvel0 = self.thermostat.chain.vel[0]
+            self.barostat.pre(iterative, self.chainvel0)
+        if self._expects(iterative, self.step_thermo):
+            if isinstance(self.barostat, MTKBarostat):
+                self.G1_add = self.barostat.add_press_cont()
+            self.thermostat.pre(iterative, self.G1_add)
+
+    def post(self, iterative, G1_add=None):
+        if self._expects(iterative, self.step_thermo):
+            if isinstance(self.barostat, MTKBarostat):
+                self.G1_add = self.barostat.add_press_cont()
+            self.thermostat.post(iterative, self.G1_add)
+        if self._expects(iterative, self.step_baro):
+            if isinstance(self.thermostat, NHCThermostat):
+                self.chainvel0 = self.thermostat.chain.vel[0]
+            self.barostat.post(iterative, self.chainvel0)
+        self.econs_correction = self.thermostat.econs_correction + self.barostat.econs_correction
+        if isinstance(self.thermostat, NHCThermostat) and not (
+                isinstance(self.barostat, MTKBarostat) and self.barostat.baro_thermo is not None):
+            # the particle chain also thermostats the cell
+            self.econs_correction += self.barostat.baro_ndof * boltzmann * self.thermostat.temp * \
+                self.thermostat.chain.pos[0]
+
+    def _expects(self, iterative, step):
+        return iterative.counter >= self.start and (iterative.counter - self.start) % step == 0
+
+
+def _combine_hooks(hooks):
+    """A thermostat and a barostat given as separate hooks are replaced by
+    their TBCombination (appended last), as the reference's integrator does
+    (yaff/sampling/verlet.py:205-233)."""
+    thermo = [h for h in hooks if getattr(h, 'method', None) == 'thermostat']
+    baro = [h for h in hooks if getattr(h, 'method', None) == 'barostat']
+    if thermo and baro:
+        hooks = [h for h in hooks if h is not thermo[0] and h is not baro[0]]
+        hooks.append(TBCombination(thermo[0], baro[0]))
+    return hooks
+
+
 class VerletIntegrator(object):
     """Velocity Verlet with the reference's hook protocol.
 
@@ -410,8 +737,27 @@ class VerletIntegrator(object):
     set by a thermostat's init, else 3 N).
     """
 
-    def __init__(self, ff, timestep, vel0=None, temp0=300.0, scalevel0=True, hooks=None, rng=None, ndof=None):
+    def __init__(self, ff, timestep=None, vel0=None, temp0=300.0, scalevel0=True, hooks=None, rng=None, ndof=None,
+                 restart=None):
         self.ff = ff
+        state = None
+        if restart is not None:
+            # continue from a RestartWriter state (the reference's restart_h5,
+            # yaff/sampling/verlet.py:113-142): positions and cell always,
+            # velocities and time step unless given
+            from .io import read_restart
+            state = read_restart(restart) if isinstance(restart, str) else restart
+            cell = getattr(ff.system, 'cell', None)
+            rv = np.asarray(state['rvecs'])
+            if cell is not None and rv.size and not np.array_equal(rv, cell.rvecs):
+                ff.update_rvecs(rv)
+            ff.system.pos[:] = state['pos']
+            if vel0 is None:
+                vel0 = state['vel']
+            if timestep is None:
+                timestep = float(state['timestep'])
+        if timestep is None:
+            raise AssertionError('No Verlet timestep is found')
         self.timestep = timestep
         system = ff.system
         self.pos = system.pos.copy()
@@ -425,16 +771,48 @@ class VerletIntegrator(object):
         self.vtens = np.zeros((3, 3))
         if hooks is not None and not isinstance(hooks, (list, tuple)):
             hooks = [hooks]
-        self.hooks = list(hooks or [])
+        self.hooks = _combine_hooks(list(hooks or []))
         self.ndof = ndof
         self.time = 0.0
         self.counter = 0
         self.cons_err = ConsErrTracker()
+        if state is not None:
+            for hook in self.hooks:
+                if isinstance(hook, VerletHook) and hasattr(hook, 'restart'):
+                    hook.restart = True   # no momentum cleaning on a restart
         self.initialize()
+        if state is not None:
+            self._restore(state)
+
+    def _restore(self, state):
+        """Counter, time, thermostat states and the conserved-energy tracker
+        of a restart record (after initialize, which recomputed the forces
+        at the restored positions)."""
+        self.counter = int(state['counter'])
+        self.time = float(state['time'])
+        vhooks = [h for h in self.hooks if isinstance(h, VerletHook)]
+        corr = np.asarray(state.get('hook_econs_correction', np.zeros(0)))
+        for k, hook in enumerate(vhooks):
+            if k < len(corr):
+                hook.econs_correction = float(corr[k])
+            chain = getattr(hook, 'chain', None)
+            if chain is not None and ('hook%d_chain_pos' % k) in state:
+                chain.pos[:] = state['hook%d_chain_pos' % k]
+                chain.vel[:] = state['hook%d_chain_vel' % k]
+                hook.econs_correction = chain.get_econs_correction()
+        if 'cons_err' in state:
+            c = state['cons_err']
+            self.cons_err.counter = int(c[0])
+            self.cons_err.ekin_m, self.cons_err.ekin_s, self.cons_err.econs_m, self.cons_err.econs_s = (
+                float(c[1]), float(c[2]), float(c[3]), float(c[4]))
+        self.ekin = self._compute_ekin()
+        self.temp = self.ekin / self.ndof * 2.0 / boltzmann
+        self.etot = self.ekin + self.epot
+        self.econs = self.etot + self.econs_correction
 
     def _verlet_hooks(self, kind):
         for hook in self.hooks:
-            if isinstance(hook, VerletHook):
+            if isinstance(hook, VerletHook) and (kind == 'init' or hook.expects_call(self.counter)):
                 getattr(hook, kind)(self)
 
     def _compute_ekin(self):
@@ -512,15 +890,46 @@ class DeviceVerlet(object):
     energy log holds (epot, ekin) of step 0 and of every step run since.
     """
 
-    def __init__(self, ff, timestep, vel0=None, temp0=300.0, scalevel0=True, rng=None, max_steps=1000,
-                 use_graph=True, thermostat=None, seed=0, ndof=None):
+    def __init__(self, ff, timestep=None, vel0=None, temp0=300.0, scalevel0=True, rng=None, max_steps=1000,
+                 use_graph=True, thermostat=None, seed=0, ndof=None, restart=None):
         from . import _lib
         from ._lib import check, ptr
         self._lib, self._check, self._ptr = _lib, check, ptr
         self.ff = ff
+        system = ff.system
+        # continue from a restart record (RestartWriter / save_restart):
+        # positions, cell, velocities, counter, time step, thermostat state
+        self.counter0 = 0
+        self.econs_offset = 0.0
+        if restart is not None:
+            from .io import read_restart
+            state = read_restart(restart) if isinstance(restart, str) else restart
+            rv = np.asarray(state['rvecs'])
+            if rv.size and not np.array_equal(rv, system.cell.rvecs):
+                ff.update_rvecs(rv)
+            system.pos[:] = state['pos']
+            if vel0 is None:
+                vel0 = state['vel']
+            if timestep is None:
+                timestep = float(state['timestep'])
+            self.counter0 = int(state['counter'])
+            if thermostat is not None:
+                thermostat.restart = True
+                corr = np.asarray(state.get('hook_econs_correction', np.zeros(0)))
+                if getattr(thermostat, 'device_kind', None) == 4 and 'hook0_chain_pos' in state:
+                    thermostat.chain.pos[:] = state['hook0_chain_pos']
+                    thermostat.chain.vel[:] = state['hook0_chain_vel']
+                    thermostat.chain.restart_pos = thermostat.chain.restart_vel = True
+                elif len(corr):
+                    # the accumulated correction of the weak-coupling and
+                    # stochastic thermostats continues from the saved value
+                    self.econs_offset = float(corr[0])
+                # a fresh noise stream for the continued run
+                seed = (int(seed) * 0x9E3779B1 + self.counter0) & 0xFFFFFFFFFFFF
+        if timestep is None:
+            raise AssertionError('No Verlet timestep is found')
         self.timestep = float(timestep)
         self.use_graph = bool(use_graph)
-        system = ff.system
         self.natom = system.natom
         self.masses = np.ascontiguousarray(system.masses, dtype=np.float64)
         if vel0 is None:
@@ -593,6 +1002,29 @@ class DeviceVerlet(object):
         self._check(self.dev.lib.yg_md_get(self.dev.ctx, self._ptr(p), self._ptr(v), self._ptr(log),
                                            ctypes.byref(n)), 'yg_md_get')
         return p, v, log[:n.value]
+
+    def save_restart(self, fn):
+        """Writes the run's current state as a restart record (the layout of
+        io.RestartWriter): counter (continuing a restarted run's count),
+        time, positions, velocities, cell, conserved energy and the
+        thermostat's state."""
+        from .io import restart_state, _write_npz
+        pos, vel, log = self.fetch()
+        hooks = []
+        corr = 0.0
+        if self.thermostat is not None:
+            corr, cp, cv = self.thermo_state()
+            if getattr(self.thermostat, 'device_kind', None) == 4:
+                self.thermostat.chain.pos[:] = cp
+                self.thermostat.chain.vel[:] = cv
+            corr += self.econs_offset
+            self.thermostat.econs_correction = corr
+            hooks = [self.thermostat]
+        counter = self.counter0 + self.counter
+        econs = float(log[-1, 0] + log[-1, 1] + corr)
+        cell = self.ff.system.cell
+        _write_npz(fn, restart_state(counter, counter * self.timestep, self.timestep, pos, vel, cell.rvecs, econs,
+                                     None, hooks))
 
     def sync_host(self):
         """Copies the device positions back into the system; the next host
