@@ -745,34 +745,69 @@ def run_reference(args, world, rank, budget_s=150.0):
 
 def run_serving(args):
     """The serving workload: independent LJ + EI + Ewald systems (natom
-    log-uniform in [64, 4000], 0.064 atoms/A^3, rcut 10 A), seeded Poisson
-    arrivals, each request 50 resident MD steps of 0.5 fs in mixed precision;
-    against the plain FP64 per-system use (ForceField + host Verlet, one
-    request at a time) on a sample of the same requests."""
+    log-uniform in [64, 4000], 0.064 atoms/A^3, rcut 10 A, skin 1 A),
+    seeded Poisson arrivals, each request 50 MD steps of 0.5 fs in mixed
+    precision, served by the fleet engine (every system in flight stepped
+    by one launch per MD phase, continuous admission by free capacity):
+    the stated rate, then an arrival-rate sweep up to saturation (all
+    requests at t = 0), each with throughput and p50 / p99 latency.  Beside
+    it: the per-system-context engine at the stated rate, and the plain FP64
+    per-system use (ForceField + host Verlet, one request at a time) on a
+    sample of the same requests."""
+    from yaff_gb300.fleet import FleetEngine, fleet_bytes
     from yaff_gb300.serve import make_workload, ServingEngine, run_sequential, summarize
     n = args.serving_requests
-    warm = make_workload(nreq=2 * args.serving_slots, rate=0.0, seed=7)
+    caps = dict(max_atoms=1 << 19, max_systems=512, max_k=1 << 21, max_steps=64)
+    eng = FleetEngine(chunk=5, **caps)
+    eng.run(make_workload(nreq=64, rate=0.0, seed=7), realtime=False)   # warm-up: capture, first builds
+    out = {'workload': '%d requests, natom log-uniform [64, 4000], 0.064/A^3, rcut 10 A, skin 1 A, LJ+EI+Ewald, '
+                       '50 MD steps of 0.5 fs each, mixed precision, seeded Poisson arrivals' % n,
+           'engine': 'fleet: all systems in flight stepped together, 8 launches per MD step (CUDA graph), '
+                     'admission every 5 steps by free slots / atom and k ranges',
+           'fleet_capacity': dict(caps, bytes=fleet_bytes(caps['max_atoms'], caps['max_systems'], caps['max_k'],
+                                                          max_steps=caps['max_steps']))}
+    sweep = []
+    for rate in (args.serving_rate, 1000.0, 4000.0, 16000.0, 0.0):
+        reqs = make_workload(nreq=n, rate=rate, seed=2024)
+        eng.peak_inflight = 0
+        launches0, steps0 = eng.fleet.launch_count(), eng.steps_run
+        wall = eng.run(reqs, realtime=rate > 0)
+        row = summarize(reqs, wall)
+        row.update({'arrival_rate_per_s': rate if rate > 0 else 'all at t=0 (saturation)',
+                    'peak_inflight': eng.peak_inflight,
+                    'launches_per_step': (eng.fleet.launch_count() - launches0) / max(1, eng.steps_run - steps0)})
+        sweep.append(row)
+    out['rate_sweep'] = sweep
+    head = sweep[0]
+    for k in ('requests', 'errors', 'wall_s', 'requests_per_s', 'atom_steps_per_s', 'latency_p50_ms',
+              'latency_p99_ms', 'arrival_rate_per_s'):
+        out[k] = head[k]
+    out['saturated_requests_per_s'] = sweep[-1]['requests_per_s']
+    out['saturated_latency_p99_ms'] = sweep[-1]['latency_p99_ms']
+    out['saturated_atom_steps_per_s'] = sweep[-1]['atom_steps_per_s']
+    eng.close()
+    # the per-system-context engine (one yg_ctx, stream and graph per request)
+    nc = min(n, 1024)
     budget = 16 << 30
-    ServingEngine(nslots=args.serving_slots, budget_bytes=budget).run(warm, realtime=False)
-    reqs = make_workload(nreq=n, rate=args.serving_rate, seed=2024)
-    eng = ServingEngine(nslots=args.serving_slots, budget_bytes=budget)
-    wall = eng.run(reqs, realtime=True)
-    s = summarize(reqs, wall)
+    ServingEngine(nslots=args.serving_slots, budget_bytes=budget).run(make_workload(nreq=32, rate=0.0, seed=7),
+                                                                     realtime=False)
+    creq = make_workload(nreq=nc, rate=0.0, seed=2024)
+    ceng = ServingEngine(nslots=args.serving_slots, budget_bytes=budget)
+    cw = ceng.run(creq, realtime=False)
+    cs = summarize(creq, cw)
+    out['per_context_engine_saturated'] = {
+        'requests': nc, 'slots': args.serving_slots, 'requests_per_s': cs['requests_per_s'],
+        'atom_steps_per_s': cs['atom_steps_per_s'], 'latency_p99_ms': cs['latency_p99_ms'],
+        'how': 'one context, stream and captured ~45-kernel step per request, all requests at t = 0'}
     nseq = min(48, n)
     seq = make_workload(nreq=n, rate=0.0, seed=2024)[:nseq]
     wseq = run_sequential(seq, precision='fp64', mode='api')
     sq = summarize(seq, wseq)
-    s.update({'arrival_rate_per_s': args.serving_rate, 'slots': args.serving_slots, 'budget_bytes': budget,
-              'peak_inflight': eng.peak_inflight, 'peak_inflight_bytes': eng.peak_inflight_bytes,
-              'max_bytes_high_over_estimate': max(r.bytes_high / float(r.estimate) for r in reqs if r.error is None),
-              'workload': '%d requests, natom log-uniform [64, 4000], 0.064/A^3, rcut 10 A, LJ+EI+Ewald, '
-                          '50 MD steps of 0.5 fs each, mixed precision, seeded Poisson arrivals' % n,
-              'sequential_fp64_api': {'requests': nseq, 'requests_per_s': sq['requests_per_s'],
-                                      'atom_steps_per_s': sq['atom_steps_per_s'],
-                                      'service_p50_ms': sq['service_p50_ms'],
-                                      'how': 'ForceField + host VerletIntegrator, FP64, one request at a time'}})
-    s['atom_steps_speedup_vs_sequential_fp64'] = s['atom_steps_per_s'] / sq['atom_steps_per_s']
-    return s
+    out['sequential_fp64_api'] = {'requests': nseq, 'requests_per_s': sq['requests_per_s'],
+                                  'atom_steps_per_s': sq['atom_steps_per_s'], 'service_p50_ms': sq['service_p50_ms'],
+                                  'how': 'ForceField + host VerletIntegrator, FP64, one request at a time'}
+    out['saturated_atom_steps_speedup_vs_sequential_fp64'] = out['saturated_atom_steps_per_s'] / sq['atom_steps_per_s']
+    return out
 
 
 def run_nve(args):

@@ -334,6 +334,50 @@ int yg_ewald_corr_noalloc(const double *pos, const double *charges, int64_t nato
                           double alpha, double dielectric, int64_t nlow, int64_t nhigh,
                           double *energy, double *gpos, double *vtens, void *stream);
 
+/* ------------------------------------------- many small systems (fleet) */
+
+/* A fleet steps many independent small periodic systems -- the serving
+ * workload: LJ + point-charge EI + Ewald, velocity Verlet -- with one launch
+ * per phase of the MD step for all systems in flight (eight launches per
+ * step, replayed from a CUDA graph), instead of one context and one launch
+ * sequence per system.  Capacities are fixed at creation (atoms, systems,
+ * k vectors, neighbour slots per atom, steps per system); systems are added
+ * and removed between steps.  Each system follows the reference's physics
+ * (pair_pot.c:277-301, :724-735; ewald.c:32-150, :289-292; ff.py:633-669;
+ * verlet.py:339-367; the skin rule of nlist.py:207-218) with FP32 pair terms,
+ * phases and structure factors and FP64 positions, velocities and energies;
+ * its trajectory does not depend on the other systems in flight.  No
+ * reference counterpart (the reference steps one system per process). */
+typedef struct yg_fleet yg_fleet;
+int yg_fleet_create(int64_t max_atoms, int max_systems, int64_t max_k, int max_neighbors, int max_steps,
+                    void *stream, yg_fleet **out);
+int yg_fleet_destroy(yg_fleet *fleet);
+/* Adds a system of natom atoms (host arrays: pos and vel natom x 3, masses,
+ * charges, LJ sigma and epsilon per atom (Lorentz-Berthelot mixing), the 3x3
+ * cell rvecs) with cutoff rcut, Verlet skin, Ewald alpha and gcut, time step
+ * dt and nsteps steps to run; *slot receives its slot.  YG_ERR_CAPACITY
+ * when a slot, the atom range or the k range does not fit. */
+int yg_fleet_add(yg_fleet *fleet, int64_t natom, const double *pos, const double *vel, const double *masses,
+                 const double *charges, const double *sigma, const double *epsilon, const double *rvecs,
+                 double rcut, double skin, double alpha, double gcut, double dt, int64_t nsteps, int *slot);
+/* Frees a slot and its ranges (after yg_fleet_get). */
+int yg_fleet_remove(yg_fleet *fleet, int slot);
+/* Advances every stepping system by up to nsteps steps (each stops at its
+ * own step count); enqueued on the fleet's stream. */
+int yg_fleet_step(yg_fleet *fleet, int64_t nsteps);
+/* Per slot (max_systems entries each, either may be NULL): state (0 empty,
+ * 1 stepping, 2 done, 3 failed: a neighbour row overflowed) and completed
+ * steps.  Waits for the fleet's stream. */
+int yg_fleet_poll(yg_fleet *fleet, int *state, int *steps);
+/* Positions, velocities (natom x 3) and the energy log ((steps + 1) x
+ * (epot, ekin), step 0 first) of a slot; any pointer may be NULL.  Returns
+ * YG_ERR_CAPACITY for a failed system. */
+int yg_fleet_get(yg_fleet *fleet, int slot, double *pos, double *vel, double *log, int64_t *nlog);
+/* Atom and k-vector capacity in use and the number of occupied slots. */
+int yg_fleet_usage(yg_fleet *fleet, int64_t *atoms_used, int *systems_used, int64_t *k_used);
+/* Kernel launches issued by the fleet so far (eight per step). */
+int64_t yg_fleet_launch_count(yg_fleet *fleet);
+
 /* ------------------------------------------------ MC trial energies ---- */
 
 /* compute_ewald_prefactors (yaff/pes/ewald.c:441-471): fac1 exp(-k^2/4a^2)/k^2

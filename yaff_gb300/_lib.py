@@ -98,6 +98,15 @@ SIGNATURES = {
     'yg_mc_trials': (_I, [_P, _I64, _P, _P, _P, _P, _P]),
     'yg_mc_apply': (_I, [_P, _I64, _P]),
     'yg_mc_launch_count': (_I64, [_P]),
+    'yg_fleet_create': (_I, [_I64, _I, _I64, _I, _I, _P, ctypes.POINTER(_P)]),
+    'yg_fleet_destroy': (_I, [_P]),
+    'yg_fleet_add': (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _D, _D, _I64, ctypes.POINTER(_I)]),
+    'yg_fleet_remove': (_I, [_P, _I]),
+    'yg_fleet_step': (_I, [_P, _I64]),
+    'yg_fleet_poll': (_I, [_P, _P, _P]),
+    'yg_fleet_get': (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(_I64)]),
+    'yg_fleet_usage': (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I), ctypes.POINTER(_I64)]),
+    'yg_fleet_launch_count': (_I64, [_P]),
     'yg_ewald_corr_noalloc':(_I, [_P, _P, _I64, _P, _P, _P, _I64, _P, _P, _D, _D, _D, _I64, _I64, _P, _P, _P,
                                    _P]),
 }
