@@ -41,7 +41,7 @@ def test_host_build_regrows_after_forced_overflow():
     e1 = ff.compute(g1, v1)
     sha1, nn1 = _digest(ff.nlist.neighs), ff.nlist.nneigh
     ff.nlist.set_capacity(1)            # 32 slots per atom: the next build overflows
-    ff.nlist.rebuild_next = True
+    ff.update_pos(spec['pos'])          # the next compute updates the list
     g2, v2 = np.zeros((n, 3)), np.zeros((3, 3))
     e2 = ff.compute(g2, v2)
     assert ff.nlist.nneigh == nn1 and _digest(ff.nlist.neighs) == sha1
@@ -134,6 +134,7 @@ def test_serving_cancel_pending_and_running_requests():
     pending.cancel()                       # withdrawn before the run starts
     order = [long_req, pending, reqs[0], reqs[2]]
     eng = ServingEngine(nslots=1, budget_bytes=1 << 32, precision='mixed', batch_steps=20)
+    eng.run(_workload(1, nmax=100, nsteps=5, seed=3), realtime=False)   # one-time set-up of the pool
     used0 = pool_used()
 
     def canceller():

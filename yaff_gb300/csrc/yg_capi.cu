@@ -559,6 +559,10 @@ int yg_check_wait_timeout(yg_ctx *c, int64_t polls, int *timed_out) {
   YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   YG_CUDA(cudaStreamSynchronize(c->stream));
   *timed_out = c->h_status[YG_ST_TIMEOUT] ? 1 : 0;
+  // the self-check's own timeout must not mark the context's next results
+  YG_CUDA(cudaMemsetAsync(c->d_status, 0, YG_ST_NWORDS * sizeof(int), c->stream));
+  YG_CUDA(cudaStreamSynchronize(c->stream));
+  c->h_status[YG_ST_TIMEOUT] = 0;
   return YG_OK;
 }
 
@@ -614,7 +618,7 @@ int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nl
 
 int yg_nlist_recompute(yg_ctx *c) {
   if (!c) return YG_ERR_ARG;
-  if (!c->have_list) {
+  if (!c->have_list || !c->rows_valid) {
     yg_set_error("no neighbour list to recompute");
     return YG_ERR_STATE;
   }
@@ -624,7 +628,7 @@ int yg_nlist_recompute(yg_ctx *c) {
 
 int yg_nlist_max_disp2(yg_ctx *c, double *out) {
   if (!c || !out) return YG_ERR_ARG;
-  if (!c->have_list) {
+  if (!c->have_list || !c->rows_valid) {
     *out = INFINITY;
     return YG_OK;
   }
@@ -633,7 +637,7 @@ int yg_nlist_max_disp2(yg_ctx *c, double *out) {
 
 int yg_nlist_export(yg_ctx *c, yg_neigh_row *rows, int64_t cap, int64_t *n) {
   if (!c || !n) return YG_ERR_ARG;
-  if (!c->have_list) {
+  if (!c->have_list || !c->rows_valid) {
     yg_set_error("no neighbour list");
     return YG_ERR_STATE;
   }
@@ -642,7 +646,7 @@ int yg_nlist_export(yg_ctx *c, yg_neigh_row *rows, int64_t cap, int64_t *n) {
 
 int yg_pair_compute(yg_ctx *c, int slot_mask, int want_grad) {
   if (!c) return YG_ERR_ARG;
-  if (!c->have_list) {
+  if (!c->have_list || !c->rows_valid) {
     yg_set_error("build the neighbour list first");
     return YG_ERR_STATE;
   }

@@ -1654,13 +1654,16 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
       if (n <= 0) continue;
       const int nab = (int)((n + 127) / 128);
       if ((rc = yg_launch_ya_umma(ctx, ctx->d_ew_yf, gb[g][0], n, nmf, nks, nab, ctx->d_ew_ya))) return rc;
+      // tile ranges per atom block: a CTA's time is its set-up (E0|E1 rows,
+      // A operand, TMEM) plus its tiles (a K-step each and the epilogue), one
+      // CTA per SM; the fewest ranges of the least estimated time
+      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = 20.0;
       int nr = 1;
-      double best = 0.0;
+      double best = 1e300;
       for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
-        const double waves = (double)nab * r / nsm;
-        const double eff = waves / std::ceil(waves);
-        if (eff > best + 1e-9) {
-          best = eff;
+        const double cost = std::ceil((double)nab * r / nsm) * (setup + tiles / r);
+        if (cost < best * (1.0 - 1e-9)) {
+          best = cost;
           nr = r;
         }
       }
@@ -1702,13 +1705,16 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
       if (n <= 0) continue;
       const int nab = (int)((n + 127) / 128);
       if ((rc = yg_launch_ya_umma(ctx, ctx->d_ew_yf, gb[g][0], n, nmf, nks, nab, ctx->d_ew_ya))) return rc;
+      // tile ranges per atom block: a CTA's time is its set-up (E0|E1 rows,
+      // A operand, TMEM) plus its tiles (a K-step each and the epilogue), one
+      // CTA per SM; the fewest ranges of the least estimated time
+      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = 20.0;
       int nr = 1;
-      double best = 0.0;
+      double best = 1e300;
       for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
-        const double waves = (double)nab * r / nsm;
-        const double eff = waves / std::ceil(waves);
-        if (eff > best + 1e-9) {
-          best = eff;
+        const double cost = std::ceil((double)nab * r / nsm) * (setup + tiles / r);
+        if (cost < best * (1.0 - 1e-9)) {
+          best = cost;
           nr = r;
         }
       }

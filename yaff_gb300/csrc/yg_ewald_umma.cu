@@ -16,18 +16,21 @@
 // truncates toward zero; with at most 3 x 4 MMAs of K = 16 per accumulator the
 // bias stays below 1e-6 of |Z|, as for the warp-level MMA form.
 //
-// Warp roles in a CTA of 192 threads (one CTA per SM, all 512 TMEM columns):
+// Warp roles in a CTA of 576 threads (one CTA per SM, all 512 TMEM columns):
 //   warp 0      bulk copies: the CTA's A operand once, then the B operand of
 //               every tile into one of two stages (a stage is refilled once
 //               the MMAs that read it have completed);
 //   warp 1      allocates TMEM; one lane issues the MMAs of a tile into one
 //               of two accumulators (256 columns each) and commits them to an
 //               mbarrier;
-//   warps 2-5   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (one atom
-//               per thread), forms P from the atom's E0|E1 row (staged in
-//               shared memory transposed, so a column's reads are
-//               conflict-free) and accumulates the three force components;
-//               then releases the accumulator.  The column list (g0, g1) of
+//   warps 2-17  epilogue, four warps per TMEM lane quarter: warp w reads
+//               lanes 32 (w % 4) .. + 31 (one atom per thread) of a quarter
+//               of the tile's columns, forms P from the atom's E0|E1 row
+//               (staged in shared memory transposed, so a column's reads
+//               are conflict-free) and accumulates the three force
+//               components; then releases the accumulator.  The four
+//               partial sums of an atom are added in a fixed order at the
+//               end.  The column list (g0, g1) of
 //               a tile is read from global memory (one warp-uniform load per
 //               column), not from a stage the producer may already refill.
 // Shared-memory operands use the no-swizzle K-major layout: 8-row x 16-byte
@@ -46,7 +49,8 @@ constexpr int UM_N = 4 * UM_COLS;      // MMA N
 constexpr int UM_KMAX = 4;             // K-steps (8 m values each) per tile, at most
 constexpr int UM_ATILE = UM_M * 32;    // bytes of one A K-step half (128 rows x 16 FP16)
 constexpr int UM_BTILE = UM_N * 32;    // bytes of one B K-step half (256 rows x 16 FP16)
-constexpr int UM_THREADS = 192;
+constexpr int UM_EPI = 16;            // epilogue warps (four per TMEM lane quarter)
+constexpr int UM_THREADS = 64 + 32 * UM_EPI;
 constexpr int UM_TMEM_COLS = 2 * UM_N;
 // instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B FP16,
 // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
@@ -211,7 +215,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     for (int s = 0; s < 2; s++) {
       um_init(&bar_b[s], 1);
       um_init(&bar_mma[s], 1);
-      um_init(&bar_acc[s], 4);
+      um_init(&bar_acc[s], UM_EPI);
     }
     stop_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -277,11 +281,14 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: TMEM lane quarter q of this warp, one atom per thread
-    const int q = warp & 3, r = 32 * q + lane;
+    // epilogue: UM_EPI warps, UM_EPI / 4 per TMEM lane quarter q (= warp % 4);
+    // warp h of a quarter takes the 32-column chunks h, h + UM_EPI / 4, ...
+    // of every tile; one atom per thread
+    constexpr int HQ = UM_EPI / 4;
+    const int q = warp & 3, h = (warp - 2) >> 2, r = 32 * q + lane;
     const float2 *row = te + (size_t)(bbase + r) * lep;
-    for (int g = 0; g < ne; g++) sE[g * UM_M + r] = row[g];
-    asm volatile("bar.sync 1, 128;" ::: "memory");
+    for (int g = h; g < ne; g += HQ) sE[g * UM_M + r] = row[g];
+    asm volatile("bar.sync 1, %0;" ::"n"(UM_EPI * 32) : "memory");
     UmAcc acc0, acc1, acc2;
     acc0.init();
     acc1.init();
@@ -294,7 +301,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
       const unsigned tb = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(s * UM_N);
       float p0 = 0.f, p1 = 0.f, p2 = 0.f;
 #pragma unroll 1
-      for (int c = 0; c < UM_N / 32; c++) {
+      for (int c = h; c < UM_N / 32; c += HQ) {
         int4 cc[8];
 #pragma unroll
         for (int jj = 0; jj < 8; jj++) cc[jj] = __ldg(cs + 8 * c + jj);
@@ -325,12 +332,25 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
       acc1.add(p1);
       acc2.add(p2);
     }
+    // the HQ partial sums of every atom, added in a fixed order; the stage
+    // buffers are idle now (the MMAs consumed every copy), so they hold them
+    double *red = reinterpret_cast<double *>(sB);
+    red[((size_t)h * UM_M + r) * 3 + 0] = (double)acc0.s;
+    red[((size_t)h * UM_M + r) * 3 + 1] = (double)acc1.s;
+    red[((size_t)h * UM_M + r) * 3 + 2] = (double)acc2.s;
+    asm volatile("bar.sync 1, %0;" ::"n"(UM_EPI * 32) : "memory");
     const int a = bbase + r;
-    if (a < a1) {
+    if (h == 0 && a < a1) {
+      double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+      for (int hh = 0; hh < HQ; hh++) {
+        t0 += red[((size_t)hh * UM_M + r) * 3 + 0];
+        t1 += red[((size_t)hh * UM_M + r) * 3 + 1];
+        t2 += red[((size_t)hh * UM_M + r) * 3 + 2];
+      }
       double *dst = out + (int64_t)blockIdx.y * rstride + (int64_t)a * 3;
-      dst[0] = (double)acc0.s * inv1;
-      dst[1] = (double)acc1.s * inv1;
-      dst[2] = (double)acc2.s * inv2;
+      dst[0] = t0 * inv1;
+      dst[1] = t1 * inv1;
+      dst[2] = t2 * inv2;
     }
   }
   um_fence_before();

@@ -135,6 +135,7 @@ struct yg_ctx {
   int cap_sorted = 0;             // allocated cell-list capacity (cells)
   GridGeom grid{};
   int have_list = 0;
+  int rows_valid = 0;             // the slot rows hold the current list (cleared by yg_nlist_set_capacity)
   int list_recomputed = 0;        // skin path ran since the last rebuild
   int fast_path = 0;
   int geom_valid = 0;             // grid, shifts and band match (cell, geom_rc)

@@ -419,7 +419,7 @@ int yg_nlist_set_capacity(yg_ctx *c, int64_t slots) {
   // the rows in the slots were laid out with the old capacity: no kernel may
   // read them again; the host path rebuilds before its next use and the
   // device-resident MD rebuilds at its next step
-  c->have_list = 0;
+  c->rows_valid = 0;
   if (c->md_ready) {
     k_set_int<<<1, 32, 0, c->stream>>>(c->d_md_ctrl + 1, 1);
     YG_LAUNCH_CHECK(c, "k_set_int");
@@ -581,6 +581,7 @@ int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nr
     left -= nb;
   }
   c->list_recomputed = 1;
+  if (nsteps > 0) c->rows_valid = 1;  // a forced rebuild ran at the first step
   for (int p = 0; p < YG_NPART; p++) c->part_valid[p] = 0;
   if (nrebuild) *nrebuild = c->md_rebuilds - reb0;
   return YG_OK;

@@ -992,6 +992,7 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
     break;
   }
   ctx->have_list = 1;
+  ctx->rows_valid = 1;
   ctx->list_recomputed = 0;
   // the sorted order changed: repack the pair parameters
   if ((rc_ = yg_pack_pair_params(ctx))) return rc_;
