@@ -264,8 +264,8 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_vkind, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,
       (void **)&c->d_total, (void **)&c->d_red, (void **)&c->d_vel, (void **)&c->d_invm, (void **)&c->d_md_ekpart,
       (void **)&c->d_md_ekin, (void **)&c->d_md_log, (void **)&c->d_md_extra, (void **)&c->d_md_step,
-      (void **)&c->d_md_ctrl, (void **)&c->d_snap_pos, (void **)&c->d_snap_vel, (void **)&c->d_snap_total,
-      (void **)&c->d_snap_step};
+      (void **)&c->d_md_ctrl, (void **)&c->d_md_thermo, (void **)&c->d_snap_pos, (void **)&c->d_snap_vel,
+      (void **)&c->d_snap_total, (void **)&c->d_snap_step, (void **)&c->d_snap_thermo};
   if (c->md_graph_exec) cudaGraphExecDestroy(c->md_graph_exec);
   if (c->md_cap_stream) cudaStreamDestroy(c->md_cap_stream);
   if (c->ew_aux) cudaStreamDestroy(c->ew_aux);
@@ -279,6 +279,10 @@ int yg_destroy(yg_ctx *c) {
       yg_free(c, (void **)&c->d_ptab64[p]);
       yg_free(c, (void **)&c->d_ptab32[p]);
     }
+    // anything the context allocated that no field above names
+    std::vector<void *> left;
+    for (auto &kv : c->alloc_bytes) left.push_back(kv.first);
+    for (void *p : left) yg_free(c, &p);
   }
   pinned_put(c->h_block, c->h_block_bytes);
   delete c;

@@ -13,14 +13,16 @@
 //                      (yaff/pes/nlist.py:207-218)
 //   build     (tile)   neighbour rows of the systems whose gate fired:
 //                      128-atom tiles of the system staged in shared memory,
-//                      every periodic image within rcut + skin, FP32
-//                      prefilter and the FP64 decision near the cutoff; a row
-//                      entry keeps the FP64 relative vector of the build
+//                      every periodic image within rcut + skin; relative
+//                      vectors as exact FP32 hi + lo differences of the
+//                      wrapped Cartesian positions plus the image shift (hi +
+//                      lo), rounded once: a row entry keeps them
 //   pair      (atom)   LJ + real-space EI over the row in FP32, the relative
 //                      vector refreshed by the displacements since the build
 //                      (the reference's skin path, nlist.c:183-232)
-//   sfac      (k)      structure factors S(k) of each system's half sphere
-//   ewald     (atom)   reciprocal-space gradient from S(k)
+//   sfac      (k)      structure factors S(k) of each system's half sphere,
+//                      and the FP32 coefficients 2 A(k) S(k) of the gradient
+//   ewald     (atom)   reciprocal-space gradient from those coefficients
 //   kick      (atom)   total gradient, second half kick, kinetic energy
 //   finish    (system) fixed-order energy sums, the log row, the counters
 // Every reduction over a system runs inside that system's own threads in a
@@ -32,7 +34,11 @@
 // (ewald.c:32-150), self and neutralizing terms (ewald.c:289-292,
 // ff.py:633-669) and velocity Verlet (verlet.py:339-367); pair terms,
 // phases and structure factors in FP32 with compensated sums, positions,
-// velocities and energies in FP64.
+// velocities and energies in FP64.  No FP64 arithmetic runs per pair or per
+// atom and k vector: the FP64 pipe of this part is a small fraction of its
+// FP32 rate.  The neighbour decision at rcut + skin is FP32 (deterministic,
+// so a system's list is the same alone and in a mix; pairs beyond rcut are
+// masked by the pair kernel and the skin rule keeps the list complete).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -42,6 +48,8 @@
 
 #define FL_TILE 128    // atoms per build tile and per atom-range granule
 #define FL_KGRAN 32    // k-vector range granule
+#define FL_RMAX 2      // periodic images searched per axis, at most
+#define FL_SHIFTS ((2 * FL_RMAX + 3) * (2 * FL_RMAX + 3) * (2 * FL_RMAX + 3))
 
 struct FleetSys {
   int a0, n, k0, nk;
@@ -65,12 +73,14 @@ struct FleetDev {
   double *pos, *vel, *pos_build, *invm, *gtot;
   double *gpair, *gew, *epair, *ekin;
   float *q, *sig, *seps;
-  float4 *pos32, *disp, *fhi, *flo;
+  float4 *disp, *fhi, *flo;  // displacement since the build; fractional coordinates (hi, lo)
+  float4 *chi, *clo;         // Cartesian position wrapped into the cell (hi, lo)
   int *sysid, *ncount;
   int4 *nbr;                // (j, FP32 relative vector at the build)
   // k vectors
   int4 *kg;                 // (g0, g1, g2, system or -1)
-  float4 *kv;               // (kx, ky, kz, 0)
+  float4 *kgf;              // (g0, g1, g2, 2 A(k) Re S(k)) as FP32
+  float4 *kv;               // (kx, ky, kz, 2 A(k) Im S(k))
   double *kpref;            // A(k) = 4 pi / V exp(-k^2 / 4 alpha^2) / k^2
   double2 *S;
   // systems
@@ -137,7 +147,6 @@ __global__ void k_fl_drift(FleetDev F, int64_t natom_cap) {
   F.disp[i] = make_float4(d[0], d[1], d[2], 0.f);
   const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   atomicMax(&S.maxd2, __float_as_uint(d2));
-  F.pos32[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
   float sh[3], sl[3];
   for (int k = 0; k < 3; k++) {
     const double fs = S.gv[3 * k] * r[0] + S.gv[3 * k + 1] * r[1] + S.gv[3 * k + 2] * r[2];
@@ -146,6 +155,17 @@ __global__ void k_fl_drift(FleetDev F, int64_t natom_cap) {
   }
   F.fhi[i] = make_float4(sh[0], sh[1], sh[2], 0.f);
   F.flo[i] = make_float4(sl[0], sl[1], sl[2], 0.f);
+  // the position wrapped into the cell, as FP32 hi + lo
+  double fl[3], rw[3];
+  for (int k = 0; k < 3; k++) fl[k] = floor(S.gv[3 * k] * r[0] + S.gv[3 * k + 1] * r[1] + S.gv[3 * k + 2] * r[2]);
+  for (int x = 0; x < 3; x++) rw[x] = r[x] - (fl[0] * S.rv[x] + fl[1] * S.rv[3 + x] + fl[2] * S.rv[6 + x]);
+  float ch[3], cl[3];
+  for (int x = 0; x < 3; x++) {
+    ch[x] = (float)rw[x];
+    cl[x] = (float)(rw[x] - (double)ch[x]);
+  }
+  F.chi[i] = make_float4(ch[0], ch[1], ch[2], 0.f);
+  F.clo[i] = make_float4(cl[0], cl[1], cl[2], 0.f);
 }
 
 __global__ void k_fl_gate(FleetDev F, int nsys) {
@@ -159,11 +179,23 @@ __global__ void k_fl_gate(FleetDev F, int nsys) {
   S.maxd2 = 0u;
 }
 
+// x + y = s + e exactly (Knuth's TwoSum; no operation may be reassociated)
+__device__ __forceinline__ void two_sum(float x, float y, float &s, float &e) {
+  s = x + y;
+  const float bb = s - x;
+  e = (x - (s - bb)) + (y - bb);
+}
+
 // One block per 128-atom tile; rows of the tile's atoms against every atom of
-// the system and every image within rcut + skin.
+// the system and every image within rcut + skin.  The difference of two
+// wrapped positions is exact as a + c (TwoSum of the hi parts, plus the lo
+// parts); its FP32 fractional part picks the wrap w, and each image n adds
+// the shift (n - w).R, tabulated per block as FP32 hi + lo from FP64.  A
+// quick FP32 test of a + shift_hi selects the candidates whose vector is then
+// summed with its error terms and rounded once.
 __global__ void __launch_bounds__(FL_TILE) k_fl_build(FleetDev F, int64_t ntile) {
-  __shared__ float4 sj[FL_TILE];
-  __shared__ double sr[9], sg[9];
+  __shared__ float4 sh[FL_TILE], sl[FL_TILE];
+  __shared__ float4 th[FL_SHIFTS], tl[FL_SHIFTS];
   const int64_t t = blockIdx.x;
   if (t >= ntile) return;
   const int64_t i0 = t * FL_TILE;
@@ -171,69 +203,72 @@ __global__ void __launch_bounds__(FL_TILE) k_fl_build(FleetDev F, int64_t ntile)
   if (s < 0) return;
   FleetSys &S = F.d_sys[s];
   if (S.state != 1 || !S.rebuild) return;
-  if (threadIdx.x < 9) {
-    sr[threadIdx.x] = S.rv[threadIdx.x];
-    sg[threadIdx.x] = S.gv[threadIdx.x];
+  const int r0 = S.rmax[0], r1 = S.rmax[1], r2 = S.rmax[2];
+  const int W0 = 2 * r0 + 3, W1 = 2 * r1 + 3, W2 = 2 * r2 + 3;  // m = n - w in [-(r+1), r+1]
+  for (int q = threadIdx.x; q < W0 * W1 * W2; q += FL_TILE) {
+    const double m0 = q % W0 - (r0 + 1), m1 = (q / W0) % W1 - (r1 + 1), m2 = q / (W0 * W1) - (r2 + 1);
+    float h[3], l[3];
+    for (int x = 0; x < 3; x++) {
+      const double v = m0 * S.rv[x] + m1 * S.rv[3 + x] + m2 * S.rv[6 + x];
+      h[x] = (float)v;
+      l[x] = (float)(v - (double)h[x]);
+    }
+    th[q] = make_float4(h[0], h[1], h[2], 0.f);
+    tl[q] = make_float4(l[0], l[1], l[2], 0.f);
   }
   const int64_t a0 = S.a0, a1 = S.a0 + S.n;
   const int64_t i = i0 + threadIdx.x;
   const bool vi = i < a1;
-  const float4 ri32 = vi ? F.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  double ri[3] = {0.0, 0.0, 0.0};
-  if (vi)
-    for (int k = 0; k < 3; k++) ri[k] = F.pos[3 * i + k];
-  const double rcs2 = S.rcs * S.rcs;
-  const float band = (float)(S.rcs + 1e-3);
-  const float band2 = band * band;
-  const int r0 = S.rmax[0], r1 = S.rmax[1], r2 = S.rmax[2];
+  const float4 hi = vi ? F.chi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 lo = vi ? F.clo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float rcs2 = (float)(S.rcs * S.rcs);
+  const float rcs2q = (float)(S.rcs * S.rcs * (1.0 + 1e-4));
   const int cap = F.cap;
+  float gf[9];
+  for (int k = 0; k < 9; k++) gf[k] = (float)S.gv[k];
   int count = 0;
-  __syncthreads();
-  float gf[9], rf[9];
-  for (int k = 0; k < 9; k++) {
-    gf[k] = (float)sg[k];
-    rf[k] = (float)sr[k];
-  }
+  int4 *row = F.nbr + i * cap;
   for (int64_t jt = a0; jt < a1; jt += FL_TILE) {
     const int64_t jl = jt + threadIdx.x;
-    sj[threadIdx.x] = jl < a1 ? F.pos32[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sh[threadIdx.x] = jl < a1 ? F.chi[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sl[threadIdx.x] = jl < a1 ? F.clo[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     const int nj = (int)(a1 - jt < FL_TILE ? a1 - jt : FL_TILE);
     if (vi) {
       for (int jj = 0; jj < nj; jj++) {
-        const float4 pj = sj[jj];
-        const float dx = pj.x - ri32.x, dy = pj.y - ri32.y, dz = pj.z - ri32.z;
-        float ds[3], w[3];
-        for (int k = 0; k < 3; k++) {
-          const float f = gf[3 * k] * dx + gf[3 * k + 1] * dy + gf[3 * k + 2] * dz;
-          w[k] = rintf(f);
-          ds[k] = f - w[k];
-        }
-        const int64_t j = jt + jj;
+        const float4 hj = sh[jj], lj = sl[jj];
+        float a[3], c[3];
+        two_sum(hj.x, -hi.x, a[0], c[0]);
+        two_sum(hj.y, -hi.y, a[1], c[1]);
+        two_sum(hj.z, -hi.z, a[2], c[2]);
+        c[0] += lj.x - lo.x;
+        c[1] += lj.y - lo.y;
+        c[2] += lj.z - lo.z;
+        int w[3];
+        for (int k = 0; k < 3; k++) w[k] = __float2int_rn(gf[3 * k] * a[0] + gf[3 * k + 1] * a[1] + gf[3 * k + 2] * a[2]);
+        const int j = (int)(jt + jj);
         for (int n2 = -r2; n2 <= r2; n2++)
           for (int n1 = -r1; n1 <= r1; n1++)
             for (int n0 = -r0; n0 <= r0; n0++) {
-              const float t0 = ds[0] + n0, t1 = ds[1] + n1, t2 = ds[2] + n2;
-              const float ex = t0 * rf[0] + t1 * rf[3] + t2 * rf[6];
-              const float ey = t0 * rf[1] + t1 * rf[4] + t2 * rf[7];
-              const float ez = t0 * rf[2] + t1 * rf[5] + t2 * rf[8];
-              if (ex * ex + ey * ey + ez * ez >= band2) continue;
-              // the FP64 decision for the same image (the prefilter's wrap)
-              double dr[3], fs[3];
-              for (int k = 0; k < 3; k++) dr[k] = F.pos[3 * j + k] - ri[k];
-              for (int k = 0; k < 3; k++)
-                fs[k] = sg[3 * k] * dr[0] + sg[3 * k + 1] * dr[1] + sg[3 * k + 2] * dr[2] - (double)w[k];
-              fs[0] += n0;
-              fs[1] += n1;
-              fs[2] += n2;
-              double d[3];
-              for (int k = 0; k < 3; k++) d[k] = fs[0] * sr[k] + fs[1] * sr[3 + k] + fs[2] * sr[6 + k];
-              const double dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-              if (dd >= rcs2 || dd == 0.0) continue;  // outside, or the atom itself
+              const int m0 = n0 - w[0], m1 = n1 - w[1], m2 = n2 - w[2];
+              if (m0 < -(r0 + 1) || m0 > r0 + 1 || m1 < -(r1 + 1) || m1 > r1 + 1 || m2 < -(r2 + 1) || m2 > r2 + 1)
+                continue;  // (an image beyond the searched range: never within rcut + skin)
+              const int q = (m0 + r0 + 1) + W0 * ((m1 + r1 + 1) + W1 * (m2 + r2 + 1));
+              const float4 Th = th[q];
+              const float qx = a[0] + Th.x, qy = a[1] + Th.y, qz = a[2] + Th.z;
+              if (!(qx * qx + qy * qy + qz * qz < rcs2q)) continue;
+              const float4 Tl = tl[q];
+              float ex, ey, ez, e0, e1, e2;
+              two_sum(a[0], Th.x, ex, e0);
+              two_sum(a[1], Th.y, ey, e1);
+              two_sum(a[2], Th.z, ez, e2);
+              ex += e0 + (c[0] + Tl.x);
+              ey += e1 + (c[1] + Tl.y);
+              ez += e2 + (c[2] + Tl.z);
+              const float d2 = ex * ex + ey * ey + ez * ez;
+              if (!(d2 < rcs2) || d2 == 0.f) continue;  // outside, or the atom itself
               if (count < cap)
-                F.nbr[i * cap + count] =
-                    make_int4((int)j, __float_as_int((float)d[0]), __float_as_int((float)d[1]),
-                              __float_as_int((float)d[2]));
+                row[count] = make_int4(j, __float_as_int(ex), __float_as_int(ey), __float_as_int(ez));
               count++;
             }
       }
@@ -243,7 +278,7 @@ __global__ void __launch_bounds__(FL_TILE) k_fl_build(FleetDev F, int64_t ntile)
   if (vi) {
     F.ncount[i] = min(count, cap);
     if (count > cap) atomicOr(&S.overflow, 1);
-    for (int k = 0; k < 3; k++) F.pos_build[3 * i + k] = ri[k];
+    for (int k = 0; k < 3; k++) F.pos_build[3 * i + k] = F.pos[3 * i + k];
     F.disp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
@@ -300,7 +335,8 @@ __global__ void k_fl_pair(FleetDev F, int64_t natom_cap) {
   F.epair[i] = (double)e - (double)ce;
 }
 
-// S(k) of every reciprocal vector of every system, one thread per k.
+// S(k) of every reciprocal vector of every system, one thread per k; then
+// the FP32 coefficients 2 A(k) S(k) that the gradient pass reads.
 __global__ void k_fl_sfac(FleetDev F, int64_t nk_cap) {
   const int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (kk >= nk_cap) return;
@@ -308,21 +344,24 @@ __global__ void k_fl_sfac(FleetDev F, int64_t nk_cap) {
   if (g.w < 0) return;
   const FleetSys &S = F.d_sys[g.w];
   if (S.state != 1) return;
-  const float g0 = (float)g.x, g1 = (float)g.y, g2 = (float)g.z;
+  const float4 gf = F.kgf[kk];
   float cr = 0.f, ci = 0.f, kr = 0.f, ki = 0.f;
   for (int64_t a = S.a0; a < S.a0 + S.n; a++) {
     const float4 hi = F.fhi[a], lo = F.flo[a];
-    const float t = frac_gs(g0, hi.x, lo.x) + frac_gs(g1, hi.y, lo.y) + frac_gs(g2, hi.z, lo.z);
+    const float t = frac_gs(gf.x, hi.x, lo.x) + frac_gs(gf.y, hi.y, lo.y) + frac_gs(gf.z, hi.z, lo.z);
     float sn, cs;
     sincospif(2.0f * t, &sn, &cs);
     const float qa = F.q[a];
     kahan_add(cr, kr, qa * cs);
     kahan_add(ci, ki, qa * sn);
   }
-  F.S[kk] = make_double2((double)cr - (double)kr, (double)ci - (double)ki);
+  const double sr = (double)cr - (double)kr, si = (double)ci - (double)ki, a2 = 2.0 * F.kpref[kk];
+  F.S[kk] = make_double2(sr, si);
+  F.kgf[kk].w = (float)(a2 * sr);
+  F.kv[kk].w = (float)(a2 * si);
 }
 
-// Reciprocal-space gradient of every atom from its system's S(k).
+// Reciprocal-space gradient of every atom from its system's coefficients.
 __global__ void k_fl_ewald(FleetDev F, int64_t natom_cap) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= natom_cap) return;
@@ -335,14 +374,11 @@ __global__ void k_fl_ewald(FleetDev F, int64_t natom_cap) {
   float gx = 0.f, gy = 0.f, gz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   if (qi != 0.f) {
     for (int64_t kk = S.k0; kk < S.k0 + S.nk; kk++) {
-      const int4 g = F.kg[kk];
-      const float t = frac_gs((float)g.x, hi.x, lo.x) + frac_gs((float)g.y, hi.y, lo.y) +
-                      frac_gs((float)g.z, hi.z, lo.z);
+      const float4 g = F.kgf[kk], k = F.kv[kk];
+      const float t = frac_gs(g.x, hi.x, lo.x) + frac_gs(g.y, hi.y, lo.y) + frac_gs(g.z, hi.z, lo.z);
       float sn, cs;
       sincospif(2.0f * t, &sn, &cs);
-      const double2 Sk = F.S[kk];
-      const float x = (float)(2.0 * F.kpref[kk]) * qi * ((float)Sk.y * cs - (float)Sk.x * sn);
-      const float4 k = F.kv[kk];
+      const float x = qi * (k.w * cs - g.w * sn);
       kahan_add(gx, cx, k.x * x);
       kahan_add(gy, cy, k.y * x);
       kahan_add(gz, cz, k.z * x);
@@ -421,8 +457,8 @@ __global__ void k_fl_finish(FleetDev F, int nsys) {
 
 void fl_free(yg_fleet *f) {
   void *bufs[] = {f->d.pos, f->d.vel, f->d.pos_build, f->d.invm, f->d.gtot, f->d.gpair, f->d.gew, f->d.epair, f->d.ekin, f->d.q,
-                  f->d.sig, f->d.seps, f->d.pos32, f->d.disp, f->d.fhi, f->d.flo, f->d.sysid, f->d.ncount, f->d.nbr, f->d.kg, f->d.kv,
-                  f->d.kpref, f->d.S, f->d.d_sys, f->d.log};
+                  f->d.sig, f->d.seps, f->d.disp, f->d.fhi, f->d.flo, f->d.chi, f->d.clo, f->d.sysid, f->d.ncount, f->d.nbr, f->d.kg, f->d.kgf,
+                  f->d.kv, f->d.kpref, f->d.S, f->d.d_sys, f->d.log};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (f->h_sys_pinned) cudaFreeHost(f->h_sys_pinned);
@@ -489,9 +525,10 @@ int yg_fleet_create(int64_t max_atoms, int max_systems, int64_t max_k, int max_n
       {(void **)&f->d.invm, Au * 8}, {(void **)&f->d.gtot, Au * 24}, {(void **)&f->d.gpair, Au * 24},
       {(void **)&f->d.gew, Au * 24}, {(void **)&f->d.epair, Au * 8}, {(void **)&f->d.ekin, Au * 8},
       {(void **)&f->d.q, Au * 4}, {(void **)&f->d.sig, Au * 4}, {(void **)&f->d.seps, Au * 4},
-      {(void **)&f->d.pos32, Au * 16}, {(void **)&f->d.disp, Au * 16}, {(void **)&f->d.fhi, Au * 16},
+      {(void **)&f->d.disp, Au * 16}, {(void **)&f->d.chi, Au * 16}, {(void **)&f->d.clo, Au * 16}, {(void **)&f->d.fhi, Au * 16},
       {(void **)&f->d.flo, Au * 16}, {(void **)&f->d.sysid, Au * 4}, {(void **)&f->d.ncount, Au * 4},
-      {(void **)&f->d.nbr, (size_t)Au * f->d.cap * 16}, {(void **)&f->d.kg, Ku * 16}, {(void **)&f->d.kv, Ku * 16},
+      {(void **)&f->d.nbr, (size_t)Au * f->d.cap * 16}, {(void **)&f->d.kg, Ku * 16}, {(void **)&f->d.kgf, Ku * 16},
+      {(void **)&f->d.kv, Ku * 16},
       {(void **)&f->d.kpref, Ku * 8}, {(void **)&f->d.S, Ku * 16}, {(void **)&f->d.d_sys, (size_t)max_systems * sizeof(FleetSys)},
       {(void **)&f->d.log, (size_t)max_systems * (max_steps + 1) * 16}};
   for (auto &b : bufs) {
@@ -574,6 +611,10 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
     const double gsp = 1.0 / std::sqrt(R[3 * k] * R[3 * k] + R[3 * k + 1] * R[3 * k + 1] + R[3 * k + 2] * R[3 * k + 2]);
     rmax[k] = (int)std::ceil((rcut + skin) / rsp - 0.5);
     gmax[k] = (int)std::ceil(gcut / gsp - 0.5);
+    if (rmax[k] > FL_RMAX) {
+      yg_set_error("yg_fleet_add: the cell is too small for rcut + skin (more than two periodic images per axis)");
+      return YG_ERR_ARG;
+    }
   }
   // the half sphere of k vectors (yaff/pes/ewald.c:54-64) and A(k)
   const double tp = 6.2831853071795864769, fp = 12.566370614359172954;
@@ -581,7 +622,7 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
   double gc2 = gcut * tp;
   gc2 *= gc2;
   std::vector<int4> kg;
-  std::vector<float4> kv;
+  std::vector<float4> kv, kgf;
   std::vector<double> kp;
   for (int g0 = -gmax[0]; g0 <= gmax[0]; g0++)
     for (int g1 = -gmax[1]; g1 <= gmax[1]; g1++)
@@ -593,6 +634,7 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
         if (ksq > gc2) continue;
         kg.push_back(make_int4(g0, g1, g2, s));
         kv.push_back(make_float4((float)k[0], (float)k[1], (float)k[2], 0.f));
+        kgf.push_back(make_float4((float)g0, (float)g1, (float)g2, 0.f));
         kp.push_back(fac1 * std::exp(-ksq * fac2) / ksq);
       }
   const int ag = (int)((natom + FL_TILE - 1) / FL_TILE);
@@ -654,6 +696,7 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
   YG_CUDA(cudaMemsetAsync(f->d.gtot + 3 * a0, 0, natom * 24, st));
   YG_CUDA(cudaMemsetAsync(f->d.ncount + a0, 0, (size_t)ag * FL_TILE * 4, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kv + S.k0, kv.data(), kv.size() * 16, h2d, st));
+  YG_CUDA(cudaMemcpyAsync(f->d.kgf + S.k0, kgf.data(), kgf.size() * 16, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kpref + S.k0, kp.data(), kp.size() * 8, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kg + S.k0, kg.data(), kg.size() * 16, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.d_sys + s, &S, sizeof(S), h2d, st));
