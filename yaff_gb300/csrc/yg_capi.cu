@@ -213,7 +213,7 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
   rc |= yg_alloc(c, (void **)&c->d_x64, N * sizeof(double4_32a));
   rc |= yg_alloc(c, (void **)&c->d_x32, N * sizeof(float4));
   rc |= yg_alloc(c, (void **)&c->d_xb, N * sizeof(float4));
-  rc |= yg_alloc(c, (void **)&c->d_ncount, N * sizeof(int));
+  rc |= yg_alloc(c, (void **)&c->d_ncount, N * sizeof(int2));
   rc |= yg_alloc(c, (void **)&c->d_status, YG_ST_NWORDS * sizeof(int));
   rc |= yg_alloc(c, (void **)&c->d_part_ev, YG_NPART * 10 * sizeof(double));
   rc |= yg_alloc(c, (void **)&c->d_part_gpos, (size_t)YG_NPART * N * 3 * sizeof(double));

@@ -146,9 +146,14 @@ struct yg_ctx {
   int64_t nlow = 0, nhigh = 0;
   int64_t nneigh = 0;
 
-  // full neighbour list: per sorted atom a slot of `nbr_cap` entries
+  // full neighbour list: per sorted atom a slot of `nbr_cap` entries; the
+  // entries within the pair cutoff (rin_build) fill the slot from the front,
+  // those of the skin shell from the back: d_ncount = (front, back) counts
   uint2 *d_nbr = nullptr;
-  int *d_ncount = nullptr;
+  int2 *d_ncount = nullptr;
+  double rin_build = 0.0;         // the pair cutoff that split the last build's rows
+  int x_fresh = 0;                // the cell-local coordinates are those of the last host build
+  const int *pair_fresh_dev = nullptr;  // while capturing the MD step: device flag "rebuilt this step"
   int64_t nbr_cap = 0;
   int64_t nbr_alloc = 0;          // entries allocated
   int *d_status = nullptr;        // YG_ST_NWORDS

@@ -360,7 +360,11 @@ static int md_step_device(yg_ctx *c, double factor, double skin) {
   if (reci && (rc = yg_launch_ewald_reci(c, 1))) return rc;
   // the build sequence refreshes the cell-local coordinates in any case
   if ((rc = yg_launch_nlist_build_gated(c, c->d_md_ctrl, (unsigned long long *)(c->d_md_ctrl + 4)))) return rc;
-  if ((rc = md_force_async(c, 0, reci))) return rc;
+  // the pair terms read the skin shell of the rows only on steps without a rebuild
+  c->pair_fresh_dev = c->d_md_ctrl;
+  rc = md_force_async(c, 0, reci);
+  c->pair_fresh_dev = nullptr;
+  if (rc) return rc;
   return md_finish_step(c, c->md_dt, 1);
 }
 

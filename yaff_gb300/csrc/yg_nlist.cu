@@ -233,7 +233,7 @@ struct BuildArgs {
   const int *estart;
   const int2 *excl;
   uint2 *nbr;
-  int *ncount;
+  int2 *ncount;     // (front, back) entry counts of every row
   int *status;
   unsigned long long *total;
   int64_t natom;
@@ -242,6 +242,9 @@ struct BuildArgs {
   int rmax[3];
   double rc2;
   float lo, hi;     // FP32 guard band on d^2
+  float rin2;       // FP32 d^2 below which an entry goes to the row's front
+                    // (the pair cutoff squared, with a margin above the
+                    // rounding of either precision's d)
   int fast;
   int filter;       // nlow/nhigh restrict the pairs
   const int *gate;  // device flag: build only when set (nullptr: always)
@@ -292,6 +295,9 @@ __device__ __forceinline__ int exact_decide(const BuildArgs &A, int oi, int oj, 
 }
 
 #define YG_RUN_MAX 8   // cells per contiguous x run of the stencil
+#ifndef YG_BUILD_PIPELINE
+#define YG_BUILD_PIPELINE 0
+#endif
 
 // One warp per sorted atom.  Every (o1, o2) row of the stencil is swept as
 // runs of x-consecutive cells that share one periodic image; the atoms of a
@@ -330,7 +336,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
   const int ci[3] = {cid % N0, (cid / N0) % N1, cid / (N0 * N1)};
   const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
   const bool need_oj = A.filter || A.estart != nullptr || !A.fast;
-  int64_t base = 0;
+  int64_t base = 0, back = 0;  // entries at the row's front and back
   int nexact = 0;
   uint2 *out = A.nbr + i * A.cap;
   const int K0 = A.grid.k[0], K1 = A.grid.k[1], K2 = A.grid.k[2];
@@ -410,8 +416,29 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
       // branch-free FP32 test, the exact replay only for the rare candidates
       // inside the guard band; 32-bit row positions
       const int cap32 = (int)min(A.cap, (int64_t)0x7fffffff);
-      int base32 = (int)base;
+      int base32 = (int)base, back32 = (int)back;
       const unsigned lt = (1u << lane) - 1u;
+#if YG_BUILD_PIPELINE
+      // the next chunk's candidate and coordinates are loaded while this
+      // chunk is tested (one load chain in flight ahead)
+      int qn = min(lane, total - 1);
+      int rqn = map[qn];
+      int4 rrn = run[rqn];
+      int jn = rrn.x + (qn - off[rqn]);
+      float4 xjn = A.xb[jn];
+      for (int q0 = 0; q0 < total; q0 += 32) {
+        const bool live = q0 + lane < total;
+        const int4 rr = rrn;
+        const int j = jn;
+        const float4 xj = xjn;
+        if (q0 + 32 < total) {
+          qn = min(q0 + 32 + lane, total - 1);
+          rqn = map[qn];
+          rrn = run[rqn];
+          jn = rrn.x + (qn - off[rqn]);
+          xjn = A.xb[jn];
+        }
+#else
       for (int q0 = 0; q0 < total; q0 += 32) {
         const int q = min(q0 + lane, total - 1);
         const bool live = q0 + lane < total;
@@ -419,6 +446,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
         const int4 rr = run[rq];
         const int j = rr.x + (q - off[rq]);
         const float4 xj = A.xb[j];
+#endif
         const int oidx = rr.z + __float_as_int(xj.w);
         const float4 sh = A.shift32[oidx];
         const float dx = (xj.x - xi.x) + sh.x;
@@ -437,18 +465,25 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
           in = exact_decide(A, oi, oj, tt, &central);
           nexact++;
         }
-        const unsigned ball = __ballot_sync(0xffffffffu, in);
+        const bool front = d2 < A.rin2;
+        const unsigned bf = __ballot_sync(0xffffffffu, in && front);
+        const unsigned bb = __ballot_sync(0xffffffffu, in && !front);
         if (in) {
-          const int pos = base32 + __popc(ball & lt);
-          if (pos < cap32) out[pos] = make_uint2((unsigned)j, (unsigned)oidx | (central ? YG_META_CENTRAL : 0u));
+          const int pos = front ? base32 + __popc(bf & lt) : back32 + __popc(bb & lt);
+          if (pos < cap32)
+            out[front ? pos : cap32 - 1 - pos] =
+                make_uint2((unsigned)j, (unsigned)oidx | (central ? YG_META_CENTRAL : 0u));
         }
-        base32 += __popc(ball);
+        base32 += __popc(bf);
+        back32 += __popc(bb);
       }
       base = base32;
+      back = back32;
     }
     for (int q0 = (mapped && A.fast && !need_oj) ? total : 0; q0 < total; q0 += 32) {
       const int q = q0 + lane;
       int in = 0, central = 1, oj = -1, oidx = 0, j = 0;
+      bool front = false;
       if (q < total) {
         if (mapped) r = map[q];
         else
@@ -473,6 +508,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
           const float dy = (xj.y - xi.y) + sh.y;
           const float dz = (xj.z - xi.z) + sh.z;
           const float d2 = dx * dx + dy * dy + dz * dz;
+          front = d2 < A.rin2;
           int decided = 0;
           if (A.fast) {
             if (d2 < A.lo) { in = 1; decided = 1; }
@@ -488,27 +524,32 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
           }
         }
       }
-      const unsigned ball = __ballot_sync(0xffffffffu, in);
+      const unsigned bf = __ballot_sync(0xffffffffu, in && front);
+      const unsigned bb = __ballot_sync(0xffffffffu, in && !front);
       if (in) {
         const int code = (central && A.estart) ? excl_code(A.estart, A.excl, oi, oj) : 0;
-        const int64_t p = base + __popc(ball & ((1u << lane) - 1u));
+        const unsigned lt = (1u << lane) - 1u;
+        const int64_t p = front ? base + __popc(bf & lt) : back + __popc(bb & lt);
         if (p < A.cap) {
           const unsigned meta = (unsigned)oidx | ((unsigned)code << YG_META_SCALE_SHIFT) |
                                 (central ? YG_META_CENTRAL : 0u);
-          out[p] = make_uint2((unsigned)j, meta);
+          out[front ? p : A.cap - 1 - p] = make_uint2((unsigned)j, meta);
         }
       }
-      base += __popc(ball);
+      base += __popc(bf);
+      back += __popc(bb);
     }
     __syncwarp();  // the next batch overwrites this warp's runs
   }
   for (int o = 16; o > 0; o >>= 1) nexact += __shfl_down_sync(0xffffffffu, nexact, o);
   if (lane == 0) {
-    A.ncount[i] = (int)min(base, A.cap);
-    if (base > A.cap) atomicOr(A.status + YG_ST_OVERFLOW, 1);
-    atomicMax(A.status + YG_ST_MAXCOUNT, (int)min(base, (int64_t)0x7fffffff));
+    // an overflowing row keeps disjoint segments (its entries are discarded)
+    const int64_t nf = min(base, A.cap), nb = min(back, A.cap - nf), all = base + back;
+    A.ncount[i] = make_int2((int)nf, (int)nb);
+    if (all > A.cap) atomicOr(A.status + YG_ST_OVERFLOW, 1);
+    atomicMax(A.status + YG_ST_MAXCOUNT, (int)min(all, (int64_t)0x7fffffff));
     if (nexact) atomicAdd(A.status + YG_ST_EXACT, nexact);
-    atomicAdd(A.total, (unsigned long long)min(base, A.cap));
+    atomicAdd(A.total, (unsigned long long)(nf + nb));
   }
 }
 
@@ -532,10 +573,10 @@ __global__ void k_export(ExportArgs E) {
   const int cid = A.cell_of[oi];
   const int ci[3] = {cid % A.grid.n[0], (cid / A.grid.n[0]) % A.grid.n[1], cid / (A.grid.n[0] * A.grid.n[1])};
   const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
-  const int cnt = A.ncount[i];
+  const int2 cn = A.ncount[i];
   const int w0 = 2 * A.grid.k[0] + 1, w1 = 2 * A.grid.k[1] + 1;
-  for (int e = lane; e < cnt; e += 32) {
-    uint2 ent = A.nbr[i * A.cap + e];
+  for (int e = lane; e < cn.x + cn.y; e += 32) {
+    uint2 ent = A.nbr[i * A.cap + (e < cn.x ? e : A.cap - cn.y + (e - cn.x))];
     int j = (int)ent.x;
     int oidx = (int)(ent.y & YG_META_OFF_MASK);
     int o0 = oidx % w0 - A.grid.k[0];
@@ -633,6 +674,19 @@ __global__ void k_pack_params(const int *__restrict__ gate, const double *__rest
   dst32[idx] = (float)x;
 }
 
+// The row split of a build: the largest cutoff of the registered pair
+// potentials (the list cutoff when there is none).  The sweep compares its
+// FP32 d^2 with rin^2 (1 + 2e-5): the FP32 d^2 and the d of either pair
+// kernel differ by far less, so no entry within a pair cutoff lands in the
+// back segment.
+double pair_split(const yg_ctx *ctx) {
+  double rin = 0.0;
+  for (int p = 0; p < YG_MAX_POT; p++)
+    if (ctx->pot[p].active && ctx->pot[p].rcut > rin) rin = ctx->pot[p].rcut;
+  if (!(rin > 0.0) || rin > ctx->rcut_total) rin = ctx->rcut_total;
+  return rin;
+}
+
 BuildArgs make_args(yg_ctx *ctx, double rc2) {
   BuildArgs A;
   A.cell = ctx->cell;
@@ -659,6 +713,10 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.rc2 = rc2;
   A.lo = 0.0f;
   A.hi = 0.0f;
+  {
+    const double rin = pair_split(ctx);
+    A.rin2 = (float)(rin * rin * (1.0 + 2e-5));
+  }
   A.fast = 0;
   A.filter = (ctx->nlow > 0 || ctx->nhigh < ctx->natom) ? 1 : 0;
   A.gate = nullptr;
@@ -708,6 +766,7 @@ int yg_launch_prep_positions(yg_ctx *ctx) {
       ctx->d_pos, ctx->have_charges ? ctx->d_charge : nullptr, ctx->d_sorted, ctx->d_org, ctx->d_cell_of,
       ctx->grid.n[0], ctx->natom, ctx->d_x64, ctx->d_x32, ctx->d_xb);
   YG_LAUNCH_CHECK(ctx, "k_prep");
+  ctx->x_fresh = 0;  // the rows no longer match the coordinates (a host build sets it again)
   return YG_OK;
 }
 
@@ -994,6 +1053,8 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   ctx->have_list = 1;
   ctx->rows_valid = 1;
   ctx->list_recomputed = 0;
+  ctx->rin_build = pair_split(ctx);
+  ctx->x_fresh = 1;
   // the sorted order changed: repack the pair parameters
   if ((rc_ = yg_pack_pair_params(ctx))) return rc_;
   return YG_OK;
@@ -1010,6 +1071,7 @@ int yg_launch_nlist_build_gated(yg_ctx *ctx, const int *gate, unsigned long long
   }
   const double rc2 = ctx->rcut_total * ctx->rcut_total;
   if ((rc_ = enqueue_build(ctx, rc2, gate, total))) return rc_;
+  ctx->rin_build = pair_split(ctx);
   k_pack_params<<<yg_blocks(ctx->natom * 4 * YG_MAX_POT, 256), 256, 0, ctx->stream>>>(gate, ctx->d_pp_src, ctx->d_sorted, ctx->natom,
                                                                      ctx->d_pp64, ctx->d_pp32);
   YG_LAUNCH_CHECK(ctx, "k_pack_params");

@@ -27,7 +27,12 @@ struct PairArgs {
   int64_t natom;
   int64_t cap;
   const uint2 *nbr;
-  const int *ncount;
+  const int2 *ncount;         // (front, back) entries of every row
+  // the back segment (the skin shell beyond every pair cutoff at the build)
+  // is read unless the coordinates are those of the build: fresh is a device
+  // flag (nonzero: rebuilt this step) or null, then `back` decides
+  const int *fresh;
+  int back;
   const int *sorted;
   const double4_32a *x64;
   const float4 *x32;
@@ -200,8 +205,12 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
       for (int k = 0; k < 4; k++)
         pi[p][k] = (MODE == YG_FP64) ? (T)A.pp64[i * 4 * YG_MAX_POT + 4 * A.pot[p].col + k]
                                      : (T)A.pp32[i * 4 * YG_MAX_POT + 4 * A.pot[p].col + k];
-    const int cnt = A.ncount[i];
+    const int2 cn = A.ncount[i];
+    const bool use_back = A.fresh ? (*A.fresh == 0) : (A.back != 0);
+    const int cnt = cn.x + (use_back ? cn.y : 0);
+    // entry e of the row: the front segment, then the back one
     const uint2 *row = A.nbr + i * A.cap;
+    const uint2 *rowb = row + (A.cap - cn.y - cn.x);
     if (K0 >= 0) {
       // compile-time potential kinds (mixed modes): every term is evaluated
       // and masked with d < r_c and a nonzero scale, no per-entry dispatch
@@ -212,10 +221,10 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
         for (int k = 0; k < 4; k++) fpi[p][k] = (float)pi[p][k];
       const float fxi = (float)xi, fyi = (float)yi, fzi = (float)zi, fqi = (float)qi;
       // the next entry of the lane is loaded one step ahead
-      uint2 ent_next = lane < cnt ? row[lane] : make_uint2(0u, 0u);
+      uint2 ent_next = lane < cnt ? (lane < cn.x ? row : rowb)[lane] : make_uint2(0u, 0u);
       for (int e = lane; e < cnt; e += 32) {
         const uint2 ent = ent_next;
-        if (e + 32 < cnt) ent_next = row[e + 32];
+        if (e + 32 < cnt) ent_next = (e + 32 < cn.x ? row : rowb)[e + 32];
         const int j = (int)ent.x;
         const int oidx = (int)(ent.y & YG_META_OFF_MASK);
         const int code = (int)((ent.y >> YG_META_SCALE_SHIFT) & 7u);
@@ -236,7 +245,7 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
       }
     }
     for (int e = (K0 >= 0) ? cnt : lane; e < cnt; e += 32) {
-      const uint2 ent = row[e];
+      const uint2 ent = (e < cn.x ? row : rowb)[e];
       const int j = (int)ent.x;
       const int oidx = (int)(ent.y & YG_META_OFF_MASK);
       const int code = (int)((ent.y >> YG_META_SCALE_SHIFT) & 7u);
@@ -443,7 +452,7 @@ int launch_pair_t(yg_ctx *ctx, PairArgs &A, int nblocks) {
 // two potentials without truncation (EI without radii, alpha > 0).
 template <int K0, int K1>
 int launch_pair_k(yg_ctx *ctx, PairArgs &A, int nblocks) {
-  if (K1 < 0) k_pair<YG_MIXED, 1, K0, K1><<<nblocks, 256, 0, ctx->stream>>>(A);
+  if constexpr (K1 < 0) k_pair<YG_MIXED, 1, K0, K1><<<nblocks, 256, 0, ctx->stream>>>(A);
   else k_pair<YG_MIXED, 2, K0, K1><<<nblocks, 256, 0, ctx->stream>>>(A);
   YG_LAUNCH_CHECK(ctx, "k_pair");
   return YG_OK;
@@ -519,6 +528,15 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   A.cap = ctx->nbr_cap;
   A.nbr = ctx->d_nbr;
   A.ncount = ctx->d_ncount;
+  {
+    // the back segment can be skipped when no potential reaches beyond the
+    // build's split and the coordinates are those the rows were built from
+    bool split_ok = true;
+    for (int q = 0; q < npot; q++)
+      if (A.pot[q].rcut > ctx->rin_build) split_ok = false;
+    A.fresh = split_ok ? ctx->pair_fresh_dev : nullptr;
+    A.back = (split_ok && ctx->x_fresh) ? 0 : 1;
+  }
   A.sorted = ctx->d_sorted;
   A.x64 = ctx->d_x64;
   A.x32 = ctx->d_x32;
