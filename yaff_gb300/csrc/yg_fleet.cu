@@ -8,7 +8,8 @@
 // cell, cutoffs, counters and state.  One MD step of every system in flight
 // is eight launches, whatever the number of systems:
 //   drift     (atom)   first half kick and drift; displacement since the
-//                      last build; fractional coordinates (FP32 hi + lo)
+//                      last build; fractional coordinates (FP32 hi + lo);
+//                      the atom's phase tables exp(2 pi i g s) per axis
 //   gate      (system) the reference's skin rule per system
 //                      (yaff/pes/nlist.py:207-218)
 //   build     (tile)   neighbour rows of the systems whose gate fired:
@@ -20,9 +21,13 @@
 //   pair      (atom)   LJ + real-space EI over the row in FP32, the relative
 //                      vector refreshed by the displacements since the build
 //                      (the reference's skin path, nlist.c:183-232)
-//   sfac      (k)      structure factors S(k) of each system's half sphere,
-//                      and the FP32 coefficients 2 A(k) S(k) of the gradient
-//   ewald     (atom)   reciprocal-space gradient from those coefficients
+//   sfac      (k)      structure factors S(k) of each system's half sphere
+//                      (a block of 128 k vectors sweeps the system's atoms
+//                      in tiles of 32 whose phase tables it stages in shared
+//                      memory: a phase is two complex products), and the
+//                      FP32 coefficients 2 A(k) S(k) of the gradient
+//   ewald     (atom)   reciprocal-space gradient from those coefficients and
+//                      the atom's own phase tables
 //   kick      (atom)   total gradient, second half kick, kinetic energy
 //   finish    (system) fixed-order energy sums, the log row, the counters
 // Every reduction over a system runs inside that system's own threads in a
@@ -47,7 +52,8 @@
 #include "yg_pairterm.cuh"
 
 #define FL_TILE 128    // atoms per build tile and per atom-range granule
-#define FL_KGRAN 32    // k-vector range granule
+#define FL_KGRAN 128   // k-vector range granule (a structure-factor block lies in one system)
+#define FL_TAB 64      // phase-table slots per atom: (G0 + 1) + (G1 + 1) + (G2 + 1) at most
 #define FL_RMAX 2      // periodic images searched per axis, at most
 #define FL_SHIFTS ((2 * FL_RMAX + 3) * (2 * FL_RMAX + 3) * (2 * FL_RMAX + 3))
 
@@ -58,6 +64,7 @@ struct FleetSys {
   int rebuild;    // the gate fired this step
   int overflow;   // a row ran out of slots at the last build
   int rmax[3];    // periodic images searched per axis
+  int gmax[3];    // reciprocal-lattice extent per axis (phase-table slots G + 1 each)
   int step;       // steps completed
   int nsteps;     // steps requested
   unsigned maxd2; // bits of the largest squared displacement since the last build (FP32, >= 0)
@@ -79,8 +86,12 @@ struct FleetDev {
   int4 *nbr;                // (j, FP32 relative vector at the build)
   // k vectors
   int4 *kg;                 // (g0, g1, g2, system or -1)
-  float4 *kgf;              // (g0, g1, g2, 2 A(k) Re S(k)) as FP32
-  float4 *kv;               // (kx, ky, kz, 2 A(k) Im S(k))
+  float4 *kv;               // (kx, ky, kz, 0)
+  float2 *kcoef;            // 2 A(k) S(k) as FP32 (written by the S pass)
+  int *kslot;               // phase-table slots |g0|, off1 + |g1|, off2 + g2 (8 bits each), then
+                            // bit 24: g0 < 0, bit 25: g1 < 0 (conjugate)
+  float2 *ptab;             // [slot][atom] exp(2 pi i g s_axis), slot = axis offset + |g|
+  int64_t acap;             // atom capacity (the slot stride of ptab)
   double *kpref;            // A(k) = 4 pi / V exp(-k^2 / 4 alpha^2) / k^2
   double2 *S;
   // systems
@@ -155,6 +166,18 @@ __global__ void k_fl_drift(FleetDev F, int64_t natom_cap) {
   }
   F.fhi[i] = make_float4(sh[0], sh[1], sh[2], 0.f);
   F.flo[i] = make_float4(sl[0], sl[1], sl[2], 0.f);
+  // phase tables: g s reduced exactly mod 1 (frac_gs), then one sincospi
+  {
+    int off = 0;
+    for (int k = 0; k < 3; k++) {
+      for (int g = 0; g <= S.gmax[k]; g++) {
+        float sn, cs;
+        sincospif(2.0f * frac_gs((float)g, sh[k], sl[k]), &sn, &cs);
+        F.ptab[(int64_t)(off + g) * F.acap + i] = make_float2(cs, sn);
+      }
+      off += S.gmax[k] + 1;
+    }
+  }
   // the position wrapped into the cell, as FP32 hi + lo
   double fl[3], rw[3];
   for (int k = 0; k < 3; k++) fl[k] = floor(S.gv[3 * k] * r[0] + S.gv[3 * k + 1] * r[1] + S.gv[3 * k + 2] * r[2]);
@@ -335,55 +358,99 @@ __global__ void k_fl_pair(FleetDev F, int64_t natom_cap) {
   F.epair[i] = (double)e - (double)ce;
 }
 
-// S(k) of every reciprocal vector of every system, one thread per k; then
-// the FP32 coefficients 2 A(k) S(k) that the gradient pass reads.
-__global__ void k_fl_sfac(FleetDev F, int64_t nk_cap) {
-  const int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (kk >= nk_cap) return;
-  const int4 g = F.kg[kk];
-  if (g.w < 0) return;
-  const FleetSys &S = F.d_sys[g.w];
-  if (S.state != 1) return;
-  const float4 gf = F.kgf[kk];
-  float cr = 0.f, ci = 0.f, kr = 0.f, ki = 0.f;
-  for (int64_t a = S.a0; a < S.a0 + S.n; a++) {
-    const float4 hi = F.fhi[a], lo = F.flo[a];
-    const float t = frac_gs(gf.x, hi.x, lo.x) + frac_gs(gf.y, hi.y, lo.y) + frac_gs(gf.z, hi.z, lo.z);
-    float sn, cs;
-    sincospif(2.0f * t, &sn, &cs);
-    const float qa = F.q[a];
-    kahan_add(cr, kr, qa * cs);
-    kahan_add(ci, ki, qa * sn);
-  }
-  const double sr = (double)cr - (double)kr, si = (double)ci - (double)ki, a2 = 2.0 * F.kpref[kk];
-  F.S[kk] = make_double2(sr, si);
-  F.kgf[kk].w = (float)(a2 * sr);
-  F.kv[kk].w = (float)(a2 * si);
+// The phase exp(i k.r) of a k vector from an atom's tables (conjugates for
+// negative g0, g1): two complex products.
+__device__ __forceinline__ float2 fl_phase(float2 e0, float2 e1, float2 e2, int ks) {
+  const float y0 = (ks >> 24) & 1 ? -e0.y : e0.y, y1 = (ks >> 25) & 1 ? -e1.y : e1.y;
+  const float pr = e0.x * e1.x - y0 * y1, pi = e0.x * y1 + y0 * e1.x;
+  return make_float2(pr * e2.x - pi * e2.y, pr * e2.y + pi * e2.x);
 }
 
-// Reciprocal-space gradient of every atom from its system's coefficients.
-__global__ void k_fl_ewald(FleetDev F, int64_t natom_cap) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= natom_cap) return;
-  const int s = F.sysid[i];
+// S(k) of 128 reciprocal vectors of one system per block (k ranges are
+// aligned to 128); the system's atoms are swept in tiles of 32 whose phase
+// tables and charges are staged in shared memory.  Then the FP32
+// coefficients 2 A(k) S(k) that the gradient pass reads.
+__global__ void __launch_bounds__(128) k_fl_sfac(FleetDev F, int64_t nk_cap) {
+  __shared__ float2 tab[FL_TAB][33];
+  __shared__ float sq[32];
+  const int64_t kb = (int64_t)blockIdx.x * 128;
+  if (kb >= nk_cap) return;
+  const int s = F.kg[kb].w;
   if (s < 0) return;
   const FleetSys &S = F.d_sys[s];
   if (S.state != 1) return;
-  const float4 hi = F.fhi[i], lo = F.flo[i];
-  const float qi = F.q[i];
-  float gx = 0.f, gy = 0.f, gz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  if (qi != 0.f) {
-    for (int64_t kk = S.k0; kk < S.k0 + S.nk; kk++) {
-      const float4 g = F.kgf[kk], k = F.kv[kk];
-      const float t = frac_gs(g.x, hi.x, lo.x) + frac_gs(g.y, hi.y, lo.y) + frac_gs(g.z, hi.z, lo.z);
-      float sn, cs;
-      sincospif(2.0f * t, &sn, &cs);
-      const float x = qi * (k.w * cs - g.w * sn);
-      kahan_add(gx, cx, k.x * x);
-      kahan_add(gy, cy, k.y * x);
-      kahan_add(gz, cz, k.z * x);
+  const int64_t kk = kb + threadIdx.x;
+  const bool mine = F.kg[kk].w == s;  // the rest of the granule is padding
+  const int ks = mine ? F.kslot[kk] : 0;
+  const int s0 = ks & 255, s1 = (ks >> 8) & 255, s2 = (ks >> 16) & 255;
+  const int ntab = S.gmax[0] + S.gmax[1] + S.gmax[2] + 3;
+  const int64_t a1 = (int64_t)S.a0 + S.n;
+  float cr = 0.f, ci = 0.f, kr = 0.f, ki = 0.f;
+  for (int64_t at = S.a0; at < a1; at += 32) {
+    const int na = (int)(a1 - at < 32 ? a1 - at : 32);
+    for (int idx = threadIdx.x; idx < ntab * 32; idx += 128) {
+      const int sl = idx >> 5, a = idx & 31;
+      tab[sl][a] = a < na ? F.ptab[(int64_t)sl * F.acap + at + a] : make_float2(0.f, 0.f);
     }
+    if (threadIdx.x < 32) sq[threadIdx.x] = (int)threadIdx.x < na ? F.q[at + threadIdx.x] : 0.f;
+    __syncthreads();
+    for (int a = 0; a < na; a++) {
+      const float2 p = fl_phase(tab[s0][a], tab[s1][a], tab[s2][a], ks);
+      const float qa = sq[a];
+      kahan_add(cr, kr, qa * p.x);
+      kahan_add(ci, ki, qa * p.y);
+    }
+    __syncthreads();
   }
+  if (!mine) return;
+  const double sr = (double)cr - (double)kr, si = (double)ci - (double)ki, a2 = 2.0 * F.kpref[kk];
+  F.S[kk] = make_double2(sr, si);
+  F.kcoef[kk] = make_float2((float)(a2 * sr), (float)(a2 * si));
+}
+
+// Reciprocal-space gradient of every atom of a 128-atom tile (one system)
+// from its own phase tables and the system's coefficients, staged 128 k
+// vectors at a time.
+__global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap) {
+  __shared__ int sks[128];
+  __shared__ float4 skv[128];
+  __shared__ float2 scf[128];
+  const int64_t i0 = (int64_t)blockIdx.x * 128;
+  if (i0 >= natom_cap) return;
+  const int s = F.sysid[i0];
+  if (s < 0) return;
+  const FleetSys &S = F.d_sys[s];
+  if (S.state != 1) return;
+  const int64_t i = i0 + threadIdx.x;
+  const bool vi = i < (int64_t)S.a0 + S.n;
+  const float qi = vi ? F.q[i] : 0.f;
+  const float2 *pt = F.ptab + i;
+  float gx = 0.f, gy = 0.f, gz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  const int64_t k1 = (int64_t)S.k0 + S.nk;
+  for (int64_t kc = S.k0; kc < k1; kc += 128) {
+    const int nkc = (int)(k1 - kc < 128 ? k1 - kc : 128);
+    if ((int)threadIdx.x < nkc) {
+      sks[threadIdx.x] = F.kslot[kc + threadIdx.x];
+      skv[threadIdx.x] = F.kv[kc + threadIdx.x];
+      scf[threadIdx.x] = F.kcoef[kc + threadIdx.x];
+    }
+    __syncthreads();
+    if (vi && qi != 0.f) {
+      for (int q = 0; q < nkc; q++) {
+        const int ks = sks[q];
+        const float2 p = fl_phase(pt[(int64_t)(ks & 255) * F.acap], pt[(int64_t)((ks >> 8) & 255) * F.acap],
+                                  pt[(int64_t)((ks >> 16) & 255) * F.acap], ks);
+        const float2 c = scf[q];
+        const float4 k = skv[q];
+        const float x = qi * (c.y * p.x - c.x * p.y);
+        kahan_add(gx, cx, k.x * x);
+        kahan_add(gy, cy, k.y * x);
+        kahan_add(gz, cz, k.z * x);
+      }
+    }
+    __syncthreads();
+  }
+  if (!vi) return;
   F.gew[3 * i] = (double)gx - (double)cx;
   F.gew[3 * i + 1] = (double)gy - (double)cy;
   F.gew[3 * i + 2] = (double)gz - (double)cz;
@@ -457,8 +524,8 @@ __global__ void k_fl_finish(FleetDev F, int nsys) {
 
 void fl_free(yg_fleet *f) {
   void *bufs[] = {f->d.pos, f->d.vel, f->d.pos_build, f->d.invm, f->d.gtot, f->d.gpair, f->d.gew, f->d.epair, f->d.ekin, f->d.q,
-                  f->d.sig, f->d.seps, f->d.disp, f->d.fhi, f->d.flo, f->d.chi, f->d.clo, f->d.sysid, f->d.ncount, f->d.nbr, f->d.kg, f->d.kgf,
-                  f->d.kv, f->d.kpref, f->d.S, f->d.d_sys, f->d.log};
+                  f->d.sig, f->d.seps, f->d.disp, f->d.fhi, f->d.flo, f->d.chi, f->d.clo, f->d.sysid, f->d.ncount, f->d.nbr, f->d.kg, f->d.kcoef,
+                  f->d.kslot, f->d.ptab, f->d.kv, f->d.kpref, f->d.S, f->d.d_sys, f->d.log};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (f->h_sys_pinned) cudaFreeHost(f->h_sys_pinned);
@@ -474,8 +541,8 @@ int fl_launch_step(yg_fleet *f, cudaStream_t st) {
   k_fl_gate<<<(f->max_systems + 127) / 128, 128, 0, st>>>(f->d, f->max_systems);
   k_fl_build<<<(int)(A / FL_TILE), FL_TILE, 0, st>>>(f->d, A / FL_TILE);
   k_fl_pair<<<nb, 256, 0, st>>>(f->d, A);
-  k_fl_sfac<<<(int)((K + 127) / 128), 128, 0, st>>>(f->d, K);
-  k_fl_ewald<<<nb, 256, 0, st>>>(f->d, A);
+  k_fl_sfac<<<(int)(K / 128), 128, 0, st>>>(f->d, K);
+  k_fl_ewald<<<(int)(A / 128), 128, 0, st>>>(f->d, A);
   k_fl_kick<<<nb, 256, 0, st>>>(f->d, A);
   k_fl_finish<<<f->max_systems, 256, 0, st>>>(f->d, f->max_systems);
   cudaError_t e = cudaGetLastError();
@@ -507,6 +574,7 @@ int yg_fleet_create(int64_t max_atoms, int max_systems, int64_t max_k, int max_n
   f->max_k = (max_k + FL_KGRAN - 1) / FL_KGRAN * FL_KGRAN;
   f->max_systems = max_systems;
   f->d.cap = (max_neighbors + 31) / 32 * 32;
+  f->d.acap = f->max_atoms;
   f->d.max_steps = max_steps;
   if (stream) {
     f->stream = (cudaStream_t)stream;
@@ -527,8 +595,8 @@ int yg_fleet_create(int64_t max_atoms, int max_systems, int64_t max_k, int max_n
       {(void **)&f->d.q, Au * 4}, {(void **)&f->d.sig, Au * 4}, {(void **)&f->d.seps, Au * 4},
       {(void **)&f->d.disp, Au * 16}, {(void **)&f->d.chi, Au * 16}, {(void **)&f->d.clo, Au * 16}, {(void **)&f->d.fhi, Au * 16},
       {(void **)&f->d.flo, Au * 16}, {(void **)&f->d.sysid, Au * 4}, {(void **)&f->d.ncount, Au * 4},
-      {(void **)&f->d.nbr, (size_t)Au * f->d.cap * 16}, {(void **)&f->d.kg, Ku * 16}, {(void **)&f->d.kgf, Ku * 16},
-      {(void **)&f->d.kv, Ku * 16},
+      {(void **)&f->d.nbr, (size_t)Au * f->d.cap * 16}, {(void **)&f->d.kg, Ku * 16}, {(void **)&f->d.kcoef, Ku * 8},
+      {(void **)&f->d.kslot, Ku * 4}, {(void **)&f->d.ptab, Au * FL_TAB * 8}, {(void **)&f->d.kv, Ku * 16},
       {(void **)&f->d.kpref, Ku * 8}, {(void **)&f->d.S, Ku * 16}, {(void **)&f->d.d_sys, (size_t)max_systems * sizeof(FleetSys)},
       {(void **)&f->d.log, (size_t)max_systems * (max_steps + 1) * 16}};
   for (auto &b : bufs) {
@@ -611,6 +679,11 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
     const double gsp = 1.0 / std::sqrt(R[3 * k] * R[3 * k] + R[3 * k + 1] * R[3 * k + 1] + R[3 * k + 2] * R[3 * k + 2]);
     rmax[k] = (int)std::ceil((rcut + skin) / rsp - 0.5);
     gmax[k] = (int)std::ceil(gcut / gsp - 0.5);
+    if (k == 2 && gmax[0] + gmax[1] + gmax[2] + 3 > FL_TAB) {
+      yg_set_error("yg_fleet_add: too many reciprocal vectors per axis for the phase tables (raise the Ewald "
+                   "alpha or lower gcut)");
+      return YG_ERR_ARG;
+    }
     if (rmax[k] > FL_RMAX) {
       yg_set_error("yg_fleet_add: the cell is too small for rcut + skin (more than two periodic images per axis)");
       return YG_ERR_ARG;
@@ -622,7 +695,8 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
   double gc2 = gcut * tp;
   gc2 *= gc2;
   std::vector<int4> kg;
-  std::vector<float4> kv, kgf;
+  std::vector<float4> kv;
+  std::vector<int> ksl;
   std::vector<double> kp;
   for (int g0 = -gmax[0]; g0 <= gmax[0]; g0++)
     for (int g1 = -gmax[1]; g1 <= gmax[1]; g1++)
@@ -634,7 +708,8 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
         if (ksq > gc2) continue;
         kg.push_back(make_int4(g0, g1, g2, s));
         kv.push_back(make_float4((float)k[0], (float)k[1], (float)k[2], 0.f));
-        kgf.push_back(make_float4((float)g0, (float)g1, (float)g2, 0.f));
+        ksl.push_back(std::abs(g0) | ((gmax[0] + 1 + std::abs(g1)) << 8) | ((gmax[0] + gmax[1] + 2 + g2) << 16) |
+                      ((g0 < 0) << 24) | ((g1 < 0) << 25));
         kp.push_back(fac1 * std::exp(-ksq * fac2) / ksq);
       }
   const int ag = (int)((natom + FL_TILE - 1) / FL_TILE);
@@ -653,7 +728,10 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
   S.nk = (int)kg.size();
   S.state = 1;
   S.init = 1;
-  for (int k = 0; k < 3; k++) S.rmax[k] = rmax[k];
+  for (int k = 0; k < 3; k++) {
+    S.rmax[k] = rmax[k];
+    S.gmax[k] = gmax[k];
+  }
   S.nsteps = (int)nsteps;
   std::memcpy(S.rv, R, sizeof(R));
   std::memcpy(S.gv, G, sizeof(G));
@@ -696,7 +774,7 @@ int yg_fleet_add(yg_fleet *f, int64_t natom, const double *pos, const double *ve
   YG_CUDA(cudaMemsetAsync(f->d.gtot + 3 * a0, 0, natom * 24, st));
   YG_CUDA(cudaMemsetAsync(f->d.ncount + a0, 0, (size_t)ag * FL_TILE * 4, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kv + S.k0, kv.data(), kv.size() * 16, h2d, st));
-  YG_CUDA(cudaMemcpyAsync(f->d.kgf + S.k0, kgf.data(), kgf.size() * 16, h2d, st));
+  YG_CUDA(cudaMemcpyAsync(f->d.kslot + S.k0, ksl.data(), ksl.size() * 4, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kpref + S.k0, kp.data(), kp.size() * 8, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.kg + S.k0, kg.data(), kg.size() * 16, h2d, st));
   YG_CUDA(cudaMemcpyAsync(f->d.d_sys + s, &S, sizeof(S), h2d, st));

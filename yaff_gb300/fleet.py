@@ -32,8 +32,8 @@ NEIGHBOR_SLOTS = 512
 
 def fleet_bytes(max_atoms, max_systems, max_k, max_neighbors=NEIGHBOR_SLOTS, max_steps=64):
     """Device memory a fleet of these capacities allocates."""
-    per_atom = 6 * 24 + 3 * 8 + 3 * 4 + 5 * 16 + 2 * 4 + 16 * max_neighbors
-    return int(max_atoms * per_atom + max_k * (16 + 16 + 16 + 8 + 16) + max_systems * (240 + 16 * (max_steps + 1)))
+    per_atom = 6 * 24 + 3 * 8 + 3 * 4 + 5 * 16 + 2 * 4 + 64 * 8 + 16 * max_neighbors
+    return int(max_atoms * per_atom + max_k * (16 + 8 + 4 + 16 + 8 + 16) + max_systems * (240 + 16 * (max_steps + 1)))
 
 
 class Fleet(object):
