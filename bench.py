@@ -46,6 +46,8 @@ def parse():
                     help='requests of the serving workload run after the main measurement (0: skip)')
     ap.add_argument('--serving-rate', type=float, default=200.0, help='Poisson arrival rate, requests/s')
     ap.add_argument('--serving-slots', type=int, default=16)
+    ap.add_argument('--serving-fleet-only', action='store_true',
+                    help='serving: the fleet engine only (no per-context engine, no sequential FP64 baseline)')
     ap.add_argument('--mc-rounds', type=int, default=10, help='MC trial-energy batches per precision (0: skip)')
     ap.add_argument('--nve-steps', type=int, default=1000, help='steps of the 24,000-atom water NVE run (0: skip)')
     return ap.parse_args()
@@ -801,6 +803,8 @@ def run_serving(args):
     out['saturated_latency_p99_ms'] = sweep[-1]['latency_p99_ms']
     out['saturated_atom_steps_per_s'] = sweep[-1]['atom_steps_per_s']
     eng.close()
+    if args.serving_fleet_only:
+        return out
     # the per-system-context engine (one yg_ctx, stream and graph per request)
     nc = min(n, 1024)
     budget = 16 << 30

@@ -230,25 +230,36 @@ __device__ __forceinline__ void mc_pair64(const McDev &D, const double *ga, doub
 
 // The same pair, mixed: the minimum-image fractional difference from the
 // 32-bit fixed-point fractions (exact integer wrap), FP32 Cartesian vector
-// and terms; pairs closer than D.near (where the terms are large:
-// erfc(alpha d) > 5e-3) or within 1e-6 of the cutoff are recomputed in FP64
-// from the FP64 fractions on the same image, so the energy difference keeps
-// ~1e-9 Ha absolute accuracy.  Parameters come as float for the FP32 terms
-// and through pa/pj64 (q, sigma, sqrt eps) for the FP64 ones.
-__device__ __forceinline__ void mc_pair32(const McDev &D, const double *fa, const unsigned *xa, float qa, float sa,
-                                          float ea, const double *pa64, const double *fj, const unsigned *xj,
-                                          float qj, float sj, float ej, const double *pj64, McSum &acc) {
+// and terms.  Pairs closer than D.near (where the terms are large:
+// erfc(alpha d) > 5e-3) or within 1e-6 of the cutoff are not evaluated here:
+// they go to the warp's queue of deferred pairs (ballot-compacted, so that
+// the FP64 terms later run on full warps instead of on the few lanes of a
+// warp that meet such a pair) and are recomputed in FP64 from the FP64
+// fractions on the same image, so the energy difference keeps ~1e-9 Ha
+// absolute accuracy.  All lanes of the warp call this together (valid marks
+// the lanes with a real pair); code = guest atom | side << 2.
+#define MC_QCAP 64  // deferred pairs per warp (a flush at 32 leaves at most 31)
+
+struct McDefer {
+  int j;         // other atom: framework index (sides 0, 2) or guest-slot index u (sides 1, 3)
+  int code;      // guest atom | side << 2 | (r0 + 8) << 4 | (r1 + 8) << 9 | (r2 + 8) << 14
+};
+
+template <typename Drain>
+__device__ __forceinline__ void mc_pair32(const McDev &D, const unsigned *xa, float qa, float sa, float ea,
+                                          const unsigned *xj, float qj, float sj, float ej, bool valid, int j,
+                                          int code, McSum &acc, McDefer *wq, int &qn, unsigned lt, Drain &drain) {
   int di[3];
-  float s[3];
+  float sfr[3];
 #pragma unroll
   for (int x = 0; x < 3; x++) {
-    di[x] = (int)(xj[x] - xa[x]);
-    s[x] = (float)di[x] * 2.3283064365386963e-10f;  // 2^-32
+    di[x] = valid ? (int)(xj[x] - xa[x]) : 0;
+    sfr[x] = (float)di[x] * 2.3283064365386963e-10f;  // 2^-32
   }
   float d0[3];
 #pragma unroll
-  for (int x = 0; x < 3; x++) d0[x] = s[0] * D.rvf[x] + s[1] * D.rvf[3 + x] + s[2] * D.rvf[6 + x];
-  acc.dmin2f = fminf(acc.dmin2f, d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
+  for (int x = 0; x < 3; x++) d0[x] = sfr[0] * D.rvf[x] + sfr[1] * D.rvf[3 + x] + sfr[2] * D.rvf[6 + x];
+  if (valid) acc.dmin2f = fminf(acc.dmin2f, d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
   for (int r0 = -D.rmax[0]; r0 <= D.rmax[0]; r0++)
     for (int r1 = -D.rmax[1]; r1 <= D.rmax[1]; r1++)
       for (int r2 = -D.rmax[2]; r2 <= D.rmax[2]; r2++) {
@@ -257,38 +268,73 @@ __device__ __forceinline__ void mc_pair32(const McDev &D, const double *fa, cons
         for (int x = 0; x < 3; x++)
           d[x] = d0[x] + (float)r0 * D.rvf[x] + (float)r1 * D.rvf[3 + x] + (float)r2 * D.rvf[6 + x];
         const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (d2 >= D.rc2f_hi) continue;
-        if (d2 < D.near2f || d2 > D.rc2f_lo) {
-          // FP64 fractional difference on the image the fixed-point wrap chose
-          double u[3];
-#pragma unroll
-          for (int x = 0; x < 3; x++) {
-            const double t = fj[x] - fa[x];
-            u[x] = t - rint(t - (double)di[x] * 2.3283064365386963e-10);
-          }
-          u[0] += r0;
-          u[1] += r1;
-          u[2] += r2;
-          double c[3];
-#pragma unroll
-          for (int x = 0; x < 3; x++) c[x] = u[0] * D.cell.rv[x] + u[1] * D.cell.rv[3 + x] + u[2] * D.cell.rv[6 + x];
-          const double d2d = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-          if (d2d < D.rc2) mc_terms64(D, sqrt(d2d), d2d, pa64[0], pa64[1], pa64[2], pj64[0], pj64[1], pj64[2], acc);
-          continue;
+        const bool in = valid && d2 < D.rc2f_hi;
+        const bool defer = in && (d2 < D.near2f || d2 > D.rc2f_lo);
+        if (in && !defer) {
+          PairPotDev lj, ei;
+          lj.kind = YG_POT_LJ;
+          lj.tr_kind = YG_TR_NONE;
+          ei.kind = YG_POT_EI;
+          ei.tr_kind = YG_TR_NONE;
+          const float inv_d = rsqrtf(d2);
+          const float dd = d2 * inv_d;
+          float v, g, v2;
+          pair_term_f32(lj, 0.f, 0.f, 0.f, 1.f, dd, d2, inv_d, sa, ea, 0.f, 0.f, sj, ej, 0.f, 0.f, 0.f, 0.f, v, g);
+          pair_term_f32(ei, 0.f, 0.f, D.alphaf, D.inv_dielf, dd, d2, inv_d, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f,
+                        qa, qj, v2, g);
+          acc.add32(v + v2);
         }
-        PairPotDev lj, ei;
-        lj.kind = YG_POT_LJ;
-        lj.tr_kind = YG_TR_NONE;
-        ei.kind = YG_POT_EI;
-        ei.tr_kind = YG_TR_NONE;
-        const float inv_d = rsqrtf(d2);
-        const float dd = d2 * inv_d;
-        float v, g, v2;
-        pair_term_f32(lj, 0.f, 0.f, 0.f, 1.f, dd, d2, inv_d, sa, ea, 0.f, 0.f, sj, ej, 0.f, 0.f, 0.f, 0.f, v, g);
-        pair_term_f32(ei, 0.f, 0.f, D.alphaf, D.inv_dielf, dd, d2, inv_d, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, qa,
-                      qj, v2, g);
-        acc.add32(v + v2);
+        const unsigned b = __ballot_sync(0xffffffffu, defer);
+        if (defer) {
+          McDefer e;
+          e.j = j;
+          e.code = code | ((r0 + 8) << 4) | ((r1 + 8) << 9) | ((r2 + 8) << 14);
+          wq[qn + __popc(b & lt)] = e;
+        }
+        qn += __popc(b);
+        drain(false);  // at most 31 left: the next image's pairs fit
       }
+}
+
+// FP64 terms of deferred pairs 0 .. n-1 of the warp's queue, one per lane;
+// the energies go to e[side].
+__device__ __forceinline__ void mc_flush(const McDev &D, const McDefer *wq, int n, int lane, int64_t gbase,
+                                         const double *fold, const double *fnew, const unsigned *xold,
+                                         const unsigned *xnew, double (&e)[4]) {
+  if (lane >= n) return;
+  const McDefer q = wq[lane];
+  const int a = q.code & 3, side = (q.code >> 2) & 3;
+  const int r[3] = {((q.code >> 4) & 31) - 8, ((q.code >> 9) & 31) - 8, ((q.code >> 14) & 31) - 8};
+  const double *fa = ((side & 2) ? fnew : fold) + 3 * a;
+  const unsigned *xa = ((side & 2) ? xnew : xold) + 3 * a;
+  const double *fj, *pj;
+  const unsigned *xj;
+  if (side & 1) {
+    fj = D.gfrac + (gbase + q.j) * 3;
+    xj = D.gfix + (gbase + q.j) * 3;
+    pj = D.gpar[q.j % D.M];
+  } else {
+    fj = D.ffrac + 3 * (int64_t)q.j;
+    xj = D.ffix + 3 * (int64_t)q.j;
+    pj = (const double *)(D.fpar + q.j);
+  }
+  // FP64 fractional difference on the image the fixed-point wrap chose
+  double u[3];
+#pragma unroll
+  for (int x = 0; x < 3; x++) {
+    const double t = fj[x] - fa[x];
+    u[x] = t - rint(t - (double)(int)(xj[x] - xa[x]) * 2.3283064365386963e-10) + r[x];
+  }
+  double c[3];
+#pragma unroll
+  for (int x = 0; x < 3; x++) c[x] = u[0] * D.cell.rv[x] + u[1] * D.cell.rv[3 + x] + u[2] * D.cell.rv[6 + x];
+  const double d2d = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+  if (!(d2d < D.rc2)) return;
+  McSum tmp;
+  tmp.init();
+  const double *pa = D.gpar[a];
+  mc_terms64(D, sqrt(d2d), d2d, pa[0], pa[1], pa[2], pj[0], pj[1], pj[2], tmp);
+  e[side] += tmp.e64;
 }
 
 // q (cos x, sin x) of one atom for one k: FP64 (the reference's op order)
@@ -325,6 +371,7 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
   __shared__ unsigned sh_xold[MC_MAXG * 3], sh_xnew[MC_MAXG * 3];
   __shared__ double red[MC_TB / 32][10];
   __shared__ double2 sh_tab[2 * MC_MAXG][3][MC_GT];
+  __shared__ McDefer sh_q[MC_TB / 32][MC_QCAP];
   const int t = blockIdx.x;
   const int4 tr = trials[t];
   const int chain = tr.x, kind = tr.y, guest = tr.z;
@@ -375,32 +422,61 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
       }
     }
   } else {
-    for (int64_t j = threadIdx.x; j < D.nframe; j += MC_TB) {
-      const float4 pf = D.fparf[j];
-      const double *pj64 = (const double *)(D.fpar + j);
+    // every lane of a warp takes the same loop trips (valid marks the real
+    // pairs): the deferred-pair queue is filled and flushed warp-wide
+    McDefer *wq = sh_q[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    int qn = 0;
+    double edef[4] = {0.0, 0.0, 0.0, 0.0};
+    auto drain = [&](bool all) {
+      while (qn >= 32 || (all && qn > 0)) {
+        __syncwarp();
+        mc_flush(D, wq, qn < 32 ? qn : 32, lane, gbase, sh_fold, sh_fnew, sh_xold, sh_xnew, edef);
+        __syncwarp();
+        const int rest = qn > 32 ? qn - 32 : 0;
+        McDefer mv;
+        if (lane < rest) mv = wq[32 + lane];
+        __syncwarp();
+        if (lane < rest) wq[lane] = mv;
+        __syncwarp();
+        qn = rest;
+      }
+    };
+    for (int64_t jb = 0; jb < D.nframe; jb += MC_TB) {
+      const int64_t j = jb + threadIdx.x;
+      const bool vj = j < D.nframe;
+      const float4 pf = vj ? D.fparf[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const unsigned *xj = D.ffix + 3 * (vj ? j : 0);
       for (int a = 0; a < M; a++) {
-        if (has_old)
-          mc_pair32(D, sh_fold + 3 * a, sh_xold + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], D.gpar[a], D.ffrac + 3 * j,
-                    D.ffix + 3 * j, pf.x, pf.y, pf.z, pj64, acc[0]);
-        if (has_new)
-          mc_pair32(D, sh_fnew + 3 * a, sh_xnew + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], D.gpar[a], D.ffrac + 3 * j,
-                    D.ffix + 3 * j, pf.x, pf.y, pf.z, pj64, acc[2]);
+        if (has_old) {
+          mc_pair32(D, sh_xold + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], xj, pf.x, pf.y, pf.z, vj, (int)j, a | (0 << 2),
+                    acc[0], wq, qn, lt, drain);
+        }
+        if (has_new) {
+          mc_pair32(D, sh_xnew + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], xj, pf.x, pf.y, pf.z, vj, (int)j, a | (2 << 2),
+                    acc[2], wq, qn, lt, drain);
+        }
       }
     }
-    for (int64_t u = threadIdx.x; u < (int64_t)ng * M; u += MC_TB) {
+    for (int64_t ub = 0; ub < (int64_t)ng * M; ub += MC_TB) {
+      const int64_t u = ub + threadIdx.x;
       const int gi = (int)(u / M), ai = (int)(u % M);
-      if (has_old && gi == guest) continue;  // the moving guest itself
-      const double *fj = D.gfrac + (gbase + u) * 3;
-      const unsigned *xj = D.gfix + (gbase + u) * 3;
+      const bool vu = u < (int64_t)ng * M && !(has_old && gi == guest);  // not the moving guest itself
+      const unsigned *xj = D.gfix + (gbase + (vu ? u : 0)) * 3;
       for (int a = 0; a < M; a++) {
-        if (has_old)
-          mc_pair32(D, sh_fold + 3 * a, sh_xold + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], D.gpar[a], fj, xj,
-                    D.gqf[ai], D.gsigf[ai], D.gsepsf[ai], D.gpar[ai], acc[1]);
-        if (has_new)
-          mc_pair32(D, sh_fnew + 3 * a, sh_xnew + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], D.gpar[a], fj, xj,
-                    D.gqf[ai], D.gsigf[ai], D.gsepsf[ai], D.gpar[ai], acc[3]);
+        if (has_old) {
+          mc_pair32(D, sh_xold + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], xj, D.gqf[ai], D.gsigf[ai], D.gsepsf[ai],
+                    vu, (int)u, a | (1 << 2), acc[1], wq, qn, lt, drain);
+        }
+        if (has_new) {
+          mc_pair32(D, sh_xnew + 3 * a, D.gqf[a], D.gsigf[a], D.gsepsf[a], xj, D.gqf[ai], D.gsigf[ai], D.gsepsf[ai],
+                    vu, (int)u, a | (3 << 2), acc[3], wq, qn, lt, drain);
+        }
       }
     }
+    drain(true);
+    for (int q = 0; q < 4; q++) acc[q].e64 += edef[q];
   }
   // reciprocal space: e^{i k.r} = T0[g0] T1[g1] T2[g2] from per-atom FP64
   // tables e^{2 pi i g s} (s = fractional coordinate), conjugated for g < 0
