@@ -818,6 +818,15 @@ def run_serving(args):
         'requests': nc, 'slots': args.serving_slots, 'requests_per_s': cs['requests_per_s'],
         'atom_steps_per_s': cs['atom_steps_per_s'], 'latency_p99_ms': cs['latency_p99_ms'],
         'how': 'one context, stream and captured ~45-kernel step per request, all requests at t = 0'}
+    # the same engine at the stated arrival rate: below saturation each
+    # request runs at the pace of its own context, not of the whole fleet
+    rreq = make_workload(nreq=n, rate=args.serving_rate, seed=2024)
+    rw = ServingEngine(nslots=args.serving_slots, budget_bytes=budget).run(rreq, realtime=True)
+    rs = summarize(rreq, rw)
+    out['per_context_engine_at_rate'] = {
+        'requests': n, 'arrival_rate_per_s': args.serving_rate, 'slots': args.serving_slots,
+        'requests_per_s': rs['requests_per_s'], 'latency_p50_ms': rs['latency_p50_ms'],
+        'latency_p99_ms': rs['latency_p99_ms'], 'errors': rs['errors']}
     nseq = min(48, n)
     seq = make_workload(nreq=n, rate=0.0, seed=2024)[:nseq]
     wseq = run_sequential(seq, precision='fp64', mode='api')

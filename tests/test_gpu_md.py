@@ -7,7 +7,8 @@ from seeded 300 K velocities.  Checks: the first 20 steps follow the oracle
 trajectory (FP64 form: 1e-8 relative on positions); the conserved-energy
 drift (linear fit, per atom and ps) and the reference's conserved-energy
 fluctuation ratio sqrt(var Econs / var Ekin) are no worse than the oracle's
-(a 25 % margin plus an absolute floor of 2e-7 Ha/atom/ps for fit noise).
+(a 25 % margin, no absolute floor: the oracle's drift on this system is
+4.6e-5 Ha/atom/ps, its fluctuation ratio 0.022).
 """
 import types
 
@@ -63,8 +64,8 @@ def test_nve_drift_no_worse_than_reference(oracle_run, precision):
             assert np.abs(a - b).max() <= 1e-8 * np.abs(b).max()
     d = abs(drift_per_ps(t, e, natom))
     d_ref = abs(drift_per_ps(t_ref, e_ref, natom))
-    assert d <= 1.25 * d_ref + 2e-7, (d, d_ref)
-    assert ratio <= 1.25 * ratio_ref + 1e-3, (ratio, ratio_ref)
+    assert d <= 1.25 * d_ref, (d, d_ref)
+    assert ratio <= 1.25 * ratio_ref, (ratio, ratio_ref)
     assert ff.nlist.nrebuild >= 1 and ff.nlist.nrecompute >= 1
 
 
@@ -101,6 +102,6 @@ def test_device_verlet_follows_reference_and_drift(oracle_run, precision):
     times = dt * np.arange(1, NSTEP + 1)
     d = abs(drift_per_ps(times, econs[1:], natom))
     d_ref = abs(drift_per_ps(t_ref, e_ref, natom))
-    assert d <= 1.25 * d_ref + 2e-7, (d, d_ref)
-    assert tr.get() <= 1.25 * ratio_ref + 1e-3, (tr.get(), ratio_ref)
+    assert d <= 1.25 * d_ref, (d, d_ref)
+    assert tr.get() <= 1.25 * ratio_ref, (tr.get(), ratio_ref)
     assert dv.nrebuild >= 1

@@ -426,6 +426,8 @@ __global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap)
   const float qi = vi ? F.q[i] : 0.f;
   const float2 *pt = F.ptab + i;
   float gx = 0.f, gy = 0.f, gz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  int key01 = -1;
+  float2 p01 = make_float2(0.f, 0.f);
   const int64_t k1 = (int64_t)S.k0 + S.nk;
   for (int64_t kc = S.k0; kc < k1; kc += 128) {
     const int nkc = (int)(k1 - kc < 128 ? k1 - kc : 128);
@@ -438,8 +440,16 @@ __global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap)
     if (vi && qi != 0.f) {
       for (int q = 0; q < nkc; q++) {
         const int ks = sks[q];
-        const float2 p = fl_phase(pt[(int64_t)(ks & 255) * F.acap], pt[(int64_t)((ks >> 8) & 255) * F.acap],
-                                  pt[(int64_t)((ks >> 16) & 255) * F.acap], ks);
+        // consecutive k vectors of a (g0, g1) column share e0 e1 (the
+        // test is uniform over the block)
+        if ((ks & 0x0300ffff) != key01) {
+          key01 = ks & 0x0300ffff;
+          const float2 e0 = pt[(int64_t)(ks & 255) * F.acap], e1 = pt[(int64_t)((ks >> 8) & 255) * F.acap];
+          const float y0 = (ks >> 24) & 1 ? -e0.y : e0.y, y1 = (ks >> 25) & 1 ? -e1.y : e1.y;
+          p01 = make_float2(e0.x * e1.x - y0 * y1, e0.x * y1 + y0 * e1.x);
+        }
+        const float2 e2 = pt[(int64_t)((ks >> 16) & 255) * F.acap];
+        const float2 p = make_float2(p01.x * e2.x - p01.y * e2.y, p01.x * e2.y + p01.y * e2.x);
         const float2 c = scf[q];
         const float4 k = skv[q];
         const float x = qi * (c.y * p.x - c.x * p.y);
