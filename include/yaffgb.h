@@ -356,7 +356,10 @@ int yg_fleet_destroy(yg_fleet *fleet);
  * charges, LJ sigma and epsilon per atom (Lorentz-Berthelot mixing), the 3x3
  * cell rvecs) with cutoff rcut, Verlet skin, Ewald alpha and gcut, time step
  * dt and nsteps steps to run; *slot receives its slot.  YG_ERR_CAPACITY
- * when a slot, the atom range or the k range does not fit. */
+ * when a slot, the atom range or the k range does not fit; YG_ERR_ARG when
+ * rcut + skin needs more than two periodic images per cell axis, or when the
+ * reciprocal-lattice extents need more than 64 phase-table entries per atom
+ * ((G0 + 1) + (G1 + 1) + (G2 + 1), G_k = ceil(gcut |r_k| - 1/2)). */
 int yg_fleet_add(yg_fleet *fleet, int64_t natom, const double *pos, const double *vel, const double *masses,
                  const double *charges, const double *sigma, const double *epsilon, const double *rvecs,
                  double rcut, double skin, double alpha, double gcut, double dt, int64_t nsteps, int *slot);
