@@ -21,6 +21,10 @@
 #include "yg_internal.cuh"
 #include "yg_pairterm.cuh"
 
+#ifndef YG_PAIR_ATOMS
+#define YG_PAIR_ATOMS 4  // atoms per warp (energy and virial reduced once per warp)
+#endif
+
 namespace {
 
 struct PairArgs {
@@ -179,16 +183,23 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
   const bool kahan = (MODE == YG_MIXED_KAHAN);
   __shared__ double red[8][NPOT * 7];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   Acc<T, kahan> E[NPOT], G[NPOT][3], V[NPOT][6];
 #pragma unroll
   for (int p = 0; p < NPOT; p++) {
     E[p].init();
 #pragma unroll
-    for (int k = 0; k < 3; k++) G[p][k].init();
-#pragma unroll
     for (int k = 0; k < 6; k++) V[p][k].init();
   }
+  // YG_PAIR_ATOMS atoms per warp, one after the other: each atom's gradient
+  // is reduced and stored after its row; energy and virial accumulate over
+  // the warp's atoms and are reduced once
+  for (int ia = 0; ia < YG_PAIR_ATOMS; ia++) {
+  const int64_t i = w0 * YG_PAIR_ATOMS + ia;
+#pragma unroll
+  for (int p = 0; p < NPOT; p++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) G[p][k].init();
   if (i < A.natom) {
     T xi, yi, zi, qi;
     if (MODE == YG_FP64) {
@@ -318,6 +329,38 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
       }
     }
   }
+  // the atom's gradient
+  if (A.want_grad && i < A.natom) {
+    const int oi = A.sorted[i];
+    if (MODE == YG_FP64) {
+#pragma unroll
+      for (int p = 0; p < NPOT; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const double gv = warp_sum<double>(G[p][k].value());
+          if (lane == 0) A.gpos[p][3 * (int64_t)oi + k] = gv;
+        }
+    } else {
+      float gh[NPOT * 3], gl[NPOT * 3];
+#pragma unroll
+      for (int p = 0; p < NPOT; p++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          gh[3 * p + k] = G[p][k].hi();
+          gl[3 * p + k] = G[p][k].lo();
+          warp_twosum(gh[3 * p + k], gl[3 * p + k]);
+        }
+      float h = gh[0], l = gl[0];
+#pragma unroll
+      for (int c = 1; c < NPOT * 3; c++)
+        if (lane == c) {
+          h = gh[c];
+          l = gl[c];
+        }
+      if (lane < NPOT * 3) A.gpos[lane / 3][3 * (int64_t)oi + lane % 3] = (double)h + (double)l;
+    }
+  }
+  }  // atoms of the warp
   if (MODE == YG_FP64) {
     // FP64 warp, block and grid reductions
     double part[NPOT * 7];
@@ -329,16 +372,6 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
     }
 #pragma unroll
     for (int v = 0; v < NPOT * 7; v++) part[v] = warp_sum<double>(part[v]);
-    if (A.want_grad && i < A.natom) {
-      const int oi = A.sorted[i];
-#pragma unroll
-      for (int p = 0; p < NPOT; p++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          const double gv = warp_sum<double>(G[p][k].value());
-          if (lane == 0) A.gpos[p][3 * (int64_t)oi + k] = gv;
-        }
-    }
     if (lane == 0) {
 #pragma unroll
       for (int v = 0; v < NPOT * 7; v++) red[wid][v] = part[v];
@@ -370,26 +403,6 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
     }
 #pragma unroll
     for (int v = 0; v < NPOT * 7; v++) warp_twosum(hi[v], lo[v]);
-    if (A.want_grad && i < A.natom) {
-      const int oi = A.sorted[i];
-      float gh[NPOT * 3], gl[NPOT * 3];
-#pragma unroll
-      for (int p = 0; p < NPOT; p++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          gh[3 * p + k] = G[p][k].hi();
-          gl[3 * p + k] = G[p][k].lo();
-          warp_twosum(gh[3 * p + k], gl[3 * p + k]);
-        }
-      float h = gh[0], l = gl[0];
-#pragma unroll
-      for (int c = 1; c < NPOT * 3; c++)
-        if (lane == c) {
-          h = gh[c];
-          l = gl[c];
-        }
-      if (lane < NPOT * 3) A.gpos[lane / 3][3 * (int64_t)oi + lane % 3] = (double)h + (double)l;
-    }
     if (lane == 0) {
 #pragma unroll
       for (int v = 0; v < NPOT * 7; v++) redf[wid][v] = make_float2(hi[v], lo[v]);
@@ -559,7 +572,7 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   A.want_grad = want_grad;
   SlotMap map;
   for (int q = 0; q < YG_MAX_POT; q++) map.slot[q] = q < npot ? slots[q] : 0;
-  const int nblocks = yg_blocks(N * 32, 256);
+  const int nblocks = yg_blocks((N + YG_PAIR_ATOMS - 1) / YG_PAIR_ATOMS * 32, 256);
   const int nval = npot * 7;
   int rc;
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap,
