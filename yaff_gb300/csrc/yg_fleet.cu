@@ -22,11 +22,10 @@
 //                      vector refreshed by the displacements since the build
 //                      (the reference's skin path, nlist.c:183-232)
 //   sfac      (k)      structure factors S(k) of each system's half sphere
-//                      (a block of 32 k vectors sweeps the system's atoms
+//                      (a block of 128 k vectors sweeps the system's atoms
 //                      in tiles of 32 whose phase tables it stages in shared
-//                      memory, a quarter of each tile per warp: a phase is
-//                      two complex products), and the FP32 coefficients
-//                      2 A(k) S(k) of the gradient
+//                      memory: a phase is two complex products), and the
+//                      FP32 coefficients 2 A(k) S(k) of the gradient
 //   ewald     (atom)   reciprocal-space gradient from those coefficients and
 //                      the atom's own phase tables
 //   kick      (atom)   total gradient, second half kick, kinetic energy
@@ -367,24 +366,20 @@ __device__ __forceinline__ float2 fl_phase(float2 e0, float2 e1, float2 e2, int 
   return make_float2(pr * e2.x - pi * e2.y, pr * e2.y + pi * e2.x);
 }
 
-// S(k) of 32 reciprocal vectors of one system per block (k ranges are
+// S(k) of 128 reciprocal vectors of one system per block (k ranges are
 // aligned to 128); the system's atoms are swept in tiles of 32 whose phase
-// tables and charges are staged in shared memory, and the four warps of the
-// block take the tile's atoms a = w, w + 4, ... (a quarter of the serial
-// loop each); their partial sums are added in warp order.  Then the FP32
+// tables and charges are staged in shared memory.  Then the FP32
 // coefficients 2 A(k) S(k) that the gradient pass reads.
 __global__ void __launch_bounds__(128) k_fl_sfac(FleetDev F, int64_t nk_cap) {
   __shared__ float2 tab[FL_TAB][33];
   __shared__ float sq[32];
-  __shared__ double part[4][32][2];
-  const int64_t kb = (int64_t)blockIdx.x * 32;
+  const int64_t kb = (int64_t)blockIdx.x * 128;
   if (kb >= nk_cap) return;
   const int s = F.kg[kb].w;
   if (s < 0) return;
   const FleetSys &S = F.d_sys[s];
   if (S.state != 1) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t kk = kb + lane;
+  const int64_t kk = kb + threadIdx.x;
   const bool mine = F.kg[kk].w == s;  // the rest of the granule is padding
   const int ks = mine ? F.kslot[kk] : 0;
   const int s0 = ks & 255, s1 = (ks >> 8) & 255, s2 = (ks >> 16) & 255;
@@ -399,7 +394,7 @@ __global__ void __launch_bounds__(128) k_fl_sfac(FleetDev F, int64_t nk_cap) {
     }
     if (threadIdx.x < 32) sq[threadIdx.x] = (int)threadIdx.x < na ? F.q[at + threadIdx.x] : 0.f;
     __syncthreads();
-    for (int a = w; a < na; a += 4) {
+    for (int a = 0; a < na; a++) {
       const float2 p = fl_phase(tab[s0][a], tab[s1][a], tab[s2][a], ks);
       const float qa = sq[a];
       kahan_add(cr, kr, qa * p.x);
@@ -407,33 +402,26 @@ __global__ void __launch_bounds__(128) k_fl_sfac(FleetDev F, int64_t nk_cap) {
     }
     __syncthreads();
   }
-  part[w][lane][0] = (double)cr - (double)kr;
-  part[w][lane][1] = (double)ci - (double)ki;
-  __syncthreads();
-  if (w != 0 || !mine) return;
-  const double sr = ((part[0][lane][0] + part[1][lane][0]) + part[2][lane][0]) + part[3][lane][0];
-  const double si = ((part[0][lane][1] + part[1][lane][1]) + part[2][lane][1]) + part[3][lane][1];
-  const double a2 = 2.0 * F.kpref[kk];
+  if (!mine) return;
+  const double sr = (double)cr - (double)kr, si = (double)ci - (double)ki, a2 = 2.0 * F.kpref[kk];
   F.S[kk] = make_double2(sr, si);
   F.kcoef[kk] = make_float2((float)(a2 * sr), (float)(a2 * si));
 }
 
-// Reciprocal-space gradient of 32 atoms of a tile (one system) per block:
-// four threads per atom, each over every fourth k vector of the system
-// (staged 128 at a time with the coefficients), from the atom's own phase
-// tables; the four partial sums are added in a fixed order.
+// Reciprocal-space gradient of every atom of a 128-atom tile (one system)
+// from its own phase tables and the system's coefficients, staged 128 k
+// vectors at a time.
 __global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap) {
   __shared__ int sks[128];
   __shared__ float4 skv[128];
   __shared__ float2 scf[128];
-  const int64_t i0 = (int64_t)blockIdx.x * 32;
+  const int64_t i0 = (int64_t)blockIdx.x * 128;
   if (i0 >= natom_cap) return;
-  const int s = F.sysid[i0 & ~(int64_t)(FL_TILE - 1)];  // the tile's first atom belongs to the system
+  const int s = F.sysid[i0];
   if (s < 0) return;
   const FleetSys &S = F.d_sys[s];
-  if (S.state != 1 || i0 >= (int64_t)S.a0 + S.n) return;  // (a block past the system's last atom)
-  const int sub = threadIdx.x & 3;
-  const int64_t i = i0 + (threadIdx.x >> 2);
+  if (S.state != 1) return;
+  const int64_t i = i0 + threadIdx.x;
   const bool vi = i < (int64_t)S.a0 + S.n;
   const float qi = vi ? F.q[i] : 0.f;
   const float2 *pt = F.ptab + i;
@@ -450,9 +438,10 @@ __global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap)
     }
     __syncthreads();
     if (vi && qi != 0.f) {
-      for (int q = sub; q < nkc; q += 4) {
+      for (int q = 0; q < nkc; q++) {
         const int ks = sks[q];
-        // k vectors of one (g0, g1) column share e0 e1
+        // consecutive k vectors of a (g0, g1) column share e0 e1 (the
+        // test is uniform over the block)
         if ((ks & 0x0300ffff) != key01) {
           key01 = ks & 0x0300ffff;
           const float2 e0 = pt[(int64_t)(ks & 255) * F.acap], e1 = pt[(int64_t)((ks >> 8) & 255) * F.acap];
@@ -471,19 +460,10 @@ __global__ void __launch_bounds__(128) k_fl_ewald(FleetDev F, int64_t natom_cap)
     }
     __syncthreads();
   }
-  // the four partial sums of the atom (lanes 4a .. 4a + 3), added in order
-  double g[3] = {(double)gx - (double)cx, (double)gy - (double)cy, (double)gz - (double)cz};
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    const double g1 = __shfl_down_sync(0xffffffffu, g[c], 1);
-    const double g2 = __shfl_down_sync(0xffffffffu, g[c], 2);
-    const double g3 = __shfl_down_sync(0xffffffffu, g[c], 3);
-    g[c] = ((g[c] + g1) + g2) + g3;
-  }
-  if (!vi || sub != 0) return;
-  F.gew[3 * i] = g[0];
-  F.gew[3 * i + 1] = g[1];
-  F.gew[3 * i + 2] = g[2];
+  if (!vi) return;
+  F.gew[3 * i] = (double)gx - (double)cx;
+  F.gew[3 * i + 1] = (double)gy - (double)cy;
+  F.gew[3 * i + 2] = (double)gz - (double)cz;
 }
 
 __global__ void k_fl_kick(FleetDev F, int64_t natom_cap) {
@@ -571,8 +551,8 @@ int fl_launch_step(yg_fleet *f, cudaStream_t st) {
   k_fl_gate<<<(f->max_systems + 127) / 128, 128, 0, st>>>(f->d, f->max_systems);
   k_fl_build<<<(int)(A / FL_TILE), FL_TILE, 0, st>>>(f->d, A / FL_TILE);
   k_fl_pair<<<nb, 256, 0, st>>>(f->d, A);
-  k_fl_sfac<<<(int)(K / 32), 128, 0, st>>>(f->d, K);
-  k_fl_ewald<<<(int)(A / 32), 128, 0, st>>>(f->d, A);
+  k_fl_sfac<<<(int)(K / 128), 128, 0, st>>>(f->d, K);
+  k_fl_ewald<<<(int)(A / 128), 128, 0, st>>>(f->d, A);
   k_fl_kick<<<nb, 256, 0, st>>>(f->d, A);
   k_fl_finish<<<f->max_systems, 256, 0, st>>>(f->d, f->max_systems);
   cudaError_t e = cudaGetLastError();

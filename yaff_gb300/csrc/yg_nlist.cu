@@ -408,13 +408,17 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
     // once (lanes fill the runs' ranges), so the sweep looks it up instead of
     // stepping through the run offsets
     const bool mapped = total <= YG_BUILD_MAP && nrun <= 256;
-    if (mapped) {
-      for (int b = lane; b < nrun; b += 32) {
+    // a run's start becomes relative to the flat candidate index (candidate
+    // q of run b is atom run[b].x + q)
+    for (int b = lane; b < nrun; b += 32) {
+      const int o = off[b];
+      run[b].x -= o;
+      if (mapped) {
         const int c1 = off[b + 1];
-        for (int c = off[b]; c < c1; c++) map[c] = (unsigned char)b;
+        for (int c = o; c < c1; c++) map[c] = (unsigned char)b;
       }
-      __syncwarp();
     }
+    __syncwarp();
     int r = 0;
     if (mapped && A.fast && !need_oj) {
       // common case (no exclusions, no nlow/nhigh filter, FP32 shortcut on):
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
       int qn = min(lane, total - 1);
       int rqn = map[qn];
       int4 rrn = run[rqn];
-      int jn = rrn.x + (qn - off[rqn]);
+      int jn = rrn.x + qn;
       float4 xjn = A.xb[jn];
       for (int q0 = 0; q0 < total; q0 += 32) {
         const bool live = q0 + lane < total;
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
           qn = min(q0 + 32 + lane, total - 1);
           rqn = map[qn];
           rrn = run[rqn];
-          jn = rrn.x + (qn - off[rqn]);
+          jn = rrn.x + qn;
           xjn = A.xb[jn];
         }
 #else
@@ -449,7 +453,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
         const bool live = q0 + lane < total;
         const int rq = map[q];
         const int4 rr = run[rq];
-        const int j = rr.x + (q - off[rq]);
+        const int j = rr.x + q;
         const float4 xj = A.xb[j];
 #endif
         const int oidx = rr.z + __float_as_int(xj.w);
@@ -494,7 +498,7 @@ __global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
         else
           while (off[r + 1] <= q) r++;
         const int4 rr = run[r];
-        j = rr.x + (q - off[r]);
+        j = rr.x + q;
         const float4 xj = A.xb[j];
         oidx = rr.z + __float_as_int(xj.w);
         const int pk = rr.w;
