@@ -60,6 +60,8 @@ struct yg_mc {
   int *d_nguest = nullptr;
   std::vector<int> nguest;
   double2 *d_S = nullptr;          // [chain][k]
+  float4 *d_Sff = nullptr;         // [chain][k] S as FP32 hi + lo (re hi, im hi, re lo, im lo), mixed trials
+  float2 *d_kpf = nullptr;         // [k] prefactor as FP32 hi + lo
   double2 *d_Sframe = nullptr;     // [k]
   double2 *d_Spart = nullptr;      // structure-factor partials
   size_t spart_cap = 0;
@@ -103,6 +105,9 @@ struct McDev {
   const double *gpos, *gfrac;
   const int *nguest;
   const double2 *S;
+  const float4 *Sff;               // mixed: S split into FP32 hi + lo per launch
+  const float2 *kpf;               // mixed: prefactors as FP32 hi + lo
+  float gqh[MC_MAXG], gql[MC_MAXG];  // guest charges as FP32 hi + lo
 };
 
 // s - floor(s) as a 32-bit fixed-point fraction: differences of two such
@@ -337,6 +342,52 @@ __device__ __forceinline__ void mc_flush(const McDev &D, const McDefer *wq, int 
   e[side] += tmp.e64;
 }
 
+// Double-float arithmetic (a value as an unevaluated FP32 sum hi + lo, about
+// 44 significant bits): the mixed trials' reciprocal sum runs on the FP32
+// pipe with close to FP64 accuracy.  The _rn intrinsics keep the compiler
+// from fusing the error-free steps.
+struct McFF {
+  float h, l;
+};
+__device__ __forceinline__ McFF ff_mul(McFF a, McFF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = __fadd_rn(p, e);
+  return McFF{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+__device__ __forceinline__ McFF ff_add(McFF a, McFF b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  float t = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  t = __fadd_rn(t, __fadd_rn(a.l, b.l));
+  const float r = __fadd_rn(s, t);
+  return McFF{r, __fsub_rn(t, __fsub_rn(r, s))};
+}
+__device__ __forceinline__ McFF ff_neg(McFF a) { return McFF{-a.h, -a.l}; }
+// acc += a b, acc left unnormalized (hi exact TwoSum, errors gathered in lo)
+__device__ __forceinline__ void ff_acc(McFF &acc, McFF a, McFF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = __fadd_rn(acc.h, p);
+  const float bb = __fsub_rn(s, acc.h);
+  const float t = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.h = s;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(t, e));
+}
+
+// The chains' structure factors as FP32 hi + lo, once per trial launch.
+__global__ void k_mc_split_s(const double2 *__restrict__ S, int64_t n, float4 *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = S[i];
+  const float xh = (float)v.x, yh = (float)v.y;
+  out[i] = make_float4(xh, yh, (float)(v.x - (double)xh), (float)(v.y - (double)yh));
+}
+
 // q (cos x, sin x) of one atom for one k: FP64 (the reference's op order)
 // or, mixed, an FP64 phase reduced exactly to [-pi, pi] and FP32 sincos.
 template <bool F64>
@@ -372,6 +423,7 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
   __shared__ double red[MC_TB / 32][10];
   __shared__ double2 sh_tab[2 * MC_MAXG][3][MC_GT];
   __shared__ McDefer sh_q[MC_TB / 32][MC_QCAP];
+  __shared__ float4 sh_tabf[F64 ? 1 : 2 * MC_MAXG][3][MC_GT];
   const int t = blockIdx.x;
   const int4 tr = trials[t];
   const int chain = tr.x, kind = tr.y, guest = tr.z;
@@ -478,6 +530,8 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
     drain(true);
     for (int q = 0; q < 4; q++) acc[q].e64 += edef[q];
   }
+  double ro = 0.0, rn = 0.0;
+  if (F64) {
   // reciprocal space: e^{i k.r} = T0[g0] T1[g1] T2[g2] from per-atom FP64
   // tables e^{2 pi i g s} (s = fractional coordinate), conjugated for g < 0
   const int G0 = D.gmax[0], G1 = D.gmax[1], G2 = D.gmax[2];
@@ -505,7 +559,6 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
   __syncthreads();
   // one (g0, g1) column per thread: P = q T0[g0] T1[g1] per atom, then
   // dS(k) = sum_atoms P T2[g2] along the column's g2 run
-  double ro = 0.0, rn = 0.0;
   const double2 *S = D.S + (int64_t)chain * D.nk;
   const int sbeg = has_old ? 0 : M, send = has_new ? 2 * M : M;
   for (int col = threadIdx.x; col < D.ncol; col += MC_TB) {
@@ -548,6 +601,92 @@ __global__ void __launch_bounds__(MC_TB, 1) k_mc_trials(const McDev D, const int
         rn += (bc * nc + bs * ns) * pref;
       }
     }
+  }
+  } else {
+    // mixed: the same sums in double-float arithmetic on per-atom FP32 hi + lo
+    // tables (from FP64 sincospi) and the chain's S split per launch
+    const int G0 = D.gmax[0], G1 = D.gmax[1], G2 = D.gmax[2];
+    const int nt = G0 + G1 + G2 + 3;
+    for (int i = threadIdx.x; i < 2 * M * nt; i += MC_TB) {
+      const int slot = i / nt;
+      int r = i - slot * nt;
+      int axis = 0;
+      if (r > G0) {
+        r -= G0 + 1;
+        axis = 1;
+        if (r > G1) {
+          r -= G1 + 1;
+          axis = 2;
+        }
+      }
+      const bool is_new = slot >= M;
+      if (is_new ? has_new : has_old) {
+        const double f = (is_new ? sh_fnew : sh_fold)[3 * (slot % M) + axis];
+        double sn, cs;
+        sincospi(2.0 * r * f, &sn, &cs);
+        const float ch = (float)cs, sh = (float)sn;
+        sh_tabf[slot][axis][r] = make_float4(ch, sh, (float)(cs - (double)ch), (float)(sn - (double)sh));
+      }
+    }
+    __syncthreads();
+    McFF fro{0.f, 0.f}, frn{0.f, 0.f};
+    const float4 *Sf = D.Sff + (int64_t)chain * D.nk;
+    const int sbeg = has_old ? 0 : M, send = has_new ? 2 * M : M;
+    for (int col = threadIdx.x; col < D.ncol; col += MC_TB) {
+      const int4 cd = D.cols[col];
+      const int kend = D.cols[col + 1].w;
+      const int a0 = cd.x < 0 ? -cd.x : cd.x, a1 = cd.y < 0 ? -cd.y : cd.y;
+      const float s0 = cd.x < 0 ? -1.f : 1.f, s1 = cd.y < 0 ? -1.f : 1.f;
+      McFF pr[2 * MC_MAXG], pim[2 * MC_MAXG];
+#pragma unroll
+      for (int slot = 0; slot < 2 * MC_MAXG; slot++) {
+        if (slot < sbeg || slot >= send) continue;
+        const float4 t0 = sh_tabf[slot][0][a0], t1 = sh_tabf[slot][1][a1];
+        const McFF e0r{t0.x, t0.z}, e0i{s0 * t0.y, s0 * t0.w}, e1r{t1.x, t1.z}, e1i{s1 * t1.y, s1 * t1.w};
+        const McFF q{D.gqh[slot % M], D.gql[slot % M]};
+        const McFF xr = ff_add(ff_mul(e0r, e1r), ff_neg(ff_mul(e0i, e1i)));
+        const McFF xi = ff_add(ff_mul(e0r, e1i), ff_mul(e0i, e1r));
+        pr[slot] = ff_mul(q, xr);
+        pim[slot] = ff_mul(q, xi);
+      }
+      for (int k = cd.w; k < kend; k++) {
+        const int g2 = cd.z + (k - cd.w);
+        const float2 pk = D.kpf[k];
+        const McFF pref{pk.x, pk.y};
+        const float4 sq = Sf[k];
+        const McFF Sr{sq.x, sq.z}, Si{sq.y, sq.w};
+        McFF oc{0.f, 0.f}, os{0.f, 0.f}, nc{0.f, 0.f}, ns{0.f, 0.f};
+#pragma unroll
+        for (int slot = 0; slot < 2 * MC_MAXG; slot++) {
+          if (slot < sbeg || slot >= send) continue;
+          const float4 t2 = sh_tabf[slot][2][g2];
+          const McFF er{t2.x, t2.z}, ei{t2.y, t2.w};
+          if (slot < M) {
+            ff_acc(oc, pr[slot], er);
+            ff_acc(oc, ff_neg(pim[slot]), ei);
+            ff_acc(os, pr[slot], ei);
+            ff_acc(os, pim[slot], er);
+          } else {
+            ff_acc(nc, pr[slot], er);
+            ff_acc(nc, ff_neg(pim[slot]), ei);
+            ff_acc(ns, pr[slot], ei);
+            ff_acc(ns, pim[slot], er);
+          }
+        }
+        if (has_old) {
+          const McFF t = ff_add(ff_mul(ff_add(Sr, ff_neg(oc)), oc), ff_mul(ff_add(Si, ff_neg(os)), os));
+          fro = ff_add(fro, ff_mul(t, pref));
+        }
+        if (has_new) {
+          const McFF bc = (kind == MC_TRANSLATE) ? ff_add(Sr, ff_neg(oc)) : Sr;
+          const McFF bs = (kind == MC_TRANSLATE) ? ff_add(Si, ff_neg(os)) : Si;
+          const McFF t = ff_add(ff_mul(bc, nc), ff_mul(bs, ns));
+          frn = ff_add(frn, ff_mul(t, pref));
+        }
+      }
+    }
+    ro = (double)fro.h + (double)fro.l;
+    rn = (double)frn.h + (double)frn.l;
   }
   // deterministic block reduction: 4 energies, 2 reciprocal sums (added),
   // 4 smallest distances (min)
@@ -711,6 +850,13 @@ McDev make_dev(const yg_mc *mc) {
   D.gfrac = mc->d_gfrac;
   D.nguest = mc->d_nguest;
   D.S = mc->d_S;
+  D.Sff = mc->d_Sff;
+  D.kpf = mc->d_kpf;
+  for (int a = 0; a < MC_MAXG; a++) {
+    const double q = a < mc->M ? mc->gq[a] : 0.0;
+    D.gqh[a] = (float)q;
+    D.gql[a] = (float)(q - (double)D.gqh[a]);
+  }
   return D;
 }
 
@@ -984,10 +1130,19 @@ int yg_mc_create(const double *rvecs, const double *gvecs, double volume, const 
   if (!rc) rc = mc_alloc((void **)&mc->d_gfrac, NG * 3 * sizeof(double));
   if (!rc) rc = mc_alloc((void **)&mc->d_nguest, (size_t)nchain * sizeof(int));
   if (!rc) rc = mc_alloc((void **)&mc->d_S, (size_t)nchain * std::max(1, mc->nk) * sizeof(double2));
+  if (!rc) rc = mc_alloc((void **)&mc->d_Sff, (size_t)nchain * std::max(1, mc->nk) * sizeof(float4));
+  if (!rc) rc = mc_alloc((void **)&mc->d_kpf, (size_t)std::max(1, mc->nk) * sizeof(float2));
+  std::vector<float2> kpf(std::max(1, mc->nk));
+  for (int k = 0; k < mc->nk; k++) {
+    const float h = (float)kv[k].w;
+    kpf[k] = make_float2(h, (float)(kv[k].w - (double)h));
+  }
   if (!rc) rc = mc_alloc((void **)&mc->d_Sframe, (size_t)std::max(1, mc->nk) * sizeof(double2));
   cudaError_t e = cudaSuccess;
   if (!rc) {
     if (mc->nk > 0) e = cudaMemcpyAsync(mc->d_k, kv.data(), kv.size() * sizeof(double4_32a), cudaMemcpyHostToDevice, mc->stream);
+    if (e == cudaSuccess && mc->nk > 0)
+      e = cudaMemcpyAsync(mc->d_kpf, kpf.data(), mc->nk * sizeof(float2), cudaMemcpyHostToDevice, mc->stream);
     if (e == cudaSuccess && mc->nk > 0)
       e = cudaMemcpyAsync(mc->d_kg, kg.data(), kg.size() * sizeof(int4), cudaMemcpyHostToDevice, mc->stream);
     if (e == cudaSuccess && nframe > 0)
@@ -1048,7 +1203,7 @@ int yg_mc_destroy(yg_mc *mc) {
   cudaStreamSynchronize(mc->stream);
   void *bufs[] = {mc->d_fparf,  mc->d_ffix,   mc->d_gfix,   mc->d_cols,   mc->d_kg,     mc->d_k,      mc->d_fpos,   mc->d_ffrac,  mc->d_fpar,     mc->d_gpos,   mc->d_gfrac,
                   mc->d_nguest, mc->d_S,      mc->d_Sframe, mc->d_Spart,    mc->d_trials, mc->d_newpos,
-                  mc->d_energy};
+                  mc->d_energy, mc->d_Sff,    mc->d_kpf};
   for (void *b : bufs)
     if (b) cudaFree(b);
   delete mc;
@@ -1165,8 +1320,13 @@ int yg_mc_trials(yg_mc *mc, int64_t ntrial, const int32_t *chain, const int32_t 
   McDev D = make_dev(mc);
   if (mc->precision == YG_FP64)
     k_mc_trials<true><<<(unsigned)ntrial, MC_TB, 0, mc->stream>>>(D, mc->d_trials, mc->d_newpos, mc->d_energy);
-  else
+  else {
+    if (mc->nk > 0) {
+      const int64_t ns = mc->nchain * (int64_t)mc->nk;
+      k_mc_split_s<<<(unsigned)((ns + 255) / 256), 256, 0, mc->stream>>>(mc->d_S, ns, mc->d_Sff);
+    }
     k_mc_trials<false><<<(unsigned)ntrial, MC_TB, 0, mc->stream>>>(D, mc->d_trials, mc->d_newpos, mc->d_energy);
+  }
   mc->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return yg_cuda_fail(e, "k_mc_trials");
