@@ -1907,6 +1907,17 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   }
   yg_free(ctx, (void **)&ctx->d_ew_uoff);
   ctx->d_ew_uoff = nullptr;
+  yg_free(ctx, (void **)&ctx->d_ew_upk);
+  ctx->d_ew_upk = nullptr;
+  // every column of the tiles as one int for the tcgen05 epilogue: |g0|,
+  // the E1 row G0 + 1 + |g1| (8 bits each), the signs of g0 and g1 (bits 16,
+  // 17); -1 for padding
+  std::vector<int> upk(std::max<size_t>(1, tiles.size()), -1);
+  for (size_t t = 0; t < tiles.size(); t++) {
+    const int4 c = tiles[t];
+    if (c.z >= 0)
+      upk[t] = std::abs(c.x) | ((G0 + 1 + std::abs(c.y)) << 8) | ((c.x < 0) << 16) | ((c.y < 0) << 17);
+  }
   yg_free(ctx, (void **)&ctx->d_ew_urange);
   ctx->d_ew_urange = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_crange);
@@ -1930,6 +1941,8 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_crange, crange.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_uoff, uoff.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_urange, urange.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_upk, upk.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_upk, upk.data(), upk.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_uoff, uoff.data(), uoff.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_urange, urange.data(), urange.size() * sizeof(int), cudaMemcpyHostToDevice,

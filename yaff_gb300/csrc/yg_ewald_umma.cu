@@ -194,7 +194,7 @@ __global__ void k_ya_umma(const uint2 *__restrict__ yf, int64_t a0, int64_t n, i
 
 __global__ void __launch_bounds__(UM_THREADS, 1)
     k_ewald_force_umma(const float2 *__restrict__ te, const uint4 *__restrict__ ya, int a0, int a1, int ne, int G0,
-                       int lep, int nks, const int4 *__restrict__ cols, const int *__restrict__ urange,
+                       int lep, int nks, const int *__restrict__ upk, const int *__restrict__ urange,
                        const int *__restrict__ uoff, const uint4 *__restrict__ ub, double inv1, double inv2,
                        double *__restrict__ out, int64_t rstride, int *__restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem_um[];
@@ -293,34 +293,49 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     acc0.init();
     acc1.init();
     acc2.init();
+    // the packed columns of the next chunk (8 ints) are loaded while the
+    // current chunk is worked on; after a tile's last chunk, the next tile's
+    // first (the table is static, so loading ahead of the MMAs is safe)
+    int4 na = make_int4(-1, -1, -1, -1), nb = na;
+    if (ntile > 0) {
+      const int4 *p = reinterpret_cast<const int4 *>(upk + (size_t)u0 * UM_COLS + 8 * h);
+      na = __ldg(p);
+      nb = __ldg(p + 1);
+    }
     for (int i = 0; i < ntile; i++) {
       const int s = i & 1;
       if (!um_wait(&bar_mma[s], (i >> 1) & 1, status, stop)) break;
       um_fence_after();
-      const int4 *cs = cols + (size_t)(u0 + i) * UM_COLS;
       const unsigned tb = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(s * UM_N);
       float p0 = 0.f, p1 = 0.f, p2 = 0.f;
 #pragma unroll 1
       for (int c = h; c < UM_N / 32; c += HQ) {
-        int4 cc[8];
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) cc[jj] = __ldg(cs + 8 * c + jj);
-        if (cc[0].z < 0) break;  // the rest of the tile is padding
+        const int4 ca = na, cb = nb;
+        const bool last = c + HQ >= UM_N / 32 || ca.x < 0;  // (padding: the rest of the tile is padding)
+        if (!last || i + 1 < ntile) {
+          const int4 *p = reinterpret_cast<const int4 *>(
+              upk + (size_t)(u0 + (last ? i + 1 : i)) * UM_COLS + 8 * (last ? h : c + HQ));
+          na = __ldg(p);
+          nb = __ldg(p + 1);
+        }
+        if (ca.x < 0) break;
         float v[32];
         um_ld32(tb + 32 * c, v);
+        const int pk[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
 #pragma unroll
         for (int jj = 0; jj < 8; jj++) {
-          const int4 col = cc[jj];
-          if (col.z >= 0) {
-            const int ag0 = col.x < 0 ? -col.x : col.x, ag1 = G0 + 1 + (col.y < 0 ? -col.y : col.y);
+          const int col = pk[jj];
+          if (col >= 0) {
+            const int ag0 = col & 255, ag1 = (col >> 8) & 255;
+            const bool n0 = (col >> 16) & 1, n1 = (col >> 17) & 1;
             const float2 e0 = sE[ag0 * UM_M + r], e1 = sE[ag1 * UM_M + r];
-            const float e0y = col.x < 0 ? -e0.y : e0.y, e1y = col.y < 0 ? -e1.y : e1.y;
+            const float e0y = n0 ? -e0.y : e0.y, e1y = n1 ? -e1.y : e1.y;
             const float pr = e0.x * e1.x - e0y * e1y;
             const float pi = e0.x * e1y + e0y * e1.x;
             const float im1 = pr * v[4 * jj + 1] + pi * v[4 * jj];
             const float im2 = pr * v[4 * jj + 3] + pi * v[4 * jj + 2];
-            p0 += (float)col.x * im1;
-            p1 += (float)col.y * im1;
+            p0 += (float)(n0 ? -ag0 : ag0) * im1;
+            p1 += (float)(n1 ? G0 + 1 - ag1 : ag1 - G0 - 1) * im1;
             p2 += im2;
           }
         }
@@ -398,7 +413,7 @@ int yg_launch_force_umma(yg_ctx *ctx, const void *te, const void *ya, int a0, in
   if (nab <= 0) return YG_OK;
   dim3 grid(nab, nr);
   k_ewald_force_umma<<<grid, UM_THREADS, smem, ctx->stream>>>(
-      (const float2 *)te, (const uint4 *)ya, a0, a1, ne, G0, lep, nks, (const int4 *)ctx->d_ew_tiles, urange,
+      (const float2 *)te, (const uint4 *)ya, a0, a1, ne, G0, lep, nks, ctx->d_ew_upk, urange,
       ctx->d_ew_uoff, (const uint4 *)ub, inv1, inv2, out, rstride, ctx->d_status);
   YG_LAUNCH_CHECK(ctx, "k_ewald_force_umma");
   return YG_OK;
