@@ -116,7 +116,12 @@ class DeviceSystem(object):
 
     def sync_charges(self):
         """Uploads the system's charges when they differ from the last upload
-        (an element-wise comparison: charges may be changed in place)."""
+        (an element-wise comparison: charges may be changed in place).  Inside
+        one ForceField evaluation (call_key set) the comparison runs once."""
+        ck = getattr(self, 'call_key', None)
+        if ck is not None and ck == getattr(self, '_charges_call', None):
+            return
+        self._charges_call = ck
         q = self.system.charges
         if self._charges_key is not None and q.shape == self._charges_key.shape and np.array_equal(q, self._charges_key):
             return

@@ -48,6 +48,7 @@ class ForcePart(object):
             self._stale = False
             self._gpos[:] = np.nan
             self._vtens[:] = np.nan
+            self._gpos_zero = False
         if self._lazy is not None:
             dev, slot, want_g, want_v = self._lazy
             self._lazy = None
@@ -63,6 +64,7 @@ class ForcePart(object):
         self._lazy = None
         self._stale = False
         self._gpos = value
+        self._gpos_zero = False
 
     @property
     def vtens(self):
@@ -182,6 +184,15 @@ class ForceField(ForcePart):
         # is updated and the pair terms are evaluated); the readback at the
         # end synchronizes before the caller gets control back
         dev.upload_positions(wait=False)
+        # the parts' set-up checks (charges) run once per evaluation
+        self._ncall = getattr(self, '_ncall', 0) + 1
+        dev.call_key = (id(self), self._ncall)
+        try:
+            return self._fused_compute(dev, gpos, vtens, add)
+        finally:
+            dev.call_key = None
+
+    def _fused_compute(self, dev, gpos, vtens, add):
         want_grad = (gpos is not None) or (vtens is not None)
         mask = 0
         for part in self.parts:
@@ -222,7 +233,10 @@ class ForceField(ForcePart):
                 part.energy = e
                 part._lazy = None
                 part._stale = False
-                part._gpos[:] = 0.0
+                if not getattr(part, '_gpos_zero', False):
+                    # no gradient: zeroed once, not per call (1.2 MB at 50,000 atoms)
+                    part._gpos[:] = 0.0
+                    part._gpos_zero = True
                 if pv is not None:
                     part._vtens[:] = pv
                     host_vtens += pv
