@@ -202,6 +202,12 @@ int yg_create(int64_t natom, int precision, void *stream, yg_ctx **out) {
     delete c;
     return rc;
   }
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c->nsm < 1)
+      c->nsm = 1;
+  }
   rc |= yg_alloc(c, (void **)&c->d_pos, N * 3 * sizeof(double));
   rc |= yg_alloc(c, (void **)&c->d_pos_build, N * 3 * sizeof(double));
   rc |= yg_alloc(c, (void **)&c->d_charge, N * sizeof(double));

@@ -92,6 +92,7 @@ struct yg_occ {
 
 struct yg_ctx {
   int64_t natom = 0;
+  int nsm = 1;                    // streaming multiprocessors of the context's device
   int precision = YG_FP64;
   cudaStream_t stream = 0;
   cudaMemPool_t pool = nullptr;   // stream-ordered pool of this context's device

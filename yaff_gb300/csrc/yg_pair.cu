@@ -22,7 +22,7 @@
 #include "yg_pairterm.cuh"
 
 #ifndef YG_PAIR_ATOMS
-#define YG_PAIR_ATOMS 4  // atoms per warp (energy and virial reduced once per warp)
+#define YG_PAIR_ATOMS 4  // atoms per warp at most (energy and virial reduced once per warp)
 #endif
 
 namespace {
@@ -54,6 +54,7 @@ struct PairArgs {
   double *gpos[YG_MAX_POT];   // per-potential gradient, orig order (natom*3)
   double *partial;            // per block: NPOT*7 (E, Vxx, Vyy, Vzz, Vxy, Vxz, Vyz)
   int want_grad;
+  int apw;                    // atoms per warp (1 .. YG_PAIR_ATOMS)
 };
 
 // Accumulator: plain (FP64 or FP32) or Kahan-compensated FP32.
@@ -191,11 +192,11 @@ __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) 
 #pragma unroll
     for (int k = 0; k < 6; k++) V[p][k].init();
   }
-  // YG_PAIR_ATOMS atoms per warp, one after the other: each atom's gradient
-  // is reduced and stored after its row; energy and virial accumulate over
-  // the warp's atoms and are reduced once
-  for (int ia = 0; ia < YG_PAIR_ATOMS; ia++) {
-  const int64_t i = w0 * YG_PAIR_ATOMS + ia;
+  // A.apw atoms per warp, one after the other: each atom's gradient is
+  // reduced and stored after its row; energy and virial accumulate over the
+  // warp's atoms and are reduced once
+  for (int ia = 0; ia < A.apw; ia++) {
+  const int64_t i = w0 * A.apw + ia;
 #pragma unroll
   for (int p = 0; p < NPOT; p++)
 #pragma unroll
@@ -572,7 +573,12 @@ int yg_launch_pair(yg_ctx *ctx, int slot_mask, int want_grad) {
   A.want_grad = want_grad;
   SlotMap map;
   for (int q = 0; q < YG_MAX_POT; q++) map.slot[q] = q < npot ? slots[q] : 0;
-  const int nblocks = yg_blocks((N + YG_PAIR_ATOMS - 1) / YG_PAIR_ATOMS * 32, 256);
+  // atoms per warp: the most (up to YG_PAIR_ATOMS) that still leaves at
+  // least two full waves of warps (4 blocks of 8 warps per SM), so that a
+  // small system keeps the machine busy to the end
+  A.apw = 1;
+  while (2 * A.apw <= YG_PAIR_ATOMS && (N / (2 * A.apw)) >= (int64_t)2 * ctx->nsm * 32) A.apw *= 2;
+  const int nblocks = yg_blocks((N + A.apw - 1) / A.apw * 32, 256);
   const int nval = npot * 7;
   int rc;
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_red, &ctx->red_cap,
