@@ -343,9 +343,10 @@ def run_gb300(args, world, rank, local):
                       'accumulate',
             'ms': t_reci * 1e3, 'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18},
             'warp_mma_f16_peak_tflops': mma_probe,
-            'traffic': 76.3e6 * nat_scale,
-            'traffic_source': 'ncu dram read+write of k_sfac_mma (40.3 MB) + k_ewald_force_umma (35.9 MB) at '
-                              '50,000 atoms' + ('' if natom == 50000 else ', scaled by atoms')}
+            'traffic': 89.0e6 * nat_scale,
+            'traffic_source': 'ncu dram read+write of k_sfac_mma (40.3 MB) + k_ya_umma (12.8 MB) + '
+                              'k_ewald_force_umma (35.9 MB) at 50,000 atoms' +
+                              ('' if natom == 50000 else ', scaled by atoms')}
     elif tcode.value == 1:
         rooflines['ewald_reciprocal'] = {
             'bound': 'tensor', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s', 'peak': pk['bf16_tflops'],
@@ -377,9 +378,10 @@ def run_gb300(args, world, rank, local):
                   'entries within the pair cutoff at the front and the skin shell at the back, exact FP64 '
                   'decisions in the FP32 guard band)',
         'ms': t_build * 1e3, 'units': {'rows': nrow, 'bytes': bbytes},
-        'traffic': 310.2e6 * nat_scale,
-        'traffic_source': 'ncu dram read+write of k_build (the candidate sweep) at 50,000 atoms: it writes both '
-                          'directions of every pair' + ('' if natom == 50000 else ', scaled by atoms')}
+        'traffic': 312.8e6 * nat_scale,
+        'traffic_source': 'ncu dram read+write of k_build (the candidate sweep) at 50,000 atoms (6.0 MB read, 306.8 '
+                          'MB written): it writes both directions of every pair' +
+                          ('' if natom == 50000 else ', scaled by atoms')}
     # (b) pair terms: 75 flops (+3 transcendentals) per half-list pair within rcut; the pairs within rcut
     # are estimated from the list by the (rcut / (rcut + skin))^3 volume ratio
     t_pair = float(np.mean(phase_times['pair']))
@@ -392,9 +394,9 @@ def run_gb300(args, world, rank, local):
         'kernel': 'k_pair<MM3, EI> (one warp per atom over its full row; each pair is evaluated from both ends; '
                   'on a fresh list the skin shell at the back of the row is not read)',
         'ms': t_pair * 1e3, 'units': {'pairs_within_rcut': npair, 'flops_per_pair': 75, 'transcendentals_per_pair': 3},
-        'traffic': 380.1e6 * nat_scale,
-        'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms' + ('' if natom == 50000 else
-                                                                             ', scaled by atoms')}
+        'traffic': 302.4e6 * nat_scale,
+        'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms (295.7 MB read, 6.7 MB written; the '
+                          'skin shell is not read on a fresh list)' + ('' if natom == 50000 else ', scaled by atoms')}
     dom = max(rooflines, key=lambda k: rooflines[k]['ms'])
     roof = dict(rooflines[dom])
     roof['name'] = dom
