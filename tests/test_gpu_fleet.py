@@ -160,3 +160,26 @@ def test_fleet_engine_serves_rejects_and_cancels():
     solo.run([again], realtime=False)
     np.testing.assert_array_equal(again.log, reqs[7].log)
     np.testing.assert_array_equal(again.pos, reqs[7].pos)
+
+
+def test_fleet_rejects_systems_it_cannot_hold():
+    """A cell smaller than (rcut + skin) / 2.5 needs more than two periodic
+    images per axis, and a large cell with a fine reciprocal grid needs more
+    than 64 phase-table entries per atom: both are refused with
+    YG_ERR_ARG (a ValueError) before anything is copied, and the fleet keeps
+    stepping its other systems."""
+    from yaff_gb300 import configs
+    from yaff_gb300.units import femtosecond
+    dt = 0.5 * femtosecond
+    fl = _fleet()
+    ok = _reqs(1, nmax=300, nsteps=5, seed=4)[0]
+    s_ok = fl.add(ok.spec, _vel(ok), 5, dt)
+    tiny = configs.serving_request(2, 1)              # a 3.1 A cube, rcut 10 A: three images per axis
+    with pytest.raises(ValueError):
+        fl.add(tiny, np.zeros((2, 3)), 5, dt)
+    fine = configs.serving_request(400, 2)
+    fine['ewald'] = dict(fine['ewald'], gcut=fine['ewald']['gcut'] * 6.0)   # about 6x the k-vectors per axis
+    with pytest.raises(ValueError):
+        fl.add(fine, np.zeros((400, 3)), 5, dt)
+    res = _run(fl, [s_ok], 5)
+    assert not res[s_ok][3] and np.isfinite(res[s_ok][2]).all()
