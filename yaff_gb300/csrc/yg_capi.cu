@@ -15,6 +15,13 @@
 
 #include "yg_internal.cuh"
 
+// The result readback writes the gradient straight into the page-locked
+// host mirror through its device alias (1), or sums it in device memory and
+// moves it with the copy engine in chunks (0).
+#ifndef YG_RB_DIRECT
+#define YG_RB_DIRECT 1
+#endif
+
 namespace {
 thread_local std::string g_last_error;
 }
@@ -830,7 +837,11 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
   // can address it (checked once per context), so no separate copy follows
   if (c->h_total_dev_state == 0) {
     void *alias = nullptr;
+#if YG_RB_DIRECT
     const cudaError_t ae = cudaHostGetDevicePointer(&alias, c->h_total, 0);
+#else
+    const cudaError_t ae = cudaErrorNotSupported;  // always the copy-engine path
+#endif
     c->h_total_dev = (ae == cudaSuccess) ? (double *)alias : nullptr;
     c->h_total_dev_state = 1;
     if (ae != cudaSuccess) cudaGetLastError();  // clear the error of the query

@@ -29,8 +29,12 @@
 #ifndef YG_CELL_DIV
 #define YG_CELL_DIV 4      // grid cells at least r_c / 4 wide
 #endif
+#ifndef YG_BUILD_RUNS
 #define YG_BUILD_RUNS 192  // candidate runs per warp held in shared memory
+#endif
+#ifndef YG_BUILD_MAP
 #define YG_BUILD_MAP 3072  // candidates per warp whose run index is tabulated (4 blocks of 8 warps fit an SM)
+#endif
 
 namespace {
 

@@ -179,7 +179,10 @@ __device__ __forceinline__ void pot_entry(const PairArgs &A, int p, int j, float
 }
 
 template <int MODE, int NPOT, int K0 = -1, int K1 = -1>
-__global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? 4 : 1) k_pair(PairArgs A) {
+#ifndef YG_PAIR_MINB
+#define YG_PAIR_MINB 4  // resident blocks per SM the specialised mixed kernel is compiled for
+#endif
+__global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? YG_PAIR_MINB : 1) k_pair(PairArgs A) {
   typedef typename std::conditional<MODE == YG_FP64, double, float>::type T;
   const bool kahan = (MODE == YG_MIXED_KAHAN);
   __shared__ double red[8][NPOT * 7];
