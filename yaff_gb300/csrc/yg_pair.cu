@@ -179,8 +179,12 @@ __device__ __forceinline__ void pot_entry(const PairArgs &A, int p, int j, float
 }
 
 template <int MODE, int NPOT, int K0 = -1, int K1 = -1>
+// Resident blocks per SM the specialised mixed kernel is compiled for: 3
+// (79 registers, no spill) measured faster in the whole evaluation than 4 (64
+// registers with a small spill): 781-784 against 768-770 evaluations/s of the
+// 50,000-atom triclinic system.
 #ifndef YG_PAIR_MINB
-#define YG_PAIR_MINB 4  // resident blocks per SM the specialised mixed kernel is compiled for
+#define YG_PAIR_MINB 3
 #endif
 __global__ void __launch_bounds__(256, (MODE == YG_MIXED && NPOT <= 2) ? YG_PAIR_MINB : 1) k_pair(PairArgs A) {
   typedef typename std::conditional<MODE == YG_FP64, double, float>::type T;
