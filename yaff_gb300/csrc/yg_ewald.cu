@@ -36,6 +36,9 @@
 namespace {
 
 #define EW_SC 128    // columns per S-pass tile
+#ifndef YG_UMMA_SETUP
+#define YG_UMMA_SETUP 20.0  // tcgen05 force pass: a CTA's set-up cost in tile-equivalents (range choice)
+#endif
 #define EW_FC 64     // columns per force-pass tile
 #define EW_MS 32     // m values per S-pass slab
 #define EW_MAXM 64   // largest supported G2 + 1
@@ -1657,7 +1660,7 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
       // tile ranges per atom block: a CTA's time is its set-up (E0|E1 rows,
       // A operand, TMEM) plus its tiles (a K-step each and the epilogue), one
       // CTA per SM; the fewest ranges of the least estimated time
-      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = 20.0;
+      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = YG_UMMA_SETUP;
       int nr = 1;
       double best = 1e300;
       for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
@@ -1708,7 +1711,7 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
       // tile ranges per atom block: a CTA's time is its set-up (E0|E1 rows,
       // A operand, TMEM) plus its tiles (a K-step each and the epilogue), one
       // CTA per SM; the fewest ranges of the least estimated time
-      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = 20.0;
+      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = YG_UMMA_SETUP;
       int nr = 1;
       double best = 1e300;
       for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {

@@ -333,7 +333,10 @@ __device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
 // Dynamic shared memory of k_build per warp: runs, run offsets, candidate map.
 #define YG_BUILD_WARP_SMEM (YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4 + YG_BUILD_MAP)
 
-__global__ void __launch_bounds__(256, 4) k_build(BuildArgs A) {
+#ifndef YG_BUILD_MINB
+#define YG_BUILD_MINB 4  // resident blocks per SM of the candidate sweep
+#endif
+__global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char build_smem[];
   if (A.gate && !*A.gate) return;
   int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
