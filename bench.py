@@ -184,7 +184,7 @@ def run_gb300(args, world, rank, local):
     dpos = [torch.tensor(positions(s), dtype=torch.float64, device='cuda')
             for s in range(args.warmup + args.steps)]
 
-    def device_step(s, rebuild=True):
+    def device_step(s, rebuild=True, defer=True):
         # the order of ForceField.compute's fused path: positions, the
         # reciprocal sum (forked onto its own stream), list, pairs, the rest
         dev.upload_positions_device(dpos[s].data_ptr())
@@ -195,7 +195,7 @@ def run_gb300(args, world, rank, local):
                 mask |= 1 << p.device_slot
         if rebuild:
             ff.nlist.rebuild_next = True   # full neighbour-list rebuild every step
-        ff.nlist.update(upload=False)
+        ff.nlist.update(upload=False, defer=defer)   # enqueued; the readback reports an overflow
         pmask = 0
         for p in ff.parts:
             if isinstance(p, yaff_gb300.ForcePartPair):
@@ -209,9 +209,22 @@ def run_gb300(args, world, rank, local):
                 mask |= 1 << p.device_slot
         return mask
 
+    def step_total(s, rebuild=True, g=None, v=None):
+        # one evaluation and its readback; a deferred rebuild that overflowed a
+        # row (its capacity has grown) is redone with a waiting rebuild
+        mask = device_step(s, rebuild)
+        try:
+            dev.get_total(mask, g, v)
+        except _lib.YaffGBError as exc:
+            if exc.status != _lib.YG_ERR_CAPACITY:
+                raise
+            ff.nlist._pending = False
+            mask = device_step(s, True, defer=False)
+            dev.get_total(mask, g, v)
+        return mask
+
     for s in range(args.warmup):
-        mask = device_step(s)
-        dev.get_total(mask, gpos, vtens)
+        mask = step_total(s, True, gpos, vtens)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -226,8 +239,7 @@ def run_gb300(args, world, rank, local):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        mask = device_step(s)
-        dev.get_total(mask, None, None)
+        mask = step_total(s)
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) * 1e-3)
@@ -241,8 +253,7 @@ def run_gb300(args, world, rank, local):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        mask = device_step(s, rebuild=False)
-        dev.get_total(mask, None, None)
+        mask = step_total(s, rebuild=False)
         e1.record(stream)
         torch.cuda.synchronize()
         skin_times.append(e0.elapsed_time(e1) * 1e-3)
@@ -301,8 +312,7 @@ def run_gb300(args, world, rank, local):
     if args.precision != 'fp64' and args.fp64_steps > 0:
         dev.set_precision('fp64')
         for s in range(1):
-            device_step(s)
-            dev.get_total(mask, None, None)
+            mask = step_total(s)
         torch.cuda.synchronize()
         tt = []
         for s in range(args.fp64_steps):
@@ -310,8 +320,7 @@ def run_gb300(args, world, rank, local):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            mask = device_step(s)
-            dev.get_total(mask, None, None)
+            mask = step_total(s)
             e1.record(stream)
             torch.cuda.synchronize()
             tt.append(e0.elapsed_time(e1) * 1e-3)
@@ -320,7 +329,7 @@ def run_gb300(args, world, rank, local):
 
     # precision sweep: every form's speed on this workload and its error
     # against the reference's own FP64 evaluation of the same positions
-    sweep = None if args.no_sweep else precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64,
+    sweep = None if args.no_sweep else precision_sweep(ff, dev, spec, args, step_total, stream, flush, fp64,
                                                          1.0 / t_step)
 
     pk, pk_src = peaks()
@@ -433,7 +442,7 @@ def workload_config(natom):
                         % format(natom, ','), 'natom': natom}
 
 
-def precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64_rate, main_rate):
+def precision_sweep(ff, dev, spec, args, step_total, stream, flush, fp64_rate, main_rate):
     """Each precision form against the reference: the error of one
     ForceField.compute(gpos, vtens) at the workload's own positions against
     tests/golden/big_triclinic50000.npz (the reference yaff ForceField.compute
@@ -506,8 +515,7 @@ def precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64_rate, 
             row['evals_per_s'] = main_rate
         else:
             for s in range(2):
-                mask = device_step(s)
-                dev.get_total(mask, None, None)
+                mask = step_total(s)
             torch.cuda.synchronize()
             tt = []
             for s in range(5):
@@ -515,8 +523,7 @@ def precision_sweep(ff, dev, spec, args, device_step, stream, flush, fp64_rate, 
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                mask = device_step(s)
-                dev.get_total(mask, None, None)
+                mask = step_total(s)
                 e1.record(stream)
                 torch.cuda.synchronize()
                 tt.append(e0.elapsed_time(e1) * 1e-3)

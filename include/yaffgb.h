@@ -185,6 +185,19 @@ int yg_ewald_force_path(yg_ctx *ctx, int path);
  * synchronization), e.g. to time it with events on the context's stream. */
 int yg_ewald_wait(yg_ctx *ctx);
 
+/* The same build enqueued without waiting for its outcome (nlist.c:30-180 as
+ * yg_nlist_build): the pair terms can be enqueued behind it at once, so the
+ * GPU does not idle while the host learns the row count.  yg_nlist_build_wait
+ * returns its outcome: YG_OK with the reference's row count in *nneigh, or
+ * YG_ERR_CAPACITY when a row overflowed its slots (the slot capacity is grown;
+ * the rows and every pair result computed from them are invalid: build again,
+ * e.g. with yg_nlist_build, and recompute), or YG_ERR_NAN for a position that
+ * could not be binned.  yg_get_total, yg_get_part, yg_nlist_export,
+ * yg_nlist_recompute and the MD entry points wait for it themselves and return
+ * that error before they read anything the rows produced. */
+int yg_nlist_build_async(yg_ctx *ctx, double rcut_total, const int64_t *rmax, int64_t nlow, int64_t nhigh);
+int yg_nlist_build_wait(yg_ctx *ctx, int64_t *nneigh);
+
 /* Skin path: keeps the pairs of the last rebuild and re-evaluates relative
  * vectors from the current positions.  Replaces nlist_recompute_low
  * (yaff/pes/nlist.c:183-232). */

@@ -65,6 +65,8 @@ SIGNATURES = {
     'yg_ewald_force_path': (_I, [_P, _I]),
     'yg_check_wait_timeout': (_I, [_P, _I64, ctypes.POINTER(_I)]),
     'yg_nlist_recompute': (_I, [_P]),
+    'yg_nlist_build_async': (_I, [_P, ctypes.c_double, _P, _I64, _I64]),
+    'yg_nlist_build_wait': (_I, [_P, ctypes.POINTER(_I64)]),
     'yg_nlist_max_disp2': (_I, [_P, ctypes.POINTER(_D)]),
     'yg_nlist_export': (_I, [_P, _P, _I64, ctypes.POINTER(_I64)]),
     'yg_pair_compute': (_I, [_P, _I, _I]),

@@ -620,6 +620,10 @@ int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nl
   c->rcut_total = rcut_total;
   c->nlow = nlow;
   c->nhigh = nhigh;
+  if (c->build_pending) {  // superseded: its status no longer matters
+    YG_CUDA(cudaEventSynchronize(c->build_ev));
+    c->build_pending = 0;
+  }
   int retry = 0;
   int rc = yg_launch_nlist_build(c, rcut_total * rcut_total, &retry);
   if (rc) {
@@ -633,8 +637,53 @@ int yg_nlist_build(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nl
   return YG_OK;
 }
 
+int yg_nlist_build_async(yg_ctx *c, double rcut_total, const int64_t *rmax, int64_t nlow, int64_t nhigh) {
+  if (!c || !rmax || !(rcut_total > 0.0)) return YG_ERR_ARG;
+  if (!c->have_cell || !c->have_pos) {
+    yg_set_error("set the cell and the positions before building the neighbour list");
+    return YG_ERR_STATE;
+  }
+  if (nlow < 0 || nhigh < nlow || nhigh > c->natom) {
+    yg_set_error("need 0 <= nlow <= nhigh <= natom");
+    return YG_ERR_ARG;
+  }
+  if (c->natom / c->cell.volume > 10.0) {
+    yg_set_error("Atom density too high");
+    return YG_ERR_DENSITY;
+  }
+  for (int k = 0; k < 3; k++) {
+    if (rmax[k] < 0 || rmax[k] > 1000) return YG_ERR_ARG;
+    c->rmax[k] = rmax[k];
+  }
+  c->rcut_total = rcut_total;
+  c->nlow = nlow;
+  c->nhigh = nhigh;
+  if (c->build_pending) {
+    YG_CUDA(cudaEventSynchronize(c->build_ev));
+    c->build_pending = 0;
+  }
+  const int rc = yg_launch_nlist_build_async(c, rcut_total * rcut_total);
+  if (rc) {
+    c->have_list = 0;
+    return rc;
+  }
+  for (int p = 0; p < YG_MAX_POT; p++) c->part_valid[YG_PART_PAIR0 + p] = 0;
+  return YG_OK;
+}
+
+int yg_nlist_build_wait(yg_ctx *c, int64_t *nneigh) {
+  if (!c) return YG_ERR_ARG;
+  const int rc = yg_launch_nlist_build_wait(c);
+  if (rc == YG_OK && nneigh) *nneigh = c->nneigh;
+  return rc;
+}
+
 int yg_nlist_recompute(yg_ctx *c) {
   if (!c) return YG_ERR_ARG;
+  if (c->build_pending) {
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) return wrc;
+  }
   if (!c->have_list || !c->rows_valid) {
     yg_set_error("no neighbour list to recompute");
     return YG_ERR_STATE;
@@ -654,6 +703,10 @@ int yg_nlist_max_disp2(yg_ctx *c, double *out) {
 
 int yg_nlist_export(yg_ctx *c, yg_neigh_row *rows, int64_t cap, int64_t *n) {
   if (!c || !n) return YG_ERR_ARG;
+  if (c->build_pending) {
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) return wrc;
+  }
   if (!c->have_list || !c->rows_valid) {
     yg_set_error("no neighbour list");
     return YG_ERR_STATE;
@@ -787,6 +840,13 @@ int yg_get_part(yg_ctx *c, int part, double *energy, double *gpos, double *vtens
     if (jrc) return jrc;
   }
   if (!c || part < 0 || part >= YG_NPART) return YG_ERR_ARG;
+  if (c->build_pending) {
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) {
+      for (int p = 0; p < YG_MAX_POT; p++) c->part_valid[YG_PART_PAIR0 + p] = 0;
+      return wrc;
+    }
+  }
   if (!c->part_valid[part]) {
     yg_set_error("part has no valid result for the current positions");
     return YG_ERR_STATE;
@@ -824,6 +884,13 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
     if (jrc) return jrc;
   }
   if (!c) return YG_ERR_ARG;
+  if (c->build_pending) {  // the rows of an enqueued build fed the pair parts
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) {
+      for (int p = 0; p < YG_MAX_POT; p++) c->part_valid[YG_PART_PAIR0 + p] = 0;
+      return wrc;
+    }
+  }
   for (int p = 0; p < YG_NPART; p++)
     if ((part_mask & (1 << p)) && !c->part_valid[p]) {
       yg_set_error("a requested part has no valid result");

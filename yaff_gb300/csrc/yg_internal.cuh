@@ -288,6 +288,8 @@ struct yg_ctx {
   double *d_total = nullptr;      // 10 + natom*3
   double *h_total = nullptr;      // pinned mirror
   cudaEvent_t rb_ev[YG_RB_CHUNKS] = {};  // chunks of the gradient readback
+  cudaEvent_t build_ev = nullptr; // an enqueued build's status and count have arrived (h_status, h_u64[6])
+  int build_pending = 0;          // a build was enqueued without waiting for its status
   double *h_total_dev = nullptr;  // device alias of h_total (page-locked, mapped), when the device has one
   int h_total_dev_state = 0;      // 0: not queried yet
   double *d_red = nullptr;        // block partials for energy/virial reductions
@@ -383,6 +385,8 @@ __device__ __forceinline__ bool img_zero(const int *r) {
 
 // ------------------------------------------------------- launchers (host)
 int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry);
+int yg_launch_nlist_build_async(yg_ctx *ctx, double rc2);
+int yg_launch_nlist_build_wait(yg_ctx *ctx);
 int yg_launch_nlist_build_gated(yg_ctx *ctx, const int *gate, unsigned long long *total);
 int yg_launch_max_disp2_async(yg_ctx *ctx, unsigned long long *out);
 int yg_launch_nlist_export(yg_ctx *ctx, yg_neigh_row *rows_host, int64_t cap, int64_t *n);

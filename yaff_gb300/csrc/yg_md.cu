@@ -437,6 +437,10 @@ int yg_md_setup(yg_ctx *c, const double *masses, const double *vel, double dt, i
     const int jrc = yg_ewald_join(c);
     if (jrc) return jrc;
   }
+  if (c && c->build_pending) {
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) return wrc;
+  }
   if (!c || !masses || !vel || !(dt > 0.0) || max_steps < 1) return YG_ERR_ARG;
   if (!c->have_list) {
     yg_set_error("yg_md_setup: build the neighbour list first");
@@ -505,6 +509,10 @@ int yg_md_run(yg_ctx *c, int64_t nsteps, int use_graph, double skin, int64_t *nr
   if (!c->md_ready) {
     yg_set_error("yg_md_run: call yg_md_setup first");
     return YG_ERR_STATE;
+  }
+  if (c->build_pending) {
+    const int wrc = yg_launch_nlist_build_wait(c);
+    if (wrc) return wrc;
   }
   if (c->md_steps_done + nsteps > c->md_max_steps) {
     yg_set_error("yg_md_run: more steps than the energy log holds");

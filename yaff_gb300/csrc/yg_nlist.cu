@@ -1081,6 +1081,61 @@ int yg_launch_nlist_build(yg_ctx *ctx, double rc2, int *retry) {
   return YG_OK;
 }
 
+// One build enqueued without waiting: its status words and pair count are
+// copied to the page-locked mirrors behind it and ctx->build_ev marks their
+// arrival; the pair parameters are repacked behind it too.  The rows are used
+// at once (the pair terms are enqueued after the build on the same stream);
+// yg_nlist_build_wait reports an overflow or a bad position before any result
+// that used them is read.
+int yg_launch_nlist_build_async(yg_ctx *ctx, double rc2) {
+  int rc_;
+  if ((rc_ = nlist_geometry(ctx, rc2))) return rc_;
+  const int64_t need = ctx->nbr_cap * ctx->natom;
+  if (need > ctx->nbr_alloc) {
+    yg_free(ctx, (void **)&ctx->d_nbr);
+    if ((rc_ = yg_alloc(ctx, (void **)&ctx->d_nbr, (size_t)need * sizeof(uint2)))) return rc_;
+    ctx->nbr_alloc = need;
+  }
+  unsigned long long *dtot = (unsigned long long *)ctx->d_red;
+  YG_CUDA(cudaMemsetAsync(ctx->d_status, 0, YG_ST_NWORDS * sizeof(int), ctx->stream));
+  if ((rc_ = enqueue_build(ctx, rc2, nullptr, dtot))) return rc_;
+  YG_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  YG_CUDA(cudaMemcpyAsync(ctx->h_u64 + 6, dtot, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!ctx->build_ev) YG_CUDA(cudaEventCreateWithFlags(&ctx->build_ev, cudaEventDisableTiming));
+  YG_CUDA(cudaEventRecord(ctx->build_ev, ctx->stream));
+  ctx->build_pending = 1;
+  ctx->have_list = 1;
+  ctx->rows_valid = 1;
+  ctx->list_recomputed = 0;
+  ctx->rin_build = pair_split(ctx);
+  ctx->x_fresh = 1;
+  return yg_pack_pair_params(ctx);
+}
+
+// Waits for an enqueued build's status.  YG_OK: ctx->nneigh holds its pair
+// count.  YG_ERR_CAPACITY: a row overflowed; the slot capacity is grown and
+// the rows are invalid until the next build (results computed from them must
+// be recomputed).  YG_ERR_NAN: a position could not be binned.
+int yg_launch_nlist_build_wait(yg_ctx *ctx) {
+  if (!ctx->build_pending) return YG_OK;
+  ctx->build_pending = 0;
+  YG_CUDA(cudaEventSynchronize(ctx->build_ev));
+  if (ctx->h_status[YG_ST_BADCELL]) {
+    ctx->rows_valid = 0;
+    yg_set_error("non-finite or huge position met while binning atoms");
+    return YG_ERR_NAN;
+  }
+  if (ctx->h_status[YG_ST_OVERFLOW]) {
+    const int64_t cap = (int64_t)(ctx->h_status[YG_ST_MAXCOUNT] * 1.15) + 64;
+    ctx->nbr_cap = (cap + 31) / 32 * 32;
+    ctx->rows_valid = 0;
+    yg_set_error("a neighbour row overflowed its slots; rebuild the list and recompute");
+    return YG_ERR_CAPACITY;
+  }
+  ctx->nneigh = (int64_t)(ctx->h_u64[6] / 2);
+  return YG_OK;
+}
+
 // A rebuild that runs only when *gate is set, for the device-driven step:
 // no host synchronization; overflow and bad positions accumulate in the
 // status words (cleared by the caller), the pair count goes to *total.

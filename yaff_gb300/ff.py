@@ -188,11 +188,21 @@ class ForceField(ForcePart):
         self._ncall = getattr(self, '_ncall', 0) + 1
         dev.call_key = (id(self), self._ncall)
         try:
-            return self._fused_compute(dev, gpos, vtens, add)
+            try:
+                return self._fused_compute(dev, gpos, vtens, add, defer=True)
+            except _lib.YaffGBError as exc:
+                if exc.status != _lib.YG_ERR_CAPACITY or self.nlist is None:
+                    raise
+                # the enqueued rebuild overflowed a row (its capacity has grown);
+                # nothing reached the caller's arrays: rebuild and evaluate again
+                self.nlist._pending = False
+                self.nlist.rebuild_next = True
+                self.needs_nlist_update = True
+                return self._fused_compute(dev, gpos, vtens, add, defer=False)
         finally:
             dev.call_key = None
 
-    def _fused_compute(self, dev, gpos, vtens, add):
+    def _fused_compute(self, dev, gpos, vtens, add, defer=False):
         want_grad = (gpos is not None) or (vtens is not None)
         mask = 0
         for part in self.parts:
@@ -200,7 +210,10 @@ class ForceField(ForcePart):
                 part._launch(want_grad)
                 mask |= 1 << part.device_slot
         if self.needs_nlist_update:
-            self.nlist.update(upload=False)
+            # the rebuild is enqueued without waiting for its row count: the
+            # pair terms follow it on the stream at once; the readback below
+            # reports an overflow before anything is added to gpos / vtens
+            self.nlist.update(upload=False, defer=defer)
             self.needs_nlist_update = False
         pair_parts = [p for p in self.parts if isinstance(p, ForcePartPair)]
         if pair_parts:

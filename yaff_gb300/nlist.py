@@ -32,7 +32,8 @@ class NeighborList(object):
         self.system = system
         self.skin = skin
         self.rcut = 0.0
-        self.nneigh = 0
+        self._nneigh = 0
+        self._pending = False   # a build was enqueued without waiting for its row count
         self.rmax = None
         if nlow < 0:
             raise ValueError('nlow must be a positive number, received %d.' % nlow)
@@ -80,8 +81,40 @@ class NeighborList(object):
         self.rebuild_next = True
         self._neighs_cache = None
 
-    def update(self, upload=True):
-        """Rebuild or recompute the list for the current system positions."""
+    @property
+    def nneigh(self):
+        """Number of rows of the list (the reference's half-list count)."""
+        if self._pending:
+            self.finish()
+        return self._nneigh
+
+    @nneigh.setter
+    def nneigh(self, value):
+        self._nneigh = value
+
+    def finish(self):
+        """Outcome of a build enqueued by update(defer=True): sets nneigh, or,
+        when a row overflowed its slots, rebuilds the list now (the slot
+        capacity has grown) and returns False: whatever was computed from the
+        deferred build's rows must be recomputed."""
+        if not self._pending:
+            return True
+        self._pending = False
+        n = ctypes.c_int64()
+        rc = self.device.lib.yg_nlist_build_wait(self.device.ctx, ctypes.byref(n))
+        if rc == _lib.YG_ERR_CAPACITY:
+            self.rebuild_next = True
+            self.update(upload=False)
+            return False
+        check(rc, 'yg_nlist_build_wait')
+        self._nneigh = n.value
+        return True
+
+    def update(self, upload=True, defer=False):
+        """Rebuild or recompute the list for the current system positions.
+        With defer, a rebuild is enqueued without waiting for its row count
+        (the caller enqueues the pair terms behind it; finish() or any result
+        readback reports an overflow)."""
         assert self.rcut > 0
         dev = self.device
         dev.sync_cell()
@@ -98,10 +131,16 @@ class NeighborList(object):
                 raise ValueError('Atom density too high')
             rmax = np.zeros(3, np.int64)
             rmax[:len(self.rmax)] = self.rmax
-            n = ctypes.c_int64()
-            check(dev.lib.yg_nlist_build(dev.ctx, self.rcut + self.skin, ptr(rmax), self.nlow, self.nhigh,
-                                         ctypes.byref(n)), 'yg_nlist_build')
-            self.nneigh = n.value
+            if defer:
+                check(dev.lib.yg_nlist_build_async(dev.ctx, self.rcut + self.skin, ptr(rmax), self.nlow,
+                                                   self.nhigh), 'yg_nlist_build_async')
+                self._pending = True
+            else:
+                self._pending = False
+                n = ctypes.c_int64()
+                check(dev.lib.yg_nlist_build(dev.ctx, self.rcut + self.skin, ptr(rmax), self.nlow, self.nhigh,
+                                             ctypes.byref(n)), 'yg_nlist_build')
+                self._nneigh = n.value
             self._built = True
             self._epoch = dev.list_epoch
             self.rebuild_next = False
