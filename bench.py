@@ -50,6 +50,9 @@ def parse():
                     help='serving: the fleet engine only (no per-context engine, no sequential FP64 baseline)')
     ap.add_argument('--mc-rounds', type=int, default=10, help='MC trial-energy batches per precision (0: skip)')
     ap.add_argument('--nve-steps', type=int, default=1000, help='steps of the 24,000-atom water NVE run (0: skip)')
+    ap.add_argument('--sfac-path', type=int, default=0, choices=[0, 1, 2],
+                    help='structure-factor pass of the main workload: 0 automatic (warp-level MMA), '
+                         '1 warp-level MMA, 2 tcgen05')
     return ap.parse_args()
 
 
@@ -170,6 +173,7 @@ def run_gb300(args, world, rank, local):
     rng = np.random.default_rng(7 + rank)
     ff = yaff_gb300.build_forcefield(spec, precision=args.precision)
     dev = yaff_gb300.device_of(ff.system)
+    _lib.check(dev.lib.yg_ewald_sfac_path(dev.ctx, args.sfac_path), 'yg_ewald_sfac_path')
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
     pos0 = spec['pos'].copy()
@@ -347,9 +351,10 @@ def run_gb300(args, world, rank, local):
         rooflines['ewald_reciprocal'] = {
             'bound': 'tensor', 'achieved': flops / t_reci / 1e12, 'unit': 'TFLOP/s', 'peak': pk['bf16_tflops'],
             'peak_source': pk_src + ' dense bf16 (burst)', 'frac': flops / t_reci / 1e12 / pk['bf16_tflops'],
-            'kernel': 'k_tables_mma + k_ys_mma + k_sfac_mma (S pass, warp MMA) + k_ya_umma + k_ewald_force_umma '
-                      '(force pass, tcgen05 with TMEM accumulators) + combine/gpos; FP16 hi/lo split, FP32 '
-                      'accumulate',
+            'kernel': 'k_tables_mma + ' + ('k_yb_umma + k_sfac_umma (S pass, tcgen05)' if args.sfac_path == 2
+                                            else 'k_ys_mma + k_sfac_mma (S pass, warp MMA)') +
+                      ' + k_ya_umma + k_ewald_force_umma (force pass, tcgen05 with TMEM accumulators) + '
+                      'combine/gpos; FP16 hi/lo split, FP32 accumulate',
             'ms': t_reci * 1e3, 'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18},
             'warp_mma_f16_peak_tflops': mma_probe,
             'traffic': 89.0e6 * nat_scale,

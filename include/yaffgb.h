@@ -178,6 +178,14 @@ int yg_check_wait_timeout(yg_ctx *ctx, int64_t polls, int *timed_out);
  * the warp-level MMA form.  Both compute the same sums. */
 int yg_ewald_force_path(yg_ctx *ctx, int path);
 
+/* Selects the kernel of the mixed-precision structure-factor (S) pass (no
+ * reference counterpart): 0 automatic (the warp-level MMA form, the faster
+ * one on GB300), 1 the warp-level MMA form, 2 the tcgen05 form (TMEM
+ * accumulators; where its staging does not fit, the warp-level form runs).
+ * Both compute the same sums (FP16-split products, FP32 accumulation over
+ * at most 32 atoms, chunk partials summed in a fixed order). */
+int yg_ewald_sfac_path(yg_ctx *ctx, int path);
+
 /* The reciprocal sum runs on an auxiliary stream of the context, forked at
  * yg_ewald_reci, so that it overlaps the neighbour build and the pair terms;
  * every call that reads its results or changes its inputs joins it back.

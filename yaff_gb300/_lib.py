@@ -63,6 +63,7 @@ SIGNATURES = {
     'yg_ewald_info': (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64)]),
     'yg_ewald_wait': (_I, [_P]),
     'yg_ewald_force_path': (_I, [_P, _I]),
+    'yg_ewald_sfac_path': (_I, [_P, _I]),
     'yg_check_wait_timeout': (_I, [_P, _I64, ctypes.POINTER(_I)]),
     'yg_nlist_recompute': (_I, [_P]),
     'yg_nlist_build_async': (_I, [_P, ctypes.c_double, _P, _I64, _I64]),

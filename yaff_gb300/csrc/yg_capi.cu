@@ -591,6 +591,14 @@ int yg_ewald_force_path(yg_ctx *c, int path) {
   return YG_OK;
 }
 
+int yg_ewald_sfac_path(yg_ctx *c, int path) {
+  if (!c || path < 0 || path > 2) return YG_ERR_ARG;
+  int rc;
+  if ((rc = yg_ewald_join(c))) return rc;
+  c->ew_sfac_path = path;
+  return YG_OK;
+}
+
 int yg_nlist_stats(yg_ctx *c, int64_t *nexact, int64_t *maxrow) {
   if (!c) return YG_ERR_ARG;
   if (nexact) *nexact = c->h_status[YG_ST_EXACT];

@@ -954,61 +954,74 @@ __device__ __forceinline__ void mma_split(float (&d)[4], const unsigned (&ah)[4]
   mma_f16(d, al, bh0, bh1);
 }
 
-// MMA tables, one warp per atom (lanes 0-2 form the fractional coordinate
-// of one axis each in FP64, the lanes then share them and take one table
-// entry each):
+// MMA tables, 32 atoms per block of 256 threads: threads 0-95 form the
+// fractional coordinate of one (atom, axis) each in FP64 and threads 96-127
+// the scaled charges (FP64 work once per atom and axis, not once per atom
+// and warp: the FP64 pipe is narrow); each warp then fills the rows of four
+// atoms, its lanes taking one table entry each:
 //   te[a][0..G0] = E0, te[a][G0+1..G0+G1+1] = E1 (float2, row stride lep);
 //   yf[a][m] = (hi, lo) FP16 pairs of qscale q E2[m] (re in the low half),
 //              m < nmf (zero beyond G2).
 // The phases follow k_tables' FP32 form.
-__global__ void k_tables_mma(const double *__restrict__ pos, const double *__restrict__ charge, int64_t natom,
-                             CellGeom cell, int G0, int G1, int G2, float qscale, int lep, int nmf,
-                             float2 *__restrict__ te, uint2 *__restrict__ yf) {
-  const int64_t a = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (a >= natom) return;
-  float sh = 0.f, sl = 0.f;
-  if (lane < 3) {
-    const double *gv = cell.gv + 3 * lane;
-    double sd = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
-    sd -= floor(sd);
-    sh = (float)sd;
-    sl = (float)(sd - (double)sh);
-  }
-  const float sh0 = __shfl_sync(0xffffffffu, sh, 0), sl0 = __shfl_sync(0xffffffffu, sl, 0);
-  const float sh1 = __shfl_sync(0xffffffffu, sh, 1), sl1 = __shfl_sync(0xffffffffu, sl, 1);
-  const float sh2 = __shfl_sync(0xffffffffu, sh, 2), sl2 = __shfl_sync(0xffffffffu, sl, 2);
-  const float q = (float)(charge[a] * (double)qscale);
-  const int ne = G0 + G1 + 2;
-  for (int slot = lane; slot < ne + nmf; slot += 32) {
-    int g;
-    float s_hi, s_lo;
-    if (slot <= G0) {
-      g = slot;
-      s_hi = sh0;
-      s_lo = sl0;
-    } else if (slot < ne) {
-      g = slot - (G0 + 1);
-      s_hi = sh1;
-      s_lo = sl1;
-    } else {
-      g = slot - ne;
-      s_hi = sh2;
-      s_lo = sl2;
+__global__ void __launch_bounds__(256) k_tables_mma(const double *__restrict__ pos, const double *__restrict__ charge,
+                                                    int64_t natom, CellGeom cell, int G0, int G1, int G2,
+                                                    float qscale, int lep, int nmf, float2 *__restrict__ te,
+                                                    uint2 *__restrict__ yf) {
+  __shared__ float s_sh[32][3], s_sl[32][3], s_q[32];
+  const int t = threadIdx.x;
+  const int64_t a0 = (int64_t)blockIdx.x * 32;
+  if (t < 96) {
+    const int la = t / 3, ax = t - 3 * (t / 3);
+    const int64_t a = a0 + la;
+    float sh = 0.f, sl = 0.f;
+    if (a < natom) {
+      const double *gv = cell.gv + 3 * ax;
+      double sd = gv[0] * pos[3 * a] + gv[1] * pos[3 * a + 1] + gv[2] * pos[3 * a + 2];
+      sd -= floor(sd);
+      sh = (float)sd;
+      sl = (float)(sd - (double)sh);
     }
-    const float fg = (float)g;
-    const float pp = fg * s_hi;
-    const float e = fmaf(fg, s_hi, -pp);
-    const float x = (pp - rintf(pp)) + fmaf(fg, s_lo, e);
-    float sn, c;
-    sincospif(2.0f * x, &sn, &c);
-    if (slot < ne) {
-      te[a * lep + slot] = make_float2(c, sn);
-    } else {
-      const bool used = g <= G2;
-      unsigned hi, lo;
-      split_h2(used ? q * c : 0.f, used ? q * sn : 0.f, hi, lo);
-      yf[a * nmf + g] = make_uint2(hi, lo);
+    s_sh[la][ax] = sh;
+    s_sl[la][ax] = sl;
+  } else if (t < 128) {
+    const int64_t a = a0 + (t - 96);
+    s_q[t - 96] = a < natom ? (float)(charge[a] * (double)qscale) : 0.f;
+  }
+  __syncthreads();
+  const int w = t >> 5, lane = t & 31;
+  const int ne = G0 + G1 + 2;
+  for (int k = 0; k < 4; k++) {
+    const int la = 4 * w + k;
+    const int64_t a = a0 + la;
+    if (a >= natom) break;
+    const float q = s_q[la];
+    for (int slot = lane; slot < ne + nmf; slot += 32) {
+      int g, ax;
+      if (slot <= G0) {
+        g = slot;
+        ax = 0;
+      } else if (slot < ne) {
+        g = slot - (G0 + 1);
+        ax = 1;
+      } else {
+        g = slot - ne;
+        ax = 2;
+      }
+      const float s_hi = s_sh[la][ax], s_lo = s_sl[la][ax];
+      const float fg = (float)g;
+      const float pp = fg * s_hi;
+      const float e = fmaf(fg, s_hi, -pp);
+      const float x = (pp - rintf(pp)) + fmaf(fg, s_lo, e);
+      float sn, c;
+      sincospif(2.0f * x, &sn, &c);
+      if (slot < ne) {
+        te[a * lep + slot] = make_float2(c, sn);
+      } else {
+        const bool used = g <= G2;
+        unsigned hi, lo;
+        split_h2(used ? q * c : 0.f, used ? q * sn : 0.f, hi, lo);
+        yf[a * nmf + g] = make_uint2(hi, lo);
+      }
     }
   }
 }
@@ -1574,36 +1587,51 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   if ((rc = yg_ensure(ctx, &ctx->d_ew_te, &ctx->ew_bytes_te, (size_t)(N + EW_MMA_TEPAD) * lep * sizeof(float2))))
     return rc;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_yf, &ctx->ew_bytes_yf, (size_t)N * nmf * sizeof(uint2)))) return rc;
-  const size_t ys_bytes = (size_t)ys_blocks * nms * 8 * sizeof(uint4);
+  // S pass: the warp-level MMA form (faster here), or on request the tcgen05
+  // form (B operand nks KB per 16-atom block) where its staging fits
+  const bool usf = ctx->ew_sfac_path == 2 && nks <= yg_umma_kmax() && yg_umma_sfac_smem(lep) > 0;
+  const size_t ys_bytes = usf ? (size_t)ys_blocks * nks * 1024 : (size_t)ys_blocks * nms * 8 * sizeof(uint4);
   if ((rc = yg_ensure(ctx, &ctx->d_ew_ys, &ctx->ew_bytes_ys, ys_bytes))) return rc;
   float2 *te = (float2 *)ctx->d_ew_te;
   YG_CUDA(cudaMemsetAsync(te + (size_t)N * lep, 0, (size_t)EW_MMA_TEPAD * lep * sizeof(float2), ctx->stream));
-  k_tables_mma<<<yg_blocks(N * 32, 256), 256, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2,
-                                                                (float)qscale, lep, nmf, te, (uint2 *)ctx->d_ew_yf);
+  k_tables_mma<<<yg_blocks(N, 32), 256, 0, ctx->stream>>>(ctx->d_pos, ctx->d_charge, N, ctx->cell, G0, G1, G2,
+                                                          (float)qscale, lep, nmf, te, (uint2 *)ctx->d_ew_yf);
   YG_LAUNCH_CHECK(ctx, "k_tables_mma");
-  k_ys_mma<<<yg_blocks(ys_blocks * nms * 8, 256), 256, 0, ctx->stream>>>(
-      (const uint2 *)ctx->d_ew_yf, N, lo, hi, gbase[1], gbase[2], ys_blocks, nmf, nms, (uint4 *)ctx->d_ew_ys);
-  YG_LAUNCH_CHECK(ctx, "k_ys_mma");
+  if (usf) {
+    if ((rc = yg_launch_yb_umma(ctx, ctx->d_ew_yf, lo, hi, gbase[1], gbase[2], ys_blocks, nmf, nks, ctx->d_ew_ys)))
+      return rc;
+  } else {
+    k_ys_mma<<<yg_blocks(ys_blocks * nms * 8, 256), 256, 0, ctx->stream>>>(
+        (const uint2 *)ctx->d_ew_yf, N, lo, hi, gbase[1], gbase[2], ys_blocks, nmf, nms, (uint4 *)ctx->d_ew_ys);
+    YG_LAUNCH_CHECK(ctx, "k_ys_mma");
+  }
   // structure factors
+  const int atb = usf ? yg_umma_sfac_atb() : EW_MMA_ATB;
   int maxchunk = 1;
-  for (int g = 0; g < nS; g++)
-    maxchunk = std::max(maxchunk, (int)((gb[g][1] - gb[g][0] + EW_MMA_ATB - 1) / EW_MMA_ATB));
+  for (int g = 0; g < nS; g++) maxchunk = std::max(maxchunk, (int)((gb[g][1] - gb[g][0] + atb - 1) / atb));
   const size_t per = (size_t)ntile64 * 64 * EW_MS;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(float2)))) return rc;
   const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
-  if ((rc = yg_smem_optin((const void *)k_sfac_mma, ssm))) return rc;
+  if (!usf && (rc = yg_smem_optin((const void *)k_sfac_mma, ssm))) return rc;
   for (int g = 0; g < nS; g++) {
     const int64_t n = gb[g][1] - gb[g][0];
     double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     if (n <= 0) continue;
-    const int nch = (int)((n + EW_MMA_ATB - 1) / EW_MMA_ATB);
-    dim3 grid(nch, ntile64, 1);
-    k_sfac_mma<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
-                                               (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8,
-                                               (int)n, G0, lep, nms, (const int4 *)ctx->d_ew_tiles,
-                                               (float2 *)ctx->d_ew_Spart, ntile64, 1, ctx->d_status);
-    YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
+    const int nch = (int)((n + atb - 1) / atb);
+    if (usf) {
+      if ((rc = yg_launch_sfac_umma(ctx, te + (size_t)gb[g][0] * lep,
+                                    (const unsigned char *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nks * 1024, (int)n,
+                                    G0, lep, nks, ctx->d_ew_tiles, ctx->d_ew_Spart, ntile64, EW_MS)))
+        return rc;
+    } else {
+      dim3 grid(nch, ntile64, 1);
+      k_sfac_mma<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
+                                                 (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8,
+                                                 (int)n, G0, lep, nms, (const int4 *)ctx->d_ew_tiles,
+                                                 (float2 *)ctx->d_ew_Spart, ntile64, 1, ctx->d_status);
+      YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
+    }
     k_sfac_reduce<float><<<yg_blocks((int64_t)per * 4, 256), 256, 0, ctx->stream>>>(
         (const float2 *)ctx->d_ew_Spart, nch, ntile64, 1, 64, (const int4 *)ctx->d_ew_tiles, nm, 1.0 / qscale, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
@@ -1644,57 +1672,6 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   }
   // force pass, per atom group
   if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_gpart, &ctx->ew_bytes_gpart, (size_t)N * 3 * sizeof(double)))) return rc;
-  if (umma) {
-    // tcgen05: one CTA per SM (all of TMEM), blocks of 128 atoms x tile ranges
-    int dev = 0, nsm = 1;
-    YG_CUDA(cudaGetDevice(&dev));
-    YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    int64_t maxblk = 1;
-    for (int g = 0; g < nS; g++) maxblk = std::max<int64_t>(maxblk, (gb[g][1] - gb[g][0] + 127) / 128);
-    if ((rc = yg_ensure(ctx, &ctx->d_ew_ya, &ctx->ew_bytes_ya, (size_t)maxblk * nks * 2 * 4096))) return rc;
-    for (int g = 0; g < nS; g++) {
-      const int64_t n = gb[g][1] - gb[g][0];
-      if (n <= 0) continue;
-      const int nab = (int)((n + 127) / 128);
-      if ((rc = yg_launch_ya_umma(ctx, ctx->d_ew_yf, gb[g][0], n, nmf, nks, nab, ctx->d_ew_ya))) return rc;
-      // tile ranges per atom block: a CTA's time is its set-up (E0|E1 rows,
-      // A operand, TMEM) plus its tiles (a K-step each and the epilogue), one
-      // CTA per SM; the fewest ranges of the least estimated time
-      const double tiles = (double)ctx->ew_ubunits + 4.0 * ctx->ew_nut, setup = YG_UMMA_SETUP;
-      int nr = 1;
-      double best = 1e300;
-      for (int r = 1; r <= std::min(EW_MMA_MAXR, ctx->ew_nut); r++) {
-        const double cost = std::ceil((double)nab * r / nsm) * (setup + tiles / r);
-        if (cost < best * (1.0 - 1e-9)) {
-          best = cost;
-          nr = r;
-        }
-      }
-      double *out = ctx->d_ew_gpart;
-      const int64_t rstride = N * 3;
-      if (nr > 1) {
-        if ((rc = yg_ensure(ctx, (void **)&ctx->d_ew_fpiece, &ctx->ew_bytes_fpiece, (size_t)nr * rstride * sizeof(double))))
-          return rc;
-        out = ctx->d_ew_fpiece;
-      }
-      const void *ubg = (const unsigned *)ctx->d_ew_ub + (size_t)(ngroup == 1 ? 0 : g) * ubstride;
-      if ((rc = yg_launch_force_umma(ctx, te, ctx->d_ew_ya, (int)gb[g][0], (int)gb[g][1], G0 + G1 + 2, G0, lep, nks,
-                                     ctx->d_ew_urange + (nr - 1) * (nr + 2) / 2, nr, ubg, 1.0 / (qscale * s1),
-                                     1.0 / (qscale * s2), out, rstride)))
-        return rc;
-      if (nr > 1) {
-        k_ewald_force_mma_combine<<<yg_blocks(n * 3, 256), 256, 0, ctx->stream>>>(ctx->d_ew_fpiece, rstride, nr,
-                                                                                  (int)gb[g][0], (int)gb[g][1],
-                                                                                  ctx->d_ew_gpart);
-        YG_LAUNCH_CHECK(ctx, "k_ewald_force_mma_combine");
-      }
-    }
-    k_ewald_gpos<<<yg_blocks(N, 256), 256, 0, ctx->stream>>>(ctx->d_ew_gpart, N, ctx->cell,
-                                                             -6.2831853071795864769 / ctx->ew_diel, gpos);
-    YG_LAUNCH_CHECK(ctx, "k_ewald_gpos");
-    ctx->part_valid[YG_PART_EWALD_RECI] = 1;
-    return YG_OK;
-  }
   if (umma) {
     // tcgen05: one CTA per SM (all of TMEM), blocks of 128 atoms x tile ranges
     int dev = 0, nsm = 1;

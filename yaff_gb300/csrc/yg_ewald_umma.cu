@@ -1,5 +1,7 @@
-// yg_ewald_umma.cu -- force pass of the mixed-precision reciprocal sum on the
-// fifth-generation tensor cores (tcgen05.mma, accumulators in tensor memory).
+// yg_ewald_umma.cu -- the two contractions of the mixed-precision reciprocal
+// sum on the fifth-generation tensor cores (tcgen05.mma, accumulators in
+// tensor memory): the force pass (below) and the structure-factor pass
+// (k_sfac_umma, further down).
 //
 // The force on atom a from the reciprocal sum (yaff/pes/ewald.c:112-125,
 // written as two contractions; see yg_ewald.cu) needs, per atom a and
@@ -39,6 +41,8 @@
 // runs out records YG_ST_TIMEOUT and stops the CTA's roles, which then wait
 // (bounded) for their own copies and MMAs still in flight before TMEM is
 // freed and the CTA exits.
+#include <cuda_fp16.h>
+
 #include "yg_internal.cuh"
 
 namespace {
@@ -62,18 +66,23 @@ constexpr size_t UM_SMEM_B = (size_t)UM_KMAX * 2 * UM_BTILE;   // 64 KB per stag
 __device__ __forceinline__ unsigned um_smem(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 // shared-memory matrix descriptor: start >> 4, leading (K) byte offset 128,
-// stride (8-row) byte offset 256, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t um_desc(unsigned saddr) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+// stride (8-row) byte offset `sbo`, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t um_desc_sbo(unsigned saddr, unsigned sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
          ((uint64_t)1 << 46);
 }
+__device__ __forceinline__ uint64_t um_desc(unsigned saddr) { return um_desc_sbo(saddr, 256); }
 
-__device__ __forceinline__ void um_mma(unsigned dtmem, uint64_t adesc, uint64_t bdesc, unsigned accumulate) {
+__device__ __forceinline__ void um_mma_i(unsigned dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         unsigned accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(UM_IDESC), "r"(accumulate)
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
+}
+__device__ __forceinline__ void um_mma(unsigned dtmem, uint64_t adesc, uint64_t bdesc, unsigned accumulate) {
+  um_mma_i(dtmem, adesc, bdesc, UM_IDESC, accumulate);
 }
 
 __device__ __forceinline__ void um_commit(unsigned long long *bar) {
@@ -97,6 +106,18 @@ __device__ __forceinline__ void um_ld32(unsigned taddr, float (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void um_ld16(unsigned taddr, float (&v)[16]) {
+  unsigned r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void um_init(unsigned long long *bar, unsigned count) {
@@ -376,6 +397,342 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// S pass on tcgen05: the structure-factor partials of one chunk of atoms and
+// one tile of 64 k-columns,
+//   S[c][m] = sum_a X[a][c] Y[a][m],  X = E0[a][g0] E1[a][g1],  Y = q E2[a][m],
+// as the real product D[128][N] = A[128][K] B[K][N] over K = atoms:
+// A rows 0-63 are Re X of the tile's columns, rows 64-127 Im X; the N = 16 j
+// columns of B are j groups of 16 (Re Y of 8 m values, then Im Y of the
+// same 8), j = ceil(extent / 8) for the tile's largest m extent.  Then
+//   Re S = D[c][Re Y] - D[c + 64][Im Y],  Im S = D[c][Im Y] + D[c + 64][Re Y].
+// Operands are FP16 hi + lo splits, each product hi*hi + hi*lo + lo*hi.
+//
+// Warps 0-7 form X for a stage of 32 atoms (thread = one k-column and 8
+// atoms: both rows, hi and lo, four 16-byte stores) into one of two A
+// buffers, from the atoms' E0|E1 rows (a ring of three stages filled by
+// bulk copies); warp 8 (one lane) issues the copies and, after the stage's
+// barrier, waits for the stage's B operand (a ring of four) and issues its
+// six MMAs into one of three 64-column TMEM accumulators, from zero, then
+// commits them.  The X warps read an accumulator back two stages later (each
+// warp its TMEM lane quarter, the two warp halves alternate 16-column
+// groups) into FP32 registers with round-to-nearest, so the tensor core's
+// truncating accumulation spans six MMAs (32 atoms) and the MMAs of two
+// stages overlap the X formation.  (Twelve MMAs per accumulator, 64 atoms,
+// biased |S| low enough to move the energy of a 3,000-atom box by 3.5e-7
+// relative.)  The warp-level MMA form measured faster (183 against 218 us at
+// 50,000 atoms: both are bound by the CUDA-core X formation, which this form
+// also stores to shared memory and synchronises), so it is the automatic
+// choice and this kernel is selected with yg_ewald_sfac_path(ctx, 2).  One CTA barrier per stage; every other
+// dependency is an mbarrier: E rows landed (X warps), B landed and MMAs
+// complete (warp 8 before refilling a B stage; the X warps before reusing an
+// A buffer or reading an accumulator).  Padding columns (past the sorted
+// list) get finite X and their partials are never read.  At the end the
+// sums go through shared memory (rows padded to 65 words) to the partial
+// S[chunk][tile][c][m] (row stride sms).
+//
+// Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices, the
+// two 8-atom halves of a K-step 128 B apart, the hi part of a row group at
+// +0 and its lo part at +256, row groups 512 B apart.  A: 8 KB per K-step
+// (16 row groups); B: 1 KB per 8 m values per K-step (two row groups), the
+// Y operand of a 16-atom block stored as nks KB in that layout (k_yb_umma).
+// Waits are bounded; a wait that runs out records YG_ST_TIMEOUT, all
+// threads leave the loop together at the next barrier, and warp 8 waits
+// (bounded) for the copies and MMAs still in flight before TMEM is freed.
+
+#ifndef YG_SFAC_ATB
+#define YG_SFAC_ATB 512   // atoms per CTA (a multiple of 32)
+#endif
+#ifndef YG_SFAC_MINB
+#define YG_SFAC_MINB 2    // resident CTAs per SM the register budget is sized for
+#endif
+
+constexpr int US_XW = 8;                       // X-forming warps
+constexpr int US_THREADS = 32 * (US_XW + 1);   // + the copy/MMA warp
+constexpr int US_KS = 32;                      // atoms per stage (two K-steps)
+constexpr int US_NT = 3;                       // E-row stages
+constexpr int US_NB = 4;                       // B stages
+constexpr int US_NACC = 3;                     // TMEM accumulators of 64 columns
+constexpr int US_ABYTES = 2 * 8192;            // A operand of a stage
+constexpr int US_BBYTES = 2 * 4096;            // B operand of a stage (at most four 8-m groups)
+constexpr int US_TMEM_COLS = 256;
+constexpr int US_DSTRIDE = 65;                 // words per row of the final D staging
+
+__device__ __forceinline__ unsigned um_h2(__half2 h) { return *reinterpret_cast<unsigned *>(&h); }
+
+// (a, b) -> FP16 pairs hi = rn(a, b), lo = rn(a - hi, b - hi).
+__device__ __forceinline__ void um_split(float a, float b, unsigned &hi, unsigned &lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 f = __half22float2(h);
+  hi = um_h2(h);
+  lo = um_h2(__floats2half2_rn(a - f.x, b - f.y));
+}
+
+// Bounded wait without a stop flag (every waiting thread polls itself).
+__device__ __forceinline__ bool um_wait_all(unsigned long long *bar, unsigned parity, int *status) {
+  for (int it = 0; it < (1 << 24); it++)
+    if (um_try(bar, parity)) return true;
+  if (status) atomicOr(status + YG_ST_TIMEOUT, 1);
+  return false;
+}
+
+// B operand of the S pass: per 16-atom block (positions relative to the atom
+// groups as in the warp-MMA form: [lo, hi), [0, lo), [hi, N), each padded to
+// whole blocks; padding atoms read zero) nks KB; one thread per 16-byte unit
+// (block, row group gi = 2 (m / 8) + (0 re, 1 im), hi/lo, 8-atom half, row
+// m % 8) packs the FP16 values of 8 atoms.
+__global__ void k_yb_umma(const uint2 *__restrict__ yf, int64_t lo, int64_t hi, int64_t natom, int64_t base1,
+                          int64_t base2, int64_t nblocks, int nmf, int nks, uint4 *__restrict__ yb) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t per = (int64_t)nks * 64;
+  if (u >= nblocks * per) return;
+  const int r = (int)(u & 7), kh = (int)((u >> 3) & 1), hl = (int)((u >> 4) & 1);
+  const int gi = (int)((u % per) >> 5);
+  const int64_t blk = u / per;
+  const int m = 8 * (gi >> 1) + r, comp = gi & 1;
+  const int64_t p0 = blk * 16;
+  int64_t a0, n, gbase;
+  if (p0 < base1) {
+    a0 = lo; n = hi - lo; gbase = 0;
+  } else if (p0 < base2) {
+    a0 = 0; n = lo; gbase = base1;
+  } else {
+    a0 = hi; n = natom - hi; gbase = base2;
+  }
+  unsigned w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int64_t rr = p0 + 8 * kh + k - gbase;
+    unsigned h16 = 0u;
+    if (rr >= 0 && rr < n && m < nmf) {
+      const uint2 v = yf[(a0 + rr) * nmf + m];
+      const unsigned half2 = hl ? v.y : v.x;
+      h16 = comp ? (half2 >> 16) : (half2 & 0xffffu);
+    }
+    w[k >> 1] |= h16 << (16 * (k & 1));
+  }
+  yb[blk * per + gi * 32 + hl * 16 + kh * 8 + r] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void __launch_bounds__(US_THREADS, YG_SFAC_MINB)
+    k_sfac_umma(const float2 *__restrict__ te, const uint4 *__restrict__ yb, int n, int G0, int lep, int nks,
+                const int4 *__restrict__ cols, float2 *__restrict__ Spart, int ntile64, int sms,
+                int *__restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem_us[];
+  __shared__ __align__(8) unsigned long long bar_te[US_NT], bar_b[US_NB], bar_mma[2];
+  __shared__ unsigned tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool ctl = warp == US_XW;
+  const int tile = blockIdx.y;
+  const int extent = cols[tile * 64].w + 1;  // columns sorted by decreasing extent
+  const int j = extent > 0 ? (extent + 7) >> 3 : 0;
+  const int abeg = blockIdx.x * YG_SFAC_ATB, aend = min(n, abeg + YG_SFAC_ATB);
+  if (j == 0 || aend <= abeg) return;  // whole CTA, before any barrier or TMEM
+  const unsigned te_bytes = (unsigned)(US_KS * lep * sizeof(float2));
+  unsigned char *sA = smem_us;                          // 2 x US_ABYTES
+  unsigned char *sT = smem_us + 2 * US_ABYTES;          // US_NT x te_bytes
+  unsigned char *sB = sT + (size_t)US_NT * te_bytes;    // US_NB x US_BBYTES
+  const uint32_t idesc = (1u << 4) | ((uint32_t)(2 * j) << 17) | ((uint32_t)(128 >> 4) << 24);
+  const int nst = (aend - abeg + US_KS - 1) / US_KS;
+  // this X thread's k-column and 8-atom slice of a stage
+  const int c = tid & 63, hk = (tid >> 6) & 3, ks_t = hk >> 1, kh_t = hk & 1;
+  int o0 = 0, o1 = 0;
+  float s0 = 1.f, s1 = 1.f;
+  if (!ctl) {
+    const int4 col = cols[tile * 64 + c];
+    o0 = col.x < 0 ? -col.x : col.x;
+    o1 = G0 + 1 + (col.y < 0 ? -col.y : col.y);
+    s0 = col.x < 0 ? -1.f : 1.f;
+    s1 = col.y < 0 ? -1.f : 1.f;
+  }
+  if (tid == 0) {
+    for (int i = 0; i < US_NT; i++) um_init(&bar_te[i], 1);
+    for (int i = 0; i < US_NB; i++) um_init(&bar_b[i], 1);
+    um_init(&bar_mma[0], 1);
+    um_init(&bar_mma[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (ctl) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(um_smem(&tmem_slot)),
+                 "r"(US_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  um_fence_before();
+  __syncthreads();
+  um_fence_after();
+  const unsigned tmem = tmem_slot;
+  // copies (warp 8, lane 0): E rows of atoms abeg + 32 s .. + 31 (te holds
+  // zero rows past the last atom), B operand of the stage's two 16-atom blocks
+  auto issue_te = [&](int s) {
+    const int b = s % US_NT;
+    um_expect(&bar_te[b], te_bytes);
+    um_copy(sT + (size_t)b * te_bytes, te + (size_t)(abeg + s * US_KS) * lep, te_bytes, &bar_te[b]);
+  };
+  auto issue_b = [&](int s) {
+    const int b = s % US_NB;
+    unsigned char *dst = sB + (size_t)b * US_BBYTES;
+    const uint4 *src = yb + (size_t)((abeg + s * US_KS) / 16) * nks * 64;
+    um_expect(&bar_b[b], 2048u * (unsigned)j);
+    um_copy(dst, src, 1024u * (unsigned)j, &bar_b[b]);
+    um_copy(dst + 4096, src + (size_t)nks * 64, 1024u * (unsigned)j, &bar_b[b]);
+  };
+  const bool leader = ctl && lane == 0;
+  int te_issued = 0, b_issued = 0, b_waited = 0, committed = 0;  // (leader's bookkeeping)
+  if (leader) {
+    for (; te_issued < min(nst, US_NT); te_issued++) issue_te(te_issued);
+    for (; b_issued < min(nst, US_NB); b_issued++) issue_b(b_issued);
+  }
+  float acc[2][16];
+#pragma unroll
+  for (int t = 0; t < 2; t++)
+#pragma unroll
+    for (int e = 0; e < 16; e++) acc[t][e] = 0.f;
+  const int q = warp & 3, hh = (warp >> 2) & 1;
+  const unsigned tl = tmem + ((unsigned)(32 * q) << 16);
+  auto readback = [&](int slot) {
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const int i = hh + 2 * t;
+      if (i < j) {
+        float v[16];
+        um_ld16(tl + (unsigned)(slot * 64 + 16 * i), v);
+#pragma unroll
+        for (int e = 0; e < 16; e++) acc[t][e] += v[e];
+      }
+    }
+  };
+  bool fail = false;
+  int s = 0;
+  for (; s < nst; s++) {
+    if (!ctl) {
+      if (!um_wait_all(&bar_te[s % US_NT], (unsigned)((s / US_NT) & 1), status)) fail = true;
+      if (!fail && s >= 2) {
+        // the MMAs of stage s - 2 are complete: A buffer s & 1 is free and
+        // accumulator (s - 2) % 3 holds that stage's sums
+        if (!um_wait_all(&bar_mma[s & 1], (unsigned)(((s - 2) >> 1) & 1), status)) {
+          fail = true;
+        } else {
+          um_fence_after();
+          readback((s - 2) % US_NACC);
+          um_fence_before();
+        }
+      }
+      const int nrow = min(US_KS, aend - (abeg + s * US_KS));
+      if (!fail && 16 * ks_t < nrow) {
+        const float2 *row =
+            reinterpret_cast<const float2 *>(sT + (size_t)(s % US_NT) * te_bytes) + (size_t)(16 * ks_t + 8 * kh_t) * lep;
+        unsigned xrh[4], xrl[4], xih[4], xil[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          float xr[2], xi[2];
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            const float2 *ra = row + (size_t)(2 * i + u) * lep;
+            const float2 e0 = ra[o0], e1 = ra[o1];
+            const float e0y = e0.y * s0, e1y = e1.y * s1;
+            xr[u] = e0.x * e1.x - e0y * e1y;
+            xi[u] = e0.x * e1y + e0y * e1.x;
+          }
+          um_split(xr[0], xr[1], xrh[i], xrl[i]);
+          um_split(xi[0], xi[1], xih[i], xil[i]);
+        }
+        unsigned char *A = sA + (size_t)(s & 1) * US_ABYTES + ks_t * 8192 + kh_t * 128 + (c & 7) * 16 + (c >> 3) * 512;
+        *reinterpret_cast<uint4 *>(A) = make_uint4(xrh[0], xrh[1], xrh[2], xrh[3]);
+        *reinterpret_cast<uint4 *>(A + 256) = make_uint4(xrl[0], xrl[1], xrl[2], xrl[3]);
+        *reinterpret_cast<uint4 *>(A + 4096) = make_uint4(xih[0], xih[1], xih[2], xih[3]);
+        *reinterpret_cast<uint4 *>(A + 4096 + 256) = make_uint4(xil[0], xil[1], xil[2], xil[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    um_fence_before();
+    if (__syncthreads_or(fail)) break;
+    um_fence_after();
+    if (leader) {
+      // E-row stage s % 3 is consumed: refill it
+      if (te_issued < nst) issue_te(te_issued++);
+      // the MMAs of stage s - 2 are complete: refill its B stage
+      if (s >= 2 && b_issued < nst) {
+        if (!um_wait_all(&bar_mma[s & 1], (unsigned)(((s - 2) >> 1) & 1), status)) fail = true;
+        else issue_b(b_issued++);
+      }
+      if (!fail && !um_wait_all(&bar_b[s % US_NB], (unsigned)((s / US_NB) & 1), status)) fail = true;
+      if (!fail) {
+        b_waited = s + 1;
+        um_fence_after();
+        const int nkv = min(US_KS, aend - (abeg + s * US_KS)) > 16 ? 2 : 1;
+        const unsigned aB = um_smem(sA + (size_t)(s & 1) * US_ABYTES);
+        const unsigned bB = um_smem(sB + (size_t)(s % US_NB) * US_BBYTES);
+        const unsigned d = tmem + (unsigned)((s % US_NACC) * 64);
+        for (int ks = 0; ks < nkv; ks++) {
+          const uint64_t ah = um_desc_sbo(aB + ks * 8192, 512), al = um_desc_sbo(aB + ks * 8192 + 256, 512);
+          const uint64_t bh = um_desc_sbo(bB + ks * 4096, 512), bl = um_desc_sbo(bB + ks * 4096 + 256, 512);
+          um_mma_i(d, ah, bh, idesc, ks > 0 ? 1u : 0u);
+          um_mma_i(d, ah, bl, idesc, 1u);
+          um_mma_i(d, al, bh, idesc, 1u);
+        }
+        um_commit(&bar_mma[s & 1]);
+        committed = s + 1;
+      }
+    }
+  }
+  if (!fail && !ctl) {
+    // the last two stages' sums
+    for (int t = max(0, nst - 2); t < nst && !fail; t++) {
+      if (!um_wait_all(&bar_mma[t & 1], (unsigned)((t >> 1) & 1), status)) {
+        fail = true;
+      } else {
+        um_fence_after();
+        readback(t % US_NACC);
+        um_fence_before();
+      }
+    }
+  }
+  fail = __syncthreads_or(fail);
+  if (fail) {
+    // copies and MMAs still in flight land before the buffers and TMEM go:
+    // E-row stages from the one the loop stopped at, B stages the leader had
+    // not waited for, the MMAs up to the last commit (one outstanding phase
+    // per barrier, so each parity is unambiguous)
+    if (leader) {
+      for (int t = min(s, te_issued); t < te_issued; t++)
+        um_drain(&bar_te[t % US_NT], (unsigned)((t / US_NT) & 1), status);
+      for (int t = b_waited; t < b_issued; t++) um_drain(&bar_b[t % US_NB], (unsigned)((t / US_NB) & 1), status);
+      if (committed > 0) um_drain(&bar_mma[(committed - 1) & 1], (unsigned)(((committed - 1) >> 1) & 1), status);
+    }
+  } else {
+    // D rows through shared memory (A and E-row buffers are idle: every copy
+    // was consumed and every MMA has completed)
+    float *Dsm = reinterpret_cast<float *>(smem_us);
+    if (!ctl) {
+      const int L = 32 * q + lane;
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        const int i = hh + 2 * t;
+        if (i < j) {
+#pragma unroll
+          for (int e = 0; e < 16; e++) Dsm[L * US_DSTRIDE + 16 * i + e] = acc[t][e];
+        }
+      }
+    }
+    __syncthreads();
+    const int nmv = 8 * j;
+    float2 *dst = Spart + ((int64_t)blockIdx.x * ntile64 + tile) * 64 * sms;
+    for (int idx = tid; idx < 64 * nmv; idx += US_THREADS) {
+      const int cc = idx / nmv, m = idx - cc * nmv;
+      const int cre = 16 * (m >> 3) + (m & 7), cim = cre + 8;
+      const float *dr = Dsm + cc * US_DSTRIDE, *di = Dsm + (cc + 64) * US_DSTRIDE;
+      dst[(int64_t)cc * sms + m] = make_float2(dr[cre] - di[cim], dr[cim] + di[cre]);
+    }
+  }
+  um_fence_before();
+  __syncthreads();
+  if (ctl) {
+    um_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(US_TMEM_COLS) : "memory");
+  }
+}
+
 }  // namespace
 
 // Dynamic shared memory of the tcgen05 force pass for ne E0|E1 entries per
@@ -387,6 +744,47 @@ size_t yg_umma_force_smem(int ne) {
 
 int yg_umma_kmax() { return UM_KMAX; }
 int yg_umma_cols() { return UM_COLS; }
+
+// Dynamic shared memory of the tcgen05 S pass for E0|E1 rows of lep float2
+// (lep even); 0 when two CTAs do not fit on a multiprocessor (228 KB, less
+// 1 KB reserved and 1 KB of static shared memory per CTA).
+size_t yg_umma_sfac_smem(int lep) {
+  const size_t need = 2 * (size_t)US_ABYTES + (size_t)US_NT * US_KS * lep * sizeof(float2) + (size_t)US_NB * US_BBYTES;
+  return (lep % 2 == 0 && need <= 112 * 1024) ? need : 0;
+}
+int yg_umma_sfac_atb() { return YG_SFAC_ATB; }
+
+// B operand of the tcgen05 S pass (nblocks 16-atom blocks, nks KB each).
+int yg_launch_yb_umma(yg_ctx *ctx, const void *yf, int64_t lo, int64_t hi, int64_t base1, int64_t base2,
+                      int64_t nblocks, int nmf, int nks, void *yb) {
+  const int64_t threads = nblocks * nks * 64;
+  if (threads <= 0) return YG_OK;
+  k_yb_umma<<<yg_blocks(threads, 256), 256, 0, ctx->stream>>>((const uint2 *)yf, lo, hi, ctx->natom, base1, base2,
+                                                              nblocks, nmf, nks, (uint4 *)yb);
+  YG_LAUNCH_CHECK(ctx, "k_yb_umma");
+  return YG_OK;
+}
+
+// Structure-factor partials of the n atoms of one group (te, yb start at the
+// group) over ntile64 column tiles: Spart[chunk][tile][c][m], row stride sms.
+int yg_launch_sfac_umma(yg_ctx *ctx, const void *te, const void *yb, int n, int G0, int lep, int nks,
+                        const void *cols, void *Spart, int ntile64, int sms) {
+  const size_t smem = yg_umma_sfac_smem(lep);
+  if (smem == 0 || nks > UM_KMAX) {
+    yg_set_error("tcgen05 Ewald S pass: k-space too large for its shared-memory layout");
+    return YG_ERR_UNSUPPORTED;
+  }
+  int rc;
+  if ((rc = yg_smem_optin((const void *)k_sfac_umma, smem))) return rc;
+  const int nch = (n + YG_SFAC_ATB - 1) / YG_SFAC_ATB;
+  if (nch <= 0) return YG_OK;
+  dim3 grid(nch, ntile64);
+  k_sfac_umma<<<grid, US_THREADS, smem, ctx->stream>>>((const float2 *)te, (const uint4 *)yb, n, G0, lep, nks,
+                                                       (const int4 *)cols, (float2 *)Spart, ntile64, sms,
+                                                       ctx->d_status);
+  YG_LAUNCH_CHECK(ctx, "k_sfac_umma");
+  return YG_OK;
+}
 
 // A operand of the atoms [a0, a0 + n) in 128-atom blocks (nblk of them).
 int yg_launch_ya_umma(yg_ctx *ctx, const void *yf, int64_t a0, int64_t n, int nmf, int nks, int64_t nblk, void *ya) {

@@ -218,12 +218,13 @@ struct yg_ctx {
   yg_occ ew_occ_fm;               // resident tensor-core force-pass blocks
   void *d_ew_te = nullptr;        // E0|E1 rows (float2), atoms padded to a multiple of 32
   void *d_ew_yf = nullptr;        // q E2 as FP16 (hi, lo) pairs per (atom, m)
-  void *d_ew_ys = nullptr;        // q E2 as FP16 B fragments per 16 atoms
+  void *d_ew_ys = nullptr;        // q E2 per 16 atoms: FP16 B fragments, or the tcgen05 S-pass B operand
   void *d_ew_wb = nullptr;        // force weights as FP16 B fragments, per group
   size_t ew_bytes_te = 0, ew_bytes_yf = 0, ew_bytes_ys = 0, ew_bytes_wb = 0;
   // tcgen05 form of the force pass (yg_ewald_umma.cu): 64-column tiles
   int ew_umma = 0;                // 1 when the k-space layout suits it
   int ew_force_path = 0;          // requested: 0 automatic, 1 warp-level MMA
+  int ew_sfac_path = 0;           // S pass requested: 0 automatic (warp-level MMA), 1 warp-level MMA, 2 tcgen05
   int ew_nut = 0;                 // 64-column tiles with work
   int ew_ubunits = 0;             // 16 KB B-operand units (tile x K-step) of one group's weights
   int *d_ew_uoff = nullptr;       // first unit of every 64-column tile (nut + 1)
@@ -411,6 +412,13 @@ int yg_launch_ya_umma(yg_ctx *ctx, const void *yf, int64_t a0, int64_t n, int nm
 int yg_launch_force_umma(yg_ctx *ctx, const void *te, const void *ya, int a0, int a1, int ne, int G0, int lep,
                          int nks, const int *urange, int nr, const void *ub, double inv1, double inv2, double *out,
                          int64_t rstride);
+// tcgen05 S pass (yg_ewald_umma.cu)
+size_t yg_umma_sfac_smem(int lep);
+int yg_umma_sfac_atb();
+int yg_launch_yb_umma(yg_ctx *ctx, const void *yf, int64_t lo, int64_t hi, int64_t base1, int64_t base2,
+                      int64_t nblocks, int nmf, int nks, void *yb);
+int yg_launch_sfac_umma(yg_ctx *ctx, const void *te, const void *yb, int n, int G0, int lep, int nks,
+                        const void *cols, void *Spart, int ntile64, int sms);
 
 // Grid-stride helper.
 static inline int yg_blocks(int64_t n, int threads) {
