@@ -260,7 +260,47 @@ struct BuildArgs {
   int filter;       // nlow/nhigh restrict the pairs
   const int *gate;  // device flag: build only when set (nullptr: always)
   const int4 *rows; // pruned stencil rows (o1, o2, lo, hi)
+  float pm[9], pw[3], pg[9], pkeep;  // per-atom row trimming (see atom_cell_lb)
 };
+
+// Lower bound on the distance from an atom at (phi0, phi1, phi2) of its home
+// cell (cell widths along each axis, from the cell's corner) to the cell at
+// offset (o0, o1, o2): the larger of the slab bounds along the three plane
+// normals (w_k times the gap along axis k) and the bound along the direction
+// u to the target cell's centre p, |d| >= u.d >= |p| - sum_k |u.M_k| / 2 for
+// every point d of that cell (M_k = its edge vectors).
+__device__ __forceinline__ float atom_cell_lb(const BuildArgs &A, float phi0, float phi1, float phi2, int o0, int o1,
+                                              int o2) {
+  const float a0 = (float)o0 - phi0, a1 = (float)o1 - phi1, a2 = (float)o2 - phi2;
+  float lb = fmaxf(A.pw[0] * fmaxf(0.f, fmaxf(a0, -a0 - 1.f)), A.pw[1] * fmaxf(0.f, fmaxf(a1, -a1 - 1.f)));
+  lb = fmaxf(lb, A.pw[2] * fmaxf(0.f, fmaxf(a2, -a2 - 1.f)));
+  const float c0 = a0 + 0.5f, c1 = a1 + 0.5f, c2 = a2 + 0.5f;
+  const float px = c0 * A.pm[0] + c1 * A.pm[3] + c2 * A.pm[6];
+  const float py = c0 * A.pm[1] + c1 * A.pm[4] + c2 * A.pm[7];
+  const float pz = c0 * A.pm[2] + c1 * A.pm[5] + c2 * A.pm[8];
+  const float pp = px * px + py * py + pz * pz;
+  if (pp > 0.f) {
+    const float inv = rsqrtf(pp);
+    const float ext = fabsf(px * A.pm[0] + py * A.pm[1] + pz * A.pm[2]) + fabsf(px * A.pm[3] + py * A.pm[4] + pz * A.pm[5]) +
+                      fabsf(px * A.pm[6] + py * A.pm[7] + pz * A.pm[8]);
+    lb = fmaxf(lb, pp * inv - 0.5f * inv * ext);
+  }
+  return lb;
+}
+
+// The x-offset interval of stencil row (o1, o2, lo, hi) that can hold
+// candidates of an atom at phi: trimmed from both ends while the cell at the
+// end is provably beyond the list's reach (cells inside are kept, so the
+// interval keeps every cell that holds a neighbour).  Empty when lo > hi.
+__device__ __forceinline__ int2 trim_row(const BuildArgs &A, int4 row, float phi0, float phi1, float phi2) {
+  int lo = row.z, hi = row.w;
+  const float a1 = (float)row.x - phi1, a2 = (float)row.y - phi2;
+  if (A.pw[1] * fmaxf(0.f, fmaxf(a1, -a1 - 1.f)) >= A.pkeep || A.pw[2] * fmaxf(0.f, fmaxf(a2, -a2 - 1.f)) >= A.pkeep)
+    return make_int2(1, 0);
+  while (lo <= hi && atom_cell_lb(A, phi0, phi1, phi2, lo, row.x, row.y) >= A.pkeep) lo++;
+  while (hi >= lo && atom_cell_lb(A, phi0, phi1, phi2, hi, row.x, row.y) >= A.pkeep) hi--;
+  return make_int2(lo, hi);
+}
 
 // Exact replay of the reference's decision for candidate (oi -> oj) whose
 // image relative to the raw position difference is t (pos_j - pos_i + t.R).
@@ -332,6 +372,10 @@ __device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
 // short runs of the fine grid do not leave lanes idle.
 // Dynamic shared memory of k_build per warp: runs, run offsets, candidate map.
 #define YG_BUILD_WARP_SMEM (YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4 + YG_BUILD_MAP)
+// the map area doubles as the trimmed-row buffer of a batch (64 int2) and
+// every warp's area stays 8-byte aligned
+static_assert(YG_BUILD_MAP >= 64 * 8 && YG_BUILD_MAP % 8 == 0 && YG_BUILD_RUNS % 2 == 0,
+              "build buffers: map of at least 512 bytes, 8-byte multiples");
 
 #ifndef YG_BUILD_MINB
 #define YG_BUILD_MINB 4  // resident blocks per SM of the candidate sweep
@@ -349,6 +393,10 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
   const int oi = A.sorted[i];
   const float4 xi = A.x32[i];
   const int cid = A.cell_of[oi];
+  // the atom's place in its cell (xi is relative to the cell's corner)
+  const float phi0 = A.pg[0] * xi.x + A.pg[1] * xi.y + A.pg[2] * xi.z;
+  const float phi1 = A.pg[3] * xi.x + A.pg[4] * xi.y + A.pg[5] * xi.z;
+  const float phi2 = A.pg[6] * xi.x + A.pg[7] * xi.y + A.pg[8] * xi.z;
   const int N0 = A.grid.n[0], N1 = A.grid.n[1], N2 = A.grid.n[2];
   const int ci[3] = {cid % N0, (cid / N0) % N1, cid / (N0 * N1)};
   const int wi[3] = {A.wimg[3 * oi], A.wimg[3 * oi + 1], A.wimg[3 * oi + 2]};
@@ -361,14 +409,18 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
   const int oidx_home = K0 + w0 * (K1 + w1 * K2);
   for (int rb = 0; rb < A.grid.nrow; rb += A.grid.rows_per_batch) {
     const int re = min(A.grid.nrow, rb + A.grid.rows_per_batch);
-    // runs per lane: count, warp scan, then write
+    // runs per lane: count, warp scan, then write; each row trimmed to the
+    // atom's reach, the trimmed interval kept in the (still idle) map area
+    // for the writing pass (a batch holds at most 64 rows)
+    int2 *trim = reinterpret_cast<int2 *>(map);
     int mine = 0;
     for (int r = rb + lane; r < re; r += 32) {
-      const int4 row = A.rows[r];
-      for (int ox = row.z; ox <= row.w;) {
+      const int2 t = trim_row(A, A.rows[r], phi0, phi1, phi2);
+      trim[r - rb] = t;
+      for (int ox = t.x; ox <= t.y;) {
         const int u0 = ci[0] + ox;
         const int c0 = u0 - floordiv(u0, N0) * N0;
-        ox += min(row.w - ox + 1, N0 - c0);
+        ox += min(t.y - ox + 1, N0 - c0);
         mine++;
       }
     }
@@ -381,7 +433,9 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
     const int nrun = __shfl_sync(0xffffffffu, incl, 31);
     int slot = incl - mine;
     for (int r = rb + lane; r < re; r += 32) {
-      const int4 row = A.rows[r];
+      const int2 t = trim[r - rb];
+      if (t.x > t.y) continue;
+      const int4 row = make_int4(A.rows[r].x, A.rows[r].y, t.x, t.y);
       const int o1 = row.x, o2 = row.y;
       const int u1 = ci[1] + o1, u2 = ci[2] + o2;
       const int n1 = floordiv(u1, N1), n2 = floordiv(u2, N2);
@@ -742,6 +796,12 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
   A.filter = (ctx->nlow > 0 || ctx->nhigh < ctx->natom) ? 1 : 0;
   A.gate = nullptr;
   A.rows = ctx->d_rows;
+  for (int k = 0; k < 9; k++) {
+    A.pm[k] = ctx->prune_pm[k];
+    A.pg[k] = ctx->prune_pg[k];
+  }
+  for (int k = 0; k < 3; k++) A.pw[k] = ctx->prune_pw[k];
+  A.pkeep = ctx->prune_keep;
   return A;
 }
 
@@ -916,7 +976,7 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
   G.nrow = (int)rows.size();
   {
     const int maxruns = (2 * G.k[0] + 1 + G.n[0] - 1) / G.n[0] + 1;  // x wraps split a row
-    G.rows_per_batch = std::max(1, YG_BUILD_RUNS / maxruns);
+    G.rows_per_batch = std::min(64, std::max(1, YG_BUILD_RUNS / maxruns));  // two rows per lane at most
     if (maxruns > YG_BUILD_RUNS) {
       yg_set_error("neighbour stencil row too long for the build kernel");
       return YG_ERR_UNSUPPORTED;
@@ -965,6 +1025,18 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
   // make the band closed under FP32 rounding of the thresholds themselves
   ctx->band_lo = nextafterf(nextafterf(lo, 0.0f), 0.0f);
   ctx->band_hi = nextafterf(nextafterf(hi, INFINITY), INFINITY);
+  // per-atom row trimming: a cell whose lower-bound distance from the atom
+  // reaches prune_keep (above the guard band by 1e-5 relative + 1e-3 bohr,
+  // far beyond the FP32 rounding of the bound) holds no candidate that could
+  // enter the list
+  for (int k = 0; k < 3; k++) {
+    ctx->prune_pw[k] = (float)(rsp[k] / G.n[k]);
+    for (int x = 0; x < 3; x++) {
+      ctx->prune_pm[3 * k + x] = (float)(C.rv[3 * k + x] / G.n[k]);
+      ctx->prune_pg[3 * k + x] = (float)(C.gv[3 * k + x] * G.n[k]);
+    }
+  }
+  ctx->prune_keep = (float)(std::sqrt((double)ctx->band_hi) * (1.0 + 1e-5) + 1e-3);
 
   // neighbour slots
   if (ctx->nbr_cap == 0) {
