@@ -143,10 +143,11 @@ struct yg_ctx {
   double geom_rc = 0.0;
   float band_lo = 0.0f, band_hi = 0.0f;  // FP32 guard band on d^2
   // per-atom trimming of the stencil rows in the candidate sweep: cell edge
-  // vectors rv_k / n_k, slab widths along the plane normals, n_k g_k (cell
-  // widths per unit of cell-local position), and the distance beyond which a
-  // cell holds no candidate of the list (above the guard band)
-  float prune_pm[9] = {0}, prune_pw[3] = {0}, prune_pg[9] = {0}, prune_keep = 0.0f;
+  // vectors M_k = rv_k / n_k, slab widths along the plane normals, n_k g_k
+  // (cell widths per unit of cell-local position), M_0 . M_k, and the
+  // distance beyond which a cell holds no candidate of the list (above the
+  // guard band)
+  float prune_pm[9] = {0}, prune_pw[3] = {0}, prune_pg[9] = {0}, prune_g0[3] = {0}, prune_keep = 0.0f;
   double rcut_total = 0.0;
   int64_t rmax[3] = {0, 0, 0};
   int64_t nlow = 0, nhigh = 0;

@@ -260,45 +260,42 @@ struct BuildArgs {
   int filter;       // nlow/nhigh restrict the pairs
   const int *gate;  // device flag: build only when set (nullptr: always)
   const int4 *rows; // pruned stencil rows (o1, o2, lo, hi)
-  float pm[9], pw[3], pg[9], pkeep;  // per-atom row trimming (see atom_cell_lb)
+  float pm[9], pw[3], pg[9], pg0[3], pkeep;  // per-atom row trimming (see trim_row)
 };
 
-// Lower bound on the distance from an atom at (phi0, phi1, phi2) of its home
-// cell (cell widths along each axis, from the cell's corner) to the cell at
-// offset (o0, o1, o2): the larger of the slab bounds along the three plane
-// normals (w_k times the gap along axis k) and the bound along the direction
-// u to the target cell's centre p, |d| >= u.d >= |p| - sum_k |u.M_k| / 2 for
-// every point d of that cell (M_k = its edge vectors).
-__device__ __forceinline__ float atom_cell_lb(const BuildArgs &A, float phi0, float phi1, float phi2, int o0, int o1,
-                                              int o2) {
-  const float a0 = (float)o0 - phi0, a1 = (float)o1 - phi1, a2 = (float)o2 - phi2;
-  float lb = fmaxf(A.pw[0] * fmaxf(0.f, fmaxf(a0, -a0 - 1.f)), A.pw[1] * fmaxf(0.f, fmaxf(a1, -a1 - 1.f)));
-  lb = fmaxf(lb, A.pw[2] * fmaxf(0.f, fmaxf(a2, -a2 - 1.f)));
-  const float c0 = a0 + 0.5f, c1 = a1 + 0.5f, c2 = a2 + 0.5f;
-  const float px = c0 * A.pm[0] + c1 * A.pm[3] + c2 * A.pm[6];
-  const float py = c0 * A.pm[1] + c1 * A.pm[4] + c2 * A.pm[7];
-  const float pz = c0 * A.pm[2] + c1 * A.pm[5] + c2 * A.pm[8];
-  const float pp = px * px + py * py + pz * pz;
-  if (pp > 0.f) {
-    const float inv = rsqrtf(pp);
-    const float ext = fabsf(px * A.pm[0] + py * A.pm[1] + pz * A.pm[2]) + fabsf(px * A.pm[3] + py * A.pm[4] + pz * A.pm[5]) +
-                      fabsf(px * A.pm[6] + py * A.pm[7] + pz * A.pm[8]);
-    lb = fmaxf(lb, pp * inv - 0.5f * inv * ext);
-  }
-  return lb;
-}
-
 // The x-offset interval of stencil row (o1, o2, lo, hi) that can hold
-// candidates of an atom at phi: trimmed from both ends while the cell at the
-// end is provably beyond the list's reach (cells inside are kept, so the
-// interval keeps every cell that holds a neighbour).  Empty when lo > hi.
+// candidates of an atom at (phi0, phi1, phi2) of its home cell (cell widths
+// along each axis, from the cell's corner): trimmed from both ends while the
+// cell at the end is provably beyond the list's reach.  The bound for the
+// cell at offset o: along the direction u to its centre p = sum_k c_k M_k
+// (c_k = o_k - phi_k + 1/2, M_k its edge vectors), every point d of the cell
+// has |d| >= u.d >= |p| - sum_k |u.M_k| / 2.  Along a row only c_0 changes,
+// so q = c_1 M_1 + c_2 M_2 and its products are formed once per row and a
+// cell costs |p|^2 = c_0^2 M_0.M_0 + 2 c_0 M_0.q + q.q and
+// p.M_k = c_0 M_0.M_k + q.M_k.  A row whose slab bound along axis 1 or 2
+// (w_k times the gap to the row) already reaches the limit is empty.  Cells
+// inside the interval are kept, so every cell holding a neighbour stays.
 __device__ __forceinline__ int2 trim_row(const BuildArgs &A, int4 row, float phi0, float phi1, float phi2) {
-  int lo = row.z, hi = row.w;
   const float a1 = (float)row.x - phi1, a2 = (float)row.y - phi2;
   if (A.pw[1] * fmaxf(0.f, fmaxf(a1, -a1 - 1.f)) >= A.pkeep || A.pw[2] * fmaxf(0.f, fmaxf(a2, -a2 - 1.f)) >= A.pkeep)
     return make_int2(1, 0);
-  while (lo <= hi && atom_cell_lb(A, phi0, phi1, phi2, lo, row.x, row.y) >= A.pkeep) lo++;
-  while (hi >= lo && atom_cell_lb(A, phi0, phi1, phi2, hi, row.x, row.y) >= A.pkeep) hi--;
+  const float c1 = a1 + 0.5f, c2 = a2 + 0.5f;
+  const float qx = c1 * A.pm[3] + c2 * A.pm[6], qy = c1 * A.pm[4] + c2 * A.pm[7], qz = c1 * A.pm[5] + c2 * A.pm[8];
+  const float qq = qx * qx + qy * qy + qz * qz;
+  const float qm0 = qx * A.pm[0] + qy * A.pm[1] + qz * A.pm[2];
+  const float qm1 = qx * A.pm[3] + qy * A.pm[4] + qz * A.pm[5];
+  const float qm2 = qx * A.pm[6] + qy * A.pm[7] + qz * A.pm[8];
+  auto beyond = [&](int o0) {
+    const float c0 = (float)o0 - phi0 + 0.5f;
+    const float pp = fmaf(c0, fmaf(c0, A.pg0[0], 2.0f * qm0), qq);
+    const float ext = fabsf(fmaf(c0, A.pg0[0], qm0)) + fabsf(fmaf(c0, A.pg0[1], qm1)) + fabsf(fmaf(c0, A.pg0[2], qm2));
+    if (!(pp > 0.f)) return false;
+    const float inv = rsqrtf(pp);
+    return pp * inv - 0.5f * inv * ext >= A.pkeep;
+  };
+  int lo = row.z, hi = row.w;
+  while (lo <= hi && beyond(lo)) lo++;
+  while (hi >= lo && beyond(hi)) hi--;
   return make_int2(lo, hi);
 }
 
@@ -800,7 +797,10 @@ BuildArgs make_args(yg_ctx *ctx, double rc2) {
     A.pm[k] = ctx->prune_pm[k];
     A.pg[k] = ctx->prune_pg[k];
   }
-  for (int k = 0; k < 3; k++) A.pw[k] = ctx->prune_pw[k];
+  for (int k = 0; k < 3; k++) {
+    A.pw[k] = ctx->prune_pw[k];
+    A.pg0[k] = ctx->prune_g0[k];
+  }
   A.pkeep = ctx->prune_keep;
   return A;
 }
@@ -1036,6 +1036,9 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
       ctx->prune_pg[3 * k + x] = (float)(C.gv[3 * k + x] * G.n[k]);
     }
   }
+  for (int k = 0; k < 3; k++)
+    ctx->prune_g0[k] = (float)((C.rv[0] * C.rv[3 * k] + C.rv[1] * C.rv[3 * k + 1] + C.rv[2] * C.rv[3 * k + 2]) /
+                               ((double)G.n[0] * G.n[k]));  // M_0 . M_k
   ctx->prune_keep = (float)(std::sqrt((double)ctx->band_hi) * (1.0 + 1e-5) + 1e-3);
 
   // neighbour slots
