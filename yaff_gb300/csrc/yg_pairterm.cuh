@@ -208,7 +208,7 @@ __device__ __forceinline__ void pair_term(const PairPotDev &P, T rcT, T parT, T 
 // 1.2e-7 everywhere), which keeps the relative accuracy of the tail where the
 // real-space Ewald term is evaluated.
 static __device__ __forceinline__ float erfc_cheb(float x) {
-  const float t = 1.0f / (1.0f + 0.5f * x);
+  const float t = __frcp_rn(1.0f + 0.5f * x);  // = 1.0f / (1 + x / 2) (both correctly rounded)
   float p = 0.17087277f;
   p = fmaf(p, t, -0.82215223f);
   p = fmaf(p, t, 1.48851587f);
@@ -243,7 +243,7 @@ static __device__ __forceinline__ void pair_term_f32(const PairPotDev &P, float 
     if (P.kind == YG_POT_MM3) {
       const float sig = pi0 + pj0;
       const float eps = pi1 * pj1;
-      const float inv_sig = 1.0f / sig;
+      const float inv_sig = __frcp_rn(sig);  // = 1.0f / sig (both correctly rounded)
       const float ex = 1.84e5f * expf(-12.0f * d * inv_sig);
       if (pi3 + pj3 == 0.0f) {
         const float s2 = sig * sig * inv_d2;
