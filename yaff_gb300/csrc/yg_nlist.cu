@@ -213,6 +213,16 @@ __global__ void k_prep(const double *__restrict__ pos, const double *__restrict_
   xb[s] = make_float4((float)x, (float)y, (float)z, __int_as_float(cell_of[a] % ncx));
 }
 
+// floor(u / n) for the cell offsets of the sweep: u = home cell + stencil
+// offset, so when the stencil half-width k is at most n the quotient is -1, 0
+// or 1 (two compares instead of an integer division by a run-time n).
+__device__ __forceinline__ int floordiv_near(int u, int n, bool near) {
+  if (near) return (u < 0) ? -1 : (u >= n ? 1 : 0);
+  int q = u / n;
+  if (u < 0 && q * n != u) q--;
+  return q;
+}
+
 __device__ __forceinline__ int floordiv(int u, int n) {
   int q = u / n;
   if (u < 0 && q * n != u) q--;
@@ -369,10 +379,11 @@ __device__ __forceinline__ int pack_img(int n0, int n1, int n2, int home) {
 // short runs of the fine grid do not leave lanes idle.
 // Dynamic shared memory of k_build per warp: runs, run offsets, candidate map.
 #define YG_BUILD_WARP_SMEM (YG_BUILD_RUNS * 16 + (YG_BUILD_RUNS + 4) * 4 + YG_BUILD_MAP)
-// the map area doubles as the trimmed-row buffer of a batch (64 int2) and
-// every warp's area stays 8-byte aligned
-static_assert(YG_BUILD_MAP >= 64 * 8 && YG_BUILD_MAP % 8 == 0 && YG_BUILD_RUNS % 2 == 0,
-              "build buffers: map of at least 512 bytes, 8-byte multiples");
+// the map area doubles as the trimmed-row buffer of a batch (at most 96
+// int2) and every warp's area stays 8-byte aligned
+#define YG_BUILD_ROWCAP 96
+static_assert(YG_BUILD_MAP >= YG_BUILD_ROWCAP * 8 && YG_BUILD_MAP % 8 == 0 && YG_BUILD_RUNS % 2 == 0,
+              "build buffers: map of at least 768 bytes, 8-byte multiples");
 
 #ifndef YG_BUILD_MINB
 #define YG_BUILD_MINB 4  // resident blocks per SM of the candidate sweep
@@ -402,13 +413,14 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
   int nexact = 0;
   uint2 *out = A.nbr + i * A.cap;
   const int K0 = A.grid.k[0], K1 = A.grid.k[1], K2 = A.grid.k[2];
+  const bool near0 = K0 <= N0, near1 = K1 <= N1, near2 = K2 <= N2;
   const int w0 = 2 * K0 + 1, w1 = 2 * K1 + 1;
   const int oidx_home = K0 + w0 * (K1 + w1 * K2);
   for (int rb = 0; rb < A.grid.nrow; rb += A.grid.rows_per_batch) {
     const int re = min(A.grid.nrow, rb + A.grid.rows_per_batch);
     // runs per lane: count, warp scan, then write; each row trimmed to the
     // atom's reach, the trimmed interval kept in the (still idle) map area
-    // for the writing pass (a batch holds at most 64 rows)
+    // for the writing pass (a batch holds at most YG_BUILD_ROWCAP rows)
     int2 *trim = reinterpret_cast<int2 *>(map);
     int mine = 0;
     for (int r = rb + lane; r < re; r += 32) {
@@ -416,7 +428,7 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
       trim[r - rb] = t;
       for (int ox = t.x; ox <= t.y;) {
         const int u0 = ci[0] + ox;
-        const int c0 = u0 - floordiv(u0, N0) * N0;
+        const int c0 = u0 - floordiv_near(u0, N0, near0) * N0;
         ox += min(t.y - ox + 1, N0 - c0);
         mine++;
       }
@@ -435,13 +447,13 @@ __global__ void __launch_bounds__(256, YG_BUILD_MINB) k_build(BuildArgs A) {
       const int4 row = make_int4(A.rows[r].x, A.rows[r].y, t.x, t.y);
       const int o1 = row.x, o2 = row.y;
       const int u1 = ci[1] + o1, u2 = ci[2] + o2;
-      const int n1 = floordiv(u1, N1), n2 = floordiv(u2, N2);
+      const int n1 = floordiv_near(u1, N1, near1), n2 = floordiv_near(u2, N2, near2);
       const int c1 = u1 - n1 * N1, c2 = u2 - n2 * N2;
       const int rowcell = N0 * (c1 + N1 * c2);
       const int orow = w0 * ((o1 + K1) + w1 * (o2 + K2));
       for (int ox = row.z; ox <= row.w;) {
         const int u0 = ci[0] + ox;
-        const int n0 = floordiv(u0, N0);
+        const int n0 = floordiv_near(u0, N0, near0);
         const int c0 = u0 - n0 * N0;
         const int len = min(row.w - ox + 1, N0 - c0);
         const int s0 = A.cell_start[rowcell + c0], s1 = A.cell_start[rowcell + c0 + len];
@@ -976,7 +988,7 @@ static int nlist_geometry(yg_ctx *ctx, double rc2) {
   G.nrow = (int)rows.size();
   {
     const int maxruns = (2 * G.k[0] + 1 + G.n[0] - 1) / G.n[0] + 1;  // x wraps split a row
-    G.rows_per_batch = std::min(64, std::max(1, YG_BUILD_RUNS / maxruns));  // two rows per lane at most
+    G.rows_per_batch = std::min(YG_BUILD_ROWCAP, std::max(1, YG_BUILD_RUNS / maxruns));  // trimmed-row buffer
     if (maxruns > YG_BUILD_RUNS) {
       yg_set_error("neighbour stencil row too long for the build kernel");
       return YG_ERR_UNSUPPORTED;
