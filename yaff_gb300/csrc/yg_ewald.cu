@@ -1889,14 +1889,19 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   ctx->d_ew_uoff = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_upk);
   ctx->d_ew_upk = nullptr;
+  yg_free(ctx, (void **)&ctx->d_ew_upf);
+  ctx->d_ew_upf = nullptr;
   // every column of the tiles as one int for the tcgen05 epilogue: |g0|,
   // the E1 row G0 + 1 + |g1| (8 bits each), the signs of g0 and g1 (bits 16,
   // 17); -1 for padding
   std::vector<int> upk(std::max<size_t>(1, tiles.size()), -1);
+  std::vector<float2> upf(std::max<size_t>(1, tiles.size()), make_float2(0.0f, 0.0f));
   for (size_t t = 0; t < tiles.size(); t++) {
     const int4 c = tiles[t];
-    if (c.z >= 0)
+    if (c.z >= 0) {
       upk[t] = std::abs(c.x) | ((G0 + 1 + std::abs(c.y)) << 8) | ((c.x < 0) << 16) | ((c.y < 0) << 17);
+      upf[t] = make_float2((float)c.x, (float)c.y);
+    }
   }
   yg_free(ctx, (void **)&ctx->d_ew_urange);
   ctx->d_ew_urange = nullptr;
@@ -1923,6 +1928,8 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_urange, urange.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_upk, upk.size() * sizeof(int)))) return rc;
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_upk, upk.data(), upk.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_upf, upf.size() * sizeof(float2)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_upf, upf.data(), upf.size() * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_uoff, uoff.data(), uoff.size() * sizeof(int), cudaMemcpyHostToDevice,
                           ctx->stream));
   YG_CUDA(cudaMemcpyAsync(ctx->d_ew_urange, urange.data(), urange.size() * sizeof(int), cudaMemcpyHostToDevice,

@@ -215,7 +215,8 @@ __global__ void k_ya_umma(const uint2 *__restrict__ yf, int64_t a0, int64_t n, i
 
 __global__ void __launch_bounds__(UM_THREADS, 1)
     k_ewald_force_umma(const float2 *__restrict__ te, const uint4 *__restrict__ ya, int a0, int a1, int ne, int G0,
-                       int lep, int nks, const int *__restrict__ upk, const int *__restrict__ urange,
+                       int lep, int nks, const int *__restrict__ upk, const float2 *__restrict__ upf,
+                       const int *__restrict__ urange,
                        const int *__restrict__ uoff, const uint4 *__restrict__ ub, double inv1, double inv2,
                        double *__restrict__ out, int64_t rstride, int *__restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem_um[];
@@ -340,6 +341,19 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
           nb = __ldg(p + 1);
         }
         if (ca.x < 0) break;
+        // the chunk's signed (g0, g1) as floats (the same for every lane)
+        float gf[16];
+        {
+          const float4 *fp = reinterpret_cast<const float4 *>(upf + (size_t)(u0 + i) * UM_COLS + 8 * c);
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const float4 f = __ldg(fp + k);
+            gf[4 * k] = f.x;
+            gf[4 * k + 1] = f.y;
+            gf[4 * k + 2] = f.z;
+            gf[4 * k + 3] = f.w;
+          }
+        }
         float v[32];
         um_ld32(tb + 32 * c, v);
         const int pk[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
@@ -355,8 +369,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
             const float pi = e0.x * e1y + e0y * e1.x;
             const float im1 = pr * v[4 * jj + 1] + pi * v[4 * jj];
             const float im2 = pr * v[4 * jj + 3] + pi * v[4 * jj + 2];
-            p0 += (float)(n0 ? -ag0 : ag0) * im1;
-            p1 += (float)(n1 ? G0 + 1 - ag1 : ag1 - G0 - 1) * im1;
+            p0 += gf[2 * jj] * im1;
+            p1 += gf[2 * jj + 1] * im1;
             p2 += im2;
           }
         }
@@ -811,7 +825,7 @@ int yg_launch_force_umma(yg_ctx *ctx, const void *te, const void *ya, int a0, in
   if (nab <= 0) return YG_OK;
   dim3 grid(nab, nr);
   k_ewald_force_umma<<<grid, UM_THREADS, smem, ctx->stream>>>(
-      (const float2 *)te, (const uint4 *)ya, a0, a1, ne, G0, lep, nks, ctx->d_ew_upk, urange,
+      (const float2 *)te, (const uint4 *)ya, a0, a1, ne, G0, lep, nks, ctx->d_ew_upk, ctx->d_ew_upf, urange,
       ctx->d_ew_uoff, (const uint4 *)ub, inv1, inv2, out, rstride, ctx->d_status);
   YG_LAUNCH_CHECK(ctx, "k_ewald_force_umma");
   return YG_OK;

@@ -235,6 +235,7 @@ struct yg_ctx {
   int ew_ubunits = 0;             // 16 KB B-operand units (tile x K-step) of one group's weights
   int *d_ew_uoff = nullptr;       // first unit of every 64-column tile (nut + 1)
   int *d_ew_upk = nullptr;        // the tiles' columns packed for the tcgen05 epilogue (-1: padding)
+  float2 *d_ew_upf = nullptr;     // the tiles' columns' signed (g0, g1) as floats (0 for padding)
   int *d_ew_urange = nullptr;     // tile-range bounds for 1..EW_MMA_MAXR ranges
   void *d_ew_ya = nullptr;        // A operand (q E2 hi/lo) per 128-atom block and K-step
   void *d_ew_ub = nullptr;        // B operand (weights hi/lo) per unit, per group
