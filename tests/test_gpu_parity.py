@@ -109,3 +109,25 @@ def test_nan_positions_raise(ygb):
     ff.update_pos(pos)
     with pytest.raises(ValueError):
         ff.compute(np.zeros((len(pos), 3)), np.zeros((3, 3)))
+
+
+def test_nan_result_leaves_callers_arrays_untouched(ygb):
+    """A NaN in the result raises ValueError before anything reaches the
+    caller's gpos / vtens, as in the reference (yaff/pes/ff.py:156-168).
+    Where the device adds the gradient into the caller's array itself
+    (pageable host memory reached through the host's page tables) the
+    result's status is checked on the device first.  A valid evaluation adds
+    into the caller's arrays."""
+    spec, data = gc.load('tric600')
+    ff = ygb.build_forcefield(spec, precision='mixed')
+    n = len(spec['pos'])
+    g0, v0 = np.zeros((n, 3)), np.zeros((3, 3))
+    e0 = ff.compute(g0, v0)
+    g, v = np.full((n, 3), 7.0), np.full((3, 3), 7.0)
+    assert ff.compute(g, v) == e0
+    assert np.allclose(g - 7.0, g0, rtol=0, atol=1e-12) and np.allclose(v - 7.0, v0, rtol=0, atol=1e-12)
+    ff.system.charges[5] = np.nan
+    g, v = np.full((n, 3), 7.0), np.full((3, 3), 7.0)
+    with pytest.raises(ValueError):
+        ff.compute(g, v)
+    assert (g == 7.0).all() and (v == 7.0).all()

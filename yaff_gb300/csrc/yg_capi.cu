@@ -21,6 +21,14 @@
 #ifndef YG_RB_DIRECT
 #define YG_RB_DIRECT 1
 #endif
+// Where the device can address pageable host memory through the host's page
+// tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, Grace systems),
+// the summed gradient is written (or added) into the caller's own array by
+// the device after a device-side check of the result status, instead of
+// being added by the host from the mirror (1); 0 keeps the mirror path.
+#ifndef YG_RB_ATS
+#define YG_RB_ATS 1
+#endif
 
 namespace {
 thread_local std::string g_last_error;
@@ -157,6 +165,17 @@ __global__ void k_total(const double *__restrict__ part_ev, const double *__rest
     gout[t] = s;
     if (isnan(s)) atomicOr(nan_flag, 1);
   }
+}
+
+// The summed gradient (device memory) into the caller's host array, added
+// (add = 1) or written, only when the result is valid: no NaN in the
+// gradient or the energy and no bounded wait that gave up.  The caller's
+// array is otherwise left as it was.
+__global__ void k_total_apply(const double *__restrict__ tot, int64_t n3, int add, const int *__restrict__ status,
+                              const double *__restrict__ ev, double *gpos) {
+  if (status[YG_ST_NANGRAD] || status[YG_ST_TIMEOUT] || isnan(ev[0])) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n3) gpos[t] = add ? gpos[t] + tot[t] : tot[t];
 }
 
 }  // namespace
@@ -908,8 +927,21 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
   const int want_gpos = gpos != nullptr;
   int64_t nthreads = want_gpos ? std::max<int64_t>(n3, 16) : 16;
   YG_CUDA(cudaMemsetAsync(c->d_status + YG_ST_NANGRAD, 0, sizeof(int), c->stream));
-  // the gradient goes straight into the page-locked mirror when the device
-  // can address it (checked once per context), so no separate copy follows
+  // the gradient goes into the caller's array from the device when it can
+  // address pageable host memory, else straight into the page-locked mirror
+  // when the device can address that (both checked once per context), so no
+  // separate copy follows
+  if (c->ats_state == 0) {
+    int dev = 0, v = 0;
+    c->ats_state = -1;
+#if YG_RB_ATS
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess && v == 1)
+      c->ats_state = 1;
+#endif
+    cudaGetLastError();
+  }
+  const bool ats = want_gpos && c->ats_state == 1;
   if (c->h_total_dev_state == 0) {
     void *alias = nullptr;
 #if YG_RB_DIRECT
@@ -921,16 +953,20 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
     c->h_total_dev_state = 1;
     if (ae != cudaSuccess) cudaGetLastError();  // clear the error of the query
   }
-  double *gout = (want_gpos && c->h_total_dev) ? c->h_total_dev + 16 : c->d_total + 16;
+  double *gout = (want_gpos && c->h_total_dev && !ats) ? c->h_total_dev + 16 : c->d_total + 16;
   k_total<<<yg_blocks(nthreads, 256), 256, 0, c->stream>>>(c->d_part_ev, c->d_part_gpos, c->natom, part_mask,
                                                           want_gpos, c->d_total, gout, c->d_status + YG_ST_NANGRAD);
   YG_LAUNCH_CHECK(c, "k_total");
+  if (ats) {
+    k_total_apply<<<yg_blocks(n3, 256), 256, 0, c->stream>>>(c->d_total + 16, n3, add, c->d_status, c->d_total, gpos);
+    YG_LAUNCH_CHECK(c, "k_total_apply");
+  }
   // status and scalars first, then the gradient in chunks: the host adds
   // (or copies) chunk k while chunk k + 1 is still being transferred
   YG_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, YG_ST_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   YG_CUDA(cudaMemcpyAsync(c->h_total, c->d_total, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  const bool direct = want_gpos && c->h_total_dev;
-  const int nchunk = (!want_gpos || direct) ? 0 : (n3 >= (1 << 16) ? YG_RB_CHUNKS : 1);
+  const bool direct = want_gpos && c->h_total_dev && !ats;
+  const int nchunk = (!want_gpos || direct || ats) ? 0 : (n3 >= (1 << 16) ? YG_RB_CHUNKS : 1);
   int64_t cut[YG_RB_CHUNKS + 1];
   for (int k = 0; k <= nchunk; k++) cut[k] = n3 * k / (nchunk ? nchunk : 1);
   for (int k = 0; k < nchunk; k++) {
@@ -965,6 +1001,7 @@ static int get_total(yg_ctx *c, int part_mask, double *energy, double *gpos, dou
     else
       memcpy(vtens, c->h_total + 1, 9 * sizeof(double));
   }
+  if (ats) return YG_OK;  // the device has added (or written) the gradient
   if (direct) {
     cut[0] = 0;
     cut[1] = n3;

@@ -300,6 +300,7 @@ struct yg_ctx {
   int build_pending = 0;          // a build was enqueued without waiting for its status
   double *h_total_dev = nullptr;  // device alias of h_total (page-locked, mapped), when the device has one
   int h_total_dev_state = 0;      // 0: not queried yet
+  int ats_state = 0;              // device reads/writes pageable host memory: 1 yes, -1 no, 0 not queried yet
   double *d_red = nullptr;        // block partials for energy/virial reductions
   size_t red_cap = 0;
   int part_valid[YG_NPART] = {0, 0, 0, 0, 0, 0};
