@@ -261,13 +261,19 @@ int yg_get_part(yg_ctx *ctx, int part, double *energy, double *gpos, double *vte
 
 /* Sums the parts in part_mask on the device and reads back the total energy,
  * gradient (may be NULL) and virial (may be NULL); per-part energies go to
- * part_energies[YG_NPART] when not NULL.  One device-to-host transfer. */
+ * part_energies[YG_NPART] when not NULL.  gpos is writable host memory of
+ * 3 natom doubles: where the device reaches pageable host memory through
+ * the host's page tables the device writes the gradient into it after
+ * checking the result on the device, otherwise the host copies it from the
+ * page-locked readback block.  A NaN or invalid result (YG_ERR_NAN,
+ * YG_ERR_CUDA) leaves gpos and vtens untouched. */
 int yg_get_total(yg_ctx *ctx, int part_mask, double *energy, double *gpos,
                  double *vtens, double *part_energies);
 
 /* As yg_get_total, but the summed gradient and virial are ADDED to gpos and
- * vtens (yaff's ForcePart.compute convention, ff.py:117-168) straight from
- * the page-locked readback block, without an intermediate copy. */
+ * vtens (yaff's ForcePart.compute convention, ff.py:117-168), by the device
+ * or from the page-locked readback block as for yg_get_total, without an
+ * intermediate copy. */
 int yg_get_total_add(yg_ctx *ctx, int part_mask, double *energy, double *gpos,
                      double *vtens, double *part_energies);
 
