@@ -23,6 +23,7 @@
 // Partial structure factors of atom chunks are summed in FP64 in a fixed
 // order; the energy, the virial and the prefactors are FP64.
 #include <algorithm>
+#include <utility>
 #include <cmath>
 #include <type_traits>
 #include <mutex>
@@ -922,6 +923,9 @@ namespace {
 
 #define EW_MMA_KS 32   // atoms per S-pass stage (two 16-atom steps)
 #define EW_MMA_ATB 512 // atoms per S-pass block
+#ifndef YG_SFAC_PAIRS
+#define YG_SFAC_PAIRS 1  // warp-MMA S pass over conjugate column pairs (X formed once per pair)
+#endif
 #ifndef EW_MMA_FT
 #define EW_MMA_FT 4    // 4-column tiles per force-pass stage
 #endif
@@ -1120,6 +1124,12 @@ __device__ __forceinline__ void sfac_mma_stage(const float2 *__restrict__ sTE, c
   }
 }
 
+// PR (conjugate pairs): cols is the pair list, 128 slots per tile (64 '+'
+// members, then their partners); X is formed for the '+' members only and
+// each accumulator gives both columns: S(g0, g1) = (RR - II, RI + IR) and
+// S(-g0, -g1) = (RR + II, RI - IR) from the sums RR = Re X Re Y, II = Im X Im
+// Y, RI = Re X Im Y, IR = Im X Re Y.
+template <bool PR>
 __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te, const uint4 *__restrict__ ys,
                                                   int n, int G0, int lep, int nms,
                                                   const int4 *__restrict__ cols, float2 *__restrict__ Spart,
@@ -1133,7 +1143,8 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
   const size_t te_bytes = (size_t)EW_MMA_KS * lep * sizeof(float2);
   const size_t ys_bytes = (size_t)(EW_MMA_KS / 16) * nms * 2 * 4 * sizeof(uint4);
   const size_t stage = te_bytes + ys_bytes;
-  const int wc0 = tile * 64 + w * 16;  // the warp's first column (largest extent)
+  constexpr int SC = PR ? 128 : 64;      // partial columns per tile
+  const int wc0 = tile * SC + w * 16;  // the warp's first column (largest extent)
   const int Mw = cols[wc0].w + 1 - mb;
   const int nt = Mw > 0 ? min(8, (Mw + 3) / 4) : 0;
   int o0[2], o1[2];
@@ -1157,7 +1168,7 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
   // te, ys start at the group's first atom and first 16-atom block
   const int abeg = blockIdx.x * EW_MMA_ATB;
   const int aend = min(n, abeg + EW_MMA_ATB);
-  const int tmax = cols[tile * 64].w + 1 - mb;    // the block's largest extent
+  const int tmax = cols[tile * SC].w + 1 - mb;    // the block's largest extent
   if (tmax > 0 && aend > abeg) {
     const int nstage = (aend - abeg + EW_MMA_KS - 1) / EW_MMA_KS;
     if (threadIdx.x == 0) {
@@ -1203,7 +1214,7 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
   }
   // S = (Re X Re Y - Im X Im Y) + i (Re X Im Y + Im X Re Y): lanes t and t^2
   // hold the Re Y and Im Y columns of the same two m values
-  const int64_t base = (((int64_t)blockIdx.x * ntile64 + tile) * nslab + slab) * (64 * EW_MS);
+  const int64_t base = (((int64_t)blockIdx.x * ntile64 + tile) * nslab + slab) * (SC * EW_MS);
 #pragma unroll
   for (int j = 0; j < 2; j++) {
     const int c = w * 16 + 8 * j + g;
@@ -1214,12 +1225,21 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
       if (n >= nt) continue;
       const int m = n * 4 + 2 * (t & 1);
       float *dst = reinterpret_cast<float *>(Spart + base + (int64_t)c * EW_MS + m);
+      float *dcj = reinterpret_cast<float *>(Spart + base + (int64_t)(64 + c) * EW_MS + m);
       if (t < 2) {
         dst[0] = acc[j][n][0] - p2;  // Re S(m), Re S(m + 1)
         dst[2] = acc[j][n][1] - p3;
+        if (PR) {
+          dcj[0] = acc[j][n][0] + p2;  // the partner's Re S(m), Re S(m + 1)
+          dcj[2] = acc[j][n][1] + p3;
+        }
       } else {
         dst[1] = acc[j][n][0] + p2;  // Im S(m), Im S(m + 1)
         dst[3] = acc[j][n][1] + p3;
+        if (PR) {
+          dcj[1] = acc[j][n][0] - p2;  // the partner's Im S(m), Im S(m + 1)
+          dcj[3] = acc[j][n][1] - p3;
+        }
       }
     }
   }
@@ -1609,10 +1629,16 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   const int atb = usf ? yg_umma_sfac_atb() : EW_MMA_ATB;
   int maxchunk = 1;
   for (int g = 0; g < nS; g++) maxchunk = std::max(maxchunk, (int)((gb[g][1] - gb[g][0] + atb - 1) / atb));
-  const size_t per = (size_t)ntile64 * 64 * EW_MS;
+  // the warp-MMA S pass runs over conjugate column pairs (128 partial
+  // columns per tile of 64 pairs)
+  const bool pairs = !usf && YG_SFAC_PAIRS;
+  const int stiles = pairs ? ctx->ew_ntp : ntile64, ssc = pairs ? 128 : 64;
+  const int4 *scols = (const int4 *)(pairs ? ctx->d_ew_pcols : ctx->d_ew_tiles);
+  const size_t per = (size_t)stiles * ssc * EW_MS;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(float2)))) return rc;
   const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
-  if (!usf && (rc = yg_smem_optin((const void *)k_sfac_mma, ssm))) return rc;
+  if (!usf && (rc = yg_smem_optin(pairs ? (const void *)k_sfac_mma<true> : (const void *)k_sfac_mma<false>, ssm)))
+    return rc;
   for (int g = 0; g < nS; g++) {
     const int64_t n = gb[g][1] - gb[g][0];
     double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
@@ -1625,15 +1651,16 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
                                     G0, lep, nks, ctx->d_ew_tiles, ctx->d_ew_Spart, ntile64, EW_MS)))
         return rc;
     } else {
-      dim3 grid(nch, ntile64, 1);
-      k_sfac_mma<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
-                                                 (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8,
-                                                 (int)n, G0, lep, nms, (const int4 *)ctx->d_ew_tiles,
-                                                 (float2 *)ctx->d_ew_Spart, ntile64, 1, ctx->d_status);
+      dim3 grid(nch, stiles, 1);
+      auto kern = pairs ? k_sfac_mma<true> : k_sfac_mma<false>;
+      kern<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
+                                            (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8, (int)n,
+                                            G0, lep, nms, scols, (float2 *)ctx->d_ew_Spart, stiles, 1, ctx->d_status);
       YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
     }
     k_sfac_reduce<float><<<yg_blocks((int64_t)per * 4, 256), 256, 0, ctx->stream>>>(
-        (const float2 *)ctx->d_ew_Spart, nch, ntile64, 1, 64, (const int4 *)ctx->d_ew_tiles, nm, 1.0 / qscale, S);
+        (const float2 *)ctx->d_ew_Spart, nch, usf ? ntile64 : stiles, 1, usf ? 64 : ssc,
+        usf ? (const int4 *)ctx->d_ew_tiles : scols, nm, 1.0 / qscale, S);
     YG_LAUNCH_CHECK(ctx, "k_sfac_reduce");
   }
   // energy, virial, weights of the force pass: B operands of the tcgen05
@@ -1823,6 +1850,48 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
     }
   std::stable_sort(tiles.begin(), tiles.end(), [](const int4 &x, const int4 &y) { return x.w > y.w; });
   while (tiles.size() % EW_SC) tiles.push_back(make_int4(0, 0, -1, -1));
+  // conjugate column pairs for the tensor-core S pass: X(-g0, -g1) is the
+  // conjugate of X(g0, g1), so one set of products gives both columns' S.
+  // Per pair the member with the larger extent comes first ('+', X formed
+  // for it), its partner (or padding) second; pairs sorted by that extent;
+  // tiles of 64 pairs laid out as 64 '+' descriptors then 64 partners.
+  {
+    std::vector<char> used((size_t)nc0 * nc1, 0);
+    std::vector<std::pair<int4, int4>> pairs;
+    const int4 pad = make_int4(0, 0, -1, -1);
+    for (const int4 &c : tiles) {
+      if (c.z < 0 || used[c.z]) continue;
+      used[c.z] = 1;
+      int4 a = c, b = pad;
+      if (c.x != 0 || c.y != 0) {
+        const int64_t pc = (int64_t)(-c.x + G0) * nc1 + (-c.y + G1);
+        if (colmhi[pc] >= 0 && !used[pc]) {
+          used[pc] = 1;
+          b = make_int4(-c.x, -c.y, (int)pc, colmhi[pc]);
+          if (b.w > a.w) std::swap(a, b);
+        }
+      }
+      pairs.push_back(std::make_pair(a, b));
+    }
+    std::stable_sort(pairs.begin(), pairs.end(),
+                     [](const std::pair<int4, int4> &x, const std::pair<int4, int4> &y) { return x.first.w > y.first.w; });
+    while (pairs.size() % 64) pairs.push_back(std::make_pair(pad, pad));
+    const size_t ntp = pairs.size() / 64;
+    std::vector<int4> pcols(ntp * 128);
+    for (size_t t = 0; t < ntp; t++)
+      for (int q = 0; q < 64; q++) {
+        pcols[t * 128 + q] = pairs[t * 64 + q].first;
+        pcols[t * 128 + 64 + q] = pairs[t * 64 + q].second;
+      }
+    ctx->ew_ntp = (int)ntp;
+    yg_free(ctx, (void **)&ctx->d_ew_pcols);
+    ctx->d_ew_pcols = nullptr;
+    int prc;
+    if ((prc = yg_alloc(ctx, (void **)&ctx->d_ew_pcols, pcols.size() * sizeof(int4)))) return prc;
+    YG_CUDA(cudaMemcpyAsync(ctx->d_ew_pcols, pcols.data(), pcols.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));  // pcols goes out of scope
+  }
   ctx->ew_ncol = nc0 * nc1;
   ctx->ew_nm = nm;
   ctx->ew_nk = nk;

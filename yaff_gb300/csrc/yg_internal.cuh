@@ -197,6 +197,8 @@ struct yg_ctx {
   int ew_nk = 0;                  // k vectors in the half sphere
   double *d_ew_pref = nullptr;    // ncol*nm prefactor (0 outside the half sphere)
   int *d_ew_tiles = nullptr;      // column tiles: (g0 base, g1 base, m_hi)
+  int *d_ew_pcols = nullptr;      // conjugate column pairs of the tensor-core S pass: per tile 64 '+' then 64 partners
+  int ew_ntp = 0;                 // tiles of 64 pairs
   int ew_ntile = 0;
   int ew_nftile = 0;              // force tiles (EW_FC columns) with work
   int *d_ew_wslot = nullptr;      // dense column -> slot in the tiled weights
