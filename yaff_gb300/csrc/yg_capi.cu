@@ -290,7 +290,7 @@ int yg_destroy(yg_ctx *c) {
       (void **)&c->d_ew_pref, (void **)&c->d_ew_tiles, (void **)&c->d_ew_tab, (void **)&c->d_ew_Spart,
       (void **)&c->d_ew_S, (void **)&c->d_ew_W, (void **)&c->d_ew_wslot, (void **)&c->d_ew_gpart, (void **)&c->d_ew_red,
       (void **)&c->d_ew_fpre, (void **)&c->d_ew_fpiece, (void **)&c->d_ew_woff, (void **)&c->d_ew_crange, (void **)&c->d_ew_te,
-      (void **)&c->d_ew_yf, (void **)&c->d_ew_ys, (void **)&c->d_ew_wb, (void **)&c->d_ew_uoff, (void **)&c->d_ew_upk, (void **)&c->d_ew_upf, (void **)&c->d_ew_pcols,
+      (void **)&c->d_ew_yf, (void **)&c->d_ew_ys, (void **)&c->d_ew_wb, (void **)&c->d_ew_uoff, (void **)&c->d_ew_upk, (void **)&c->d_ew_upf, (void **)&c->d_ew_pcols, (void **)&c->d_ew_uslot,
       (void **)&c->d_ew_urange, (void **)&c->d_ew_ya, (void **)&c->d_ew_ub,
       (void **)&c->d_delta_ij, (void **)&c->d_delta, (void **)&c->d_ic, (void **)&c->d_icval, (void **)&c->d_vpar,
       (void **)&c->d_vkind, (void **)&c->d_vE, (void **)&c->d_part_ev, (void **)&c->d_part_gpos,

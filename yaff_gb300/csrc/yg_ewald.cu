@@ -448,6 +448,7 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
                                const int *__restrict__ wslot, int64_t wstride, typename C2<T>::t *__restrict__ W,
                                unsigned *__restrict__ wbw, const int *__restrict__ woff, int64_t wbstride,
                                unsigned *__restrict__ ubw, const int *__restrict__ uoff, int64_t ubstride,
+                               const int *__restrict__ uslot,
                                double wsc1, double wsc2, double *__restrict__ partial) {
   __shared__ double red[256 / 32][7];
   int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -513,13 +514,15 @@ __global__ void k_ewald_energy(const double *__restrict__ S, int nS, int64_t nk_
           wb_put(rq0 + 128, bsel, 0, (float)(a2 * ur), (float)(-a2 * ui));
           wb_put(rq1 + 128, bsel, 0, (float)(a2 * ui), (float)(a2 * ur));
         }
-        const int ut = slot >> 6, uks = mm >> 3;
-        if (ubw && uks < uoff[ut + 1] - uoff[ut]) {
+        // the tcgen05 force pass's own tile list (conjugate pairs) places the column at us
+        const int us = ubw ? uslot[colx] : -1;
+        const int ut = us >> 6, uks = mm >> 3;
+        if (ubw && us >= 0 && uks < uoff[ut + 1] - uoff[ut]) {
           // tcgen05 B operand: row n = 4 j + q of the tile (q: Z re, Z im,
           // Z2 re, Z2 im), K element 2 ml + (re, im) of m = 8 ks + ml; in the
           // no-swizzle K-major layout the (re, im) pair is one 32-bit word
           unsigned *unit = ubw + (int64_t)g * ubstride + (int64_t)(uoff[ut] + uks) * 4096;
-          const int j = slot & 63, ml = mm & 7;
+          const int j = us & 63, ml = mm & 7;
           const double a1 = wsc1, a2 = wsc2 * mm;
           const int wb0 = (ml >> 2) * 32 + (ml & 3);
           const int n0 = 4 * j;
@@ -1521,7 +1524,7 @@ int run_reci(yg_ctx *ctx, int want_grad) {
   const double fac2 = 0.25 / ctx->ew_alpha / ctx->ew_alpha;
   k_ewald_energy<T><<<eb, 256, 0, ctx->stream>>>(ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell,
                                                 fac2, ngroup, ctx->d_ew_wslot, wstride, (CT *)ctx->d_ew_W,
-                                                nullptr, nullptr, 0, nullptr, nullptr, 0, 0.0, 0.0, partial);
+                                                nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, 0.0, 0.0, partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -1684,7 +1687,7 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
   k_ewald_energy<float><<<eb, 256, 0, ctx->stream>>>(
       ctx->d_ew_S, nS, nk_dense, ctx->d_ew_pref, G0, G1, nm, ctx->cell, fac2, ngroup, ctx->d_ew_wslot, 0, nullptr,
       umma ? nullptr : (unsigned *)ctx->d_ew_wb, ctx->d_ew_woff, wbstride, umma ? (unsigned *)ctx->d_ew_ub : nullptr,
-      ctx->d_ew_uoff, ubstride, s1, s2, partial);
+      ctx->d_ew_uoff, ubstride, ctx->d_ew_uslot, s1, s2, partial);
   YG_LAUNCH_CHECK(ctx, "k_ewald_energy");
   double *sums = partial + (size_t)eb * 7;
   if ((rc = yg_launch_reduce_ev(ctx, partial, eb, 7, sums))) return rc;
@@ -1850,15 +1853,14 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
     }
   std::stable_sort(tiles.begin(), tiles.end(), [](const int4 &x, const int4 &y) { return x.w > y.w; });
   while (tiles.size() % EW_SC) tiles.push_back(make_int4(0, 0, -1, -1));
-  // conjugate column pairs for the tensor-core S pass: X(-g0, -g1) is the
-  // conjugate of X(g0, g1), so one set of products gives both columns' S.
-  // Per pair the member with the larger extent comes first ('+', X formed
-  // for it), its partner (or padding) second; pairs sorted by that extent;
-  // tiles of 64 pairs laid out as 64 '+' descriptors then 64 partners.
+  // conjugate column pairs: X(-g0, -g1) is the conjugate of X(g0, g1), so
+  // the S pass forms one set of products per pair and the tcgen05 force pass
+  // one P per pair.  Per pair the member with the larger extent comes first
+  // ('+'), its partner (or padding) second; pairs sorted by that extent.
+  const int4 pad = make_int4(0, 0, -1, -1);
+  std::vector<std::pair<int4, int4>> pairs;
   {
     std::vector<char> used((size_t)nc0 * nc1, 0);
-    std::vector<std::pair<int4, int4>> pairs;
-    const int4 pad = make_int4(0, 0, -1, -1);
     for (const int4 &c : tiles) {
       if (c.z < 0 || used[c.z]) continue;
       used[c.z] = 1;
@@ -1875,14 +1877,15 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
     }
     std::stable_sort(pairs.begin(), pairs.end(),
                      [](const std::pair<int4, int4> &x, const std::pair<int4, int4> &y) { return x.first.w > y.first.w; });
-    while (pairs.size() % 64) pairs.push_back(std::make_pair(pad, pad));
-    const size_t ntp = pairs.size() / 64;
-    std::vector<int4> pcols(ntp * 128);
-    for (size_t t = 0; t < ntp; t++)
-      for (int q = 0; q < 64; q++) {
-        pcols[t * 128 + q] = pairs[t * 64 + q].first;
-        pcols[t * 128 + 64 + q] = pairs[t * 64 + q].second;
-      }
+  }
+  // S pass (warp MMA): tiles of 64 pairs laid out as 64 '+' then 64 partners
+  {
+    const size_t ntp = (pairs.size() + 63) / 64;
+    std::vector<int4> pcols(std::max<size_t>(1, ntp) * 128, pad);
+    for (size_t q = 0; q < pairs.size(); q++) {
+      pcols[(q / 64) * 128 + q % 64] = pairs[q].first;
+      pcols[(q / 64) * 128 + 64 + q % 64] = pairs[q].second;
+    }
     ctx->ew_ntp = (int)ntp;
     yg_free(ctx, (void **)&ctx->d_ew_pcols);
     ctx->d_ew_pcols = nullptr;
@@ -1936,10 +1939,27 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   // tcgen05 force pass: 64-column tiles with work, their B-operand units (one
   // per 8 m values of the tile's extent) and tile ranges of equal cost
   // (three MMAs per K-step against an epilogue worth about four)
-  std::vector<int> uoff(1, 0);
+  // With YG_FORCE_PAIRS its 64-column tiles hold 32 conjugate pairs: the '+'
+  // members in columns 0-31, their partners (or padding) in 32-63; the weights
+  // of every column go to its slot of this list (uslot).
   const int ucols = yg_umma_cols();
-  for (size_t t = 0; t * ucols < tiles.size() && tiles[t * ucols].w >= 0; t++)
-    uoff.push_back(uoff.back() + (tiles[t * ucols].w + 8) / 8);
+  std::vector<int4> utiles;
+  if (YG_FORCE_PAIRS) {
+    const size_t half = ucols / 2, nt = (pairs.size() + half - 1) / half;
+    utiles.assign(std::max<size_t>(1, nt) * ucols, pad);
+    for (size_t q = 0; q < pairs.size(); q++) {
+      utiles[(q / half) * ucols + q % half] = pairs[q].first;
+      utiles[(q / half) * ucols + half + q % half] = pairs[q].second;
+    }
+  } else {
+    utiles = tiles;
+  }
+  std::vector<int> uslot((size_t)nc0 * nc1, -1);
+  for (size_t i = 0; i < utiles.size(); i++)
+    if (utiles[i].z >= 0) uslot[utiles[i].z] = (int)i;
+  std::vector<int> uoff(1, 0);
+  for (size_t t = 0; t * ucols < utiles.size() && utiles[t * ucols].w >= 0; t++)
+    uoff.push_back(uoff.back() + (utiles[t * ucols].w + 8) / 8);
   ctx->ew_nut = (int)uoff.size() - 1;
   ctx->ew_ubunits = uoff.back();
   ctx->ew_umma = (ctx->ew_mma && (nm + 7) / 8 <= yg_umma_kmax() && yg_umma_force_smem(G0 + G1 + 2) > 0) ? 1 : 0;
@@ -1963,10 +1983,10 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   // every column of the tiles as one int for the tcgen05 epilogue: |g0|,
   // the E1 row G0 + 1 + |g1| (8 bits each), the signs of g0 and g1 (bits 16,
   // 17); -1 for padding
-  std::vector<int> upk(std::max<size_t>(1, tiles.size()), -1);
-  std::vector<float2> upf(std::max<size_t>(1, tiles.size()), make_float2(0.0f, 0.0f));
-  for (size_t t = 0; t < tiles.size(); t++) {
-    const int4 c = tiles[t];
+  std::vector<int> upk(std::max<size_t>(1, utiles.size()), -1);
+  std::vector<float2> upf(std::max<size_t>(1, utiles.size()), make_float2(0.0f, 0.0f));
+  for (size_t t = 0; t < utiles.size(); t++) {
+    const int4 c = utiles[t];
     if (c.z >= 0) {
       upk[t] = std::abs(c.x) | ((G0 + 1 + std::abs(c.y)) << 8) | ((c.x < 0) << 16) | ((c.y < 0) << 17);
       upf[t] = make_float2((float)c.x, (float)c.y);
@@ -1979,6 +1999,8 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   yg_free(ctx, (void **)&ctx->d_ew_woff);
   ctx->d_ew_woff = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_wslot);
+  yg_free(ctx, (void **)&ctx->d_ew_uslot);
+  ctx->d_ew_uslot = nullptr;
   yg_free(ctx, (void **)&ctx->d_ew_pref);
   yg_free(ctx, (void **)&ctx->d_ew_tiles);
   yg_free(ctx, (void **)&ctx->d_ew_S);
@@ -1990,6 +2012,9 @@ int yg_launch_ewald_setup(yg_ctx *ctx) {
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_tiles, std::max<size_t>(1, tiles.size()) * sizeof(int4)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_S, 3 * 2 * nk_dense * sizeof(double)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_wslot, wslot.size() * sizeof(int)))) return rc;
+  if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_uslot, uslot.size() * sizeof(int)))) return rc;
+  YG_CUDA(cudaMemcpyAsync(ctx->d_ew_uslot, uslot.data(), uslot.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_fpre, fpre.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_woff, woff.size() * sizeof(int)))) return rc;
   if ((rc = yg_alloc(ctx, (void **)&ctx->d_ew_crange, crange.size() * sizeof(int)))) return rc;

@@ -213,6 +213,13 @@ __global__ void k_ya_umma(const uint2 *__restrict__ yf, int64_t a0, int64_t n, i
   ya[base + UM_ATILE / 16 + off] = lo;
 }
 
+// PAIR: the tile's columns 0-31 are the '+' members of conjugate pairs and
+// 32-63 their partners (or padding, whose weights are zero); the partner of
+// (g0, g1) is (-g0, -g1) with P' = conj P, so a pair adds
+//   g0 (Im(P Z) - Im(conj P Z')), g1 (Im(P Z) - Im(conj P Z')),
+//   Im(P Z2) + Im(conj P Z2')
+// with P formed once; each epilogue warp takes one chunk of 8 pairs.
+template <bool PAIR>
 __global__ void __launch_bounds__(UM_THREADS, 1)
     k_ewald_force_umma(const float2 *__restrict__ te, const uint4 *__restrict__ ya, int a0, int a1, int ne, int G0,
                        int lep, int nks, const int *__restrict__ upk, const float2 *__restrict__ upf,
@@ -330,8 +337,50 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
       um_fence_after();
       const unsigned tb = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(s * UM_N);
       float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+      if (PAIR) {
+        // pair chunk h: '+' columns 8 h .. 8 h + 7 (TMEM chunk h), partners
+        // 32 + 8 h .. (chunk h + 4); four pairs at a time
+        const int4 ca = na, cb = nb;
+        if (i + 1 < ntile) {
+          const int4 *p = reinterpret_cast<const int4 *>(upk + (size_t)(u0 + i + 1) * UM_COLS + 8 * h);
+          na = __ldg(p);
+          nb = __ldg(p + 1);
+        }
+        if (ca.x >= 0) {
+          const float4 *fp = reinterpret_cast<const float4 *>(upf + (size_t)(u0 + i) * UM_COLS + 8 * h);
+          const int pk[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+#pragma unroll
+          for (int sub = 0; sub < 2; sub++) {
+            const float4 f0 = __ldg(fp + 2 * sub), f1 = __ldg(fp + 2 * sub + 1);
+            const float gf[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+            float v[16], w[16];
+            um_ld16(tb + 32 * h + 16 * sub, v);
+            um_ld16(tb + 32 * (h + 4) + 16 * sub, w);
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) {
+              const int col = pk[4 * sub + jj];
+              if (col >= 0) {
+                const int ag0 = col & 255, ag1 = (col >> 8) & 255;
+                const bool n0 = (col >> 16) & 1, n1 = (col >> 17) & 1;
+                const float2 e0 = sE[ag0 * UM_M + r], e1 = sE[ag1 * UM_M + r];
+                const float e0y = n0 ? -e0.y : e0.y, e1y = n1 ? -e1.y : e1.y;
+                const float pr = e0.x * e1.x - e0y * e1y;
+                const float pi = e0.x * e1y + e0y * e1.x;
+                const float im1 = pr * v[4 * jj + 1] + pi * v[4 * jj];
+                const float im2 = pr * v[4 * jj + 3] + pi * v[4 * jj + 2];
+                const float jm1 = pr * w[4 * jj + 1] - pi * w[4 * jj];
+                const float jm2 = pr * w[4 * jj + 3] - pi * w[4 * jj + 2];
+                const float d1 = im1 - jm1;
+                p0 += gf[2 * jj] * d1;
+                p1 += gf[2 * jj + 1] * d1;
+                p2 += im2 + jm2;
+              }
+            }
+          }
+        }
+      }
 #pragma unroll 1
-      for (int c = h; c < UM_N / 32; c += HQ) {
+      for (int c = h; !PAIR && c < UM_N / 32; c += HQ) {
         const int4 ca = na, cb = nb;
         const bool last = c + HQ >= UM_N / 32 || ca.x < 0;  // (padding: the rest of the tile is padding)
         if (!last || i + 1 < ntile) {
@@ -820,11 +869,12 @@ int yg_launch_force_umma(yg_ctx *ctx, const void *te, const void *ya, int a0, in
     return YG_ERR_UNSUPPORTED;
   }
   int rc;
-  if ((rc = yg_smem_optin((const void *)k_ewald_force_umma, smem))) return rc;
+  auto kern = k_ewald_force_umma<YG_FORCE_PAIRS != 0>;
+  if ((rc = yg_smem_optin((const void *)kern, smem))) return rc;
   const int nab = (a1 - a0 + UM_M - 1) / UM_M;
   if (nab <= 0) return YG_OK;
   dim3 grid(nab, nr);
-  k_ewald_force_umma<<<grid, UM_THREADS, smem, ctx->stream>>>(
+  kern<<<grid, UM_THREADS, smem, ctx->stream>>>(
       (const float2 *)te, (const uint4 *)ya, a0, a1, ne, G0, lep, nks, ctx->d_ew_upk, ctx->d_ew_upf, urange,
       ctx->d_ew_uoff, (const uint4 *)ub, inv1, inv2, out, rstride, ctx->d_status);
   YG_LAUNCH_CHECK(ctx, "k_ewald_force_umma");

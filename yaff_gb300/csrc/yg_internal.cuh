@@ -16,6 +16,9 @@
 
 #define YG_MAX_POT 3
 #define YG_RB_CHUNKS 4   // chunks of the pipelined gradient readback
+#ifndef YG_FORCE_PAIRS
+#define YG_FORCE_PAIRS 1  // tcgen05 Ewald force pass over conjugate column pairs (P formed once per pair)
+#endif
 #define YG_WARP 32
 
 // Device status words (yg_ctx::d_status)
@@ -199,6 +202,7 @@ struct yg_ctx {
   int *d_ew_tiles = nullptr;      // column tiles: (g0 base, g1 base, m_hi)
   int *d_ew_pcols = nullptr;      // conjugate column pairs of the tensor-core S pass: per tile 64 '+' then 64 partners
   int ew_ntp = 0;                 // tiles of 64 pairs
+  int *d_ew_uslot = nullptr;      // slot of every dense column in the tcgen05 force pass's tile list (-1: none)
   int ew_ntile = 0;
   int ew_nftile = 0;              // force tiles (EW_FC columns) with work
   int *d_ew_wslot = nullptr;      // dense column -> slot in the tiled weights
