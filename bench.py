@@ -357,9 +357,9 @@ def run_gb300(args, world, rank, local):
                       'combine/gpos; FP16 hi/lo split, FP32 accumulate',
             'ms': t_reci * 1e3, 'units': {'atom_k': natom * nk, 'flops_per_atom_k': 18},
             'warp_mma_f16_peak_tflops': mma_probe,
-            'traffic': 89.0e6 * nat_scale,
-            'traffic_source': 'ncu dram read+write of k_sfac_mma (40.3 MB) + k_ya_umma (12.8 MB) + '
-                              'k_ewald_force_umma (35.9 MB) at 50,000 atoms' +
+            'traffic': 82.7e6 * nat_scale,
+            'traffic_source': 'ncu dram read+write of k_sfac_mma (33.7 MB) + k_ya_umma (12.8 MB) + '
+                              'k_ewald_force_umma (36.2 MB) at 50,000 atoms' +
                               ('' if natom == 50000 else ', scaled by atoms')}
     elif tcode.value == 1:
         rooflines['ewald_reciprocal'] = {
