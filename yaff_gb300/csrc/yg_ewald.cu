@@ -926,7 +926,7 @@ namespace {
 
 #define EW_MMA_KS 32   // atoms per S-pass stage (two 16-atom steps)
 #ifndef EW_MMA_ATB
-#define EW_MMA_ATB 1024 // atoms per S-pass block (a multiple of 32; 1024: 973 / 965 against 951 evals/s for 512)
+#define EW_MMA_ATB 512 // fewest atoms per S-pass block (the launch picks the chunk, a multiple of 32)
 #endif
 #ifndef YG_SFAC_PAIRS
 #define YG_SFAC_PAIRS 1  // warp-MMA S pass over conjugate column pairs (X formed once per pair)
@@ -1079,7 +1079,7 @@ __global__ void k_ys_mma(const uint2 *__restrict__ yf, int64_t natom, int64_t lo
   ys[u] = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// S pass on the tensor cores.  grid = (atom chunks of EW_MMA_ATB, 64-column
+// S pass on the tensor cores.  grid = (atom chunks of atb atoms, 64-column
 // tiles, m slabs); 4 warps, warp w owns columns 16 w .. 16 w + 15 of the
 // tile as two 8-column MMA row tiles (rows 0-7: Re X, rows 8-15: Im X) and
 // NT n-tiles of 4 m values (columns 0-3: Re Y, 4-7: Im Y) of the slab.  The
@@ -1138,7 +1138,7 @@ template <bool PR>
 __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te, const uint4 *__restrict__ ys,
                                                   int n, int G0, int lep, int nms,
                                                   const int4 *__restrict__ cols, float2 *__restrict__ Spart,
-                                                  int ntile64, int nslab, int *__restrict__ status) {
+                                                  int ntile64, int nslab, int atb, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_mma[];
   __shared__ unsigned long long bars[2];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1171,8 +1171,8 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
 #pragma unroll
       for (int e = 0; e < 4; e++) acc[j][n][e] = 0.f;
   // te, ys start at the group's first atom and first 16-atom block
-  const int abeg = blockIdx.x * EW_MMA_ATB;
-  const int aend = min(n, abeg + EW_MMA_ATB);
+  const int abeg = blockIdx.x * atb;
+  const int aend = min(n, abeg + atb);
   const int tmax = cols[tile * SC].w + 1 - mb;    // the block's largest extent
   if (tmax > 0 && aend > abeg) {
     const int nstage = (aend - abeg + EW_MMA_KS - 1) / EW_MMA_KS;
@@ -1630,25 +1630,43 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
         (const uint2 *)ctx->d_ew_yf, N, lo, hi, gbase[1], gbase[2], ys_blocks, nmf, nms, (uint4 *)ctx->d_ew_ys);
     YG_LAUNCH_CHECK(ctx, "k_ys_mma");
   }
-  // structure factors
-  const int atb = usf ? yg_umma_sfac_atb() : EW_MMA_ATB;
-  int maxchunk = 1;
-  for (int g = 0; g < nS; g++) maxchunk = std::max(maxchunk, (int)((gb[g][1] - gb[g][0] + atb - 1) / atb));
-  // the warp-MMA S pass runs over conjugate column pairs (128 partial
-  // columns per tile of 64 pairs)
+  // structure factors: the warp-MMA S pass runs over conjugate column pairs
+  // (128 partial columns per tile of 64 pairs)
   const bool pairs = !usf && YG_SFAC_PAIRS;
   const int stiles = pairs ? ctx->ew_ntp : ntile64, ssc = pairs ? 128 : 64;
   const int4 *scols = (const int4 *)(pairs ? ctx->d_ew_pcols : ctx->d_ew_tiles);
+  const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
+  const void *skern = pairs ? (const void *)k_sfac_mma<true> : (const void *)k_sfac_mma<false>;
+  int sslots = 0;
+  if (!usf) {
+    if ((rc = yg_smem_optin(skern, ssm))) return rc;
+    if ((rc = resident_blocks(skern, 128, ssm, &ctx->ew_occ_s, &sslots))) return rc;
+  }
+  // atoms per S-pass block: the fewest chunks whose blocks (chunks x tiles)
+  // still fit one wave of resident blocks, at least EW_MMA_ATB, a multiple of
+  // 32 (50,000 atoms on 17 pair tiles and 608 slots: 1,440 atoms, 35 x 17
+  // blocks; one wave of 1,536-atom chunks measured 991 / 998 evals/s against
+  // 976 / 979 for 1,024-atom chunks, 1.37 waves)
+  auto chunk_of = [&](int64_t n) -> int {
+    if (usf) return yg_umma_sfac_atb();
+    const int64_t per_tile = std::max<int64_t>(1, sslots / std::max(1, stiles));
+    int64_t a = (n + per_tile - 1) / per_tile;
+    a = (a + 31) / 32 * 32;
+    return (int)std::max<int64_t>(EW_MMA_ATB, a);
+  };
+  int maxchunk = 1;
+  for (int g = 0; g < nS; g++) {
+    const int64_t n = gb[g][1] - gb[g][0];
+    if (n > 0) maxchunk = std::max(maxchunk, (int)((n + chunk_of(n) - 1) / chunk_of(n)));
+  }
   const size_t per = (size_t)stiles * ssc * EW_MS;
   if ((rc = yg_ensure(ctx, &ctx->d_ew_Spart, &ctx->ew_bytes_Spart, per * maxchunk * sizeof(float2)))) return rc;
-  const size_t ssm = 2 * ((size_t)EW_MMA_KS * lep * sizeof(float2) + (size_t)(EW_MMA_KS / 16) * nms * 8 * sizeof(uint4));
-  if (!usf && (rc = yg_smem_optin(pairs ? (const void *)k_sfac_mma<true> : (const void *)k_sfac_mma<false>, ssm)))
-    return rc;
   for (int g = 0; g < nS; g++) {
     const int64_t n = gb[g][1] - gb[g][0];
     double *S = ctx->d_ew_S + (size_t)g * 2 * nk_dense;
     YG_CUDA(cudaMemsetAsync(S, 0, 2 * nk_dense * sizeof(double), ctx->stream));
     if (n <= 0) continue;
+    const int atb = chunk_of(n);
     const int nch = (int)((n + atb - 1) / atb);
     if (usf) {
       if ((rc = yg_launch_sfac_umma(ctx, te + (size_t)gb[g][0] * lep,
@@ -1660,7 +1678,8 @@ int run_reci_mma(yg_ctx *ctx, int want_grad) {
       auto kern = pairs ? k_sfac_mma<true> : k_sfac_mma<false>;
       kern<<<grid, 128, ssm, ctx->stream>>>(te + (size_t)gb[g][0] * lep,
                                             (const uint4 *)ctx->d_ew_ys + (size_t)(gbase[g] / 16) * nms * 8, (int)n,
-                                            G0, lep, nms, scols, (float2 *)ctx->d_ew_Spart, stiles, 1, ctx->d_status);
+                                            G0, lep, nms, scols, (float2 *)ctx->d_ew_Spart, stiles, 1, atb,
+                                            ctx->d_status);
       YG_LAUNCH_CHECK(ctx, "k_sfac_mma");
     }
     k_sfac_reduce<float><<<yg_blocks((int64_t)per * 4, 256), 256, 0, ctx->stream>>>(

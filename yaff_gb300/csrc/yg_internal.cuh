@@ -228,6 +228,7 @@ struct yg_ctx {
   int *d_ew_woff = nullptr;       // first fragment unit of every 4-column tile (nft4 + 1)
   int *d_ew_crange = nullptr;     // column-range bounds of the force pass for 1..EW_MMA_MAXR ranges
   yg_occ ew_occ_fm;               // resident tensor-core force-pass blocks
+  yg_occ ew_occ_s;                // resident warp-MMA S-pass blocks
   void *d_ew_te = nullptr;        // E0|E1 rows (float2), atoms padded to a multiple of 32
   void *d_ew_yf = nullptr;        // q E2 as FP16 (hi, lo) pairs per (atom, m)
   void *d_ew_ys = nullptr;        // q E2 per 16 atoms: FP16 B fragments, or the tcgen05 S-pass B operand
