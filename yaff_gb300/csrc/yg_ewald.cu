@@ -1085,8 +1085,9 @@ __global__ void k_ys_mma(const uint2 *__restrict__ yf, int64_t natom, int64_t lo
 // NT n-tiles of 4 m values (columns 0-3: Re Y, 4-7: Im Y) of the slab.  The
 // E0|E1 rows and the Y fragments of 32 atoms at a time arrive by
 // double-buffered bulk copies (te holds 32 rows past the last atom, ys two
-// blocks past the last group).  Partial layout as k_sfac with 64 columns:
-// [chunk][tile][slab][c][m].
+// blocks past the last group).  Partial layout as k_sfac with 64 columns
+// ([chunk][tile][slab][c][m]), or with 128 over conjugate pairs (PR below:
+// a tile of 64 pairs, the warps own 16 pairs each).
 template <int NT>
 __device__ __forceinline__ void sfac_mma_stage(const float2 *__restrict__ sTE, const uint4 *__restrict__ sYS, int lep,
                                                int nms, int mb, int nrow, const int (&o0)[2], const int (&o1)[2],
@@ -1138,7 +1139,7 @@ template <bool PR>
 __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te, const uint4 *__restrict__ ys,
                                                   int n, int G0, int lep, int nms,
                                                   const int4 *__restrict__ cols, float2 *__restrict__ Spart,
-                                                  int ntile64, int nslab, int atb, int *__restrict__ status) {
+                                                  int ntile, int nslab, int atb, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_mma[];
   __shared__ unsigned long long bars[2];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1219,7 +1220,7 @@ __global__ void __launch_bounds__(128) k_sfac_mma(const float2 *__restrict__ te,
   }
   // S = (Re X Re Y - Im X Im Y) + i (Re X Im Y + Im X Re Y): lanes t and t^2
   // hold the Re Y and Im Y columns of the same two m values
-  const int64_t base = (((int64_t)blockIdx.x * ntile64 + tile) * nslab + slab) * (SC * EW_MS);
+  const int64_t base = (((int64_t)blockIdx.x * ntile + tile) * nslab + slab) * (SC * EW_MS);
 #pragma unroll
   for (int j = 0; j < 2; j++) {
     const int c = w * 16 + 8 * j + g;
