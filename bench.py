@@ -408,8 +408,8 @@ def run_gb300(args, world, rank, local):
         'kernel': 'k_pair<MM3, EI> (one warp per atom over its full row; each pair is evaluated from both ends; '
                   'on a fresh list the skin shell at the back of the row is not read)',
         'ms': t_pair * 1e3, 'units': {'pairs_within_rcut': npair, 'flops_per_pair': 75, 'transcendentals_per_pair': 3},
-        'traffic': 302.4e6 * nat_scale,
-        'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms (295.7 MB read, 6.7 MB written; the '
+        'traffic': 300.7e6 * nat_scale,
+        'traffic_source': 'ncu dram read+write of k_pair at 50,000 atoms (295.9 MB read, 4.8 MB written; the '
                           'skin shell is not read on a fresh list)' + ('' if natom == 50000 else ', scaled by atoms')}
     dom = max(rooflines, key=lambda k: rooflines[k]['ms'])
     roof = dict(rooflines[dom])
